@@ -1,0 +1,161 @@
+/* upcgen-gb300 -- C ABI of the GB300 two-photon luminosity / nuclear cross
+ * section / event-sampling library.
+ *
+ * Drop-in boundary for upcgen's UpcGenerator / UpcCrossSection path.  The
+ * reference exposes a C++ class API (include/UpcGenerator.h:55-128,
+ * include/UpcCrossSection.h:65-240, built as the Upcgenlib library by
+ * CMakeLists.txt:83-91); every entry point below names the method it
+ * replaces.  A C++ facade with the reference's class and method names sits on
+ * top of this ABI in include/upcgen_gb300.hpp.
+ *
+ * Conventions
+ *   - every function returns an int status (UPCG_OK = 0, negative on error)
+ *     and never exits or aborts; upcg_last_error() gives a message;
+ *   - the caller owns every buffer passed in; the handle owns device memory;
+ *   - pointers are host pointers unless the name ends in _device;
+ *   - a handle is bound to one CUDA stream (upcg_set_stream); distinct handles
+ *     may be used from distinct threads.
+ */
+#ifndef UPCGEN_GB300_H_
+#define UPCGEN_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UPCG_OK 0
+#define UPCG_ERR_ARG (-1)       /* bad argument / unknown value */
+#define UPCG_ERR_CUDA (-2)      /* CUDA error (message in upcg_last_error) */
+#define UPCG_ERR_STATE (-3)     /* call out of order (e.g. before upcg_init) */
+#define UPCG_ERR_PROCESS (-4)   /* PROC_ID outside this path */
+#define UPCG_ERR_NUMERIC (-5)   /* QAGS failure the reference would abort on */
+#define UPCG_ERR_NOMEM (-6)
+#define UPCG_ERR_SIZE (-7)      /* output buffer too small */
+
+typedef struct upcg_generator upcg_generator;
+
+/* One accepted event, 48 bytes: pair mass / rapidity / cos(theta), charge
+ * sign of particle 0 (+1/-1; +1 for neutral products), then px,py,pz,E of the
+ * two final-state particles (leptons; the two photons for an ALP). */
+typedef struct upcg_event {
+  float m, y, z, sign;
+  float p0[4];
+  float p1[4];
+} upcg_event;
+
+/* ---- life cycle / configuration (UpcGenerator) ------------------------ */
+/* UpcGenerator::UpcGenerator, src/UpcGenerator.cpp:30-40 (Pb-Pb at 5020 GeV) */
+int upcg_create(upcg_generator** out);
+/* UpcGenerator::~UpcGenerator, src/UpcGenerator.cpp:42-55 */
+int upcg_destroy(upcg_generator* g);
+/* UpcGenerator::setParameterValue, src/UpcGenerator.cpp:183-305; parameters.in
+ * keys; keys of other paths (PYTHIA_*, USE_*_OUTPUT, SHADOWING, ...) are
+ * accepted and ignored as the reference ignores unknown keys */
+int upcg_set_parameter(upcg_generator* g, const char* key, const char* value);
+/* UpcGenerator::setParFile + configGeneratorFromFile, src/UpcGenerator.cpp:318-346 */
+int upcg_config_from_file(upcg_generator* g, const char* path);
+/* UpcGenerator::setCollisionSystem, src/UpcGenerator.cpp:307-316 */
+int upcg_set_collision_system(upcg_generator* g, float sqrts, int nucl_z, int nucl_a);
+/* UpcGenerator::setSeed, include/UpcGenerator.h:104-113 */
+int upcg_set_seed(upcg_generator* g, long seed);
+/* UpcGenerator::setNumThreads, include/UpcGenerator.h:95 (accepted; the GPU
+ * path does not use host threads) */
+int upcg_set_num_threads(upcg_generator* g, int n);
+/* UpcGenerator::setDebugLevel, include/UpcGenerator.h:92 */
+int upcg_set_debug_level(upcg_generator* g, int level);
+/* UpcGenerator::setLumiFileDirectory, include/UpcGenerator.h:87: directory
+ * of the luminosity cache (see upcg_set_lumi_cache) */
+int upcg_set_lumi_file_directory(upcg_generator* g, const char* dir);
+/* 1: reuse / write a luminosity cache keyed by a hash of every input of the
+ * table (the reference's twoPhotonLumi.root is keyed by nothing,
+ * src/UpcCrossSection.cpp:481-491); 0 (default): always compute */
+int upcg_set_lumi_cache(upcg_generator* g, int enable);
+/* CUDA stream (cudaStream_t) for every launch of this handle; NULL = the
+ * handle's own stream */
+int upcg_set_stream(upcg_generator* g, void* stream);
+/* Luminosity method: 0 = plain FP64 (default; the reference's quadrature),
+ * 1 = fast form (tensor-core contraction, <= 1e-4 relative) */
+int upcg_set_lumi_method(upcg_generator* g, int method);
+
+/* ---- initialisation (UpcGenerator::init) ------------------------------ */
+/* UpcGenerator::init, src/UpcGenerator.cpp:57-181: process overrides, nuclear
+ * tables (UpcCrossSection::init :116-137), two-photon luminosity
+ * (prepareTwoPhotonLumi :463-592), nuclear cross section and samplers
+ * (computeNuclXsection :630-713) */
+int upcg_init(upcg_generator* g);
+/* UpcGenerator::computeNuclXsection, src/UpcGenerator.cpp:630-713 (re-run the
+ * fold and sampler set-up on the current luminosity) */
+int upcg_compute_nucl_xsection(upcg_generator* g);
+/* UpcGenerator::totNuclX / fidNuclX, include/UpcGenerator.h:120-121 (mb) */
+int upcg_tot_nucl_x(const upcg_generator* g, double* mb);
+int upcg_fid_nucl_x(const upcg_generator* g, double* mb);
+/* effective grid after the process overrides of UpcGenerator::init */
+int upcg_get_grid(const upcg_generator* g, double* mmin, double* mmax, int* nm,
+                  double* ymin, double* ymax, int* ny, double* zmin, double* zmax,
+                  int* nz);
+
+/* ---- tables ------------------------------------------------------------ */
+/* hD2LDMDY of prepareTwoPhotonLumi (src/UpcCrossSection.cpp:506-571):
+ * out[im*ny + iy] = L(m_im, y_iy) dm dy (bin (im+1, iy+1)); polarized:
+ * hD2LDMDY_s into out, hD2LDMDY_p into out2 (may be NULL otherwise) */
+int upcg_lumi_table(upcg_generator* g, double* out, size_t n, double* out2);
+int upcg_lumi_table_device(upcg_generator* g, const double** out, const double** out2);
+/* nucCSYM of calcNucCrossSectionYM (src/UpcCrossSection.cpp:594-698):
+ * out[iy*nm + im] (nb) and its total (mb) */
+int upcg_nuc_cs_ym(upcg_generator* g, double* out, size_t n, double* tot_mb);
+/* fillCrossSectionZM (src/UpcCrossSection.cpp:337-362), flag 0/1/2:
+ * out[im*nz + iz] */
+int upcg_cs_zm_table(upcg_generator* g, int flag, double* out, size_t n);
+
+/* ---- point evaluations (UpcCrossSection methods, batched, on the GPU) ---- */
+/* fluxPoint, src/UpcCrossSection.cpp:166-178 */
+int upcg_flux_point(upcg_generator* g, const double* b, const double* k, double* out, size_t n);
+/* fluxForm, src/UpcCrossSection.cpp:194-218 (QAGS on the device) */
+int upcg_flux_form(upcg_generator* g, const double* b, const double* k, double* out, size_t n);
+/* calcFormFac, src/UpcCrossSection.cpp:436-445 */
+int upcg_form_factor(upcg_generator* g, const double* q2, double* out, size_t n);
+/* calcBreakupProb, src/UpcCrossSection.cpp:752-1019 */
+int upcg_breakup_prob(upcg_generator* g, const double* b, int mode, double* out, size_t n);
+/* the splines gslSplineGAA / gslSplineBreakP / gslSplineFormFac
+ * (src/UpcCrossSection.cpp:411-413, 431-433, 458-460): which = 0/1/2 */
+int upcg_eval_spline(upcg_generator* g, int which, const double* x, double* out, size_t n);
+/* calcTwoPhotonLumi, src/UpcCrossSection.cpp:221-271 (out2 == NULL), or
+ * calcTwoPhotonLumiPol :274-335 (scalar into out, pseudoscalar into out2) */
+int upcg_two_photon_lumi(upcg_generator* g, const double* m, const double* y, double* out,
+                         double* out2, size_t n);
+/* UpcElemProcess::calcCrossSectionM / MPolS / MPolPS of the configured
+ * process (flag 0/1/2), src/UpcTwoPhotonDilep.cpp:46-122, src/UpcTwoPhotonALP.cpp:28-33 */
+int upcg_cs_m(upcg_generator* g, const double* m, int flag, double* out, size_t n);
+
+/* ---- events (UpcGenerator::generateEvents) ------------------------------ */
+/* The event loop of src/UpcGenerator.cpp:834-889: the first n accepted events
+ * of the candidate sequence; *rejected = candidates rejected by the cuts
+ * before the n-th accepted one; updates fidNuclX.  mbin (may be NULL) gets
+ * UpcSampler2D::getBinY of each event's mass (include/UpcSampler.h:130-133). */
+int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t* mbin,
+                         int64_t* rejected);
+int upcg_generate_events_device(upcg_generator* g, int64_t n, upcg_event* out_device,
+                                int32_t* mbin_device, int64_t* rejected);
+/* UpcGenerator::generateEvent, src/UpcGenerator.cpp:715-832: one candidate.
+ * Returns 1 (accepted) or 0 (rejected by the cuts) in *accepted and the
+ * event in *ev; candidates are drawn from the same sequence as
+ * upcg_generate_events. */
+int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted);
+
+/* ---- diagnostics --------------------------------------------------------- */
+/* Philox4x32-10 uniforms of the event stream (seed, counter) -- for tests */
+int upcg_philox(uint64_t seed, uint64_t counter0, size_t n, uint32_t* out4);
+/* timings of the last upcg_init phases (ms) and QAGS statistics */
+int upcg_last_timings(const upcg_generator* g, double* ms, size_t n);
+int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_intervals,
+                    uint64_t* evals);
+const char* upcg_last_error(void);
+const char* upcg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UPCGEN_GB300_H_ */

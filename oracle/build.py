@@ -1,0 +1,66 @@
+"""Build recipe for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+* ``build_oracle()`` compiles the FP64 C++/OpenMP restatement in this folder
+  into ``oracle/_build/libupcg_oracle.so``.
+* ``build_ref()`` compiles the two translation units of the reference that build
+  without ROOT/GSL -- ``src/UpcTwoPhotonDilep.cpp`` and ``src/UpcTwoPhotonALP.cpp``
+  -- together with ``ref_shim.cpp`` into ``oracle/_ref/libupcref_elem.so``, when
+  the reference sources are present.  The rest of the reference needs ROOT and
+  GSL and is not buildable here.
+
+``-ffp-contract=off`` keeps the x86 and aarch64 builds bit-identical (gcc
+contracts a*b+c into FMAs by default on aarch64).
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+ORACLE_SO = os.path.join(BUILD_DIR, "libupcg_oracle.so")
+REF_SO = os.path.join(REF_DIR, "libupcref_elem.so")
+REFERENCE_ROOT = os.environ.get("UPCG_REFERENCE_ROOT", "/root/reference")
+
+_SOURCES = ["oracle_cs.cpp", "oracle_gen.cpp"]
+_HEADERS = ["oracle_num.hpp", "oracle_ctx.hpp", "upcg_oracle.h"]
+_FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_oracle(force=False):
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    srcs = [os.path.join(HERE, s) for s in _SOURCES]
+    deps = srcs + [os.path.join(HERE, h) for h in _HEADERS]
+    if force or _stale(ORACLE_SO, deps):
+        cmd = ["g++", *_FLAGS, *srcs, "-o", ORACLE_SO + ".tmp"]
+        subprocess.run(cmd, check=True)
+        os.replace(ORACLE_SO + ".tmp", ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_ref(force=False):
+    """Compile the reference's elementary cross sections; None if absent."""
+    src = os.path.join(REFERENCE_ROOT, "src")
+    inc = os.path.join(REFERENCE_ROOT, "include")
+    units = [os.path.join(src, "UpcTwoPhotonDilep.cpp"), os.path.join(src, "UpcTwoPhotonALP.cpp")]
+    if not all(os.path.exists(u) for u in units):
+        return REF_SO if os.path.exists(REF_SO) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    shim = os.path.join(HERE, "ref_shim.cpp")
+    if force or _stale(REF_SO, units + [shim]):
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+               "-I", inc, *units, shim, "-o", REF_SO + ".tmp"]
+        subprocess.run(cmd, check=True)
+        os.replace(REF_SO + ".tmp", REF_SO)
+    return REF_SO
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))

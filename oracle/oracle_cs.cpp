@@ -1,0 +1,694 @@
+// CPU oracle -- UpcCrossSection restatement (TEST INFRASTRUCTURE ONLY).
+//
+// Follows src/UpcCrossSection.cpp of the reference function by function; each
+// function names the lines it restates.  Deliberate differences, all without
+// effect on any number the reference prints:
+//   * no lock file / ROOT cache: the luminosity table is returned directly;
+//   * calcBreakupProb keeps its tables per context instead of in function
+//     statics (the reference fills them on the first call of the process), and
+//     skips the single-neutron sum p1n, which never reaches its return value;
+//   * the breakup spline is built on knots up to b = 20 fm plus a 256-knot
+//     margin: the reference only evaluates it at min(b, 20)
+//     (src/UpcCrossSection.cpp:260), and the natural-spline coupling decays as
+//     0.268^n, so the truncated spline is identical in double precision there.
+#include <omp.h>
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "oracle_ctx.hpp"
+
+namespace uo {
+
+// ------------------------------------------------------------- constants --
+// include/UpcPhysConstants.h:26-32
+const double kAlpha = 1.0 / 137.035999074;
+const double kHc = 0.1973269718;
+const double kMProt = 0.9382720813;
+const double kMEl = 0.000510998946;
+const double kMMu = 0.1056583745;
+const double kMTau = 1.77686;
+
+// include/UpcCrossSection.h:91-111 (the reference's 16-digit GL-10 table)
+const double kW10[10] = {0.0666713443086881, 0.1494513491505806, 0.2190863625159820,
+                         0.2692667193099963, 0.2955242247147529, 0.2955242247147529,
+                         0.2692667193099963, 0.2190863625159820, 0.1494513491505806,
+                         0.0666713443086881};
+const double kX10[10] = {-0.9739065285171717, -0.8650633666889845, -0.6794095682990244,
+                         -0.4333953941292472, -0.1488743389816312, 0.1488743389816312,
+                         0.4333953941292472,  0.6794095682990244,  0.8650633666889845,
+                         0.9739065285171717};
+
+// src/UpcCrossSection.cpp:46-49
+const double kQ2min = 1e-9, kQ2max = 2.;
+const int kNQ2 = 1000000;
+const double kDQ2 = (kQ2max - kQ2min) / kNQ2;
+
+Ctx::Ctx() {
+  const double g0 = 5020. / (2. * kMProt);
+  // UpcCrossSection() runs before any parameter is read, so gtot always
+  // corresponds to the default sqrt(s) = 5020 GeV (src/UpcCrossSection.cpp:53,
+  // include/UpcCrossSection.h:83-85).
+  gtot = std::cosh((std::acosh(g0) + std::acosh(g0)) / 2.);
+  set_collision(5020.f, 82, 208);
+}
+
+void Ctx::set_collision(float s, int z, int a) {  // src/UpcGenerator.cpp:307-316
+  sqrts = s;
+  g1 = sqrts / (2. * kMProt);
+  g2 = sqrts / (2. * kMProt);
+  Z = z;
+  A = a;
+}
+
+int Ctx::set_param(const std::string& k, const std::string& v) {
+  // src/UpcGenerator.cpp:183-305
+  try {
+    if (k == "NEVENTS") nEvents = std::stol(v);
+    else if (k == "SQRTS") { sqrts = std::stod(v); g1 = g2 = sqrts / (2. * kMProt); }
+    else if (k == "PROC_ID") procID = std::stoi(v);
+    else if (k == "LEP_A") aLep = std::stod(v);
+    else if (k == "ALP_MASS") alpMass = std::stod(v);
+    else if (k == "ALP_WIDTH") alpWidth = std::stod(v);
+    else if (k == "DO_PT_CUT") doPtCut = std::stoi(v);
+    else if (k == "PT_MIN") minPt = std::stod(v);
+    else if (k == "DO_ETA_CUT") doEtaCut = std::stoi(v);
+    else if (k == "ETA_MIN") minEta = std::stod(v);
+    else if (k == "ETA_MAX") maxEta = std::stod(v);
+    else if (k == "ZMIN") zmin = std::stod(v);
+    else if (k == "ZMAX") zmax = std::stod(v);
+    else if (k == "MMIN") mmin = std::stod(v);
+    else if (k == "MMAX") mmax = std::stod(v);
+    else if (k == "YMIN") ymin = std::stod(v);
+    else if (k == "YMAX") ymax = std::stod(v);
+    else if (k == "BINS_Z") nz = std::stoi(v);
+    else if (k == "BINS_M") nm = std::stoi(v);
+    else if (k == "BINS_Y") ny = std::stoi(v);
+    else if (k == "WS_R") R = std::stod(v);
+    else if (k == "WS_A") a = std::stod(v);
+    else if (k == "NUCLEUS_Z") Z = std::stoi(v);
+    else if (k == "NUCLEUS_A") A = std::stoi(v);
+    else if (k == "FLUX_POINT") isPoint = std::stoi(v);
+    else if (k == "BREAKUP_MODE") breakupMode = std::stoi(v);
+    else if (k == "NON_ZERO_GAM_PT") useNonzeroGamPt = std::stoi(v);
+    else if (k == "USE_POLARIZED_CS") usePolarizedCS = std::stoi(v);
+    else if (k == "SEED") seed = std::stol(v);
+    else return 1;  // accepted and ignored (PYTHIA_*, output flags, ...)
+  } catch (...) {
+    return -1;
+  }
+  return 0;
+}
+
+// ------------------------------------------------- elementary processes --
+// src/UpcTwoPhotonDilep.cpp:29-44, src/UpcGenerator.cpp:117-129
+int Ctx::setup_process() {
+  ignoreCSZ = false;
+  if (procID == 51) {  // src/UpcGenerator.cpp:105-115
+    ignoreCSZ = true;
+    mmin = alpMass - 4. * alpWidth;
+    mmax = alpMass + 4. * alpWidth;
+    mPart = alpMass;
+    partPDG = 51;
+    isCharged = false;
+    return 0;
+  }
+  if (procID == 11 || procID == 13 || procID == 15) {
+    partPDG = procID;
+    isCharged = true;
+    mPart = procID == 11 ? kMEl : (procID == 13 ? kMMu : kMTau);
+    if (mmin < mPart * 2.) mmin = mPart * 2.;
+    return 0;
+  }
+  return -1;  // light-by-light, dipion and vector mesons are not on this path
+}
+
+double Ctx::cs_m(double m, int flag) const {
+  if (procID == 51) {  // src/UpcTwoPhotonALP.cpp:28-33
+    if (flag) return 0;
+    double cs = 4. * M_PI * M_PI * alpWidth / (mPart * mPart);
+    cs *= kHc * kHc * 1e7 * kAlpha * kAlpha;
+    return cs;
+  }
+  if (flag == 0) {  // src/UpcTwoPhotonDilep.cpp:46-61
+    double s = m * m;
+    double x = 4 * mPart * mPart / s;
+    double b = std::sqrt(1 - x);
+    double y = std::atanh(b);
+    double cs = 0;
+    cs += (2 + 2 * x - x * x) * y - b * (1 + x);
+    cs += 4 * y * aLep;
+    cs += (4 * b / x + y) * aLep * aLep;
+    cs += (4 * b / x - 2 * y) * aLep * aLep * aLep;
+    cs += ((7. / 12.) * b / x + (1. / 6.) * b / x / x - 0.5 * y) * aLep * aLep * aLep * aLep;
+    cs *= 4 * kHc * kHc * 1e7 * kAlpha * kAlpha * M_PI / s;
+    return cs;
+  }
+  double r = 2 * mPart / m;  // src/UpcTwoPhotonDilep.cpp:85-97, 111-122
+  if (r > 1) return 0;
+  if (flag == 1)
+    return 4 * M_PI * kAlpha * kAlpha * kHc * kHc / m / m *
+           ((1 + r * r - 3. / 4. * r * r * r * r) * 2 * std::log(1 / r + std::sqrt(1 / r / r - 1)) -
+            (1 + 3. / 2. * r * r) * std::sqrt(1 - r * r));
+  return 4 * M_PI * kAlpha * kAlpha * kHc * kHc / m / m *
+         ((1 + r * r - 1. / 4. * r * r * r * r) * 2 * std::log(1 / r + std::sqrt(1 / r / r - 1)) -
+          (1 + 1. / 2. * r * r) * std::sqrt(1 - r * r));
+}
+
+double Ctx::cs_zm(double z, double m, int flag) const {
+  if (procID == 51) return 0;  // include/UpcTwoPhotonALP.h:50-58
+  if (flag == 0) {             // src/UpcTwoPhotonDilep.cpp:63-83
+    double s = m * m;
+    double k = std::sqrt(s) / 2.;
+    double p = std::sqrt(k * k - mPart * mPart);
+    double norm = 2 * M_PI * kAlpha * kAlpha / s * p / k;
+    double kt = -2 * k * (k - z * p) / mPart / mPart;
+    double ku = -2 * k * (k + z * p) / mPart / mPart;
+    double ks = kt + ku;
+    double kp = kt * ku;
+    double kq = 1. / kt + 1. / ku;
+    double kr = ku / kt + kt / ku;
+    double cs = 0;
+    cs += -8. * (4. * kq * kq + 4. * kq - kr);
+    cs += 16. * (2. + kr) * aLep;
+    cs += 4. * (2. - 4. * ks + kr) * aLep * aLep;
+    cs += -8. * (2. + 2. * ks + kr) * aLep * aLep * aLep;
+    cs += -4. * (4. + 2. * ks + 2. * kr - kp) * aLep * aLep * aLep * aLep;
+    cs *= norm;
+    return cs;
+  }
+  double mLep2 = mPart * mPart;
+  double m2 = m * m;
+  double z2 = z * z;
+  double cs = 2 * M_PI * kAlpha * kAlpha;
+  if (flag == 1) {  // src/UpcTwoPhotonDilep.cpp:99-109
+    cs *= m2 - 4 * mLep2;
+    cs *= std::sqrt(m2 - 4 * mLep2);
+    cs *= (4 * mLep2 * (3 - 2 * z2 + z2 * z2)) + m2 * (1 - z2 * z2);
+  } else {  // src/UpcTwoPhotonDilep.cpp:124-134
+    cs *= std::sqrt(m2 - 4 * mLep2);
+    cs *= m2 * m2 * (1 - z2 * z2) + 8 * m2 * mLep2 * (1 - z2 + z2 * z2) -
+          16 * mLep2 * mLep2 * (1 - z2) * (1 - z2);
+  }
+  cs /= m2 * m * (m2 * (1 - z2) + 4 * mLep2 * z2) * (m2 * (1 - z2) + 4 * mLep2 * z2);
+  return cs;
+}
+
+// ---------------------------------------------------------- nucleus -----
+double Ctx::calc_ws_rho() const {  // src/UpcCrossSection.cpp:152-163
+  const int nb = 200;
+  double bmax = 20.;
+  double db = bmax / (nb - 1.);
+  double v[nb];
+  for (int ib = 0; ib < nb; ib++) {
+    double r = ib * db;
+    v[ib] = r * r / (1. + std::exp((r - R) / a));
+  }
+  return A / simpson(nb, v, db) / 4. / M_PI;
+}
+
+void Ctx::prepare_gaa() {  // src/UpcCrossSection.cpp:364-414
+  const int nb = 200;
+  double bmax = 20.;
+  double db = bmax / (nb - 1);
+  double ssm = std::pow(sqrts, 2) / std::pow(2 * kMProt + 2.1206, 2);
+  double csNN = 0.1 * (34.41 + 0.2720 * std::pow(std::log(ssm), 2) +
+                       13.07 * std::pow(ssm, -0.4473) - 7.394 * std::pow(ssm, -0.5486));
+  std::vector<double> vB(nb), vTA(nb), row(nb), vs(nb), vGAA(nb);
+  for (int ib = 0; ib < nb; ib++) {
+    double b = ib * db;
+    for (int iz = 0; iz < nb; iz++) {
+      double z = iz * db;
+      double r = std::sqrt(b * b + z * z);
+      row[iz] = rho0 / (1 + std::exp((r - R) / a));
+    }
+    vTA[ib] = 2. * simpson(nb, row.data(), db);
+    vB[ib] = b;
+  }
+  NaturalSpline ta;
+  ta.build(vB.data(), vTA.data(), nb);
+  for (int ib = 0; ib < nb; ib++) {
+    double b = ib * db;
+    for (int is = 0; is < nb; is++) {
+      double s = is * db;
+      double sum_phi = 0;
+      for (int k = 0; k < 10; k++) {
+        if (kX10[k] < 0) continue;
+        double r = std::sqrt(b * b + s * s + 2. * b * s * std::cos(M_PI * kX10[k]));
+        sum_phi += 2. * M_PI * kW10[k] * ta.eval(r < bmax ? r : bmax);
+      }
+      vs[is] = 2. * s * ta.eval(s < bmax ? s : bmax) * sum_phi;
+    }
+    vGAA[ib] = std::exp(-csNN * simpson(nb, vs.data(), db));
+  }
+  gaa.build(vB.data(), vGAA.data(), nb);
+  cs_nn = csNN;
+}
+
+double Ctx::calc_form_fac(double Q2) const {  // src/UpcCrossSection.cpp:436-445
+  double Q = std::sqrt(Q2) / kHc;
+  double coshVal = std::cosh(M_PI * Q * a);
+  double sinhVal = std::sinh(M_PI * Q * a);
+  double ff = 4 * M_PI * M_PI * rho0 * a * a * a / (Q * a * Q * a * sinhVal * sinhVal) *
+              (M_PI * Q * a * coshVal * std::sin(Q * R) - Q * R * std::cos(Q * R) * sinhVal);
+  ff += 8 * M_PI * rho0 * a * a * a * std::exp(-R / a) / (1 + Q * Q * a * a) / (1 + Q * Q * a * a);
+  return ff;
+}
+
+void Ctx::prepare_form_fac() {  // src/UpcCrossSection.cpp:447-461
+  std::vector<double> q2(kNQ2), ff(kNQ2);
+#pragma omp parallel for schedule(static) num_threads(numThreads)
+  for (int i = 0; i < kNQ2; i++) {
+    q2[i] = kQ2min + i * kDQ2;
+    ff[i] = calc_form_fac(q2[i]);
+  }
+  formfac.build(q2.data(), ff.data(), kNQ2);
+}
+
+// ----------------------------------------------------- breakup (Starlight) --
+// Photo-neutron cross-section tables of src/UpcCrossSection.cpp:778-851 (data
+// tables, 1-based as in the reference; index 0 unused).
+static const double e1t[23] = {0., 103., 106., 112., 119., 127., 132., 145., 171., 199., 230., 235.,
+                               254., 280., 300., 320., 330., 333., 373., 390., 420., 426., 440.};
+static const double s1t[23] = {0., 12.0, 11.5, 12.0, 12.0, 12.0, 15.0, 17.0, 28.0, 33.0,
+                               52.0, 60.0, 70.0, 76.0, 85.0, 86.0, 89.0, 89.0, 75.0, 76.0, 69.0, 59.0, 61.0};
+static const double e2t[12] = {0., 2000., 3270., 4100., 4810., 6210., 6600.,
+                               7790., 8400., 9510., 13600., 16400.};
+static const double s2t[12] = {0., .1266, .1080, .0805, .1017, .0942, .0844, .0841, .0755, .0827,
+                               .0626, .0740};
+static const double e3t[29] = {0., 26., 28., 30., 32., 34., 36., 38., 40., 44., 46., 48., 50., 52., 55.,
+                               57., 62., 64., 66., 69., 72., 74., 76., 79., 82., 86., 92., 98., 103.};
+static const double s3t[29] = {0., 30., 21.5, 22.5, 18.5, 17.5, 15., 14.5, 19., 17.5, 16., 14.,
+                               20., 16.5, 17.5, 17., 15.5, 18., 15.5, 15.5, 15., 13.5, 18., 14.5, 15.5, 12.5, 13.,
+                               13., 12.};
+static const double sigt[160] = {
+    0., .4245, .4870, .5269, .4778, .4066, .3341, .2444, .2245, .2005,
+    .1783, .1769, .1869, .1940, .2117, .2226, .2327, .2395, .2646, .2790, .2756,
+    .2607, .2447, .2211, .2063, .2137, .2088, .2017, .2050, .2015, .2121, .2175,
+    .2152, .1917, .1911, .1747, .1650, .1587, .1622, .1496, .1486, .1438, .1556,
+    .1468, .1536, .1544, .1536, .1468, .1535, .1442, .1515, .1559, .1541, .1461,
+    .1388, .1565, .1502, .1503, .1454, .1389, .1445, .1425, .1415, .1424, .1432,
+    .1486, .1539, .1354, .1480, .1443, .1435, .1491, .1435, .1380, .1317, .1445,
+    .1375, .1449, .1359, .1383, .1390, .1361, .1286, .1359, .1395, .1327, .1387,
+    .1431, .1403, .1404, .1389, .1410, .1304, .1363, .1241, .1284, .1299, .1325,
+    .1343, .1387, .1328, .1444, .1334, .1362, .1302, .1338, .1339, .1304, .1314,
+    .1287, .1404, .1383, .1292, .1436, .1280, .1326, .1321, .1268, .1278, .1243,
+    .1239, .1271, .1213, .1338, .1287, .1343, .1231, .1317, .1214, .1370, .1232,
+    .1301, .1348, .1294, .1278, .1227, .1218, .1198, .1193, .1342, .1323, .1248,
+    .1220, .1139, .1271, .1224, .1347, .1249, .1163, .1362, .1236, .1462, .1356,
+    .1198, .1419, .1324, .1288, .1336, .1335, .1266};
+static const double sigtn[160] = {
+    0., .3125, .3930, .4401, .4582, .3774, .3329, .2996, .2715, .2165,
+    .2297, .1861, .1551, .2020, .2073, .2064, .2193, .2275, .2384, .2150, .2494,
+    .2133, .2023, .1969, .1797, .1693, .1642, .1463, .1280, .1555, .1489, .1435,
+    .1398, .1573, .1479, .1493, .1417, .1403, .1258, .1354, .1394, .1420, .1364,
+    .1325, .1455, .1326, .1397, .1286, .1260, .1314, .1378, .1353, .1264, .1471,
+    .1650, .1311, .1261, .1348, .1277, .1518, .1297, .1452, .1453, .1598, .1323,
+    .1234, .1212, .1333, .1434, .1380, .1330, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12};
+
+// Table set-up of src/UpcCrossSection.cpp:853-969 for lead (the reference
+// hard-codes zp = 82, ap = 208 whatever the configured nucleus, :758-759).
+void Ctx::prepare_breakup_tables() {
+  const double zp = 82, ap = 208;
+  const double si1 = 640., gg1 = 4.05, o1 = 13.42;
+  const double hbarcmev = 197.3269718, pi = 3.14159;
+  bu_gammatarg = 2. * g1 * g1 - 1.;
+  bu_omaxx = g1 > 500. ? 1.E10 : 1.E7;
+  bu_o0 = 7.4;
+  const double delo = .05;
+  const double scon = .1 * gg1 * gg1 * si1;
+  bu_zcon = zp / (bu_gammatarg * (pi) * (hbarcmev)) * zp / (bu_gammatarg * (pi) * (hbarcmev)) / 137.04;
+  bu_ee.assign(10001, 0.0);
+  bu_se.assign(10001, 0.0);
+  double* ee = bu_ee.data();
+  double* se = bu_se.data();
+  int ne = int((25. - bu_o0) / delo) + 1;
+  for (int i = 1; i <= ne; i++) {
+    ee[i] = bu_o0 + (i - 1) * delo;
+    se[i] = scon * ee[i] * ee[i] /
+            (((o1 * o1 - ee[i] * ee[i]) * (o1 * o1 - ee[i] * ee[i])) + ee[i] * ee[i] * gg1 * gg1);
+  }
+  int ij = ne;
+  for (int j = 1; j <= 27; j++) { ij = ij + 1; ee[ij] = e3t[j]; se[ij] = .1 * ap * s3t[j] / 208.; }
+  for (int j = 1; j <= 22; j++) { ij = ij + 1; ee[ij] = e1t[j]; se[ij] = .1 * ap * s1t[j] / 208.; }
+  for (int j = 9; j <= 70; j++) {
+    ij = ij + 1;
+    ee[ij] = ee[ij - 1] + 25.;
+    se[ij] = .1 * (zp * sigt[j] + (ap - zp) * sigtn[j]);
+  }
+  for (int j = 1; j <= 11; j++) { ij = ij + 1; ee[ij] = e2t[j]; se[ij] = .1 * ap * s2t[j]; }
+  const double x = .0677, y = .129, eps = .0808, eta = .4525, em = .94;
+  const double exx = std::pow(10, .05);
+  double s = .002 * em * ee[ij];
+  double ictr = 100;
+  if (bu_gammatarg > (2. * 150. * 150.)) ictr = 150;
+  for (int j = 1; j <= ictr; j++) {
+    ij = ij + 1;
+    s = s * exx;
+    ee[ij] = 1000. * .5 * (s - em * em) / em;
+    double pom = x * std::pow(s, eps);
+    double vec = y * std::pow(s, (-eta));
+    se[ij] = .1 * .65 * ap * (pom + vec);
+  }
+  ee[ij + 1] = 99999999999.;
+  bu_n = ij + 1;
+}
+
+// src/UpcCrossSection.cpp:972-1018 (XN sum and the mode formulas)
+double Ctx::breakup_prob(double b, int mode) const {
+  const double hbarcmev = 197.3269718;
+  const double* ee = bu_ee.data();
+  const double* se = bu_se.data();
+  double pxn = 0.;
+  double omax = std::min(bu_omaxx, 4. * bu_gammatarg * (hbarcmev) / b);
+  if (omax < bu_o0) return 0.;
+  double gk1m = bessel_k1_as(ee[1] * b / ((hbarcmev) * bu_gammatarg));
+  int k = 2;
+  while (ee[k] < omax) {
+    double gk1 = bessel_k1_as(ee[k] * b / ((hbarcmev) * bu_gammatarg));
+    pxn = pxn + bu_zcon * (ee[k] - ee[k - 1]) * .5 *
+                    (se[k - 1] * ee[k - 1] * gk1m * gk1m + se[k] * ee[k] * gk1 * gk1);
+    k = k + 1;
+    gk1m = gk1;
+  }
+  double p = 0.;
+  if (mode == 1) p = 1.;
+  if (mode == 2) p = (1 - std::exp(-1 * pxn)) * (1 - std::exp(-1 * pxn));
+  if (mode == 3) p = std::exp(-2 * pxn);
+  if (mode == 4) p = 2. * std::exp(-pxn) * (1. - std::exp(-pxn));
+  return p;
+}
+
+void Ctx::prepare_breakup() {  // src/UpcCrossSection.cpp:416-434
+  const double bmin = 1e-6, bmax = 1000;
+  const int nbc = 1000000;
+  const double db = (bmax - bmin) / nbc;
+  const int nuse = (int)((20. - bmin) / db) + 257;  // knots up to 20 fm + margin
+  std::vector<double> vb(nuse), vp(nuse);
+#pragma omp parallel for schedule(static) num_threads(numThreads)
+  for (int i = 0; i < nuse; i++) {
+    double b = bmin + db * i;
+    vb[i] = b;
+    vp[i] = breakup_prob(b, breakupMode);
+  }
+  breakup.build(vb.data(), vp.data(), nuse);
+}
+
+// -------------------------------------------------------------- fluxes --
+double Ctx::flux_point(double b, double k) const {  // src/UpcCrossSection.cpp:166-178
+  double g = g1;
+  double x = b * k / g / kHc;
+  double K0 = 0, K1 = 0;
+  if (x > 1e-10) bessel_k01(x, &K0, &K1);
+  return factor * k / g / g * (K1 * K1 + K0 * K0 / g / g);
+}
+
+double Ctx::flux_form(double b, double k, QagsResult* info) const {  // :181-218
+  if (isPoint || b > 2. * R) {
+    if (info) *info = QagsResult{};
+    return flux_point(b, k);
+  }
+  const double w = k, g = g1;
+  auto integrand = [&](double q) {
+    double t = q * q + w * w / g / g;
+    double ff = formfac.eval(t < kQ2max ? t : kQ2max - kDQ2);
+    return q * q * ff / t * ::j1(b * q / kHc);
+  };
+  QagsResult r = qags(integrand, 0., 10., 1e-4, 1e-4, 1000);
+  if (info) *info = r;
+  double Q = r.result / A;
+  return factor * Q * Q / k;
+}
+
+// ------------------------------------------------ two-photon luminosity --
+double Ctx::two_photon_lumi(double M, double Y) const {  // :221-271
+  double k1 = M / 2. * std::exp(Y);
+  double k2 = M / 2. * std::exp(-Y);
+  double b1min = isPoint ? R : 0.05 * R;
+  double b2min = isPoint ? R : 0.05 * R;
+  double b1max = std::max(5. * g1 * kHc / k1, 5. * R);
+  double b2max = std::max(5. * g2 * kHc / k2, 5. * R);
+  double ld1 = (std::log(b1max) - std::log(b1min)) / nb1;
+  double ld2 = (std::log(b2max) - std::log(b2min)) / nb2;
+  std::vector<double> flux(nb2);
+  for (int j = 0; j < nb2; j++) {
+    double b2l = b2min * std::exp(j * ld2);
+    double b2h = b2min * std::exp((j + 1.) * ld2);
+    double b2 = (b2h + b2l) / 2.;
+    flux[j] = flux_form(b2, k2, nullptr);
+  }
+  double sum = 0;
+  for (int i = 0; i < nb1; i++) {
+    double sum_b2 = 0.;
+    double b1l = b1min * std::exp(i * ld1);
+    double b1h = b1min * std::exp((i + 1) * ld1);
+    double b1 = (b1h + b1l) / 2.;
+    for (int j = 0; j < nb2; j++) {
+      double b2l = b2min * std::exp(j * ld2);
+      double b2h = b2min * std::exp((j + 1) * ld2);
+      double b2 = (b2h + b2l) / 2.;
+      double sum_phi = 0.;
+      for (int k = 0; k < 10; k++) {
+        if (kX10[k] < 0) continue;
+        double phi = M_PI * kX10[k];
+        double b = std::sqrt(b1 * b1 + b2 * b2 + 2. * b1 * b2 * std::cos(phi));
+        double brk = 1.;
+        if (breakupMode != 1) brk = breakup.eval(b < 20. ? b : 20.);
+        double g = b < 20. ? gaa.eval(b) : 1.;
+        sum_phi += brk * g * kW10[k];
+      }
+      sum_b2 += flux[j] * sum_phi * b2 * (b2h - b2l);
+    }
+    sum += flux_form(b1, k1, nullptr) * sum_b2 * b1 * (b1h - b1l);
+  }
+  return 2 * M_PI * M_PI * M * sum;
+}
+
+void Ctx::two_photon_lumi_pol(double M, double Y, double* ns, double* np) const {  // :274-335
+  double k1 = M / 2. * std::exp(Y);
+  double k2 = M / 2. * std::exp(-Y);
+  double b1min = isPoint ? 1 * R : 0.05 * R;
+  double b2min = isPoint ? 1 * R : 0.05 * R;
+  double b1max = std::max(5. * g1 * kHc / k1, 5 * R);
+  double b2max = std::max(5. * g2 * kHc / k2, 5 * R);
+  double ld1 = (std::log(b1max) - std::log(b1min)) / nb1;
+  double ld2 = (std::log(b2max) - std::log(b2min)) / nb2;
+  std::vector<double> flux(nb2);
+  for (int j = 0; j < nb2; ++j) {
+    double b2l = b2min * std::exp(j * ld2);
+    double b2h = b2min * std::exp((j + 1) * ld2);
+    flux[j] = flux_form((b2h + b2l) / 2., k2, nullptr);
+  }
+  double s1s = 0, s1p = 0;
+  for (int i = 0; i < nb1; i++) {
+    double b1l = b1min * std::exp(i * ld1);
+    double b1h = b1min * std::exp((i + 1) * ld1);
+    double b1 = (b1h + b1l) / 2.;
+    double ff_b1 = flux_form(b1, k1, nullptr);
+    double s2s = 0, s2p = 0;
+    for (int j = 0; j < nb2; ++j) {
+      double b2l = b2min * std::exp(j * ld2);
+      double b2h = b2min * std::exp((j + 1) * ld2);
+      double b2 = (b2h + b2l) / 2.;
+      double sps = 0., spp = 0.;
+      for (int k = 0; k < 10; k++) {
+        if (kX10[k] < 0) continue;
+        double phi = M_PI * kX10[k];
+        double cphi = std::cos(phi);
+        double sphi = std::sin(phi);
+        double b = std::sqrt(b1 * b1 + b2 * b2 - 2. * b1 * b2 * cphi);
+        double brk = 1.;
+        if (breakupMode != 1) brk = breakup.eval(b < 20. ? b : 20.);
+        double g = b < 20 ? gaa.eval(b) : 1.;
+        sps += brk * g * kW10[k] * cphi * cphi;
+        spp += brk * g * kW10[k] * sphi * sphi;
+      }
+      s2s += sps * flux[j] * b2 * (b2h - b2l);
+      s2p += spp * flux[j] * b2 * (b2h - b2l);
+    }
+    s1s += s2s * ff_b1 * b1 * (b1h - b1l);
+    s1p += s2p * ff_b1 * b1 * (b1h - b1l);
+  }
+  *ns = 2. * M_PI * M_PI * M * s1s;
+  *np = 2. * M_PI * M_PI * M * s1p;
+}
+
+// UpcGenerator::init process overrides + UpcCrossSection::init (without the
+// luminosity table, which uo_lumi_table fills).
+int Ctx::init_tables() {
+  if (setup_process() != 0) return -2;
+  factor = Z * Z * kAlpha / M_PI / M_PI / kHc / kHc;  // src/UpcCrossSection.cpp:120
+  rho0 = calc_ws_rho();
+  prepare_gaa();
+  prepare_form_fac();
+  prepare_breakup_tables();
+  if (breakupMode > 1) prepare_breakup();
+  initialized = true;
+  return 0;
+}
+
+// prepareTwoPhotonLumi's OpenMP region (src/UpcCrossSection.cpp:515-576):
+// static m-slices per thread, left bin edges, lumi*dm*dy.
+int Ctx::lumi_table(double* out, double* out2, int im_lo, int im_hi) const {
+  const double dy = (ymax - ymin) / ny;
+  const double dm = (mmax - mmin) / nm;
+  const int nthr = numThreads < 1 ? 1 : numThreads;
+  const int span = im_hi - im_lo;
+#pragma omp parallel num_threads(nthr)
+  {
+    const int t = omp_get_thread_num();
+    const int lo = im_lo + span * t / nthr;
+    const int hi = im_lo + span * (t + 1) / nthr;
+    for (int im = lo; im < hi; ++im) {
+      double m = mmin + dm * im;
+      for (int iy = 0; iy < ny; ++iy) {
+        double y = ymin + dy * iy;
+        const size_t o = (size_t)(im - im_lo) * ny + iy;
+        if (usePolarizedCS) {
+          double ls, lp;
+          two_photon_lumi_pol(m, y, &ls, &lp);
+          out[o] = ls * dm * dy;
+          if (out2) out2[o] = lp * dm * dy;
+        } else {
+          out[o] = two_photon_lumi(m, y) * dm * dy;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+// src/UpcCrossSection.cpp:337-362
+void Ctx::cs_zm_table(int flag, double* out) const {
+  constexpr double scalingFactor = 0.1973269718 * 0.1973269718 * 1e7;
+  double dm = (mmax - mmin) / nm;
+  double dz = (zmax - zmin) / nz;
+  for (int im = 0; im < nm; ++im) {
+    double m = mmin + dm * im;
+    for (int iz = 0; iz < nz; ++iz) {
+      double z = zmin + dz * iz;
+      out[(size_t)im * nz + iz] = cs_zm(z, m, flag) * scalingFactor / dm;
+    }
+  }
+}
+
+// src/UpcCrossSection.cpp:594-698 (fold, summed in m-slice order)
+void Ctx::nuc_cs_ym(const double* lumi, const double* lumi2, double* cs, double* ratio,
+                    double* tot) const {
+  double dm = (mmax - mmin) / nm;
+  double total = 0;
+  for (int im = 0; im < nm; ++im) {
+    double m = mmin + dm * im;
+    for (int iy = 0; iy < ny; ++iy) {
+      const size_t lo = (size_t)im * ny + iy;
+      const size_t co = (size_t)iy * nm + im;
+      if (!usePolarizedCS) {
+        cs[co] = cs_m(m, 0) * lumi[lo];
+      } else {
+        double nuccs_s = lumi[lo] * cs_m(m, 1);
+        double nuccs_p = lumi2[lo] * cs_m(m, 2);
+        cs[co] = (nuccs_s + nuccs_p) * 1e7;
+        if (ratio) ratio[co] = nuccs_s / nuccs_p;
+      }
+      total += cs[co];
+    }
+  }
+  *tot = total * 1e-6;
+}
+
+}  // namespace uo
+
+// ------------------------------------------------------------ C interface --
+using uo::Ctx;
+
+extern "C" {
+uo_ctx* uo_create(void) { return new uo_ctx(); }
+void uo_destroy(uo_ctx* h) { delete h; }
+int uo_set_param(uo_ctx* h, const char* k, const char* v) { return h->c.set_param(k, v); }
+void uo_set_num_threads(uo_ctx* h, int n) { h->c.numThreads = n; }
+int uo_init_tables(uo_ctx* h) { return h->c.init_tables(); }
+void uo_grid(const uo_ctx* h, double* mmin, double* mmax, int* nm, double* ymin,
+             double* ymax, int* ny, double* zmin, double* zmax, int* nz) {
+  *mmin = h->c.mmin; *mmax = h->c.mmax; *nm = h->c.nm;
+  *ymin = h->c.ymin; *ymax = h->c.ymax; *ny = h->c.ny;
+  *zmin = h->c.zmin; *zmax = h->c.zmax; *nz = h->c.nz;
+}
+double uo_rho0(const uo_ctx* h) { return h->c.rho0; }
+double uo_gamma(const uo_ctx* h) { return h->c.g1; }
+void uo_bessel_k01(double x, double* k0, double* k1) { uo::bessel_k01(x, k0, k1); }
+double uo_bessel_k1_as(double x) { return uo::bessel_k1_as(x); }
+double uo_simpson(int n, const double* v, double h) { return uo::simpson(n, v, h); }
+
+// Test integrands for the QAGS pins: 0: x^p0 (p0 > -1), 1: cos(p0 x)*exp(-p1 x),
+// 2: log(x)/sqrt(x)-like singular x^p0*log(x), 3: p0-oscillatory J1 Hankel kernel
+// x^2/(x^2+p1) J1(p0 x).
+int uo_qags_test(int id, double p0, double p1, double a, double b, double epsabs,
+                 double epsrel, int limit, double* result, double* abserr, int* neval,
+                 int* nint) {
+  auto f = [&](double x) -> double {
+    switch (id) {
+      case 0: return std::pow(x, p0);
+      case 1: return std::cos(p0 * x) * std::exp(-p1 * x);
+      case 2: return std::pow(x, p0) * std::log(x);
+      default: return x * x / (x * x + p1) * ::j1(p0 * x);
+    }
+  };
+  uo::QagsResult r = uo::qags(f, a, b, epsabs, epsrel, limit);
+  *result = r.result; *abserr = r.abserr; *neval = r.neval; *nint = r.nintervals;
+  return r.status;
+}
+
+void uo_spline_natural(int n, const double* x, const double* y, int m, const double* xe,
+                       double* ye) {
+  uo::NaturalSpline s;
+  s.build(x, y, n);
+  for (int i = 0; i < m; ++i) ye[i] = s.eval(xe[i]);
+}
+
+double uo_flux_point(const uo_ctx* h, double b, double k) { return h->c.flux_point(b, k); }
+double uo_flux_form(const uo_ctx* h, double b, double k, int* status, int* neval, int* nint) {
+  uo::QagsResult r;
+  double v = h->c.flux_form(b, k, &r);
+  if (status) *status = r.status;
+  if (neval) *neval = r.neval;
+  if (nint) *nint = r.nintervals;
+  return v;
+}
+double uo_form_factor(const uo_ctx* h, double q2) { return h->c.calc_form_fac(q2); }
+double uo_form_factor_spline(const uo_ctx* h, double q2) { return h->c.formfac.eval(q2); }
+double uo_gaa(const uo_ctx* h, double b) { return h->c.gaa.eval(b); }
+double uo_breakup_prob(const uo_ctx* h, double b, int mode) { return h->c.breakup_prob(b, mode); }
+double uo_breakup_spline(const uo_ctx* h, double b) { return h->c.breakup.eval(b); }
+double uo_two_photon_lumi(const uo_ctx* h, double m, double y) { return h->c.two_photon_lumi(m, y); }
+void uo_two_photon_lumi_pol(const uo_ctx* h, double m, double y, double* ls, double* lp) {
+  h->c.two_photon_lumi_pol(m, y, ls, lp);
+}
+double uo_cs_m(const uo_ctx* h, double m, int flag) { return h->c.cs_m(m, flag); }
+double uo_cs_zm(const uo_ctx* h, double z, double m, int flag) { return h->c.cs_zm(z, m, flag); }
+int uo_lumi_table(uo_ctx* h, double* lumi, double* lumi2, int im_lo, int im_hi) {
+  if (!h->c.initialized) return -1;
+  return h->c.lumi_table(lumi, lumi2, im_lo, im_hi);
+}
+int uo_cs_zm_table(const uo_ctx* h, int flag, double* out) {
+  h->c.cs_zm_table(flag, out);
+  return 0;
+}
+int uo_nuc_cs_ym(const uo_ctx* h, const double* lumi, const double* lumi2, double* cs,
+                 double* ratio, double* tot_mb) {
+  h->c.nuc_cs_ym(lumi, lumi2, cs, ratio, tot_mb);
+  return 0;
+}
+int uo_sampler_bin(int nbins, double lo, double hi, double x) {
+  // include/UpcSampler.h:124-134, including the misplaced int(): the
+  // numerator is truncated before the division by the range.
+  return int(nbins * (x - lo)) / (hi - lo);
+}
+}

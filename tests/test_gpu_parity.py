@@ -1,0 +1,226 @@
+"""GPU parity of the plain FP64 path against the CPU oracle (relative 1e-10).
+
+Every product value comes through the C ABI of libupcgen_gb300.so; the oracle
+is the FP64 restatement of the reference (oracle/).
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10  # plain FP64 path vs the oracle, relative
+
+C1 = {"NUCLEUS_Z": 82, "NUCLEUS_A": 208, "WS_R": 6.68, "WS_A": 0.447, "SQRTS": 5020,
+      "PROC_ID": 13, "LEP_A": 0, "FLUX_POINT": 1, "BREAKUP_MODE": 1,
+      "MMIN": 3.56, "MMAX": 50, "BINS_M": 201, "YMIN": -6, "YMAX": 6, "BINS_Y": 61,
+      "ZMIN": -1, "ZMAX": 1, "BINS_Z": 100, "SEED": 1}
+# config-2 physics (WS form-factor flux, XNXN, tau pairs) on a coarser grid
+C2S = dict(C1, PROC_ID=15, FLUX_POINT=0, BREAKUP_MODE=2, BINS_M=21, BINS_Y=13,
+           DO_PT_CUT=1, PT_MIN=1, DO_ETA_CUT=1, ETA_MIN=-2.4, ETA_MAX=2.4)
+
+
+def _oracle(oracle_mod, params):
+    o = oracle_mod.Oracle(params, threads=os.cpu_count())
+    o.init_tables()
+    return o
+
+
+def _gen(ug, params):
+    g = ug.UpcGenerator(params)
+    g.init()
+    return g
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    den = np.maximum(np.abs(b), 1e-300)
+    return np.max(np.abs(a - b) / den)
+
+
+def test_philox_known_answers(ug):
+    # Random123 known-answer vectors for philox4x32-10
+    out = ug.philox(0, 0, 1)
+    assert [hex(v) for v in out[0]] == ["0x6627e8d5", "0xe169c58d", "0xbc57ac4c", "0x9b00dbd8"]
+
+
+@pytest.mark.parametrize("params", [C1, dict(C1, BREAKUP_MODE=2, FLUX_POINT=0)])
+def test_tables_vs_oracle(ug, oracle_mod, params):
+    g = _gen(ug, dict(params, BINS_M=3, BINS_Y=3))
+    o = _oracle(oracle_mod, params)
+    cs = g.nucProcessCS
+    b = np.linspace(0.0, 20.0, 777)
+    gref = np.array([o.gaa(x) for x in b])
+    assert np.max(np.abs(cs.spline("gaa", b) - gref) / np.maximum(np.abs(gref), 1e-3)) < 1e-12
+    q2 = np.concatenate([np.geomspace(1e-9, 1.99, 500), [1.999998]])
+    ff_ref = np.array([o.form_factor(x) for x in q2])
+    assert rel(cs.calcFormFac(q2), ff_ref) < 1e-10
+    assert rel(cs.spline("formfac", q2), [o.form_factor_spline(x) for x in q2]) < 1e-10
+    bb = np.geomspace(1e-6, 999.0, 300)
+    for mode in (2, 3, 4):
+        assert rel(cs.calcBreakupProb(bb, mode), [o.breakup_prob(x, mode) for x in bb]) < 1e-12
+    if params["BREAKUP_MODE"] > 1:
+        bs = np.linspace(1e-6, 20.0, 999)
+        assert rel(cs.spline("breakup", bs), [o.breakup_spline(x) for x in bs]) < 1e-10
+
+
+def test_flux_vs_oracle(ug, oracle_mod):
+    params = dict(C1, FLUX_POINT=0, BINS_M=3, BINS_Y=3)
+    g = _gen(ug, params)
+    o = _oracle(oracle_mod, params)
+    rng = np.random.default_rng(7)
+    b = rng.uniform(0.05 * 6.68, 30.0, 400)
+    k = np.exp(rng.uniform(np.log(4.4e-3), np.log(1e3), 400))
+    fp = g.nucProcessCS.fluxPoint(b, k)
+    assert rel(fp, [o.flux_point(x, y) for x, y in zip(b, k)]) < 1e-12
+    ff = g.nucProcessCS.fluxForm(b, k)
+    ref = np.array([o.flux_form(x, y) for x, y in zip(b, k)])
+    assert rel(ff, ref) < TOL
+    assert g.qagsStats()["failures"] == 0
+
+
+def test_lumi_config1_full_grid(ug, oracle_mod):
+    g = _gen(ug, C1)
+    o = _oracle(oracle_mod, C1)
+    lumi = g.lumiTable()
+    ref = o.lumi_table()
+    assert lumi.shape == (201, 61)
+    assert rel(lumi, ref) < TOL
+    cs, tot = g.nucCSYM()
+    rcs, rtot, _ = o.nuc_cs_ym(ref)
+    assert rel(cs, rcs) < TOL
+    assert abs(tot / rtot - 1) < TOL
+
+
+def test_lumi_form_factor_xnxn(ug, oracle_mod):
+    g = _gen(ug, C2S)
+    o = _oracle(oracle_mod, C2S)
+    lumi = g.lumiTable()
+    ref = o.lumi_table()
+    assert rel(lumi, ref) < TOL
+    st = g.qagsStats()
+    assert st["failures"] == 0 and st["max_intervals"] < 1000
+    cs, tot = g.nucCSYM()
+    rcs, rtot, _ = o.nuc_cs_ym(ref)
+    assert abs(tot / rtot - 1) < TOL
+
+
+@pytest.mark.parametrize("mode", [3, 4])
+def test_lumi_breakup_modes(ug, oracle_mod, mode):
+    p = dict(C1, BREAKUP_MODE=mode, BINS_M=15, BINS_Y=11)
+    assert rel(_gen(ug, p).lumiTable(), _oracle(oracle_mod, p).lumi_table()) < TOL
+
+
+def test_lumi_polarized(ug, oracle_mod):
+    p = dict(C1, BREAKUP_MODE=2, USE_POLARIZED_CS=1, BINS_M=11, BINS_Y=9)
+    g = _gen(ug, p)
+    s, ps = g.lumiTable(polarized=True)
+    rs, rp = _oracle(oracle_mod, p).lumi_table(polarized=True)
+    assert rel(s, rs) < TOL and rel(ps, rp) < TOL
+
+
+def test_lumi_alp_other_nucleus(ug, oracle_mod):
+    p = dict(C1, PROC_ID=51, ALP_MASS=1, ALP_WIDTH=0.01, NUCLEUS_Z=79, NUCLEUS_A=197,
+             WS_R=6.38, WS_A=0.535, SQRTS=200, BREAKUP_MODE=4, BINS_M=21, BINS_Y=25)
+    g = _gen(ug, p)
+    o = _oracle(oracle_mod, p)
+    assert g.grid()["mmin"] == pytest.approx(0.96) and g.grid()["mmax"] == pytest.approx(1.04)
+    ref = o.lumi_table()
+    assert rel(g.lumiTable(), ref) < TOL
+    _, tot = g.nucCSYM()
+    assert abs(tot / o.nuc_cs_ym(ref)[1] - 1) < TOL
+
+
+def test_cs_zm_tables(ug, oracle_mod):
+    for flag in (0, 1, 2):
+        p = dict(C1, PROC_ID=15)
+        g = ug.UpcGenerator(p)
+        o = oracle_mod.Oracle(p)
+        o.init_tables()
+        assert rel(g.crossSectionZM(flag), o.cs_zm_table(flag)) < 1e-12
+
+
+def test_point_lumi_entry(ug, oracle_mod):
+    g = ug.UpcGenerator(C2S)
+    o = _oracle(oracle_mod, C2S)
+    m = np.array([3.6, 10.0, 49.0, 20.0])
+    y = np.array([-5.9, 0.0, 2.5, 5.5])
+    assert rel(g.nucProcessCS.calcTwoPhotonLumi(m, y), [o.two_photon_lumi(a, b) for a, b in zip(m, y)]) < TOL
+
+
+def _chi2_two_sample(a, b, bins):
+    from scipy import stats
+    ha, _ = np.histogram(a, bins)
+    hb, _ = np.histogram(b, bins)
+    na, nb = ha.sum(), hb.sum()
+    keep = (ha + hb) > 0
+    ha, hb = ha[keep].astype(float), hb[keep].astype(float)
+    chi2 = np.sum((ha * np.sqrt(nb / na) - hb * np.sqrt(na / nb)) ** 2 / (ha + hb))
+    return stats.chi2.sf(chi2, keep.sum() - 1)
+
+
+def _pt(p):
+    return np.hypot(p[:, 0], p[:, 1])
+
+
+def _eta(p):
+    return np.arcsinh(p[:, 2] / np.maximum(_pt(p), 1e-30))
+
+
+@pytest.mark.parametrize("gampt", [0, 1])
+def test_events_distributions(ug, oracle_mod, gampt):
+    p = dict(C1, BINS_M=41, BINS_Y=21, NON_ZERO_GAM_PT=gampt, DO_PT_CUT=1, PT_MIN=1.0,
+             DO_ETA_CUT=1, ETA_MIN=-2.4, ETA_MAX=2.4)
+    g = _gen(ug, p)
+    o = _oracle(oracle_mod, p)
+    lumi = o.lumi_table()
+    cs, tot, _ = o.nuc_cs_ym(lumi)
+    n = 60000 if gampt else 200000
+    rec, rej_o, mbin_o = o.generate(cs, o.cs_zm_table(0), n, 12345)
+    ev, rej_g, mbin_g = g.generateEvents(n, with_mbin=True)
+    pg = np.concatenate([ev["p0"], ev["p1"]])
+    po = np.concatenate([rec[:, 4:8], rec[:, 8:12]])
+    checks = {
+        "m": (ev["m"], rec[:, 0], np.linspace(3.56, 50, 41)),
+        "y": (ev["y"], rec[:, 1], np.linspace(-6, 6, 25)),
+        "z": (ev["z"], rec[:, 2], np.linspace(-1, 1, 21)),
+        "pt": (_pt(pg), _pt(po), np.linspace(1.0, 25.0, 25)),
+        "eta": (_eta(pg), _eta(po), np.linspace(-2.4, 2.4, 25)),
+    }
+    for name, (a, b, bins) in checks.items():
+        pv = _chi2_two_sample(a, b, bins)
+        assert pv > 1e-4, f"{name}: chi2 p-value {pv:.2e}"
+    # acceptance fractions agree within statistics
+    fa, fb = n / (n + rej_g), n / (n + rej_o)
+    sig = np.sqrt(fa * (1 - fa) / (n + rej_g) + fb * (1 - fb) / (n + rej_o))
+    assert abs(fa - fb) < 5 * sig + 1e-3
+    assert g.fidNuclX() == pytest.approx(g.totNuclX() * n / (n + rej_g), rel=1e-12)
+    # every kept event passes the cuts
+    assert np.all(_pt(ev["p0"]) >= 1.0 - 1e-5) and np.all(np.abs(_eta(ev["p1"])) <= 2.4 + 1e-5)
+
+
+def test_events_sequence_and_bins(ug, oracle_mod):
+    p = dict(C2S, BINS_M=21, BINS_Y=13)
+    g = _gen(ug, p)
+    ev_all, rej_all, mb = g.generateEvents(20000, with_mbin=True)
+    g.setSeed(1)
+    a, ra = g.generateEvents(7000)
+    b, rb = g.generateEvents(13000)
+    assert ra + rb == rej_all
+    assert np.array_equal(np.concatenate([a, b]).view(np.uint8), ev_all.view(np.uint8))
+    # getBinY with the reference's truncation, on the stored masses away from
+    # the truncation boundaries
+    grid = g.grid()
+    x = 21 * (ev_all["m"].astype(np.float64) - grid["mmin"])
+    ok = np.abs(x - np.round(x)) > 1e-3
+    lo, hi = grid["mmin"], grid["mmin"] + (grid["mmax"] - grid["mmin"]) / 21 * 21
+    ref = np.array([oracle_mod.sampler_bin(21, lo, hi, float(m)) for m in ev_all["m"][ok]])
+    assert np.array_equal(mb[ok], ref)
+
+
+def test_generate_event_single(ug):
+    p = dict(C2S, BINS_M=11, BINS_Y=7)
+    g = _gen(ug, p)
+    flags = [g.generateEvent()[0] for _ in range(3000)]
+    assert set(flags) <= {0, 1} and 0 < sum(flags) < 3000

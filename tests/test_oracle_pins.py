@@ -1,0 +1,192 @@
+"""Pins of the CPU oracle (no GPU).
+
+The reference cannot be built here (ROOT/GSL), so the oracle is pinned
+(1) against the reference's own elementary cross sections, compiled from its
+sources (golden ref_elem.json, bit for bit), (2) primitive by primitive against
+scipy, and (3) against the independent numpy/scipy restatement in
+tests/golden/make_golden.py (golden numpy_restatement.json).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+from scipy import integrate, interpolate, special
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    with open(os.path.join(GOLD, name)) as f:
+        return json.load(f)
+
+
+def test_elementary_cs_bit_exact_vs_reference(oracle_mod):
+    g = load("ref_elem.json")
+    for e in g["dilep"]:
+        o = oracle_mod.Oracle({"PROC_ID": e["pdg"], "LEP_A": e["alep"]})
+        o.init_tables()
+        for flag in (0, 1, 2):
+            assert o.cs_m(e["m"], flag) == e["cs_m"][flag]
+            for z, v in zip(e["z"], e["cs_zm"][flag]):
+                got = o.cs_zm(z, e["m"], flag)
+                assert got == v or (np.isnan(got) and np.isnan(v)), (e["pdg"], flag, z, got, v)
+    for e in g["alp"]:
+        o = oracle_mod.Oracle({"PROC_ID": 51, "ALP_MASS": e["mass"], "ALP_WIDTH": e["width"]})
+        o.init_tables()
+        assert o.cs_m(e["m"], 0) == e["cs_m"]
+
+
+def test_live_reference_elementary(oracle_mod):
+    L = oracle_mod.ref_lib()
+    if L is None:
+        pytest.skip("reference sources not present on this machine")
+    o = oracle_mod.Oracle({"PROC_ID": 15})
+    o.init_tables()
+    for m in np.geomspace(3.56, 50, 23):
+        assert o.cs_m(m, 0) == L.uref_dilep_cs_m(15, 0.0, m, 0)
+        for z in np.linspace(-0.99, 0.99, 9):
+            assert o.cs_zm(z, m, 0) == L.uref_dilep_cs_zm(15, 0.0, z, m, 0)
+
+
+def test_bessel_k_vs_scipy(oracle_mod):
+    x = np.concatenate([np.geomspace(1e-9, 2, 300), np.linspace(2, 30, 300), np.linspace(30, 700, 100)])
+    for xi in x:
+        k0, k1 = oracle_mod.bessel_k01(float(xi))
+        assert k0 == pytest.approx(special.k0(xi), rel=5e-15, abs=0)
+        assert k1 == pytest.approx(special.k1(xi), rel=5e-15, abs=0)
+
+
+def test_abramowitz_stegun_k1(oracle_mod):
+    # A&S 9.8.7/9.8.8 quote |error| < 8e-9 (x K1 e^x scale); relative ~2e-7
+    for xi in np.geomspace(1e-6, 50, 400):
+        assert oracle_mod.bessel_k1_as(float(xi)) == pytest.approx(special.k1(xi), rel=3e-7)
+
+
+def test_gauss_kronrod_exactness():
+    from numpy.polynomial import legendre
+    xg = np.array([0.995657163025808080735527280689003, 0.973906528517171720077964012084452,
+                   0.930157491355708226001207180059508, 0.865063366688984510732096688423493,
+                   0.780817726586416897063717578345042, 0.679409568299024406234327365114874,
+                   0.562757134668604683339000099272694, 0.433395394129247190799265943165784,
+                   0.294392862701460198131126603103866, 0.148874338981631210884826001129720, 0.0])
+    wk = np.array([0.011694638867371874278064396062192, 0.032558162307964727478818972459390,
+                   0.054755896574351996031381300244580, 0.075039674810919952767043140916190,
+                   0.093125454583697605535065465083366, 0.109387158802297641899210590325805,
+                   0.123491976262065851077208980430855, 0.134709217311473325928054001771707,
+                   0.142775938577060080797094273138717, 0.147739104901338491374841515972068,
+                   0.149445554002916905664936468389821])
+    wg = np.array([0.066671344308688137593568809893332, 0.149451349150580593145776339657697,
+                   0.219086362515982043995534934228163, 0.269266719309996355091226921569469,
+                   0.295524224714752870173892994651338])
+    xs = np.concatenate([-xg[:10], xg[::-1]])
+    ws = np.concatenate([wk[:10], wk[::-1]])
+    for p in range(0, 32):
+        exact = 0.0 if p % 2 else 2.0 / (p + 1)
+        assert np.dot(ws, xs ** p) == pytest.approx(exact, abs=1e-14)
+    gx, gw = legendre.leggauss(10)
+    assert np.allclose(np.sort(np.abs(gx))[::2], np.sort(xg[1:10:2]), atol=1e-15)
+    assert np.allclose(np.sort(gw)[::2], np.sort(wg), atol=1e-15)
+
+
+@pytest.mark.parametrize("fid,p0,p1,a,b", [
+    (0, 2.5, 0, 0.0, 1.0), (1, 7.0, 0.3, 0.0, 10.0), (2, -0.5, 0, 0.0, 1.0),
+    (3, 30.0, 0.01, 0.0, 10.0), (3, 400.0, 1e-4, 0.0, 10.0)])
+def test_qags_vs_quadpack(oracle_mod, fid, p0, p1, a, b):
+    f = {0: lambda x: x ** p0, 1: lambda x: np.cos(p0 * x) * np.exp(-p1 * x),
+         2: lambda x: x ** p0 * np.log(x), 3: lambda x: x * x / (x * x + p1) * special.j1(p0 * x)}[fid]
+    r, e, ne, ni, st = oracle_mod.qags_test(fid, p0, p1, a, b, 1e-4, 1e-4)
+    q = integrate.quad(f, a, b, epsabs=1e-4, epsrel=1e-4, limit=1000, full_output=1)
+    assert st == 0
+    # same algorithm: same number of evaluations; results agree to rounding
+    # (extrapolated results to the extrapolation's own accuracy)
+    assert ne == q[2]["neval"]
+    assert r == pytest.approx(q[0], rel=1e-9, abs=1e-12)
+
+
+def test_spline_vs_scipy(oracle_mod):
+    rng = np.random.default_rng(3)
+    x = np.cumsum(rng.uniform(0.1, 1.0, 300))
+    y = np.sin(x) * np.exp(-0.01 * x)
+    xe = np.sort(rng.uniform(x[0], x[-1], 1000))
+    ref = interpolate.CubicSpline(x, y, bc_type="natural")(xe)
+    assert np.allclose(oracle_mod.spline_natural(x, y, xe), ref, rtol=0, atol=1e-13)
+
+
+def test_simpson_weights(oracle_mod):
+    v = np.arange(10.0) ** 2
+    h = 0.5
+    expected = (v[0] + v[-1] + 4 * v[1:-1:2].sum() + 2 * v[2:-1:2].sum()) * h / 3
+    assert oracle_mod.simpson(v, h) == expected
+
+
+def test_sampler_bin_truncation(oracle_mod):
+    # include/UpcSampler.h:124-134: int(n*(x-x0)) / (x1-x0), truncated again
+    for x in np.random.default_rng(5).uniform(3.56, 50.0, 2000):
+        expected = int(int(1001 * (x - 3.56)) / (50.0 - 3.56))
+        assert oracle_mod.sampler_bin(1001, 3.56, 50.0, float(x)) == expected
+    # differs from the plain bin index for some masses (the reference's quirk)
+    xs = np.linspace(3.56, 49.99, 20011)
+    plain = np.floor((xs - 3.56) / (50 - 3.56) * 1001).astype(int)
+    quirk = np.array([oracle_mod.sampler_bin(1001, 3.56, 50.0, float(x)) for x in xs])
+    assert np.any(plain != quirk) and np.all(np.abs(plain - quirk) <= 1)
+
+
+class TestNumpyRestatement:
+    g = load("numpy_restatement.json")
+
+    @pytest.fixture(scope="class")
+    def o(self, oracle_mod):
+        o = oracle_mod.Oracle({"PROC_ID": 15, "BREAKUP_MODE": 2, "FLUX_POINT": 0})
+        o.init_tables()
+        return o
+
+    def test_rho0_gaa(self, o):
+        assert o.rho0() == pytest.approx(self.g["rho0"], rel=1e-14)
+        for b, v in zip(self.g["gaa"]["b"], self.g["gaa"]["v"]):
+            # G_AA spans 300 decades; below ~1e-20 the spline is rounding-level
+            assert o.gaa(b) == pytest.approx(v, rel=1e-11, abs=1e-14)
+
+    def test_form_factor(self, o):
+        ff = self.g["form_factor"]
+        for q2, v, s in zip(ff["q2"], ff["v"], ff["spline"]):
+            assert o.form_factor(q2) == pytest.approx(v, rel=1e-9)
+            assert o.form_factor_spline(q2) == pytest.approx(s, rel=1e-9)
+
+    def test_breakup(self, o):
+        br = self.g["breakup"]
+        for mode, vals in br["modes"].items():
+            for b, v in zip(br["b"], vals):
+                assert o.breakup_prob(b, int(mode)) == pytest.approx(v, rel=1e-11, abs=1e-300)
+        sp = self.g["breakup_spline_xnxn"]
+        for b, v in zip(sp["b"], sp["v"]):
+            assert o.breakup_spline(b) == pytest.approx(v, rel=1e-11, abs=1e-300)
+
+    def test_flux_form(self, o):
+        for e in self.g["flux_form"]:
+            assert o.flux_form(e["b"], e["k"]) == pytest.approx(e["v"], rel=1e-9)
+
+    def test_lumi_cells(self, oracle_mod):
+        for c in self.g["lumi_cells"]:
+            o = oracle_mod.Oracle({"PROC_ID": 13, "FLUX_POINT": c["flux_point"], "BREAKUP_MODE": c["mode"]})
+            o.init_tables()
+            assert o.two_photon_lumi(c["M"], c["Y"]) == pytest.approx(c["L"], rel=1e-10)
+
+
+def test_breakup_mode_identity(oracle_mod):
+    # modes 2 + 3 + 4 sum to one: (1-e)^2 + e^2 + 2e(1-e) = 1
+    o = oracle_mod.Oracle({"PROC_ID": 13})
+    o.init_tables()
+    for b in np.geomspace(1e-3, 900, 60):
+        s = sum(o.breakup_prob(b, m) for m in (2, 3, 4))
+        assert s == pytest.approx(1.0, abs=1e-15)
+
+
+def test_gaa_limits(oracle_mod):
+    o = oracle_mod.Oracle({"PROC_ID": 13})
+    o.init_tables()
+    assert o.gaa(0.0) < 1e-100          # central collisions never survive
+    assert o.gaa(19.99) == pytest.approx(1.0, abs=2e-4)
+    w = np.array([0.2955242247147529, 0.2692667193099963, 0.2190863625159820,
+                  0.1494513491505806, 0.0666713443086881])
+    assert w.sum() == pytest.approx(0.9999999999999999, abs=2e-16)

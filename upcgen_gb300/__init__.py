@@ -1,0 +1,294 @@
+"""upcgen-gb300: GB300 (sm_103a) implementation of upcgen's two-photon
+luminosity, nuclear cross-section and (m, y, z) event-sampling path.
+
+Python mirror of the reference's ``UpcGenerator`` / ``UpcCrossSection`` API
+(include/UpcGenerator.h:55-128, include/UpcCrossSection.h:65-240) over the C ABI
+of ``include/upcgen_gb300.h``, implemented by ``libupcgen_gb300.so``.  There is
+no CPU implementation behind it: if the CUDA library is absent or no GPU is
+visible, constructing a generator raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = ["UpcGenerator", "UpcCrossSection", "UpcgError", "EVENT_DTYPE", "library_path",
+           "load_library", "philox"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+library_path = os.path.join(_HERE, "libupcgen_gb300.so")
+
+EVENT_DTYPE = np.dtype([("m", "<f4"), ("y", "<f4"), ("z", "<f4"), ("sign", "<f4"),
+                        ("p0", "<f4", (4,)), ("p1", "<f4", (4,))])
+assert EVENT_DTYPE.itemsize == 48
+
+# every symbol include/upcgen_gb300.h declares
+ABI_SYMBOLS = [
+    "upcg_create", "upcg_destroy", "upcg_set_parameter", "upcg_config_from_file",
+    "upcg_set_collision_system", "upcg_set_seed", "upcg_set_num_threads",
+    "upcg_set_debug_level", "upcg_set_lumi_file_directory", "upcg_set_lumi_cache",
+    "upcg_set_stream", "upcg_set_lumi_method", "upcg_init", "upcg_compute_nucl_xsection",
+    "upcg_tot_nucl_x", "upcg_fid_nucl_x", "upcg_get_grid", "upcg_lumi_table",
+    "upcg_lumi_table_device", "upcg_nuc_cs_ym", "upcg_cs_zm_table", "upcg_flux_point",
+    "upcg_flux_form", "upcg_form_factor", "upcg_breakup_prob", "upcg_eval_spline",
+    "upcg_two_photon_lumi", "upcg_cs_m", "upcg_generate_events",
+    "upcg_generate_events_device", "upcg_generate_event", "upcg_philox",
+    "upcg_last_timings", "upcg_qags_stats", "upcg_last_error", "upcg_version",
+]
+
+
+class UpcgError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load (never build) the CUDA library; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or library_path
+    if not os.path.exists(path):
+        raise UpcgError(f"{path} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(path)
+    vp, cp, i, d, sz = C.c_void_p, C.c_char_p, C.c_int, C.c_double, C.c_size_t
+    i64, u64 = C.c_int64, C.c_uint64
+    dp = C.POINTER(C.c_double)
+    sig = {
+        "upcg_create": [C.POINTER(vp)], "upcg_destroy": [vp],
+        "upcg_set_parameter": [vp, cp, cp], "upcg_config_from_file": [vp, cp],
+        "upcg_set_collision_system": [vp, C.c_float, i, i], "upcg_set_seed": [vp, C.c_long],
+        "upcg_set_num_threads": [vp, i], "upcg_set_debug_level": [vp, i],
+        "upcg_set_lumi_file_directory": [vp, cp], "upcg_set_lumi_cache": [vp, i],
+        "upcg_set_stream": [vp, vp], "upcg_set_lumi_method": [vp, i], "upcg_init": [vp],
+        "upcg_compute_nucl_xsection": [vp], "upcg_tot_nucl_x": [vp, dp],
+        "upcg_fid_nucl_x": [vp, dp],
+        "upcg_get_grid": [vp, dp, dp, C.POINTER(i), dp, dp, C.POINTER(i), dp, dp, C.POINTER(i)],
+        "upcg_lumi_table": [vp, vp, sz, vp], "upcg_lumi_table_device": [vp, vp, vp],
+        "upcg_nuc_cs_ym": [vp, vp, sz, dp], "upcg_cs_zm_table": [vp, i, vp, sz],
+        "upcg_flux_point": [vp, vp, vp, vp, sz], "upcg_flux_form": [vp, vp, vp, vp, sz],
+        "upcg_form_factor": [vp, vp, vp, sz], "upcg_breakup_prob": [vp, vp, i, vp, sz],
+        "upcg_eval_spline": [vp, i, vp, vp, sz], "upcg_two_photon_lumi": [vp, vp, vp, vp, vp, sz],
+        "upcg_cs_m": [vp, vp, i, vp, sz], "upcg_generate_events": [vp, i64, vp, vp, C.POINTER(i64)],
+        "upcg_generate_events_device": [vp, i64, vp, vp, C.POINTER(i64)],
+        "upcg_generate_event": [vp, vp, C.POINTER(i)], "upcg_philox": [u64, u64, sz, vp],
+        "upcg_last_timings": [vp, dp, sz],
+        "upcg_qags_stats": [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)],
+        "upcg_last_error": [], "upcg_version": [],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = cp if name in ("upcg_last_error", "upcg_version") else i
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise UpcgError(f"status {rc}: {_lib.upcg_last_error().decode(errors='replace')}")
+    return rc
+
+
+def _arr(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def philox(seed, counter0, n):
+    """Philox4x32-10 words of the event stream, computed on the GPU."""
+    L = load_library()
+    out = np.zeros((n, 4), dtype=np.uint32)
+    _check(L.upcg_philox(seed, counter0, n, _p(out)))
+    return out
+
+
+class UpcCrossSection:
+    """Batched views of the UpcCrossSection methods of a generator."""
+
+    def __init__(self, gen):
+        self._g = gen
+
+    def _pts(self, fn, *arrays, extra=()):
+        arrays = [_arr(a) for a in arrays]
+        out = np.zeros_like(arrays[0])
+        _check(fn(*([self._g._h] + [_p(a) for a in arrays] + list(extra) + [_p(out), out.size])))
+        return out
+
+    def fluxPoint(self, b, k):  # src/UpcCrossSection.cpp:166-178
+        b, k = np.broadcast_arrays(_arr(b), _arr(k))
+        return self._pts(self._g._L.upcg_flux_point, b, k)
+
+    def fluxForm(self, b, k):  # src/UpcCrossSection.cpp:194-218
+        b, k = np.broadcast_arrays(_arr(b), _arr(k))
+        return self._pts(self._g._L.upcg_flux_form, b, k)
+
+    def calcFormFac(self, q2):  # src/UpcCrossSection.cpp:436-445
+        return self._pts(self._g._L.upcg_form_factor, q2)
+
+    def calcBreakupProb(self, b, mode):  # src/UpcCrossSection.cpp:752-1019
+        b = _arr(b)
+        out = np.zeros_like(b)
+        _check(self._g._L.upcg_breakup_prob(self._g._h, _p(b), int(mode), _p(out), out.size))
+        return out
+
+    def spline(self, which, x):
+        """Tabulated splines: 'gaa', 'breakup' or 'formfac'."""
+        idx = {"gaa": 0, "breakup": 1, "formfac": 2}[which]
+        x = _arr(x)
+        out = np.zeros_like(x)
+        _check(self._g._L.upcg_eval_spline(self._g._h, idx, _p(x), _p(out), out.size))
+        return out
+
+    def calcTwoPhotonLumi(self, M, Y):  # src/UpcCrossSection.cpp:221-271
+        M, Y = np.broadcast_arrays(_arr(M), _arr(Y))
+        M, Y = _arr(M), _arr(Y)
+        out = np.zeros_like(M)
+        _check(self._g._L.upcg_two_photon_lumi(self._g._h, _p(M), _p(Y), _p(out), None, out.size))
+        return out
+
+    def calcTwoPhotonLumiPol(self, M, Y):  # src/UpcCrossSection.cpp:274-335
+        M, Y = np.broadcast_arrays(_arr(M), _arr(Y))
+        M, Y = _arr(M), _arr(Y)
+        s, p = np.zeros_like(M), np.zeros_like(M)
+        _check(self._g._L.upcg_two_photon_lumi(self._g._h, _p(M), _p(Y), _p(s), _p(p), s.size))
+        return s, p
+
+    def calcCrossSectionM(self, m, flag=0):  # elementary process sigma(m)
+        m = _arr(m)
+        out = np.zeros_like(m)
+        _check(self._g._L.upcg_cs_m(self._g._h, _p(m), int(flag), _p(out), out.size))
+        return out
+
+
+class UpcGenerator:
+    """Mirror of upcgen's UpcGenerator (include/UpcGenerator.h:55-128)."""
+
+    def __init__(self, params=None, lib_path=None):
+        self._L = load_library(lib_path)
+        h = C.c_void_p()
+        _check(self._L.upcg_create(C.byref(h)))
+        self._h = h
+        self._parfile = "parameters.in"
+        self.nucProcessCS = UpcCrossSection(self)
+        for k, v in (params or {}).items():
+            self.setParameterValue(k, v)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                self._L.upcg_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    # -- configuration
+    def setParameterValue(self, parameter, parValue):
+        _check(self._L.upcg_set_parameter(self._h, str(parameter).encode(), str(parValue).encode()))
+
+    def setParFile(self, parfilename):
+        self._parfile = parfilename
+
+    def configGeneratorFromFile(self):
+        _check(self._L.upcg_config_from_file(self._h, self._parfile.encode()))
+
+    def setCollisionSystem(self, sqrts, nucl_z, nucl_a):
+        _check(self._L.upcg_set_collision_system(self._h, float(sqrts), int(nucl_z), int(nucl_a)))
+
+    def setSeed(self, seed):
+        _check(self._L.upcg_set_seed(self._h, int(seed)))
+
+    def setNumThreads(self, n):
+        _check(self._L.upcg_set_num_threads(self._h, int(n)))
+
+    def setDebugLevel(self, level):
+        _check(self._L.upcg_set_debug_level(self._h, int(level)))
+
+    def setLumiFileDirectory(self, directory):
+        _check(self._L.upcg_set_lumi_file_directory(self._h, str(directory).encode()))
+
+    def setLumiCache(self, enable):
+        _check(self._L.upcg_set_lumi_cache(self._h, int(bool(enable))))
+
+    def setStream(self, stream_handle):
+        _check(self._L.upcg_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))
+
+    def setLumiMethod(self, method):
+        _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1}.get(method, method)))
+
+    # -- computation
+    def init(self):
+        _check(self._L.upcg_init(self._h))
+
+    def computeNuclXsection(self):
+        _check(self._L.upcg_compute_nucl_xsection(self._h))
+
+    def totNuclX(self):
+        v = C.c_double()
+        _check(self._L.upcg_tot_nucl_x(self._h, C.byref(v)))
+        return v.value
+
+    def fidNuclX(self):
+        v = C.c_double()
+        _check(self._L.upcg_fid_nucl_x(self._h, C.byref(v)))
+        return v.value
+
+    def grid(self):
+        v = [C.c_double() for _ in range(6)]
+        n = [C.c_int() for _ in range(3)]
+        _check(self._L.upcg_get_grid(self._h, C.byref(v[0]), C.byref(v[1]), C.byref(n[0]),
+                                     C.byref(v[2]), C.byref(v[3]), C.byref(n[1]),
+                                     C.byref(v[4]), C.byref(v[5]), C.byref(n[2])))
+        return dict(mmin=v[0].value, mmax=v[1].value, nm=n[0].value, ymin=v[2].value,
+                    ymax=v[3].value, ny=n[1].value, zmin=v[4].value, zmax=v[5].value, nz=n[2].value)
+
+    def lumiTable(self, polarized=False):
+        g = self.grid()
+        out = np.zeros((g["nm"], g["ny"]))
+        out2 = np.zeros_like(out) if polarized else None
+        _check(self._L.upcg_lumi_table(self._h, _p(out), out.size, _p(out2) if polarized else None))
+        return (out, out2) if polarized else out
+
+    def nucCSYM(self):
+        g = self.grid()
+        out = np.zeros((g["ny"], g["nm"]))
+        tot = C.c_double()
+        _check(self._L.upcg_nuc_cs_ym(self._h, _p(out), out.size, C.byref(tot)))
+        return out, tot.value
+
+    def crossSectionZM(self, flag=0):
+        g = self.grid()
+        out = np.zeros((g["nm"], g["nz"]))
+        _check(self._L.upcg_cs_zm_table(self._h, int(flag), _p(out), out.size))
+        return out
+
+    def generateEvents(self, n, with_mbin=False):
+        """The accepted-event loop; returns (events, rejected[, mbin])."""
+        out = np.zeros(int(n), dtype=EVENT_DTYPE)
+        mb = np.zeros(int(n), dtype=np.int32) if with_mbin else None
+        rej = C.c_int64()
+        _check(self._L.upcg_generate_events(self._h, int(n), _p(out), _p(mb) if with_mbin else None,
+                                            C.byref(rej)))
+        return (out, rej.value, mb) if with_mbin else (out, rej.value)
+
+    def generateEvent(self):
+        """One candidate: (1 or 0, event record), as UpcGenerator::generateEvent."""
+        ev = np.zeros(1, dtype=EVENT_DTYPE)
+        acc = C.c_int()
+        _check(self._L.upcg_generate_event(self._h, _p(ev), C.byref(acc)))
+        return acc.value, ev[0]
+
+    def timings(self):
+        v = (C.c_double * 8)()
+        _check(self._L.upcg_last_timings(self._h, v, 8))
+        return {"tables_ms": v[0], "lumi_ms": v[1], "xsec_ms": v[2]}
+
+    def qagsStats(self):
+        f, m, e = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(self._L.upcg_qags_stats(self._h, C.byref(f), C.byref(m), C.byref(e)))
+        return {"failures": f.value, "max_intervals": m.value, "evals": e.value}

@@ -1,0 +1,971 @@
+// Host side of the C ABI (include/upcgen_gb300.h): configuration with the
+// reference's parameters.in keys, table / luminosity / fold / sampler set-up
+// on the GPU, and the accepted-event loop.
+//
+// Reference: src/UpcGenerator.cpp (UpcGenerator), src/UpcCrossSection.cpp
+// (UpcCrossSection::init and its prepare* helpers).
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/upcgen_gb300.h"
+#include "upcg_internal.h"
+
+using namespace upcg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(UPCG_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,             \
+                  cudaGetErrorString(e_));                                               \
+  } while (0)
+
+// include/UpcCrossSection.h:91-111 (positive half of the reference's GL-10 table)
+const double kW10pos[5] = {0.2955242247147529, 0.2692667193099963, 0.2190863625159820,
+                           0.1494513491505806, 0.0666713443086881};
+const double kX10pos[5] = {0.1488743389816312, 0.4333953941292472, 0.6794095682990244,
+                           0.8650633666889845, 0.9739065285171717};
+const double kQ2min = 1e-9, kQ2max = 2.;
+const int kNQ2 = 1000000;
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc((void**)&p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+};
+
+}  // namespace
+
+struct upcg_generator {
+  // ---- configuration (defaults: include/UpcCrossSection.h:73-172,
+  //      include/UpcGenerator.h:62-73, UpcGenerator() :30-40)
+  double R = 6.68, a = 0.447;
+  int Z = 82, A = 208;
+  double sqrts = 5020., g1 = 0, g2 = 0, gtot = 0;
+  int procID = 15;
+  double aLep = 0, alpMass = 1., alpWidth = 0.010;
+  double zmin = -1, zmax = 1, mmin = 3.56, mmax = 50., ymin = -6., ymax = 6.;
+  int nz = 100, nm = 1001, ny = 121;
+  bool isPoint = true, useNonzeroGamPt = true, usePolarizedCS = false;
+  int breakupMode = 1;
+  bool doPtCut = false, doEtaCut = false;
+  double minPt = 0, minEta = 0, maxEta = 0;
+  long seed = 0, nEvents = 1000;
+  int numThreads = 1, debug = 0;
+  std::string lumiDir = ".";
+  bool lumiCache = false;
+  int lumiMethod = 0;
+  // ---- derived
+  double mPart = 0;
+  int partPDG = 0;
+  bool isCharged = true, ignoreCSZ = false;
+  double factor = 0, rho0 = 0, csNN = 0;
+  double bu_gammatarg = 0, bu_omaxx = 0, bu_zcon = 0;
+  // ---- device state
+  cudaStream_t own = nullptr, stream = nullptr;
+  DBuf<double> ff_y, ff_c, brk_y, brk_c, ee, se, lumi, lumi2, cs, ratio, cszm, cszm2, cszm3;
+  DBuf<double> cdf2, cdfz, cdfz2, cdfz3, flux, partial, tot, rho_tmp, gws, pts_a, pts_b, pts_c;
+  DBuf<double4> ff_coef, gaa_coef, brk_coef;
+  DBuf<int> ntab, nq, ovf, tile_count;
+  DBuf<unsigned int> work;
+  DBuf<QagsStats> stats;
+  DBuf<float> ptcdf;
+  DBuf<uint32_t> mask;
+  DBuf<int64_t> tile_off, total;
+  DBuf<EventRecord> evbuf;
+  DBuf<int32_t> mbinbuf;
+  int brk_n = 0;
+  bool tables_ready = false, lumi_ready = false, xsec_ready = false;
+  double totCS = 0, fidCS = 0;
+  uint64_t next_cand = 0;
+  double acc_rate = 1.0;
+  QagsStats last_stats{};
+  double timings[8] = {0};
+  // single-event interface
+  std::vector<EventRecord> ev_batch;
+  std::vector<uint8_t> ev_flag;
+  size_t ev_pos = 0;
+
+  upcg_generator() {
+    const double g0 = 5020. / (2. * kMProt);
+    // UpcCrossSection() runs before any parameter is read: gtot keeps the
+    // default sqrt(s) (src/UpcCrossSection.cpp:51-54, include/UpcCrossSection.h:83-85).
+    gtot = std::cosh((std::acosh(g0) + std::acosh(g0)) / 2.);
+    set_collision(5020.f, 82, 208);
+  }
+  ~upcg_generator() {
+    if (own) cudaStreamDestroy(own);
+  }
+  void set_collision(float s, int z, int aa) {
+    sqrts = s;
+    g1 = sqrts / (2. * kMProt);
+    g2 = sqrts / (2. * kMProt);
+    Z = z;
+    A = aa;
+  }
+  cudaStream_t st() {
+    if (stream) return stream;
+    if (!own) cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking);
+    return own;
+  }
+  void invalidate() { tables_ready = lumi_ready = xsec_ready = false; }
+
+  int set_param(const std::string& k, const std::string& v);
+  int setup_process();
+  int build_tables();
+  int build_lumi();
+  int build_xsec();
+  LumiParams lumi_params() const;
+  FoldParams fold_params() const;
+  EventParams event_params() const;
+  int gen_events_device(int64_t n, EventRecord* out, int32_t* mbin, int64_t* rejected);
+};
+
+int upcg_generator::set_param(const std::string& k, const std::string& v) {
+  // src/UpcGenerator.cpp:183-305
+  try {
+    if (k == "NEVENTS") nEvents = std::stol(v);
+    else if (k == "SQRTS") { sqrts = std::stod(v); g1 = g2 = sqrts / (2. * kMProt); }
+    else if (k == "PROC_ID") procID = std::stoi(v);
+    else if (k == "LEP_A") aLep = std::stod(v);
+    else if (k == "ALP_MASS") alpMass = std::stod(v);
+    else if (k == "ALP_WIDTH") alpWidth = std::stod(v);
+    else if (k == "DO_PT_CUT") doPtCut = std::stoi(v);
+    else if (k == "PT_MIN") minPt = std::stod(v);
+    else if (k == "DO_ETA_CUT") doEtaCut = std::stoi(v);
+    else if (k == "ETA_MIN") minEta = std::stod(v);
+    else if (k == "ETA_MAX") maxEta = std::stod(v);
+    else if (k == "ZMIN") zmin = std::stod(v);
+    else if (k == "ZMAX") zmax = std::stod(v);
+    else if (k == "MMIN") mmin = std::stod(v);
+    else if (k == "MMAX") mmax = std::stod(v);
+    else if (k == "YMIN") ymin = std::stod(v);
+    else if (k == "YMAX") ymax = std::stod(v);
+    else if (k == "BINS_Z") nz = std::stoi(v);
+    else if (k == "BINS_M") nm = std::stoi(v);
+    else if (k == "BINS_Y") ny = std::stoi(v);
+    else if (k == "WS_R") R = std::stod(v);
+    else if (k == "WS_A") a = std::stod(v);
+    else if (k == "NUCLEUS_Z") Z = std::stoi(v);
+    else if (k == "NUCLEUS_A") A = std::stoi(v);
+    else if (k == "FLUX_POINT") isPoint = std::stoi(v);
+    else if (k == "BREAKUP_MODE") breakupMode = std::stoi(v);
+    else if (k == "NON_ZERO_GAM_PT") useNonzeroGamPt = std::stoi(v);
+    else if (k == "USE_POLARIZED_CS") usePolarizedCS = std::stoi(v);
+    else if (k == "SEED") seed = std::stol(v);
+    else return UPCG_OK;  // keys of other paths: accepted and ignored
+  } catch (...) {
+    return fail(UPCG_ERR_ARG, "bad value '%s' for %s", v.c_str(), k.c_str());
+  }
+  invalidate();
+  return UPCG_OK;
+}
+
+// Process-specific overrides of UpcGenerator::init (src/UpcGenerator.cpp:66-140)
+// and the lepton masses of UpcTwoPhotonDilep (src/UpcTwoPhotonDilep.cpp:29-44).
+int upcg_generator::setup_process() {
+  ignoreCSZ = false;
+  if (procID == 51) {
+    ignoreCSZ = true;
+    mmin = alpMass - 4. * alpWidth;
+    mmax = alpMass + 4. * alpWidth;
+    mPart = alpMass;
+    partPDG = 51;
+    isCharged = false;
+    if (usePolarizedCS) return fail(UPCG_ERR_PROCESS, "polarized cross section needs a dilepton process");
+    return UPCG_OK;
+  }
+  if (procID == 11 || procID == 13 || procID == 15) {
+    partPDG = procID;
+    isCharged = true;
+    mPart = procID == 11 ? kMEl : (procID == 13 ? kMMu : kMTau);
+    if (mmin < mPart * 2.) mmin = mPart * 2.;
+    return UPCG_OK;
+  }
+  return fail(UPCG_ERR_PROCESS, "PROC_ID %d is not on the two-photon luminosity path", procID);
+}
+
+LumiParams upcg_generator::lumi_params() const {
+  LumiParams p{};
+  p.nm = nm; p.ny = ny;
+  p.mmin = mmin; p.dm = (mmax - mmin) / nm;
+  p.ymin = ymin; p.dy = (ymax - ymin) / ny;
+  p.R = R; p.g1 = g1; p.g2 = g2; p.factor = factor;
+  p.A = A; p.isPoint = isPoint; p.breakupMode = breakupMode; p.polarized = usePolarizedCS;
+  for (int q = 0; q < 5; ++q) {
+    p.cosk[q] = std::cos(M_PI * kX10pos[q]);
+    p.sink[q] = std::sin(M_PI * kX10pos[q]);
+    p.wk[q] = kW10pos[q];
+  }
+  const double dbg = 20. / (200 - 1);
+  p.gaa = SplineU{gaa_coef.p, 0.0, dbg, 1.0 / dbg, 200};
+  const double dbb = (1000. - 1e-6) / 1000000;
+  p.brk = SplineU{brk_coef.p, 1e-6, dbb, 1.0 / dbb, brk_n};
+  const double dq = (kQ2max - kQ2min) / kNQ2;
+  p.ff = SplineU{ff_coef.p, kQ2min, dq, 1.0 / dq, kNQ2};
+  p.q2max = kQ2max;
+  p.q2clamp = kQ2max - dq;
+  return p;
+}
+
+FoldParams upcg_generator::fold_params() const {
+  FoldParams f{};
+  f.nm = nm; f.ny = ny; f.nz = nz;
+  f.mmin = mmin; f.dm = (mmax - mmin) / nm;
+  f.zmin = zmin; f.dz = (zmax - zmin) / nz;
+  f.procID = procID; f.polarized = usePolarizedCS;
+  f.mPart = mPart; f.aLep = aLep; f.alpWidth = alpWidth;
+  return f;
+}
+
+EventParams upcg_generator::event_params() const {
+  EventParams e{};
+  e.nm = nm; e.ny = ny; e.nz = nz;
+  e.mmin = mmin; e.mmax = mmax; e.dm = (mmax - mmin) / nm;
+  e.ymin = ymin; e.dy = (ymax - ymin) / ny;
+  e.zmin = zmin; e.dz = (zmax - zmin) / nz;
+  e.ignoreCSZ = ignoreCSZ; e.procID = procID; e.useNonzeroGamPt = useNonzeroGamPt;
+  e.doPtCut = doPtCut; e.doEtaCut = doEtaCut;
+  e.minPt = minPt; e.minEta = minEta; e.maxEta = maxEta;
+  e.mPart = (float)mPart; e.partPDG = partPDG;
+  e.seed = (uint64_t)seed;
+  // photon-pT spectra on a log grid of e = k^2/gtot^2 covering the cell range
+  const double kmin = mmin / 2. * std::exp(-std::max(std::fabs(ymin), std::fabs(ymax))) * 0.5;
+  const double kmax = mmax / 2. * std::exp(std::max(std::fabs(ymin), std::fabs(ymax))) * 2.0;
+  e.gtot = gtot;
+  e.pt_ne = 1024;
+  e.pt_nbins = 5000;
+  e.pt_lne0 = std::log(kmin * kmin / (gtot * gtot));
+  e.pt_dlne = (std::log(kmax * kmax / (gtot * gtot)) - e.pt_lne0) / (e.pt_ne - 1);
+  e.pt_width = 6. * kHc / R / 5000;
+  return e;
+}
+
+namespace {
+// calcWSRho (src/UpcCrossSection.cpp:152-163) on the device: one thread,
+// 200 terms in the reference's order.
+__global__ void k_ws_rho(double R, double a, int A, double* out) {
+  if (threadIdx.x != 0) return;
+  const int nb = 200;
+  const double db = 20. / (nb - 1.);
+  auto v = [&](int ib) {
+    const double r = ib * db;
+    return r * r / (1. + exp((r - R) / a));
+  };
+  double sum = v(0) + v(nb - 1);
+  for (int i = 1; i < nb - 1; i += 2) sum += 4. * v(i);
+  for (int i = 2; i < nb - 1; i += 2) sum += 2. * v(i);
+  *out = A / (sum * db / 3.) / 4. / kPi;
+}
+}  // namespace
+
+int upcg_generator::build_tables() {
+  int rc = setup_process();
+  if (rc) return rc;
+  cudaStream_t s = st();
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, s);
+  factor = Z * Z * kAlpha / M_PI / M_PI / kHc / kHc;  // src/UpcCrossSection.cpp:120
+  CK(rho_tmp.ensure(1));
+  k_ws_rho<<<1, 32, 0, s>>>(R, a, A, rho_tmp.p);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&rho0, rho_tmp.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  // sigma_NN (PDG 2016 fit), src/UpcCrossSection.cpp:368-369
+  const double ssm = std::pow(sqrts, 2) / std::pow(2 * kMProt + 2.1206, 2);
+  csNN = 0.1 * (34.41 + 0.2720 * std::pow(std::log(ssm), 2) + 13.07 * std::pow(ssm, -0.4473) -
+                7.394 * std::pow(ssm, -0.5486));
+  GaaConsts gk;
+  for (int q = 0; q < 5; ++q) {
+    gk.cosk[q] = std::cos(M_PI * kX10pos[q]);
+    gk.wk[q] = kW10pos[q];
+  }
+  CK(gaa_coef.ensure(199));
+  CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, s));
+  // form factor on 1e6 knots
+  const double dq = (kQ2max - kQ2min) / kNQ2;
+  CK(ff_y.ensure(kNQ2));
+  CK(ff_c.ensure(kNQ2));
+  CK(ff_coef.ensure(kNQ2 - 1));
+  CK(launch_formfac_values(ff_y.p, kNQ2, kQ2min, dq, rho0, R, a, s));
+  CK(build_spline_uniform(ff_y.p, kNQ2, kQ2min, dq, ff_c.p, ff_coef.p, s));
+  // breakup: calcBreakupProb's static set-up, per configuration
+  bu_gammatarg = 2. * g1 * g1 - 1.;
+  bu_omaxx = g1 > 500. ? 1.E10 : 1.E7;
+  {
+    const double zp = 82, pi = 3.14159, hbarcmev = 197.3269718;
+    bu_zcon = zp / (bu_gammatarg * (pi) * (hbarcmev)) * zp / (bu_gammatarg * (pi) * (hbarcmev)) / 137.04;
+  }
+  CK(ee.ensure(kBreakupTabMax));
+  CK(se.ensure(kBreakupTabMax));
+  CK(ntab.ensure(1));
+  const double dbb = (1000. - 1e-6) / 1000000;
+  // knots up to 20 fm + margin: the path evaluates the spline at min(b, 20)
+  brk_n = (int)((20. - 1e-6) / dbb) + 257;
+  CK(brk_y.ensure(brk_n));
+  CK(brk_c.ensure(brk_n));
+  CK(brk_coef.ensure(brk_n - 1));
+  if (breakupMode > 1) {
+    CK(launch_breakup(bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n, 1e-6, dbb, ee.p, se.p,
+                      ntab.p, brk_y.p, s));
+    CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, s));
+  } else {
+    // calcBreakupProb's energy table is still prepared for the point entry
+    CK(launch_breakup(bu_gammatarg, bu_omaxx, bu_zcon, 2, 1, 1e-6, dbb, ee.p, se.p, ntab.p,
+                      brk_y.p, s));
+  }
+  cudaEventRecord(t1, s);
+  CK(cudaEventSynchronize(t1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  timings[0] = ms;
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  tables_ready = true;
+  return UPCG_OK;
+}
+
+int upcg_generator::build_lumi() {
+  cudaStream_t s = st();
+  const LumiParams p = lumi_params();
+  const int ncell = nm * ny;
+  CK(lumi.ensure(ncell));
+  if (usePolarizedCS) CK(lumi2.ensure(ncell));
+  const int chunk = std::min(ncell, 65536);
+  CK(flux.ensure((size_t)chunk * 2 * kNb));
+  CK(nq.ensure((size_t)chunk * 2));
+  CK(work.ensure(1));
+  CK(stats.ensure(1));
+  const int ovf_cap = 1 << 20;
+  CK(ovf.ensure(ovf_cap));
+  CK(cudaMemsetAsync(stats.p, 0, sizeof(QagsStats), s));
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, s);
+  for (int c0 = 0; c0 < ncell; c0 += chunk) {
+    const int nc = std::min(chunk, ncell - c0);
+    CK(launch_lumi_nodes(p, c0, nc, flux.p, nq.p, s));
+    if (!isPoint) {
+      QagsStats before{};
+      CK(cudaMemcpyAsync(&before, stats.p, sizeof before, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      CK(cudaMemsetAsync(&stats.p->overflow, 0, sizeof(unsigned), s));
+      CK(launch_lumi_qags(p, c0, nc, flux.p, nq.p, work.p, ovf.p, ovf_cap, stats.p, nullptr, 0, s));
+      unsigned novf = 0;
+      CK(cudaMemcpyAsync(&novf, &stats.p->overflow, sizeof novf, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (novf > 0) {
+        if ((int)novf > ovf_cap) return fail(UPCG_ERR_NUMERIC, "too many QAGS overflows (%u)", novf);
+        const int warps = 512;
+        CK(gws.ensure(qags_global_ws_doubles_per_warp() * warps));
+        CK(launch_lumi_qags_overflow(p, c0, flux.p, ovf.p, (int)novf, work.p, stats.p, gws.p,
+                                     warps, s));
+      }
+    }
+    CK(launch_lumi_band(p, c0, nc, flux.p, lumi.p + 0, usePolarizedCS ? lumi2.p : nullptr, s));
+  }
+  cudaEventRecord(t1, s);
+  CK(cudaEventSynchronize(t1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  timings[1] = ms;
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  CK(cudaMemcpyAsync(&last_stats, stats.p, sizeof last_stats, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  lumi_ready = true;
+  return UPCG_OK;
+}
+
+int upcg_generator::build_xsec() {
+  cudaStream_t s = st();
+  const FoldParams f = fold_params();
+  const int ncell = nm * ny;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, s);
+  CK(cs.ensure(ncell));
+  CK(ratio.ensure(usePolarizedCS ? ncell : 1));
+  CK(partial.ensure((ncell + 255) / 256 + 1));
+  CK(tot.ensure(1));
+  CK(launch_fold(f, lumi.p, usePolarizedCS ? lumi2.p : nullptr, cs.p, ratio.p, partial.p, tot.p, s));
+  CK(cdf2.ensure((size_t)ncell + 1));
+  CK(launch_cdf_2d(cs.p, ncell, cdf2.p, nullptr, s));
+  if (!usePolarizedCS) {
+    CK(cszm.ensure((size_t)nm * nz));
+    CK(launch_cs_zm(f, 0, cszm.p, s));
+    CK(cdfz.ensure((size_t)nm * (nz + 1)));
+    if (!ignoreCSZ) CK(launch_cdf_rows(cszm.p, nm, nz, cdfz.p, s));
+  } else {
+    CK(cszm2.ensure((size_t)nm * nz));
+    CK(cszm3.ensure((size_t)nm * nz));
+    CK(launch_cs_zm(f, 1, cszm2.p, s));
+    CK(launch_cs_zm(f, 2, cszm3.p, s));
+    CK(cdfz2.ensure((size_t)nm * (nz + 1)));
+    CK(cdfz3.ensure((size_t)nm * (nz + 1)));
+    CK(launch_cdf_rows(cszm2.p, nm, nz, cdfz2.p, s));
+    CK(launch_cdf_rows(cszm3.p, nm, nz, cdfz3.p, s));
+  }
+  const EventParams e = event_params();
+  CK(ptcdf.ensure((size_t)e.pt_ne * (e.pt_nbins + 1)));
+  CK(launch_photon_pt_tables(e, lumi_params().ff, ptcdf.p, s));
+  CK(cudaMemcpyAsync(&totCS, tot.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  cudaEventRecord(t1, s);
+  CK(cudaEventSynchronize(t1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  timings[2] = ms;
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  fidCS = totCS;
+  next_cand = 0;
+  ev_batch.clear();
+  ev_flag.clear();
+  ev_pos = 0;
+  xsec_ready = true;
+  return UPCG_OK;
+}
+
+namespace {
+// Candidate index of the need-th accepted candidate (need >= 1) of a chunk.
+__global__ void k_find_cut(const int* cnt, const int64_t* off, const uint32_t* mask, int ntiles,
+                           int64_t need, int64_t* out) {
+  if (threadIdx.x != 0) return;
+  int lo = 0, hi = ntiles;  // last tile with off <= need-1
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= need - 1) lo = mid; else hi = mid;
+  }
+  int rem = (int)(need - 1 - off[lo]);
+  for (int w = 0; w < 8; ++w) {
+    uint32_t b = mask[(size_t)lo * 8 + w];
+    const int pc = __popc(b);
+    if (rem < pc) {
+      for (;;) {
+        const int bit = __ffs(b) - 1;
+        if (rem == 0) { *out = (int64_t)lo * 256 + w * 32 + bit; return; }
+        b &= b - 1;
+        --rem;
+      }
+    }
+    rem -= pc;
+  }
+  *out = -1;
+  (void)cnt;
+}
+}  // namespace
+
+int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin,
+                                      int64_t* rejected) {
+  if (!xsec_ready) return fail(UPCG_ERR_STATE, "upcg_init has not run");
+  if (usePolarizedCS) return fail(UPCG_ERR_PROCESS, "polarized event sampling is not on this path");
+  cudaStream_t s = st();
+  const EventParams e = event_params();
+  const double* zc = ignoreCSZ ? cdf2.p : cdfz.p;
+  int64_t rej = 0;
+  if (!doPtCut && !doEtaCut) {
+    CK(launch_events_write(e, cdf2.p, zc, ptcdf.p, next_cand, n, nullptr, nullptr, 0, n, out, mbin, s));
+    next_cand += (uint64_t)n;
+    *rejected = 0;
+    return UPCG_OK;
+  }
+  int64_t done = 0;
+  const int64_t kMaxChunk = (int64_t)1 << 28;
+  while (done < n) {
+    const int64_t need = n - done;
+    int64_t nc = (int64_t)std::ceil(need / std::max(acc_rate, 1e-4) * 1.05) + 4096;
+    nc = std::min(std::max<int64_t>(nc, 1 << 16), kMaxChunk);
+    nc = (nc + 255) / 256 * 256;
+    const int tiles = (int)(nc / 256);
+    CK(mask.ensure((size_t)tiles * 8));
+    CK(tile_count.ensure(tiles));
+    CK(tile_off.ensure(tiles + 1));
+    CK(total.ensure(2));
+    CK(launch_events_flags(e, cdf2.p, zc, ptcdf.p, next_cand, nc, mask.p, tile_count.p, s));
+    CK(launch_scan_tiles(tile_count.p, tile_off.p, tiles, total.p, s));
+    CK(launch_events_write(e, cdf2.p, zc, ptcdf.p, next_cand, nc, mask.p, tile_off.p, done, n,
+                           out, mbin, s));
+    int64_t acc = 0;
+    CK(cudaMemcpyAsync(&acc, total.p, sizeof acc, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    acc_rate = std::max(1e-6, (double)acc / (double)nc);
+    if (acc >= need) {
+      CK(cudaMemsetAsync(total.p + 1, 0xff, sizeof(int64_t), s));
+      k_find_cut<<<1, 32, 0, s>>>(tile_count.p, tile_off.p, mask.p, tiles, need, total.p + 1);
+      CK(cudaGetLastError());
+      int64_t cut = -1;
+      CK(cudaMemcpyAsync(&cut, total.p + 1, sizeof cut, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (cut < 0) return fail(UPCG_ERR_CUDA, "event cut search failed");
+      rej += (cut + 1) - need;
+      next_cand += (uint64_t)(cut + 1);
+      done = n;
+    } else {
+      rej += nc - acc;
+      next_cand += (uint64_t)nc;
+      done += acc;
+    }
+  }
+  *rejected = rej;
+  return UPCG_OK;
+}
+
+// ------------------------------------------------------------------ ABI ----
+extern "C" {
+
+int upcg_create(upcg_generator** out) {
+  // No device work here: configuration calls run without a GPU and the first
+  // computing call reports a missing device.
+  if (!out) return fail(UPCG_ERR_ARG, "null handle pointer");
+  *out = new upcg_generator();
+  return UPCG_OK;
+}
+
+int upcg_destroy(upcg_generator* g) {
+  delete g;
+  return UPCG_OK;
+}
+
+int upcg_set_parameter(upcg_generator* g, const char* key, const char* value) {
+  if (!g || !key || !value) return fail(UPCG_ERR_ARG, "null argument");
+  return g->set_param(key, value);
+}
+
+int upcg_config_from_file(upcg_generator* g, const char* path) {
+  // src/UpcGenerator.cpp:318-346: '#' lines skipped, trailing comments
+  // trimmed, "KEY value" pairs; a missing file keeps the defaults.
+  if (!g || !path) return fail(UPCG_ERR_ARG, "null argument");
+  std::ifstream in(path);
+  if (!in) return UPCG_OK;
+  std::string line, key, val;
+  while (std::getline(in, line)) {
+    if (!line.empty() && line[0] == '#') continue;
+    line.erase(std::find(line.begin(), line.end(), '#'), line.end());
+    std::istringstream iss(line);
+    std::string k2, v2;
+    if (!(iss >> k2 >> v2)) continue;
+    key = k2;
+    val = v2;
+    int rc = g->set_param(key, val);
+    if (rc < 0) return rc;
+  }
+  return UPCG_OK;
+}
+
+int upcg_set_collision_system(upcg_generator* g, float sqrts, int z, int a) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  g->set_collision(sqrts, z, a);
+  g->invalidate();
+  return UPCG_OK;
+}
+
+int upcg_set_seed(upcg_generator* g, long seed) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  g->seed = seed;
+  g->next_cand = 0;
+  g->ev_batch.clear();
+  g->ev_pos = 0;
+  return UPCG_OK;
+}
+
+int upcg_set_num_threads(upcg_generator* g, int n) {
+  if (!g || n < 1) return fail(UPCG_ERR_ARG, "bad thread count");
+  g->numThreads = n;
+  return UPCG_OK;
+}
+
+int upcg_set_debug_level(upcg_generator* g, int level) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  g->debug = level;
+  return UPCG_OK;
+}
+
+int upcg_set_lumi_file_directory(upcg_generator* g, const char* dir) {
+  if (!g || !dir) return fail(UPCG_ERR_ARG, "null argument");
+  g->lumiDir = dir;
+  return UPCG_OK;
+}
+
+int upcg_set_lumi_cache(upcg_generator* g, int enable) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  g->lumiCache = enable != 0;
+  return UPCG_OK;
+}
+
+int upcg_set_stream(upcg_generator* g, void* stream) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  g->stream = (cudaStream_t)stream;
+  return UPCG_OK;
+}
+
+int upcg_set_lumi_method(upcg_generator* g, int method) {
+  if (!g || method < 0 || method > 1) return fail(UPCG_ERR_ARG, "bad luminosity method");
+  if (method != g->lumiMethod) g->invalidate();
+  g->lumiMethod = method;
+  return UPCG_OK;
+}
+
+int upcg_init(upcg_generator* g) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(UPCG_ERR_CUDA, "no CUDA device visible");
+  if (g->nm < 1 || g->ny < 1 || g->nz < 1) return fail(UPCG_ERR_ARG, "empty grid");
+  if (g->breakupMode < 1 || g->breakupMode > 4) return fail(UPCG_ERR_ARG, "BREAKUP_MODE must be 1..4");
+  if (g->lumiMethod != 0) return fail(UPCG_ERR_ARG, "fast form not built into this library");
+  int rc = g->build_tables();
+  if (rc) return rc;
+  rc = g->build_lumi();
+  if (rc) return rc;
+  return g->build_xsec();
+}
+
+int upcg_compute_nucl_xsection(upcg_generator* g) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  if (!g->lumi_ready) return fail(UPCG_ERR_STATE, "luminosity not computed");
+  return g->build_xsec();
+}
+
+int upcg_tot_nucl_x(const upcg_generator* g, double* mb) {
+  if (!g || !mb) return fail(UPCG_ERR_ARG, "null argument");
+  *mb = g->totCS;
+  return UPCG_OK;
+}
+
+int upcg_fid_nucl_x(const upcg_generator* g, double* mb) {
+  if (!g || !mb) return fail(UPCG_ERR_ARG, "null argument");
+  *mb = g->fidCS;
+  return UPCG_OK;
+}
+
+int upcg_get_grid(const upcg_generator* g, double* mmin, double* mmax, int* nm, double* ymin,
+                  double* ymax, int* ny, double* zmin, double* zmax, int* nz) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  if (mmin) *mmin = g->mmin;
+  if (mmax) *mmax = g->mmax;
+  if (nm) *nm = g->nm;
+  if (ymin) *ymin = g->ymin;
+  if (ymax) *ymax = g->ymax;
+  if (ny) *ny = g->ny;
+  if (zmin) *zmin = g->zmin;
+  if (zmax) *zmax = g->zmax;
+  if (nz) *nz = g->nz;
+  return UPCG_OK;
+}
+
+int upcg_lumi_table(upcg_generator* g, double* out, size_t n, double* out2) {
+  if (!g || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (!g->lumi_ready) return fail(UPCG_ERR_STATE, "luminosity not computed");
+  const size_t need = (size_t)g->nm * g->ny;
+  if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
+  CK(cudaMemcpyAsync(out, g->lumi.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  if (out2 && g->usePolarizedCS)
+    CK(cudaMemcpyAsync(out2, g->lumi2.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(cudaStreamSynchronize(g->st()));
+  return UPCG_OK;
+}
+
+int upcg_lumi_table_device(upcg_generator* g, const double** out, const double** out2) {
+  if (!g || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (!g->lumi_ready) return fail(UPCG_ERR_STATE, "luminosity not computed");
+  *out = g->lumi.p;
+  if (out2) *out2 = g->usePolarizedCS ? g->lumi2.p : nullptr;
+  return UPCG_OK;
+}
+
+int upcg_nuc_cs_ym(upcg_generator* g, double* out, size_t n, double* tot_mb) {
+  if (!g || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "cross section not computed");
+  const size_t need = (size_t)g->nm * g->ny;
+  if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
+  CK(cudaMemcpyAsync(out, g->cs.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(cudaStreamSynchronize(g->st()));
+  if (tot_mb) *tot_mb = g->totCS;
+  return UPCG_OK;
+}
+
+int upcg_cs_zm_table(upcg_generator* g, int flag, double* out, size_t n) {
+  if (!g || !out || flag < 0 || flag > 2) return fail(UPCG_ERR_ARG, "bad argument");
+  if (!g->tables_ready) {
+    int rc = g->setup_process();
+    if (rc) return rc;
+  }
+  const size_t need = (size_t)g->nm * g->nz;
+  if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
+  DBuf<double> tmp;
+  CK(tmp.ensure(need));
+  CK(launch_cs_zm(g->fold_params(), flag, tmp.p, g->st()));
+  CK(cudaMemcpyAsync(out, tmp.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(cudaStreamSynchronize(g->st()));
+  return UPCG_OK;
+}
+
+namespace {
+int points_in(upcg_generator* g, const double* a, const double* b, size_t n) {
+  CK(g->pts_a.ensure(n));
+  CK(g->pts_c.ensure(n));
+  CK(cudaMemcpyAsync(g->pts_a.p, a, n * sizeof(double), cudaMemcpyHostToDevice, g->st()));
+  if (b) {
+    CK(g->pts_b.ensure(n));
+    CK(cudaMemcpyAsync(g->pts_b.p, b, n * sizeof(double), cudaMemcpyHostToDevice, g->st()));
+  }
+  return UPCG_OK;
+}
+int points_out(upcg_generator* g, double* out, size_t n) {
+  CK(cudaMemcpyAsync(out, g->pts_c.p, n * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(cudaStreamSynchronize(g->st()));
+  return UPCG_OK;
+}
+int need_tables(upcg_generator* g) {
+  if (g->tables_ready) return UPCG_OK;
+  return g->build_tables();
+}
+}  // namespace
+
+int upcg_flux_point(upcg_generator* g, const double* b, const double* k, double* out, size_t n) {
+  if (!g || !b || !k || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (n == 0) return UPCG_OK;
+  int rc = need_tables(g);
+  if (rc) return rc;
+  rc = points_in(g, b, k, n);
+  if (rc) return rc;
+  CK(launch_flux_points(g->lumi_params(), g->pts_a.p, g->pts_b.p, g->pts_c.p, (int)n, 0, nullptr, g->st()));
+  return points_out(g, out, n);
+}
+
+int upcg_flux_form(upcg_generator* g, const double* b, const double* k, double* out, size_t n) {
+  if (!g || !b || !k || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (n == 0) return UPCG_OK;
+  int rc = need_tables(g);
+  if (rc) return rc;
+  rc = points_in(g, b, k, n);
+  if (rc) return rc;
+  CK(g->stats.ensure(1));
+  CK(cudaMemsetAsync(g->stats.p, 0, sizeof(QagsStats), g->st()));
+  CK(launch_flux_points(g->lumi_params(), g->pts_a.p, g->pts_b.p, g->pts_c.p, (int)n, 1, g->stats.p,
+                        g->st()));
+  rc = points_out(g, out, n);
+  if (rc) return rc;
+  CK(cudaMemcpy(&g->last_stats, g->stats.p, sizeof(QagsStats), cudaMemcpyDeviceToHost));
+  return UPCG_OK;
+}
+
+int upcg_form_factor(upcg_generator* g, const double* q2, double* out, size_t n) {
+  if (!g || !q2 || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (n == 0) return UPCG_OK;
+  int rc = need_tables(g);
+  if (rc) return rc;
+  rc = points_in(g, q2, nullptr, n);
+  if (rc) return rc;
+  CK(launch_formfac_points(g->pts_a.p, g->pts_c.p, (int)n, g->rho0, g->R, g->a, g->st()));
+  return points_out(g, out, n);
+}
+
+int upcg_breakup_prob(upcg_generator* g, const double* b, int mode, double* out, size_t n) {
+  if (!g || !b || !out || mode < 1 || mode > 4) return fail(UPCG_ERR_ARG, "bad argument");
+  if (n == 0) return UPCG_OK;
+  int rc = need_tables(g);
+  if (rc) return rc;
+  rc = points_in(g, b, nullptr, n);
+  if (rc) return rc;
+  CK(launch_breakup_points(g->bu_gammatarg, g->bu_omaxx, g->bu_zcon, mode, g->ee.p, g->se.p,
+                           g->ntab.p, g->pts_a.p, g->pts_c.p, (int)n, g->st()));
+  return points_out(g, out, n);
+}
+
+int upcg_eval_spline(upcg_generator* g, int which, const double* x, double* out, size_t n) {
+  if (!g || !x || !out || which < 0 || which > 2) return fail(UPCG_ERR_ARG, "bad argument");
+  if (n == 0) return UPCG_OK;
+  int rc = need_tables(g);
+  if (rc) return rc;
+  if (which == 1 && g->breakupMode == 1) return fail(UPCG_ERR_STATE, "no breakup spline for BREAKUP_MODE 1");
+  rc = points_in(g, x, nullptr, n);
+  if (rc) return rc;
+  const LumiParams p = g->lumi_params();
+  const SplineU& s = which == 0 ? p.gaa : (which == 1 ? p.brk : p.ff);
+  CK(launch_spline_eval(s, g->pts_a.p, g->pts_c.p, (int)n, g->st()));
+  return points_out(g, out, n);
+}
+
+int upcg_two_photon_lumi(upcg_generator* g, const double* m, const double* y, double* out,
+                         double* out2, size_t n) {
+  // Cells at arbitrary (m, y): a one-row grid per point through the same kernels.
+  if (!g || !m || !y || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (n == 0) return UPCG_OK;
+  int rc = need_tables(g);
+  if (rc) return rc;
+  const bool pol = out2 != nullptr;
+  for (size_t i = 0; i < n; ++i) {
+    LumiParams p = g->lumi_params();
+    p.nm = 1; p.ny = 1; p.mmin = m[i]; p.ymin = y[i]; p.dm = 1.0; p.dy = 1.0;
+    p.polarized = pol;
+    CK(g->flux.ensure(2 * kNb));
+    CK(g->nq.ensure(2));
+    CK(g->work.ensure(1));
+    CK(g->stats.ensure(1));
+    CK(g->ovf.ensure(1 << 10));
+    CK(g->pts_c.ensure(2));
+    CK(launch_lumi_nodes(p, 0, 1, g->flux.p, g->nq.p, g->st()));
+    if (!g->isPoint) {
+      CK(cudaMemsetAsync(g->stats.p, 0, sizeof(QagsStats), g->st()));
+      CK(launch_lumi_qags(p, 0, 1, g->flux.p, g->nq.p, g->work.p, g->ovf.p, 1 << 10, g->stats.p,
+                          nullptr, 0, g->st()));
+      unsigned novf = 0;
+      CK(cudaMemcpyAsync(&novf, &g->stats.p->overflow, sizeof novf, cudaMemcpyDeviceToHost, g->st()));
+      CK(cudaStreamSynchronize(g->st()));
+      if (novf > 0) {
+        const int warps = 64;
+        CK(g->gws.ensure(qags_global_ws_doubles_per_warp() * warps));
+        CK(launch_lumi_qags_overflow(p, 0, g->flux.p, g->ovf.p, (int)novf, g->work.p, g->stats.p,
+                                     g->gws.p, warps, g->st()));
+      }
+    }
+    CK(launch_lumi_band(p, 0, 1, g->flux.p, g->pts_c.p, pol ? g->pts_c.p + 1 : nullptr, g->st()));
+    double v[2] = {0, 0};
+    CK(cudaMemcpyAsync(v, g->pts_c.p, sizeof v, cudaMemcpyDeviceToHost, g->st()));
+    CK(cudaStreamSynchronize(g->st()));
+    out[i] = v[0];
+    if (pol) out2[i] = v[1];
+  }
+  return UPCG_OK;
+}
+
+int upcg_cs_m(upcg_generator* g, const double* m, int flag, double* out, size_t n) {
+  if (!g || !m || !out || flag < 0 || flag > 2) return fail(UPCG_ERR_ARG, "bad argument");
+  if (n == 0) return UPCG_OK;
+  int rc = g->setup_process();
+  if (rc) return rc;
+  rc = points_in(g, m, nullptr, n);
+  if (rc) return rc;
+  CK(launch_cs_m_points(g->fold_params(), g->pts_a.p, g->pts_c.p, (int)n, flag, g->st()));
+  return points_out(g, out, n);
+}
+
+int upcg_generate_events_device(upcg_generator* g, int64_t n, upcg_event* out_device,
+                                int32_t* mbin_device, int64_t* rejected) {
+  if (!g || !out_device || !rejected || n < 0) return fail(UPCG_ERR_ARG, "bad argument");
+  if (n == 0) { *rejected = 0; return UPCG_OK; }
+  int rc = g->gen_events_device(n, reinterpret_cast<EventRecord*>(out_device), mbin_device, rejected);
+  if (rc) return rc;
+  g->fidCS = g->totCS * (double)n / (double)(n + *rejected);  // src/UpcGenerator.cpp:889
+  return UPCG_OK;
+}
+
+int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t* mbin,
+                         int64_t* rejected) {
+  if (!g || !out || !rejected || n < 0) return fail(UPCG_ERR_ARG, "bad argument");
+  if (n == 0) { *rejected = 0; return UPCG_OK; }
+  CK(g->evbuf.ensure((size_t)n));
+  if (mbin) CK(g->mbinbuf.ensure((size_t)n));
+  int rc = upcg_generate_events_device(g, n, reinterpret_cast<upcg_event*>(g->evbuf.p),
+                                       mbin ? g->mbinbuf.p : nullptr, rejected);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out, g->evbuf.p, (size_t)n * sizeof(EventRecord), cudaMemcpyDeviceToHost, g->st()));
+  if (mbin)
+    CK(cudaMemcpyAsync(mbin, g->mbinbuf.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, g->st()));
+  CK(cudaStreamSynchronize(g->st()));
+  return UPCG_OK;
+}
+
+int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted) {
+  // The next candidate of the sequence upcg_generate_events draws from, with
+  // its accept flag (1 = passes the cuts, 0 = rejected), as generateEvent.
+  if (!g || !ev || !accepted) return fail(UPCG_ERR_ARG, "null argument");
+  if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "upcg_init has not run");
+  if (g->usePolarizedCS) return fail(UPCG_ERR_PROCESS, "polarized event sampling is not on this path");
+  if (g->ev_pos >= g->ev_flag.size()) {
+    const int64_t nb = 4096;
+    DBuf<EventRecord> rec;
+    DBuf<uint8_t> flg;
+    CK(rec.ensure(nb));
+    CK(flg.ensure(nb));
+    const EventParams e = g->event_params();
+    const double* zc = g->ignoreCSZ ? g->cdf2.p : g->cdfz.p;
+    CK(launch_events_all(e, g->cdf2.p, zc, g->ptcdf.p, g->next_cand, nb, rec.p, flg.p, g->st()));
+    g->ev_batch.resize(nb);
+    g->ev_flag.resize(nb);
+    CK(cudaMemcpyAsync(g->ev_batch.data(), rec.p, nb * sizeof(EventRecord), cudaMemcpyDeviceToHost, g->st()));
+    CK(cudaMemcpyAsync(g->ev_flag.data(), flg.p, nb, cudaMemcpyDeviceToHost, g->st()));
+    CK(cudaStreamSynchronize(g->st()));
+    g->next_cand += (uint64_t)nb;
+    g->ev_pos = 0;
+  }
+  const size_t i = g->ev_pos++;
+  const bool cuts = g->doPtCut || g->doEtaCut;
+  *accepted = cuts ? g->ev_flag[i] : 1;
+  *reinterpret_cast<EventRecord*>(ev) = g->ev_batch[i];
+  return UPCG_OK;
+}
+
+int upcg_philox(uint64_t seed, uint64_t counter0, size_t n, uint32_t* out4) {
+  if (!out4) return fail(UPCG_ERR_ARG, "null argument");
+  if (n == 0) return UPCG_OK;
+  DBuf<uint32_t> d;
+  CK(d.ensure(4 * n));
+  CK(launch_philox_dump(seed, counter0, (int64_t)n, d.p, 0));
+  CK(cudaMemcpy(out4, d.p, 4 * n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  return UPCG_OK;
+}
+
+int upcg_last_timings(const upcg_generator* g, double* ms, size_t n) {
+  if (!g || !ms) return fail(UPCG_ERR_ARG, "null argument");
+  for (size_t i = 0; i < n && i < 8; ++i) ms[i] = g->timings[i];
+  return UPCG_OK;
+}
+
+int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_intervals,
+                    uint64_t* evals) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  if (failures) *failures = g->last_stats.failures;
+  if (max_intervals) *max_intervals = g->last_stats.max_intervals;
+  if (evals) *evals = g->last_stats.evals;
+  return UPCG_OK;
+}
+
+const char* upcg_last_error(void) { return g_err.c_str(); }
+const char* upcg_version(void) { return "upcgen-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,445 @@
+// Event sampling: (y, m) from the nuclear cross section, z = cos(theta) from
+// the elementary one, pair transverse momentum from the photon pT spectra,
+// two-body kinematics and the pT / eta cuts.
+//
+// Reference: UpcGenerator::generateEvent / generateEvents
+// (src/UpcGenerator.cpp:715-889), pairProduction (:388-423),
+// twoPartDecayUniform (:526-561), checkKinCuts (:563-587),
+// UpcCrossSection::getPairMomentum / getPhotonPt (src/UpcCrossSection.cpp:1021-1074),
+// UpcSampler1D/2D (include/UpcSampler.h:37-142).
+//
+// Random numbers: Philox4x32-10 (Salmon et al., SC'11) keyed by SEED, one
+// counter per candidate event, so candidate i is the same whatever the launch
+// shape.  Accepted events keep candidate order: pass 1 marks accepted
+// candidates in a bit mask and counts them per 256-candidate tile, a scan of
+// the tile counts gives each tile its output offset, and pass 2 regenerates
+// only the accepted candidates of each tile into their slots.  The first N
+// accepted candidates are kept and the rejected ones before the N-th are
+// counted, which is the reference's generateEvents loop.
+//
+// Kinematics are FP32; the (y, m) and z CDFs and their inversion are FP64.
+#include "upcg_internal.h"
+
+namespace upcg {
+
+namespace {
+
+__device__ __forceinline__ uint4 philox_round(uint4 c, uint2 k) {
+  const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+  const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+  return make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+}
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k.x += 0x9E3779B9u;
+      k.y += 0xBB67AE85u;
+    }
+    c = philox_round(c, k);
+  }
+  return c;
+}
+
+__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {  // [0, 1)
+  const uint64_t x = ((uint64_t)a << 21) ^ (uint64_t)(b >> 11);
+  return (double)(x & ((1ull << 53) - 1)) * (1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ float u24(uint32_t a) {  // [0, 1)
+  return (float)(a >> 8) * (1.0f / 16777216.0f);
+}
+
+constexpr float kTwoPiF = 6.28318530717958647692f;
+
+// cdf[k] <= r < cdf[k+1] over n bins (the last non-empty bin if r >= cdf[n]).
+__device__ __forceinline__ int cdf_find(const double* __restrict__ cdf, int n, double r) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (r >= __ldg(cdf + mid)) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int cdf_find_f(const float* __restrict__ cdf, int n, float r) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (r >= __ldg(cdf + mid)) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Photon pT from the tabulated spectrum closest in ln(k^2/gtot^2): the table
+// at grid point i or i+1, chosen with the interpolation weight.
+__device__ float photon_pt(const EventParams& e, const float* __restrict__ tabs, double k,
+                           float u, float usel) {
+  const double ered = (k * k) / (e.gtot * e.gtot);
+  double t = (log(ered) - e.pt_lne0) / e.pt_dlne;
+  t = t < 0. ? 0. : (t > e.pt_ne - 1 ? e.pt_ne - 1 : t);
+  int i = (int)t;
+  if (i > e.pt_ne - 2) i = e.pt_ne - 2;
+  const float fr = (float)(t - i);
+  if (usel < fr) ++i;
+  const float* I = tabs + (size_t)i * (e.pt_nbins + 1);
+  const int ib = cdf_find_f(I, e.pt_nbins, u);
+  const float lo = __ldg(I + ib), hi = __ldg(I + ib + 1);
+  const float w = (float)e.pt_width;
+  float x = ib * w;
+  if (hi > lo) x += w * (u - lo) / (hi - lo);
+  return x;
+}
+
+struct Cand {
+  double m, y, z;
+  float sign;
+  float p0[4], p1[4];
+  int mbin;
+};
+
+__device__ __forceinline__ float eta_f(float px, float py, float pz) {
+  const float pt = sqrtf(px * px + py * py);
+  if (pt > 0.f) return asinhf(pz / pt);
+  if (pz == 0.f) return 0.f;
+  return pz > 0.f ? 10e10f : -10e10f;
+}
+
+// Boost a rest-frame momentum v (energy ev) by the frame of the 4-vector
+// (px, py, pz, E) of invariant mass M: p' = v + P [ (P.v)/(M (E + M)) + ev/M ].
+__device__ __forceinline__ void boost_by(float vx, float vy, float vz, float ev, float px,
+                                         float py, float pz, float E, float M, float* out) {
+  const float pv = px * vx + py * vy + pz * vz;
+  const float f = pv / (M * (E + M)) + ev / M;
+  out[0] = vx + f * px;
+  out[1] = vy + f * py;
+  out[2] = vz + f * pz;
+  out[3] = (E * ev + pv) / M;
+}
+
+__device__ bool gen_candidate(const EventParams& e, const double* __restrict__ cdf2,
+                              const double* __restrict__ cdfz, const float* __restrict__ pttab,
+                              uint64_t idx, Cand& c) {
+  const uint2 key = make_uint2((uint32_t)e.seed, (uint32_t)(e.seed >> 32));
+  const uint32_t clo = (uint32_t)idx, chi = (uint32_t)(idx >> 32);
+  const uint4 r0 = philox4x32_10(make_uint4(clo, chi, 0u, 0x55504347u), key);
+  const uint4 r1 = philox4x32_10(make_uint4(clo, chi, 1u, 0x55504347u), key);
+  const uint4 r2 = philox4x32_10(make_uint4(clo, chi, 2u, 0x55504347u), key);
+  // (y, m): gsl_histogram2d_pdf_sample with r1 for the bin and y, r2 for m
+  const int n2 = e.ny * e.nm;
+  const double ra = u53(r0.x, r0.y), rb = u53(r0.z, r0.w);
+  const int k = cdf_find(cdf2, n2, ra);
+  const int iy = k / e.nm, im = k - iy * e.nm;
+  const double c0 = __ldg(cdf2 + k), c1 = __ldg(cdf2 + k + 1);
+  const double delta = c1 > c0 ? (ra - c0) / (c1 - c0) : 0.;
+  const double ylo = e.ymin + e.dy * iy, yhi = e.ymin + e.dy * (iy + 1);
+  const double mlo = e.mmin + e.dm * im, mhi = e.mmin + e.dm * (im + 1);
+  c.y = ylo + delta * (yhi - ylo);
+  c.m = mlo + rb * (mhi - mlo);
+  // getBinY (include/UpcSampler.h:130-133), the int() truncating the numerator
+  const double medge_hi = e.mmin + e.dm * e.nm;
+  int mb = (int)((double)(int)(e.nm * (c.m - e.mmin)) / (medge_hi - e.mmin));
+  mb = mb < 0 ? 0 : (mb > e.nm - 1 ? e.nm - 1 : mb);
+  c.mbin = mb;
+  // z = cos(theta)
+  const double rz = u53(r1.x, r1.y);
+  if (!e.ignoreCSZ) {
+    const double* cz = cdfz + (size_t)mb * (e.nz + 1);
+    const int iz = cdf_find(cz, e.nz, rz);
+    const double z0 = __ldg(cz + iz), z1 = __ldg(cz + iz + 1);
+    const double dl = z1 > z0 ? (rz - z0) / (z1 - z0) : 0.;
+    const double zlo = e.zmin + e.dz * iz, zhi = e.zmin + e.dz * (iz + 1);
+    c.z = zlo + dl * (zhi - zlo);
+  } else {
+    c.z = -1. + 2. * rz;
+  }
+  // pair momentum (getPairMomentum)
+  const float m = (float)c.m, y = (float)c.y;
+  float ppx = 0.f, ppy = 0.f, mt = m;
+  if (e.useNonzeroGamPt) {
+    const double k1 = c.m / 2 * exp(c.y), k2 = c.m / 2 * exp(-c.y);
+    const float a1 = kTwoPiF * u24(r1.z), a2 = kTwoPiF * u24(r1.w);
+    const float pt1 = photon_pt(e, pttab, k1, u24(r2.x), u24(r2.y));
+    const float pt2 = photon_pt(e, pttab, k2, u24(r2.z), u24(r2.w));
+    float s1, c1f, s2, c2f;
+    sincosf(a1, &s1, &c1f);
+    sincosf(a2, &s2, &c2f);
+    ppx = pt1 * c1f + pt2 * c2f;
+    ppy = pt1 * s1 + pt2 * s2;
+    mt = sqrtf(m * m + ppx * ppx + ppy * ppy);
+  }
+  const float ppz = mt * sinhf(y), pE = mt * coshf(y);
+  const uint4 r3 = philox4x32_10(make_uint4(clo, chi, 3u, 0x55504347u), key);
+  if (e.procID != 51) {
+    // pairProduction: back-to-back leptons, |p| = sqrt(M^2/4 - m_l^2), boosted
+    const float pmag = sqrtf(fmaxf(m * m * 0.25f - e.mPart * e.mPart, 0.f));
+    const float cz = (float)c.z;
+    const float sz = sqrtf(fmaxf(1.f - cz * cz, 0.f));
+    float sp, cp;
+    sincosf(kTwoPiF * u24(r3.x), &sp, &cp);
+    const float vx = pmag * sz * cp, vy = pmag * sz * sp, vz = pmag * cz;
+    const float ev = sqrtf(pmag * pmag + e.mPart * e.mPart);
+    boost_by(vx, vy, vz, ev, ppx, ppy, ppz, pE, m, c.p0);
+    boost_by(-vx, -vy, -vz, ev, ppx, ppy, ppz, pE, m, c.p1);
+    c.sign = (r3.y & 1u) ? 1.f : -1.f;
+    for (int q = 0; q < 2; ++q) {
+      const float* pp = q ? c.p1 : c.p0;
+      if (e.doPtCut && sqrtf(pp[0] * pp[0] + pp[1] * pp[1]) < (float)e.minPt) return false;
+      if (e.doEtaCut) {
+        const float et = eta_f(pp[0], pp[1], pp[2]);
+        if (et < (float)e.minEta || et > (float)e.maxEta) return false;
+      }
+    }
+    return true;
+  }
+  // ALP: cuts on the ALP, then the isotropic two-photon decay
+  if (e.doPtCut && sqrtf(ppx * ppx + ppy * ppy) < (float)e.minPt) return false;
+  if (e.doEtaCut) {
+    const float et = eta_f(ppx, ppy, ppz);
+    if (et < (float)e.minEta || et > (float)e.maxEta) return false;
+  }
+  const float eph = 0.5f * m;
+  float sp, cp;
+  sincosf(kTwoPiF * u24(r3.x), &sp, &cp);
+  const float ct = -1.f + 2.f * u24(r3.z);
+  const float st = sqrtf(fmaxf(1.f - ct * ct, 0.f));
+  float vx = eph * st * cp, vy = eph * st * sp, vz = eph * ct;
+  // RotateUz onto the ALP direction (a rotation of an isotropic decay)
+  const float pm = sqrtf(ppx * ppx + ppy * ppy + ppz * ppz);
+  if (pm > 0.f) {
+    const float u1 = ppx / pm, u2 = ppy / pm, u3 = ppz / pm;
+    float up = u1 * u1 + u2 * u2;
+    if (up > 0.f) {
+      up = sqrtf(up);
+      const float x = (u1 * u3 * vx - u2 * vy + u1 * up * vz) / up;
+      const float yy = (u2 * u3 * vx + u1 * vy + u2 * up * vz) / up;
+      const float z = (u3 * u3 * vx - vx + u3 * up * vz) / up;
+      vx = x; vy = yy; vz = z;
+    } else if (u3 < 0.f) {
+      vx = -vx; vz = -vz;
+    }
+  }
+  boost_by(-vx, -vy, -vz, eph, ppx, ppy, ppz, pE, m, c.p0);
+  boost_by(vx, vy, vz, eph, ppx, ppy, ppz, pE, m, c.p1);
+  c.sign = 1.f;
+  return true;
+}
+
+constexpr int kTile = 256;
+
+__global__ void __launch_bounds__(kTile) k_events_flags(EventParams e, const double* __restrict__ cdf2,
+                                                        const double* __restrict__ cdfz,
+                                                        const float* __restrict__ pttab,
+                                                        uint64_t cand0, int64_t ncand,
+                                                        uint32_t* __restrict__ mask,
+                                                        int* __restrict__ tile_count) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  const int64_t local = (int64_t)blockIdx.x * kTile + threadIdx.x;
+  bool ok = false;
+  if (local < ncand) {
+    Cand c;
+    ok = gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)local, c);
+  }
+  const unsigned bal = __ballot_sync(0xffffffffu, ok);
+  if ((threadIdx.x & 31) == 0) {
+    mask[(size_t)blockIdx.x * (kTile / 32) + (threadIdx.x >> 5)] = bal;
+    atomicAdd(&cnt, __popc(bal));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) tile_count[blockIdx.x] = cnt;
+}
+
+__global__ void __launch_bounds__(kTile) k_events_write(EventParams e, const double* __restrict__ cdf2,
+                                                        const double* __restrict__ cdfz,
+                                                        const float* __restrict__ pttab,
+                                                        uint64_t cand0, int64_t ncand,
+                                                        const uint32_t* __restrict__ mask,
+                                                        const int64_t* __restrict__ tile_off,
+                                                        int64_t out_base, int64_t nmax,
+                                                        EventRecord* __restrict__ out,
+                                                        int32_t* __restrict__ mbin) {
+  __shared__ uint32_t sm[kTile / 32];
+  __shared__ int pre[kTile / 32 + 1];
+  const int tile = blockIdx.x;
+  const int64_t base = tile_off ? tile_off[tile] : (int64_t)tile * kTile;
+  if (out_base + base >= nmax) return;
+  if (threadIdx.x < kTile / 32)
+    sm[threadIdx.x] = mask ? mask[(size_t)tile * (kTile / 32) + threadIdx.x] : 0xffffffffu;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    pre[0] = 0;
+    for (int w = 0; w < kTile / 32; ++w) pre[w + 1] = pre[w] + __popc(sm[w]);
+  }
+  __syncthreads();
+  const int total = pre[kTile / 32];
+  const int r = threadIdx.x;  // r-th accepted candidate of the tile
+  if (r >= total) return;
+  int w = 0;
+  while (pre[w + 1] <= r) ++w;
+  int rem = r - pre[w];
+  uint32_t bits = sm[w];
+  int lane = 0;
+  for (;;) {
+    const int b = __ffs(bits) - 1;
+    if (rem == 0) { lane = b; break; }
+    bits &= bits - 1;
+    --rem;
+  }
+  const int64_t local = (int64_t)tile * kTile + w * 32 + lane;
+  if (local >= ncand) return;
+  const int64_t slot = out_base + base + r;
+  if (slot >= nmax) return;
+  Cand c;
+  gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)local, c);
+  EventRecord rec;
+  rec.m = (float)c.m;
+  rec.y = (float)c.y;
+  rec.z = (float)c.z;
+  rec.sign = c.sign;
+  for (int q = 0; q < 4; ++q) { rec.p0[q] = c.p0[q]; rec.p1[q] = c.p1[q]; }
+  out[slot] = rec;
+  if (mbin) mbin[slot] = c.mbin;
+}
+
+// Exclusive scan of the tile counts (one CTA; tiles per chunk <= 2^20) and the total.
+__global__ void k_scan_tiles(const int* __restrict__ cnt, int64_t* __restrict__ off, int n,
+                             int64_t* __restrict__ total) {
+  __shared__ int64_t red[1024];
+  const int t = threadIdx.x;
+  const int chunk = (n + 1023) / 1024;
+  const int lo = t * chunk, hi = min(lo + chunk, n);
+  int64_t s = 0;
+  for (int i = lo; i < hi; ++i) s += cnt[i];
+  red[t] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int64_t add = t >= o ? red[t - o] : 0;
+    __syncthreads();
+    red[t] += add;
+    __syncthreads();
+  }
+  int64_t run = t > 0 ? red[t - 1] : 0;
+  for (int i = lo; i < hi; ++i) {
+    off[i] = run;
+    run += cnt[i];
+  }
+  if (t == 1023) *total = red[1023];
+}
+
+// Photon pT spectra: dN/dpT ~ F(pT^2 + e)^2 pT^3 / (pT^2 + e)^2 on 5000 bins of
+// [0, 6 hc / R] (content at the upper bin edge), for e = k^2/gtot^2 on a log grid.
+__global__ void k_pt_tables(EventParams e, SplineU ff, float* __restrict__ out) {
+  extern __shared__ double sd[];
+  const int ie = blockIdx.x;
+  const double ered = exp(e.pt_lne0 + e.pt_dlne * ie);
+  const int nb = e.pt_nbins;
+  const double pi2x4 = 4 * kPi * kPi;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const double pt = e.pt_width * (b + 1);
+    const double arg = pt * pt + ered;
+    const double f = spline_eval(ff, arg);
+    sd[b] = (f * f) * pt * pt * pt / (pi2x4 * arg * arg);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // sequential cumulative sum in FP64 (5000 terms)
+    double s = 0.;
+    for (int b = 0; b < nb; ++b) {
+      s += sd[b];
+      sd[b] = s;
+    }
+  }
+  __syncthreads();
+  const double tot = sd[nb - 1];
+  float* o = out + (size_t)ie * (nb + 1);
+  if (threadIdx.x == 0) o[0] = 0.f;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) o[b + 1] = (float)(sd[b] / tot);
+}
+
+// Every candidate of [cand0, cand0 + n) with its accept flag (single-event API).
+__global__ void k_events_all(EventParams e, const double* __restrict__ cdf2,
+                             const double* __restrict__ cdfz, const float* __restrict__ pttab,
+                             uint64_t cand0, int64_t n, EventRecord* __restrict__ out,
+                             uint8_t* __restrict__ flag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Cand c;
+  const bool ok = gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)i, c);
+  EventRecord rec;
+  rec.m = (float)c.m;
+  rec.y = (float)c.y;
+  rec.z = (float)c.z;
+  rec.sign = c.sign;
+  for (int q = 0; q < 4; ++q) { rec.p0[q] = c.p0[q]; rec.p1[q] = c.p1[q]; }
+  out[i] = rec;
+  flag[i] = ok ? 1 : 0;
+}
+
+__global__ void k_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t c = c0 + (uint64_t)i;
+  const uint4 r = philox4x32_10(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0u, 0u),
+                                make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+  out[4 * i + 0] = r.x;
+  out[4 * i + 1] = r.y;
+  out[4 * i + 2] = r.z;
+  out[4 * i + 3] = r.w;
+}
+
+}  // namespace
+
+cudaError_t launch_events_all(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
+                              const float* d_ptcdf, uint64_t cand0, int64_t n, EventRecord* d_out,
+                              uint8_t* d_flag, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_events_all<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, n,
+                                                           d_out, d_flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* d_out,
+                               cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_philox_dump<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(seed, c0, n, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, float* d_cdf,
+                                    cudaStream_t st) {
+  const size_t smem = sizeof(double) * e.pt_nbins;
+  cudaFuncSetAttribute(k_pt_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_pt_tables<<<e.pt_ne, 256, smem, st>>>(e, ff, d_cdf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
+                                const float* d_ptcdf, uint64_t cand0, int64_t ncand,
+                                uint32_t* d_mask, int* d_tile_count, cudaStream_t st) {
+  const int64_t tiles = (ncand + kTile - 1) / kTile;
+  k_events_flags<<<(unsigned)tiles, kTile, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, ncand,
+                                                   d_mask, d_tile_count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_events_write(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
+                                const float* d_ptcdf, uint64_t cand0, int64_t ncand,
+                                const uint32_t* d_mask, const int64_t* d_tile_off,
+                                int64_t out_base, int64_t nmax, EventRecord* d_out,
+                                int32_t* d_mbin, cudaStream_t st) {
+  const int64_t tiles = (ncand + kTile - 1) / kTile;
+  k_events_write<<<(unsigned)tiles, kTile, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, ncand,
+                                                   d_mask, d_tile_off, out_base, nmax, d_out,
+                                                   d_mbin);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
+                              cudaStream_t st) {
+  k_scan_tiles<<<1, 1024, 0, st>>>(d_count, d_off, n, d_total);
+  return cudaGetLastError();
+}
+
+}  // namespace upcg

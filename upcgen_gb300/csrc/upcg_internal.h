@@ -1,0 +1,131 @@
+// Internal interface between the host library (upcg_api.cpp) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "upcg_device.cuh"
+
+namespace upcg {
+
+constexpr int kNb = 120;                // b-bins per side (include/UpcCrossSection.h:116-117)
+constexpr int kBreakupTabMax = 1024;    // capacity of the photo-neutron energy table
+constexpr int kQagsCapSmem = 64;        // QAGS intervals held in shared memory per warp
+constexpr int kQagsLimit = 1000;        // QAGS limit of src/UpcCrossSection.cpp:209
+
+struct GaaConsts {
+  double cosk[5];  // cos(pi x_k) for the positive GL-10 abscissas
+  double wk[5];    // their weights (include/UpcCrossSection.h:91-111)
+};
+
+// Everything a luminosity kernel needs about one configuration.
+struct LumiParams {
+  int nm, ny;
+  double mmin, dm, ymin, dy;
+  double R, g1, g2, factor;
+  int A, isPoint, breakupMode, polarized;
+  double cosk[5], sink[5], wk[5];
+  SplineU gaa, brk, ff;
+  double q2max, q2clamp;  // Q2max and Q2max - dQ2 (src/UpcCrossSection.cpp:188)
+};
+
+// Per-launch statistics of the QAGS flux kernel.
+struct QagsStats {
+  unsigned int failures;     // nodes whose QAGS returned a non-zero GSL status
+  unsigned int overflow;     // nodes needing more than kQagsCapSmem intervals
+  unsigned int max_intervals;
+  unsigned long long evals;  // integrand evaluations
+};
+
+// tables
+cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
+                                 double4* d_coef, cudaStream_t st);
+cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, double rho0,
+                                  double R, double a, cudaStream_t st);
+cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaConsts& k,
+                       double4* d_coef, cudaStream_t st);
+cudaError_t launch_breakup(double gammatarg, double omaxx, double zcon, int mode, int n,
+                           double x0, double h, double* d_ee, double* d_se, int* d_ntab,
+                           double* d_out, cudaStream_t st);
+cudaError_t launch_spline_eval(const SplineU& s, const double* d_x, double* d_y, int n,
+                               cudaStream_t st);
+
+// luminosity (plain FP64)
+cudaError_t launch_lumi_nodes(const LumiParams& p, int cell0, int ncells, double* d_flux,
+                              int* d_nq, cudaStream_t st);
+cudaError_t launch_lumi_qags(const LumiParams& p, int cell0, int ncells, double* d_flux,
+                             const int* d_nq, unsigned int* d_work, int* d_ovf_list,
+                             int ovf_cap, QagsStats* d_stats, double* d_gws, int gws_warps,
+                             cudaStream_t st);
+cudaError_t launch_lumi_qags_overflow(const LumiParams& p, int cell0, double* d_flux,
+                                      const int* d_ovf_list, int n_ovf, unsigned int* d_work,
+                                      QagsStats* d_stats, double* d_gws, int gws_warps,
+                                      cudaStream_t st);
+size_t qags_global_ws_doubles_per_warp();
+cudaError_t launch_lumi_band(const LumiParams& p, int cell0, int ncells, const double* d_flux,
+                             double* d_lumi, double* d_lumi2, cudaStream_t st);
+// point evaluations for the parity entry points
+cudaError_t launch_flux_points(const LumiParams& p, const double* d_b, const double* d_k,
+                               double* d_out, int n, int form, QagsStats* d_stats,
+                               cudaStream_t st);
+cudaError_t launch_breakup_points(double gammatarg, double omaxx, double zcon, int mode,
+                                  const double* d_ee, const double* d_se, const int* d_ntab,
+                                  const double* d_b, double* d_out, int n, cudaStream_t st);
+cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, double rho0,
+                                  double R, double a, cudaStream_t st);
+
+// fold + samplers
+struct FoldParams {
+  int nm, ny, nz;
+  double mmin, dm, zmin, dz;
+  int procID, polarized;
+  double mPart, aLep, alpWidth;
+};
+cudaError_t launch_cs_zm(const FoldParams& f, int flag, double* d_out, cudaStream_t st);
+cudaError_t launch_fold(const FoldParams& f, const double* d_lumi, const double* d_lumi2,
+                        double* d_cs, double* d_ratio, double* d_partial, double* d_tot,
+                        cudaStream_t st);
+cudaError_t launch_cs_m_points(const FoldParams& f, const double* d_m, double* d_out, int n,
+                               int flag, cudaStream_t st);
+cudaError_t launch_cdf_2d(const double* d_w, int64_t n, double* d_cdf, double* d_scratch,
+                          cudaStream_t st);
+cudaError_t launch_cdf_rows(const double* d_w, int rows, int len, double* d_cdf,
+                            cudaStream_t st);
+
+// events
+struct EventParams {
+  int nm, ny, nz;
+  double mmin, mmax, dm, ymin, dy, zmin, dz;
+  int ignoreCSZ, procID, useNonzeroGamPt, doPtCut, doEtaCut;
+  double minPt, minEta, maxEta;
+  float mPart;
+  int partPDG;
+  uint64_t seed;
+  // photon-pT tables
+  int pt_ne, pt_nbins;
+  double pt_lne0, pt_dlne, pt_width, gtot;
+};
+struct EventRecord {  // 48 bytes
+  float m, y, z, sign;
+  float p0[4];
+  float p1[4];
+};
+cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, float* d_cdf,
+                                    cudaStream_t st);
+cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
+                                const float* d_ptcdf, uint64_t cand0, int64_t ncand,
+                                uint32_t* d_mask, int* d_tile_count, cudaStream_t st);
+cudaError_t launch_events_write(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
+                                const float* d_ptcdf, uint64_t cand0, int64_t ncand,
+                                const uint32_t* d_mask, const int64_t* d_tile_off,
+                                int64_t out_base, int64_t nmax, EventRecord* d_out,
+                                int32_t* d_mbin, cudaStream_t st);
+cudaError_t launch_events_all(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
+                              const float* d_ptcdf, uint64_t cand0, int64_t n, EventRecord* d_out,
+                              uint8_t* d_flag, cudaStream_t st);
+cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* d_out,
+                               cudaStream_t st);
+cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
+                              cudaStream_t st);
+
+}  // namespace upcg

@@ -1,0 +1,411 @@
+// Nuclear tables on the GPU: Woods-Saxon form factor, G_AA(b), Coulomb-breakup
+// probability, and the natural cubic splines through them.
+//
+// Reference: src/UpcCrossSection.cpp
+//   calcFormFac :436-445, prepareFormFac :447-461     -> k_formfac_values
+//   prepareGAA :364-414                               -> k_gaa
+//   calcBreakupProb :752-1019, prepareBreakupProb :416-434
+//                                                    -> k_breakup_setup, k_breakup_values
+//   gsl_interp_cspline (natural) construction          -> k_spline_window, k_spline_coef
+//
+// The spline system is solved in independent windows: every thread solves the
+// natural-spline tridiagonal system on its 32 output knots plus 48 knots of
+// padding on each side, with zero second derivative at the window edges.  The
+// system is diagonally dominant (ratio 2-sqrt(3) per knot on uniform grids),
+// so the padding error is below 1e-27 relative -- the same solution as a
+// global solve in double precision, with ~1e6 knots done in one launch.
+#include "upcg_device.cuh"
+#include "upcg_internal.h"
+
+namespace upcg {
+
+namespace {
+
+constexpr int kWinOut = 32;
+constexpr int kWinPad = 48;
+constexpr int kWinMax = kWinOut + 2 * kWinPad;
+
+__device__ __forceinline__ double knot(double x0, double h, int i) { return x0 + i * h; }
+
+// Natural-spline second-derivative halves c_i on uniform knots x0 + i*h.
+__global__ void k_spline_window(const double* __restrict__ y, int n, double x0, double h,
+                                double* __restrict__ c) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = 1 + t * kWinOut;  // first output knot
+  if (s > n - 2) {
+    if (t == 0) { c[0] = 0.0; c[n - 1] = 0.0; }
+    return;
+  }
+  if (t == 0) { c[0] = 0.0; c[n - 1] = 0.0; }
+  const int e = min(s + kWinOut, n - 1);  // exclusive
+  const int L = max(1, s - kWinPad);
+  const int U = min(n - 2, e - 1 + kWinPad);
+  double cp[kWinMax], dp[kWinMax];
+  double xm = knot(x0, h, L - 1), xc = knot(x0, h, L), xp = knot(x0, h, L + 1);
+  double ym = y[L - 1], yc = y[L], yp = y[L + 1];
+  double h0 = xc - xm, h1 = xp - xc;
+  {
+    const double diag = 2.0 * (h0 + h1);
+    const double rhs = 3.0 * ((yp - yc) / h1 - (yc - ym) / h0);
+    cp[0] = h1 / diag;
+    dp[0] = rhs / diag;
+  }
+  for (int i = L + 1; i <= U; ++i) {
+    xm = xc; xc = xp; xp = knot(x0, h, i + 1);
+    ym = yc; yc = yp; yp = y[i + 1];
+    h0 = xc - xm; h1 = xp - xc;
+    const double diag = 2.0 * (h0 + h1);
+    const double rhs = 3.0 * ((yp - yc) / h1 - (yc - ym) / h0);
+    const int j = i - L;
+    const double den = diag - h0 * cp[j - 1];
+    cp[j] = h1 / den;
+    dp[j] = (rhs - h0 * dp[j - 1]) / den;
+  }
+  double cn = dp[U - L];
+  if (U < e) c[U] = cn;  // U >= e-1 always; U == e-1 only in the last window
+  for (int i = U - 1; i >= L; --i) {
+    const int j = i - L;
+    cn = dp[j] - cp[j] * cn;
+    if (i >= s && i < e) c[i] = cn;
+  }
+}
+
+__global__ void k_spline_coef(const double* __restrict__ y, const double* __restrict__ c,
+                              int n, double x0, double h, double4* __restrict__ coef) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const double xl = knot(x0, h, i), xr = knot(x0, h, i + 1);
+  const double hh = xr - xl;
+  const double dy = y[i + 1] - y[i];
+  const double b = dy / hh - hh * (c[i + 1] + 2.0 * c[i]) / 3.0;
+  const double d = (c[i + 1] - c[i]) / (3.0 * hh);
+  coef[i] = make_double4(y[i], b, c[i], d);
+}
+
+// calcFormFac (src/UpcCrossSection.cpp:436-445) on Q2 = Q2min + i*dQ2.
+__global__ void k_formfac_values(double* __restrict__ out, int n, double x0, double h,
+                                 double rho0, double R, double a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double Q2 = x0 + i * h;
+  const double Q = sqrt(Q2) / kHc;
+  const double coshVal = cosh(kPi * Q * a);
+  const double sinhVal = sinh(kPi * Q * a);
+  double ff = 4 * kPi * kPi * rho0 * a * a * a / (Q * a * Q * a * sinhVal * sinhVal) *
+              (kPi * Q * a * coshVal * sin(Q * R) - Q * R * cos(Q * R) * sinhVal);
+  ff += 8 * kPi * rho0 * a * a * a * exp(-R / a) / (1 + Q * Q * a * a) / (1 + Q * Q * a * a);
+  out[i] = ff;
+}
+
+// Sequential natural spline for the 200-knot tables of prepareGAA, run by
+// one thread on shared-memory arrays.
+__device__ void spline_serial(const double* y, int n, double h, double* c, double* cp,
+                              double* dp, double4* coef) {
+  const int m = n - 2;
+  for (int i = 0; i < m; ++i) {
+    const double xa = i * h, xb = (i + 1) * h, xc = (i + 2) * h;
+    const double h0 = xb - xa, h1 = xc - xb;
+    const double diag = 2.0 * (h0 + h1);
+    const double rhs = 3.0 * ((y[i + 2] - y[i + 1]) / h1 - (y[i + 1] - y[i]) / h0);
+    if (i == 0) {
+      cp[0] = h1 / diag;
+      dp[0] = rhs / diag;
+    } else {
+      const double den = diag - h0 * cp[i - 1];
+      cp[i] = h1 / den;
+      dp[i] = (rhs - h0 * dp[i - 1]) / den;
+    }
+  }
+  c[0] = 0.0;
+  c[n - 1] = 0.0;
+  c[m] = dp[m - 1];
+  for (int i = m - 2; i >= 0; --i) c[i + 1] = dp[i] - cp[i] * c[i + 2];
+  for (int i = 0; i < n - 1; ++i) {
+    const double xl = i * h, xr = (i + 1) * h, hh = xr - xl;
+    const double dy = y[i + 1] - y[i];
+    coef[i] = make_double4(y[i], dy / hh - hh * (c[i + 1] + 2.0 * c[i]) / 3.0, c[i],
+                           (c[i + 1] - c[i]) / (3.0 * hh));
+  }
+}
+
+__device__ __forceinline__ double eval_u(const double4* coef, int n, double h, double x) {
+  SplineU s{coef, 0.0, h, 1.0 / h, n};
+  return spline_eval_smem(s, coef, x);
+}
+
+// prepareGAA (src/UpcCrossSection.cpp:364-414): one CTA of >= 200 threads.
+__global__ void k_gaa(double rho0, double R, double a, double csNN, GaaConsts k,
+                      double4* __restrict__ gaa_coef) {
+  constexpr int nb = 200;
+  __shared__ double sTA[nb], sG[nb], sc[nb], scp[nb], sdp[nb];
+  __shared__ double4 sTAc[nb - 1];
+  const double bmax = 20.;
+  const double db = bmax / (nb - 1);
+  const int ib = threadIdx.x;
+  if (ib < nb) {
+    const double b = ib * db;
+    double sum = 0, first = 0, last = 0;
+    {
+      double r = sqrt(b * b);
+      first = rho0 / (1 + exp((r - R) / a));
+      const double z = (nb - 1) * db;
+      r = sqrt(b * b + z * z);
+      last = rho0 / (1 + exp((r - R) / a));
+    }
+    sum = first + last;
+    for (int iz = 1; iz < nb - 1; iz += 2) {
+      const double z = iz * db, r = sqrt(b * b + z * z);
+      sum += 4. * (rho0 / (1 + exp((r - R) / a)));
+    }
+    for (int iz = 2; iz < nb - 1; iz += 2) {
+      const double z = iz * db, r = sqrt(b * b + z * z);
+      sum += 2. * (rho0 / (1 + exp((r - R) / a)));
+    }
+    sTA[ib] = 2. * (sum * db / 3.);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) spline_serial(sTA, nb, db, sc, scp, sdp, sTAc);
+  __syncthreads();
+  if (ib < nb) {
+    const double b = ib * db;
+    double vs[nb];
+    for (int is = 0; is < nb; ++is) {
+      const double s = is * db;
+      double sum_phi = 0;
+      for (int q = 0; q < 5; ++q) {
+        const double r = sqrt(b * b + s * s + 2. * b * s * k.cosk[q]);
+        sum_phi += 2. * kPi * k.wk[q] * eval_u(sTAc, nb, db, r < bmax ? r : bmax);
+      }
+      vs[is] = 2. * s * eval_u(sTAc, nb, db, s < bmax ? s : bmax) * sum_phi;
+    }
+    double sum = vs[0] + vs[nb - 1];
+    for (int i = 1; i < nb - 1; i += 2) sum += 4. * vs[i];
+    for (int i = 2; i < nb - 1; i += 2) sum += 2. * vs[i];
+    sG[ib] = exp(-csNN * (sum * db / 3.));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    spline_serial(sG, nb, db, sc, scp, sdp, sTAc);
+    for (int i = 0; i < nb - 1; ++i) gaa_coef[i] = sTAc[i];
+  }
+}
+
+// Photo-neutron data of src/UpcCrossSection.cpp:778-851, 1-based (index 0 unused).
+__constant__ double kE1[23] = {0., 103., 106., 112., 119., 127., 132., 145., 171., 199., 230., 235.,
+                               254., 280., 300., 320., 330., 333., 373., 390., 420., 426., 440.};
+__constant__ double kS1[23] = {0., 12.0, 11.5, 12.0, 12.0, 12.0, 15.0, 17.0, 28.0, 33.0,
+                               52.0, 60.0, 70.0, 76.0, 85.0, 86.0, 89.0, 89.0, 75.0, 76.0, 69.0, 59.0, 61.0};
+__constant__ double kE2[12] = {0., 2000., 3270., 4100., 4810., 6210., 6600.,
+                               7790., 8400., 9510., 13600., 16400.};
+__constant__ double kS2[12] = {0., .1266, .1080, .0805, .1017, .0942, .0844, .0841, .0755, .0827,
+                               .0626, .0740};
+__constant__ double kE3[29] = {0., 26., 28., 30., 32., 34., 36., 38., 40., 44., 46., 48., 50., 52., 55.,
+                               57., 62., 64., 66., 69., 72., 74., 76., 79., 82., 86., 92., 98., 103.};
+__constant__ double kS3[29] = {0., 30., 21.5, 22.5, 18.5, 17.5, 15., 14.5, 19., 17.5, 16., 14.,
+                               20., 16.5, 17.5, 17., 15.5, 18., 15.5, 15.5, 15., 13.5, 18., 14.5, 15.5, 12.5, 13.,
+                               13., 12.};
+__constant__ double kSigt[160] = {
+    0., .4245, .4870, .5269, .4778, .4066, .3341, .2444, .2245, .2005,
+    .1783, .1769, .1869, .1940, .2117, .2226, .2327, .2395, .2646, .2790, .2756,
+    .2607, .2447, .2211, .2063, .2137, .2088, .2017, .2050, .2015, .2121, .2175,
+    .2152, .1917, .1911, .1747, .1650, .1587, .1622, .1496, .1486, .1438, .1556,
+    .1468, .1536, .1544, .1536, .1468, .1535, .1442, .1515, .1559, .1541, .1461,
+    .1388, .1565, .1502, .1503, .1454, .1389, .1445, .1425, .1415, .1424, .1432,
+    .1486, .1539, .1354, .1480, .1443, .1435, .1491, .1435, .1380, .1317, .1445,
+    .1375, .1449, .1359, .1383, .1390, .1361, .1286, .1359, .1395, .1327, .1387,
+    .1431, .1403, .1404, .1389, .1410, .1304, .1363, .1241, .1284, .1299, .1325,
+    .1343, .1387, .1328, .1444, .1334, .1362, .1302, .1338, .1339, .1304, .1314,
+    .1287, .1404, .1383, .1292, .1436, .1280, .1326, .1321, .1268, .1278, .1243,
+    .1239, .1271, .1213, .1338, .1287, .1343, .1231, .1317, .1214, .1370, .1232,
+    .1301, .1348, .1294, .1278, .1227, .1218, .1198, .1193, .1342, .1323, .1248,
+    .1220, .1139, .1271, .1224, .1347, .1249, .1163, .1362, .1236, .1462, .1356,
+    .1198, .1419, .1324, .1288, .1336, .1335, .1266};
+__constant__ double kSigtn[160] = {
+    0., .3125, .3930, .4401, .4582, .3774, .3329, .2996, .2715, .2165,
+    .2297, .1861, .1551, .2020, .2073, .2064, .2193, .2275, .2384, .2150, .2494,
+    .2133, .2023, .1969, .1797, .1693, .1642, .1463, .1280, .1555, .1489, .1435,
+    .1398, .1573, .1479, .1493, .1417, .1403, .1258, .1354, .1394, .1420, .1364,
+    .1325, .1455, .1326, .1397, .1286, .1260, .1314, .1378, .1353, .1264, .1471,
+    .1650, .1311, .1261, .1348, .1277, .1518, .1297, .1452, .1453, .1598, .1323,
+    .1234, .1212, .1333, .1434, .1380, .1330, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
+    .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12};
+
+// Energy / cross-section table of calcBreakupProb's first-call set-up
+// (src/UpcCrossSection.cpp:893-969); lead values as hard-coded there.
+// One thread: the table is a ~650-entry recurrence.
+__global__ void k_breakup_setup(double gammatarg, double* __restrict__ ee,
+                                double* __restrict__ se, int* __restrict__ n_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double zp = 82, ap = 208;
+  const double si1 = 640., gg1 = 4.05, o1 = 13.42, o0 = 7.4;
+  const double delo = .05;
+  const double scon = .1 * gg1 * gg1 * si1;
+  const int ne = int((25. - o0) / delo) + 1;
+  for (int i = 1; i <= ne; i++) {
+    ee[i] = o0 + (i - 1) * delo;
+    se[i] = scon * ee[i] * ee[i] /
+            (((o1 * o1 - ee[i] * ee[i]) * (o1 * o1 - ee[i] * ee[i])) + ee[i] * ee[i] * gg1 * gg1);
+  }
+  int ij = ne;
+  for (int j = 1; j <= 27; j++) { ij++; ee[ij] = kE3[j]; se[ij] = .1 * ap * kS3[j] / 208.; }
+  for (int j = 1; j <= 22; j++) { ij++; ee[ij] = kE1[j]; se[ij] = .1 * ap * kS1[j] / 208.; }
+  for (int j = 9; j <= 70; j++) {
+    ij++;
+    ee[ij] = ee[ij - 1] + 25.;
+    se[ij] = .1 * (zp * kSigt[j] + (ap - zp) * kSigtn[j]);
+  }
+  for (int j = 1; j <= 11; j++) { ij++; ee[ij] = kE2[j]; se[ij] = .1 * ap * kS2[j]; }
+  const double x = .0677, y = .129, eps = .0808, eta = .4525, em = .94;
+  const double exx = pow(10., .05);
+  double s = .002 * em * ee[ij];
+  const int ictr = gammatarg > (2. * 150. * 150.) ? 150 : 100;
+  for (int j = 1; j <= ictr; j++) {
+    ij++;
+    s = s * exx;
+    ee[ij] = 1000. * .5 * (s - em * em) / em;
+    se[ij] = .1 * .65 * ap * (x * pow(s, eps) + y * pow(s, (-eta)));
+  }
+  ee[ij + 1] = 99999999999.;
+  *n_out = ij + 2;
+}
+
+// calcBreakupProb (src/UpcCrossSection.cpp:972-1018) on b = bmin + i*db.
+// The single-neutron sum p1n of the reference never reaches its result and is
+// not computed.
+__global__ void k_breakup_values(const double* __restrict__ ee_g, const double* __restrict__ se_g,
+                                 const int* __restrict__ n_tab, int n, double x0, double h,
+                                 int mode, double gammatarg, double omaxx, double zcon,
+                                 double* __restrict__ out) {
+  extern __shared__ double s_tab[];
+  const int nt = *n_tab;
+  double* see = s_tab;
+  double* sse = s_tab + nt;
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+    see[i] = ee_g[i];
+    sse[i] = se_g[i];
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double b = x0 + i * h;
+  const double hbarcmev = 197.3269718, o0 = 7.4;
+  double pxn = 0.;
+  const double omax = fmin(omaxx, 4. * gammatarg * (hbarcmev) / b);
+  double p = 0.;
+  if (!(omax < o0)) {
+    double gk1m = bessel_k1_as(see[1] * b / ((hbarcmev) * gammatarg));
+    int k = 2;
+    while (k < nt && see[k] < omax) {
+      const double gk1 = bessel_k1_as(see[k] * b / ((hbarcmev) * gammatarg));
+      pxn = pxn + zcon * (see[k] - see[k - 1]) * .5 *
+                      (sse[k - 1] * see[k - 1] * gk1m * gk1m + sse[k] * see[k] * gk1 * gk1);
+      k = k + 1;
+      gk1m = gk1;
+    }
+    if (mode == 1) p = 1.;
+    if (mode == 2) p = (1 - exp(-1 * pxn)) * (1 - exp(-1 * pxn));
+    if (mode == 3) p = exp(-2 * pxn);
+    if (mode == 4) p = 2. * exp(-pxn) * (1. - exp(-pxn));
+  }
+  out[i] = p;
+}
+
+// calcBreakupProb at arbitrary b (the point entry of the C ABI).
+__global__ void k_breakup_pts(const double* __restrict__ ee_g, const double* __restrict__ se_g,
+                              const int* __restrict__ n_tab, const double* __restrict__ bv, int n,
+                              int mode, double gammatarg, double omaxx, double zcon,
+                              double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int nt = *n_tab;
+  const double b = bv[i];
+  const double hbarcmev = 197.3269718, o0 = 7.4;
+  double pxn = 0.;
+  const double omax = fmin(omaxx, 4. * gammatarg * (hbarcmev) / b);
+  double p = 0.;
+  if (!(omax < o0)) {
+    double gk1m = bessel_k1_as(ee_g[1] * b / ((hbarcmev) * gammatarg));
+    int k = 2;
+    while (k < nt && ee_g[k] < omax) {
+      const double gk1 = bessel_k1_as(ee_g[k] * b / ((hbarcmev) * gammatarg));
+      pxn = pxn + zcon * (ee_g[k] - ee_g[k - 1]) * .5 *
+                      (se_g[k - 1] * ee_g[k - 1] * gk1m * gk1m + se_g[k] * ee_g[k] * gk1 * gk1);
+      k = k + 1;
+      gk1m = gk1;
+    }
+    if (mode == 1) p = 1.;
+    if (mode == 2) p = (1 - exp(-1 * pxn)) * (1 - exp(-1 * pxn));
+    if (mode == 3) p = exp(-2 * pxn);
+    if (mode == 4) p = 2. * exp(-pxn) * (1. - exp(-pxn));
+  }
+  out[i] = p;
+}
+
+__global__ void k_formfac_pts(const double* __restrict__ q2, double* __restrict__ out, int n,
+                              double rho0, double R, double a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double Q = sqrt(q2[i]) / kHc;
+  const double coshVal = cosh(kPi * Q * a);
+  const double sinhVal = sinh(kPi * Q * a);
+  double ff = 4 * kPi * kPi * rho0 * a * a * a / (Q * a * Q * a * sinhVal * sinhVal) *
+              (kPi * Q * a * coshVal * sin(Q * R) - Q * R * cos(Q * R) * sinhVal);
+  ff += 8 * kPi * rho0 * a * a * a * exp(-R / a) / (1 + Q * Q * a * a) / (1 + Q * Q * a * a);
+  out[i] = ff;
+}
+
+}  // namespace
+
+cudaError_t launch_breakup_points(double gammatarg, double omaxx, double zcon, int mode,
+                                  const double* d_ee, const double* d_se, const int* d_ntab,
+                                  const double* d_b, double* d_out, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_breakup_pts<<<(n + 127) / 128, 128, 0, st>>>(d_ee, d_se, d_ntab, d_b, n, mode, gammatarg,
+                                                 omaxx, zcon, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, double rho0,
+                                  double R, double a, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_formfac_pts<<<(n + 255) / 256, 256, 0, st>>>(d_q2, d_out, n, rho0, R, a);
+  return cudaGetLastError();
+}
+
+cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
+                                 double4* d_coef, cudaStream_t st) {
+  const int nthreads = (n - 2 + kWinOut - 1) / kWinOut;
+  const int tb = 128;
+  k_spline_window<<<(nthreads + tb - 1) / tb > 0 ? (nthreads + tb - 1) / tb : 1, tb, 0, st>>>(
+      d_y, n, x0, h, d_c);
+  k_spline_coef<<<(n - 1 + 255) / 256, 256, 0, st>>>(d_y, d_c, n, x0, h, d_coef);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, double rho0,
+                                  double R, double a, cudaStream_t st) {
+  k_formfac_values<<<(n + 255) / 256, 256, 0, st>>>(d_out, n, x0, h, rho0, R, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaConsts& k,
+                       double4* d_coef, cudaStream_t st) {
+  k_gaa<<<1, 256, 0, st>>>(rho0, R, a, csNN, k, d_coef);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_breakup(double gammatarg, double omaxx, double zcon, int mode, int n,
+                           double x0, double h, double* d_ee, double* d_se, int* d_ntab,
+                           double* d_out, cudaStream_t st) {
+  k_breakup_setup<<<1, 32, 0, st>>>(gammatarg, d_ee, d_se, d_ntab);
+  const size_t smem = 2 * sizeof(double) * kBreakupTabMax;
+  k_breakup_values<<<(n + 127) / 128, 128, smem, st>>>(d_ee, d_se, d_ntab, n, x0, h, mode,
+                                                        gammatarg, omaxx, zcon, d_out);
+  return cudaGetLastError();
+}
+
+}  // namespace upcg
