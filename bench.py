@@ -1,17 +1,18 @@
 """Benchmark: two-photon luminosity / cross-section tables and event sampling.
 
-Workload (default): the full-grid Pb-Pb configuration -- Woods-Saxon
+Workload (default "c2"): the full-grid Pb-Pb configuration -- Woods-Saxon
 form-factor flux (FLUX_POINT 0), gamma-gamma -> tau tau (PROC_ID 15), XNXN
 breakup (BREAKUP_MODE 2), m in [3.56, 50] GeV x 1001 bins, y in [-6, 6] x 121
-bins, z x 100 bins, pT > 1 GeV and |eta| < 2.4, 1e7 accepted events.
-Synthetic in the only sense that applies: the inputs are these parameters.
+bins, z x 100 bins, pT > 1 GeV and |eta| < 2.4, 1e7 accepted events.  The
+inputs are this parameter set (no dataset is involved).
 
-One step = the complete table build of UpcGenerator::init on the GPU (form
-factor, G_AA and breakup tables, the 121,121-cell luminosity, the nuclear
-cross section and the sampling CDFs), timed with CUDA events on the library's
-stream; the 1e7-event sampling is timed as a second phase of the same step.
-`value` = luminosity cells / second of the table build, `events_per_s` =
-accepted events / second.  The L2 (129 MB) is flushed before every timed phase.
+One step = the complete table build of UpcGenerator::init on the GPU: nuclear
+tables (form factor, G_AA, breakup), the 121,121-cell luminosity, the nuclear
+cross section and the sampling CDFs.  It is timed with CUDA events on the
+library's stream, after a 256 MB L2 flush.  `value` is cells / s of the fast
+form (tensor-core contraction, checked here against the plain FP64 path to
+<= 1e-4); the plain FP64 path is timed in the same run.  The 1e7-event
+sampling is a second timed phase (events_per_s).
 
 --impl reference times the CPU restatement of the reference (oracle/, C++ with
 OpenMP on every host core) on a bounded sample of the same workload.
@@ -42,6 +43,7 @@ WORKLOADS = {
 }
 EVENTS = {"c2": 10_000_000, "c1": 100_000}
 METRIC = "gamma-gamma lumi (m,y) cells/s"
+FAST_GRID_P = 1024  # radial grid of the fast form (csrc/upcg_fast.cu)
 
 
 def peaks():
@@ -49,7 +51,7 @@ def peaks():
     if os.path.exists(p):
         with open(p) as f:
             return json.load(f), "measured"
-    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
 class ClockSampler:
@@ -60,10 +62,7 @@ class ClockSampler:
               "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index=0):
-        self.index = index
-        self.rows = []
-        self.proc = None
-        self.thread = None
+        self.index, self.rows, self.proc, self.thread = index, [], None, None
 
     def start(self):
         try:
@@ -93,10 +92,16 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[0]) for r in self.rows if num(r[0]) is not None]
+        mx = [num(r[1]) for r in self.rows if num(r[1]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if "Active" in r[3 + i]})
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
                 "samples": len(self.rows)}
@@ -108,27 +113,30 @@ def run_reference(args):
     params = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
     o = Oracle(params, threads=threads)
+    t0 = time.perf_counter()
     o.init_tables()
+    t_init = time.perf_counter() - t0
     g = o.grid()
-    # sample: the first R m-rows (all ny rapidities) -- ~10-30 s of CPU work
-    rows = args.ref_rows or (16 if args.workload == "c2" else g["nm"])
-    times = []
-    for _ in range(max(args.warmup, 0) and 1):
+    # sample: the first R m-rows (all rapidities), ~10-30 s of CPU work
+    rows = args.ref_rows or (64 if args.workload == "c2" else g["nm"])
+    for _ in range(min(args.warmup, 1)):
         o.lumi_table(0, 1)
+    times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         o.lumi_table(0, rows)
         times.append(time.perf_counter() - t0)
     cells = rows * g["ny"]
     v = cells / float(np.mean(times))
+    sample = f"first {rows} of {g['nm']} m-rows x {g['ny']} y-bins = {cells} cells per step"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "params": params,
-                       "sample": f"first {rows} m-rows x {g['ny']} y-bins = {cells} cells"},
+            "config": {"workload": args.workload, "sample": sample},
+            "init_tables_s": t_init,
             "cpu_baseline": {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
-                             "sample": f"{cells} cells (first {rows} of {g['nm']} m-rows)"},
+                             "sample": sample},
             "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -150,7 +158,7 @@ def cpu_baseline_sample(workload, seconds=15.0):
         rows = min(g["nm"], rows * 4)
     cells = rows * g["ny"]
     return {"value": cells / dt, "unit": "cells/s", "cores": threads, "kind": "port",
-            "sample": f"{cells} cells (first {rows} of {g['nm']} m-rows), one pass"}
+            "sample": f"{cells} cells (first {rows} of {g['nm']} m-rows, low masses), one pass"}
 
 
 def main():
@@ -162,6 +170,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--events", type=int, default=None)
     ap.add_argument("--ref-rows", type=int, default=None)
+    ap.add_argument("--plain-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
 
@@ -173,6 +182,7 @@ def main():
         return
 
     import torch
+
     import upcgen_gb300 as ug
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
@@ -184,11 +194,14 @@ def main():
     params["SEED"] = 1 + rank  # independent replicas: weak scaling over ranks
     nev = args.events if args.events is not None else EVENTS[args.workload]
     stream = torch.cuda.Stream()
-    gen = ug.UpcGenerator(params)
-    gen.setStream(stream.cuda_stream)
-    g0 = gen.grid()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     evbuf = torch.empty(max(nev, 1) * 48, dtype=torch.uint8, device="cuda")
+
+    def make(method):
+        g = ug.UpcGenerator(params)
+        g.setStream(stream.cuda_stream)
+        g.setLumiMethod(method)
+        return g
 
     def flush_l2():
         with torch.cuda.stream(stream):
@@ -199,81 +212,106 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    def step():
-        s0, s1, s2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    def step(gen, with_events):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         flush_l2()
         s0.record(stream)
         gen.init()
         s1.record(stream)
-        flush_l2()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        rej = ug.C.c_int64()
-        ug._check(gen._L.upcg_generate_events_device(gen._h, nev, ug.C.c_void_p(evbuf.data_ptr()),
-                                                     None, ug.C.byref(rej)))
-        s2.record(stream)
+        ev_ms, rej = None, None
+        if with_events and nev:
+            flush_l2()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = ug.C.c_int64()
+            ug._check(gen._L.upcg_generate_events_device(gen._h, nev, ug.C.c_void_p(evbuf.data_ptr()),
+                                                         None, ug.C.byref(r)))
+            e1.record(stream)
+            stream.synchronize()
+            ev_ms, rej = e0.elapsed_time(e1), r.value
         stream.synchronize()
-        return s0.elapsed_time(s1), e0.elapsed_time(s2), rej.value
+        return s0.elapsed_time(s1), ev_ms, rej, gen.timings()
 
+    fast, plain = make("fast"), make("plain")
+    g0 = fast.grid()
+    cells = g0["nm"] * g0["ny"]
     for _ in range(args.warmup):
-        step()
+        step(fast, True)
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    t_tab, t_ev, rejs, phases = [], [], [], []
-    for _ in range(args.steps):
-        a, b, r = step()
-        t_tab.append(a)
-        t_ev.append(b)
-        rejs.append(r)
-        phases.append(gen.timings())
+    runs = [step(fast, True) for _ in range(args.steps)]
     barrier()
     clk = clocks.stop()
-    ms_tab = float(np.mean(t_tab))
-    ms_ev = float(np.mean(t_ev))
+    ms_tab = float(np.mean([r[0] for r in runs]))
+    ms_ev = float(np.mean([r[1] for r in runs])) if nev else None
+    ms_contract = float(np.mean([r[3]["contract_ms"] for r in runs]))
     if dist is not None:
-        t = torch.tensor([ms_tab, ms_ev], device="cuda")
+        t = torch.tensor([ms_tab, ms_ev or 0.0, ms_contract], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_tab, ms_ev = float(t[0]), float(t[1])
-    cells = g0["nm"] * g0["ny"]
+        ms_tab, ms_ev, ms_contract = float(t[0]), float(t[1]) or None, float(t[2])
     value = world * cells / (ms_tab * 1e-3)
 
-    # end to end through the public API with host buffers (D2H of the tables
-    # and of the events inside the timed region)
-    host_ev = np.zeros(nev, dtype=ug.EVENT_DTYPE)
+    # plain FP64 path on the same workload (the fast form's reference)
+    pk = args.plain_steps if args.plain_steps is not None else (2 if args.workload == "c2" else args.steps)
+    step(plain, False)
+    pruns = [step(plain, False) for _ in range(pk)]
+    ms_plain = float(np.mean([r[0] for r in pruns]))
+    lf, lp = fast.lumiTable(), plain.lumiTable()
+    _, tot_f = fast.nucCSYM()
+    _, tot_p = plain.nucCSYM()
+    big = np.abs(lp) >= 1e-9 * np.abs(lp).max()
+    rel = np.abs(lf - lp)[big] / np.abs(lp[big])
+
+    # end to end through the public API with host buffers
+    host_ev = np.zeros(nev, dtype=ug.EVENT_DTYPE) if nev else None
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    gen.init()
-    lumi = gen.lumiTable()
-    cs, tot = gen.nucCSYM()
+    fast.init()
+    lumi = fast.lumiTable()
+    cs, tot = fast.nucCSYM()
     t1 = time.perf_counter()
-    _, rej_h = gen.generateEvents(nev) if nev else (None, 0)
+    rej_h = fast.generateEvents(nev)[1] if nev else 0
     t2 = time.perf_counter()
-    e2e_cells = cells / (t1 - t0)
-    e2e_events = nev / (t2 - t1) if nev else None
 
-    pk, pk_kind = peaks()
-    ph = phases[-1]
+    pk_vals, pk_kind = peaks()
+    P = FAST_GRID_P
+    cells_pad = (cells + 127) // 128 * 128
+    alg_flops = 2.0 * cells_pad * P * P  # A1 (cells x P) . G (P x P)
+    achieved = alg_flops / (ms_contract * 1e-3) / 1e12
+    peak = pk_vals.get("bf16_tflops", 1900.0)
+    ph = runs[-1][3]
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_tab,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (parameter set; no dataset)",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+bf16x3",
+        "data": "synthetic (the workload is a parameter set)",
         "config": {"workload": f"{args.workload}: Pb-Pb {g0['nm']}x{g0['ny']} (m,y) cells, "
                                f"FLUX_POINT {params['FLUX_POINT']}, BREAKUP_MODE {params['BREAKUP_MODE']}, "
                                f"PROC_ID {params['PROC_ID']}, {nev} events",
-                   "lumi_method": "plain FP64", "l2": "flushed (256 MB write) before each timed phase"},
+                   "lumi_method": "fast form (tcgen05 3xBF16 contraction)",
+                   "l2": "flushed (256 MB write) before each timed phase"},
+        "fast_vs_plain": {"max_rel_err_cells_above_1e-9_of_max": float(rel.max()),
+                          "median_rel_err": float(np.median(rel)),
+                          "sigma_tot_rel_err": abs(tot_f / tot_p - 1),
+                          "plain_ms_per_step": ms_plain,
+                          "plain_cells_per_s": cells / (ms_plain * 1e-3),
+                          "speedup": ms_plain / ms_tab},
         "events_per_s": world * nev / (ms_ev * 1e-3) if nev else None,
-        "ms_events": ms_ev,
-        "rejected_per_step": rejs[-1],
+        "ms_events": ms_ev, "rejected_per_step": runs[-1][2],
         "sigma_tot_mb": tot,
-        "phases_ms": ph,
-        "e2e": {"value": e2e_cells, "unit": "cells/s", "h2d_bytes_per_step": 0,
+        "phases_ms": ph, "plain_phases_ms": pruns[-1][3],
+        "e2e": {"value": cells / (t1 - t0), "unit": "cells/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(lumi.nbytes + cs.nbytes),
-                "events_per_s": e2e_events, "events_d2h_bytes": nev * 48},
+                "events_per_s": nev / (t2 - t1) if nev else None,
+                "events_d2h_bytes_per_step": nev * 48},
+        "roofline": {"kernel": "k_contract (tcgen05.mma kind::f16, 3xBF16)", "bound": "tensor",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": f"algorithmic 2*cells*P^2 = {alg_flops:.3e} FLOP per table "
+                             f"(issued 3x for the hi/lo split); peak = {pk_kind} bf16 burst"},
         "gpu_launches": None,
         "clocks": clk,
-        "peaks": {"source": pk_kind},
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.workload)

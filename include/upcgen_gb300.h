@@ -77,7 +77,9 @@ int upcg_set_lumi_cache(upcg_generator* g, int enable);
  * handle's own stream */
 int upcg_set_stream(upcg_generator* g, void* stream);
 /* Luminosity method: 0 = plain FP64 (default; the reference's quadrature),
- * 1 = fast form (tensor-core contraction, <= 1e-4 relative) */
+ * 1 = fast form (flux tables + tensor-core contraction, <= 1e-4 relative to
+ * the converged quadrature), 2 = the fast form's contraction on the plain
+ * path's node fluxes (diagnostic) */
 int upcg_set_lumi_method(upcg_generator* g, int method);
 
 /* ---- initialisation (UpcGenerator::init) ------------------------------ */
@@ -148,7 +150,17 @@ int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted);
 /* ---- diagnostics --------------------------------------------------------- */
 /* Philox4x32-10 uniforms of the event stream (seed, counter) -- for tests */
 int upcg_philox(uint64_t seed, uint64_t counter0, size_t n, uint32_t* out4);
-/* timings of the last upcg_init phases (ms) and QAGS statistics */
+/* The tensor-core contraction of the fast form on random data (ncells x P
+ * operands, P a multiple of 256) against an FP64 contraction of the same
+ * bf16 hi/lo values: max relative error per cell (negative: the kernel's
+ * error word) and the contraction time in ms -- for tests */
+int upcg_selftest_contract(int ncells, int P, uint64_t seed, double* max_rel, double* ms);
+/* The fast form's form-factor flux amplitude table Q[512][256] on
+ * (ln w, ln b) and its grid {ln w0, h_w, ln b0, h_b} -- for tests */
+int upcg_fast_flux_table(upcg_generator* g, double* out, size_t n, double* grid);
+/* timings of the last upcg_init phases (ms): [0] tables [1] luminosity
+ * [2] cross section + samplers [3] nodes [4] QAGS [5] band quadrature or
+ * tensor-core contraction [6] fast-form projection + kernel build */
 int upcg_last_timings(const upcg_generator* g, double* ms, size_t n);
 int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_intervals,
                     uint64_t* evals);

@@ -96,6 +96,7 @@ int Ctx::set_param(const std::string& k, const std::string& v) {
     else if (k == "NON_ZERO_GAM_PT") useNonzeroGamPt = std::stoi(v);
     else if (k == "USE_POLARIZED_CS") usePolarizedCS = std::stoi(v);
     else if (k == "SEED") seed = std::stol(v);
+    else if (k == "ORACLE_FLUX_EPS") fluxEps = std::stod(v);
     else return 1;  // accepted and ignored (PYTHIA_*, output flags, ...)
   } catch (...) {
     return -1;
@@ -422,7 +423,7 @@ double Ctx::flux_form(double b, double k, QagsResult* info) const {  // :181-218
     double ff = formfac.eval(t < kQ2max ? t : kQ2max - kDQ2);
     return q * q * ff / t * ::j1(b * q / kHc);
   };
-  QagsResult r = qags(integrand, 0., 10., 1e-4, 1e-4, 1000);
+  QagsResult r = qags(integrand, 0., 10., fluxEps, fluxEps, 1000);
   if (info) *info = r;
   double Q = r.result / A;
   return factor * Q * Q / k;

@@ -34,6 +34,11 @@ struct Ctx {
   double minPt = 0, minEta = 0, maxEta = 0;
   long seed = 0, nEvents = 1000;
   int numThreads = 1;
+  // Tolerance of the form-factor flux QAGS (epsabs = epsrel).  The reference
+  // fixes 1e-4 (src/UpcCrossSection.cpp:209); the key ORACLE_FLUX_EPS, which
+  // the reference does not have, tightens it so that tests can tell the
+  // reference's quadrature noise from the error of an approximation.
+  double fluxEps = 1e-4;
   // derived
   double factor = 0, cs_nn = 0;
   bool initialized = false;

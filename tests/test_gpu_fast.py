@@ -1,0 +1,100 @@
+"""Fast form (tensor-core contraction) against the FP64 oracle.
+
+Budget: 1e-4 relative per luminosity cell and on sigma_tot.  The fast form
+keeps the reference's per-cell impact-parameter nodes; its error comes from
+the survival kernel's interpolation on the fixed radial grid, the flux
+tables, and the BF16 hi/lo split with FP32 accumulation.
+
+With the form-factor flux the reference integrates each node's flux by QAGS
+at epsabs = epsrel = 1e-4 (src/UpcCrossSection.cpp:209).  That quadrature
+stops early on the oscillating Bessel integrand at some nodes (at b = 4.55
+fm, k = 10.75 GeV it returns a flux 5 % above the converged integral), so the
+reference's own cells carry errors of up to a few 1e-4 in the bulk and
+factors at the rapidity edges, where the photon energy reaches TeV.  The
+fast form integrates to convergence; its cells are checked against the
+oracle run with a converged flux quadrature (ORACLE_FLUX_EPS = 1e-10), and
+its sigma_tot against the reference's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FAST_TOL = 1e-4
+
+C1 = {"NUCLEUS_Z": 82, "NUCLEUS_A": 208, "WS_R": 6.68, "WS_A": 0.447, "SQRTS": 5020,
+      "PROC_ID": 13, "LEP_A": 0, "FLUX_POINT": 1, "BREAKUP_MODE": 1,
+      "MMIN": 3.56, "MMAX": 50, "BINS_M": 201, "YMIN": -6, "YMAX": 6, "BINS_Y": 61,
+      "ZMIN": -1, "ZMAX": 1, "BINS_Z": 100, "SEED": 1}
+
+
+@pytest.mark.parametrize("ncells,P", [(256, 256), (1000, 1024)])
+def test_contraction_vs_fp64(ug, ncells, P):
+    err, ms = ug.selftest_contract(ncells, P, seed=3)
+    assert err >= 0, f"contraction kernel error word {-err}"
+    # hi*hi + hi*lo + lo*hi of the same bf16 pairs, FP32 accumulation
+    assert err < 2e-5, err
+
+
+def _fast_vs_oracle(ug, oracle_mod, params):
+    g = ug.UpcGenerator(params)
+    g.setLumiMethod("fast")
+    g.init()
+    lumi = g.lumiTable()
+    o = oracle_mod.Oracle(params, threads=os.cpu_count())
+    o.init_tables()
+    ref = o.lumi_table()
+    if params.get("FLUX_POINT", 1):
+        conv = ref  # closed-form flux: no quadrature noise in the reference
+    else:
+        oc = oracle_mod.Oracle(dict(params, ORACLE_FLUX_EPS=1e-10), threads=os.cpu_count())
+        oc.init_tables()
+        conv = oc.lumi_table()
+    rel = np.abs(lumi - conv) / np.abs(conv)
+    _, tot = g.nucCSYM()
+    _, rtot, _ = o.nuc_cs_ym(ref)
+    return rel, abs(tot / rtot - 1), g
+
+
+def test_fast_config1_full_grid(ug, oracle_mod):
+    rel, rtot, g = _fast_vs_oracle(ug, oracle_mod, C1)
+    assert rel.max() < FAST_TOL, (rel.max(), np.unravel_index(rel.argmax(), rel.shape))
+    assert rtot < FAST_TOL
+    t = g.timings()
+    assert t["contract_ms"] > 0
+
+
+@pytest.mark.parametrize("mode", [2, 3, 4])
+def test_fast_breakup_modes(ug, oracle_mod, mode):
+    rel, rtot, _ = _fast_vs_oracle(ug, oracle_mod, dict(C1, BREAKUP_MODE=mode, BINS_M=41, BINS_Y=25))
+    assert rel.max() < FAST_TOL and rtot < FAST_TOL
+
+
+def test_fast_form_factor_flux(ug, oracle_mod):
+    p = dict(C1, PROC_ID=15, FLUX_POINT=0, BREAKUP_MODE=2, BINS_M=21, BINS_Y=13)
+    rel, rtot, _ = _fast_vs_oracle(ug, oracle_mod, p)
+    assert rel.max() < FAST_TOL and rtot < FAST_TOL
+
+
+def test_fast_light_nucleus(ug, oracle_mod):
+    p = dict(C1, PROC_ID=51, ALP_MASS=1, ALP_WIDTH=0.01, NUCLEUS_Z=8, NUCLEUS_A=16,
+             WS_R=2.608, WS_A=0.513, SQRTS=5360, BREAKUP_MODE=3, BINS_M=21, BINS_Y=25)
+    rel, rtot, _ = _fast_vs_oracle(ug, oracle_mod, p)
+    assert rel.max() < FAST_TOL and rtot < FAST_TOL
+
+
+def test_fast_contraction_on_reference_fluxes(ug):
+    """Method 2: the plain path's node fluxes (the reference's QAGS) through
+    the projection and the tensor-core contraction -- isolates the
+    contraction's error from the flux tables'."""
+    p = dict(C1, PROC_ID=15, FLUX_POINT=0, BREAKUP_MODE=2, BINS_M=41, BINS_Y=25)
+    out = {}
+    for meth in ("plain", "hybrid"):
+        g = ug.UpcGenerator(p)
+        g.setLumiMethod(meth)
+        g.init()
+        out[meth] = g.lumiTable()
+    rel = np.abs(out["hybrid"] / out["plain"] - 1)
+    assert rel.max() < 2e-5, rel.max()

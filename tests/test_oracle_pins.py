@@ -190,3 +190,30 @@ def test_gaa_limits(oracle_mod):
     w = np.array([0.2955242247147529, 0.2692667193099963, 0.2190863625159820,
                   0.1494513491505806, 0.0666713443086881])
     assert w.sum() == pytest.approx(0.9999999999999999, abs=2e-16)
+
+
+def test_reference_flux_quadrature_noise(oracle_mod):
+    """The reference's form-factor flux QAGS (epsabs = epsrel = 1e-4,
+    src/UpcCrossSection.cpp:209) stops early at some nodes: at b = 4.5545 fm,
+    k = 10.75 GeV it returns a flux 5 % above the converged integral.  With
+    ORACLE_FLUX_EPS = 1e-10 the oracle's flux agrees with an independent
+    adaptive quadrature (scipy) to 1e-9."""
+    p = {"PROC_ID": 15, "FLUX_POINT": 0, "BREAKUP_MODE": 2}
+    o = oracle_mod.Oracle(p)
+    o.init_tables()
+    oc = oracle_mod.Oracle(dict(p, ORACLE_FLUX_EPS=1e-10))
+    oc.init_tables()
+    b, k = 4.5545, 10.75
+    g, hc, A = o.gamma(), 0.1973269718, 208
+    q2c = 2 - (2 - 1e-9) / 1e6
+
+    def integrand(q):
+        t = q * q + (k / g) ** 2
+        return q * q * o.form_factor_spline(t if t < 2 else q2c) / t * special.j1(b * q / hc)
+
+    v, _ = integrate.quad(integrand, 0, 10, epsabs=1e-13, epsrel=1e-12, limit=5000)
+    fconv = oc.flux_form(b, k)
+    fref = o.flux_form(b, k)
+    scale = fconv / (v / A) ** 2 * k  # the flux's constant factor
+    assert scale == pytest.approx(82 ** 2 / 137.035999074 / np.pi ** 2 / hc ** 2, rel=1e-9)
+    assert fref / fconv - 1 == pytest.approx(0.0527, abs=2e-3)

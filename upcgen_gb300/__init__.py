@@ -34,6 +34,7 @@ ABI_SYMBOLS = [
     "upcg_two_photon_lumi", "upcg_cs_m", "upcg_generate_events",
     "upcg_generate_events_device", "upcg_generate_event", "upcg_philox",
     "upcg_last_timings", "upcg_qags_stats", "upcg_last_error", "upcg_version",
+    "upcg_selftest_contract", "upcg_fast_flux_table",
 ]
 
 
@@ -77,6 +78,8 @@ def load_library(path=None):
         "upcg_last_timings": [vp, dp, sz],
         "upcg_qags_stats": [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)],
         "upcg_last_error": [], "upcg_version": [],
+        "upcg_selftest_contract": [i, i, u64, dp, dp],
+        "upcg_fast_flux_table": [vp, vp, sz, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -98,6 +101,14 @@ def _arr(x):
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def selftest_contract(ncells, P, seed=1):
+    """Tensor-core contraction vs FP64 on random data: (max rel err, ms)."""
+    L = load_library()
+    e, t = C.c_double(), C.c_double()
+    _check(L.upcg_selftest_contract(int(ncells), int(P), int(seed), C.byref(e), C.byref(t)))
+    return e.value, t.value
 
 
 def philox(seed, counter0, n):
@@ -219,7 +230,7 @@ class UpcGenerator:
         _check(self._L.upcg_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))
 
     def setLumiMethod(self, method):
-        _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1}.get(method, method)))
+        _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1, "hybrid": 2}.get(method, method)))
 
     # -- computation
     def init(self):
@@ -286,7 +297,8 @@ class UpcGenerator:
     def timings(self):
         v = (C.c_double * 8)()
         _check(self._L.upcg_last_timings(self._h, v, 8))
-        return {"tables_ms": v[0], "lumi_ms": v[1], "xsec_ms": v[2]}
+        return {"tables_ms": v[0], "lumi_ms": v[1], "xsec_ms": v[2], "nodes_ms": v[3],
+                "qags_ms": v[4], "contract_ms": v[5], "project_ms": v[6]}
 
     def qagsStats(self):
         f, m, e = C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -105,13 +105,17 @@ struct upcg_generator {
   DBuf<double> ff_y, ff_c, brk_y, brk_c, ee, se, lumi, lumi2, cs, ratio, cszm, cszm2, cszm3;
   DBuf<double> cdf2, cdfz, cdfz2, cdfz3, flux, partial, tot, rho_tmp, gws, pts_a, pts_b, pts_c;
   DBuf<double4> ff_coef, gaa_coef, brk_coef;
-  DBuf<int> ntab, nq, ovf, tile_count;
+  DBuf<int> ntab, nq, ovf, tile_count, mirror;
   DBuf<unsigned int> work;
   DBuf<QagsStats> stats;
   DBuf<float> ptcdf;
   DBuf<uint32_t> mask;
   DBuf<int64_t> tile_off, total;
   DBuf<EventRecord> evbuf;
+  DBuf<uint16_t> fgh, fgl, fah, fal;  // fast form: bf16 hi/lo of G and of the projections
+  DBuf<float> fa2, fpart;
+  DBuf<double> ffar, fk1, fk0, fq, fqn, fwn, fH, fJ;
+  DBuf<unsigned> ferr;
   DBuf<int32_t> mbinbuf;
   int brk_n = 0;
   bool tables_ready = false, lumi_ready = false, xsec_ready = false;
@@ -244,6 +248,7 @@ LumiParams upcg_generator::lumi_params() const {
   p.ff = SplineU{ff_coef.p, kQ2min, dq, 1.0 / dq, kNQ2};
   p.q2max = kQ2max;
   p.q2clamp = kQ2max - dq;
+  p.mirror = nullptr;
   return p;
 }
 
@@ -281,6 +286,30 @@ EventParams upcg_generator::event_params() const {
 }
 
 namespace {
+// Nodes and weights of the n-point Gauss-Legendre rule on [-1, 1] (Newton
+// iteration on P_n from the Chebyshev-like initial guesses).
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.resize(n);
+  w.resize(n);
+  for (int i = 0; i < n; ++i) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    x[i] = z;
+    w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
 // calcWSRho (src/UpcCrossSection.cpp:152-163) on the device: one thread,
 // 200 terms in the reference's order.
 __global__ void k_ws_rho(double R, double a, int A, double* out) {
@@ -321,7 +350,7 @@ int upcg_generator::build_tables() {
     gk.cosk[q] = std::cos(M_PI * kX10pos[q]);
     gk.wk[q] = kW10pos[q];
   }
-  CK(gaa_coef.ensure(199));
+  CK(gaa_coef.ensure(2 * 199 + 50));  // G_AA spline + build scratch (launch_gaa)
   CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, s));
   // form factor on 1e6 knots
   const double dq = (kQ2max - kQ2min) / kNQ2;
@@ -368,11 +397,24 @@ int upcg_generator::build_tables() {
 
 int upcg_generator::build_lumi() {
   cudaStream_t s = st();
-  const LumiParams p = lumi_params();
   const int ncell = nm * ny;
   CK(lumi.ensure(ncell));
   if (usePolarizedCS) CK(lumi2.ensure(ncell));
-  const int chunk = std::min(ncell, 65536);
+  // mirror rapidities (see LumiParams::mirror); chunks hold whole m-rows
+  std::vector<int> mir(ny, -1);
+  const double dy = (ymax - ymin) / ny;
+  for (int a = 0; a < ny; ++a) {
+    const double ya = ymin + dy * a;
+    for (int b = 0; b < ny; ++b) {
+      const double yb = ymin + dy * b;
+      if (b != a && std::fabs(ya + yb) <= 8 * 2.220446049250313e-16 * std::fabs(ya)) { mir[a] = b; break; }
+    }
+  }
+  CK(mirror.ensure(ny));
+  CK(cudaMemcpyAsync(mirror.p, mir.data(), ny * sizeof(int), cudaMemcpyHostToDevice, s));
+  LumiParams p = lumi_params();
+  p.mirror = mirror.p;
+  const int chunk = std::max(1, std::min(ncell, 65536) / ny) * ny;
   CK(flux.ensure((size_t)chunk * 2 * kNb));
   CK(nq.ensure((size_t)chunk * 2));
   CK(work.ensure(1));
@@ -380,19 +422,92 @@ int upcg_generator::build_lumi() {
   const int ovf_cap = 1 << 20;
   CK(ovf.ensure(ovf_cap));
   CK(cudaMemsetAsync(stats.p, 0, sizeof(QagsStats), s));
-  cudaEvent_t t0, t1;
-  cudaEventCreate(&t0);
-  cudaEventCreate(&t1);
-  cudaEventRecord(t0, s);
+  // 1: fast form (flux tables + tensor-core contraction); 2: the same
+  // contraction on the plain path's exact node fluxes (QAGS / K0,K1)
+  const bool fast = lumiMethod >= 1;
+  const bool node_flux = lumiMethod == 2 || !fast;
+  if (fast && usePolarizedCS)
+    return fail(UPCG_ERR_ARG, "the fast form covers the unpolarized luminosity");
+  const int P = fast_grid_points();
+  const double fu0 = std::log(0.1), fh = (std::log(256.) - std::log(0.1)) / (P - 1);
+  const int chunk_pad = (chunk + 127) / 128 * 128;
+  if (fast) {
+    CK(fgh.ensure((size_t)P * P));
+    CK(fgl.ensure((size_t)P * P));
+    CK(fah.ensure((size_t)chunk_pad * P));
+    CK(fal.ensure((size_t)chunk_pad * P));
+    CK(fa2.ensure((size_t)chunk_pad * P));
+    CK(ffar.ensure(2 * (size_t)chunk_pad));
+    CK(fpart.ensure((size_t)chunk * (P / 256)));
+    CK(ferr.ensure(1));
+    CK(cudaMemsetAsync(ferr.p, 0, sizeof(unsigned), s));
+  }
+  // phase timers: 0 whole, 1 nodes, 2 qags, 3 band / contraction, 4 projection + G
+  std::vector<cudaEvent_t> ev;
+  auto mark = [&]() {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s);
+    ev.push_back(e);
+    return (int)ev.size() - 1;
+  };
+  std::vector<std::pair<int, std::pair<int, int>>> spans;  // (phase, (begin, end))
+  const int w0 = mark();
+  FastFluxTables ftab{};
+  if (fast) {
+    const int b = mark();
+    CK(launch_fast_G(p, fu0, fh, P, fgh.p, fgl.p, s));
+    // flux tables: K0/K1 on ln x; Q(w, b) on 512 x 256 (ln w, ln b) points by
+    // 160 Gauss-Legendre panels of 16 points on q in [0, 10]
+    const int nk = flux_table_ktab_n();
+    CK(fk1.ensure(nk));
+    CK(fk0.ensure(nk));
+    ftab.k1t = fk1.p;
+    ftab.k0t = fk0.p;
+    ftab.nw = 512;
+    ftab.nb = 256;
+    const double ymx = std::max(std::fabs(ymin), std::fabs(ymax));
+    const double kmin = mmin / 2. * std::exp(-ymx) * 0.9, kmax = mmax / 2. * std::exp(ymx) * 1.1;
+    ftab.lw0 = std::log(kmin);
+    ftab.hw = (std::log(kmax) - ftab.lw0) / (ftab.nw - 1);
+    ftab.lb0 = std::log(0.05 * R * 0.999);
+    ftab.hb = (std::log(2. * R * 1.001) - ftab.lb0) / (ftab.nb - 1);
+    const int npan = 160, ngl = 16, nqn = npan * ngl;
+    if (!isPoint) {
+      std::vector<double> gx, gw, qn(nqn), wn(nqn);
+      gauss_legendre(ngl, gx, gw);
+      for (int pa = 0; pa < npan; ++pa) {
+        const double lo = 10.0 * pa / npan, hi = 10.0 * (pa + 1) / npan;
+        for (int j = 0; j < ngl; ++j) {
+          qn[pa * ngl + j] = 0.5 * (hi - lo) * gx[j] + 0.5 * (hi + lo);
+          wn[pa * ngl + j] = 0.5 * (hi - lo) * gw[j];
+        }
+      }
+      CK(fqn.ensure(nqn));
+      CK(fwn.ensure(nqn));
+      CK(fq.ensure((size_t)ftab.nw * ftab.nb));
+      CK(fH.ensure((size_t)ftab.nw * nqn));
+      CK(fJ.ensure((size_t)nqn * ftab.nb));
+      CK(cudaMemcpyAsync(fqn.p, qn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(fwn.p, wn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
+      ftab.qt = fq.p;
+    }
+    CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, s));
+    spans.push_back({4, {b, mark()}});
+  }
   for (int c0 = 0; c0 < ncell; c0 += chunk) {
     const int nc = std::min(chunk, ncell - c0);
-    CK(launch_lumi_nodes(p, c0, nc, flux.p, nq.p, s));
-    if (!isPoint) {
-      QagsStats before{};
-      CK(cudaMemcpyAsync(&before, stats.p, sizeof before, cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
+    int b = 0;
+    if (node_flux) {
+      b = mark();
+      CK(launch_lumi_nodes(p, c0, nc, flux.p, nq.p, s));
+      spans.push_back({1, {b, mark()}});
+    }
+    if (!isPoint && node_flux) {
       CK(cudaMemsetAsync(&stats.p->overflow, 0, sizeof(unsigned), s));
+      b = mark();
       CK(launch_lumi_qags(p, c0, nc, flux.p, nq.p, work.p, ovf.p, ovf_cap, stats.p, nullptr, 0, s));
+      spans.push_back({2, {b, mark()}});
       unsigned novf = 0;
       CK(cudaMemcpyAsync(&novf, &stats.p->overflow, sizeof novf, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
@@ -404,15 +519,39 @@ int upcg_generator::build_lumi() {
                                      warps, s));
       }
     }
-    CK(launch_lumi_band(p, c0, nc, flux.p, lumi.p + 0, usePolarizedCS ? lumi2.p : nullptr, s));
+    if (!fast) {
+      b = mark();
+      CK(launch_lumi_band(p, c0, nc, flux.p, lumi.p + 0, usePolarizedCS ? lumi2.p : nullptr, s));
+      spans.push_back({3, {b, mark()}});
+    } else {
+      const int ncp = (nc + 127) / 128 * 128;
+      b = mark();
+      CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, node_flux ? flux.p : nullptr, &ftab,
+                             fah.p, fal.p, fa2.p, ffar.p, s));
+      spans.push_back({4, {b, mark()}});
+      b = mark();
+      CK(launch_contract(fah.p, fal.p, fgh.p, fgl.p, fa2.p, ncp, nc, P, fpart.p, ferr.p, s));
+      spans.push_back({3, {b, mark()}});
+      CK(launch_fast_finish(p, c0, nc, P / 256, fpart.p, ffar.p, lumi.p, s));
+    }
   }
-  cudaEventRecord(t1, s);
-  CK(cudaEventSynchronize(t1));
+  const int w1 = mark();
+  CK(cudaEventSynchronize(ev[w1]));
   float ms = 0;
-  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventElapsedTime(&ms, ev[w0], ev[w1]);
   timings[1] = ms;
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
+  for (int k = 3; k < 8; ++k) timings[k] = 0;
+  for (auto& sp : spans) {
+    float t = 0;
+    cudaEventElapsedTime(&t, ev[sp.second.first], ev[sp.second.second]);
+    timings[2 + sp.first] += t;  // [3] nodes [4] qags [5] band/contract [6] projection+G
+  }
+  for (auto e : ev) cudaEventDestroy(e);
+  if (fast) {
+    unsigned herr = 0;
+    CK(cudaMemcpy(&herr, ferr.p, sizeof herr, cudaMemcpyDeviceToHost));
+    if (herr) return fail(UPCG_ERR_CUDA, "tensor-core contraction timed out (code %u)", herr);
+  }
   CK(cudaMemcpyAsync(&last_stats, stats.p, sizeof last_stats, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   lumi_ready = true;
@@ -514,6 +653,10 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
   }
   int64_t done = 0;
   const int64_t kMaxChunk = (int64_t)1 << 28;
+  // the reference's loop never ends when the cuts reject everything
+  // (src/UpcGenerator.cpp:840-889); this one gives up after 2^34 candidates
+  // in a row without an accepted event
+  int64_t dry = 0;
   while (done < n) {
     const int64_t need = n - done;
     int64_t nc = (int64_t)std::ceil(need / std::max(acc_rate, 1e-4) * 1.05) + 4096;
@@ -532,6 +675,9 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     CK(cudaMemcpyAsync(&acc, total.p, sizeof acc, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     acc_rate = std::max(1e-6, (double)acc / (double)nc);
+    dry = acc == 0 ? dry + nc : 0;
+    if (dry >= ((int64_t)1 << 34))
+      return fail(UPCG_ERR_NUMERIC, "no candidate passed the cuts in %lld draws", (long long)dry);
     if (acc >= need) {
       CK(cudaMemsetAsync(total.p + 1, 0xff, sizeof(int64_t), s));
       k_find_cut<<<1, 32, 0, s>>>(tile_count.p, tile_off.p, mask.p, tiles, need, total.p + 1);
@@ -642,7 +788,7 @@ int upcg_set_stream(upcg_generator* g, void* stream) {
 }
 
 int upcg_set_lumi_method(upcg_generator* g, int method) {
-  if (!g || method < 0 || method > 1) return fail(UPCG_ERR_ARG, "bad luminosity method");
+  if (!g || method < 0 || method > 2) return fail(UPCG_ERR_ARG, "bad luminosity method");
   if (method != g->lumiMethod) g->invalidate();
   g->lumiMethod = method;
   return UPCG_OK;
@@ -655,7 +801,6 @@ int upcg_init(upcg_generator* g) {
     return fail(UPCG_ERR_CUDA, "no CUDA device visible");
   if (g->nm < 1 || g->ny < 1 || g->nz < 1) return fail(UPCG_ERR_ARG, "empty grid");
   if (g->breakupMode < 1 || g->breakupMode > 4) return fail(UPCG_ERR_ARG, "BREAKUP_MODE must be 1..4");
-  if (g->lumiMethod != 0) return fail(UPCG_ERR_ARG, "fast form not built into this library");
   int rc = g->build_tables();
   if (rc) return rc;
   rc = g->build_lumi();
@@ -962,6 +1107,28 @@ int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_i
   if (failures) *failures = g->last_stats.failures;
   if (max_intervals) *max_intervals = g->last_stats.max_intervals;
   if (evals) *evals = g->last_stats.evals;
+  return UPCG_OK;
+}
+
+int upcg_fast_flux_table(upcg_generator* g, double* out, size_t n, double* grid) {
+  if (!g || !out || !grid) return fail(UPCG_ERR_ARG, "null argument");
+  if (!g->lumi_ready || g->lumiMethod != 1 || g->isPoint || !g->fq.p)
+    return fail(UPCG_ERR_STATE, "no fast-form flux table (fast method, FLUX_POINT 0, after init)");
+  const size_t need = (size_t)512 * 256;
+  if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
+  CK(cudaMemcpy(out, g->fq.p, need * sizeof(double), cudaMemcpyDeviceToHost));
+  const double ymx = std::max(std::fabs(g->ymin), std::fabs(g->ymax));
+  const double kmin = g->mmin / 2. * std::exp(-ymx) * 0.9, kmax = g->mmax / 2. * std::exp(ymx) * 1.1;
+  grid[0] = std::log(kmin);
+  grid[1] = (std::log(kmax) - grid[0]) / 511;
+  grid[2] = std::log(0.05 * g->R * 0.999);
+  grid[3] = (std::log(2. * g->R * 1.001) - grid[2]) / 255;
+  return UPCG_OK;
+}
+
+int upcg_selftest_contract(int ncells, int P, uint64_t seed, double* max_rel, double* ms) {
+  if (!max_rel || !ms || ncells < 1 || P < 256 || P % 256) return fail(UPCG_ERR_ARG, "bad argument");
+  CK(contract_selftest(ncells, P, seed, max_rel, ms));
   return UPCG_OK;
 }
 

@@ -5,7 +5,8 @@
 //   * K0, K1 (gsl_sf_bessel_K0/K1 in src/UpcCrossSection.cpp:171-172):
 //     ascending series (A&S 9.6.11/9.6.13) for x <= 2, trapezoid rule on
 //     K_nu(x) = int_0^inf exp(-x cosh t) cosh(nu t) dt (A&S 9.6.24) with step
-//     0.2 for 2 < x <= 30, Hankel asymptotic series above 30.
+//     0.15 for 2 < x <= 18.5 (aliasing error below exp(-(2 pi / h)^2 / 2x) <
+//     1e-17), Hankel asymptotic series above 18.5 (truncation below e^{-2x}).
 //   * K1 of ROOT's TMath::BesselK1 (src/UpcCrossSection.cpp:982-999): the
 //     Abramowitz & Stegun polynomials 9.8.3 / 9.8.7 / 9.8.8, whose ~1e-7
 //     error the breakup probability inherits.
@@ -28,16 +29,18 @@ constexpr double kMTau = 1.77686;
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kEulerGamma = 0.57721566490153286061;
 
-// cosh(n h) - 1 for h = 0.2, n = 1..32 (2 sinh^2(n h / 2)).
-__constant__ static double kCoshM1[32] = {
-    0.020066755619075848, 0.081072371838454838, 0.1854652182422678, 0.33743494630484461,
-    0.54308063481524382, 0.81065556732437483, 1.1508984653931409, 1.5774644711948853,
-    2.1074731763172663, 2.7621956910836309, 3.5679083288982283, 4.5569471669655091,
-    5.7690058066080132, 7.2527284168611361, 9.0676619957777636, 11.286646200543862,
-    13.998736658678677, 17.31277908306264, 21.361777632578498, 26.30823283601649,
-    32.350663308872811, 39.731573002435603, 48.747183738839247, 59.759323632891977,
-    73.209948524787848, 89.638879219785991, 109.70546639256487, 134.21505264493462,
-    164.1512937321971, 200.71563612245592, 245.37553526194637, 299.92334971467767};
+// cosh(n h) - 1 for h = 0.15, n = 1..40 (2 sinh^2(n h / 2)).
+__constant__ static double kCoshM1[40] = {
+    0.011271109576670463, 0.045338514128860481, 0.10297016855597102, 0.18546521824226767,
+    0.29468328467684468, 0.43308638544877426, 0.60379443358715978, 0.8106555673243746,
+    1.0583328956714328, 1.3524096152432474, 1.6995148679003012, 2.1074731763172654,
+    2.585480826087903, 3.144313170410316, 3.7965675304601945, 4.5569471669655064,
+    5.4425927243320906, 6.4734686188062902, 7.67281308072124, 9.0676619957777636,
+    10.689458353904875, 12.574761044029561, 14.766068972562996, 17.31277908306263,
+    20.272299872959394, 23.71134550848798, 27.707439710042841, 32.350663308872811,
+    37.745684868920648, 44.014120148530033, 51.297273589522334, 59.759323632891935,
+    69.591023665202954, 81.014002023233587, 94.28575798851459, 109.70546639256477,
+    127.6207216815091, 148.43537346625885, 172.61863018894627, 200.71563612245592};
 
 __device__ __forceinline__ void bessel_k01(double x, double& k0, double& k1) {
   if (x <= 2.0) {
@@ -60,24 +63,24 @@ __device__ __forceinline__ void bessel_k01(double x, double& k0, double& k1) {
     }
     k0 = -(lg + kEulerGamma) * i0 + s0;
     k1 = 1.0 / x + lg * (0.5 * x * i1s) - 0.25 * x * s1;
-  } else if (x <= 30.0) {
+  } else if (x <= 18.5) {
     double s0 = 0.5, s1 = 0.5;
 #pragma unroll 1
-    for (int n = 0; n < 32; ++n) {
+    for (int n = 0; n < 40; ++n) {
       const double cm1 = kCoshM1[n];
       const double e = exp(-x * cm1);
       s0 += e;
       s1 += e * (1.0 + cm1);
       if (x * cm1 > 50.0) break;
     }
-    const double ex = exp(-x) * 0.2;
+    const double ex = exp(-x) * 0.15;
     k0 = s0 * ex;
     k1 = s1 * ex;
   } else {
     const double pre = sqrt(kPi / (2.0 * x)) * exp(-x);
     double a0 = 1.0, a1 = 1.0, t0 = 1.0, t1 = 1.0;
 #pragma unroll 1
-    for (int k = 1; k < 30; ++k) {
+    for (int k = 1; k < 40; ++k) {
       const double q = 2.0 * k - 1.0;
       t0 *= (0.0 - q * q) / (k * 8.0 * x);
       t1 *= (4.0 - q * q) / (k * 8.0 * x);

@@ -27,6 +27,11 @@ struct LumiParams {
   double cosk[5], sink[5], wk[5];
   SplineU gaa, brk, ff;
   double q2max, q2clamp;  // Q2max and Q2max - dQ2 (src/UpcCrossSection.cpp:188)
+  // mirror[iy] = iy' with y_iy' = -y_iy to within 8 ulps (or -1): the second
+  // photon of cell (m, y) then has the first photon's energy of cell (m, y'),
+  // k2 = m/2 e^{-y} = m/2 e^{y'}, and reuses that side's fluxes (identical to
+  // ~1e-15).  nullptr disables the reuse.
+  const int* mirror;
 };
 
 // Per-launch statistics of the QAGS flux kernel.
@@ -73,6 +78,33 @@ cudaError_t launch_breakup_points(double gammatarg, double omaxx, double zcon, i
                                   const double* d_b, double* d_out, int n, cudaStream_t st);
 cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, double rho0,
                                   double R, double a, cudaStream_t st);
+
+// fast form (tensor-core contraction), upcg_fast.cu
+int fast_grid_points();
+cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, void* gh, void* gl,
+                          cudaStream_t st);
+// Flux tables of the fast form: scaled K0/K1 on ln x, and Q(w, b) of the
+// form-factor flux on (ln w, ln b) (built by the Hankel product H.J).
+struct FastFluxTables {
+  const double *k1t, *k0t;
+  const double* qt;  // [nw][nb]
+  int nw, nb;
+  double lw0, hw, lb0, hb;
+};
+int flux_table_ktab_n();
+cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
+                              int nq, double* d_H, double* d_J, cudaStream_t st);
+cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
+                                int ncells, int ncells_pad, const double* flux_nodes,
+                                const FastFluxTables* t, void* ah, void* al, float* a2,
+                                double* far_term, cudaStream_t st);
+cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
+                            const float* a2, int ncells_pad, int ncells, int P, float* partial,
+                            unsigned* d_err, cudaStream_t st);
+cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
+                               const float* partial, const double* far_term, double* lumi,
+                               cudaStream_t st);
+cudaError_t contract_selftest(int ncells, int P, uint64_t seed, double* max_rel, double* ms);
 
 // fold + samplers
 struct FoldParams {

@@ -66,7 +66,9 @@ __global__ void __launch_bounds__(256) k_lumi_nodes(LumiParams p, int cell0, dou
   const int side = threadIdx.x >> 7, i = threadIdx.x & 127;
   if (threadIdx.x < 2) cnt[threadIdx.x] = 0;
   __syncthreads();
-  if (i < kNb) {
+  const int iy = cell - (cell / p.ny) * p.ny;
+  const bool mirrored = side == 1 && p.mirror != nullptr && p.mirror[iy] >= 0;
+  if (i < kNb && !mirrored) {
     CellGeom g;
     cell_geom(p, cell, g);
     double b, w;
@@ -107,7 +109,8 @@ __device__ __forceinline__ double ff_integrand(const LumiParams& p, double q, do
 __device__ __forceinline__ double rescale_err(double err, double resabs, double resasc) {
   err = fabs(err);
   if (resasc != 0 && err != 0) {
-    const double scale = pow(200 * err / resasc, 1.5);
+    const double q = 200 * err / resasc;
+    const double scale = q * sqrt(q);  // (200 err / resasc)^1.5
     err = scale < 1 ? resasc * scale : resasc;
   }
   if (resabs > 2.2250738585072014e-308 / (50 * 2.220446049250313e-16)) {
@@ -557,12 +560,16 @@ __global__ void __launch_bounds__(kBandThreads) k_lumi_band(LumiParams p, int ce
   for (int i = tid; i < p.gaa.n - 1; i += kBandThreads) sg[i] = p.gaa.coef[i];
   if (tid < kNb) {
     const double* f = flux + (size_t)blockIdx.x * 2 * kNb;
+    const int iy = cell - (cell / p.ny) * p.ny;
+    const double* f2 = f + kNb;
+    if (p.mirror != nullptr && p.mirror[iy] >= 0)  // side 0 of the mirror cell (same m-row)
+      f2 = flux + ((size_t)blockIdx.x + (p.mirror[iy] - iy)) * 2 * kNb;
     for (int s = 0; s < 2; ++s) {
       double b, w;
       node_b(g.bmin, g.ld[s], tid, b, w);
       sb[s][tid] = b;
       sbf[s][tid] = (float)b;
-      sw[s][tid] = f[s * kNb + tid] * w;  // flux * b * (bh - bl)
+      sw[s][tid] = (s ? f2 : f)[tid] * w;  // flux * b * (bh - bl)
     }
   }
   __syncthreads();

@@ -133,9 +133,10 @@ __device__ __forceinline__ double eval_u(const double4* coef, int n, double h, d
   return spline_eval_smem(s, coef, x);
 }
 
-// prepareGAA (src/UpcCrossSection.cpp:364-414): one CTA of >= 200 threads.
+// prepareGAA (src/UpcCrossSection.cpp:364-414), first part: T_A(b) on 200
+// nodes (Simpson over z) and its natural spline; one CTA of >= 200 threads.
 __global__ void k_gaa(double rho0, double R, double a, double csNN, GaaConsts k,
-                      double4* __restrict__ gaa_coef) {
+                      double4* __restrict__ gaa_coef, double4* __restrict__ ta_coef) {
   constexpr int nb = 200;
   __shared__ double sTA[nb], sG[nb], sc[nb], scp[nb], sdp[nb];
   __shared__ double4 sTAc[nb - 1];
@@ -164,30 +165,55 @@ __global__ void k_gaa(double rho0, double R, double a, double csNN, GaaConsts k,
     sTA[ib] = 2. * (sum * db / 3.);
   }
   __syncthreads();
-  if (threadIdx.x == 0) spline_serial(sTA, nb, db, sc, scp, sdp, sTAc);
+  if (threadIdx.x == 0) {
+    spline_serial(sTA, nb, db, sc, scp, sdp, sTAc);
+    for (int i = 0; i < nb - 1; ++i) ta_coef[i] = sTAc[i];
+  }
+  (void)csNN;
+  (void)k;
+  (void)gaa_coef;
+  (void)sG;
+}
+
+// G_AA(b_ib) = exp(-sigma_NN T_AA(b_ib)): one CTA per b, one thread per s.
+__global__ void __launch_bounds__(256) k_gaa_rows(const double4* __restrict__ ta_coef, double csNN,
+                                                  GaaConsts k, double* __restrict__ gaa_y) {
+  constexpr int nb = 200;
+  __shared__ double4 sTAc[nb - 1];
+  __shared__ double vs[nb];
+  const double bmax = 20.;
+  const double db = bmax / (nb - 1);
+  for (int i = threadIdx.x; i < nb - 1; i += blockDim.x) sTAc[i] = ta_coef[i];
   __syncthreads();
-  if (ib < nb) {
-    const double b = ib * db;
-    double vs[nb];
-    for (int is = 0; is < nb; ++is) {
-      const double s = is * db;
-      double sum_phi = 0;
-      for (int q = 0; q < 5; ++q) {
-        const double r = sqrt(b * b + s * s + 2. * b * s * k.cosk[q]);
-        sum_phi += 2. * kPi * k.wk[q] * eval_u(sTAc, nb, db, r < bmax ? r : bmax);
-      }
-      vs[is] = 2. * s * eval_u(sTAc, nb, db, s < bmax ? s : bmax) * sum_phi;
+  const int ib = blockIdx.x, is = threadIdx.x;
+  const double b = ib * db;
+  if (is < nb) {
+    const double s = is * db;
+    double sum_phi = 0;
+    for (int q = 0; q < 5; ++q) {
+      const double r = sqrt(b * b + s * s + 2. * b * s * k.cosk[q]);
+      sum_phi += 2. * kPi * k.wk[q] * eval_u(sTAc, nb, db, r < bmax ? r : bmax);
     }
+    vs[is] = 2. * s * eval_u(sTAc, nb, db, s < bmax ? s : bmax) * sum_phi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // Simpson weights in the reference's order
     double sum = vs[0] + vs[nb - 1];
     for (int i = 1; i < nb - 1; i += 2) sum += 4. * vs[i];
     for (int i = 2; i < nb - 1; i += 2) sum += 2. * vs[i];
-    sG[ib] = exp(-csNN * (sum * db / 3.));
+    gaa_y[ib] = exp(-csNN * (sum * db / 3.));
   }
+}
+
+__global__ void k_gaa_spline(const double* __restrict__ gaa_y, double4* __restrict__ gaa_coef) {
+  constexpr int nb = 200;
+  __shared__ double sG[nb], sc[nb], scp[nb], sdp[nb];
+  __shared__ double4 co[nb - 1];
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sG[i] = gaa_y[i];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    spline_serial(sG, nb, db, sc, scp, sdp, sTAc);
-    for (int i = 0; i < nb - 1; ++i) gaa_coef[i] = sTAc[i];
-  }
+  if (threadIdx.x == 0) spline_serial(sG, nb, 20. / (nb - 1), sc, scp, sdp, co);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb - 1; i += blockDim.x) gaa_coef[i] = co[i];
 }
 
 // Photo-neutron data of src/UpcCrossSection.cpp:778-851, 1-based (index 0 unused).
@@ -394,7 +420,13 @@ cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, dou
 
 cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaConsts& k,
                        double4* d_coef, cudaStream_t st) {
-  k_gaa<<<1, 256, 0, st>>>(rho0, R, a, csNN, k, d_coef);
+  // d_coef holds 199 G_AA intervals followed by scratch for the T_A spline
+  // (199 intervals) and the 200 G_AA values (the buffer has 2*199+50 double4).
+  double4* ta = d_coef + 199;
+  double* gy = reinterpret_cast<double*>(d_coef + 2 * 199);
+  k_gaa<<<1, 256, 0, st>>>(rho0, R, a, csNN, k, d_coef, ta);
+  k_gaa_rows<<<200, 256, 0, st>>>(ta, csNN, k, gy);
+  k_gaa_spline<<<1, 256, 0, st>>>(gy, d_coef);
   return cudaGetLastError();
 }
 
