@@ -240,8 +240,10 @@ def main():
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
+    n_launch0 = ug.kernel_launches()
     runs = [step(fast, True) for _ in range(args.steps)]
     barrier()
+    n_launch = ug.kernel_launches() - n_launch0
     clk = clocks.stop()
     ms_tab = float(np.mean([r[0] for r in runs]))
     ms_ev = float(np.mean([r[1] for r in runs])) if nev else None
@@ -310,7 +312,7 @@ def main():
                      "frac": achieved / peak, "traffic": None,
                      "note": f"algorithmic 2*cells*P^2 = {alg_flops:.3e} FLOP per table "
                              f"(issued 3x for the hi/lo split); peak = {pk_kind} bf16 burst"},
-        "gpu_launches": None,
+        "gpu_launches": n_launch,
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -164,6 +164,8 @@ int upcg_fast_flux_table(upcg_generator* g, double* out, size_t n, double* grid)
 int upcg_last_timings(const upcg_generator* g, double* ms, size_t n);
 int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_intervals,
                     uint64_t* evals);
+/* kernels launched by the library in this process so far (all handles) */
+int upcg_kernel_launches(uint64_t* n);
 const char* upcg_last_error(void);
 const char* upcg_version(void);
 

@@ -34,7 +34,7 @@ ABI_SYMBOLS = [
     "upcg_two_photon_lumi", "upcg_cs_m", "upcg_generate_events",
     "upcg_generate_events_device", "upcg_generate_event", "upcg_philox",
     "upcg_last_timings", "upcg_qags_stats", "upcg_last_error", "upcg_version",
-    "upcg_selftest_contract", "upcg_fast_flux_table",
+    "upcg_selftest_contract", "upcg_fast_flux_table", "upcg_kernel_launches",
 ]
 
 
@@ -80,6 +80,7 @@ def load_library(path=None):
         "upcg_last_error": [], "upcg_version": [],
         "upcg_selftest_contract": [i, i, u64, dp, dp],
         "upcg_fast_flux_table": [vp, vp, sz, vp],
+        "upcg_kernel_launches": [C.POINTER(u64)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -109,6 +110,14 @@ def selftest_contract(ncells, P, seed=1):
     e, t = C.c_double(), C.c_double()
     _check(L.upcg_selftest_contract(int(ncells), int(P), int(seed), C.byref(e), C.byref(t)))
     return e.value, t.value
+
+
+def kernel_launches():
+    """Kernels the library has launched in this process so far."""
+    L = load_library()
+    n = C.c_uint64()
+    _check(L.upcg_kernel_launches(C.byref(n)))
+    return n.value
 
 
 def philox(seed, counter0, n):

@@ -9,6 +9,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -23,6 +24,12 @@
 #include "upcg_internal.h"
 
 using namespace upcg;
+
+namespace upcg {
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace upcg
 
 namespace {
 
@@ -102,9 +109,29 @@ struct upcg_generator {
   double bu_gammatarg = 0, bu_omaxx = 0, bu_zcon = 0;
   // ---- device state
   cudaStream_t own = nullptr, stream = nullptr;
-  DBuf<double> ff_y, ff_c, brk_y, brk_c, ee, se, lumi, lumi2, cs, ratio, cszm, cszm2, cszm3;
-  DBuf<double> cdf2, cdfz, cdfz2, cdfz3, flux, partial, tot, rho_tmp, gws, pts_a, pts_b, pts_c;
-  DBuf<double4> ff_coef, gaa_coef, brk_coef;
+  DBuf<double> ff_y, ff_c, brk_y, brk_c, lumi, lumi2, cs, ratio, cszm, cszm2, cszm3;
+  DBuf<double> cdf2, cdfz, cdfz2, cdfz3, flux, partial, tot, gws, pts_a, pts_b, pts_c;
+  DBuf<double4> ff_coef, gaa_coef, ta_coef, brk_coef;
+  DBuf<double> gaa_work, bu_tab, cdf_scratch;  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
+  std::vector<double> bu_host;
+  int bu_nt = 0;
+  // side streams of the table set-up and their fork / join events
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  cudaError_t side_streams() {
+    for (int i = 0; i < 2; ++i) {
+      if (!side[i]) {
+        cudaError_t e = cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking);
+        if (e != cudaSuccess) return e;
+      }
+      if (!ev_join[i]) {
+        cudaError_t e = cudaEventCreateWithFlags(&ev_join[i], cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    if (!ev_fork) return cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
+    return cudaSuccess;
+  }
   DBuf<int> ntab, nq, ovf, tile_count, mirror;
   DBuf<unsigned int> work;
   DBuf<QagsStats> stats;
@@ -114,7 +141,8 @@ struct upcg_generator {
   DBuf<EventRecord> evbuf;
   DBuf<uint16_t> fgh, fgl, fah, fal;  // fast form: bf16 hi/lo of G and of the projections
   DBuf<float> fa2, fpart;
-  DBuf<double> ffar, fk1, fk0, fq, fqn, fwn, fH, fJ;
+  DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2;
+  DBuf<float> fs32, fq32;
   DBuf<unsigned> ferr;
   DBuf<int32_t> mbinbuf;
   int brk_n = 0;
@@ -137,6 +165,11 @@ struct upcg_generator {
     set_collision(5020.f, 82, 208);
   }
   ~upcg_generator() {
+    for (int i = 0; i < 2; ++i) {
+      if (side[i]) cudaStreamDestroy(side[i]);
+      if (ev_join[i]) cudaEventDestroy(ev_join[i]);
+    }
+    if (ev_fork) cudaEventDestroy(ev_fork);
     if (own) cudaStreamDestroy(own);
   }
   void set_collision(float s, int z, int aa) {
@@ -310,20 +343,19 @@ void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
   }
 }
 
-// calcWSRho (src/UpcCrossSection.cpp:152-163) on the device: one thread,
-// 200 terms in the reference's order.
-__global__ void k_ws_rho(double R, double a, int A, double* out) {
-  if (threadIdx.x != 0) return;
+// calcWSRho (src/UpcCrossSection.cpp:152-163): a 200-term Simpson sum in the
+// reference's order, on the host (one serial FP64 chain).
+double ws_rho_host(double R, double a, int A) {
   const int nb = 200;
   const double db = 20. / (nb - 1.);
   auto v = [&](int ib) {
     const double r = ib * db;
-    return r * r / (1. + exp((r - R) / a));
+    return r * r / (1. + std::exp((r - R) / a));
   };
   double sum = v(0) + v(nb - 1);
   for (int i = 1; i < nb - 1; i += 2) sum += 4. * v(i);
   for (int i = 2; i < nb - 1; i += 2) sum += 2. * v(i);
-  *out = A / (sum * db / 3.) / 4. / kPi;
+  return A / (sum * db / 3.) / 4. / kPi;
 }
 }  // namespace
 
@@ -331,16 +363,13 @@ int upcg_generator::build_tables() {
   int rc = setup_process();
   if (rc) return rc;
   cudaStream_t s = st();
+  CK(side_streams());
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   cudaEventRecord(t0, s);
   factor = Z * Z * kAlpha / M_PI / M_PI / kHc / kHc;  // src/UpcCrossSection.cpp:120
-  CK(rho_tmp.ensure(1));
-  k_ws_rho<<<1, 32, 0, s>>>(R, a, A, rho_tmp.p);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(&rho0, rho_tmp.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  rho0 = ws_rho_host(R, a, A);
   // sigma_NN (PDG 2016 fit), src/UpcCrossSection.cpp:368-369
   const double ssm = std::pow(sqrts, 2) / std::pow(2 * kMProt + 2.1206, 2);
   csNN = 0.1 * (34.41 + 0.2720 * std::pow(std::log(ssm), 2) + 13.07 * std::pow(ssm, -0.4473) -
@@ -350,15 +379,6 @@ int upcg_generator::build_tables() {
     gk.cosk[q] = std::cos(M_PI * kX10pos[q]);
     gk.wk[q] = kW10pos[q];
   }
-  CK(gaa_coef.ensure(2 * 199 + 50));  // G_AA spline + build scratch (launch_gaa)
-  CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, s));
-  // form factor on 1e6 knots
-  const double dq = (kQ2max - kQ2min) / kNQ2;
-  CK(ff_y.ensure(kNQ2));
-  CK(ff_c.ensure(kNQ2));
-  CK(ff_coef.ensure(kNQ2 - 1));
-  CK(launch_formfac_values(ff_y.p, kNQ2, kQ2min, dq, rho0, R, a, s));
-  CK(build_spline_uniform(ff_y.p, kNQ2, kQ2min, dq, ff_c.p, ff_coef.p, s));
   // breakup: calcBreakupProb's static set-up, per configuration
   bu_gammatarg = 2. * g1 * g1 - 1.;
   bu_omaxx = g1 > 500. ? 1.E10 : 1.E7;
@@ -366,24 +386,49 @@ int upcg_generator::build_tables() {
     const double zp = 82, pi = 3.14159, hbarcmev = 197.3269718;
     bu_zcon = zp / (bu_gammatarg * (pi) * (hbarcmev)) * zp / (bu_gammatarg * (pi) * (hbarcmev)) / 137.04;
   }
-  CK(ee.ensure(kBreakupTabMax));
-  CK(se.ensure(kBreakupTabMax));
+  bu_host.assign(4 * kBreakupTabMax, 0.);
+  bu_nt = breakup_energy_table(bu_gammatarg, bu_host.data(), bu_host.data() + kBreakupTabMax);
+  for (int k = 1; k < bu_nt; ++k) {
+    bu_host[2 * kBreakupTabMax + k] = std::log(bu_host[k]);
+    bu_host[3 * kBreakupTabMax + k] = 1. / bu_host[k];
+  }
+  // three independent chains: G_AA on the handle's stream, the form factor
+  // and the breakup probability on two side streams
+  CK(cudaEventRecord(ev_fork, s));
+  CK(cudaStreamWaitEvent(side[0], ev_fork, 0));
+  CK(cudaStreamWaitEvent(side[1], ev_fork, 0));
+  CK(gaa_coef.ensure(199));
+  CK(ta_coef.ensure(199));
+  CK(gaa_work.ensure(800));
+  CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s));
+  // form factor on 1e6 knots
+  const double dq = (kQ2max - kQ2min) / kNQ2;
+  CK(ff_y.ensure(kNQ2));
+  CK(ff_c.ensure(kNQ2));
+  CK(ff_coef.ensure(kNQ2 - 1));
+  CK(launch_formfac_values(ff_y.p, kNQ2, kQ2min, dq, rho0, R, a, side[0]));
+  CK(build_spline_uniform(ff_y.p, kNQ2, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
+  CK(cudaEventRecord(ev_join[0], side[0]));
+  // breakup probability: knots up to 20 fm + margin (the path evaluates the
+  // spline at min(b, 20))
+  CK(bu_tab.ensure(4 * kBreakupTabMax));
   CK(ntab.ensure(1));
+  CK(cudaMemcpyAsync(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double),
+                     cudaMemcpyHostToDevice, side[1]));
+  CK(cudaMemcpyAsync(ntab.p, &bu_nt, sizeof(int), cudaMemcpyHostToDevice, side[1]));
   const double dbb = (1000. - 1e-6) / 1000000;
-  // knots up to 20 fm + margin: the path evaluates the spline at min(b, 20)
   brk_n = (int)((20. - 1e-6) / dbb) + 257;
   CK(brk_y.ensure(brk_n));
   CK(brk_c.ensure(brk_n));
   CK(brk_coef.ensure(brk_n - 1));
   if (breakupMode > 1) {
-    CK(launch_breakup(bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n, 1e-6, dbb, ee.p, se.p,
-                      ntab.p, brk_y.p, s));
-    CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, s));
-  } else {
-    // calcBreakupProb's energy table is still prepared for the point entry
-    CK(launch_breakup(bu_gammatarg, bu_omaxx, bu_zcon, 2, 1, 1e-6, dbb, ee.p, se.p, ntab.p,
-                      brk_y.p, s));
+    CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
+                             1e-6, dbb, brk_y.p, side[1]));
+    CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1]));
   }
+  CK(cudaEventRecord(ev_join[1], side[1]));
+  CK(cudaStreamWaitEvent(s, ev_join[0], 0));
+  CK(cudaStreamWaitEvent(s, ev_join[1], 0));
   cudaEventRecord(t1, s);
   CK(cudaEventSynchronize(t1));
   float ms = 0;
@@ -454,6 +499,7 @@ int upcg_generator::build_lumi() {
   std::vector<std::pair<int, std::pair<int, int>>> spans;  // (phase, (begin, end))
   const int w0 = mark();
   FastFluxTables ftab{};
+  double c_far = 0.;
   if (fast) {
     const int b = mark();
     CK(launch_fast_G(p, fu0, fh, P, fgh.p, fgl.p, s));
@@ -461,9 +507,9 @@ int upcg_generator::build_lumi() {
     // 160 Gauss-Legendre panels of 16 points on q in [0, 10]
     const int nk = flux_table_ktab_n();
     CK(fk1.ensure(nk));
-    CK(fk0.ensure(nk));
-    ftab.k1t = fk1.p;
-    ftab.k0t = fk0.p;
+    CK(fs32.ensure(nk));
+    ftab.st = fk1.p;
+    ftab.st32 = fs32.p;
     ftab.nw = 512;
     ftab.nb = 256;
     const double ymx = std::max(std::fabs(ymin), std::fabs(ymax));
@@ -486,13 +532,32 @@ int upcg_generator::build_lumi() {
       CK(fqn.ensure(nqn));
       CK(fwn.ensure(nqn));
       CK(fq.ensure((size_t)ftab.nw * ftab.nb));
+      CK(fq32.ensure((size_t)ftab.nw * ftab.nb));
       CK(fH.ensure((size_t)ftab.nw * nqn));
       CK(fJ.ensure((size_t)nqn * ftab.nb));
       CK(cudaMemcpyAsync(fqn.p, qn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(fwn.p, wn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
       ftab.qt = fq.p;
+      ftab.qt32 = fq32.p;
     }
     CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, s));
+    // ln(m/2) per mass row, and the survival kernel beyond b = 20 fm
+    std::vector<double> lnm2(nm);
+    for (int im = 0; im < nm; ++im) lnm2[im] = std::log((p.mmin + p.dm * im) / 2.);
+    CK(flnm2.ensure(nm));
+    CK(cudaMemcpyAsync(flnm2.p, lnm2.data(), nm * sizeof(double), cudaMemcpyHostToDevice, s));
+    double P20 = 1.;
+    if (breakupMode != 1) {
+      const double x20 = 20.;
+      CK(pts_a.ensure(1));
+      CK(pts_c.ensure(1));
+      CK(cudaMemcpyAsync(pts_a.p, &x20, sizeof x20, cudaMemcpyHostToDevice, s));
+      CK(launch_spline_eval(p.brk, pts_a.p, pts_c.p, 1, s));
+      CK(cudaMemcpyAsync(&P20, pts_c.p, sizeof P20, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
+    c_far = 0.;
+    for (int q = 0; q < 5; ++q) c_far += P20 * 1. * p.wk[q];
     spans.push_back({4, {b, mark()}});
   }
   for (int c0 = 0; c0 < ncell; c0 += chunk) {
@@ -526,8 +591,8 @@ int upcg_generator::build_lumi() {
     } else {
       const int ncp = (nc + 127) / 128 * 128;
       b = mark();
-      CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, node_flux ? flux.p : nullptr, &ftab,
-                             fah.p, fal.p, fa2.p, ffar.p, s));
+      CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, flnm2.p, c_far,
+                             node_flux ? flux.p : nullptr, &ftab, fah.p, fal.p, fa2.p, ffar.p, s));
       spans.push_back({4, {b, mark()}});
       b = mark();
       CK(launch_contract(fah.p, fal.p, fgh.p, fgl.p, fa2.p, ncp, nc, P, fpart.p, ferr.p, s));
@@ -572,7 +637,8 @@ int upcg_generator::build_xsec() {
   CK(tot.ensure(1));
   CK(launch_fold(f, lumi.p, usePolarizedCS ? lumi2.p : nullptr, cs.p, ratio.p, partial.p, tot.p, s));
   CK(cdf2.ensure((size_t)ncell + 1));
-  CK(launch_cdf_2d(cs.p, ncell, cdf2.p, nullptr, s));
+  CK(cdf_scratch.ensure(cdf_2d_scratch_doubles(ncell)));
+  CK(launch_cdf_2d(cs.p, ncell, cdf2.p, cdf_scratch.p, s));
   if (!usePolarizedCS) {
     CK(cszm.ensure((size_t)nm * nz));
     CK(launch_cs_zm(f, 0, cszm.p, s));
@@ -680,6 +746,7 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
       return fail(UPCG_ERR_NUMERIC, "no candidate passed the cuts in %lld draws", (long long)dry);
     if (acc >= need) {
       CK(cudaMemsetAsync(total.p + 1, 0xff, sizeof(int64_t), s));
+      note_launch();
       k_find_cut<<<1, 32, 0, s>>>(tile_count.p, tile_off.p, mask.p, tiles, need, total.p + 1);
       CK(cudaGetLastError());
       int64_t cut = -1;
@@ -956,7 +1023,7 @@ int upcg_breakup_prob(upcg_generator* g, const double* b, int mode, double* out,
   if (rc) return rc;
   rc = points_in(g, b, nullptr, n);
   if (rc) return rc;
-  CK(launch_breakup_points(g->bu_gammatarg, g->bu_omaxx, g->bu_zcon, mode, g->ee.p, g->se.p,
+  CK(launch_breakup_points(g->bu_gammatarg, g->bu_omaxx, g->bu_zcon, mode, g->bu_tab.p, g->bu_tab.p + kBreakupTabMax,
                            g->ntab.p, g->pts_a.p, g->pts_c.p, (int)n, g->st()));
   return points_out(g, out, n);
 }
@@ -1133,6 +1200,12 @@ int upcg_selftest_contract(int ncells, int P, uint64_t seed, double* max_rel, do
 }
 
 const char* upcg_last_error(void) { return g_err.c_str(); }
+int upcg_kernel_launches(uint64_t* n) {
+  if (!n) return fail(UPCG_ERR_ARG, "null pointer");
+  *n = launch_count();
+  return UPCG_OK;
+}
+
 const char* upcg_version(void) { return "upcgen-gb300 0.1 (sm_103a)"; }
 
 }  // extern "C"

@@ -395,6 +395,7 @@ cudaError_t launch_events_all(const EventParams& e, const double* d_cdf2, const 
                               const float* d_ptcdf, uint64_t cand0, int64_t n, EventRecord* d_out,
                               uint8_t* d_flag, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  note_launch();
   k_events_all<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, n,
                                                            d_out, d_flag);
   return cudaGetLastError();
@@ -403,6 +404,7 @@ cudaError_t launch_events_all(const EventParams& e, const double* d_cdf2, const 
 cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* d_out,
                                cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  note_launch();
   k_philox_dump<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(seed, c0, n, d_out);
   return cudaGetLastError();
 }
@@ -411,6 +413,7 @@ cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, flo
                                     cudaStream_t st) {
   const size_t smem = sizeof(double) * e.pt_nbins;
   cudaFuncSetAttribute(k_pt_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  note_launch();
   k_pt_tables<<<e.pt_ne, 256, smem, st>>>(e, ff, d_cdf);
   return cudaGetLastError();
 }
@@ -419,6 +422,7 @@ cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, cons
                                 const float* d_ptcdf, uint64_t cand0, int64_t ncand,
                                 uint32_t* d_mask, int* d_tile_count, cudaStream_t st) {
   const int64_t tiles = (ncand + kTile - 1) / kTile;
+  note_launch();
   k_events_flags<<<(unsigned)tiles, kTile, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, ncand,
                                                    d_mask, d_tile_count);
   return cudaGetLastError();
@@ -430,6 +434,7 @@ cudaError_t launch_events_write(const EventParams& e, const double* d_cdf2, cons
                                 int64_t out_base, int64_t nmax, EventRecord* d_out,
                                 int32_t* d_mbin, cudaStream_t st) {
   const int64_t tiles = (ncand + kTile - 1) / kTile;
+  note_launch();
   k_events_write<<<(unsigned)tiles, kTile, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, ncand,
                                                    d_mask, d_tile_off, out_base, nmax, d_out,
                                                    d_mbin);
@@ -438,6 +443,7 @@ cudaError_t launch_events_write(const EventParams& e, const double* d_cdf2, cons
 
 cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
                               cudaStream_t st) {
+  note_launch();
   k_scan_tiles<<<1, 1024, 0, st>>>(d_count, d_off, n, d_total);
   return cudaGetLastError();
 }

@@ -273,20 +273,11 @@ struct FastGrid {
   int P;
   double u0, h, inv_h;  // r_p = exp(u0 + p h)
   double r_near;        // nodes up to here are projected
+  // per-cell constants of the projection, in logs (set by launch_fast_project)
+  const double* lnm2;   // ln(m_im / 2)
+  double ln5ghc1, ln5ghc2, ln5R, lnbmin, ln2R, ln_rnear, lnghc, lnc_pt, lnc_ff;
+  double c_far;         // G where every azimuth has b >= 20 fm: P(20) sum_k w_k
 };
-
-// 4-point Lagrange weights in ln r for node b; returns the first grid index.
-__device__ __forceinline__ int lagrange4(const FastGrid& fg, double b, double w[4]) {
-  const double t = (log(b) - fg.u0) * fg.inv_h;
-  int p0 = (int)floor(t) - 1;
-  p0 = p0 < 0 ? 0 : (p0 > fg.P - 4 ? fg.P - 4 : p0);
-  const double s = t - p0;
-  w[0] = -(s - 1.) * (s - 2.) * (s - 3.) / 6.;
-  w[1] = s * (s - 2.) * (s - 3.) / 2.;
-  w[2] = -s * (s - 1.) * (s - 3.) / 2.;
-  w[3] = s * (s - 1.) * (s - 2.) / 6.;
-  return p0;
-}
 
 // G_pq = sum_k w_k P(min(b,20)) (b<20 ? G_AA(b) : 1), b^2 = r_p^2 + r_q^2 + 2 r_p r_q cos phi_k,
 // in FP64, stored as bf16 hi + bf16 lo.
@@ -318,21 +309,23 @@ __global__ void k_fast_G(LumiParams p, FastGrid fg, __nv_bfloat16* __restrict__ 
 
 // ------------------------------------------------------- flux tables ----
 // Point flux: N = factor k/g^2 (K1(x)^2 + K0(x)^2/g^2), x = b k/(g hc).  The
-// table holds ln(K^2) + 2x (smooth, O(1)) on a uniform grid in ln x; the
-// flux is rebuilt with exp(table - 2x) in FP64.
+// table holds S(ln x) = ln(K1^2 + K0^2/g^2) + 2x (smooth, O(1)) on a uniform
+// grid in ln x, in FP64 and as an FP32 copy; ln N = ln(factor k/g^2) + S - 2x.
 constexpr int kKTabN = 8192;
 constexpr double kKTabU0 = -16.11809565095832;  // ln(1e-7)
 constexpr double kKTabU1 = 5.703782474656201;   // ln(300): beyond it the flux is below 1e-250 and
                                                 // is taken as zero (exp(-2x) underflows near x = 354)
 
-__global__ void k_ktab(double g, double* __restrict__ t1) {
+__global__ void k_ktab(double g, double* __restrict__ t1, float* __restrict__ t32) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kKTabN) return;
   const double h = (kKTabU1 - kKTabU0) / (kKTabN - 1);
   const double x = exp(kKTabU0 + i * h);
   double K0, K1;
   bessel_k01(x, K0, K1);
-  t1[i] = log(K1 * K1 + K0 * K0 / g / g) + 2. * x;
+  const double v = log(K1 * K1 + K0 * K0 / g / g) + 2. * x;
+  t1[i] = v;
+  t32[i] = (float)v;
 }
 
 // Form-factor flux amplitude Q(w, b) = int_0^10 q^2 F(q^2 + w^2/g^2)/(q^2 + w^2/g^2)
@@ -360,10 +353,11 @@ __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, doub
   J[(size_t)n * nb + j] = j1(b * qn[n] / kHc);
 }
 
-// C[M][N] = A[M][K] B[K][N], FP64, 64x64 tiles (M, N multiples of 64, K of 16).
+// C[M][N] = A[M][K] B[K][N], FP64, 64x64 tiles (M, N multiples of 64, K of 16);
+// C32 (optional) receives an FP32 copy.
 __global__ void __launch_bounds__(256) k_dgemm(const double* __restrict__ A,
                                                const double* __restrict__ B, double* __restrict__ C,
-                                               int M, int N, int K) {
+                                               float* __restrict__ C32, int M, int N, int K) {
   __shared__ double sa[16][64 + 1], sb[16][64 + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
@@ -393,10 +387,27 @@ __global__ void __launch_bounds__(256) k_dgemm(const double* __restrict__ A,
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) C[(size_t)(m0 + ty * 4 + i) * N + n0 + tx * 4 + j] = acc[i][j];
+    for (int j = 0; j < 4; ++j) {
+      const size_t o = (size_t)(m0 + ty * 4 + i) * N + n0 + tx * 4 + j;
+      C[o] = acc[i][j];
+      if (C32) C32[o] = (float)acc[i][j];
+    }
 }
 
-// 4-point Lagrange weights at fractional position t of a uniform table of n points.
+// 4-point Lagrange weights at fractional position t of a uniform table of n
+// points (first point p0, clamped so that the stencil stays inside).
+__device__ __forceinline__ int lag4f(float t, int n, float w[4]) {
+  int p0 = (int)floorf(t) - 1;
+  p0 = p0 < 0 ? 0 : (p0 > n - 4 ? n - 4 : p0);
+  const float s = t - (float)p0;
+  const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
+  w[0] = -s1 * s2 * s3 * (1.f / 6.f);
+  w[1] = s * s2 * s3 * 0.5f;
+  w[2] = -s * s1 * s3 * 0.5f;
+  w[3] = s * s1 * s2 * (1.f / 6.f);
+  return p0;
+}
+
 __device__ __forceinline__ int lag4(double t, int n, double w[4]) {
   int p0 = (int)floor(t) - 1;
   p0 = p0 < 0 ? 0 : (p0 > n - 4 ? n - 4 : p0);
@@ -409,158 +420,249 @@ __device__ __forceinline__ int lag4(double t, int n, double w[4]) {
 }
 
 struct FluxTabs {
-  const double *k1t, *k0t;  // point-flux table
-  const double* qt;         // Q[nw][nb]
+  const float* s32;  // S(ln x), kKTabN points
+  const float* q32;  // Q[nw][nb]
   int nw, nb;
   double lw0, hw, lb0, hb;
 };
 
-__device__ __forceinline__ double flux_point_tab(const LumiParams& p, const FluxTabs& ft, double b,
-                                                 double k) {
-  const double g = p.g1;
-  const double x = b * k / g / kHc;
-  if (x > 300.) return 0.;
-  const double h = (kKTabU1 - kKTabU0) / (kKTabN - 1);
-  double w[4];
-  const int i0 = lag4((log(x) - kKTabU0) / h, kKTabN, w);
-  double s1 = 0., s0 = 0.;
-#pragma unroll
-  for (int m = 0; m < 4; ++m) {
-    s1 += w[m] * __ldg(ft.k1t + i0 + m);
-    s0 += w[m] * __ldg(ft.k0t + i0 + m);
-  }
-  return p.factor * k / g / g * (exp(s1 - 2. * x) + exp(s0 - 2. * x) / g / g);
-}
-
-__device__ __forceinline__ double flux_form_tab(const LumiParams& p, const FluxTabs& ft, double b,
-                                                double k, double lnk) {
-  double ww[4], wb[4];
-  const int iw = lag4((lnk - ft.lw0) / ft.hw, ft.nw, ww);
-  const int ib = lag4((log(b) - ft.lb0) / ft.hb, ft.nb, wb);
-  double Q = 0.;
-#pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const double* row = ft.qt + (size_t)(iw + a) * ft.nb + ib;
-    Q += ww[a] * (wb[0] * __ldg(row) + wb[1] * __ldg(row + 1) + wb[2] * __ldg(row + 2) +
-                  wb[3] * __ldg(row + 3));
-  }
-  Q /= p.A;
-  return p.factor * Q * Q / k;
-}
-
-// Per cell: nodes, fluxes, far sums, and the projections A1 (bf16 hi/lo, the
-// GEMM operand) and A2 (FP32, for the epilogue).
+// ------------------------------------------------------------ projection --
+// One CTA per cell.  Per side (photon), everything that decides which
+// formula or which part a node belongs to is taken in FP64 from the
+// reference's own node positions ((bl + bh)/2, src/UpcCrossSection.cpp:
+// 232-262); the per-node work runs in FP32 in log space: ln a_i with
+// a_i = N(b_i, k) b_i (bh - bl)_i.  Each side is normalised by its largest
+// near-node weight, so cells whose luminosity lies far below FP32's range
+// keep full precision; the scale returns in FP64 in k_fast_finish.
 constexpr int kProjThreads = 256;
+
+struct SideC {
+  float lnb0, ld;   // ln b_i = lnb0 + i ld
+  float lnw0;       // ln(b_i (bh - bl)_i) = 2 ln b_i + lnw0
+  float tk0, tkd;   // point-flux table coordinate of node i: tk0 + i tkd
+  float lnxk;       // ln x_i = ln b_i + lnxk
+  float lnc_pt;     // ln(factor k / g^2)
+  float lnc_ff;     // ln(factor / (A^2 k))
+  float tb0, tbd;   // Q-table b coordinate of node i: tb0 + i tbd
+  int n_form;       // nodes 0 .. n_form-1 take the form-factor flux (b <= 2R)
+  int n_near;       // nodes 0 .. n_near-1 lie at b <= r_near
+  int iw;           // Q-table w row of the photon energy
+  float ww[4];
+};
+
+// ln((1 + e^d)/2) - d/2 = ln cosh(d/2), by its Taylor series in z = d/2
+// (|z| <= 0.1 here: the truncation is below 1e-16).  With it the reference's
+// node midpoints b_i = (bl + bh)/2 (src/UpcCrossSection.cpp:236-238) are
+// ln b_i = ln bmin + (i + 1/2) d + ln cosh(d/2) without an FP64 exp, which
+// this part's FP64 pipe (1/64 of the FP32 rate) cannot afford per cell.
+__device__ __forceinline__ double ln_cosh_half(double d) {
+  const double z2 = 0.25 * d * d;
+  // ln cosh z = z^2/2 - z^4/12 + z^6/45 - 17 z^8/2520 + 31 z^10/14175 - 691 z^12/935550
+  double r = -691. / 935550.;
+  r = fma(r, z2, 31. / 14175.);
+  r = fma(r, z2, -17. / 2520.);
+  r = fma(r, z2, 1. / 45.);
+  r = fma(r, z2, -1. / 12.);
+  r = fma(r, z2, 0.5);
+  return r * z2;
+}
+
+// number of nodes i in [0, kNb) with ln b_i = lnb0 + i d <= lnX
+__device__ __forceinline__ int count_le(double lnb0, double d, double lnX) {
+  const double t = floor((lnX - lnb0) / d) + 1.;
+  return t < 0. ? 0 : (t > kNb ? kNb : (int)t);
+}
 
 __global__ void __launch_bounds__(kProjThreads) k_fast_project(
     LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
     const double* __restrict__ flux_nodes, __nv_bfloat16* __restrict__ ah,
     __nv_bfloat16* __restrict__ al, float* __restrict__ a2, double* __restrict__ far_term) {
-  extern __shared__ float sacc[];  // [2][P], rows normalised by the side's largest node weight
-  __shared__ double sa[2][kNb];    // node weights a_i = N(b_i) b_i (bh - bl)_i
-  __shared__ double sb[2][kNb];    // ln b_i
-  __shared__ double sred[6][kProjThreads / 32];
+  __shared__ SideC sc[2];
+  __shared__ float s_an[2][kNb];   // a_i / max near a (near nodes), 0 beyond
+  __shared__ float s_t[2][kNb];    // radial-grid coordinate of near node i
+  __shared__ float s_qk[2][256];   // Q(k_side, b_j) on the table's b grid
+  __shared__ float s_red[3][2][kProjThreads / 32];
+  __shared__ float s_lamax[2];
   const int lc = blockIdx.x;
-  const int cell = cell0 + lc;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int i = tid; i < 2 * fg.P; i += kProjThreads) sacc[i] = 0.f;
-  double s_near[2] = {0., 0.}, s_far[2] = {0., 0.}, amax[2] = {0., 0.};
-  if (lc < ncells && tid < 2 * kNb) {
-    const int side = tid / kNb, i = tid - side * kNb;
-    const int im = cell / p.ny, iy = cell - (cell / p.ny) * p.ny;
-    const double M = p.mmin + p.dm * im, Y = p.ymin + p.dy * iy;
-    const double k = side ? M / 2. * exp(-Y) : M / 2. * exp(Y);
-    const double bmin = p.isPoint ? p.R : 0.05 * p.R;
-    const double bmax = fmax(5. * (side ? p.g2 : p.g1) * kHc / k, 5. * p.R);
-    const double lbmin = log(bmin);
-    const double ld = (log(bmax) - lbmin) / kNb;
-    double b, w, f, lnb;
-    if (flux_nodes) {  // exact node fluxes from the plain node kernels
-      const double bl = bmin * exp(i * ld), bh = bmin * exp((i + 1) * ld);
-      b = (bh + bl) / 2.;
-      w = b * (bh - bl);
-      lnb = log(b);
-      const bool mir = side == 1 && p.mirror != nullptr && p.mirror[iy] >= 0;
-      f = mir ? flux_nodes[((size_t)(lc + p.mirror[iy] - iy) * 2) * kNb + i]
-              : flux_nodes[((size_t)lc * 2 + side) * kNb + i];
-    } else {  // the reference's nodes, fluxes from the tables
-      const double e = expm1(ld);  // bh = bl (1 + e), b = bl (1 + e/2)
-      const double bl = bmin * exp(i * ld);
-      b = bl * (1. + 0.5 * e);
-      w = b * (bl * e);
-      lnb = lbmin + i * ld + log1p(0.5 * e);
-      if (p.isPoint || b > 2. * p.R) {
-        // N = factor k/g^2 (K1^2 + K0^2/g^2) = factor k/g^2 exp(S(ln x) - 2x)
-        const double g = p.g1;
-        const double x = b * k / g / kHc;
-        const double h = (kKTabU1 - kKTabU0) / (kKTabN - 1);
-        double lw[4];
-        const int i0 = lag4((lnb + log(k / g / kHc) - kKTabU0) / h, kKTabN, lw);
-        double sv = 0.;
-#pragma unroll
-        for (int m = 0; m < 4; ++m) sv += lw[m] * __ldg(ft.k1t + i0 + m);
-        f = x > 300. ? 0. : p.factor * k / g / g * exp(sv - 2. * x);
-      } else {
-        f = flux_form_tab(p, ft, b, k, log(k));
-      }
+  const size_t row = (size_t)lc * fg.P;
+  if (lc >= ncells) {  // padding rows of the last 128-cell tile
+    for (int q = tid; q < fg.P; q += kProjThreads) {
+      ah[row + q] = __float2bfloat16(0.f);
+      al[row + q] = __float2bfloat16(0.f);
+      a2[row + q] = 0.f;
     }
-    const double a = f * w;
-    sa[side][i] = a;
-    sb[side][i] = lnb;
-    if (b <= fg.r_near) {
-      s_near[side] = a;
-      amax[side] = fabs(a);
-    } else {
-      s_far[side] = a;
-    }
+    return;
   }
-  // block sums (fixed order) and each side's largest near-node weight: the
-  // rows are normalised by it (bf16 / FP32 share a range that cells with
-  // L ~ 1e-90 would underflow)
-  double v[6] = {s_near[0], s_near[1], s_far[0], s_far[1], amax[0], amax[1]};
-  for (int j = 0; j < 6; ++j) {
-    double x = v[j];
+  const int cell = cell0 + lc;
+  const int im = cell / p.ny, iy = cell - (cell / p.ny) * p.ny;
+  if (tid < 2) {  // side constants: a few FP64 operations, no FP64 exp or log per side
+    const int side = tid;
+    const double Y = p.ymin + p.dy * iy;
+    const double lnk = fg.lnm2[im] + (side ? -Y : Y);  // k = m/2 e^{+-y} (:224-225)
+    // bmax = max(5 g hc / k, 5R) (:229-230); g = g2 for the second photon
+    const double lnbmax = fmax((side ? fg.ln5ghc2 : fg.ln5ghc1) - lnk, fg.ln5R);
+    const double d = (lnbmax - fg.lnbmin) / kNb;
+    const double lnb0 = fg.lnbmin + 0.5 * d + ln_cosh_half(d);
+    const double hK = (kKTabU1 - kKTabU0) / (kKTabN - 1);
+    const double lnxk = lnk - fg.lnghc;  // x = b k / (g1 hc): fluxPoint and the form
+                                         // integrand use g1 (:169, :198)
+    SideC c;
+    c.lnb0 = (float)lnb0;
+    c.ld = (float)d;
+    c.lnw0 = logf(2.f * tanhf(0.5f * (float)d));  // b (bh - bl) = b^2 2 tanh(d/2)
+    c.tk0 = (float)((lnb0 + lnxk - kKTabU0) / hK);
+    c.tkd = (float)(d / hK);
+    c.lnxk = (float)lnxk;
+    c.lnc_pt = (float)(fg.lnc_pt + lnk);
+    c.lnc_ff = (float)(fg.lnc_ff - lnk);
+    c.n_form = p.isPoint ? 0 : count_le(lnb0, d, fg.ln2R);
+    c.n_near = count_le(lnb0, d, fg.ln_rnear);
+    c.tb0 = 0.f;
+    c.tbd = 0.f;
+    c.iw = 0;
+    c.ww[0] = c.ww[1] = c.ww[2] = c.ww[3] = 0.f;
+    if (!p.isPoint && ft.q32) {
+      c.tb0 = (float)((lnb0 - ft.lb0) / ft.hb);
+      c.tbd = (float)(d / ft.hb);
+      double w[4];
+      c.iw = lag4((lnk - ft.lw0) / ft.hw, ft.nw, w);
+      for (int a = 0; a < 4; ++a) c.ww[a] = (float)w[a];
+    }
+    sc[side] = c;
+  }
+  __syncthreads();
+  if (!p.isPoint && ft.q32 && !flux_nodes) {  // the photon energy's Q row
+    for (int j = tid; j < 2 * ft.nb; j += kProjThreads) {
+      const int side = j / ft.nb, jj = j - side * ft.nb;
+      const SideC& c = sc[side];
+      const float* q = ft.q32 + (size_t)c.iw * ft.nb + jj;
+      s_qk[side][jj] = c.ww[0] * __ldg(q) + c.ww[1] * __ldg(q + ft.nb) +
+                       c.ww[2] * __ldg(q + 2 * ft.nb) + c.ww[3] * __ldg(q + 3 * ft.nb);
+    }
+    __syncthreads();
+  }
+  // ln a_i, one node per thread
+  const int side = tid / kNb, i = tid - side * kNb;
+  const bool node = tid < 2 * kNb;
+  float la = -INFINITY;
+  bool near = false;
+  if (node) {
+    const SideC& c = sc[side];
+    const float lnb = fmaf((float)i, c.ld, c.lnb0);
+    near = i < c.n_near;
+    if (flux_nodes) {  // the plain path's node fluxes (QAGS / K0, K1)
+      const bool mir = side == 1 && p.mirror != nullptr && p.mirror[iy] >= 0;
+      const double f = mir ? flux_nodes[((size_t)(lc + p.mirror[iy] - iy) * 2) * kNb + i]
+                           : flux_nodes[((size_t)lc * 2 + side) * kNb + i];
+      if (f > 0.) la = (float)log(f) + 2.f * lnb + c.lnw0;
+    } else if (i >= c.n_form) {  // point flux: ln N = ln(factor k/g^2) + S - 2x
+      const float tk = fmaf((float)i, c.tkd, c.tk0);
+      if (tk <= (float)(kKTabN - 1)) {  // x <= 300; beyond, the flux is taken as zero
+        float w[4];
+        const int i0 = lag4f(tk, kKTabN, w);
+        const float S = w[0] * __ldg(ft.s32 + i0) + w[1] * __ldg(ft.s32 + i0 + 1) +
+                        w[2] * __ldg(ft.s32 + i0 + 2) + w[3] * __ldg(ft.s32 + i0 + 3);
+        const float x = expf(lnb + c.lnxk);
+        la = c.lnc_pt + S - 2.f * x + 2.f * lnb + c.lnw0;
+      }
+    } else {  // form-factor flux: N = factor Q^2 / (A^2 k)
+      float w[4];
+      const int j0 = lag4f(fmaf((float)i, c.tbd, c.tb0), ft.nb, w);
+      const float Q = w[0] * s_qk[side][j0] + w[1] * s_qk[side][j0 + 1] +
+                      w[2] * s_qk[side][j0 + 2] + w[3] * s_qk[side][j0 + 3];
+      if (Q != 0.f) la = c.lnc_ff + 2.f * logf(fabsf(Q)) + 2.f * lnb + c.lnw0;
+    }
+    if (near) s_t[side][i] = (lnb - (float)fg.u0) * (float)fg.inv_h;
+  }
+  // each side's largest near-node ln a
+  {
+    float m0 = (node && near && side == 0) ? la : -INFINITY;
+    float m1 = (node && near && side == 1) ? la : -INFINITY;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const double y = __shfl_xor_sync(0xffffffffu, x, o);
-      x = j < 4 ? x + y : fmax(x, y);
+      m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+      m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
     }
-    if (lane == 0) sred[j][wid] = x;
+    if (lane == 0) {
+      s_red[0][0][wid] = m0;
+      s_red[0][1][wid] = m1;
+    }
+    __syncthreads();
+    if (tid < 2) {
+      float m = -INFINITY;
+      for (int w = 0; w < kProjThreads / 32; ++w) m = fmaxf(m, s_red[0][tid][w]);
+      s_lamax[tid] = m == -INFINITY ? 0.f : m;  // a side without flux: all weights 0
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  double S[6] = {0, 0, 0, 0, 0, 0};
-  for (int j = 0; j < 6; ++j)
-    for (int w = 0; w < kProjThreads / 32; ++w) S[j] = j < 4 ? S[j] + sred[j][w] : fmax(S[j], sred[j][w]);
-  const double sc1 = S[4] > 0. ? S[4] : 1., sc2 = S[5] > 0. ? S[5] : 1.;
-  // scatter the near nodes onto the radial grid (4-point Lagrange in ln r)
-  if (lc < ncells && tid < 2 * kNb) {
-    const int side = tid / kNb, i = tid - side * kNb;
-    const double a = sa[side][i];
-    const double lnb = sb[side][i];
-    if (lnb <= log(fg.r_near)) {
-      double lw[4];
-      const int p0 = lag4((lnb - fg.u0) * fg.inv_h, fg.P, lw);
-      const double an = a / (side ? sc2 : sc1);
+  // normalised weights; near and far sums per side (fixed order)
+  float an = 0.f;
+  if (node) {
+    an = la == -INFINITY ? 0.f : expf(la - s_lamax[side]);
+    s_an[side][i] = near ? an : 0.f;
+  }
+  {
+    float v[4] = {0.f, 0.f, 0.f, 0.f};  // near0, near1, far0, far1
+    if (node) v[(near ? 0 : 2) + side] = an;
 #pragma unroll
-      for (int m = 0; m < 4; ++m) atomicAdd(&sacc[side * fg.P + p0 + m], (float)(an * lw[m]));
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+    if (lane == 0) {
+      s_red[1][0][wid] = v[0];
+      s_red[1][1][wid] = v[1];
+      s_red[2][0][wid] = v[2];
+      s_red[2][1][wid] = v[3];
     }
   }
   __syncthreads();
-  const size_t row = (size_t)lc * fg.P;
-  for (int q = tid; q < fg.P; q += kProjThreads) {
-    const float x = sacc[q];
-    const __nv_bfloat16 hi = __float2bfloat16(x);
-    ah[row + q] = hi;
-    al[row + q] = __float2bfloat16(x - __bfloat162float(hi));
-    a2[row + q] = sacc[fg.P + q];
+  // gather onto the radial grid: A_side[q] = sum_i an_i phi_{q - p0_i}(s_i),
+  // nodes in increasing order (deterministic, no atomics)
+  for (int e = tid; e < 2 * fg.P; e += kProjThreads) {
+    const int sd = e / fg.P, q = e - sd * fg.P;
+    const int nn = sc[sd].n_near;
+    float acc = 0.f;
+    if (nn > 0) {
+      const float t0 = s_t[sd][0];
+      const float r = sc[sd].ld * (float)fg.inv_h;
+      int i0 = (int)floorf(((float)q - 2.f - t0) / r) - 2;
+      i0 = i0 < 0 ? 0 : i0;
+      for (int j = i0; j < nn; ++j) {
+        const float t = s_t[sd][j];
+        int p0 = (int)floorf(t) - 1;
+        p0 = p0 < 0 ? 0 : (p0 > fg.P - 4 ? fg.P - 4 : p0);
+        if (p0 > q) break;
+        const int m = q - p0;
+        if (m > 3) continue;
+        const float s = t - (float)p0;
+        const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
+        const float w = m == 0 ? -s1 * s2 * s3 * (1.f / 6.f)
+                      : m == 1 ? s * s2 * s3 * 0.5f
+                      : m == 2 ? -s * s1 * s3 * 0.5f
+                               : s * s1 * s2 * (1.f / 6.f);
+        acc = fmaf(s_an[sd][j], w, acc);
+      }
+    }
+    if (sd == 0) {
+      const __nv_bfloat16 hi = __float2bfloat16(acc);
+      ah[row + q] = hi;
+      al[row + q] = __float2bfloat16(acc - __bfloat162float(hi));
+    } else {
+      a2[row + q] = acc;
+    }
   }
-  if (tid == 0 && lc < ncells) {
-    const double P20 = p.breakupMode != 1 ? spline_eval(p.brk, 20.) : 1.;
-    double c = 0.;
-    for (int q = 0; q < 5; ++q) c += P20 * 1. * p.wk[q];
-    // c (S1far S2 + S1near S2far); the contraction part is scaled by sc1 sc2
-    far_term[2 * lc] = c * (S[2] * (S[1] + S[3]) + S[0] * S[3]);
-    far_term[2 * lc + 1] = sc1 * sc2;
+  if (tid == 0) {
+    double S[4] = {0., 0., 0., 0.};  // near0, near1, far0, far1
+    for (int w = 0; w < kProjThreads / 32; ++w) {
+      S[0] += s_red[1][0][w];
+      S[1] += s_red[1][1][w];
+      S[2] += s_red[2][0][w];
+      S[3] += s_red[2][1][w];
+    }
+    // G = c wherever one node is far: c (S1far S2 + S1near S2far), normalised
+    far_term[2 * lc] = fg.c_far * (S[2] * (S[1] + S[3]) + S[0] * S[3]);
+    far_term[2 * lc + 1] = (double)s_lamax[0] + (double)s_lamax[1];  // ln of the scale
   }
 }
 
@@ -574,7 +676,7 @@ __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles,
   const double M = p.mmin + p.dm * im;
   double t2 = 0.;
   for (int t = 0; t < ntiles; ++t) t2 += (double)partial[(size_t)lc * ntiles + t];
-  const double s = far_term[2 * lc] + far_term[2 * lc + 1] * t2;
+  const double s = exp(far_term[2 * lc + 1]) * (far_term[2 * lc] + t2);
   lumi[cell] = 2 * kPi * kPi * M * s * p.dm * p.dy;
 }
 
@@ -671,6 +773,7 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
   }
   ContractArgs args{P / BK, ncells, P, P / BN, a2, partial, d_err};
   dim3 grid(ncells_pad / BM, P / BN);
+  note_launch();
   k_contract<<<grid, 192, kContractSmem, st>>>(tAh, tAl, tBh, tBl, args);
   return cudaGetLastError();
 }
@@ -679,19 +782,34 @@ cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, void*
                           cudaStream_t st) {
   FastGrid fg{P, u0, h, 1.0 / h, 250.};
   dim3 grid((P + 255) / 256, P);
+  note_launch();
   k_fast_G<<<grid, 256, 0, st>>>(p, fg, (__nv_bfloat16*)gh, (__nv_bfloat16*)gl);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
-                                int ncells, int ncells_pad, const double* flux_nodes,
-                                const FastFluxTables* t, void* ah, void* al, float* a2,
-                                double* far_term, cudaStream_t st) {
+                                int ncells, int ncells_pad, const double* lnm2, double c_far,
+                                const double* flux_nodes, const FastFluxTables* t, void* ah,
+                                void* al, float* a2, double* far_term, cudaStream_t st) {
   FastGrid fg{P, u0, h, 1.0 / h, 250.};
+  fg.lnm2 = lnm2;
+  fg.ln5ghc1 = std::log(5. * p.g1 * kHc);
+  fg.ln5ghc2 = std::log(5. * p.g2 * kHc);
+  fg.ln5R = std::log(5. * p.R);
+  fg.lnbmin = std::log(p.isPoint ? p.R : 0.05 * p.R);
+  fg.ln2R = std::log(2. * p.R);
+  fg.ln_rnear = std::log(fg.r_near);
+  fg.lnghc = std::log(p.g1 * kHc);
+  fg.lnc_pt = std::log(p.factor / p.g1 / p.g1);
+  fg.lnc_ff = std::log(p.factor / ((double)p.A * p.A));
+  fg.c_far = c_far;
   FluxTabs ft{};
-  if (t) ft = FluxTabs{t->k1t, t->k0t, t->qt, t->nw, t->nb, t->lw0, t->hw, t->lb0, t->hb};
-  const size_t smem = 2 * sizeof(float) * P;
-  k_fast_project<<<ncells_pad, kProjThreads, smem, st>>>(p, fg, ft, cell0, ncells, flux_nodes,
+  if (t) {
+    if (t->nb > 256) return cudaErrorInvalidValue;  // s_qk holds one Q row
+    ft = FluxTabs{t->st32, t->qt32, t->nw, t->nb, t->lw0, t->hw, t->lb0, t->hb};
+  }
+  note_launch();
+  k_fast_project<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, flux_nodes,
                                                         (__nv_bfloat16*)ah, (__nv_bfloat16*)al,
                                                         a2, far_term);
   return cudaGetLastError();
@@ -699,14 +817,18 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
 
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
                               int nq, double* d_H, double* d_J, cudaStream_t st) {
-  k_ktab<<<(kKTabN + 255) / 256, 256, 0, st>>>(p.g1, const_cast<double*>(t->k1t));
+  note_launch();
+  k_ktab<<<(kKTabN + 255) / 256, 256, 0, st>>>(p.g1, t->st, t->st32);
   if (!p.isPoint) {
     dim3 gh((nq + 255) / 256, t->nw);
+    note_launch();
     k_qtab_H<<<gh, 256, 0, st>>>(p, d_qn, d_wn, nq, t->lw0, t->hw, d_H);
     dim3 gj((t->nb + 255) / 256, nq);
+    note_launch();
     k_qtab_J<<<gj, 256, 0, st>>>(d_qn, nq, t->lb0, t->hb, t->nb, d_J);
     dim3 gg(t->nb / 64, t->nw / 64);
-    k_dgemm<<<gg, 256, 0, st>>>(d_H, d_J, const_cast<double*>(t->qt), t->nw, t->nb, nq);
+    note_launch();
+    k_dgemm<<<gg, 256, 0, st>>>(d_H, d_J, t->qt, t->qt32, t->nw, t->nb, nq);
   }
   return cudaGetLastError();
 }
@@ -716,6 +838,7 @@ int flux_table_ktab_n() { return kKTabN; }
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
                                const float* partial, const double* far_term, double* lumi,
                                cudaStream_t st) {
+  note_launch();
   k_fast_finish<<<(ncells + 255) / 256, 256, 0, st>>>(p, cell0, ncells, ntiles, partial, far_term,
                                                       lumi);
   return cudaGetLastError();
@@ -737,8 +860,11 @@ cudaError_t contract_selftest(int ncells, int P, uint64_t seed, double* max_rel,
   cudaMalloc(&err, 4);
   cudaMemset(err, 0, 4);
   const size_t na = (size_t)pad * P, ng = (size_t)P * P;
+  note_launch();
   k_fill_random<<<(unsigned)((na + 255) / 256), 256>>>(ah, al, nullptr, na, seed, 0);
+  note_launch();
   k_fill_random<<<(unsigned)((ng + 255) / 256), 256>>>(gh, gl, nullptr, ng, seed ^ 0x1234, 0);
+  note_launch();
   k_fill_random<<<(unsigned)((na + 255) / 256), 256>>>(nullptr, nullptr, a2, na, seed ^ 0x777, 0);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -750,6 +876,7 @@ cudaError_t contract_selftest(int ncells, int P, uint64_t seed, double* max_rel,
   float t = 0;
   cudaEventElapsedTime(&t, e0, e1);
   *ms = t;
+  note_launch();
   k_contract_ref<<<ncells, 256>>>(ah, al, gh, gl, a2, ncells, P, ref);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   unsigned herr = 0;

@@ -146,41 +146,104 @@ __global__ void k_reduce_total(const double* __restrict__ partial, int n, double
   if (threadIdx.x == 0) *out = red[0] * scale;
 }
 
-// One CTA builds the normalised cumulative sum of n weights (n up to a few 1e6).
-constexpr int kCdfThreads = 1024;
+// Normalised cumulative sum of n weights (gsl_histogram_pdf_init:
+// cdf[0] = 0, cdf[i+1] = cdf[i] + (w_i / mean) / n) as a three-level scan over
+// tiles of kCdfTile weights: tile sums of w -> mean; tile sums of the scaled
+// terms -> exclusive tile offsets; per-tile scan with its offset.  Only the
+// summation order differs from the sequential recurrence (relative 1e-16).
+constexpr int kCdfThreads = 256;
+constexpr int kCdfItems = 4;
+constexpr int kCdfTile = kCdfThreads * kCdfItems;
 
-__global__ void __launch_bounds__(kCdfThreads) k_cdf_2d(const double* __restrict__ w, int64_t n,
-                                                        double* __restrict__ cdf) {
-  __shared__ double red[kCdfThreads];
-  const int t = threadIdx.x;
-  const int64_t chunk = (n + kCdfThreads - 1) / kCdfThreads;
-  const int64_t lo = t * chunk, hi = lo + chunk < n ? lo + chunk : n;
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
   double s = 0.;
-  for (int64_t i = lo; i < hi; ++i) s += w[i];
-  red[t] = s;
+  for (int w = 0; w < kCdfThreads / 32; ++w) s += red[w];
   __syncthreads();
-  for (int st = kCdfThreads / 2; st > 0; st >>= 1) {
-    if (t < st) red[t] += red[t + st];
-    __syncthreads();
+  return s;
+}
+
+// mode 0: tile sums of w; mode 1: tile sums of (w / mean) / n
+__global__ void __launch_bounds__(kCdfThreads) k_cdf_tiles(const double* __restrict__ w, int64_t n,
+                                                          const double* __restrict__ mean, int mode,
+                                                          double* __restrict__ part) {
+  __shared__ double red[kCdfThreads / 32];
+  const int64_t base = (int64_t)blockIdx.x * kCdfTile;
+  const double m = mode ? *mean : 1.;
+  double v = 0.;
+#pragma unroll
+  for (int k = 0; k < kCdfItems; ++k) {
+    const int64_t i = base + (int64_t)threadIdx.x * kCdfItems + k;
+    if (i < n) v += mode ? (w[i] / m) / (double)n : w[i];
   }
-  const double mean = red[0] / (double)n;
-  __syncthreads();
+  const double s = block_sum(v, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// one CTA: mode 0 -> mean = sum(part) / n; mode 1 -> exclusive scan of part
+__global__ void __launch_bounds__(1024) k_cdf_top(double* __restrict__ part, int ntiles, int64_t n,
+                                                  int mode, double* __restrict__ mean) {
+  __shared__ double sh[1024];
+  const int t = threadIdx.x;
+  const int per = (ntiles + 1023) / 1024;
+  const int lo = t * per, hi = lo + per < ntiles ? lo + per : ntiles;
   double loc = 0.;
-  for (int64_t i = lo; i < hi; ++i) loc += (w[i] / mean) / n;
-  red[t] = loc;
+  for (int i = lo; i < hi; ++i) loc += part[i];
+  sh[t] = loc;
   __syncthreads();
-  // inclusive Hillis-Steele scan of the per-thread sums
-  for (int off = 1; off < kCdfThreads; off <<= 1) {
-    const double add = t >= off ? red[t - off] : 0.;
+  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
+    const double add = t >= off ? sh[t - off] : 0.;
     __syncthreads();
-    red[t] += add;
+    sh[t] += add;
     __syncthreads();
   }
-  double run = t > 0 ? red[t - 1] : 0.;
-  if (t == 0) cdf[0] = 0.;
-  for (int64_t i = lo; i < hi; ++i) {
-    run += (w[i] / mean) / n;
-    cdf[i + 1] = run;
+  if (mode == 0) {
+    if (t == 0) *mean = sh[1023] / (double)n;
+    return;
+  }
+  double run = t > 0 ? sh[t - 1] : 0.;
+  for (int i = lo; i < hi; ++i) {
+    const double v = part[i];
+    part[i] = run;
+    run += v;
+  }
+}
+
+__global__ void __launch_bounds__(kCdfThreads) k_cdf_write(const double* __restrict__ w, int64_t n,
+                                                          const double* __restrict__ mean,
+                                                          const double* __restrict__ off,
+                                                          double* __restrict__ cdf) {
+  __shared__ double sh[kCdfThreads];
+  const int t = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * kCdfTile + (int64_t)t * kCdfItems;
+  const double m = *mean;
+  double v[kCdfItems];
+  double loc = 0.;
+#pragma unroll
+  for (int k = 0; k < kCdfItems; ++k) {
+    const int64_t i = base + k;
+    v[k] = i < n ? (w[i] / m) / (double)n : 0.;
+    loc += v[k];
+  }
+  sh[t] = loc;
+  __syncthreads();
+  for (int o = 1; o < kCdfThreads; o <<= 1) {
+    const double add = t >= o ? sh[t - o] : 0.;
+    __syncthreads();
+    sh[t] += add;
+    __syncthreads();
+  }
+  double run = off[blockIdx.x] + (t > 0 ? sh[t - 1] : 0.);
+  if (blockIdx.x == 0 && t == 0) cdf[0] = 0.;
+#pragma unroll
+  for (int k = 0; k < kCdfItems; ++k) {
+    const int64_t i = base + k;
+    run += v[k];
+    if (i < n) cdf[i + 1] = run;
   }
 }
 
@@ -205,6 +268,7 @@ __global__ void k_cdf_rows(const double* __restrict__ w, int rows, int len,
 
 cudaError_t launch_cs_zm(const FoldParams& f, int flag, double* d_out, cudaStream_t st) {
   const int n = f.nm * f.nz;
+  note_launch();
   k_cs_zm<<<(n + 255) / 256, 256, 0, st>>>(f, flag, d_out);
   return cudaGetLastError();
 }
@@ -212,6 +276,7 @@ cudaError_t launch_cs_zm(const FoldParams& f, int flag, double* d_out, cudaStrea
 cudaError_t launch_cs_m_points(const FoldParams& f, const double* d_m, double* d_out, int n,
                                int flag, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  note_launch();
   k_cs_m_pts<<<(n + 255) / 256, 256, 0, st>>>(f, d_m, d_out, n, flag);
   return cudaGetLastError();
 }
@@ -221,20 +286,37 @@ cudaError_t launch_fold(const FoldParams& f, const double* d_lumi, const double*
                         cudaStream_t st) {
   const int n = f.nm * f.ny;
   const int blocks = (n + kFoldThreads - 1) / kFoldThreads;
+  note_launch();
   k_fold<<<blocks, kFoldThreads, 0, st>>>(f, d_lumi, d_lumi2, d_cs, d_ratio, d_partial);
+  note_launch();
   k_reduce_total<<<1, 1024, 0, st>>>(d_partial, blocks, 1e-6, d_tot);
   return cudaGetLastError();
 }
 
+int cdf_2d_scratch_doubles(int64_t n) { return (int)((n + kCdfTile - 1) / kCdfTile) + 2; }
+
 cudaError_t launch_cdf_2d(const double* d_w, int64_t n, double* d_cdf, double* d_scratch,
                           cudaStream_t st) {
-  (void)d_scratch;
-  k_cdf_2d<<<1, kCdfThreads, 0, st>>>(d_w, n, d_cdf);
+  // d_scratch: tile sums | mean (cdf_2d_scratch_doubles(n))
+  const int ntiles = (int)((n + kCdfTile - 1) / kCdfTile);
+  double* part = d_scratch;
+  double* mean = d_scratch + ntiles + 1;
+  note_launch();
+  k_cdf_tiles<<<ntiles, kCdfThreads, 0, st>>>(d_w, n, mean, 0, part);
+  note_launch();
+  k_cdf_top<<<1, 1024, 0, st>>>(part, ntiles, n, 0, mean);
+  note_launch();
+  k_cdf_tiles<<<ntiles, kCdfThreads, 0, st>>>(d_w, n, mean, 1, part);
+  note_launch();
+  k_cdf_top<<<1, 1024, 0, st>>>(part, ntiles, n, 1, mean);
+  note_launch();
+  k_cdf_write<<<ntiles, kCdfThreads, 0, st>>>(d_w, n, mean, part, d_cdf);
   return cudaGetLastError();
 }
 
 cudaError_t launch_cdf_rows(const double* d_w, int rows, int len, double* d_cdf,
                             cudaStream_t st) {
+  note_launch();
   k_cdf_rows<<<(rows + 127) / 128, 128, 0, st>>>(d_w, rows, len, d_cdf);
   return cudaGetLastError();
 }

@@ -42,16 +42,26 @@ struct QagsStats {
   unsigned long long evals;  // integrand evaluations
 };
 
+// Every kernel launch of the library calls note_launch() first; the count
+// (upcg_kernel_launches) lets a caller see how many kernels a call issued.
+void note_launch();
+unsigned long long launch_count();
+
 // tables
 cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
                                  double4* d_coef, cudaStream_t st);
 cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, double rho0,
                                   double R, double a, cudaStream_t st);
+// G_AA spline (199 intervals into d_coef); d_ta_coef: 199 intervals of the
+// T_A spline; d_work: 800 doubles of scratch
 cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaConsts& k,
-                       double4* d_coef, cudaStream_t st);
-cudaError_t launch_breakup(double gammatarg, double omaxx, double zcon, int mode, int n,
-                           double x0, double h, double* d_ee, double* d_se, int* d_ntab,
-                           double* d_out, cudaStream_t st);
+                       double4* d_coef, double4* d_ta_coef, double* d_work, cudaStream_t st);
+// calcBreakupProb's energy / cross-section table (host); returns its length
+int breakup_energy_table(double gammatarg, double* ee, double* se);
+// d_tab = [ee | se | ln ee | 1/ee], each kBreakupTabMax long, nt entries used
+cudaError_t launch_breakup_values(const double* d_tab, int nt, double gammatarg, double omaxx,
+                                  double zcon, int mode, int n, double x0, double h,
+                                  double* d_out, cudaStream_t st);
 cudaError_t launch_spline_eval(const SplineU& s, const double* d_x, double* d_y, int n,
                                cudaStream_t st);
 
@@ -86,18 +96,22 @@ cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, void*
 // Flux tables of the fast form: scaled K0/K1 on ln x, and Q(w, b) of the
 // form-factor flux on (ln w, ln b) (built by the Hankel product H.J).
 struct FastFluxTables {
-  const double *k1t, *k0t;
-  const double* qt;  // [nw][nb]
+  double* st;    // point-flux table S(ln x) (FP64)
+  float* st32;   // its FP32 copy
+  double* qt;    // form-factor flux amplitude Q[nw][nb] (FP64)
+  float* qt32;   // its FP32 copy
   int nw, nb;
   double lw0, hw, lb0, hb;
 };
 int flux_table_ktab_n();
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
                               int nq, double* d_H, double* d_J, cudaStream_t st);
+// lnm2[im] = ln(m_im / 2); c_far = P(20 fm) sum_k w_k, the survival kernel
+// wherever every azimuth has b >= 20 fm
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
-                                int ncells, int ncells_pad, const double* flux_nodes,
-                                const FastFluxTables* t, void* ah, void* al, float* a2,
-                                double* far_term, cudaStream_t st);
+                                int ncells, int ncells_pad, const double* lnm2, double c_far,
+                                const double* flux_nodes, const FastFluxTables* t, void* ah,
+                                void* al, float* a2, double* far_term, cudaStream_t st);
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
                             const float* a2, int ncells_pad, int ncells, int P, float* partial,
                             unsigned* d_err, cudaStream_t st);
@@ -119,6 +133,7 @@ cudaError_t launch_fold(const FoldParams& f, const double* d_lumi, const double*
                         cudaStream_t st);
 cudaError_t launch_cs_m_points(const FoldParams& f, const double* d_m, double* d_out, int n,
                                int flag, cudaStream_t st);
+int cdf_2d_scratch_doubles(int64_t n);
 cudaError_t launch_cdf_2d(const double* d_w, int64_t n, double* d_cdf, double* d_scratch,
                           cudaStream_t st);
 cudaError_t launch_cdf_rows(const double* d_w, int rows, int len, double* d_cdf,

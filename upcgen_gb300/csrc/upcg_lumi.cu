@@ -712,6 +712,7 @@ size_t qags_global_ws_doubles_per_warp() {
 
 cudaError_t launch_lumi_nodes(const LumiParams& p, int cell0, int ncells, double* d_flux,
                               int* d_nq, cudaStream_t st) {
+  note_launch();
   k_lumi_nodes<<<ncells, 256, 0, st>>>(p, cell0, d_flux, d_nq);
   return cudaGetLastError();
 }
@@ -728,6 +729,7 @@ cudaError_t launch_lumi_qags(const LumiParams& p, int cell0, int ncells, double*
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lumi_qags, kQagsWarps * 32, 0);
   const int blocks = sms * (per_sm > 0 ? per_sm : 1);
   cudaMemsetAsync(d_work, 0, sizeof(unsigned int), st);
+  note_launch();
   k_lumi_qags<<<blocks, kQagsWarps * 32, 0, st>>>(p, cell0, ncells, d_flux, d_nq, d_work,
                                                    d_ovf_list, ovf_cap, d_stats);
   return cudaGetLastError();
@@ -741,6 +743,7 @@ cudaError_t launch_lumi_qags_overflow(const LumiParams& p, int cell0, double* d_
   cudaMemsetAsync(d_work, 0, sizeof(unsigned int), st);
   const int threads = 128;
   const int blocks = (gws_warps * 32 + threads - 1) / threads;
+  note_launch();
   k_lumi_qags_overflow<<<blocks, threads, 0, st>>>(p, cell0, d_flux, d_ovf_list, n_ovf, d_work,
                                                    d_stats, d_gws, gws_warps);
   return cudaGetLastError();
@@ -748,6 +751,7 @@ cudaError_t launch_lumi_qags_overflow(const LumiParams& p, int cell0, double* d_
 
 cudaError_t launch_lumi_band(const LumiParams& p, int cell0, int ncells, const double* d_flux,
                              double* d_lumi, double* d_lumi2, cudaStream_t st) {
+  note_launch();
   k_lumi_band<<<ncells, kBandThreads, 0, st>>>(p, cell0, d_flux, d_lumi, d_lumi2);
   return cudaGetLastError();
 }
@@ -757,6 +761,7 @@ cudaError_t launch_flux_points(const LumiParams& p, const double* d_b, const dou
                                cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   if (!form || p.isPoint) {
+    note_launch();
     k_flux_point_pts<<<(n + 255) / 256, 256, 0, st>>>(p, d_b, d_k, d_out, n);
     return cudaGetLastError();
   }
@@ -765,6 +770,7 @@ cudaError_t launch_flux_points(const LumiParams& p, const double* d_b, const dou
   cudaError_t e = cudaMallocAsync((void**)&gws,
                                   qags_global_ws_doubles_per_warp() * sizeof(double) * warps, st);
   if (e != cudaSuccess) return e;
+  note_launch();
   k_flux_form_pts<<<(warps * 32 + 127) / 128, 128, 0, st>>>(p, d_b, d_k, d_out, n, d_stats, gws,
                                                             warps);
   e = cudaGetLastError();
@@ -775,6 +781,7 @@ cudaError_t launch_flux_points(const LumiParams& p, const double* d_b, const dou
 cudaError_t launch_spline_eval(const SplineU& s, const double* d_x, double* d_y, int n,
                                cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  note_launch();
   k_spline_pts<<<(n + 255) / 256, 256, 0, st>>>(s, d_x, d_y, n);
   return cudaGetLastError();
 }

@@ -3,9 +3,9 @@
 //
 // Reference: src/UpcCrossSection.cpp
 //   calcFormFac :436-445, prepareFormFac :447-461     -> k_formfac_values
-//   prepareGAA :364-414                               -> k_gaa
+//   prepareGAA :364-414                               -> k_ta_values, k_gaa_rows
 //   calcBreakupProb :752-1019, prepareBreakupProb :416-434
-//                                                    -> k_breakup_setup, k_breakup_values
+//                                  -> breakup_energy_table (host), k_breakup_values
 //   gsl_interp_cspline (natural) construction          -> k_spline_window, k_spline_coef
 //
 // The spline system is solved in independent windows: every thread solves the
@@ -14,6 +14,8 @@
 // system is diagonally dominant (ratio 2-sqrt(3) per knot on uniform grids),
 // so the padding error is below 1e-27 relative -- the same solution as a
 // global solve in double precision, with ~1e6 knots done in one launch.
+#include <cmath>
+
 #include "upcg_device.cuh"
 #include "upcg_internal.h"
 
@@ -97,82 +99,32 @@ __global__ void k_formfac_values(double* __restrict__ out, int n, double x0, dou
   out[i] = ff;
 }
 
-// Sequential natural spline for the 200-knot tables of prepareGAA, run by
-// one thread on shared-memory arrays.
-__device__ void spline_serial(const double* y, int n, double h, double* c, double* cp,
-                              double* dp, double4* coef) {
-  const int m = n - 2;
-  for (int i = 0; i < m; ++i) {
-    const double xa = i * h, xb = (i + 1) * h, xc = (i + 2) * h;
-    const double h0 = xb - xa, h1 = xc - xb;
-    const double diag = 2.0 * (h0 + h1);
-    const double rhs = 3.0 * ((y[i + 2] - y[i + 1]) / h1 - (y[i + 1] - y[i]) / h0);
-    if (i == 0) {
-      cp[0] = h1 / diag;
-      dp[0] = rhs / diag;
-    } else {
-      const double den = diag - h0 * cp[i - 1];
-      cp[i] = h1 / den;
-      dp[i] = (rhs - h0 * dp[i - 1]) / den;
-    }
-  }
-  c[0] = 0.0;
-  c[n - 1] = 0.0;
-  c[m] = dp[m - 1];
-  for (int i = m - 2; i >= 0; --i) c[i + 1] = dp[i] - cp[i] * c[i + 2];
-  for (int i = 0; i < n - 1; ++i) {
-    const double xl = i * h, xr = (i + 1) * h, hh = xr - xl;
-    const double dy = y[i + 1] - y[i];
-    coef[i] = make_double4(y[i], dy / hh - hh * (c[i + 1] + 2.0 * c[i]) / 3.0, c[i],
-                           (c[i + 1] - c[i]) / (3.0 * hh));
-  }
-}
-
 __device__ __forceinline__ double eval_u(const double4* coef, int n, double h, double x) {
   SplineU s{coef, 0.0, h, 1.0 / h, n};
   return spline_eval_smem(s, coef, x);
 }
 
 // prepareGAA (src/UpcCrossSection.cpp:364-414), first part: T_A(b) on 200
-// nodes (Simpson over z) and its natural spline; one CTA of >= 200 threads.
-__global__ void k_gaa(double rho0, double R, double a, double csNN, GaaConsts k,
-                      double4* __restrict__ gaa_coef, double4* __restrict__ ta_coef) {
+// nodes, Simpson over z; one CTA per b, one thread per z node, the weighted
+// sum taken in the reference's order by one thread.
+__global__ void __launch_bounds__(256) k_ta_values(double rho0, double R, double a,
+                                                   double* __restrict__ ta_y) {
   constexpr int nb = 200;
-  __shared__ double sTA[nb], sG[nb], sc[nb], scp[nb], sdp[nb];
-  __shared__ double4 sTAc[nb - 1];
-  const double bmax = 20.;
-  const double db = bmax / (nb - 1);
-  const int ib = threadIdx.x;
-  if (ib < nb) {
-    const double b = ib * db;
-    double sum = 0, first = 0, last = 0;
-    {
-      double r = sqrt(b * b);
-      first = rho0 / (1 + exp((r - R) / a));
-      const double z = (nb - 1) * db;
-      r = sqrt(b * b + z * z);
-      last = rho0 / (1 + exp((r - R) / a));
-    }
-    sum = first + last;
-    for (int iz = 1; iz < nb - 1; iz += 2) {
-      const double z = iz * db, r = sqrt(b * b + z * z);
-      sum += 4. * (rho0 / (1 + exp((r - R) / a)));
-    }
-    for (int iz = 2; iz < nb - 1; iz += 2) {
-      const double z = iz * db, r = sqrt(b * b + z * z);
-      sum += 2. * (rho0 / (1 + exp((r - R) / a)));
-    }
-    sTA[ib] = 2. * (sum * db / 3.);
+  __shared__ double v[nb];
+  const double db = 20. / (nb - 1);
+  const double b = blockIdx.x * db;
+  const int iz = threadIdx.x;
+  if (iz < nb) {
+    const double z = iz * db, r = sqrt(b * b + z * z);
+    v[iz] = rho0 / (1 + exp((r - R) / a));
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    spline_serial(sTA, nb, db, sc, scp, sdp, sTAc);
-    for (int i = 0; i < nb - 1; ++i) ta_coef[i] = sTAc[i];
+  if (iz == 0) {
+    double sum = v[0] + v[nb - 1];
+    for (int i = 1; i < nb - 1; i += 2) sum += 4. * v[i];
+    for (int i = 2; i < nb - 1; i += 2) sum += 2. * v[i];
+    ta_y[blockIdx.x] = 2. * (sum * db / 3.);
   }
-  (void)csNN;
-  (void)k;
-  (void)gaa_coef;
-  (void)sG;
 }
 
 // G_AA(b_ib) = exp(-sigma_NN T_AA(b_ib)): one CTA per b, one thread per s.
@@ -205,32 +157,21 @@ __global__ void __launch_bounds__(256) k_gaa_rows(const double4* __restrict__ ta
   }
 }
 
-__global__ void k_gaa_spline(const double* __restrict__ gaa_y, double4* __restrict__ gaa_coef) {
-  constexpr int nb = 200;
-  __shared__ double sG[nb], sc[nb], scp[nb], sdp[nb];
-  __shared__ double4 co[nb - 1];
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) sG[i] = gaa_y[i];
-  __syncthreads();
-  if (threadIdx.x == 0) spline_serial(sG, nb, 20. / (nb - 1), sc, scp, sdp, co);
-  __syncthreads();
-  for (int i = threadIdx.x; i < nb - 1; i += blockDim.x) gaa_coef[i] = co[i];
-}
-
 // Photo-neutron data of src/UpcCrossSection.cpp:778-851, 1-based (index 0 unused).
-__constant__ double kE1[23] = {0., 103., 106., 112., 119., 127., 132., 145., 171., 199., 230., 235.,
+const double kE1[23] = {0., 103., 106., 112., 119., 127., 132., 145., 171., 199., 230., 235.,
                                254., 280., 300., 320., 330., 333., 373., 390., 420., 426., 440.};
-__constant__ double kS1[23] = {0., 12.0, 11.5, 12.0, 12.0, 12.0, 15.0, 17.0, 28.0, 33.0,
+const double kS1[23] = {0., 12.0, 11.5, 12.0, 12.0, 12.0, 15.0, 17.0, 28.0, 33.0,
                                52.0, 60.0, 70.0, 76.0, 85.0, 86.0, 89.0, 89.0, 75.0, 76.0, 69.0, 59.0, 61.0};
-__constant__ double kE2[12] = {0., 2000., 3270., 4100., 4810., 6210., 6600.,
+const double kE2[12] = {0., 2000., 3270., 4100., 4810., 6210., 6600.,
                                7790., 8400., 9510., 13600., 16400.};
-__constant__ double kS2[12] = {0., .1266, .1080, .0805, .1017, .0942, .0844, .0841, .0755, .0827,
+const double kS2[12] = {0., .1266, .1080, .0805, .1017, .0942, .0844, .0841, .0755, .0827,
                                .0626, .0740};
-__constant__ double kE3[29] = {0., 26., 28., 30., 32., 34., 36., 38., 40., 44., 46., 48., 50., 52., 55.,
+const double kE3[29] = {0., 26., 28., 30., 32., 34., 36., 38., 40., 44., 46., 48., 50., 52., 55.,
                                57., 62., 64., 66., 69., 72., 74., 76., 79., 82., 86., 92., 98., 103.};
-__constant__ double kS3[29] = {0., 30., 21.5, 22.5, 18.5, 17.5, 15., 14.5, 19., 17.5, 16., 14.,
+const double kS3[29] = {0., 30., 21.5, 22.5, 18.5, 17.5, 15., 14.5, 19., 17.5, 16., 14.,
                                20., 16.5, 17.5, 17., 15.5, 18., 15.5, 15.5, 15., 13.5, 18., 14.5, 15.5, 12.5, 13.,
                                13., 12.};
-__constant__ double kSigt[160] = {
+const double kSigt[160] = {
     0., .4245, .4870, .5269, .4778, .4066, .3341, .2444, .2245, .2005,
     .1783, .1769, .1869, .1940, .2117, .2226, .2327, .2395, .2646, .2790, .2756,
     .2607, .2447, .2211, .2063, .2137, .2088, .2017, .2050, .2015, .2121, .2175,
@@ -246,7 +187,7 @@ __constant__ double kSigt[160] = {
     .1301, .1348, .1294, .1278, .1227, .1218, .1198, .1193, .1342, .1323, .1248,
     .1220, .1139, .1271, .1224, .1347, .1249, .1163, .1362, .1236, .1462, .1356,
     .1198, .1419, .1324, .1288, .1336, .1335, .1266};
-__constant__ double kSigtn[160] = {
+const double kSigtn[160] = {
     0., .3125, .3930, .4401, .4582, .3774, .3329, .2996, .2715, .2165,
     .2297, .1861, .1551, .2020, .2073, .2064, .2193, .2275, .2384, .2150, .2494,
     .2133, .2023, .1969, .1797, .1693, .1642, .1463, .1280, .1555, .1489, .1435,
@@ -260,12 +201,13 @@ __constant__ double kSigtn[160] = {
     .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12,
     .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12, .12};
 
+}  // namespace
+
 // Energy / cross-section table of calcBreakupProb's first-call set-up
-// (src/UpcCrossSection.cpp:893-969); lead values as hard-coded there.
-// One thread: the table is a ~650-entry recurrence.
-__global__ void k_breakup_setup(double gammatarg, double* __restrict__ ee,
-                                double* __restrict__ se, int* __restrict__ n_out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// (src/UpcCrossSection.cpp:893-969); lead values as hard-coded there.  A
+// ~650-entry recurrence: built on the host (a serial FP64 chain is the
+// slowest thing a GPU can run), then copied.
+int breakup_energy_table(double gammatarg, double* ee, double* se) {
   const double zp = 82, ap = 208;
   const double si1 = 640., gg1 = 4.05, o1 = 13.42, o0 = 7.4;
   const double delo = .05;
@@ -286,47 +228,67 @@ __global__ void k_breakup_setup(double gammatarg, double* __restrict__ ee,
   }
   for (int j = 1; j <= 11; j++) { ij++; ee[ij] = kE2[j]; se[ij] = .1 * ap * kS2[j]; }
   const double x = .0677, y = .129, eps = .0808, eta = .4525, em = .94;
-  const double exx = pow(10., .05);
+  const double exx = std::pow(10., .05);
   double s = .002 * em * ee[ij];
   const int ictr = gammatarg > (2. * 150. * 150.) ? 150 : 100;
   for (int j = 1; j <= ictr; j++) {
     ij++;
     s = s * exx;
     ee[ij] = 1000. * .5 * (s - em * em) / em;
-    se[ij] = .1 * .65 * ap * (x * pow(s, eps) + y * pow(s, (-eta)));
+    se[ij] = .1 * .65 * ap * (x * std::pow(s, eps) + y * std::pow(s, (-eta)));
   }
+  ee[0] = se[0] = 0.;
   ee[ij + 1] = 99999999999.;
-  *n_out = ij + 2;
+  se[ij + 1] = 0.;
+  return ij + 2;
 }
+
+namespace {
 
 // calcBreakupProb (src/UpcCrossSection.cpp:972-1018) on b = bmin + i*db.
 // The single-neutron sum p1n of the reference never reaches its result and is
-// not computed.
-__global__ void k_breakup_values(const double* __restrict__ ee_g, const double* __restrict__ se_g,
-                                 const int* __restrict__ n_tab, int n, double x0, double h,
-                                 int mode, double gammatarg, double omaxx, double zcon,
+// not computed.  Per (b, E_k) the A&S K1 needs ln(x/2) and 1/x of
+// x = E_k b / (hc gamma_t): both come from per-energy tables (ln E_k, 1/E_k)
+// and one log and one division per b, so the inner loop is FMAs only.
+__global__ void k_breakup_values(const double* __restrict__ tab, int nt, int n, double x0,
+                                 double h, int mode, double gammatarg, double omaxx, double zcon,
                                  double* __restrict__ out) {
-  extern __shared__ double s_tab[];
-  const int nt = *n_tab;
-  double* see = s_tab;
-  double* sse = s_tab + nt;
-  for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-    see[i] = ee_g[i];
-    sse[i] = se_g[i];
+  extern __shared__ double s_tab[];  // ee | se | ln ee | 1/ee
+  for (int i = threadIdx.x; i < 4 * nt; i += blockDim.x) {
+    const int part = i / nt, j = i - part * nt;
+    s_tab[i] = tab[part * kBreakupTabMax + j];
   }
   __syncthreads();
+  const double* see = s_tab;
+  const double* sse = s_tab + nt;
+  const double* slne = s_tab + 2 * nt;
+  const double* sinv = s_tab + 3 * nt;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double b = x0 + i * h;
   const double hbarcmev = 197.3269718, o0 = 7.4;
+  const double beta = b / ((hbarcmev) * gammatarg);  // x = E beta
+  const double ln_half_beta = log(0.5 * beta);
+  const double inv_beta = 1. / beta;
+  auto k1 = [&](int k) {
+    const double x = see[k] * beta;
+    if (x > 2.) return bessel_k1_as(x);
+    const double y = x * x * 0.25;
+    const double u = x * x * (1. / 14.0625);  // (x / 3.75)^2
+    const double i1 = x * (0.5 + u * (0.87890594 + u * (0.51498869 + u * (0.15084934 +
+                      u * (0.2658733e-1 + u * (0.301532e-2 + u * 0.32411e-3))))));
+    return (slne[k] + ln_half_beta) * i1 +
+           (sinv[k] * inv_beta) * (1. + y * (0.15443144 + y * (-0.67278579 + y * (-0.18156897 +
+           y * (-0.1919402e-1 + y * (-0.110404e-2 + y * (-0.4686e-4)))))));
+  };
   double pxn = 0.;
   const double omax = fmin(omaxx, 4. * gammatarg * (hbarcmev) / b);
   double p = 0.;
   if (!(omax < o0)) {
-    double gk1m = bessel_k1_as(see[1] * b / ((hbarcmev) * gammatarg));
+    double gk1m = k1(1);
     int k = 2;
     while (k < nt && see[k] < omax) {
-      const double gk1 = bessel_k1_as(see[k] * b / ((hbarcmev) * gammatarg));
+      const double gk1 = k1(k);
       pxn = pxn + zcon * (see[k] - see[k - 1]) * .5 *
                       (sse[k - 1] * see[k - 1] * gk1m * gk1m + sse[k] * see[k] * gk1 * gk1);
       k = k + 1;
@@ -390,6 +352,7 @@ cudaError_t launch_breakup_points(double gammatarg, double omaxx, double zcon, i
                                   const double* d_ee, const double* d_se, const int* d_ntab,
                                   const double* d_b, double* d_out, int n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  note_launch();
   k_breakup_pts<<<(n + 127) / 128, 128, 0, st>>>(d_ee, d_se, d_ntab, d_b, n, mode, gammatarg,
                                                  omaxx, zcon, d_out);
   return cudaGetLastError();
@@ -398,6 +361,7 @@ cudaError_t launch_breakup_points(double gammatarg, double omaxx, double zcon, i
 cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, double rho0,
                                   double R, double a, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  note_launch();
   k_formfac_pts<<<(n + 255) / 256, 256, 0, st>>>(d_q2, d_out, n, rho0, R, a);
   return cudaGetLastError();
 }
@@ -406,37 +370,55 @@ cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, 
                                  double4* d_coef, cudaStream_t st) {
   const int nthreads = (n - 2 + kWinOut - 1) / kWinOut;
   const int tb = 128;
+  note_launch();
   k_spline_window<<<(nthreads + tb - 1) / tb > 0 ? (nthreads + tb - 1) / tb : 1, tb, 0, st>>>(
       d_y, n, x0, h, d_c);
+  note_launch();
   k_spline_coef<<<(n - 1 + 255) / 256, 256, 0, st>>>(d_y, d_c, n, x0, h, d_coef);
   return cudaGetLastError();
 }
 
 cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, double rho0,
                                   double R, double a, cudaStream_t st) {
+  note_launch();
   k_formfac_values<<<(n + 255) / 256, 256, 0, st>>>(d_out, n, x0, h, rho0, R, a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaConsts& k,
-                       double4* d_coef, cudaStream_t st) {
-  // d_coef holds 199 G_AA intervals followed by scratch for the T_A spline
-  // (199 intervals) and the 200 G_AA values (the buffer has 2*199+50 double4).
-  double4* ta = d_coef + 199;
-  double* gy = reinterpret_cast<double*>(d_coef + 2 * 199);
-  k_gaa<<<1, 256, 0, st>>>(rho0, R, a, csNN, k, d_coef, ta);
-  k_gaa_rows<<<200, 256, 0, st>>>(ta, csNN, k, gy);
-  k_gaa_spline<<<1, 256, 0, st>>>(gy, d_coef);
-  return cudaGetLastError();
+                       double4* d_coef, double4* d_ta_coef, double* d_work, cudaStream_t st) {
+  // d_work: T_A values | T_A spline scratch | G_AA values | G_AA spline scratch (200 each)
+  constexpr int nb = 200;
+  const double db = 20. / (nb - 1);
+  double* ta_y = d_work;
+  double* ta_c = d_work + nb;
+  double* g_y = d_work + 2 * nb;
+  double* g_c = d_work + 3 * nb;
+  note_launch();
+  k_ta_values<<<nb, 256, 0, st>>>(rho0, R, a, ta_y);
+  cudaError_t e = build_spline_uniform(ta_y, nb, 0., db, ta_c, d_ta_coef, st);
+  if (e != cudaSuccess) return e;
+  note_launch();
+  k_gaa_rows<<<nb, 256, 0, st>>>(d_ta_coef, csNN, k, g_y);
+  return build_spline_uniform(g_y, nb, 0., db, g_c, d_coef, st);
 }
 
-cudaError_t launch_breakup(double gammatarg, double omaxx, double zcon, int mode, int n,
-                           double x0, double h, double* d_ee, double* d_se, int* d_ntab,
-                           double* d_out, cudaStream_t st) {
-  k_breakup_setup<<<1, 32, 0, st>>>(gammatarg, d_ee, d_se, d_ntab);
-  const size_t smem = 2 * sizeof(double) * kBreakupTabMax;
-  k_breakup_values<<<(n + 127) / 128, 128, smem, st>>>(d_ee, d_se, d_ntab, n, x0, h, mode,
-                                                        gammatarg, omaxx, zcon, d_out);
+cudaError_t launch_breakup_values(const double* d_tab, int nt, double gammatarg, double omaxx,
+                                  double zcon, int mode, int n, double x0, double h,
+                                  double* d_out, cudaStream_t st) {
+  if (nt > kBreakupTabMax) return cudaErrorInvalidValue;
+  const size_t smem = 4 * sizeof(double) * nt;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_breakup_values,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(4 * sizeof(double) * kBreakupTabMax));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  note_launch();
+  k_breakup_values<<<(n + 127) / 128, 128, smem, st>>>(d_tab, nt, n, x0, h, mode, gammatarg,
+                                                        omaxx, zcon, d_out);
   return cudaGetLastError();
 }
 
