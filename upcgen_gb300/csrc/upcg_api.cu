@@ -141,8 +141,9 @@ struct upcg_generator {
   DBuf<EventRecord> evbuf;
   DBuf<uint16_t> fgh, fgl, fah, fal;  // fast form: bf16 hi/lo of G and of the projections
   DBuf<float> fa2, fpart;
-  DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2;
+  DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq;
   DBuf<float> fs32, fq32;
+  DBuf<float4> fgaa32, fbrk32;
   DBuf<unsigned> ferr;
   DBuf<int32_t> mbinbuf;
   int brk_n = 0;
@@ -502,7 +503,20 @@ int upcg_generator::build_lumi() {
   double c_far = 0.;
   if (fast) {
     const int b = mark();
-    CK(launch_fast_G(p, fu0, fh, P, fgh.p, fgl.p, s));
+    // the breakup probability at 20 fm: the survival kernel beyond b = 20 fm
+    double P20 = 1.;
+    if (breakupMode != 1) {
+      const double x20 = 20.;
+      CK(pts_a.ensure(1));
+      CK(pts_c.ensure(1));
+      CK(cudaMemcpyAsync(pts_a.p, &x20, sizeof x20, cudaMemcpyHostToDevice, s));
+      CK(launch_spline_eval(p.brk, pts_a.p, pts_c.p, 1, s));
+      CK(cudaMemcpyAsync(&P20, pts_c.p, sizeof P20, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
+    CK(fgaa32.ensure(p.gaa.n));
+    CK(fbrk32.ensure(breakupMode != 1 ? p.brk.n : 1));
+    CK(launch_fast_G(p, fu0, fh, P, P20, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s));
     // flux tables: K0/K1 on ln x; Q(w, b) on 512 x 256 (ln w, ln b) points by
     // 160 Gauss-Legendre panels of 16 points on q in [0, 10]
     const int nk = flux_table_ktab_n();
@@ -540,22 +554,13 @@ int upcg_generator::build_lumi() {
       ftab.qt = fq.p;
       ftab.qt32 = fq32.p;
     }
-    CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, s));
+    if (!isPoint) CK(fpartq.ensure(flux_table_part_doubles(ftab.nw, ftab.nb)));
+    CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, s));
     // ln(m/2) per mass row, and the survival kernel beyond b = 20 fm
     std::vector<double> lnm2(nm);
     for (int im = 0; im < nm; ++im) lnm2[im] = std::log((p.mmin + p.dm * im) / 2.);
     CK(flnm2.ensure(nm));
     CK(cudaMemcpyAsync(flnm2.p, lnm2.data(), nm * sizeof(double), cudaMemcpyHostToDevice, s));
-    double P20 = 1.;
-    if (breakupMode != 1) {
-      const double x20 = 20.;
-      CK(pts_a.ensure(1));
-      CK(pts_c.ensure(1));
-      CK(cudaMemcpyAsync(pts_a.p, &x20, sizeof x20, cudaMemcpyHostToDevice, s));
-      CK(launch_spline_eval(p.brk, pts_a.p, pts_c.p, 1, s));
-      CK(cudaMemcpyAsync(&P20, pts_c.p, sizeof P20, cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-    }
     c_far = 0.;
     for (int q = 0; q < 5; ++q) c_far += P20 * 1. * p.wk[q];
     spans.push_back({4, {b, mark()}});

@@ -344,11 +344,35 @@ __global__ void k_pt_tables(EventParams e, SplineU ff, float* __restrict__ out) 
     sd[b] = (f * f) * pt * pt * pt / (pi2x4 * arg * arg);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {  // sequential cumulative sum in FP64 (5000 terms)
-    double s = 0.;
-    for (int b = 0; b < nb; ++b) {
-      s += sd[b];
-      sd[b] = s;
+  {  // cumulative sum in FP64: contiguous runs per thread, block scan of the run sums
+    __shared__ double sw[32];
+    const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, wid = t >> 5;
+    const int per = (nb + nt - 1) / nt;
+    const int lo = t * per, hi = lo + per < nb ? lo + per : nb;
+    double run = 0.;
+    for (int b = lo; b < hi; ++b) run += sd[b];
+    double incl = run;  // inclusive scan of the run sums: warps, then warp totals
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) sw[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      double v = lane < nt / 32 ? sw[lane] : 0.;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+      }
+      sw[lane] = v;
+    }
+    __syncthreads();
+    double acc = (wid > 0 ? sw[wid - 1] : 0.) + incl - run;
+    for (int b = lo; b < hi; ++b) {
+      acc += sd[b];
+      sd[b] = acc;
     }
   }
   __syncthreads();

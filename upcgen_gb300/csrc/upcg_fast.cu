@@ -279,32 +279,68 @@ struct FastGrid {
   double c_far;         // G where every azimuth has b >= 20 fm: P(20) sum_k w_k
 };
 
-// G_pq = sum_k w_k P(min(b,20)) (b<20 ? G_AA(b) : 1), b^2 = r_p^2 + r_q^2 + 2 r_p r_q cos phi_k,
-// in FP64, stored as bf16 hi + bf16 lo.
-__global__ void k_fast_G(LumiParams p, FastGrid fg, __nv_bfloat16* __restrict__ gh,
+// FP32 copy of a uniform-knot spline (coefficients {y, b, c, d} per interval)
+struct SplineF {
+  const float4* coef;
+  float x0, h, inv_h;
+  int n;
+};
+
+__device__ __forceinline__ float spline_eval_f(const SplineF& s, const float4* coef, float x) {
+  int i = (int)floorf((x - s.x0) * s.inv_h);
+  i = i < 0 ? 0 : (i > s.n - 2 ? s.n - 2 : i);
+  float xi = s.x0 + i * s.h;
+  if (x < xi && i > 0) {
+    --i;
+    xi = s.x0 + i * s.h;
+  }
+  const float4 c = coef[i];
+  const float d = x - xi;
+  return c.x + d * (c.y + d * (c.z + d * c.w));
+}
+
+__global__ void k_coef_f32(const double4* __restrict__ in, float4* __restrict__ out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4 c = in[i];
+  out[i] = make_float4((float)c.x, (float)c.y, (float)c.z, (float)c.w);
+}
+
+struct GParams {
+  SplineF gaa, brk;
+  int has_brk;
+  float P20, cosk[5], wk[5];
+  float u0, h;
+};
+
+// G_pq = sum_k w_k P(min(b,20)) (b<20 ? G_AA(b) : 1), b^2 = r_p^2 + r_q^2 +
+// 2 r_p r_q cos phi_k (the azimuthal sum of src/UpcCrossSection.cpp:250-262)
+// in FP32 -- the bf16 hi/lo pair it is stored as keeps 2^-16 of it.
+__global__ void k_fast_G(GParams gp, int P, __nv_bfloat16* __restrict__ gh,
                          __nv_bfloat16* __restrict__ gl) {
-  __shared__ double4 sg[200];
-  for (int i = threadIdx.x; i < p.gaa.n - 1; i += blockDim.x) sg[i] = p.gaa.coef[i];
+  __shared__ float4 sg[200];
+  for (int i = threadIdx.x; i < gp.gaa.n - 1 && i < 200; i += blockDim.x) sg[i] = gp.gaa.coef[i];
   __syncthreads();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int pp = blockIdx.y;
-  if (q >= fg.P) return;
-  const double rp = exp(fg.u0 + pp * fg.h), rq = exp(fg.u0 + q * fg.h);
-  const double P20 = p.breakupMode != 1 ? spline_eval(p.brk, 20.) : 1.;
-  double g = 0.;
+  if (q >= P) return;
+  const float rp = expf(gp.u0 + pp * gp.h), rq = expf(gp.u0 + q * gp.h);
+  float g = 0.f;
+#pragma unroll
   for (int k = 0; k < 5; ++k) {
-    const double bsq = rp * rp + rq * rq + 2. * rp * rq * p.cosk[k];
-    double v = P20;
-    if (bsq < 400.) {
-      const double b = sqrt(bsq);
-      if (b < 20.) v = (p.breakupMode != 1 ? spline_eval(p.brk, b) : 1.) * spline_eval_smem(p.gaa, sg, b);
+    const float bsq = rp * rp + rq * rq + 2.f * rp * rq * gp.cosk[k];
+    float v = gp.P20;
+    if (bsq < 400.f) {
+      const float b = sqrtf(bsq);
+      if (b < 20.f)
+        v = (gp.has_brk ? spline_eval_f(gp.brk, gp.brk.coef, b) : 1.f) * spline_eval_f(gp.gaa, sg, b);
     }
-    g += v * p.wk[k];
+    g += v * gp.wk[k];
   }
-  const __nv_bfloat16 hi = __double2bfloat16(g);
-  const __nv_bfloat16 lo = __double2bfloat16(g - (double)__bfloat162float(hi));
-  gh[(size_t)pp * fg.P + q] = hi;
-  gl[(size_t)pp * fg.P + q] = lo;
+  const __nv_bfloat16 hi = __float2bfloat16(g);
+  const __nv_bfloat16 lo = __float2bfloat16(g - __bfloat162float(hi));
+  gh[(size_t)pp * P + q] = hi;
+  gl[(size_t)pp * P + q] = lo;
 }
 
 // ------------------------------------------------------- flux tables ----
@@ -353,16 +389,21 @@ __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, doub
   J[(size_t)n * nb + j] = j1(b * qn[n] / kHc);
 }
 
-// C[M][N] = A[M][K] B[K][N], FP64, 64x64 tiles (M, N multiples of 64, K of 16);
-// C32 (optional) receives an FP32 copy.
+// Split-K FP64 product: Cp[s][M][N] = A[M][Ks] B[Ks][N] over the s-th slice
+// of K (kslice columns; M, N multiples of 64, kslice of 16), 64x64 tiles.
+// The 512 x 256 table is 32 tiles, a fifth of the SMs; the K slices give the
+// rest of the machine work.
 __global__ void __launch_bounds__(256) k_dgemm(const double* __restrict__ A,
-                                               const double* __restrict__ B, double* __restrict__ C,
-                                               float* __restrict__ C32, int M, int N, int K) {
+                                               const double* __restrict__ B,
+                                               double* __restrict__ Cp, int M, int N, int K,
+                                               int kslice) {
   __shared__ double sa[16][64 + 1], sb[16][64 + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  const int kb = blockIdx.z * kslice, ke = kb + kslice;
+  double* C = Cp + (size_t)blockIdx.z * M * N;
   double acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += 16) {
+  for (int k0 = kb; k0 < ke; k0 += 16) {
     for (int e = threadIdx.x; e < 16 * 64; e += 256) {
       const int r = e >> 4, c = e & 15;  // A tile: 64 rows x 16 cols
       sa[c][r] = A[(size_t)(m0 + r) * K + k0 + c];
@@ -387,11 +428,18 @@ __global__ void __launch_bounds__(256) k_dgemm(const double* __restrict__ A,
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const size_t o = (size_t)(m0 + ty * 4 + i) * N + n0 + tx * 4 + j;
-      C[o] = acc[i][j];
-      if (C32) C32[o] = (float)acc[i][j];
-    }
+    for (int j = 0; j < 4; ++j) C[(size_t)(m0 + ty * 4 + i) * N + n0 + tx * 4 + j] = acc[i][j];
+}
+
+// C = sum over the slices in order (FP64), and its FP32 copy
+__global__ void k_dgemm_reduce(const double* __restrict__ Cp, int nslice, size_t mn,
+                               double* __restrict__ C, float* __restrict__ C32) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= mn) return;
+  double v = 0.;
+  for (int z = 0; z < nslice; ++z) v += Cp[(size_t)z * mn + i];
+  C[i] = v;
+  C32[i] = (float)v;
 }
 
 // 4-point Lagrange weights at fractional position t of a uniform table of n
@@ -408,22 +456,11 @@ __device__ __forceinline__ int lag4f(float t, int n, float w[4]) {
   return p0;
 }
 
-__device__ __forceinline__ int lag4(double t, int n, double w[4]) {
-  int p0 = (int)floor(t) - 1;
-  p0 = p0 < 0 ? 0 : (p0 > n - 4 ? n - 4 : p0);
-  const double s = t - p0;
-  w[0] = -(s - 1.) * (s - 2.) * (s - 3.) / 6.;
-  w[1] = s * (s - 2.) * (s - 3.) / 2.;
-  w[2] = -s * (s - 1.) * (s - 3.) / 2.;
-  w[3] = s * (s - 1.) * (s - 2.) / 6.;
-  return p0;
-}
-
 struct FluxTabs {
   const float* s32;  // S(ln x), kKTabN points
   const float* q32;  // Q[nw][nb]
   int nw, nb;
-  double lw0, hw, lb0, hb;
+  double lw0, inv_hw, lb0, inv_hb;
 };
 
 // ------------------------------------------------------------ projection --
@@ -438,6 +475,8 @@ constexpr int kProjThreads = 256;
 
 struct SideC {
   float lnb0, ld;   // ln b_i = lnb0 + i ld
+  float tg0, tgd;   // radial-grid coordinate of node i: tg0 + i tgd
+  float inv_tgd;
   float lnw0;       // ln(b_i (bh - bl)_i) = 2 ln b_i + lnw0
   float tk0, tkd;   // point-flux table coordinate of node i: tk0 + i tkd
   float lnxk;       // ln x_i = ln b_i + lnxk
@@ -465,12 +504,6 @@ __device__ __forceinline__ double ln_cosh_half(double d) {
   r = fma(r, z2, -1. / 12.);
   r = fma(r, z2, 0.5);
   return r * z2;
-}
-
-// number of nodes i in [0, kNb) with ln b_i = lnb0 + i d <= lnX
-__device__ __forceinline__ int count_le(double lnb0, double d, double lnX) {
-  const double t = floor((lnX - lnb0) / d) + 1.;
-  return t < 0. ? 0 : (t > kNb ? kNb : (int)t);
 }
 
 __global__ void __launch_bounds__(kProjThreads) k_fast_project(
@@ -502,32 +535,48 @@ __global__ void __launch_bounds__(kProjThreads) k_fast_project(
     const double lnk = fg.lnm2[im] + (side ? -Y : Y);  // k = m/2 e^{+-y} (:224-225)
     // bmax = max(5 g hc / k, 5R) (:229-230); g = g2 for the second photon
     const double lnbmax = fmax((side ? fg.ln5ghc2 : fg.ln5ghc1) - lnk, fg.ln5R);
-    const double d = (lnbmax - fg.lnbmin) / kNb;
+    const double d = (lnbmax - fg.lnbmin) * (1. / kNb);
+    const double inv_d = 1. / d;  // the one FP64 division per side
     const double lnb0 = fg.lnbmin + 0.5 * d + ln_cosh_half(d);
-    const double hK = (kKTabU1 - kKTabU0) / (kKTabN - 1);
+    constexpr double inv_hK = (kKTabN - 1) / (kKTabU1 - kKTabU0);
     const double lnxk = lnk - fg.lnghc;  // x = b k / (g1 hc): fluxPoint and the form
                                          // integrand use g1 (:169, :198)
     SideC c;
     c.lnb0 = (float)lnb0;
     c.ld = (float)d;
+    c.tg0 = (float)((lnb0 - fg.u0) * fg.inv_h);
+    c.tgd = (float)(d * fg.inv_h);
+    c.inv_tgd = (float)(inv_d * fg.h);
     c.lnw0 = logf(2.f * tanhf(0.5f * (float)d));  // b (bh - bl) = b^2 2 tanh(d/2)
-    c.tk0 = (float)((lnb0 + lnxk - kKTabU0) / hK);
-    c.tkd = (float)(d / hK);
+    c.tk0 = (float)((lnb0 + lnxk - kKTabU0) * inv_hK);
+    c.tkd = (float)(d * inv_hK);
     c.lnxk = (float)lnxk;
     c.lnc_pt = (float)(fg.lnc_pt + lnk);
     c.lnc_ff = (float)(fg.lnc_ff - lnk);
-    c.n_form = p.isPoint ? 0 : count_le(lnb0, d, fg.ln2R);
-    c.n_near = count_le(lnb0, d, fg.ln_rnear);
+    // node counts below 2R and r_near: ln b_i <= ln X for i < floor((ln X - lnb0)/d) + 1
+    auto count_le = [&](double lnX) {
+      const double t = floor((lnX - lnb0) * inv_d) + 1.;
+      return t < 0. ? 0 : (t > kNb ? kNb : (int)t);
+    };
+    c.n_form = p.isPoint ? 0 : count_le(fg.ln2R);
+    c.n_near = count_le(fg.ln_rnear);
     c.tb0 = 0.f;
     c.tbd = 0.f;
     c.iw = 0;
     c.ww[0] = c.ww[1] = c.ww[2] = c.ww[3] = 0.f;
     if (!p.isPoint && ft.q32) {
-      c.tb0 = (float)((lnb0 - ft.lb0) / ft.hb);
-      c.tbd = (float)(d / ft.hb);
-      double w[4];
-      c.iw = lag4((lnk - ft.lw0) / ft.hw, ft.nw, w);
-      for (int a = 0; a < 4; ++a) c.ww[a] = (float)w[a];
+      c.tb0 = (float)((lnb0 - ft.lb0) * ft.inv_hb);
+      c.tbd = (float)(d * ft.inv_hb);
+      const double tw = (lnk - ft.lw0) * ft.inv_hw;
+      int p0 = (int)floor(tw) - 1;
+      p0 = p0 < 0 ? 0 : (p0 > ft.nw - 4 ? ft.nw - 4 : p0);
+      c.iw = p0;
+      const float sw = (float)(tw - p0);
+      const float s1 = sw - 1.f, s2 = sw - 2.f, s3 = sw - 3.f;
+      c.ww[0] = -s1 * s2 * s3 * (1.f / 6.f);
+      c.ww[1] = sw * s2 * s3 * 0.5f;
+      c.ww[2] = -sw * s1 * s3 * 0.5f;
+      c.ww[3] = sw * s1 * s2 * (1.f / 6.f);
     }
     sc[side] = c;
   }
@@ -573,7 +622,7 @@ __global__ void __launch_bounds__(kProjThreads) k_fast_project(
                       w[2] * s_qk[side][j0 + 2] + w[3] * s_qk[side][j0 + 3];
       if (Q != 0.f) la = c.lnc_ff + 2.f * logf(fabsf(Q)) + 2.f * lnb + c.lnw0;
     }
-    if (near) s_t[side][i] = (lnb - (float)fg.u0) * (float)fg.inv_h;
+    if (near) s_t[side][i] = fmaf((float)i, c.tgd, c.tg0);
   }
   // each side's largest near-node ln a
   {
@@ -625,8 +674,7 @@ __global__ void __launch_bounds__(kProjThreads) k_fast_project(
     float acc = 0.f;
     if (nn > 0) {
       const float t0 = s_t[sd][0];
-      const float r = sc[sd].ld * (float)fg.inv_h;
-      int i0 = (int)floorf(((float)q - 2.f - t0) / r) - 2;
+      int i0 = (int)floorf(((float)q - 2.f - t0) * sc[sd].inv_tgd) - 2;
       i0 = i0 < 0 ? 0 : i0;
       for (int j = i0; j < nn; ++j) {
         const float t = s_t[sd][j];
@@ -778,12 +826,29 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
   return cudaGetLastError();
 }
 
-cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, void* gh, void* gl,
-                          cudaStream_t st) {
-  FastGrid fg{P, u0, h, 1.0 / h, 250.};
+cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, double P20,
+                          float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st) {
+  if (p.gaa.n - 1 > 200) return cudaErrorInvalidValue;
+  GParams gp{};
+  note_launch();
+  k_coef_f32<<<(p.gaa.n - 1 + 255) / 256, 256, 0, st>>>(p.gaa.coef, d_gaa32, p.gaa.n - 1);
+  gp.gaa = SplineF{d_gaa32, (float)p.gaa.x0, (float)p.gaa.h, (float)p.gaa.inv_h, p.gaa.n};
+  gp.has_brk = p.breakupMode != 1;
+  if (gp.has_brk) {
+    note_launch();
+    k_coef_f32<<<(p.brk.n - 1 + 255) / 256, 256, 0, st>>>(p.brk.coef, d_brk32, p.brk.n - 1);
+    gp.brk = SplineF{d_brk32, (float)p.brk.x0, (float)p.brk.h, (float)p.brk.inv_h, p.brk.n};
+  }
+  gp.P20 = (float)P20;
+  for (int k = 0; k < 5; ++k) {
+    gp.cosk[k] = (float)p.cosk[k];
+    gp.wk[k] = (float)p.wk[k];
+  }
+  gp.u0 = (float)u0;
+  gp.h = (float)h;
   dim3 grid((P + 255) / 256, P);
   note_launch();
-  k_fast_G<<<grid, 256, 0, st>>>(p, fg, (__nv_bfloat16*)gh, (__nv_bfloat16*)gl);
+  k_fast_G<<<grid, 256, 0, st>>>(gp, P, (__nv_bfloat16*)gh, (__nv_bfloat16*)gl);
   return cudaGetLastError();
 }
 
@@ -806,7 +871,7 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
   FluxTabs ft{};
   if (t) {
     if (t->nb > 256) return cudaErrorInvalidValue;  // s_qk holds one Q row
-    ft = FluxTabs{t->st32, t->qt32, t->nw, t->nb, t->lw0, t->hw, t->lb0, t->hb};
+    ft = FluxTabs{t->st32, t->qt32, t->nw, t->nb, t->lw0, 1. / t->hw, t->lb0, 1. / t->hb};
   }
   note_launch();
   k_fast_project<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, flux_nodes,
@@ -815,8 +880,10 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
   return cudaGetLastError();
 }
 
+int flux_table_part_doubles(int nw, int nb) { return 8 * nw * nb; }
+
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
-                              int nq, double* d_H, double* d_J, cudaStream_t st) {
+                              int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st) {
   note_launch();
   k_ktab<<<(kKTabN + 255) / 256, 256, 0, st>>>(p.g1, t->st, t->st32);
   if (!p.isPoint) {
@@ -826,9 +893,16 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
     dim3 gj((t->nb + 255) / 256, nq);
     note_launch();
     k_qtab_J<<<gj, 256, 0, st>>>(d_qn, nq, t->lb0, t->hb, t->nb, d_J);
-    dim3 gg(t->nb / 64, t->nw / 64);
+    // K = nq split into nq / kslice slices; d_part holds them
+    const int nslice = nq % (8 * 16) == 0 ? 8 : 1;
+    const int kslice = nq / nslice;
+    dim3 gg(t->nb / 64, t->nw / 64, nslice);
     note_launch();
-    k_dgemm<<<gg, 256, 0, st>>>(d_H, d_J, t->qt, t->qt32, t->nw, t->nb, nq);
+    k_dgemm<<<gg, 256, 0, st>>>(d_H, d_J, d_part, t->nw, t->nb, nq, kslice);
+    const size_t mn = (size_t)t->nw * t->nb;
+    note_launch();
+    k_dgemm_reduce<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(d_part, nslice, mn, t->qt,
+                                                                 t->qt32);
   }
   return cudaGetLastError();
 }

@@ -91,8 +91,9 @@ cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, doub
 
 // fast form (tensor-core contraction), upcg_fast.cu
 int fast_grid_points();
-cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, void* gh, void* gl,
-                          cudaStream_t st);
+// d_gaa32 / d_brk32: FP32 copies of the G_AA and breakup splines' intervals
+cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, double P20,
+                          float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st);
 // Flux tables of the fast form: scaled K0/K1 on ln x, and Q(w, b) of the
 // form-factor flux on (ln w, ln b) (built by the Hankel product H.J).
 struct FastFluxTables {
@@ -104,8 +105,10 @@ struct FastFluxTables {
   double lw0, hw, lb0, hb;
 };
 int flux_table_ktab_n();
+// d_part: flux_table_part_doubles(nw, nb) doubles of split-K scratch
+int flux_table_part_doubles(int nw, int nb);
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
-                              int nq, double* d_H, double* d_J, cudaStream_t st);
+                              int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st);
 // lnm2[im] = ln(m_im / 2); c_far = P(20 fm) sum_k w_k, the survival kernel
 // wherever every azimuth has b >= 20 fm
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,

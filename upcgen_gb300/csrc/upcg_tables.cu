@@ -6,14 +6,12 @@
 //   prepareGAA :364-414                               -> k_ta_values, k_gaa_rows
 //   calcBreakupProb :752-1019, prepareBreakupProb :416-434
 //                                  -> breakup_energy_table (host), k_breakup_values
-//   gsl_interp_cspline (natural) construction          -> k_spline_window, k_spline_coef
+//   gsl_interp_cspline (natural) construction          -> k_spline_c, k_spline_coef
 //
-// The spline system is solved in independent windows: every thread solves the
-// natural-spline tridiagonal system on its 32 output knots plus 48 knots of
-// padding on each side, with zero second derivative at the window edges.  The
-// system is diagonally dominant (ratio 2-sqrt(3) per knot on uniform grids),
-// so the padding error is below 1e-27 relative -- the same solution as a
-// global solve in double precision, with ~1e6 knots done in one launch.
+// The natural-spline system on uniform knots is solved by its closed-form
+// inverse kernel (see k_spline_c): one independent dot product per knot, the
+// same solution as a global tridiagonal solve to 1e-16, with 1e6 knots in
+// one launch.
 #include <cmath>
 
 #include "upcg_device.cuh"
@@ -23,64 +21,64 @@ namespace upcg {
 
 namespace {
 
-constexpr int kWinOut = 32;
-constexpr int kWinPad = 48;
-constexpr int kWinMax = kWinOut + 2 * kWinPad;
+// Natural cubic spline on uniform knots x_i = x0 + i h (gsl_interp_cspline).
+// The second-derivative halves c_i solve c_{i-1} + 4 c_i + c_{i+1} = s_i with
+// s_i = 3 (y_{i+1} - 2 y_i + y_{i-1}) / h^2 and c_0 = c_{n-1} = 0.  The
+// inverse of the (1, 4, 1) operator on the infinite lattice is the kernel
+// G_m = (-rho)^|m| / (2 sqrt 3), rho = 2 - sqrt 3, and the natural ends are
+// odd reflections of s about knots 0 and n-1 (they make c vanish there), so
+//   c_i = sum_j (G_{i-j} - G_{i+j} - G_{i-(2(n-1)-j)}) s_j.
+// Terms with |m| > kSplHalf are below rho^27 / (2 sqrt 3) = 8e-17 of the
+// largest and are dropped: every c_i is an independent 55-term FP64 dot
+// product -- no serial recurrence and no division per knot.
+constexpr int kSplHalf = 27;
+constexpr int kSplThreads = 256;
+struct SplKernel {
+  double g[kSplHalf + 1];
+};
 
 __device__ __forceinline__ double knot(double x0, double h, int i) { return x0 + i * h; }
 
-// Natural-spline second-derivative halves c_i on uniform knots x0 + i*h.
-__global__ void k_spline_window(const double* __restrict__ y, int n, double x0, double h,
-                                double* __restrict__ c) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int s = 1 + t * kWinOut;  // first output knot
-  if (s > n - 2) {
-    if (t == 0) { c[0] = 0.0; c[n - 1] = 0.0; }
+__global__ void __launch_bounds__(kSplThreads) k_spline_c(const double* __restrict__ y, int n,
+                                                         double s_scale, SplKernel G,
+                                                         double* __restrict__ c) {
+  __shared__ double ss[kSplThreads + 2 * kSplHalf];
+  const int i0 = blockIdx.x * kSplThreads;
+  // s_j for j in [i0 - half, i0 + 256 + half), zero outside [1, n-2]
+  for (int t = threadIdx.x; t < kSplThreads + 2 * kSplHalf; t += kSplThreads) {
+    const int j = i0 - kSplHalf + t;
+    ss[t] = (j >= 1 && j <= n - 2) ? s_scale * ((y[j + 1] - y[j]) - (y[j] - y[j - 1])) : 0.;
+  }
+  __syncthreads();
+  const int i = i0 + threadIdx.x;
+  if (i >= n) return;
+  if (i == 0 || i == n - 1) {
+    c[i] = 0.;
     return;
   }
-  if (t == 0) { c[0] = 0.0; c[n - 1] = 0.0; }
-  const int e = min(s + kWinOut, n - 1);  // exclusive
-  const int L = max(1, s - kWinPad);
-  const int U = min(n - 2, e - 1 + kWinPad);
-  double cp[kWinMax], dp[kWinMax];
-  double xm = knot(x0, h, L - 1), xc = knot(x0, h, L), xp = knot(x0, h, L + 1);
-  double ym = y[L - 1], yc = y[L], yp = y[L + 1];
-  double h0 = xc - xm, h1 = xp - xc;
-  {
-    const double diag = 2.0 * (h0 + h1);
-    const double rhs = 3.0 * ((yp - yc) / h1 - (yc - ym) / h0);
-    cp[0] = h1 / diag;
-    dp[0] = rhs / diag;
+  const double* sc = ss + threadIdx.x + kSplHalf;  // sc[j - i] = s_j
+  double v = G.g[0] * sc[0];
+#pragma unroll
+  for (int m = 1; m <= kSplHalf; ++m) v += G.g[m] * (sc[-m] + sc[m]);
+  // left image: s_j at distance m = i + j (j >= 1); right image: j = 2(n-1) - i - m
+  for (int m = i + 1; m <= kSplHalf; ++m) v -= G.g[m] * sc[m - 2 * i];
+  for (int m = n - i; m <= kSplHalf; ++m) {
+    const int j = 2 * (n - 1) - i - m;
+    if (j >= 1) v -= G.g[m] * sc[j - i];
   }
-  for (int i = L + 1; i <= U; ++i) {
-    xm = xc; xc = xp; xp = knot(x0, h, i + 1);
-    ym = yc; yc = yp; yp = y[i + 1];
-    h0 = xc - xm; h1 = xp - xc;
-    const double diag = 2.0 * (h0 + h1);
-    const double rhs = 3.0 * ((yp - yc) / h1 - (yc - ym) / h0);
-    const int j = i - L;
-    const double den = diag - h0 * cp[j - 1];
-    cp[j] = h1 / den;
-    dp[j] = (rhs - h0 * dp[j - 1]) / den;
-  }
-  double cn = dp[U - L];
-  if (U < e) c[U] = cn;  // U >= e-1 always; U == e-1 only in the last window
-  for (int i = U - 1; i >= L; --i) {
-    const int j = i - L;
-    cn = dp[j] - cp[j] * cn;
-    if (i >= s && i < e) c[i] = cn;
-  }
+  c[i] = v;
 }
 
-__global__ void k_spline_coef(const double* __restrict__ y, const double* __restrict__ c,
-                              int n, double x0, double h, double4* __restrict__ coef) {
+// {y_i, b_i, c_i, d_i} per interval, as gsl_interp_cspline (the knot spacing
+// is the uniform h; 1/h and h/3 from the host)
+__global__ void k_spline_coef(const double* __restrict__ y, const double* __restrict__ c, int n,
+                              double inv_h, double h3, double inv_3h,
+                              double4* __restrict__ coef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
-  const double xl = knot(x0, h, i), xr = knot(x0, h, i + 1);
-  const double hh = xr - xl;
   const double dy = y[i + 1] - y[i];
-  const double b = dy / hh - hh * (c[i + 1] + 2.0 * c[i]) / 3.0;
-  const double d = (c[i + 1] - c[i]) / (3.0 * hh);
+  const double b = dy * inv_h - h3 * (c[i + 1] + 2.0 * c[i]);
+  const double d = (c[i + 1] - c[i]) * inv_3h;
   coef[i] = make_double4(y[i], b, c[i], d);
 }
 
@@ -250,9 +248,15 @@ namespace {
 // not computed.  Per (b, E_k) the A&S K1 needs ln(x/2) and 1/x of
 // x = E_k b / (hc gamma_t): both come from per-energy tables (ln E_k, 1/E_k)
 // and one log and one division per b, so the inner loop is FMAs only.
-__global__ void k_breakup_values(const double* __restrict__ tab, int nt, int n, double x0,
-                                 double h, int mode, double gammatarg, double omaxx, double zcon,
-                                 double* __restrict__ out) {
+// One warp per b: lane l takes the energies k = 2 + 32 j + l, the
+// trapezoid's left value f_{k-1} comes from the neighbouring lane, and the
+// warp sums its terms at the end (the reference sums them in k order; the
+// difference is rounding).  A thread per b would be a 650-step serial FP64
+// chain, which on this part's narrow FP64 pipe is latency-bound.
+__global__ void __launch_bounds__(256) k_breakup_values(const double* __restrict__ tab, int nt,
+                                                        int n, double x0, double h, int mode,
+                                                        double gammatarg, double omaxx,
+                                                        double zcon, double* __restrict__ out) {
   extern __shared__ double s_tab[];  // ee | se | ln ee | 1/ee
   for (int i = threadIdx.x; i < 4 * nt; i += blockDim.x) {
     const int part = i / nt, j = i - part * nt;
@@ -263,43 +267,56 @@ __global__ void k_breakup_values(const double* __restrict__ tab, int nt, int n, 
   const double* sse = s_tab + nt;
   const double* slne = s_tab + 2 * nt;
   const double* sinv = s_tab + 3 * nt;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= n) return;  // whole warps leave together
   const double b = x0 + i * h;
   const double hbarcmev = 197.3269718, o0 = 7.4;
   const double beta = b / ((hbarcmev) * gammatarg);  // x = E beta
   const double ln_half_beta = log(0.5 * beta);
   const double inv_beta = 1. / beta;
-  auto k1 = [&](int k) {
+  // f_k = se_k ee_k K1(ee_k beta)^2
+  auto f = [&](int k) {
     const double x = see[k] * beta;
-    if (x > 2.) return bessel_k1_as(x);
-    const double y = x * x * 0.25;
-    const double u = x * x * (1. / 14.0625);  // (x / 3.75)^2
-    const double i1 = x * (0.5 + u * (0.87890594 + u * (0.51498869 + u * (0.15084934 +
-                      u * (0.2658733e-1 + u * (0.301532e-2 + u * 0.32411e-3))))));
-    return (slne[k] + ln_half_beta) * i1 +
+    double K1;
+    if (x > 2.) {
+      K1 = bessel_k1_as(x);
+    } else {
+      const double y = x * x * 0.25;
+      const double u = x * x * (1. / 14.0625);  // (x / 3.75)^2
+      const double i1 = x * (0.5 + u * (0.87890594 + u * (0.51498869 + u * (0.15084934 +
+                        u * (0.2658733e-1 + u * (0.301532e-2 + u * 0.32411e-3))))));
+      K1 = (slne[k] + ln_half_beta) * i1 +
            (sinv[k] * inv_beta) * (1. + y * (0.15443144 + y * (-0.67278579 + y * (-0.18156897 +
            y * (-0.1919402e-1 + y * (-0.110404e-2 + y * (-0.4686e-4)))))));
+    }
+    return sse[k] * see[k] * K1 * K1;
   };
-  double pxn = 0.;
   const double omax = fmin(omaxx, 4. * gammatarg * (hbarcmev) / b);
   double p = 0.;
   if (!(omax < o0)) {
-    double gk1m = k1(1);
-    int k = 2;
-    while (k < nt && see[k] < omax) {
-      const double gk1 = k1(k);
-      pxn = pxn + zcon * (see[k] - see[k - 1]) * .5 *
-                      (sse[k - 1] * see[k - 1] * gk1m * gk1m + sse[k] * see[k] * gk1 * gk1);
-      k = k + 1;
-      gk1m = gk1;
+    double part = 0.;
+    double carry = lane == 31 ? f(1) : 0.;  // f_{k-1} of lane 0 in the first round
+    for (int k0 = 2; k0 < nt; k0 += 32) {
+      const int k = k0 + lane;
+      const bool in = k < nt && see[k] < omax;
+      const double fk = in ? f(k) : 0.;
+      double fm = __shfl_up_sync(0xffffffffu, fk, 1);
+      const double c = __shfl_sync(0xffffffffu, carry, 31);
+      if (lane == 0) fm = c;
+      if (in) part += (see[k] - see[k - 1]) * .5 * (fm + fk);
+      carry = fk;
+      if (!__any_sync(0xffffffffu, in)) break;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    const double pxn = zcon * part;
     if (mode == 1) p = 1.;
     if (mode == 2) p = (1 - exp(-1 * pxn)) * (1 - exp(-1 * pxn));
     if (mode == 3) p = exp(-2 * pxn);
     if (mode == 4) p = 2. * exp(-pxn) * (1. - exp(-pxn));
   }
-  out[i] = p;
+  if (lane == 0) out[i] = p;
 }
 
 // calcBreakupProb at arbitrary b (the point entry of the C ABI).
@@ -368,13 +385,24 @@ cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, doub
 
 cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
                                  double4* d_coef, cudaStream_t st) {
-  const int nthreads = (n - 2 + kWinOut - 1) / kWinOut;
-  const int tb = 128;
+  (void)x0;
+  if (n < 2 * kSplHalf + 4) return cudaErrorInvalidValue;  // the two end images must not meet
+  static SplKernel G = [] {
+    SplKernel k{};
+    const double rho = 2. - std::sqrt(3.);
+    double p = 1. / (2. * std::sqrt(3.));
+    for (int m = 0; m <= kSplHalf; ++m) {
+      k.g[m] = p;
+      p *= -rho;
+    }
+    return k;
+  }();
   note_launch();
-  k_spline_window<<<(nthreads + tb - 1) / tb > 0 ? (nthreads + tb - 1) / tb : 1, tb, 0, st>>>(
-      d_y, n, x0, h, d_c);
+  k_spline_c<<<(n + kSplThreads - 1) / kSplThreads, kSplThreads, 0, st>>>(d_y, n, 3. / (h * h), G,
+                                                                         d_c);
   note_launch();
-  k_spline_coef<<<(n - 1 + 255) / 256, 256, 0, st>>>(d_y, d_c, n, x0, h, d_coef);
+  k_spline_coef<<<(n - 1 + 255) / 256, 256, 0, st>>>(d_y, d_c, n, 1. / h, h / 3., 1. / (3. * h),
+                                                     d_coef);
   return cudaGetLastError();
 }
 
@@ -417,8 +445,8 @@ cudaError_t launch_breakup_values(const double* d_tab, int nt, double gammatarg,
     attr = true;
   }
   note_launch();
-  k_breakup_values<<<(n + 127) / 128, 128, smem, st>>>(d_tab, nt, n, x0, h, mode, gammatarg,
-                                                        omaxx, zcon, d_out);
+  k_breakup_values<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, smem, st>>>(
+      d_tab, nt, n, x0, h, mode, gammatarg, omaxx, zcon, d_out);
   return cudaGetLastError();
 }
 
