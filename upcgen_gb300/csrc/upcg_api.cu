@@ -141,9 +141,9 @@ struct upcg_generator {
   DBuf<EventRecord> evbuf;
   DBuf<uint16_t> fgh, fgl, fah, fal;  // fast form: bf16 hi/lo of G and of the projections
   DBuf<float> fa2, fpart;
-  DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq;
+  DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq, fsides;
   DBuf<float> fs32, fq32;
-  DBuf<float4> fgaa32, fbrk32;
+  DBuf<float4> fgaa32, fbrk32, ff32;
   DBuf<unsigned> ferr;
   DBuf<int32_t> mbinbuf;
   int brk_n = 0;
@@ -483,7 +483,8 @@ int upcg_generator::build_lumi() {
     CK(fah.ensure((size_t)chunk_pad * P));
     CK(fal.ensure((size_t)chunk_pad * P));
     CK(fa2.ensure((size_t)chunk_pad * P));
-    CK(ffar.ensure(2 * (size_t)chunk_pad));
+    CK(ffar.ensure(2 * (size_t)chunk_pad));  // one float4 per cell
+    CK(fsides.ensure((2 * (size_t)chunk * fast_side_bytes() + 7) / 8));
     CK(fpart.ensure((size_t)chunk * (P / 256)));
     CK(ferr.ensure(1));
     CK(cudaMemsetAsync(ferr.p, 0, sizeof(unsigned), s));
@@ -597,12 +598,13 @@ int upcg_generator::build_lumi() {
       const int ncp = (nc + 127) / 128 * 128;
       b = mark();
       CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, flnm2.p, c_far,
-                             node_flux ? flux.p : nullptr, &ftab, fah.p, fal.p, fa2.p, ffar.p, s));
+                             node_flux ? flux.p : nullptr, &ftab, fsides.p, fah.p, fal.p, fa2.p,
+                             ffar.p, s));
       spans.push_back({4, {b, mark()}});
       b = mark();
       CK(launch_contract(fah.p, fal.p, fgh.p, fgl.p, fa2.p, ncp, nc, P, fpart.p, ferr.p, s));
       spans.push_back({3, {b, mark()}});
-      CK(launch_fast_finish(p, c0, nc, P / 256, fpart.p, ffar.p, lumi.p, s));
+      CK(launch_fast_finish(p, c0, nc, P / 256, c_far, fpart.p, ffar.p, lumi.p, s));
     }
   }
   const int w1 = mark();
@@ -661,7 +663,8 @@ int upcg_generator::build_xsec() {
   }
   const EventParams e = event_params();
   CK(ptcdf.ensure((size_t)e.pt_ne * (e.pt_nbins + 1)));
-  CK(launch_photon_pt_tables(e, lumi_params().ff, ptcdf.p, s));
+  CK(ff32.ensure(kNQ2));
+  CK(launch_photon_pt_tables(e, lumi_params().ff, ff32.p, ptcdf.p, s));
   CK(cudaMemcpyAsync(&totCS, tot.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   cudaEventRecord(t1, s);
   CK(cudaEventSynchronize(t1));

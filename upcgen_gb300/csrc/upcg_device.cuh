@@ -160,6 +160,29 @@ __device__ __forceinline__ double spline_eval_smem(const SplineU& s, const doubl
   return c.x + d * (c.y + d * (c.z + d * c.w));
 }
 
+// FP32 copy of a uniform-knot spline (coefficients {y, b, c, d} per interval)
+struct SplineF {
+  const float4* coef;
+  float x0, h, inv_h;
+  int n;
+};
+
+__device__ __forceinline__ float spline_eval_f(const SplineF& s, const float4* coef, float x) {
+  int i = (int)floorf((x - s.x0) * s.inv_h);
+  i = i < 0 ? 0 : (i > s.n - 2 ? s.n - 2 : i);
+  float xi = s.x0 + i * s.h;
+  if (x < xi && i > 0) {
+    --i;
+    xi = s.x0 + i * s.h;
+  }
+  const float4 c = coef[i];
+  const float d = x - xi;
+  return c.x + d * (c.y + d * (c.z + d * c.w));
+}
+
+// FP32 copy of n spline intervals
+__global__ void k_coef_f32(const double4* __restrict__ in, float4* __restrict__ out, int n);
+
 // 21-point Gauss-Kronrod rule (Kronrod extension of the 10-point Gauss rule).
 __constant__ static double kXgk[11] = {
     0.995657163025808080735527280689003, 0.973906528517171720077964012084452,

@@ -330,56 +330,59 @@ __global__ void k_scan_tiles(const int* __restrict__ cnt, int64_t* __restrict__ 
 }
 
 // Photon pT spectra: dN/dpT ~ F(pT^2 + e)^2 pT^3 / (pT^2 + e)^2 on 5000 bins of
-// [0, 6 hc / R] (content at the upper bin edge), for e = k^2/gtot^2 on a log grid.
-__global__ void k_pt_tables(EventParams e, SplineU ff, float* __restrict__ out) {
-  extern __shared__ double sd[];
+// [0, 6 hc / R] (content at the upper bin edge), for e = k^2/gtot^2 on a log
+// grid.  FP32 throughout (the tables are FP32), from an FP32 copy of the
+// form-factor spline.
+__global__ void k_pt_tables(EventParams e, SplineF ff, float* __restrict__ out) {
+  extern __shared__ float sdf[];
   const int ie = blockIdx.x;
-  const double ered = exp(e.pt_lne0 + e.pt_dlne * ie);
+  const float ered = expf((float)e.pt_lne0 + (float)e.pt_dlne * ie);
   const int nb = e.pt_nbins;
-  const double pi2x4 = 4 * kPi * kPi;
+  const float inv_pi2x4 = (float)(1. / (4 * kPi * kPi));
+  const float w = (float)e.pt_width;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-    const double pt = e.pt_width * (b + 1);
-    const double arg = pt * pt + ered;
-    const double f = spline_eval(ff, arg);
-    sd[b] = (f * f) * pt * pt * pt / (pi2x4 * arg * arg);
+    const float pt = w * (b + 1);
+    const float arg = pt * pt + ered;
+    const float f = spline_eval_f(ff, ff.coef, arg);
+    sdf[b] = (f * f) * pt * pt * pt * inv_pi2x4 / (arg * arg);
   }
   __syncthreads();
-  {  // cumulative sum in FP64: contiguous runs per thread, block scan of the run sums
-    __shared__ double sw[32];
+  {  // cumulative sum: contiguous runs per thread, block scan of the run sums
+    __shared__ float sw[32];
     const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, wid = t >> 5;
     const int per = (nb + nt - 1) / nt;
     const int lo = t * per, hi = lo + per < nb ? lo + per : nb;
-    double run = 0.;
-    for (int b = lo; b < hi; ++b) run += sd[b];
-    double incl = run;  // inclusive scan of the run sums: warps, then warp totals
+    float run = 0.f;
+    for (int b = lo; b < hi; ++b) run += sdf[b];
+    float incl = run;  // inclusive scan of the run sums: warps, then warp totals
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const double y = __shfl_up_sync(0xffffffffu, incl, o);
+      const float y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
     if (lane == 31) sw[wid] = incl;
     __syncthreads();
     if (wid == 0) {
-      double v = lane < nt / 32 ? sw[lane] : 0.;
+      float v = lane < nt / 32 ? sw[lane] : 0.f;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const double y = __shfl_up_sync(0xffffffffu, v, o);
+        const float y = __shfl_up_sync(0xffffffffu, v, o);
         if (lane >= o) v += y;
       }
       sw[lane] = v;
     }
     __syncthreads();
-    double acc = (wid > 0 ? sw[wid - 1] : 0.) + incl - run;
+    float acc = (wid > 0 ? sw[wid - 1] : 0.f) + incl - run;
     for (int b = lo; b < hi; ++b) {
-      acc += sd[b];
-      sd[b] = acc;
+      acc += sdf[b];
+      sdf[b] = acc;
     }
   }
   __syncthreads();
-  const double tot = sd[nb - 1];
+  const float inv_tot = 1.f / sdf[nb - 1];
   float* o = out + (size_t)ie * (nb + 1);
   if (threadIdx.x == 0) o[0] = 0.f;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) o[b + 1] = (float)(sd[b] / tot);
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) o[b + 1] = sdf[b] * inv_tot;
 }
 
 // Every candidate of [cand0, cand0 + n) with its accept flag (single-event API).
@@ -433,12 +436,15 @@ cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, float* d_cdf,
-                                    cudaStream_t st) {
-  const size_t smem = sizeof(double) * e.pt_nbins;
-  cudaFuncSetAttribute(k_pt_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, float4* d_ff32,
+                                    float* d_cdf, cudaStream_t st) {
+  const size_t smem = sizeof(float) * e.pt_nbins;
+  if (smem > 48 * 1024) return cudaErrorInvalidValue;
   note_launch();
-  k_pt_tables<<<e.pt_ne, 256, smem, st>>>(e, ff, d_cdf);
+  k_coef_f32<<<(ff.n - 1 + 255) / 256, 256, 0, st>>>(ff.coef, d_ff32, ff.n - 1);
+  const SplineF f32{d_ff32, (float)ff.x0, (float)ff.h, (float)ff.inv_h, ff.n};
+  note_launch();
+  k_pt_tables<<<e.pt_ne, 256, smem, st>>>(e, f32, d_cdf);
   return cudaGetLastError();
 }
 

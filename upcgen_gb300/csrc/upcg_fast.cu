@@ -279,33 +279,6 @@ struct FastGrid {
   double c_far;         // G where every azimuth has b >= 20 fm: P(20) sum_k w_k
 };
 
-// FP32 copy of a uniform-knot spline (coefficients {y, b, c, d} per interval)
-struct SplineF {
-  const float4* coef;
-  float x0, h, inv_h;
-  int n;
-};
-
-__device__ __forceinline__ float spline_eval_f(const SplineF& s, const float4* coef, float x) {
-  int i = (int)floorf((x - s.x0) * s.inv_h);
-  i = i < 0 ? 0 : (i > s.n - 2 ? s.n - 2 : i);
-  float xi = s.x0 + i * s.h;
-  if (x < xi && i > 0) {
-    --i;
-    xi = s.x0 + i * s.h;
-  }
-  const float4 c = coef[i];
-  const float d = x - xi;
-  return c.x + d * (c.y + d * (c.z + d * c.w));
-}
-
-__global__ void k_coef_f32(const double4* __restrict__ in, float4* __restrict__ out, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double4 c = in[i];
-  out[i] = make_float4((float)c.x, (float)c.y, (float)c.z, (float)c.w);
-}
-
 struct GParams {
   SplineF gaa, brk;
   int has_brk;
@@ -472,6 +445,7 @@ struct FluxTabs {
 // near-node weight, so cells whose luminosity lies far below FP32's range
 // keep full precision; the scale returns in FP64 in k_fast_finish.
 constexpr int kProjThreads = 256;
+constexpr int kMaxP = 1024;  // radial grid points (the projection's shared-memory row)
 
 struct SideC {
   float lnb0, ld;   // ln b_i = lnb0 + i ld
@@ -506,16 +480,78 @@ __device__ __forceinline__ double ln_cosh_half(double d) {
   return r * z2;
 }
 
+// Side constants of every (cell, photon): one thread each, so that the few
+// FP64 operations they need run on full warps (an FP64 warp instruction
+// costs the same with 2 active lanes as with 32 on this part).
+__global__ void k_fast_sides(LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
+                             SideC* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * ncells) return;
+  const int lc = t >> 1, side = t & 1;
+  const int cell = cell0 + lc;
+  const int im = cell / p.ny, iy = cell - (cell / p.ny) * p.ny;
+  const double Y = p.ymin + p.dy * iy;
+  const double lnk = fg.lnm2[im] + (side ? -Y : Y);  // k = m/2 e^{+-y} (:224-225)
+  // bmax = max(5 g hc / k, 5R) (:229-230); g = g2 for the second photon
+  const double lnbmax = fmax((side ? fg.ln5ghc2 : fg.ln5ghc1) - lnk, fg.ln5R);
+  const double d = (lnbmax - fg.lnbmin) * (1. / kNb);
+  const double inv_d = 1. / d;  // the one FP64 division per side
+  const double lnb0 = fg.lnbmin + 0.5 * d + ln_cosh_half(d);
+  constexpr double inv_hK = (kKTabN - 1) / (kKTabU1 - kKTabU0);
+  const double lnxk = lnk - fg.lnghc;  // x = b k / (g1 hc): fluxPoint and the form
+                                       // integrand use g1 (:169, :198)
+  SideC c;
+  c.lnb0 = (float)lnb0;
+  c.ld = (float)d;
+  c.tg0 = (float)((lnb0 - fg.u0) * fg.inv_h);
+  c.tgd = (float)(d * fg.inv_h);
+  c.inv_tgd = (float)(inv_d * fg.h);
+  c.lnw0 = logf(2.f * tanhf(0.5f * (float)d));  // b (bh - bl) = b^2 2 tanh(d/2)
+  c.tk0 = (float)((lnb0 + lnxk - kKTabU0) * inv_hK);
+  c.tkd = (float)(d * inv_hK);
+  c.lnxk = (float)lnxk;
+  c.lnc_pt = (float)(fg.lnc_pt + lnk);
+  c.lnc_ff = (float)(fg.lnc_ff - lnk);
+  // node counts below 2R and r_near: ln b_i <= ln X for i < floor((ln X - lnb0)/d) + 1
+  auto count_le = [&](double lnX) {
+    const double t = floor((lnX - lnb0) * inv_d) + 1.;
+    return t < 0. ? 0 : (t > kNb ? kNb : (int)t);
+  };
+  c.n_form = p.isPoint ? 0 : count_le(fg.ln2R);
+  c.n_near = count_le(fg.ln_rnear);
+  c.tb0 = 0.f;
+  c.tbd = 0.f;
+  c.iw = 0;
+  c.ww[0] = c.ww[1] = c.ww[2] = c.ww[3] = 0.f;
+  if (!p.isPoint && ft.q32) {
+    c.tb0 = (float)((lnb0 - ft.lb0) * ft.inv_hb);
+    c.tbd = (float)(d * ft.inv_hb);
+    const double tw = (lnk - ft.lw0) * ft.inv_hw;
+    int p0 = (int)floor(tw) - 1;
+    p0 = p0 < 0 ? 0 : (p0 > ft.nw - 4 ? ft.nw - 4 : p0);
+    c.iw = p0;
+    const float sw = (float)(tw - p0);
+    const float s1 = sw - 1.f, s2 = sw - 2.f, s3 = sw - 3.f;
+    c.ww[0] = -s1 * s2 * s3 * (1.f / 6.f);
+    c.ww[1] = sw * s2 * s3 * 0.5f;
+    c.ww[2] = -sw * s1 * s3 * 0.5f;
+    c.ww[3] = sw * s1 * s2 * (1.f / 6.f);
+  }
+  out[t] = c;
+}
+
 __global__ void __launch_bounds__(kProjThreads) k_fast_project(
     LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
-    const double* __restrict__ flux_nodes, __nv_bfloat16* __restrict__ ah,
-    __nv_bfloat16* __restrict__ al, float* __restrict__ a2, double* __restrict__ far_term) {
+    const SideC* __restrict__ sides, const double* __restrict__ flux_nodes,
+    __nv_bfloat16* __restrict__ ah, __nv_bfloat16* __restrict__ al, float* __restrict__ a2,
+    float4* __restrict__ far_term) {
   __shared__ SideC sc[2];
   __shared__ float s_an[2][kNb];   // a_i / max near a (near nodes), 0 beyond
   __shared__ float s_t[2][kNb];    // radial-grid coordinate of near node i
   __shared__ float s_qk[2][256];   // Q(k_side, b_j) on the table's b grid
   __shared__ float s_red[3][2][kProjThreads / 32];
   __shared__ float s_lamax[2];
+  __shared__ __align__(16) float s_row[2][kMaxP];  // A_side on the radial grid
   const int lc = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const size_t row = (size_t)lc * fg.P;
@@ -529,57 +565,9 @@ __global__ void __launch_bounds__(kProjThreads) k_fast_project(
   }
   const int cell = cell0 + lc;
   const int im = cell / p.ny, iy = cell - (cell / p.ny) * p.ny;
-  if (tid < 2) {  // side constants: a few FP64 operations, no FP64 exp or log per side
-    const int side = tid;
-    const double Y = p.ymin + p.dy * iy;
-    const double lnk = fg.lnm2[im] + (side ? -Y : Y);  // k = m/2 e^{+-y} (:224-225)
-    // bmax = max(5 g hc / k, 5R) (:229-230); g = g2 for the second photon
-    const double lnbmax = fmax((side ? fg.ln5ghc2 : fg.ln5ghc1) - lnk, fg.ln5R);
-    const double d = (lnbmax - fg.lnbmin) * (1. / kNb);
-    const double inv_d = 1. / d;  // the one FP64 division per side
-    const double lnb0 = fg.lnbmin + 0.5 * d + ln_cosh_half(d);
-    constexpr double inv_hK = (kKTabN - 1) / (kKTabU1 - kKTabU0);
-    const double lnxk = lnk - fg.lnghc;  // x = b k / (g1 hc): fluxPoint and the form
-                                         // integrand use g1 (:169, :198)
-    SideC c;
-    c.lnb0 = (float)lnb0;
-    c.ld = (float)d;
-    c.tg0 = (float)((lnb0 - fg.u0) * fg.inv_h);
-    c.tgd = (float)(d * fg.inv_h);
-    c.inv_tgd = (float)(inv_d * fg.h);
-    c.lnw0 = logf(2.f * tanhf(0.5f * (float)d));  // b (bh - bl) = b^2 2 tanh(d/2)
-    c.tk0 = (float)((lnb0 + lnxk - kKTabU0) * inv_hK);
-    c.tkd = (float)(d * inv_hK);
-    c.lnxk = (float)lnxk;
-    c.lnc_pt = (float)(fg.lnc_pt + lnk);
-    c.lnc_ff = (float)(fg.lnc_ff - lnk);
-    // node counts below 2R and r_near: ln b_i <= ln X for i < floor((ln X - lnb0)/d) + 1
-    auto count_le = [&](double lnX) {
-      const double t = floor((lnX - lnb0) * inv_d) + 1.;
-      return t < 0. ? 0 : (t > kNb ? kNb : (int)t);
-    };
-    c.n_form = p.isPoint ? 0 : count_le(fg.ln2R);
-    c.n_near = count_le(fg.ln_rnear);
-    c.tb0 = 0.f;
-    c.tbd = 0.f;
-    c.iw = 0;
-    c.ww[0] = c.ww[1] = c.ww[2] = c.ww[3] = 0.f;
-    if (!p.isPoint && ft.q32) {
-      c.tb0 = (float)((lnb0 - ft.lb0) * ft.inv_hb);
-      c.tbd = (float)(d * ft.inv_hb);
-      const double tw = (lnk - ft.lw0) * ft.inv_hw;
-      int p0 = (int)floor(tw) - 1;
-      p0 = p0 < 0 ? 0 : (p0 > ft.nw - 4 ? ft.nw - 4 : p0);
-      c.iw = p0;
-      const float sw = (float)(tw - p0);
-      const float s1 = sw - 1.f, s2 = sw - 2.f, s3 = sw - 3.f;
-      c.ww[0] = -s1 * s2 * s3 * (1.f / 6.f);
-      c.ww[1] = sw * s2 * s3 * 0.5f;
-      c.ww[2] = -sw * s1 * s3 * 0.5f;
-      c.ww[3] = sw * s1 * s2 * (1.f / 6.f);
-    }
-    sc[side] = c;
-  }
+  if (tid < 2) sc[tid] = sides[2 * lc + tid];
+  for (int q = 4 * tid; q < 2 * kMaxP; q += 4 * kProjThreads)
+    *reinterpret_cast<float4*>(&s_row[0][0] + q) = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncthreads();
   if (!p.isPoint && ft.q32 && !flux_nodes) {  // the photon energy's Q row
     for (int j = tid; j < 2 * ft.nb; j += kProjThreads) {
@@ -666,56 +654,58 @@ __global__ void __launch_bounds__(kProjThreads) k_fast_project(
     }
   }
   __syncthreads();
-  // gather onto the radial grid: A_side[q] = sum_i an_i phi_{q - p0_i}(s_i),
-  // nodes in increasing order (deterministic, no atomics)
-  for (int e = tid; e < 2 * fg.P; e += kProjThreads) {
-    const int sd = e / fg.P, q = e - sd * fg.P;
-    const int nn = sc[sd].n_near;
-    float acc = 0.f;
-    if (nn > 0) {
-      const float t0 = s_t[sd][0];
-      int i0 = (int)floorf(((float)q - 2.f - t0) * sc[sd].inv_tgd) - 2;
-      i0 = i0 < 0 ? 0 : i0;
-      for (int j = i0; j < nn; ++j) {
-        const float t = s_t[sd][j];
-        int p0 = (int)floorf(t) - 1;
-        p0 = p0 < 0 ? 0 : (p0 > fg.P - 4 ? fg.P - 4 : p0);
-        if (p0 > q) break;
-        const int m = q - p0;
-        if (m > 3) continue;
-        const float s = t - (float)p0;
-        const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
-        const float w = m == 0 ? -s1 * s2 * s3 * (1.f / 6.f)
-                      : m == 1 ? s * s2 * s3 * 0.5f
-                      : m == 2 ? -s * s1 * s3 * 0.5f
-                               : s * s1 * s2 * (1.f / 6.f);
-        acc = fmaf(s_an[sd][j], w, acc);
-      }
+  // scatter onto the radial grid: A_side[p0_i + m] += an_i phi_m(s_i).  Nodes
+  // i = r (mod np) go in pass r, np = ceil(4.5 / spacing): within a pass the
+  // 4-point stencils are disjoint, so no atomics and a fixed summation order.
+  const int np = (int)ceilf(4.5f * fmaxf(sc[0].inv_tgd, sc[1].inv_tgd));
+  for (int pass = 0; pass < np; ++pass) {
+    if (node && near && i % np == pass) {
+      const float t = s_t[side][i];
+      const int p0 = (int)floorf(t) - 1;  // in [0, P-4]: the host checks the grid's span
+      const float s = t - (float)p0;
+      const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
+      const float a = s_an[side][i];
+      float* r = &s_row[side][p0];
+      r[0] = fmaf(a, -s1 * s2 * s3 * (1.f / 6.f), r[0]);
+      r[1] = fmaf(a, s * s2 * s3 * 0.5f, r[1]);
+      r[2] = fmaf(a, -s * s1 * s3 * 0.5f, r[2]);
+      r[3] = fmaf(a, s * s1 * s2 * (1.f / 6.f), r[3]);
     }
-    if (sd == 0) {
-      const __nv_bfloat16 hi = __float2bfloat16(acc);
-      ah[row + q] = hi;
-      al[row + q] = __float2bfloat16(acc - __bfloat162float(hi));
-    } else {
-      a2[row + q] = acc;
-    }
+    __syncthreads();
+  }
+  // 4 grid points per thread: bf16 hi / lo of side 0, FP32 of side 1
+  for (int q = 4 * tid; q < fg.P; q += 4 * kProjThreads) {
+    const float4 x = *reinterpret_cast<const float4*>(&s_row[0][q]);
+    const __nv_bfloat162 h01 = __floats2bfloat162_rn(x.x, x.y);
+    const __nv_bfloat162 h23 = __floats2bfloat162_rn(x.z, x.w);
+    const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+    const __nv_bfloat162 l01 = __floats2bfloat162_rn(x.x - f01.x, x.y - f01.y);
+    const __nv_bfloat162 l23 = __floats2bfloat162_rn(x.z - f23.x, x.w - f23.y);
+    uint2 hv, lv;
+    hv.x = *reinterpret_cast<const uint32_t*>(&h01);
+    hv.y = *reinterpret_cast<const uint32_t*>(&h23);
+    lv.x = *reinterpret_cast<const uint32_t*>(&l01);
+    lv.y = *reinterpret_cast<const uint32_t*>(&l23);
+    *reinterpret_cast<uint2*>(ah + row + q) = hv;
+    *reinterpret_cast<uint2*>(al + row + q) = lv;
+    *reinterpret_cast<float4*>(a2 + row + q) = *reinterpret_cast<const float4*>(&s_row[1][q]);
   }
   if (tid == 0) {
-    double S[4] = {0., 0., 0., 0.};  // near0, near1, far0, far1
+    float S[4] = {0.f, 0.f, 0.f, 0.f};  // near0, near1, far0, far1
     for (int w = 0; w < kProjThreads / 32; ++w) {
       S[0] += s_red[1][0][w];
       S[1] += s_red[1][1][w];
       S[2] += s_red[2][0][w];
       S[3] += s_red[2][1][w];
     }
-    // G = c wherever one node is far: c (S1far S2 + S1near S2far), normalised
-    far_term[2 * lc] = fg.c_far * (S[2] * (S[1] + S[3]) + S[0] * S[3]);
-    far_term[2 * lc + 1] = (double)s_lamax[0] + (double)s_lamax[1];  // ln of the scale
+    // G = c wherever one node is far: (S1far S2 + S1near S2far), normalised;
+    // the two ln scales; k_fast_finish combines them in FP64
+    far_term[lc] = make_float4(S[2] * (S[1] + S[3]) + S[0] * S[3], s_lamax[0], s_lamax[1], 0.f);
   }
 }
 
-__global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles,
-                              const float* __restrict__ partial, const double* __restrict__ far_term,
+__global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, double c_far,
+                              const float* __restrict__ partial, const float4* __restrict__ far_term,
                               double* __restrict__ lumi) {
   const int lc = blockIdx.x * blockDim.x + threadIdx.x;
   if (lc >= ncells) return;
@@ -724,7 +714,8 @@ __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles,
   const double M = p.mmin + p.dm * im;
   double t2 = 0.;
   for (int t = 0; t < ntiles; ++t) t2 += (double)partial[(size_t)lc * ntiles + t];
-  const double s = exp(far_term[2 * lc + 1]) * (far_term[2 * lc] + t2);
+  const float4 f = far_term[lc];
+  const double s = exp((double)f.y + (double)f.z) * (c_far * (double)f.x + t2);
   lumi[cell] = 2 * kPi * kPi * M * s * p.dm * p.dy;
 }
 
@@ -854,8 +845,8 @@ cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, doubl
 
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
-                                const double* flux_nodes, const FastFluxTables* t, void* ah,
-                                void* al, float* a2, double* far_term, cudaStream_t st) {
+                                const double* flux_nodes, const FastFluxTables* t, void* d_sides,
+                                void* ah, void* al, float* a2, void* far_term, cudaStream_t st) {
   FastGrid fg{P, u0, h, 1.0 / h, 250.};
   fg.lnm2 = lnm2;
   fg.ln5ghc1 = std::log(5. * p.g1 * kHc);
@@ -869,16 +860,25 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
   fg.lnc_ff = std::log(p.factor / ((double)p.A * p.A));
   fg.c_far = c_far;
   FluxTabs ft{};
+  if (P != kMaxP || P % (4 * kProjThreads) != 0) return cudaErrorInvalidValue;
+  // every near node's 4-point stencil inside the grid: b_min >= r_1, b <= r_near < r_{P-3}
+  if (std::log(p.isPoint ? p.R : 0.05 * p.R) < u0 + h || std::log(250.) > u0 + (P - 4) * h)
+    return cudaErrorInvalidValue;
   if (t) {
     if (t->nb > 256) return cudaErrorInvalidValue;  // s_qk holds one Q row
     ft = FluxTabs{t->st32, t->qt32, t->nw, t->nb, t->lw0, 1. / t->hw, t->lb0, 1. / t->hb};
   }
+  SideC* sides = static_cast<SideC*>(d_sides);
   note_launch();
-  k_fast_project<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, flux_nodes,
+  k_fast_sides<<<(2 * ncells + 255) / 256, 256, 0, st>>>(p, fg, ft, cell0, ncells, sides);
+  note_launch();
+  k_fast_project<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, sides, flux_nodes,
                                                         (__nv_bfloat16*)ah, (__nv_bfloat16*)al,
-                                                        a2, far_term);
+                                                        a2, static_cast<float4*>(far_term));
   return cudaGetLastError();
 }
+
+size_t fast_side_bytes() { return sizeof(SideC); }
 
 int flux_table_part_doubles(int nw, int nb) { return 8 * nw * nb; }
 
@@ -910,11 +910,11 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
 int flux_table_ktab_n() { return kKTabN; }
 
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
-                               const float* partial, const double* far_term, double* lumi,
-                               cudaStream_t st) {
+                               double c_far, const float* partial, const void* far_term,
+                               double* lumi, cudaStream_t st) {
   note_launch();
-  k_fast_finish<<<(ncells + 255) / 256, 256, 0, st>>>(p, cell0, ncells, ntiles, partial, far_term,
-                                                      lumi);
+  k_fast_finish<<<(ncells + 255) / 256, 256, 0, st>>>(p, cell0, ncells, ntiles, c_far, partial,
+                                                      static_cast<const float4*>(far_term), lumi);
   return cudaGetLastError();
 }
 

@@ -113,14 +113,17 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
 // wherever every azimuth has b >= 20 fm
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
-                                const double* flux_nodes, const FastFluxTables* t, void* ah,
-                                void* al, float* a2, double* far_term, cudaStream_t st);
+                                const double* flux_nodes, const FastFluxTables* t, void* d_sides,
+                                void* ah, void* al, float* a2, void* far_term, cudaStream_t st);
+// bytes of the per-(cell, photon) constants (d_sides holds 2 per cell);
+// far_term holds one float4 per cell
+size_t fast_side_bytes();
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
                             const float* a2, int ncells_pad, int ncells, int P, float* partial,
                             unsigned* d_err, cudaStream_t st);
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
-                               const float* partial, const double* far_term, double* lumi,
-                               cudaStream_t st);
+                               double c_far, const float* partial, const void* far_term,
+                               double* lumi, cudaStream_t st);
 cudaError_t contract_selftest(int ncells, int P, uint64_t seed, double* max_rel, double* ms);
 
 // fold + samplers
@@ -160,8 +163,9 @@ struct EventRecord {  // 48 bytes
   float p0[4];
   float p1[4];
 };
-cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, float* d_cdf,
-                                    cudaStream_t st);
+// d_ff32: scratch for the FP32 copy of the form-factor spline (ff.n - 1 intervals)
+cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, float4* d_ff32,
+                                    float* d_cdf, cudaStream_t st);
 cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                                 const float* d_ptcdf, uint64_t cand0, int64_t ncand,
                                 uint32_t* d_mask, int* d_tile_count, cudaStream_t st);

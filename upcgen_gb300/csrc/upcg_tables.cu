@@ -383,6 +383,13 @@ cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, doub
   return cudaGetLastError();
 }
 
+__global__ void k_coef_f32(const double4* __restrict__ in, float4* __restrict__ out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4 c = in[i];
+  out[i] = make_float4((float)c.x, (float)c.y, (float)c.z, (float)c.w);
+}
+
 cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
                                  double4* d_coef, cudaStream_t st) {
   (void)x0;
