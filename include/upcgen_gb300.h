@@ -117,6 +117,28 @@ int upcg_cs_zm_table(upcg_generator* g, int flag, double* out, size_t n);
 int upcg_flux_point(upcg_generator* g, const double* b, const double* k, double* out, size_t n);
 /* fluxForm, src/UpcCrossSection.cpp:194-218 (QAGS on the device) */
 int upcg_flux_form(upcg_generator* g, const double* b, const double* k, double* out, size_t n);
+/* No counterpart in the reference.  upcg_flux_form on DEVICE buffers without
+ * any device-memory allocation: for callers that may not allocate once they
+ * run -- code inside a larger CUDA stream capture, where an allocation would
+ * break or serialise the capture, and applications whose memory pool owns all
+ * HBM after start-up, where a driver allocation fails or evicts the pool.
+ * The QAGS scratch lives in 2.6 MB of static device memory of the library
+ * (64 warp workspaces and one statistics word); nothing is allocated here.
+ *   - n <= UPCG_NOALLOC_MAX_POINTS, else UPCG_ERR_SIZE;
+ *   - needs the tables of a completed upcg_init (else UPCG_ERR_STATE);
+ *   - the call clears the statistics word itself (cudaMemsetAsync on the
+ *     handle's stream); the workspaces need no clearing;
+ *   - asynchronous on the handle's stream; failures_device (device, may be
+ *     NULL) receives the number of points whose QAGS returned a non-zero
+ *     status (the reference aborts there);
+ *   - the first call on a device looks up the scratch address
+ *     (cudaGetSymbolAddress) and should come before any stream capture;
+ *   - the scratch is shared by all handles: calls that overlap in time (two
+ *     streams or two host threads) race on it and must be serialised. */
+#define UPCG_NOALLOC_MAX_POINTS 16777216
+int upcg_flux_form_device_noalloc(upcg_generator* g, const double* b_device,
+                                  const double* k_device, double* out_device, size_t n,
+                                  uint32_t* failures_device);
 /* calcFormFac, src/UpcCrossSection.cpp:436-445 */
 int upcg_form_factor(upcg_generator* g, const double* q2, double* out, size_t n);
 /* calcBreakupProb, src/UpcCrossSection.cpp:752-1019 */

@@ -35,6 +35,7 @@ ABI_SYMBOLS = [
     "upcg_generate_events_device", "upcg_generate_event", "upcg_philox",
     "upcg_last_timings", "upcg_qags_stats", "upcg_last_error", "upcg_version",
     "upcg_selftest_contract", "upcg_fast_flux_table", "upcg_kernel_launches",
+    "upcg_flux_form_device_noalloc",
 ]
 
 
@@ -81,6 +82,7 @@ def load_library(path=None):
         "upcg_selftest_contract": [i, i, u64, dp, dp],
         "upcg_fast_flux_table": [vp, vp, sz, vp],
         "upcg_kernel_launches": [C.POINTER(u64)],
+        "upcg_flux_form_device_noalloc": [vp, vp, vp, vp, sz, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -147,6 +149,14 @@ class UpcCrossSection:
     def fluxForm(self, b, k):  # src/UpcCrossSection.cpp:194-218
         b, k = np.broadcast_arrays(_arr(b), _arr(k))
         return self._pts(self._g._L.upcg_flux_form, b, k)
+
+    def fluxFormDeviceNoAlloc(self, b_ptr, k_ptr, out_ptr, n, failures_ptr=None):
+        """fluxForm on device buffers (raw device pointers, n doubles each)
+        without any device allocation (upcg_flux_form_device_noalloc; no
+        counterpart in the reference).  Asynchronous on the generator's stream."""
+        _check(self._g._L.upcg_flux_form_device_noalloc(
+            self._g._h, C.c_void_p(b_ptr), C.c_void_p(k_ptr), C.c_void_p(out_ptr), int(n),
+            C.c_void_p(failures_ptr) if failures_ptr else None))
 
     def calcFormFac(self, q2):  # src/UpcCrossSection.cpp:436-445
         return self._pts(self._g._L.upcg_form_factor, q2)

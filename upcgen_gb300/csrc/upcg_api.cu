@@ -1013,6 +1013,21 @@ int upcg_flux_form(upcg_generator* g, const double* b, const double* k, double* 
   return UPCG_OK;
 }
 
+int upcg_flux_form_device_noalloc(upcg_generator* g, const double* b_device,
+                                  const double* k_device, double* out_device, size_t n,
+                                  uint32_t* failures_device) {
+  if (!g || !b_device || !k_device || !out_device) return fail(UPCG_ERR_ARG, "null argument");
+  if (n > UPCG_NOALLOC_MAX_POINTS)
+    return fail(UPCG_ERR_SIZE, "upcg_flux_form_device_noalloc: %zu points, at most %d per call", n,
+                UPCG_NOALLOC_MAX_POINTS);
+  if (!g->tables_ready)
+    return fail(UPCG_ERR_STATE, "upcg_flux_form_device_noalloc needs the tables of upcg_init");
+  if (n == 0) return UPCG_OK;
+  CK(launch_flux_form_noalloc(g->lumi_params(), b_device, k_device, out_device, (int)n,
+                              failures_device, g->st()));
+  return UPCG_OK;
+}
+
 int upcg_form_factor(upcg_generator* g, const double* q2, double* out, size_t n) {
   if (!g || !q2 || !out) return fail(UPCG_ERR_ARG, "null argument");
   if (n == 0) return UPCG_OK;

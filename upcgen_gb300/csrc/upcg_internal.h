@@ -80,6 +80,12 @@ size_t qags_global_ws_doubles_per_warp();
 cudaError_t launch_lumi_band(const LumiParams& p, int cell0, int ncells, const double* d_flux,
                              double* d_lumi, double* d_lumi2, cudaStream_t st);
 // point evaluations for the parity entry points
+// fluxForm on device buffers with the QAGS scratch in static device memory
+// (no allocation); d_failures (device, may be null) receives the count of
+// points whose QAGS returned a non-zero status
+cudaError_t launch_flux_form_noalloc(const LumiParams& p, const double* d_b, const double* d_k,
+                                     double* d_out, int n, unsigned* d_failures,
+                                     cudaStream_t st);
 cudaError_t launch_flux_points(const LumiParams& p, const double* d_b, const double* d_k,
                                double* d_out, int n, int form, QagsStats* d_stats,
                                cudaStream_t st);

@@ -20,6 +20,8 @@
 //                 is the set of node pairs for which some azimuth gives b < 20.
 //                 This is the reference's sum regrouped; pairs outside the band
 //                 contribute exactly zero to the second term.
+#include <mutex>
+
 #include "upcg_internal.h"
 
 namespace upcg {
@@ -775,6 +777,68 @@ cudaError_t launch_flux_points(const LumiParams& p, const double* d_b, const dou
                                                             warps);
   e = cudaGetLastError();
   cudaFreeAsync(gws, st);
+  return e;
+}
+
+// ---- no-allocation flux entry ------------------------------------------------
+// Scratch of upcg_flux_form_device_noalloc in static device memory: the QAGS
+// workspaces of kNoAllocWarps warps (40.5 KB each, 2.6 MB in all) and one
+// statistics word.  Every call uses all of it, so calls that overlap in time
+// (two streams, two host threads) race on it.
+namespace {
+constexpr int kNoAllocWarps = 64;
+__device__ __align__(256) unsigned char g_noalloc_ws[kNoAllocWarps * sizeof(QWs<kQagsLimit>)];
+__device__ __align__(256) QagsStats g_noalloc_stats;
+}  // namespace
+
+// Device addresses of the static scratch, looked up once per device with that
+// device current (cudaGetSymbolAddress; no allocation).
+static cudaError_t noalloc_scratch(double** ws, QagsStats** stats) {
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static void* ws_ptr[kMaxDev];
+  static void* st_ptr[kMaxDev];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!ws_ptr[dev]) {
+    void* w = nullptr;
+    void* t = nullptr;
+    if ((e = cudaGetSymbolAddress(&w, g_noalloc_ws)) != cudaSuccess) return e;
+    if ((e = cudaGetSymbolAddress(&t, g_noalloc_stats)) != cudaSuccess) return e;
+    ws_ptr[dev] = w;
+    st_ptr[dev] = t;
+  }
+  *ws = static_cast<double*>(ws_ptr[dev]);
+  *stats = static_cast<QagsStats*>(st_ptr[dev]);
+  return cudaSuccess;
+}
+
+cudaError_t launch_flux_form_noalloc(const LumiParams& p, const double* d_b, const double* d_k,
+                                     double* d_out, int n, unsigned* d_failures,
+                                     cudaStream_t st) {
+  double* ws = nullptr;
+  QagsStats* stats = nullptr;
+  cudaError_t e = noalloc_scratch(&ws, &stats);
+  if (e != cudaSuccess) return e;
+  // the statistics word must start at zero; the workspaces need no clearing
+  // (each warp writes an interval before it reads it)
+  if ((e = cudaMemsetAsync(stats, 0, sizeof(QagsStats), st)) != cudaSuccess) return e;
+  if (p.isPoint) {
+    note_launch();
+    k_flux_point_pts<<<(n + 255) / 256, 256, 0, st>>>(p, d_b, d_k, d_out, n);
+  } else {
+    const int warps = n < kNoAllocWarps ? n : kNoAllocWarps;
+    note_launch();
+    k_flux_form_pts<<<(warps * 32 + 127) / 128, 128, 0, st>>>(p, d_b, d_k, d_out, n, stats, ws,
+                                                              warps);
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (d_failures)
+    e = cudaMemcpyAsync(d_failures, &stats->failures, sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                        st);
   return e;
 }
 
