@@ -132,7 +132,8 @@ struct upcg_generator {
     if (!ev_fork) return cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
     return cudaSuccess;
   }
-  DBuf<int> ntab, nq, ovf, tile_count, mirror;
+  DBuf<int> ntab, nq, ovf, tile_count, mirror, guide2, guidez;
+  DBuf<uint16_t> guidept;
   DBuf<unsigned int> work;
   DBuf<QagsStats> stats;
   DBuf<float> ptcdf;
@@ -316,6 +317,16 @@ EventParams upcg_generator::event_params() const {
   e.pt_lne0 = std::log(kmin * kmin / (gtot * gtot));
   e.pt_dlne = (std::log(kmax * kmax / (gtot * gtot)) - e.pt_lne0) / (e.pt_ne - 1);
   e.pt_width = 6. * kHc / R / 5000;
+  e.pt_c0 = (float)(2. * std::log(gtot) + e.pt_lne0);
+  e.pt_inv_dlne = (float)(1. / e.pt_dlne);
+  int g2n = 1;
+  while (g2n < nm * ny) g2n <<= 1;
+  e.g2 = guide2.p;
+  e.g2_n = g2n;
+  e.gz = guidez.p;
+  e.gz_n = 128;
+  e.gpt = guidept.p;
+  e.gpt_n = 4096;
   return e;
 }
 
@@ -665,6 +676,13 @@ int upcg_generator::build_xsec() {
   CK(ptcdf.ensure((size_t)e.pt_ne * (e.pt_nbins + 1)));
   CK(ff32.ensure(kNQ2));
   CK(launch_photon_pt_tables(e, lumi_params().ff, ff32.p, ptcdf.p, s));
+  if (!usePolarizedCS) {
+    CK(guide2.ensure(e.g2_n));
+    CK(guidez.ensure((size_t)nm * e.gz_n));
+    CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
+    const EventParams eg = event_params();  // with the guide buffers allocated
+    CK(launch_guides(eg, cdf2.p, cdfz.p, ptcdf.p, guide2.p, guidez.p, guidept.p, s));
+  }
   CK(cudaMemcpyAsync(&totCS, tot.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   cudaEventRecord(t1, s);
   CK(cudaEventSynchronize(t1));

@@ -72,19 +72,52 @@ __device__ __forceinline__ int cdf_find_f(const float* __restrict__ cdf, int n, 
   return lo;
 }
 
+// The same answers as cdf_find / cdf_find_f (the largest k < n with
+// cdf[k] <= r), started from a guide-table entry k0 <= answer: a few forward
+// steps, or a binary search over [k, n) through a run of empty bins.
+__device__ __forceinline__ int cdf_find_from(const double* __restrict__ cdf, int n, int k,
+                                             double r) {
+#pragma unroll 1
+  for (int s = 0; s < 8; ++s) {
+    if (k + 1 >= n || __ldg(cdf + k + 1) > r) return k;
+    ++k;
+  }
+  int hi = n;
+  while (hi - k > 1) {
+    const int mid = (k + hi) >> 1;
+    if (r >= __ldg(cdf + mid)) k = mid; else hi = mid;
+  }
+  return k;
+}
+
+__device__ __forceinline__ int cdf_find_from_f(const float* __restrict__ cdf, int n, int k,
+                                               float r) {
+#pragma unroll 1
+  for (int s = 0; s < 8; ++s) {
+    if (k + 1 >= n || __ldg(cdf + k + 1) > r) return k;
+    ++k;
+  }
+  int hi = n;
+  while (hi - k > 1) {
+    const int mid = (k + hi) >> 1;
+    if (r >= __ldg(cdf + mid)) k = mid; else hi = mid;
+  }
+  return k;
+}
+
 // Photon pT from the tabulated spectrum closest in ln(k^2/gtot^2): the table
 // at grid point i or i+1, chosen with the interpolation weight.
-__device__ float photon_pt(const EventParams& e, const float* __restrict__ tabs, double k,
+__device__ float photon_pt(const EventParams& e, const float* __restrict__ tabs, float lnk,
                            float u, float usel) {
-  const double ered = (k * k) / (e.gtot * e.gtot);
-  double t = (log(ered) - e.pt_lne0) / e.pt_dlne;
-  t = t < 0. ? 0. : (t > e.pt_ne - 1 ? e.pt_ne - 1 : t);
+  float t = (2.f * lnk - e.pt_c0) * e.pt_inv_dlne;
+  t = t < 0.f ? 0.f : (t > (float)(e.pt_ne - 1) ? (float)(e.pt_ne - 1) : t);
   int i = (int)t;
   if (i > e.pt_ne - 2) i = e.pt_ne - 2;
-  const float fr = (float)(t - i);
+  const float fr = t - (float)i;
   if (usel < fr) ++i;
   const float* I = tabs + (size_t)i * (e.pt_nbins + 1);
-  const int ib = cdf_find_f(I, e.pt_nbins, u);
+  const int ib = cdf_find_from_f(I, e.pt_nbins,
+                                 __ldg(e.gpt + (size_t)i * e.gpt_n + (int)(u * (float)e.gpt_n)), u);
   const float lo = __ldg(I + ib), hi = __ldg(I + ib + 1);
   const float w = (float)e.pt_width;
   float x = ib * w;
@@ -129,7 +162,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   // (y, m): gsl_histogram2d_pdf_sample with r1 for the bin and y, r2 for m
   const int n2 = e.ny * e.nm;
   const double ra = u53(r0.x, r0.y), rb = u53(r0.z, r0.w);
-  const int k = cdf_find(cdf2, n2, ra);
+  const int k = cdf_find_from(cdf2, n2, __ldg(e.g2 + (int)(ra * (double)e.g2_n)), ra);
   const int iy = k / e.nm, im = k - iy * e.nm;
   const double c0 = __ldg(cdf2 + k), c1 = __ldg(cdf2 + k + 1);
   const double delta = c1 > c0 ? (ra - c0) / (c1 - c0) : 0.;
@@ -146,7 +179,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   const double rz = u53(r1.x, r1.y);
   if (!e.ignoreCSZ) {
     const double* cz = cdfz + (size_t)mb * (e.nz + 1);
-    const int iz = cdf_find(cz, e.nz, rz);
+    const int iz = cdf_find_from(cz, e.nz, __ldg(e.gz + (size_t)mb * e.gz_n + (int)(rz * (double)e.gz_n)), rz);
     const double z0 = __ldg(cz + iz), z1 = __ldg(cz + iz + 1);
     const double dl = z1 > z0 ? (rz - z0) / (z1 - z0) : 0.;
     const double zlo = e.zmin + e.dz * iz, zhi = e.zmin + e.dz * (iz + 1);
@@ -158,10 +191,11 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   const float m = (float)c.m, y = (float)c.y;
   float ppx = 0.f, ppy = 0.f, mt = m;
   if (e.useNonzeroGamPt) {
-    const double k1 = c.m / 2 * exp(c.y), k2 = c.m / 2 * exp(-c.y);
+    // ln k1,2 = ln(m/2) +- y
+    const float lnm2 = logf(0.5f * m);
     const float a1 = kTwoPiF * u24(r1.z), a2 = kTwoPiF * u24(r1.w);
-    const float pt1 = photon_pt(e, pttab, k1, u24(r2.x), u24(r2.y));
-    const float pt2 = photon_pt(e, pttab, k2, u24(r2.z), u24(r2.w));
+    const float pt1 = photon_pt(e, pttab, lnm2 + y, u24(r2.x), u24(r2.y));
+    const float pt2 = photon_pt(e, pttab, lnm2 - y, u24(r2.z), u24(r2.w));
     float s1, c1f, s2, c2f;
     sincosf(a1, &s1, &c1f);
     sincosf(a2, &s2, &c2f);
@@ -385,6 +419,24 @@ __global__ void k_pt_tables(EventParams e, SplineF ff, float* __restrict__ out) 
   for (int b = threadIdx.x; b < nb; b += blockDim.x) o[b + 1] = sdf[b] * inv_tot;
 }
 
+// Guide tables: bucket j of K starts at the answer of the plain search for
+// r = j / K (exact in floating point for K a power of two).
+__global__ void k_guide_rows_d(const double* __restrict__ cdf, int rows, int len, int K,
+                               int* __restrict__ guide) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)rows * K) return;
+  const int r = (int)(t / K), j = (int)(t - (int64_t)r * K);
+  guide[t] = cdf_find(cdf + (size_t)r * (len + 1), len, (double)j / (double)K);
+}
+
+__global__ void k_guide_rows_f(const float* __restrict__ cdf, int rows, int len, int K,
+                               uint16_t* __restrict__ guide) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)rows * K) return;
+  const int r = (int)(t / K), j = (int)(t - (int64_t)r * K);
+  guide[t] = (uint16_t)cdf_find_f(cdf + (size_t)r * (len + 1), len, (float)j / (float)K);
+}
+
 // Every candidate of [cand0, cand0 + n) with its accept flag (single-event API).
 __global__ void k_events_all(EventParams e, const double* __restrict__ cdf2,
                              const double* __restrict__ cdfz, const float* __restrict__ pttab,
@@ -433,6 +485,27 @@ cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* 
   if (n <= 0) return cudaSuccess;
   note_launch();
   k_philox_dump<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(seed, c0, n, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
+                          const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
+                          cudaStream_t st) {
+  if (e.pt_nbins > 65535) return cudaErrorInvalidValue;
+  const int n2 = e.nm * e.ny;
+  note_launch();
+  k_guide_rows_d<<<(e.g2_n + 255) / 256, 256, 0, st>>>(d_cdf2, 1, n2, e.g2_n, d_g2);
+  if (!e.ignoreCSZ) {
+    const int64_t nz = (int64_t)e.nm * e.gz_n;
+    note_launch();
+    k_guide_rows_d<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(d_cdfz, e.nm, e.nz, e.gz_n, d_gz);
+  }
+  if (e.useNonzeroGamPt) {
+    const int64_t np = (int64_t)e.pt_ne * e.gpt_n;
+    note_launch();
+    k_guide_rows_f<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(d_ptcdf, e.pt_ne, e.pt_nbins,
+                                                                 e.gpt_n, d_gpt);
+  }
   return cudaGetLastError();
 }
 

@@ -163,7 +163,21 @@ struct EventParams {
   // photon-pT tables
   int pt_ne, pt_nbins;
   double pt_lne0, pt_dlne, pt_width, gtot;
+  float pt_c0, pt_inv_dlne;  // table coordinate of ln k: (2 ln k - pt_c0) * pt_inv_dlne
+  // guide tables of the CDF inversions: bucket j of K holds the largest bin k
+  // with cdf[k] <= j / K, so a search starts at most a few bins below its answer
+  const int* g2;        // (y, m) CDF, K = g2_n buckets
+  int g2_n;
+  const int* gz;        // z CDF of every mass row, gz_n buckets per row
+  int gz_n;
+  const uint16_t* gpt;  // photon-pT tables, gpt_n buckets per table
+  int gpt_n;
 };
+// guide tables (EventParams) of the built CDFs; d_g2 / d_gz / d_gpt sized
+// g2_n, nm * gz_n, pt_ne * gpt_n
+cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
+                          const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
+                          cudaStream_t st);
 struct EventRecord {  // 48 bytes
   float m, y, z, sign;
   float p0[4];
