@@ -5,8 +5,8 @@
  * reference exposes a C++ class API (include/UpcGenerator.h:55-128,
  * include/UpcCrossSection.h:65-240, built as the Upcgenlib library by
  * CMakeLists.txt:83-91); every entry point below names the method it
- * replaces.  A C++ facade with the reference's class and method names sits on
- * top of this ABI in include/upcgen_gb300.hpp.
+ * replaces.  A header-only C++ facade with the reference's class and method
+ * names sits on top of this ABI in include/upcgen_gb300.hpp.
  *
  * Conventions
  *   - every function returns an int status (UPCG_OK = 0, negative on error)
@@ -154,6 +154,11 @@ int upcg_two_photon_lumi(upcg_generator* g, const double* m, const double* y, do
  * process (flag 0/1/2), src/UpcTwoPhotonDilep.cpp:46-122, src/UpcTwoPhotonALP.cpp:28-33 */
 int upcg_cs_m(upcg_generator* g, const double* m, int flag, double* out, size_t n);
 
+/* PDG code of the final-state particles of the configured process and
+ * whether they are charged (UpcGenerator::init, src/UpcGenerator.cpp:66-140):
+ * the lepton for PROC_ID 11/13/15, 51 for the ALP (its decay photons are 22) */
+int upcg_particle_pdg(upcg_generator* g, int* pdg, int* charged);
+
 /* ---- events (UpcGenerator::generateEvents) ------------------------------ */
 /* The event loop of src/UpcGenerator.cpp:834-889: the first n accepted events
  * of the candidate sequence; *rejected = candidates rejected by the cuts
@@ -188,6 +193,9 @@ int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_i
                     uint64_t* evals);
 /* kernels launched by the library in this process so far (all handles) */
 int upcg_kernel_launches(uint64_t* n);
+/* host-to-device and device-to-host bytes the library has copied in this
+ * process so far (all handles) */
+int upcg_copy_bytes(uint64_t* h2d, uint64_t* d2h);
 const char* upcg_last_error(void);
 const char* upcg_version(void);
 

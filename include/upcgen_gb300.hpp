@@ -1,0 +1,231 @@
+// upcgen-gb300 -- header-only C++ facade over the C ABI (upcgen_gb300.h) with
+// the reference's class and method names, so that a host written against
+// upcgen's UpcGenerator (include/UpcGenerator.h:55-128) and UpcCrossSection
+// (include/UpcCrossSection.h:65-240) switches by changing its include and
+// namespace.  ROOT-free: TLorentzVector / TParticle become the plain
+// LorentzVector / Particle below.
+//
+// Differences from the reference's classes:
+//   * errors throw upcgen_gb300::Error (the reference exits the process);
+//   * generateEvents() does not write ROOT/HepMC files; generateEvents(n)
+//     returns the accepted events, and eventRecords(n) the raw 48-byte records;
+//   * setSeed() seeds the Philox event stream (the reference reseeds gRandom).
+#ifndef UPCGEN_GB300_HPP_
+#define UPCGEN_GB300_HPP_
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "upcgen_gb300.h"
+
+namespace upcgen_gb300 {
+
+class Error : public std::runtime_error {
+ public:
+  Error(int code, const char* what) : std::runtime_error(what ? what : "upcgen-gb300 error"), code_(code) {}
+  int code() const { return code_; }
+
+ private:
+  int code_;
+};
+
+inline void check(int rc) {
+  if (rc != UPCG_OK) throw Error(rc, upcg_last_error());
+}
+
+struct LorentzVector {  // px, py, pz, E (GeV)
+  double px = 0, py = 0, pz = 0, e = 0;
+};
+
+struct Particle {  // the fields of TParticle the generator fills
+  int pdg = 0, status = 0, mother = 0;
+  LorentzVector p;
+};
+
+class UpcCrossSection;
+
+class UpcGenerator {
+ public:
+  UpcGenerator() { check(upcg_create(&h_)); }
+  ~UpcGenerator() { upcg_destroy(h_); }
+  UpcGenerator(const UpcGenerator&) = delete;
+  UpcGenerator& operator=(const UpcGenerator&) = delete;
+
+  // ---- configuration (src/UpcGenerator.cpp:183-346)
+  void setParameterValue(const std::string& parameter, const std::string& parValue) {
+    check(upcg_set_parameter(h_, parameter.c_str(), parValue.c_str()));
+  }
+  void setParFile(const std::string& parfilename) { parFile_ = parfilename; }
+  void configGeneratorFromFile() { check(upcg_config_from_file(h_, parFile_.c_str())); }
+  void setLumiFileDirectory(const std::string& directory) {
+    check(upcg_set_lumi_file_directory(h_, directory.c_str()));
+  }
+  void setDebugLevel(int level) { check(upcg_set_debug_level(h_, level)); }
+  void setNumThreads(int n) { check(upcg_set_num_threads(h_, n)); }
+  void setCollisionSystem(float sqrts, int nucl_z, int nucl_a) {
+    check(upcg_set_collision_system(h_, sqrts, nucl_z, nucl_a));
+  }
+  void setSeed(int seedIn) { check(upcg_set_seed(h_, seedIn)); }
+  // 0 plain FP64 (the reference's quadrature), 1 fast form
+  void setLumiMethod(int method) { check(upcg_set_lumi_method(h_, method)); }
+  void setStream(void* cuda_stream) { check(upcg_set_stream(h_, cuda_stream)); }
+
+  // ---- initial calculations (src/UpcGenerator.cpp:57-181, 630-713)
+  void init() { check(upcg_init(h_)); }
+  void computeNuclXsection() { check(upcg_compute_nucl_xsection(h_)); }
+  double totNuclX() const {
+    double v = 0;
+    check(upcg_tot_nucl_x(h_, &v));
+    return v;
+  }
+  double fidNuclX() const {
+    double v = 0;
+    check(upcg_fid_nucl_x(h_, &v));
+    return v;
+  }
+
+  // ---- events (src/UpcGenerator.cpp:715-926)
+  // One candidate: 1 (accepted) or 0 (rejected by the cuts); the outputs are
+  // cleared and filled like the reference's vectors.
+  long generateEvent(std::vector<int>& pdgs, std::vector<int>& statuses, std::vector<int>& mothers,
+                     std::vector<LorentzVector>& particles) {
+    upcg_event ev;
+    int accepted = 0;
+    check(upcg_generate_event(h_, &ev, &accepted));
+    pdgs.clear();
+    statuses.clear();
+    mothers.clear();
+    particles.clear();
+    fill(ev, pdgs, statuses, mothers, particles);
+    genParticles_.clear();
+    for (size_t i = 0; i < pdgs.size(); ++i)
+      genParticles_.push_back(Particle{pdgs[i], statuses[i], mothers[i], particles[i]});
+    return accepted;
+  }
+  const std::vector<Particle>& getParticles() const { return genParticles_; }
+
+  // The first n accepted events of the candidate sequence (the reference's
+  // loop without the file output); *rejected gets the rejected count.
+  std::vector<upcg_event> eventRecords(int64_t n, int64_t* rejected = nullptr) {
+    std::vector<upcg_event> out((size_t)n);
+    int64_t rej = 0;
+    check(upcg_generate_events(h_, n, out.data(), nullptr, &rej));
+    if (rejected) *rejected = rej;
+    return out;
+  }
+  std::vector<std::vector<Particle>> generateEvents(int64_t n) {
+    std::vector<std::vector<Particle>> evs;
+    std::vector<int> pdgs, st, mo;
+    std::vector<LorentzVector> ps;
+    for (const upcg_event& e : eventRecords(n)) {
+      pdgs.clear();
+      st.clear();
+      mo.clear();
+      ps.clear();
+      fill(e, pdgs, st, mo, ps);
+      std::vector<Particle> v;
+      for (size_t i = 0; i < pdgs.size(); ++i) v.push_back(Particle{pdgs[i], st[i], mo[i], ps[i]});
+      evs.push_back(std::move(v));
+    }
+    return evs;
+  }
+
+  upcg_generator* handle() const { return h_; }
+
+ private:
+  // pairProduction (src/UpcGenerator.cpp:388-423): two leptons, status 23,
+  // mother 0, charges sign1 = +-1, sign2 = -sign1; the ALP (status 23) and its
+  // two decay photons (pdg 22, status 33, mother 1) as twoPartDecayUniform
+  // (:526-561).
+  void fill(const upcg_event& e, std::vector<int>& pdgs, std::vector<int>& statuses,
+            std::vector<int>& mothers, std::vector<LorentzVector>& particles) {
+    int pdg = 0, charged = 0;
+    check(upcg_particle_pdg(h_, &pdg, &charged));
+    const LorentzVector a{e.p0[0], e.p0[1], e.p0[2], e.p0[3]};
+    const LorentzVector b{e.p1[0], e.p1[1], e.p1[2], e.p1[3]};
+    if (pdg == 51) {
+      particles.push_back(LorentzVector{a.px + b.px, a.py + b.py, a.pz + b.pz, a.e + b.e});
+      pdgs.push_back(pdg);
+      statuses.push_back(23);
+      mothers.push_back(0);
+      for (const LorentzVector& g : {a, b}) {
+        particles.push_back(g);
+        pdgs.push_back(22);
+        statuses.push_back(33);
+        mothers.push_back(1);
+      }
+      return;
+    }
+    const int s1 = charged ? (e.sign > 0 ? 1 : -1) : 1;
+    const int s2 = charged ? -s1 : 1;
+    particles.push_back(a);
+    particles.push_back(b);
+    pdgs.push_back(s1 * pdg);
+    pdgs.push_back(s2 * pdg);
+    statuses.push_back(23);
+    statuses.push_back(23);
+    mothers.push_back(0);
+    mothers.push_back(0);
+  }
+
+  upcg_generator* h_ = nullptr;
+  std::string parFile_ = "parameters.in";
+  std::vector<Particle> genParticles_;
+};
+
+// Batched views of UpcCrossSection's methods on a generator's tables
+// (src/UpcCrossSection.cpp): each takes n points and returns n values.
+class UpcCrossSection {
+ public:
+  explicit UpcCrossSection(UpcGenerator& g) : h_(g.handle()) {}
+  std::vector<double> fluxPoint(const std::vector<double>& b, const std::vector<double>& k) {
+    return pts2(b, k, &upcg_flux_point);
+  }
+  std::vector<double> fluxForm(const std::vector<double>& b, const std::vector<double>& k) {
+    return pts2(b, k, &upcg_flux_form);
+  }
+  std::vector<double> calcFormFac(const std::vector<double>& q2) {
+    std::vector<double> out(q2.size());
+    check(upcg_form_factor(h_, q2.data(), out.data(), q2.size()));
+    return out;
+  }
+  std::vector<double> calcBreakupProb(const std::vector<double>& b, int mode) {
+    std::vector<double> out(b.size());
+    check(upcg_breakup_prob(h_, b.data(), mode, out.data(), b.size()));
+    return out;
+  }
+  std::vector<double> calcTwoPhotonLumi(const std::vector<double>& m, const std::vector<double>& y) {
+    if (m.size() != y.size()) throw Error(UPCG_ERR_ARG, "m and y differ in length");
+    std::vector<double> out(m.size());
+    check(upcg_two_photon_lumi(h_, m.data(), y.data(), out.data(), nullptr, m.size()));
+    return out;
+  }
+  // hD2LDMDY of prepareTwoPhotonLumi: [nm][ny], L dm dy
+  std::vector<double> lumiTable(size_t n) {
+    std::vector<double> out(n);
+    check(upcg_lumi_table(h_, out.data(), n, nullptr));
+    return out;
+  }
+  // nucCSYM of calcNucCrossSectionYM: [ny][nm] (nb) and the total (mb)
+  std::vector<double> calcNucCrossSectionYM(size_t n, double* tot_mb) {
+    std::vector<double> out(n);
+    check(upcg_nuc_cs_ym(h_, out.data(), n, tot_mb));
+    return out;
+  }
+
+ private:
+  using Pts2 = int (*)(upcg_generator*, const double*, const double*, double*, size_t);
+  std::vector<double> pts2(const std::vector<double>& b, const std::vector<double>& k, Pts2 f) {
+    if (b.size() != k.size()) throw Error(UPCG_ERR_ARG, "b and k differ in length");
+    std::vector<double> out(b.size());
+    check(f(h_, b.data(), k.data(), out.data(), b.size()));
+    return out;
+  }
+  upcg_generator* h_;
+};
+
+}  // namespace upcgen_gb300
+
+#endif  // UPCGEN_GB300_HPP_

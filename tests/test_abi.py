@@ -63,3 +63,47 @@ def test_compute_without_gpu_fails_loudly(ug):
     g = ug.UpcGenerator({"BINS_M": 3, "BINS_Y": 3})
     with pytest.raises(ug.UpcgError):
         g.init()
+
+
+FACADE_PROGRAM = r"""
+#include <cstdio>
+#include "upcgen_gb300.hpp"
+int main() {
+  using namespace upcgen_gb300;
+  UpcGenerator gen;
+  gen.setParameterValue("PROC_ID", "13");
+  gen.setParameterValue("BINS_M", "11");
+  gen.setCollisionSystem(5360.f, 82, 208);
+  int pdg = 0, charged = 0;
+  check(upcg_particle_pdg(gen.handle(), &pdg, &charged));
+  int thrown = 0;
+  try {
+    gen.setParameterValue("BINS_M", "not-a-number");
+  } catch (const Error& e) {
+    thrown = e.code() == UPCG_ERR_ARG;
+  }
+  std::printf("%d %d %d\n", pdg, charged, thrown);
+  return 0;
+}
+"""
+
+
+def test_cpp_facade_compiles_and_configures(ug, tmp_path):
+    """include/upcgen_gb300.hpp: the reference's class names over the C ABI
+    (configuration only -- no GPU here)."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = tmp_path / "facade.cpp"
+    src.write_text(FACADE_PROGRAM)
+    exe = tmp_path / "facade"
+    lib = ug.library_path
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src),
+                        lib, f"-Wl,-rpath,{os.path.dirname(lib)}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == ["13", "1", "1"]

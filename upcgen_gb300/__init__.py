@@ -35,7 +35,7 @@ ABI_SYMBOLS = [
     "upcg_generate_events_device", "upcg_generate_event", "upcg_philox",
     "upcg_last_timings", "upcg_qags_stats", "upcg_last_error", "upcg_version",
     "upcg_selftest_contract", "upcg_fast_flux_table", "upcg_kernel_launches",
-    "upcg_flux_form_device_noalloc",
+    "upcg_flux_form_device_noalloc", "upcg_copy_bytes", "upcg_particle_pdg",
 ]
 
 
@@ -83,6 +83,8 @@ def load_library(path=None):
         "upcg_fast_flux_table": [vp, vp, sz, vp],
         "upcg_kernel_launches": [C.POINTER(u64)],
         "upcg_flux_form_device_noalloc": [vp, vp, vp, vp, sz, vp],
+        "upcg_copy_bytes": [C.POINTER(u64), C.POINTER(u64)],
+        "upcg_particle_pdg": [vp, C.POINTER(i), C.POINTER(i)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -120,6 +122,14 @@ def kernel_launches():
     n = C.c_uint64()
     _check(L.upcg_kernel_launches(C.byref(n)))
     return n.value
+
+
+def copy_bytes():
+    """(host-to-device, device-to-host) bytes the library has copied so far."""
+    L = load_library()
+    a, b = C.c_uint64(), C.c_uint64()
+    _check(L.upcg_copy_bytes(C.byref(a), C.byref(b)))
+    return a.value, b.value
 
 
 def philox(seed, counter0, n):

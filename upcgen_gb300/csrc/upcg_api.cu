@@ -32,6 +32,26 @@ unsigned long long launch_count() { return g_launches.load(std::memory_order_rel
 }  // namespace upcg
 
 namespace {
+// host <-> device bytes the library has copied (upcg_copy_bytes)
+std::atomic<unsigned long long> g_h2d{0}, g_d2h{0};
+
+void count_copy(size_t n, cudaMemcpyKind k) {
+  if (k == cudaMemcpyHostToDevice) g_h2d.fetch_add(n, std::memory_order_relaxed);
+  if (k == cudaMemcpyDeviceToHost) g_d2h.fetch_add(n, std::memory_order_relaxed);
+}
+
+cudaError_t mcpy(void* dst, const void* src, size_t n, cudaMemcpyKind k, cudaStream_t s) {
+  count_copy(n, k);
+  return cudaMemcpyAsync(dst, src, n, k, s);
+}
+
+cudaError_t mcpy_sync(void* dst, const void* src, size_t n, cudaMemcpyKind k) {
+  count_copy(n, k);
+  return cudaMemcpy(dst, src, n, k);
+}
+}  // namespace
+
+namespace {
 
 thread_local std::string g_err;
 
@@ -425,9 +445,9 @@ int upcg_generator::build_tables() {
   // spline at min(b, 20))
   CK(bu_tab.ensure(4 * kBreakupTabMax));
   CK(ntab.ensure(1));
-  CK(cudaMemcpyAsync(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double),
+  CK(mcpy(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double),
                      cudaMemcpyHostToDevice, side[1]));
-  CK(cudaMemcpyAsync(ntab.p, &bu_nt, sizeof(int), cudaMemcpyHostToDevice, side[1]));
+  CK(mcpy(ntab.p, &bu_nt, sizeof(int), cudaMemcpyHostToDevice, side[1]));
   const double dbb = (1000. - 1e-6) / 1000000;
   brk_n = (int)((20. - 1e-6) / dbb) + 257;
   CK(brk_y.ensure(brk_n));
@@ -468,7 +488,7 @@ int upcg_generator::build_lumi() {
     }
   }
   CK(mirror.ensure(ny));
-  CK(cudaMemcpyAsync(mirror.p, mir.data(), ny * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(mcpy(mirror.p, mir.data(), ny * sizeof(int), cudaMemcpyHostToDevice, s));
   LumiParams p = lumi_params();
   p.mirror = mirror.p;
   const int chunk = std::max(1, std::min(ncell, 65536) / ny) * ny;
@@ -521,9 +541,9 @@ int upcg_generator::build_lumi() {
       const double x20 = 20.;
       CK(pts_a.ensure(1));
       CK(pts_c.ensure(1));
-      CK(cudaMemcpyAsync(pts_a.p, &x20, sizeof x20, cudaMemcpyHostToDevice, s));
+      CK(mcpy(pts_a.p, &x20, sizeof x20, cudaMemcpyHostToDevice, s));
       CK(launch_spline_eval(p.brk, pts_a.p, pts_c.p, 1, s));
-      CK(cudaMemcpyAsync(&P20, pts_c.p, sizeof P20, cudaMemcpyDeviceToHost, s));
+      CK(mcpy(&P20, pts_c.p, sizeof P20, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
     }
     CK(fgaa32.ensure(p.gaa.n));
@@ -561,8 +581,8 @@ int upcg_generator::build_lumi() {
       CK(fq32.ensure((size_t)ftab.nw * ftab.nb));
       CK(fH.ensure((size_t)ftab.nw * nqn));
       CK(fJ.ensure((size_t)nqn * ftab.nb));
-      CK(cudaMemcpyAsync(fqn.p, qn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
-      CK(cudaMemcpyAsync(fwn.p, wn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
+      CK(mcpy(fqn.p, qn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
+      CK(mcpy(fwn.p, wn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
       ftab.qt = fq.p;
       ftab.qt32 = fq32.p;
     }
@@ -572,7 +592,7 @@ int upcg_generator::build_lumi() {
     std::vector<double> lnm2(nm);
     for (int im = 0; im < nm; ++im) lnm2[im] = std::log((p.mmin + p.dm * im) / 2.);
     CK(flnm2.ensure(nm));
-    CK(cudaMemcpyAsync(flnm2.p, lnm2.data(), nm * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(mcpy(flnm2.p, lnm2.data(), nm * sizeof(double), cudaMemcpyHostToDevice, s));
     c_far = 0.;
     for (int q = 0; q < 5; ++q) c_far += P20 * 1. * p.wk[q];
     spans.push_back({4, {b, mark()}});
@@ -591,7 +611,7 @@ int upcg_generator::build_lumi() {
       CK(launch_lumi_qags(p, c0, nc, flux.p, nq.p, work.p, ovf.p, ovf_cap, stats.p, nullptr, 0, s));
       spans.push_back({2, {b, mark()}});
       unsigned novf = 0;
-      CK(cudaMemcpyAsync(&novf, &stats.p->overflow, sizeof novf, cudaMemcpyDeviceToHost, s));
+      CK(mcpy(&novf, &stats.p->overflow, sizeof novf, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       if (novf > 0) {
         if ((int)novf > ovf_cap) return fail(UPCG_ERR_NUMERIC, "too many QAGS overflows (%u)", novf);
@@ -632,10 +652,10 @@ int upcg_generator::build_lumi() {
   for (auto e : ev) cudaEventDestroy(e);
   if (fast) {
     unsigned herr = 0;
-    CK(cudaMemcpy(&herr, ferr.p, sizeof herr, cudaMemcpyDeviceToHost));
+    CK(mcpy_sync(&herr, ferr.p, sizeof herr, cudaMemcpyDeviceToHost));
     if (herr) return fail(UPCG_ERR_CUDA, "tensor-core contraction timed out (code %u)", herr);
   }
-  CK(cudaMemcpyAsync(&last_stats, stats.p, sizeof last_stats, cudaMemcpyDeviceToHost, s));
+  CK(mcpy(&last_stats, stats.p, sizeof last_stats, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   lumi_ready = true;
   return UPCG_OK;
@@ -683,7 +703,7 @@ int upcg_generator::build_xsec() {
     const EventParams eg = event_params();  // with the guide buffers allocated
     CK(launch_guides(eg, cdf2.p, cdfz.p, ptcdf.p, guide2.p, guidez.p, guidept.p, s));
   }
-  CK(cudaMemcpyAsync(&totCS, tot.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(mcpy(&totCS, tot.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   cudaEventRecord(t1, s);
   CK(cudaEventSynchronize(t1));
   float ms = 0;
@@ -764,7 +784,7 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     CK(launch_events_write(e, cdf2.p, zc, ptcdf.p, next_cand, nc, mask.p, tile_off.p, done, n,
                            out, mbin, s));
     int64_t acc = 0;
-    CK(cudaMemcpyAsync(&acc, total.p, sizeof acc, cudaMemcpyDeviceToHost, s));
+    CK(mcpy(&acc, total.p, sizeof acc, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     acc_rate = std::max(1e-6, (double)acc / (double)nc);
     dry = acc == 0 ? dry + nc : 0;
@@ -776,7 +796,7 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
       k_find_cut<<<1, 32, 0, s>>>(tile_count.p, tile_off.p, mask.p, tiles, need, total.p + 1);
       CK(cudaGetLastError());
       int64_t cut = -1;
-      CK(cudaMemcpyAsync(&cut, total.p + 1, sizeof cut, cudaMemcpyDeviceToHost, s));
+      CK(mcpy(&cut, total.p + 1, sizeof cut, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       if (cut < 0) return fail(UPCG_ERR_CUDA, "event cut search failed");
       rej += (cut + 1) - need;
@@ -939,9 +959,9 @@ int upcg_lumi_table(upcg_generator* g, double* out, size_t n, double* out2) {
   if (!g->lumi_ready) return fail(UPCG_ERR_STATE, "luminosity not computed");
   const size_t need = (size_t)g->nm * g->ny;
   if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
-  CK(cudaMemcpyAsync(out, g->lumi.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(mcpy(out, g->lumi.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
   if (out2 && g->usePolarizedCS)
-    CK(cudaMemcpyAsync(out2, g->lumi2.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+    CK(mcpy(out2, g->lumi2.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
   CK(cudaStreamSynchronize(g->st()));
   return UPCG_OK;
 }
@@ -959,7 +979,7 @@ int upcg_nuc_cs_ym(upcg_generator* g, double* out, size_t n, double* tot_mb) {
   if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "cross section not computed");
   const size_t need = (size_t)g->nm * g->ny;
   if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
-  CK(cudaMemcpyAsync(out, g->cs.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(mcpy(out, g->cs.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
   CK(cudaStreamSynchronize(g->st()));
   if (tot_mb) *tot_mb = g->totCS;
   return UPCG_OK;
@@ -976,7 +996,7 @@ int upcg_cs_zm_table(upcg_generator* g, int flag, double* out, size_t n) {
   DBuf<double> tmp;
   CK(tmp.ensure(need));
   CK(launch_cs_zm(g->fold_params(), flag, tmp.p, g->st()));
-  CK(cudaMemcpyAsync(out, tmp.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(mcpy(out, tmp.p, need * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
   CK(cudaStreamSynchronize(g->st()));
   return UPCG_OK;
 }
@@ -985,15 +1005,15 @@ namespace {
 int points_in(upcg_generator* g, const double* a, const double* b, size_t n) {
   CK(g->pts_a.ensure(n));
   CK(g->pts_c.ensure(n));
-  CK(cudaMemcpyAsync(g->pts_a.p, a, n * sizeof(double), cudaMemcpyHostToDevice, g->st()));
+  CK(mcpy(g->pts_a.p, a, n * sizeof(double), cudaMemcpyHostToDevice, g->st()));
   if (b) {
     CK(g->pts_b.ensure(n));
-    CK(cudaMemcpyAsync(g->pts_b.p, b, n * sizeof(double), cudaMemcpyHostToDevice, g->st()));
+    CK(mcpy(g->pts_b.p, b, n * sizeof(double), cudaMemcpyHostToDevice, g->st()));
   }
   return UPCG_OK;
 }
 int points_out(upcg_generator* g, double* out, size_t n) {
-  CK(cudaMemcpyAsync(out, g->pts_c.p, n * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(mcpy(out, g->pts_c.p, n * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
   CK(cudaStreamSynchronize(g->st()));
   return UPCG_OK;
 }
@@ -1027,7 +1047,7 @@ int upcg_flux_form(upcg_generator* g, const double* b, const double* k, double* 
                         g->st()));
   rc = points_out(g, out, n);
   if (rc) return rc;
-  CK(cudaMemcpy(&g->last_stats, g->stats.p, sizeof(QagsStats), cudaMemcpyDeviceToHost));
+  CK(mcpy_sync(&g->last_stats, g->stats.p, sizeof(QagsStats), cudaMemcpyDeviceToHost));
   return UPCG_OK;
 }
 
@@ -1107,7 +1127,7 @@ int upcg_two_photon_lumi(upcg_generator* g, const double* m, const double* y, do
       CK(launch_lumi_qags(p, 0, 1, g->flux.p, g->nq.p, g->work.p, g->ovf.p, 1 << 10, g->stats.p,
                           nullptr, 0, g->st()));
       unsigned novf = 0;
-      CK(cudaMemcpyAsync(&novf, &g->stats.p->overflow, sizeof novf, cudaMemcpyDeviceToHost, g->st()));
+      CK(mcpy(&novf, &g->stats.p->overflow, sizeof novf, cudaMemcpyDeviceToHost, g->st()));
       CK(cudaStreamSynchronize(g->st()));
       if (novf > 0) {
         const int warps = 64;
@@ -1118,7 +1138,7 @@ int upcg_two_photon_lumi(upcg_generator* g, const double* m, const double* y, do
     }
     CK(launch_lumi_band(p, 0, 1, g->flux.p, g->pts_c.p, pol ? g->pts_c.p + 1 : nullptr, g->st()));
     double v[2] = {0, 0};
-    CK(cudaMemcpyAsync(v, g->pts_c.p, sizeof v, cudaMemcpyDeviceToHost, g->st()));
+    CK(mcpy(v, g->pts_c.p, sizeof v, cudaMemcpyDeviceToHost, g->st()));
     CK(cudaStreamSynchronize(g->st()));
     out[i] = v[0];
     if (pol) out2[i] = v[1];
@@ -1156,9 +1176,9 @@ int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t*
   int rc = upcg_generate_events_device(g, n, reinterpret_cast<upcg_event*>(g->evbuf.p),
                                        mbin ? g->mbinbuf.p : nullptr, rejected);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(out, g->evbuf.p, (size_t)n * sizeof(EventRecord), cudaMemcpyDeviceToHost, g->st()));
+  CK(mcpy(out, g->evbuf.p, (size_t)n * sizeof(EventRecord), cudaMemcpyDeviceToHost, g->st()));
   if (mbin)
-    CK(cudaMemcpyAsync(mbin, g->mbinbuf.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, g->st()));
+    CK(mcpy(mbin, g->mbinbuf.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, g->st()));
   CK(cudaStreamSynchronize(g->st()));
   return UPCG_OK;
 }
@@ -1180,8 +1200,8 @@ int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted) {
     CK(launch_events_all(e, g->cdf2.p, zc, g->ptcdf.p, g->next_cand, nb, rec.p, flg.p, g->st()));
     g->ev_batch.resize(nb);
     g->ev_flag.resize(nb);
-    CK(cudaMemcpyAsync(g->ev_batch.data(), rec.p, nb * sizeof(EventRecord), cudaMemcpyDeviceToHost, g->st()));
-    CK(cudaMemcpyAsync(g->ev_flag.data(), flg.p, nb, cudaMemcpyDeviceToHost, g->st()));
+    CK(mcpy(g->ev_batch.data(), rec.p, nb * sizeof(EventRecord), cudaMemcpyDeviceToHost, g->st()));
+    CK(mcpy(g->ev_flag.data(), flg.p, nb, cudaMemcpyDeviceToHost, g->st()));
     CK(cudaStreamSynchronize(g->st()));
     g->next_cand += (uint64_t)nb;
     g->ev_pos = 0;
@@ -1199,7 +1219,7 @@ int upcg_philox(uint64_t seed, uint64_t counter0, size_t n, uint32_t* out4) {
   DBuf<uint32_t> d;
   CK(d.ensure(4 * n));
   CK(launch_philox_dump(seed, counter0, (int64_t)n, d.p, 0));
-  CK(cudaMemcpy(out4, d.p, 4 * n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  CK(mcpy_sync(out4, d.p, 4 * n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
   return UPCG_OK;
 }
 
@@ -1224,7 +1244,7 @@ int upcg_fast_flux_table(upcg_generator* g, double* out, size_t n, double* grid)
     return fail(UPCG_ERR_STATE, "no fast-form flux table (fast method, FLUX_POINT 0, after init)");
   const size_t need = (size_t)512 * 256;
   if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
-  CK(cudaMemcpy(out, g->fq.p, need * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(mcpy_sync(out, g->fq.p, need * sizeof(double), cudaMemcpyDeviceToHost));
   const double ymx = std::max(std::fabs(g->ymin), std::fabs(g->ymax));
   const double kmin = g->mmin / 2. * std::exp(-ymx) * 0.9, kmax = g->mmax / 2. * std::exp(ymx) * 1.1;
   grid[0] = std::log(kmin);
@@ -1241,6 +1261,22 @@ int upcg_selftest_contract(int ncells, int P, uint64_t seed, double* max_rel, do
 }
 
 const char* upcg_last_error(void) { return g_err.c_str(); }
+int upcg_particle_pdg(upcg_generator* g, int* pdg, int* charged) {
+  if (!g || !pdg) return fail(UPCG_ERR_ARG, "null argument");
+  const int rc = g->setup_process();
+  if (rc) return rc;
+  *pdg = g->partPDG;
+  if (charged) *charged = g->isCharged ? 1 : 0;
+  return UPCG_OK;
+}
+
+int upcg_copy_bytes(uint64_t* h2d, uint64_t* d2h) {
+  if (!h2d || !d2h) return fail(UPCG_ERR_ARG, "null pointer");
+  *h2d = g_h2d.load(std::memory_order_relaxed);
+  *d2h = g_d2h.load(std::memory_order_relaxed);
+  return UPCG_OK;
+}
+
 int upcg_kernel_launches(uint64_t* n) {
   if (!n) return fail(UPCG_ERR_ARG, "null pointer");
   *n = launch_count();

@@ -164,7 +164,9 @@ __global__ void __launch_bounds__(192, 1) k_contract(const __grid_constant__ CUt
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int mt = blockIdx.x, nt = blockIdx.y;
+  // the N tiles of one 128-cell row block are adjacent in launch order, so
+  // the row block's A tiles come from DRAM once and from L2 for the others
+  const int nt = blockIdx.x, mt = blockIdx.y;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full_bar[s], 1);
@@ -811,7 +813,7 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
     attr = true;
   }
   ContractArgs args{P / BK, ncells, P, P / BN, a2, partial, d_err};
-  dim3 grid(ncells_pad / BM, P / BN);
+  dim3 grid(P / BN, ncells_pad / BM);
   note_launch();
   k_contract<<<grid, 192, kContractSmem, st>>>(tAh, tAl, tBh, tBl, args);
   return cudaGetLastError();
