@@ -99,6 +99,20 @@ int upcg_get_grid(const upcg_generator* g, double* mmin, double* mmax, int* nm,
                   double* ymin, double* ymax, int* ny, double* zmin, double* zmax,
                   int* nz);
 
+/* ---- sharding (no counterpart in the reference; the reference's OpenMP
+ * m-slices of prepareTwoPhotonLumi, src/UpcCrossSection.cpp:537-538, across
+ * processes) ------------------------------------------------------------- */
+/* compute only the luminosity m-rows [im0, im1) in upcg_init (im1 = -1: to the
+ * end); the other rows stay zero */
+int upcg_set_row_range(upcg_generator* g, int im0, int im1);
+/* install a full luminosity table (as upcg_lumi_table returns it; the
+ * pseudoscalar one in table2 when polarized) and build the cross section and
+ * samplers from it (upcg_compute_nucl_xsection) */
+int upcg_set_lumi_table(upcg_generator* g, const double* table, size_t n, const double* table2);
+/* start the candidate sequence of the event entries at this Philox counter
+ * (after upcg_init, which resets it to 0): disjoint ranges per shard */
+int upcg_set_candidate_offset(upcg_generator* g, uint64_t counter);
+
 /* ---- tables ------------------------------------------------------------ */
 /* hD2LDMDY of prepareTwoPhotonLumi (src/UpcCrossSection.cpp:506-571):
  * out[im*ny + iy] = L(m_im, y_iy) dm dy (bin (im+1, iy+1)); polarized:

@@ -36,6 +36,7 @@ ABI_SYMBOLS = [
     "upcg_last_timings", "upcg_qags_stats", "upcg_last_error", "upcg_version",
     "upcg_selftest_contract", "upcg_fast_flux_table", "upcg_kernel_launches",
     "upcg_flux_form_device_noalloc", "upcg_copy_bytes", "upcg_particle_pdg",
+    "upcg_set_row_range", "upcg_set_lumi_table", "upcg_set_candidate_offset",
 ]
 
 
@@ -85,6 +86,8 @@ def load_library(path=None):
         "upcg_flux_form_device_noalloc": [vp, vp, vp, vp, sz, vp],
         "upcg_copy_bytes": [C.POINTER(u64), C.POINTER(u64)],
         "upcg_particle_pdg": [vp, C.POINTER(i), C.POINTER(i)],
+        "upcg_set_row_range": [vp, i, i], "upcg_set_lumi_table": [vp, vp, sz, vp],
+        "upcg_set_candidate_offset": [vp, u64],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -260,6 +263,18 @@ class UpcGenerator:
 
     def setLumiMethod(self, method):
         _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1, "hybrid": 2}.get(method, method)))
+
+    # -- sharding over m-rows (upcgen_gb300.shard)
+    def setRowRange(self, im0, im1=-1):
+        _check(self._L.upcg_set_row_range(self._h, int(im0), int(im1)))
+
+    def setLumiTable(self, table, table2=None):
+        t = _arr(table).ravel()
+        t2 = _arr(table2).ravel() if table2 is not None else None
+        _check(self._L.upcg_set_lumi_table(self._h, _p(t), t.size, _p(t2) if t2 is not None else None))
+
+    def setCandidateOffset(self, counter):
+        _check(self._L.upcg_set_candidate_offset(self._h, int(counter)))
 
     # -- computation
     def init(self):

@@ -121,6 +121,7 @@ struct upcg_generator {
   std::string lumiDir = ".";
   bool lumiCache = false;
   int lumiMethod = 0;
+  int row_lo = 0, row_hi = -1;  // m-rows of the luminosity this handle computes (-1: all)
   // ---- derived
   double mPart = 0;
   int partPDG = 0;
@@ -477,6 +478,14 @@ int upcg_generator::build_lumi() {
   const int ncell = nm * ny;
   CK(lumi.ensure(ncell));
   if (usePolarizedCS) CK(lumi2.ensure(ncell));
+  // a shard computes the m-rows [row_lo, row_hi) and leaves the others zero
+  const int r0 = std::min(std::max(row_lo, 0), nm);
+  const int r1 = row_hi < 0 ? nm : std::min(std::max(row_hi, r0), nm);
+  const int cell_lo = r0 * ny, cell_hi = r1 * ny;
+  if (cell_lo > 0 || cell_hi < ncell) {
+    CK(cudaMemsetAsync(lumi.p, 0, (size_t)ncell * sizeof(double), s));
+    if (usePolarizedCS) CK(cudaMemsetAsync(lumi2.p, 0, (size_t)ncell * sizeof(double), s));
+  }
   // mirror rapidities (see LumiParams::mirror); chunks hold whole m-rows
   std::vector<int> mir(ny, -1);
   const double dy = (ymax - ymin) / ny;
@@ -597,8 +606,8 @@ int upcg_generator::build_lumi() {
     for (int q = 0; q < 5; ++q) c_far += P20 * 1. * p.wk[q];
     spans.push_back({4, {b, mark()}});
   }
-  for (int c0 = 0; c0 < ncell; c0 += chunk) {
-    const int nc = std::min(chunk, ncell - c0);
+  for (int c0 = cell_lo; c0 < cell_hi; c0 += chunk) {
+    const int nc = std::min(chunk, cell_hi - c0);
     int b = 0;
     if (node_flux) {
       b = mark();
@@ -1261,6 +1270,45 @@ int upcg_selftest_contract(int ncells, int P, uint64_t seed, double* max_rel, do
 }
 
 const char* upcg_last_error(void) { return g_err.c_str(); }
+int upcg_set_row_range(upcg_generator* g, int im0, int im1) {
+  if (!g || im0 < 0 || (im1 >= 0 && im1 < im0)) return fail(UPCG_ERR_ARG, "bad row range");
+  g->row_lo = im0;
+  g->row_hi = im1;
+  g->invalidate();
+  return UPCG_OK;
+}
+
+int upcg_set_lumi_table(upcg_generator* g, const double* table, size_t n, const double* table2) {
+  if (!g || !table) return fail(UPCG_ERR_ARG, "null argument");
+  const size_t ncell = (size_t)g->nm * g->ny;
+  if (n != ncell) return fail(UPCG_ERR_SIZE, "table has %zu cells, the grid %zu", n, ncell);
+  if (g->usePolarizedCS && !table2) return fail(UPCG_ERR_ARG, "polarized: two tables needed");
+  if (!g->tables_ready) {
+    const int rc = g->build_tables();
+    if (rc) return rc;
+  }
+  cudaStream_t s = g->st();
+  CK(g->lumi.ensure(ncell));
+  CK(mcpy(g->lumi.p, table, ncell * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (g->usePolarizedCS) {
+    CK(g->lumi2.ensure(ncell));
+    CK(mcpy(g->lumi2.p, table2, ncell * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  g->lumi_ready = true;
+  return g->build_xsec();
+}
+
+int upcg_set_candidate_offset(upcg_generator* g, uint64_t counter) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "upcg_init has not run");
+  g->next_cand = counter;
+  g->ev_batch.clear();
+  g->ev_flag.clear();
+  g->ev_pos = 0;
+  return UPCG_OK;
+}
+
 int upcg_particle_pdg(upcg_generator* g, int* pdg, int* charged) {
   if (!g || !pdg) return fail(UPCG_ERR_ARG, "null argument");
   const int rc = g->setup_process();
