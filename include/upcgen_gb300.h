@@ -79,7 +79,9 @@ int upcg_set_stream(upcg_generator* g, void* stream);
 /* Luminosity method: 0 = plain FP64 (default; the reference's quadrature),
  * 1 = fast form (flux tables + tensor-core contraction, <= 1e-4 relative to
  * the converged quadrature), 2 = the fast form's contraction on the plain
- * path's node fluxes (diagnostic) */
+ * path's node fluxes (diagnostic), 3 = grid form (point flux): fixed
+ * 4096-energy x 2048-radius grids, L = N G N^T as two tensor-core products
+ * (its own quadrature: the difference to the reference is stated by the tests) */
 int upcg_set_lumi_method(upcg_generator* g, int method);
 
 /* ---- initialisation (UpcGenerator::init) ------------------------------ */

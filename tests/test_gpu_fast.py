@@ -107,3 +107,27 @@ def test_fast_contraction_on_reference_fluxes(ug):
         out[meth] = g.lumiTable()
     rel = np.abs(out["hybrid"] / out["plain"] - 1)
     assert rel.max() < 2e-5, rel.max()
+
+
+def test_grid_form_config3(ug, oracle_mod):
+    """Luminosity method 3 (grid form, the precision form of the point-flux
+    configuration with XnXn breakup): a 4096 x 2048 flux matrix, G on 2048
+    radii in 1 .. 500 fm, L = N G N^T as two tensor-core products.  Its own
+    quadrature differs from the reference's per-cell midpoint rule; measured on
+    201 x 61: 1.7e-3 max / 6.1e-4 median relative on cells above 1e-5 of the
+    maximum, 4.4e-4 on sigma_tot.  The bounds below state that difference."""
+    p = dict(C1, BREAKUP_MODE=2)
+    g = ug.UpcGenerator(p)
+    g.setLumiMethod("grid")
+    g.init()
+    lumi = g.lumiTable()
+    _, tot = g.nucCSYM()
+    o = oracle_mod.Oracle(p, threads=os.cpu_count())
+    o.init_tables()
+    ref = o.lumi_table()
+    _, rtot, _ = o.nuc_cs_ym(ref)
+    big = np.abs(ref) >= 1e-5 * np.abs(ref).max()
+    rel = np.abs(lumi / ref - 1)[big]
+    assert rel.max() < 5e-3 and np.median(rel) < 1.5e-3, (rel.max(), np.median(rel))
+    assert abs(tot / rtot - 1) < 1e-3
+    assert g.timings()["contract_ms"] > 0

@@ -166,6 +166,10 @@ struct upcg_generator {
   DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq, fsides;
   DBuf<float> fs32, fq32;
   DBuf<float4> fgaa32, fbrk32, ff32;
+  // grid form: G, flux matrix, T = N G (bf16 hi/lo), Lg, row sums and tails
+  DBuf<uint16_t> gg_h, gg_l, gn_h, gn_l, gt_h, gt_l;
+  DBuf<float> g_lg;
+  DBuf<double> g_rowsum, g_tail;
   DBuf<unsigned> ferr;
   DBuf<int32_t> mbinbuf;
   int brk_n = 0;
@@ -213,6 +217,8 @@ struct upcg_generator {
   int setup_process();
   int build_tables();
   int build_lumi();
+  int build_lumi_grid();
+  int breakup_at_20(double* P20);
   int build_xsec();
   LumiParams lumi_params() const;
   FoldParams fold_params() const;
@@ -473,7 +479,110 @@ int upcg_generator::build_tables() {
   return UPCG_OK;
 }
 
+// the breakup probability at 20 fm (the survival kernel beyond b = 20 fm)
+int upcg_generator::breakup_at_20(double* P20) {
+  *P20 = 1.;
+  if (breakupMode == 1) return UPCG_OK;
+  cudaStream_t s = st();
+  const LumiParams p = lumi_params();
+  const double x20 = 20.;
+  CK(pts_a.ensure(1));
+  CK(pts_c.ensure(1));
+  CK(mcpy(pts_a.p, &x20, sizeof x20, cudaMemcpyHostToDevice, s));
+  CK(launch_spline_eval(p.brk, pts_a.p, pts_c.p, 1, s));
+  CK(mcpy(P20, pts_c.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return UPCG_OK;
+}
+
+// Luminosity method 3: the grid (precision) form of upcg_grid.cu -- a 4096 x
+// 2048 flux matrix on the table's photon-energy range and radii 1 .. 500 fm,
+// G on the radial grid, T = N G and Lg = T N^T on the tensor cores.
+int upcg_generator::build_lumi_grid() {
+  if (!isPoint) return fail(UPCG_ERR_PROCESS, "the grid form covers the point flux (FLUX_POINT 1)");
+  if (usePolarizedCS) return fail(UPCG_ERR_PROCESS, "the grid form covers the unpolarized luminosity");
+  cudaStream_t s = st();
+  const int ncell = nm * ny;
+  CK(lumi.ensure(ncell));
+  const LumiParams p = lumi_params();
+  const int nw = 4096, nr = 2048;
+  GridForm gf{};
+  gf.nw = nw;
+  gf.nr = nr;
+  const double ymx = std::max(std::fabs(ymin), std::fabs(ymax));
+  const double kmin = mmin / 2. * std::exp(-ymx) * 0.99, kmax = mmax / 2. * std::exp(ymx) * 1.01;
+  gf.lw0 = std::log(kmin);
+  gf.hw = (std::log(kmax) - gf.lw0) / (nw - 1);
+  gf.lr0 = std::log(1.0);
+  gf.hr = (std::log(500.0) - gf.lr0) / (nr - 1);
+  double P20 = 1.;
+  int rc = breakup_at_20(&P20);
+  if (rc) return rc;
+  gf.c_far = 0.;
+  for (int q = 0; q < 5; ++q) gf.c_far += P20 * 1. * p.wk[q];
+  std::vector<cudaEvent_t> ev(4);
+  for (auto& e : ev) {
+    cudaEventCreate(&e);
+  }
+  cudaEventRecord(ev[0], s);
+  // point-flux table S(ln x)
+  const int nk = flux_table_ktab_n();
+  CK(fk1.ensure(nk));
+  CK(fs32.ensure(nk));
+  FastFluxTables ftab{};
+  ftab.st = fk1.p;
+  ftab.st32 = fs32.p;
+  CK(build_flux_tables(p, &ftab, nullptr, nullptr, 0, nullptr, nullptr, nullptr, s));
+  double su0 = 0, su1 = 0;
+  flux_table_ktab_range(&su0, &su1);
+  gf.s32 = fs32.p;
+  gf.su0 = su0;
+  gf.sinv_h = (nk - 1) / (su1 - su0);
+  gf.sn = nk;
+  // G on the radial grid, the flux matrix
+  CK(gg_h.ensure((size_t)nr * nr));
+  CK(gg_l.ensure((size_t)nr * nr));
+  CK(fgaa32.ensure(p.gaa.n));
+  CK(fbrk32.ensure(breakupMode != 1 ? p.brk.n : 1));
+  CK(launch_fast_G(p, gf.lr0, gf.hr, nr, P20, fgaa32.p, fbrk32.p, gg_h.p, gg_l.p, s));
+  const size_t nwp = (size_t)(nw + 127) / 128 * 128;
+  CK(gn_h.ensure(nwp * nr));
+  CK(gn_l.ensure(nwp * nr));
+  CK(gt_h.ensure(nwp * nr));
+  CK(gt_l.ensure(nwp * nr));
+  CK(g_rowsum.ensure(nw));
+  CK(g_tail.ensure(nw));
+  CK(g_lg.ensure((size_t)nw * nw));
+  CK(launch_grid_flux(p, gf, gn_h.p, gn_l.p, g_rowsum.p, g_tail.p, s));
+  cudaEventRecord(ev[1], s);
+  CK(ferr.ensure(1));
+  CK(cudaMemsetAsync(ferr.p, 0, sizeof(unsigned), s));
+  CK(launch_gemm_bf16x3(gn_h.p, gn_l.p, gg_h.p, gg_l.p, nw, nr, nr, nullptr, gt_h.p, gt_l.p,
+                        ferr.p, s));
+  CK(launch_gemm_bf16x3(gt_h.p, gt_l.p, gn_h.p, gn_l.p, nw, nw, nr, g_lg.p, nullptr, nullptr,
+                        ferr.p, s));
+  cudaEventRecord(ev[2], s);
+  CK(launch_grid_cells(p, gf, g_lg.p, g_rowsum.p, g_tail.p, lumi.p, s));
+  cudaEventRecord(ev[3], s);
+  CK(cudaEventSynchronize(ev[3]));
+  float t01 = 0, t12 = 0, t03 = 0;
+  cudaEventElapsedTime(&t01, ev[0], ev[1]);
+  cudaEventElapsedTime(&t12, ev[1], ev[2]);
+  cudaEventElapsedTime(&t03, ev[0], ev[3]);
+  for (auto e : ev) cudaEventDestroy(e);
+  for (int k = 3; k < 8; ++k) timings[k] = 0;
+  timings[1] = t03;
+  timings[5] = t12;  // the two tensor-core products
+  timings[6] = t01;  // tables, G, flux matrix
+  unsigned herr = 0;
+  CK(mcpy_sync(&herr, ferr.p, sizeof herr, cudaMemcpyDeviceToHost));
+  if (herr) return fail(UPCG_ERR_CUDA, "tensor-core product timed out (code %u)", herr);
+  lumi_ready = true;
+  return UPCG_OK;
+}
+
 int upcg_generator::build_lumi() {
+  if (lumiMethod == 3) return build_lumi_grid();
   cudaStream_t s = st();
   const int ncell = nm * ny;
   CK(lumi.ensure(ncell));
@@ -910,7 +1019,7 @@ int upcg_set_stream(upcg_generator* g, void* stream) {
 }
 
 int upcg_set_lumi_method(upcg_generator* g, int method) {
-  if (!g || method < 0 || method > 2) return fail(UPCG_ERR_ARG, "bad luminosity method");
+  if (!g || method < 0 || method > 3) return fail(UPCG_ERR_ARG, "bad luminosity method");
   if (method != g->lumiMethod) g->invalidate();
   g->lumiMethod = method;
   return UPCG_OK;

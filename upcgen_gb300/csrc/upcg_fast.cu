@@ -150,6 +150,13 @@ struct ContractArgs {
   const float* a2;  // [cells_pad][P]
   float* partial;   // [cells][ntiles]
   unsigned* err;
+  // store epilogue (general product D = A B^T): when out_f32 or out_hi is set
+  // the D tile goes to memory instead of the row-dot with a2 -- FP32, or as a
+  // bf16 hi/lo pair that feeds a following product; rows < ncells, ld = ldo
+  float* out_f32;
+  __nv_bfloat16* out_hi;
+  __nv_bfloat16* out_lo;
+  int ldo;
 };
 
 __global__ void __launch_bounds__(192, 1) k_contract(const __grid_constant__ CUtensorMap tAh,
@@ -244,7 +251,35 @@ __global__ void __launch_bounds__(192, 1) k_contract(const __grid_constant__ CUt
     const int row = quad * 32 + lane;
     const int cell = mt * BM + row;
     float acc = 0.f;
-    if (ok) {
+    if (args.out_f32 || args.out_hi) {
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float v[16];
+        if (ok) tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, v);
+        if (!ok || cell >= args.ncells) continue;
+        const size_t o = (size_t)cell * args.ldo + nt * BN + c0;
+        if (args.out_f32) {
+          float4* d = reinterpret_cast<float4*>(args.out_f32 + o);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) d[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else {
+          uint32_t hw[8], lw[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+            const float2 f = __bfloat1622float2(h);
+            const __nv_bfloat162 l = __floats2bfloat162_rn(v[2 * q] - f.x, v[2 * q + 1] - f.y);
+            hw[q] = *reinterpret_cast<const uint32_t*>(&h);
+            lw[q] = *reinterpret_cast<const uint32_t*>(&l);
+          }
+          uint4* dh = reinterpret_cast<uint4*>(args.out_hi + o);
+          uint4* dl = reinterpret_cast<uint4*>(args.out_lo + o);
+          dh[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          dh[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+          dl[0] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+          dl[1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+        }
+      }
+    } else if (ok) {
       const float* a2 = args.a2 + (size_t)cell * args.P + nt * BN;
       for (int c0 = 0; c0 < BN; c0 += 16) {
         float v[16];
@@ -259,7 +294,8 @@ __global__ void __launch_bounds__(192, 1) k_contract(const __grid_constant__ CUt
         }
       }
     }
-    if (cell < args.ncells) args.partial[(size_t)cell * args.ntiles + nt] = ok ? acc : 0.f;
+    if (!args.out_f32 && !args.out_hi && cell < args.ncells)
+      args.partial[(size_t)cell * args.ntiles + nt] = ok ? acc : 0.f;
   }
   tc_fence_before();
   __syncthreads();
@@ -812,8 +848,36 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  ContractArgs args{P / BK, ncells, P, P / BN, a2, partial, d_err};
+  ContractArgs args{P / BK, ncells, P, P / BN, a2, partial, d_err, nullptr, nullptr, nullptr, 0};
   dim3 grid(P / BN, ncells_pad / BM);
+  note_launch();
+  k_contract<<<grid, 192, kContractSmem, st>>>(tAh, tAl, tBh, tBl, args);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, const void* bl,
+                               int M, int N, int K, float* out_f32, void* out_hi, void* out_lo,
+                               unsigned* d_err, cudaStream_t st) {
+  // A [M_pad][K], B [N][K] (K contiguous, bf16 hi/lo); D = A B^T, M_pad = M
+  // rounded up to 128 rows of A (the rows beyond M are read, not stored)
+  if (M <= 0 || N % BN != 0 || K % BK != 0 || (!out_f32 && !(out_hi && out_lo)))
+    return cudaErrorInvalidValue;
+  const int Mpad = (M + BM - 1) / BM * BM;
+  CUtensorMap tAh, tAl, tBh, tBl;
+  cudaError_t e;
+  if ((e = make_map(&tAh, ah, Mpad, K, BM)) != cudaSuccess) return e;
+  if ((e = make_map(&tAl, al, Mpad, K, BM)) != cudaSuccess) return e;
+  if ((e = make_map(&tBh, bh, N, K, BN)) != cudaSuccess) return e;
+  if ((e = make_map(&tBl, bl, N, K, BN)) != cudaSuccess) return e;
+  static bool attr = false;
+  if (!attr) {
+    e = cudaFuncSetAttribute(k_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  ContractArgs args{K / BK, M, K, N / BN, nullptr, nullptr, d_err, out_f32,
+                    static_cast<__nv_bfloat16*>(out_hi), static_cast<__nv_bfloat16*>(out_lo), N};
+  dim3 grid(N / BN, Mpad / BM);
   note_launch();
   k_contract<<<grid, 192, kContractSmem, st>>>(tAh, tAl, tBh, tBl, args);
   return cudaGetLastError();
@@ -910,6 +974,10 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
 }
 
 int flux_table_ktab_n() { return kKTabN; }
+void flux_table_ktab_range(double* u0, double* u1) {
+  *u0 = kKTabU0;
+  *u1 = kKTabU1;
+}
 
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
                                double c_far, const float* partial, const void* far_term,

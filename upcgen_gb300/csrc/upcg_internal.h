@@ -47,6 +47,24 @@ struct QagsStats {
 void note_launch();
 unsigned long long launch_count();
 
+// grid (precision) form of the luminosity, point flux: see upcg_grid.cu
+struct GridForm {
+  int nw, nr;                // photon-energy and radial grid points
+  double lw0, hw, lr0, hr;   // ln w = lw0 + i hw, ln r = lr0 + j hr
+  const float* s32;          // point-flux table S(ln x)
+  double su0, sinv_h;        // its grid: index = (ln x - su0) * sinv_h
+  int sn;
+  double c_far;              // survival kernel beyond 20 fm
+};
+// flux matrix N[w][r] b^2 dln(b) weights (bf16 hi/lo, rows padded to 128) and
+// per-row sums / analytic tails beyond the last radius (FP64)
+cudaError_t launch_grid_flux(const LumiParams& p, const GridForm& gf, void* nh, void* nl,
+                             double* rowsum, double* tail, cudaStream_t st);
+// cells of the table from Lg[w1][w2] (FP32) and the row sums / tails
+cudaError_t launch_grid_cells(const LumiParams& p, const GridForm& gf, const float* lg,
+                              const double* rowsum, const double* tail, double* lumi,
+                              cudaStream_t st);
+
 // tables
 cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
                                  double4* d_coef, cudaStream_t st);
@@ -111,6 +129,8 @@ struct FastFluxTables {
   double lw0, hw, lb0, hb;
 };
 int flux_table_ktab_n();
+// the point-flux table's grid: S at u0 + i (u1 - u0) / (n - 1), u = ln x
+void flux_table_ktab_range(double* u0, double* u1);
 // d_part: flux_table_part_doubles(nw, nb) doubles of split-K scratch
 int flux_table_part_doubles(int nw, int nb);
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
@@ -124,6 +144,13 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
 // bytes of the per-(cell, photon) constants (d_sides holds 2 per cell);
 // far_term holds one float4 per cell
 size_t fast_side_bytes();
+// General product on tcgen05, three-term bf16 split with FP32 accumulation:
+// D[M][N] = A B^T for A [ceil128(M)][K], B [N][K] (K contiguous, bf16 hi/lo
+// pairs; N % 256 == 0, K % 64 == 0).  D goes to out_f32 (FP32) or to
+// out_hi / out_lo (a bf16 hi/lo pair for a following product), ld = N.
+cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, const void* bl,
+                               int M, int N, int K, float* out_f32, void* out_hi, void* out_lo,
+                               unsigned* d_err, cudaStream_t st);
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
                             const float* a2, int ncells_pad, int ncells, int P, float* partial,
                             unsigned* d_err, cudaStream_t st);
