@@ -164,8 +164,8 @@ def cpu_baseline_sample(workload, seconds=15.0):
 # DRAM traffic per launch from one ncu capture of the c2 workload (65,536-cell
 # chunk; profiles/k_contract_c2.md, profiles/k_fast_project_c2.md), scaled by
 # cells for the other chunk: bytes per cell
-CONTRACT_DRAM_BYTES_PER_CELL = None
-PROJECT_DRAM_BYTES_PER_CELL = None
+CONTRACT_DRAM_BYTES_PER_CELL = (460.295168e6 + 4.016384e6) / 55680  # read + write, one launch
+PROJECT_DRAM_BYTES_PER_CELL = (9.432832e6 + 394.498816e6) / 55680
 
 
 def main():
@@ -343,13 +343,16 @@ def main():
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "note": f"algorithmic 2*cells*P^2 = {alg_flops:.3e} FLOP per table over "
                              f"{nlaunch_contract} launches (the hi/lo split issues it 3x); "
-                             f"peak = {pk_kind} bf16 burst; traffic = DRAM bytes per launch"},
+                             f"peak = {pk_kind} bf16 burst; traffic = DRAM bytes per launch "
+                             f"(profiles/k_contract_c2.md)"},
         "roofline_projection": {
             "kernel": "k_fast_sides + k_fast_project", "bound": "hbm",
             "achieved": 8.0 * P * cells / (ms_project * 1e-3) / 1e9 if ms_project else None,
             "peak": pk_vals.get("hbm_gbs", 6800.0), "unit": "GB/s",
+            "traffic": PROJECT_DRAM_BYTES_PER_CELL * cells / nlaunch_contract,
             "note": "algorithmic bytes = the 8 KB per cell of contraction operands written "
-                    "(A1 bf16 hi + lo, A2 fp32); project_ms also holds the G and flux-table builds"},
+                    "(A1 bf16 hi + lo, A2 fp32); project_ms also holds the G and flux-table builds; "
+                    "traffic = DRAM bytes per launch (profiles/k_fast_project_c2.md)"},
         "gpu_launches": n_launch,
         "clocks": clk,
     }

@@ -190,6 +190,41 @@ int upcg_generate_events_device(upcg_generator* g, int64_t n, upcg_event* out_de
  * upcg_generate_events. */
 int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted);
 
+/* ---- learned flux surrogate (no counterpart in the reference) -------------
+ * An MLP (inputs ln w, ln b, R, a, ln g; four hidden layers of 128 SiLU; BF16
+ * weights, FP32 accumulation) for y = ln(Q_ff / Q_pt), the log-ratio of
+ * fluxForm's form-factor amplitude (src/UpcCrossSection.cpp:181-218) to the
+ * point-charge one, trained on the GPU by the library's own forward, backward
+ * and Adam kernels on points labelled by the form-factor quadrature.
+ * Training box: w in [1e-3, 1e2] GeV, b in [0.049 R, 500] fm, R in [5, 7.5]
+ * fm, a in [0.40, 0.60] fm, g in [100, 3000].  Inputs x are normalised to
+ * [-1, 1] over the box (upcg_mlp_box gives its bounds). */
+typedef struct upcg_mlp upcg_mlp;
+int upcg_mlp_create(upcg_mlp** out, uint64_t seed);
+int upcg_mlp_destroy(upcg_mlp* h);
+/* {ln w lo, ln w hi, b lo / R, ln b hi, R lo, R hi, a lo, a hi, g lo, g hi} */
+int upcg_mlp_box(const upcg_mlp* h, float* out, size_t n);
+/* n training points and labels on the device (weights 0 where k b / hc > 30) */
+int upcg_mlp_make_data(upcg_mlp* h, int64_t n, uint64_t seed);
+int upcg_mlp_get_data(upcg_mlp* h, int64_t i0, int64_t n, float* x, float* y, float* w);
+/* Adam over the points: epochs x (n / batch) steps, cosine-decayed step size;
+ * last_loss = weighted mean squared error of the last batch */
+int upcg_mlp_train(upcg_mlp* h, int epochs, int batch, float lr, double* last_loss);
+/* gradient of sum_i w_i (y(x_i) - y_i)^2 / n at the current parameters (no
+ * update): grads[upcg_mlp parameter count] */
+int upcg_mlp_gradients(upcg_mlp* h, const float* x, const float* y, const float* w, int n,
+                       float* grads, size_t ng, double* loss);
+/* FP32 master parameters: W1[128][5] b1 W2[128][128] b2 W3 b3 W4 b4 W5[128] b5 */
+int upcg_mlp_params(upcg_mlp* h, float* out, size_t n);
+int upcg_mlp_set_params(upcg_mlp* h, const float* in, size_t n);
+int upcg_mlp_predict(upcg_mlp* h, const float* x, int n, float* y);
+int upcg_mlp_timings(const upcg_mlp* h, double* labels_ms, double* train_ms);
+/* luminosity method 4: the fast form with the Q(w, b) table rows inside the
+ * surrogate's box from the MLP, the rest from the quadrature; the handle keeps
+ * the pointer (the surrogate must outlive its use) */
+int upcg_set_flux_surrogate(upcg_generator* g, upcg_mlp* h);
+int upcg_surrogate_rows(const upcg_generator* g, int* rows);
+
 /* ---- diagnostics --------------------------------------------------------- */
 /* Philox4x32-10 uniforms of the event stream (seed, counter) -- for tests */
 int upcg_philox(uint64_t seed, uint64_t counter0, size_t n, uint32_t* out4);

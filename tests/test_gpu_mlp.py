@@ -1,0 +1,158 @@
+"""The learned flux surrogate: gradients of the library's fused backward
+kernel against an FP64 restatement of the network, labels against the
+oracle's flux quadrature, training on the GPU, and what the trained network
+gains in the fast form (luminosity method 4)."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HC = 0.1973269718
+
+
+def bf16(a):
+    """Round-to-nearest-even to bfloat16, as float32."""
+    u = np.asarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+SHAPES = [("W1", (128, 5)), ("b1", (128,)), ("W2", (128, 128)), ("b2", (128,)),
+          ("W3", (128, 128)), ("b3", (128,)), ("W4", (128, 128)), ("b4", (128,)),
+          ("W5", (128,)), ("b5", (1,))]
+
+
+def unpack(p):
+    out, o = {}, 0
+    for k, sh in SHAPES:
+        n = int(np.prod(sh))
+        out[k] = np.asarray(p[o:o + n], dtype=np.float64).reshape(sh)
+        o += n
+    return out
+
+
+def pack(d):
+    return np.concatenate([d[k].ravel() for k, _ in SHAPES])
+
+
+def silu(z):
+    return z / (1 + np.exp(-z))
+
+
+def silu_d(z):
+    s = 1 / (1 + np.exp(-z))
+    return s * (1 + z * (1 - s))
+
+
+def ref_grad(p, x, y, w):
+    """FP64 forward / backward with the kernels' bf16 weights and FP32 biases."""
+    P = unpack(p)
+    W = {k: bf16(P[k]).astype(np.float64) for k in ("W1", "W2", "W3", "W4", "W5")}
+    x = x.astype(np.float64)
+    z1 = x @ W["W1"].T + P["b1"]
+    z2 = silu(z1) @ W["W2"].T + P["b2"]
+    z3 = silu(z2) @ W["W3"].T + P["b3"]
+    z4 = silu(z3) @ W["W4"].T + P["b4"]
+    yh = silu(z4) @ W["W5"] + P["b5"][0]
+    n = len(y)
+    r = yh - y
+    loss = np.sum(w * r * r) / n
+    g = 2 * w * r / n
+    G = {"W5": silu(z4).T @ g, "b5": np.array([g.sum()])}
+    d4 = g[:, None] * W["W5"][None, :] * silu_d(z4)
+    G["W4"], G["b4"] = d4.T @ silu(z3), d4.sum(0)
+    d3 = (d4 @ W["W4"]) * silu_d(z3)
+    G["W3"], G["b3"] = d3.T @ silu(z2), d3.sum(0)
+    d2 = (d3 @ W["W3"]) * silu_d(z2)
+    G["W2"], G["b2"] = d2.T @ silu(z1), d2.sum(0)
+    d1 = (d2 @ W["W2"]) * silu_d(z1)
+    G["W1"], G["b1"] = d1.T @ x, d1.sum(0)
+    return pack(G), loss
+
+
+def test_gradients_vs_fp64_restatement(ug):
+    s = ug.FluxSurrogate(seed=11)
+    rng = np.random.default_rng(5)
+    n = 53  # not a multiple of the 16-sample CTA tile
+    x = rng.uniform(-1, 1, (n, 5)).astype(np.float32)
+    y = rng.normal(0, 0.5, n).astype(np.float32)
+    w = (rng.uniform(size=n) > 0.2).astype(np.float32)
+    g, loss = s.gradients(x, y, w)
+    gr, lr = ref_grad(s.params(), x, y, w)
+    assert loss == pytest.approx(lr, rel=1e-4)
+    o = 0
+    for k, sh in SHAPES:
+        m = int(np.prod(sh))
+        a, b = g[o:o + m], gr[o:o + m]
+        assert np.max(np.abs(a - b)) <= 2e-4 * np.max(np.abs(b)) + 1e-9, k
+        o += m
+
+
+def test_labels_vs_oracle_quadrature(ug, oracle_mod):
+    """Training labels for b <= 2R: ln(Q_ff / Q_pt) with Q_ff from the oracle's
+    converged fluxForm quadrature at the point's nucleus."""
+    from scipy import special
+    s = ug.FluxSurrogate(seed=3)
+    s.make_data(4096, seed=9)
+    x, y, w = s.data(0, 4096)
+    bx = s.box()
+    lw = (x[:, 0] + 1) / 2 * (bx["lw_hi"] - bx["lw_lo"]) + bx["lw_lo"]
+    R = (x[:, 2] + 1) / 2 * (bx["R_hi"] - bx["R_lo"]) + bx["R_lo"]
+    a = (x[:, 3] + 1) / 2 * (bx["a_hi"] - bx["a_lo"]) + bx["a_lo"]
+    lg = (x[:, 4] + 1) / 2 * (np.log(bx["g_hi"]) - np.log(bx["g_lo"])) + np.log(bx["g_lo"])
+    lb_lo = np.log(bx["bf_lo"] * bx["R_lo"])
+    lb = (x[:, 1] + 1) / 2 * (bx["lb_hi"] - lb_lo) + lb_lo
+    pick = np.where((w > 0) & (np.exp(lb) <= 2 * R))[0][:6]
+    assert len(pick) == 6
+    for i in pick:
+        g = float(np.exp(lg[i]))
+        sqrts = 2 * 0.9382720813 * g
+        o = oracle_mod.Oracle({"PROC_ID": 13, "FLUX_POINT": 0, "WS_R": float(R[i]), "WS_A": float(a[i]),
+                               "SQRTS": sqrts, "ORACLE_FLUX_EPS": 1e-10})
+        o.init_tables()
+        k, b = float(np.exp(lw[i])), float(np.exp(lb[i]))
+        n_ff = o.flux_form(b, k)
+        kap = k / g
+        q_pt = kap * special.k1(kap * b / HC)
+        fac = 82 * 82 / 137.035999074 / np.pi ** 2 / HC ** 2
+        y_ref = 0.5 * np.log(n_ff * k / fac) - np.log(q_pt)
+        assert y[i] == pytest.approx(y_ref, abs=2e-4), (i, b, k)
+
+
+def _trained(ug, n=1 << 20, epochs=6):
+    s = ug.FluxSurrogate(seed=7)
+    s.make_data(n, seed=21)
+    s.train(epochs, batch=4096, lr=2e-3)
+    return s
+
+
+def test_training_and_surrogate_luminosity(ug):
+    """After training on 2^20 points the network follows held-out labels; in
+    the fast form its Q table rows replace the quadrature's inside the box."""
+    s = _trained(ug)
+    held = ug.FluxSurrogate(seed=8)
+    held.make_data(1 << 16, seed=99)
+    x, y, w = held.data(0, 1 << 16)
+    pred = s.predict(x)
+    err = np.abs(pred - y)[w > 0]
+    rms = float(np.sqrt(np.mean(err ** 2)))
+    assert rms < 2e-2, rms
+    P = {"NUCLEUS_Z": 82, "NUCLEUS_A": 208, "WS_R": 6.68, "WS_A": 0.447, "SQRTS": 5020,
+         "PROC_ID": 15, "FLUX_POINT": 0, "BREAKUP_MODE": 2, "MMIN": 3.56, "MMAX": 50,
+         "BINS_M": 41, "YMIN": -6, "YMAX": 6, "BINS_Y": 25}
+    ref = ug.UpcGenerator(P)
+    ref.setLumiMethod("fast")
+    ref.init()
+    g = ug.UpcGenerator(P)
+    g.setFluxSurrogate(s)
+    g.setLumiMethod("surrogate")
+    g.init()
+    assert g.surrogateRows() >= 256
+    a, b = g.lumiTable(), ref.lumiTable()
+    big = np.abs(b) >= 1e-5 * np.abs(b).max()
+    rel = np.abs(a / b - 1)[big]
+    _, ta = g.nucCSYM()
+    _, tb = ref.nucCSYM()
+    assert np.median(rel) < 5e-3 and abs(ta / tb - 1) < 5e-3, (np.median(rel), rel.max(), ta / tb - 1)

@@ -37,6 +37,10 @@ ABI_SYMBOLS = [
     "upcg_selftest_contract", "upcg_fast_flux_table", "upcg_kernel_launches",
     "upcg_flux_form_device_noalloc", "upcg_copy_bytes", "upcg_particle_pdg",
     "upcg_set_row_range", "upcg_set_lumi_table", "upcg_set_candidate_offset",
+    "upcg_mlp_create", "upcg_mlp_destroy", "upcg_mlp_box", "upcg_mlp_make_data",
+    "upcg_mlp_get_data", "upcg_mlp_train", "upcg_mlp_gradients", "upcg_mlp_params",
+    "upcg_mlp_set_params", "upcg_mlp_predict", "upcg_mlp_timings", "upcg_set_flux_surrogate",
+    "upcg_surrogate_rows",
 ]
 
 
@@ -88,6 +92,14 @@ def load_library(path=None):
         "upcg_particle_pdg": [vp, C.POINTER(i), C.POINTER(i)],
         "upcg_set_row_range": [vp, i, i], "upcg_set_lumi_table": [vp, vp, sz, vp],
         "upcg_set_candidate_offset": [vp, u64],
+        "upcg_mlp_create": [C.POINTER(vp), u64], "upcg_mlp_destroy": [vp],
+        "upcg_mlp_box": [vp, vp, sz], "upcg_mlp_make_data": [vp, i64, u64],
+        "upcg_mlp_get_data": [vp, i64, i64, vp, vp, vp],
+        "upcg_mlp_train": [vp, i, i, C.c_float, dp],
+        "upcg_mlp_gradients": [vp, vp, vp, vp, i, vp, sz, dp],
+        "upcg_mlp_params": [vp, vp, sz], "upcg_mlp_set_params": [vp, vp, sz],
+        "upcg_mlp_predict": [vp, vp, i, vp], "upcg_mlp_timings": [vp, dp, dp],
+        "upcg_set_flux_surrogate": [vp, vp], "upcg_surrogate_rows": [vp, C.POINTER(i)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -141,6 +153,85 @@ def philox(seed, counter0, n):
     out = np.zeros((n, 4), dtype=np.uint32)
     _check(L.upcg_philox(seed, counter0, n, _p(out)))
     return out
+
+
+class FluxSurrogate:
+    """The learned flux surrogate (upcg_mlp_*): y = ln(Q_ff / Q_pt) from
+    normalised (ln w, ln b, R, a, ln g)."""
+
+    N_PARAMS = 5 * 128 + 128 + 3 * (128 * 128 + 128) + 128 + 1
+
+    def __init__(self, seed=1):
+        self._L = load_library()
+        self._h = C.c_void_p()
+        _check(self._L.upcg_mlp_create(C.byref(self._h), int(seed)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.upcg_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def box(self):
+        b = np.zeros(10, dtype=np.float32)
+        _check(self._L.upcg_mlp_box(self._h, _p(b), 10))
+        keys = ["lw_lo", "lw_hi", "bf_lo", "lb_hi", "R_lo", "R_hi", "a_lo", "a_hi", "g_lo", "g_hi"]
+        return dict(zip(keys, (float(v) for v in b)))
+
+    def normalise(self, w, b, R, a, g):
+        bx = self.box()
+        u = np.empty((np.size(w), 5), dtype=np.float32)
+        lb_lo = np.log(bx["bf_lo"] * bx["R_lo"])
+        u[:, 0] = 2 * (np.log(w) - bx["lw_lo"]) / (bx["lw_hi"] - bx["lw_lo"]) - 1
+        u[:, 1] = 2 * (np.log(b) - lb_lo) / (bx["lb_hi"] - lb_lo) - 1
+        u[:, 2] = 2 * (np.asarray(R) - bx["R_lo"]) / (bx["R_hi"] - bx["R_lo"]) - 1
+        u[:, 3] = 2 * (np.asarray(a) - bx["a_lo"]) / (bx["a_hi"] - bx["a_lo"]) - 1
+        u[:, 4] = 2 * (np.log(g) - np.log(bx["g_lo"])) / (np.log(bx["g_hi"]) - np.log(bx["g_lo"])) - 1
+        return u
+
+    def make_data(self, n, seed=1):
+        _check(self._L.upcg_mlp_make_data(self._h, int(n), int(seed)))
+
+    def data(self, i0, n):
+        x = np.zeros((n, 5), dtype=np.float32)
+        y = np.zeros(n, dtype=np.float32)
+        w = np.zeros(n, dtype=np.float32)
+        _check(self._L.upcg_mlp_get_data(self._h, int(i0), int(n), _p(x), _p(y), _p(w)))
+        return x, y, w
+
+    def train(self, epochs, batch=4096, lr=2e-3):
+        loss = C.c_double()
+        _check(self._L.upcg_mlp_train(self._h, int(epochs), int(batch), C.c_float(lr), C.byref(loss)))
+        return loss.value
+
+    def gradients(self, x, y, w):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        g = np.zeros(self.N_PARAMS, dtype=np.float32)
+        loss = C.c_double()
+        _check(self._L.upcg_mlp_gradients(self._h, _p(x), _p(y), _p(w), len(y), _p(g), g.size,
+                                          C.byref(loss)))
+        return g, loss.value
+
+    def params(self):
+        p = np.zeros(self.N_PARAMS, dtype=np.float32)
+        _check(self._L.upcg_mlp_params(self._h, _p(p), p.size))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(self._L.upcg_mlp_set_params(self._h, _p(p), p.size))
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros(len(x), dtype=np.float32)
+        _check(self._L.upcg_mlp_predict(self._h, _p(x), len(x), _p(y)))
+        return y
+
+    def timings(self):
+        a, b = C.c_double(), C.c_double()
+        _check(self._L.upcg_mlp_timings(self._h, C.byref(a), C.byref(b)))
+        return {"labels_ms": a.value, "train_ms": b.value}
 
 
 class UpcCrossSection:
@@ -262,7 +353,7 @@ class UpcGenerator:
         _check(self._L.upcg_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))
 
     def setLumiMethod(self, method):
-        _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1, "hybrid": 2, "grid": 3}.get(method, method)))
+        _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1, "hybrid": 2, "grid": 3, "surrogate": 4}.get(method, method)))
 
     # -- sharding over m-rows (upcgen_gb300.shard)
     def setRowRange(self, im0, im1=-1):
@@ -272,6 +363,15 @@ class UpcGenerator:
         t = _arr(table).ravel()
         t2 = _arr(table2).ravel() if table2 is not None else None
         _check(self._L.upcg_set_lumi_table(self._h, _p(t), t.size, _p(t2) if t2 is not None else None))
+
+    def setFluxSurrogate(self, surrogate):
+        self._surrogate = surrogate  # kept alive with the generator
+        _check(self._L.upcg_set_flux_surrogate(self._h, surrogate._h if surrogate else None))
+
+    def surrogateRows(self):
+        r = C.c_int()
+        _check(self._L.upcg_surrogate_rows(self._h, C.byref(r)))
+        return r.value
 
     def setCandidateOffset(self, counter):
         _check(self._L.upcg_set_candidate_offset(self._h, int(counter)))

@@ -9,6 +9,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <new>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -102,6 +103,28 @@ struct DBuf {
 
 }  // namespace
 
+// The learned flux surrogate (upcg_mlp.cu): parameters, Adam state,
+// training points, and the scratch of a training step.
+struct upcg_mlp {
+  MlpBox box{};
+  cudaStream_t own = nullptr;
+  DBuf<float> pf, m, v, part, lossp, xs, ys, ws, tx, ty, tw, out;
+  DBuf<uint16_t> pb;
+  DBuf<int> idx;
+  DBuf<double> glx, glw;
+  int64_t ndata = 0;
+  int step = 0;
+  uint64_t seed = 0;
+  double train_ms = 0, labels_ms = 0;
+  ~upcg_mlp() {
+    if (own) cudaStreamDestroy(own);
+  }
+  cudaStream_t st() {
+    if (!own) cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking);
+    return own;
+  }
+};
+
 struct upcg_generator {
   // ---- configuration (defaults: include/UpcCrossSection.h:73-172,
   //      include/UpcGenerator.h:62-73, UpcGenerator() :30-40)
@@ -122,6 +145,8 @@ struct upcg_generator {
   bool lumiCache = false;
   int lumiMethod = 0;
   int row_lo = 0, row_hi = -1;  // m-rows of the luminosity this handle computes (-1: all)
+  upcg_mlp* surrogate = nullptr;  // luminosity method 4: Q(w, b) rows from the MLP
+  int surrogate_rows = 0;         // rows of the last Q table that came from it
   // ---- derived
   double mPart = 0;
   int partPDG = 0;
@@ -619,8 +644,10 @@ int upcg_generator::build_lumi() {
   CK(cudaMemsetAsync(stats.p, 0, sizeof(QagsStats), s));
   // 1: fast form (flux tables + tensor-core contraction); 2: the same
   // contraction on the plain path's exact node fluxes (QAGS / K0,K1)
-  const bool fast = lumiMethod >= 1;
+  const bool fast = lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4;
   const bool node_flux = lumiMethod == 2 || !fast;
+  if (lumiMethod == 4 && !surrogate)
+    return fail(UPCG_ERR_STATE, "luminosity method 4 needs a surrogate (upcg_set_flux_surrogate)");
   if (fast && usePolarizedCS)
     return fail(UPCG_ERR_ARG, "the fast form covers the unpolarized luminosity");
   const int P = fast_grid_points();
@@ -704,8 +731,33 @@ int upcg_generator::build_lumi() {
       ftab.qt = fq.p;
       ftab.qt32 = fq32.p;
     }
+    // method 4: the rows inside the surrogate's box from the MLP (rows in
+    // blocks of 64), the others from the quadrature
+    int w_sur = 0;
+    const double gam = g1;
+    if (lumiMethod == 4 && !isPoint) {
+      const MlpBox& bx = surrogate->box;
+      const bool inside = R >= bx.R_lo && R <= bx.R_hi && a >= bx.a_lo && a <= bx.a_hi &&
+                          gam >= bx.g_lo && gam <= bx.g_hi && ftab.lw0 >= bx.lw_lo &&
+                          ftab.lb0 >= std::log(bx.bf_lo * R) &&
+                          ftab.lb0 + (ftab.nb - 1) * ftab.hb <= bx.lb_hi;
+      if (inside) {
+        const int nin = (int)std::floor((bx.lw_hi - ftab.lw0) / ftab.hw) + 1;
+        w_sur = std::max(0, std::min(ftab.nw, nin)) / 64 * 64;
+      }
+    }
     if (!isPoint) CK(fpartq.ensure(flux_table_part_doubles(ftab.nw, ftab.nb)));
-    CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, s));
+    CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, s, w_sur));
+    if (w_sur > 0) {
+      const int n = w_sur * ftab.nb;
+      CK(surrogate->tx.ensure((size_t)n * 5));
+      CK(surrogate->out.ensure(n));
+      CK(launch_mlp_table_inputs(surrogate->box, ftab, 0, w_sur, (float)R, (float)a, (float)gam,
+                                 surrogate->tx.p, s));
+      CK(launch_mlp_infer(surrogate->pb.p, surrogate->pf.p, surrogate->tx.p, n, surrogate->out.p, s));
+      CK(launch_mlp_table_fill(ftab, 0, w_sur, gam, (double)A, surrogate->out.p, s));
+    }
+    surrogate_rows = w_sur;
     // ln(m/2) per mass row, and the survival kernel beyond b = 20 fm
     std::vector<double> lnm2(nm);
     for (int im = 0; im < nm; ++im) lnm2[im] = std::log((p.mmin + p.dm * im) / 2.);
@@ -1019,7 +1071,7 @@ int upcg_set_stream(upcg_generator* g, void* stream) {
 }
 
 int upcg_set_lumi_method(upcg_generator* g, int method) {
-  if (!g || method < 0 || method > 3) return fail(UPCG_ERR_ARG, "bad luminosity method");
+  if (!g || method < 0 || method > 4) return fail(UPCG_ERR_ARG, "bad luminosity method");
   if (method != g->lumiMethod) g->invalidate();
   g->lumiMethod = method;
   return UPCG_OK;
@@ -1358,7 +1410,7 @@ int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_i
 
 int upcg_fast_flux_table(upcg_generator* g, double* out, size_t n, double* grid) {
   if (!g || !out || !grid) return fail(UPCG_ERR_ARG, "null argument");
-  if (!g->lumi_ready || g->lumiMethod != 1 || g->isPoint || !g->fq.p)
+  if (!g->lumi_ready || (g->lumiMethod != 1 && g->lumiMethod != 4) || g->isPoint || !g->fq.p)
     return fail(UPCG_ERR_STATE, "no fast-form flux table (fast method, FLUX_POINT 0, after init)");
   const size_t need = (size_t)512 * 256;
   if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
@@ -1437,6 +1489,254 @@ int upcg_copy_bytes(uint64_t* h2d, uint64_t* d2h) {
 int upcg_kernel_launches(uint64_t* n) {
   if (!n) return fail(UPCG_ERR_ARG, "null pointer");
   *n = launch_count();
+  return UPCG_OK;
+}
+
+// ---- learned flux surrogate ------------------------------------------------
+int upcg_mlp_create(upcg_mlp** out, uint64_t seed) {
+  if (!out) return fail(UPCG_ERR_ARG, "null argument");
+  upcg_mlp* h = new (std::nothrow) upcg_mlp();
+  if (!h) return fail(UPCG_ERR_NOMEM, "out of host memory");
+  // training box: w in [1e-3, 1e2] GeV, b in [0.049 R, 500] fm, R in [5, 7.5] fm,
+  // a in [0.40, 0.60] fm, g in [100, 3000]
+  h->box = MlpBox{(float)std::log(1e-3), (float)std::log(1e2), 0.049f, (float)std::log(500.),
+                  5.f, 7.5f, 0.40f, 0.60f, 100.f, 3000.f};
+  h->seed = seed;
+  const int np = mlp_param_count();
+  std::vector<float> p(np, 0.f);
+  // uniform +-sqrt(6 / fan_in) for the SiLU layers (He, uniform), +-sqrt(3 / fan_in)
+  // for the output layer; biases 0 (a counter-based splitmix64 stream)
+  uint64_t st = seed * 0x9E3779B97F4A7C15ull + 1;
+  auto uni = [&]() {
+    st += 0x9E3779B97F4A7C15ull;
+    uint64_t x = st;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+  };
+  const int kH = 128, kIn = 5;
+  int o = 0;
+  auto fill = [&](int n, int fan_in, double gain) {
+    const double lim = std::sqrt(gain / fan_in);
+    for (int i = 0; i < n; ++i) p[o++] = (float)((2. * uni() - 1.) * lim);
+  };
+  fill(kH * kIn, kIn, 6.);
+  o += kH;
+  for (int l = 0; l < 3; ++l) {
+    fill(kH * kH, kH, 6.);
+    o += kH;
+  }
+  fill(kH, kH, 3.);
+  o += 1;
+  cudaStream_t s = h->st();
+  auto bad = [&](cudaError_t e) {
+    if (e == cudaSuccess) return false;
+    fail(UPCG_ERR_CUDA, "upcg_mlp_create: %s", cudaGetErrorString(e));
+    return true;
+  };
+  if (bad(h->pf.ensure(np)) || bad(h->m.ensure(np)) || bad(h->v.ensure(np)) ||
+      bad(h->pb.ensure(np)) ||
+      bad(mcpy(h->pf.p, p.data(), np * sizeof(float), cudaMemcpyHostToDevice, s)) ||
+      bad(cudaMemsetAsync(h->m.p, 0, np * sizeof(float), s)) ||
+      bad(cudaMemsetAsync(h->v.p, 0, np * sizeof(float), s)) ||
+      bad(launch_mlp_to_bf16(h->pf.p, h->pb.p, s)) || bad(cudaStreamSynchronize(s))) {
+    delete h;
+    return UPCG_ERR_CUDA;
+  }
+  std::vector<double> gx, gw;
+  gauss_legendre(12, gx, gw);
+  if (bad(h->glx.ensure(12)) || bad(h->glw.ensure(12)) ||
+      bad(mcpy(h->glx.p, gx.data(), 12 * sizeof(double), cudaMemcpyHostToDevice, s)) ||
+      bad(mcpy(h->glw.p, gw.data(), 12 * sizeof(double), cudaMemcpyHostToDevice, s)) ||
+      bad(cudaStreamSynchronize(s))) {
+    delete h;
+    return UPCG_ERR_CUDA;
+  }
+  *out = h;
+  return UPCG_OK;
+}
+
+int upcg_mlp_destroy(upcg_mlp* h) {
+  delete h;
+  return UPCG_OK;
+}
+
+int upcg_mlp_box(const upcg_mlp* h, float* out, size_t n) {
+  if (!h || !out || n < 10) return fail(UPCG_ERR_ARG, "bad argument");
+  const MlpBox& b = h->box;
+  const float v[10] = {b.lw_lo, b.lw_hi, b.bf_lo, b.lb_hi, b.R_lo, b.R_hi, b.a_lo, b.a_hi, b.g_lo, b.g_hi};
+  std::memcpy(out, v, sizeof v);
+  return UPCG_OK;
+}
+
+int upcg_mlp_make_data(upcg_mlp* h, int64_t n, uint64_t seed) {
+  if (!h || n <= 0 || n > (int64_t)1 << 26) return fail(UPCG_ERR_ARG, "bad argument");
+  cudaStream_t s = h->st();
+  CK(h->xs.ensure((size_t)n * 5));
+  CK(h->ys.ensure(n));
+  CK(h->ws.ensure(n));
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, s);
+  CK(launch_mlp_labels(h->box, seed, 0, (int)n, h->glx.p, h->glw.p, h->xs.p, h->ys.p, h->ws.p, s));
+  cudaEventRecord(t1, s);
+  CK(cudaEventSynchronize(t1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  h->labels_ms = ms;
+  h->ndata = n;
+  return UPCG_OK;
+}
+
+int upcg_mlp_get_data(upcg_mlp* h, int64_t i0, int64_t n, float* x, float* y, float* w) {
+  if (!h || i0 < 0 || n < 0 || i0 + n > h->ndata) return fail(UPCG_ERR_ARG, "bad range");
+  cudaStream_t s = h->st();
+  if (x) CK(mcpy(x, h->xs.p + i0 * 5, (size_t)n * 5 * sizeof(float), cudaMemcpyDeviceToHost, s));
+  if (y) CK(mcpy(y, h->ys.p + i0, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s));
+  if (w) CK(mcpy(w, h->ws.p + i0, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return UPCG_OK;
+}
+
+int upcg_mlp_train(upcg_mlp* h, int epochs, int batch, float lr, double* last_loss) {
+  if (!h || epochs < 0 || batch < 16 || h->ndata < batch) return fail(UPCG_ERR_ARG, "bad argument");
+  cudaStream_t s = h->st();
+  const int np = mlp_param_count();
+  const int ctas = (batch + mlp_step_samples() - 1) / mlp_step_samples();
+  CK(h->part.ensure((size_t)ctas * np));
+  CK(h->lossp.ensure(ctas));
+  CK(h->idx.ensure(h->ndata));
+  std::vector<int> perm((size_t)h->ndata);
+  for (int64_t i = 0; i < h->ndata; ++i) perm[i] = (int)i;
+  uint64_t rs = h->seed ^ 0xD1B54A32D192ED03ull;
+  auto next = [&]() {
+    rs ^= rs << 13;
+    rs ^= rs >> 7;
+    rs ^= rs << 17;
+    return rs;
+  };
+  const int steps_per_epoch = (int)(h->ndata / batch);
+  const int total = epochs * steps_per_epoch;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, s);
+  for (int ep = 0; ep < epochs; ++ep) {
+    for (int64_t i = h->ndata - 1; i > 0; --i) std::swap(perm[i], perm[next() % (uint64_t)(i + 1)]);
+    CK(mcpy(h->idx.p, perm.data(), h->ndata * sizeof(int), cudaMemcpyHostToDevice, s));
+    for (int b = 0; b < steps_per_epoch; ++b) {
+      // cosine decay of the step size over the run
+      const int k = ep * steps_per_epoch + b;
+      const float lrk = lr * 0.5f * (1.f + std::cos(3.14159265f * (float)k / (float)total));
+      CK(launch_mlp_step(h->pb.p, h->pf.p, h->xs.p, h->ys.p, h->ws.p, h->idx.p + (size_t)b * batch,
+                         batch, 1.f / batch, h->part.p, h->lossp.p, s));
+      ++h->step;
+      CK(launch_mlp_adam(h->part.p, ctas, h->pf.p, h->pb.p, h->m.p, h->v.p, lrk, h->step, nullptr, s));
+    }
+  }
+  cudaEventRecord(t1, s);
+  std::vector<float> lp(ctas);
+  CK(mcpy(lp.data(), h->lossp.p, ctas * sizeof(float), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  h->train_ms = ms;
+  if (last_loss) {
+    double l = 0;
+    for (float v : lp) l += v;
+    *last_loss = l;
+  }
+  return UPCG_OK;
+}
+
+int upcg_mlp_gradients(upcg_mlp* h, const float* x, const float* y, const float* w, int n,
+                       float* grads, size_t ng, double* loss) {
+  const int np = mlp_param_count();
+  if (!h || !x || !y || !w || !grads || n <= 0 || ng < (size_t)np)
+    return fail(UPCG_ERR_ARG, "bad argument");
+  cudaStream_t s = h->st();
+  const int ctas = (n + mlp_step_samples() - 1) / mlp_step_samples();
+  CK(h->tx.ensure((size_t)n * 5));
+  CK(h->ty.ensure(n));
+  CK(h->tw.ensure(n));
+  CK(h->idx.ensure(std::max<int64_t>(h->ndata, n)));
+  CK(h->part.ensure((size_t)ctas * np));
+  CK(h->lossp.ensure(ctas));
+  CK(h->out.ensure(np));
+  std::vector<int> iota(n);
+  for (int i = 0; i < n; ++i) iota[i] = i;
+  CK(mcpy(h->tx.p, x, (size_t)n * 5 * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(mcpy(h->ty.p, y, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(mcpy(h->tw.p, w, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(mcpy(h->idx.p, iota.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(launch_mlp_step(h->pb.p, h->pf.p, h->tx.p, h->ty.p, h->tw.p, h->idx.p, n, 1.f / n, h->part.p,
+                     h->lossp.p, s));
+  CK(launch_mlp_adam(h->part.p, ctas, h->pf.p, h->pb.p, h->m.p, h->v.p, 0.f, 1, h->out.p, s));
+  CK(mcpy(grads, h->out.p, np * sizeof(float), cudaMemcpyDeviceToHost, s));
+  std::vector<float> lp(ctas);
+  CK(mcpy(lp.data(), h->lossp.p, ctas * sizeof(float), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (loss) {
+    double l = 0;
+    for (float v : lp) l += v;
+    *loss = l;
+  }
+  return UPCG_OK;
+}
+
+int upcg_mlp_params(upcg_mlp* h, float* out, size_t n) {
+  const int np = mlp_param_count();
+  if (!h || !out || n < (size_t)np) return fail(UPCG_ERR_ARG, "bad argument");
+  CK(mcpy(out, h->pf.p, np * sizeof(float), cudaMemcpyDeviceToHost, h->st()));
+  CK(cudaStreamSynchronize(h->st()));
+  return UPCG_OK;
+}
+
+int upcg_mlp_set_params(upcg_mlp* h, const float* in, size_t n) {
+  const int np = mlp_param_count();
+  if (!h || !in || n != (size_t)np) return fail(UPCG_ERR_ARG, "bad argument");
+  cudaStream_t s = h->st();
+  CK(mcpy(h->pf.p, in, np * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(launch_mlp_to_bf16(h->pf.p, h->pb.p, s));
+  CK(cudaStreamSynchronize(s));
+  return UPCG_OK;
+}
+
+int upcg_mlp_predict(upcg_mlp* h, const float* x, int n, float* y) {
+  if (!h || !x || !y || n <= 0) return fail(UPCG_ERR_ARG, "bad argument");
+  cudaStream_t s = h->st();
+  CK(h->tx.ensure((size_t)n * 5));
+  CK(h->out.ensure(std::max(n, mlp_param_count())));
+  CK(mcpy(h->tx.p, x, (size_t)n * 5 * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(launch_mlp_infer(h->pb.p, h->pf.p, h->tx.p, n, h->out.p, s));
+  CK(mcpy(y, h->out.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return UPCG_OK;
+}
+
+int upcg_mlp_timings(const upcg_mlp* h, double* labels_ms, double* train_ms) {
+  if (!h) return fail(UPCG_ERR_ARG, "null handle");
+  if (labels_ms) *labels_ms = h->labels_ms;
+  if (train_ms) *train_ms = h->train_ms;
+  return UPCG_OK;
+}
+
+int upcg_set_flux_surrogate(upcg_generator* g, upcg_mlp* h) {
+  if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  g->surrogate = h;
+  if (g->lumiMethod == 4) g->invalidate();
+  return UPCG_OK;
+}
+
+int upcg_surrogate_rows(const upcg_generator* g, int* rows) {
+  if (!g || !rows) return fail(UPCG_ERR_ARG, "null argument");
+  *rows = g->surrogate_rows;
   return UPCG_OK;
 }
 

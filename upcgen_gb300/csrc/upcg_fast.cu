@@ -949,26 +949,33 @@ size_t fast_side_bytes() { return sizeof(SideC); }
 int flux_table_part_doubles(int nw, int nb) { return 8 * nw * nb; }
 
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
-                              int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st) {
+                              int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st,
+                              int w_lo) {
   note_launch();
   k_ktab<<<(kKTabN + 255) / 256, 256, 0, st>>>(p.g1, t->st, t->st32);
-  if (!p.isPoint) {
-    dim3 gh((nq + 255) / 256, t->nw);
+  // Q rows [w_lo, nw) by the quadrature (w_lo a multiple of 64; the rows below
+  // come from elsewhere)
+  const int rows = t->nw - w_lo;
+  if (!p.isPoint && rows > 0) {
+    if (w_lo % 64 != 0) return cudaErrorInvalidValue;
+    const double lw = t->lw0 + w_lo * t->hw;
+    dim3 gh((nq + 255) / 256, rows);
     note_launch();
-    k_qtab_H<<<gh, 256, 0, st>>>(p, d_qn, d_wn, nq, t->lw0, t->hw, d_H);
+    k_qtab_H<<<gh, 256, 0, st>>>(p, d_qn, d_wn, nq, lw, t->hw, d_H);
     dim3 gj((t->nb + 255) / 256, nq);
     note_launch();
     k_qtab_J<<<gj, 256, 0, st>>>(d_qn, nq, t->lb0, t->hb, t->nb, d_J);
     // K = nq split into nq / kslice slices; d_part holds them
     const int nslice = nq % (8 * 16) == 0 ? 8 : 1;
     const int kslice = nq / nslice;
-    dim3 gg(t->nb / 64, t->nw / 64, nslice);
+    dim3 gg(t->nb / 64, rows / 64, nslice);
     note_launch();
-    k_dgemm<<<gg, 256, 0, st>>>(d_H, d_J, d_part, t->nw, t->nb, nq, kslice);
-    const size_t mn = (size_t)t->nw * t->nb;
+    k_dgemm<<<gg, 256, 0, st>>>(d_H, d_J, d_part, rows, t->nb, nq, kslice);
+    const size_t mn = (size_t)rows * t->nb;
+    const size_t off = (size_t)w_lo * t->nb;
     note_launch();
-    k_dgemm_reduce<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(d_part, nslice, mn, t->qt,
-                                                                 t->qt32);
+    k_dgemm_reduce<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(d_part, nslice, mn, t->qt + off,
+                                                                 t->qt32 + off);
   }
   return cudaGetLastError();
 }

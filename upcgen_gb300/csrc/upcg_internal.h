@@ -133,8 +133,10 @@ int flux_table_ktab_n();
 void flux_table_ktab_range(double* u0, double* u1);
 // d_part: flux_table_part_doubles(nw, nb) doubles of split-K scratch
 int flux_table_part_doubles(int nw, int nb);
+// point-flux table, and the Q(w, b) rows [w_lo, nw) by the Hankel quadrature
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
-                              int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st);
+                              int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st,
+                              int w_lo = 0);
 // lnm2[im] = ln(m_im / 2); c_far = P(20 fm) sum_k w_k, the survival kernel
 // wherever every azimuth has b >= 20 fm
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
@@ -228,5 +230,30 @@ cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* 
                                cudaStream_t st);
 cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
                               cudaStream_t st);
+
+// learned flux surrogate (upcg_mlp.cu).  Box of the training points: ln w in
+// [lw_lo, lw_hi], ln b from ln(bf_lo R) to lb_hi, R, a uniform, g uniform.
+struct MlpBox {
+  float lw_lo, lw_hi, bf_lo, lb_hi, R_lo, R_hi, a_lo, a_hi, g_lo, g_hi;
+};
+int mlp_param_count();
+int mlp_step_samples();
+cudaError_t launch_mlp_labels(const MlpBox& bx, uint64_t seed, uint64_t i0, int n,
+                              const double* d_glx, const double* d_glw, float* xs, float* ys,
+                              float* ws, cudaStream_t st);
+cudaError_t launch_mlp_step(const void* pb, const float* pf, const float* xs, const float* ys,
+                            const float* ws, const int* idx, int nbatch, float inv_wsum,
+                            float* part, float* lossp, cudaStream_t st);
+cudaError_t launch_mlp_adam(const float* part, int nparts, float* pf, void* pb, float* m, float* v,
+                            float lr, int step, float* grad_out, cudaStream_t st);
+cudaError_t launch_mlp_to_bf16(const float* pf, void* pb, cudaStream_t st);
+cudaError_t launch_mlp_infer(const void* pb, const float* pf, const float* xs, int n, float* out,
+                             cudaStream_t st);
+// inputs of the surrogate on the fast form's Q(w, b) table rows [w0, w1)
+// (normalised to the box) and the table entries A Q_pt e^y from its outputs
+cudaError_t launch_mlp_table_inputs(const MlpBox& bx, const FastFluxTables& t, int w0, int w1,
+                                    float R, float a, float g, float* xs, cudaStream_t st);
+cudaError_t launch_mlp_table_fill(const FastFluxTables& t, int w0, int w1, double g, double A,
+                                  const float* ys, cudaStream_t st);
 
 }  // namespace upcg
