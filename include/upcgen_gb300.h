@@ -238,7 +238,8 @@ int upcg_selftest_contract(int ncells, int P, uint64_t seed, double* max_rel, do
 int upcg_fast_flux_table(upcg_generator* g, double* out, size_t n, double* grid);
 /* timings of the last upcg_init phases (ms): [0] tables [1] luminosity
  * [2] cross section + samplers [3] nodes [4] QAGS [5] band quadrature or
- * tensor-core contraction [6] fast-form projection + kernel build */
+ * tensor-core contraction [6] fast-form projection + kernel build [7] of
+ * which the flux tables (quadrature and surrogate rows) */
 int upcg_last_timings(const upcg_generator* g, double* ms, size_t n);
 int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_intervals,
                     uint64_t* evals);

@@ -442,7 +442,7 @@ class UpcGenerator:
         v = (C.c_double * 8)()
         _check(self._L.upcg_last_timings(self._h, v, 8))
         return {"tables_ms": v[0], "lumi_ms": v[1], "xsec_ms": v[2], "nodes_ms": v[3],
-                "qags_ms": v[4], "contract_ms": v[5], "project_ms": v[6]}
+                "qags_ms": v[4], "contract_ms": v[5], "project_ms": v[6], "fluxtab_ms": v[7]}
 
     def qagsStats(self):
         f, m, e = C.c_uint64(), C.c_uint64(), C.c_uint64()

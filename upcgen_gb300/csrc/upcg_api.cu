@@ -747,6 +747,7 @@ int upcg_generator::build_lumi() {
       }
     }
     if (!isPoint) CK(fpartq.ensure(flux_table_part_doubles(ftab.nw, ftab.nb)));
+    const int ft0 = mark();  // flux-table build: quadrature rows + surrogate rows
     CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, s, w_sur));
     if (w_sur > 0) {
       const int n = w_sur * ftab.nb;
@@ -758,6 +759,7 @@ int upcg_generator::build_lumi() {
       CK(launch_mlp_table_fill(ftab, 0, w_sur, gam, (double)A, surrogate->out.p, s));
     }
     surrogate_rows = w_sur;
+    spans.push_back({5, {ft0, mark()}});
     // ln(m/2) per mass row, and the survival kernel beyond b = 20 fm
     std::vector<double> lnm2(nm);
     for (int im = 0; im < nm; ++im) lnm2[im] = std::log((p.mmin + p.dm * im) / 2.);

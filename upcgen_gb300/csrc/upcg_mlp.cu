@@ -31,7 +31,7 @@ constexpr int oW3 = oB2 + kH, oB3 = oW3 + kH * kH;
 constexpr int oW4 = oB3 + kH, oB4 = oW4 + kH * kH;
 constexpr int oW5 = oB4 + kH, oB5 = oW5 + kH;
 constexpr int kParams = oB5 + 1;
-constexpr int kStepSamples = 16;   // samples per CTA of k_mlp_step
+constexpr int kStepSamples = 32;   // samples per CTA of k_mlp_step
 constexpr int kStepThreads = 256;
 
 __device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
@@ -187,8 +187,15 @@ __device__ void load_net(MlpSmem& S, const __nv_bfloat16* __restrict__ pb, const
 }
 
 // forward of ns samples: z[l][s][o] pre-activations (l = 0..3), y[s]
+// act[s][i] = SiLU(z[s][i]), once per layer (not once per output neuron)
 template <int NS>
-__device__ void forward(const MlpSmem& S, const float (*u)[kIn], float (*z)[NS][kH], float* y) {
+__device__ __forceinline__ void activate(const float (*z)[kH], float (*act)[kH]) {
+  for (int e = threadIdx.x; e < NS * kH; e += blockDim.x) act[e / kH][e % kH] = silu(z[e / kH][e % kH]);
+}
+
+template <int NS>
+__device__ void forward(const MlpSmem& S, const float (*u)[kIn], float (*z)[NS][kH],
+                        float (*act)[kH], float* y) {
   const int o = threadIdx.x & (kH - 1), sg = threadIdx.x >> 7;  // 2 sample groups
   constexpr int per = NS / 2;
   {
@@ -206,23 +213,28 @@ __device__ void forward(const MlpSmem& S, const float (*u)[kIn], float (*z)[NS][
   }
   __syncthreads();
   for (int l = 1; l < 4; ++l) {
+    activate<NS>(z[l - 1], act);
+    __syncthreads();
     float acc[per];
 #pragma unroll
     for (int k = 0; k < per; ++k) acc[k] = S.b[l][o];
     for (int i = 0; i < kH; ++i) {
       const float wv = __bfloat162float(S.w[l - 1][o][i]);
 #pragma unroll
-      for (int k = 0; k < per; ++k) acc[k] += wv * silu(z[l - 1][sg + 2 * k][i]);
+      for (int k = 0; k < per; ++k) acc[k] += wv * act[sg + 2 * k][i];
     }
+    __syncthreads();  // act is rewritten by the next layer
 #pragma unroll
     for (int k = 0; k < per; ++k) z[l][sg + 2 * k][o] = acc[k];
     __syncthreads();
   }
+  activate<NS>(z[3], act);
+  __syncthreads();
   // output: one warp per sample group of samples, lanes over neurons
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int s = wid; s < NS; s += blockDim.x / 32) {
     float v = 0.f;
-    for (int i = lane; i < kH; i += 32) v += S.w5[i] * silu(z[3][s][i]);
+    for (int i = lane; i < kH; i += 32) v += S.w5[i] * act[s][i];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if (lane == 0) y[s] = v + S.b5;
@@ -242,6 +254,7 @@ __global__ void __launch_bounds__(kStepThreads) k_mlp_step(
   float(*z)[NS][kH] = reinterpret_cast<float(*)[NS][kH]>(smem + sizeof(MlpSmem));
   float(*d)[kH] = reinterpret_cast<float(*)[kH]>(smem + sizeof(MlpSmem) + sizeof(float) * 4 * NS * kH);
   float(*dn)[kH] = d + NS;
+  float(*act)[kH] = dn + NS;
   __shared__ float u[NS][kIn], y[NS], g[NS];
   load_net(S, pb, pf);
   const int base = blockIdx.x * NS;
@@ -250,7 +263,7 @@ __global__ void __launch_bounds__(kStepThreads) k_mlp_step(
     u[s][j] = base + s < nbatch ? xs[(size_t)idx[base + s] * kIn + j] : 0.f;
   }
   __syncthreads();
-  forward<NS>(S, u, z, y);
+  forward<NS>(S, u, z, act, y);
   float* P = part + (size_t)blockIdx.x * kParams;
   if (threadIdx.x < NS) {
     const int s = threadIdx.x;
@@ -272,9 +285,10 @@ __global__ void __launch_bounds__(kStepThreads) k_mlp_step(
   }
   const int o = threadIdx.x & (kH - 1), sg = threadIdx.x >> 7;
   // output layer: dW5[i] = sum_s g_s a4[s][i], db5 = sum_s g_s; delta4 = g W5 silu'(z4)
+  // (act holds a4 after the forward pass)
   if (threadIdx.x < kH) {
     float acc = 0.f;
-    for (int s = 0; s < NS; ++s) acc += g[s] * silu(z[3][s][o]);
+    for (int s = 0; s < NS; ++s) acc += g[s] * act[s][o];
     P[oW5 + o] = acc;
   }
   if (threadIdx.x == kH) {
@@ -289,11 +303,13 @@ __global__ void __launch_bounds__(kStepThreads) k_mlp_step(
     const int offW = l == 1 ? oW2 : (l == 2 ? oW3 : oW4);
     const int offB = l == 1 ? oB2 : (l == 2 ? oB3 : oB4);
     // dW[o][i] = sum_s d[s][o] a_{l-1}[s][i]; each thread 64 entries
+    activate<NS>(z[l - 1], act);
+    __syncthreads();
     for (int e = threadIdx.x; e < kH * kH; e += blockDim.x) {
       const int oo = e / kH, ii = e % kH;
       float acc = 0.f;
 #pragma unroll 4
-      for (int s = 0; s < NS; ++s) acc += d[s][oo] * silu(z[l - 1][s][ii]);
+      for (int s = 0; s < NS; ++s) acc += d[s][oo] * act[s][ii];
       P[offW + e] = acc;
     }
     if (threadIdx.x < kH) {
@@ -355,7 +371,28 @@ __global__ void k_mlp_to_bf16(const float* __restrict__ pf, __nv_bfloat16* __res
   if (i < kParams) pb[i] = __float2bfloat16(pf[i]);
 }
 
-constexpr int kInferSamples = 32;
+constexpr int kInferSamples = 64;
+constexpr int kAs = kH + 8;  // padded row stride (bf16) of the tensor-core operands
+
+// Inference on the tensor cores (mma.sync m16n8k16, bf16 in, FP32 accumulate):
+// per 64-sample tile and layer, act[64][128] . W^T; activations between
+// layers rounded to bf16 (the operand type), bias + SiLU in FP32.
+struct MlpSmemI {
+  __nv_bfloat16 w1[kH][kIn];
+  __align__(16) __nv_bfloat16 w[3][kH][kAs];  // [l][out][in]
+  __align__(16) __nv_bfloat16 act[2][kInferSamples][kAs];
+  float w5[kH];
+  float b[4][kH];
+  float b5;
+};
+
+__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+      "{%8, %9}, {%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
 
 __global__ void __launch_bounds__(kStepThreads) k_mlp_infer(const __nv_bfloat16* __restrict__ pb,
                                                             const float* __restrict__ pf,
@@ -363,18 +400,88 @@ __global__ void __launch_bounds__(kStepThreads) k_mlp_infer(const __nv_bfloat16*
                                                             float* __restrict__ out) {
   constexpr int NS = kInferSamples;
   extern __shared__ __align__(16) uint8_t smem[];
-  MlpSmem& S = *reinterpret_cast<MlpSmem*>(smem);
-  float(*z)[NS][kH] = reinterpret_cast<float(*)[NS][kH]>(smem + sizeof(MlpSmem));
+  MlpSmemI& S = *reinterpret_cast<MlpSmemI*>(smem);
   __shared__ float u[NS][kIn], y[NS];
-  load_net(S, pb, pf);
-  const int base = blockIdx.x * NS;
-  for (int e = threadIdx.x; e < NS * kIn; e += blockDim.x) {
-    const int s = e / kIn, j = e % kIn;
-    u[s][j] = base + s < n ? xs[(size_t)(base + s) * kIn + j] : 0.f;
+  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) S.w1[i / kIn][i % kIn] = pb[oW1 + i];
+  for (int l = 0; l < 3; ++l) {
+    const int off = l == 0 ? oW2 : (l == 1 ? oW3 : oW4);
+    for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) S.w[l][i / kH][i % kH] = pb[off + i];
   }
+  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
+    S.w5[i] = __bfloat162float(pb[oW5 + i]);
+    S.b[0][i] = pf[oB1 + i];
+    S.b[1][i] = pf[oB2 + i];
+    S.b[2][i] = pf[oB3 + i];
+    S.b[3][i] = pf[oB4 + i];
+  }
+  if (threadIdx.x == 0) S.b5 = pf[oB5];
   __syncthreads();
-  forward<NS>(S, u, z, y);
-  if (threadIdx.x < NS && base + (int)threadIdx.x < n) out[base + threadIdx.x] = y[threadIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // warp w: rows 16 (w & 3) .. +16, output columns 64 (w >> 2) .. +64 (8 n-blocks)
+  const int m0 = 16 * (warp & 3), n0 = 64 * (warp >> 2);
+  const int r = lane >> 2, c = (lane & 3) * 2;
+  const int ntiles = (n + NS - 1) / NS;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int base = tile * NS;
+    for (int e = threadIdx.x; e < NS * kIn; e += blockDim.x) {
+      const int s = e / kIn, j = e % kIn;
+      u[s][j] = base + s < n ? xs[(size_t)(base + s) * kIn + j] : 0.f;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NS * kH; e += blockDim.x) {  // layer 1 (5 inputs)
+      const int s = e / kH, o = e % kH;
+      float v = S.b[0][o];
+#pragma unroll
+      for (int j = 0; j < kIn; ++j) v += __bfloat162float(S.w1[o][j]) * u[s][j];
+      S.act[0][s][o] = __float2bfloat16(silu(v));
+    }
+    __syncthreads();
+    int cur = 0;
+    for (int l = 0; l < 3; ++l) {
+      float d[8][4];
+#pragma unroll
+      for (int nb = 0; nb < 8; ++nb)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) d[nb][q] = 0.f;
+#pragma unroll
+      for (int k0 = 0; k0 < kH; k0 += 16) {
+        uint32_t af[4];
+        af[0] = *reinterpret_cast<const uint32_t*>(&S.act[cur][m0 + r][k0 + c]);
+        af[1] = *reinterpret_cast<const uint32_t*>(&S.act[cur][m0 + r + 8][k0 + c]);
+        af[2] = *reinterpret_cast<const uint32_t*>(&S.act[cur][m0 + r][k0 + c + 8]);
+        af[3] = *reinterpret_cast<const uint32_t*>(&S.act[cur][m0 + r + 8][k0 + c + 8]);
+#pragma unroll
+        for (int nb = 0; nb < 8; ++nb) {
+          const int nn = n0 + 8 * nb + r;  // output neuron of this lane's B column
+          uint32_t bf[2];
+          bf[0] = *reinterpret_cast<const uint32_t*>(&S.w[l][nn][k0 + c]);
+          bf[1] = *reinterpret_cast<const uint32_t*>(&S.w[l][nn][k0 + c + 8]);
+          mma16816(d[nb], af, bf);
+        }
+      }
+      // bias + SiLU -> the other activation buffer (bf16)
+#pragma unroll
+      for (int nb = 0; nb < 8; ++nb) {
+        const int col = n0 + 8 * nb + c;
+        const float b0 = S.b[l + 1][col], b1 = S.b[l + 1][col + 1];
+        *reinterpret_cast<__nv_bfloat162*>(&S.act[cur ^ 1][m0 + r][col]) =
+            __floats2bfloat162_rn(silu(d[nb][0] + b0), silu(d[nb][1] + b1));
+        *reinterpret_cast<__nv_bfloat162*>(&S.act[cur ^ 1][m0 + r + 8][col]) =
+            __floats2bfloat162_rn(silu(d[nb][2] + b0), silu(d[nb][3] + b1));
+      }
+      cur ^= 1;
+      __syncthreads();
+    }
+    for (int s = warp; s < NS; s += blockDim.x / 32) {
+      float v = 0.f;
+      for (int i = lane; i < kH; i += 32) v += S.w5[i] * __bfloat162float(S.act[cur][s][i]);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      if (lane == 0) y[s] = v + S.b5;
+    }
+    __syncthreads();
+    if (threadIdx.x < NS && base + (int)threadIdx.x < n) out[base + threadIdx.x] = y[threadIdx.x];
+  }
 }
 
 __global__ void k_mlp_table_inputs(MlpBox bx, FastFluxTables t, int w0, int w1, float R, float a,
@@ -424,8 +531,8 @@ cudaError_t launch_mlp_table_fill(const FastFluxTables& t, int w0, int w1, doubl
 
 int mlp_param_count() { return kParams; }
 
-size_t mlp_step_smem() { return sizeof(MlpSmem) + sizeof(float) * (4 + 2) * kStepSamples * kH; }
-size_t mlp_infer_smem() { return sizeof(MlpSmem) + sizeof(float) * 4 * kInferSamples * kH; }
+size_t mlp_step_smem() { return sizeof(MlpSmem) + sizeof(float) * (4 + 3) * kStepSamples * kH; }
+size_t mlp_infer_smem() { return sizeof(MlpSmemI); }
 int mlp_step_samples() { return kStepSamples; }
 
 cudaError_t launch_mlp_labels(const MlpBox& bx, uint64_t seed, uint64_t i0, int n,
@@ -479,8 +586,12 @@ cudaError_t launch_mlp_infer(const void* pb, const float* pf, const float* xs, i
     if (e != cudaSuccess) return e;
     attr = true;
   }
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int tiles = (n + kInferSamples - 1) / kInferSamples;
   note_launch();
-  k_mlp_infer<<<(n + kInferSamples - 1) / kInferSamples, kStepThreads, mlp_infer_smem(), st>>>(
+  k_mlp_infer<<<tiles < sms ? tiles : sms, kStepThreads, mlp_infer_smem(), st>>>(
       static_cast<const __nv_bfloat16*>(pb), pf, xs, n, out);
   return cudaGetLastError();
 }
