@@ -9,6 +9,8 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <new>
 #include <atomic>
 #include <chrono>
@@ -125,6 +127,103 @@ struct upcg_mlp {
   }
 };
 
+namespace {
+// Autotuner of the persistent contraction: for a work size it times both
+// tile shapes (256-wide x 2 stages, 128-wide x 3 stages) on synthetic
+// operands of that size, once per process and device, and keeps the faster.
+struct TuneKey {
+  int dev, rows, P;
+  bool operator<(const TuneKey& o) const {
+    return dev != o.dev ? dev < o.dev : (rows != o.rows ? rows < o.rows : P < o.P);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;
+std::map<int, std::pair<double, double>> g_tune_ms;  // last timings per rows bucket
+
+int tune_bucket(int rows) {  // power-of-two buckets of the row count
+  int b = 128;
+  while (b < rows) b <<= 1;
+  return b;
+}
+}  // namespace
+
+// shape and grid for `rows_pad` stacked rows (nvalid of them valid) at P
+int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid) {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  *grid = sms;
+  const TuneKey key{dev, tune_bucket(rows_pad), P};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      *shape = it->second;
+      return UPCG_OK;
+    }
+  }
+  // synthetic operands of the bucket's size, timed with events on a private stream
+  const int rows = key.rows;
+  DBuf<uint16_t> a, g;
+  DBuf<float> a2, part;
+  DBuf<int4> items;
+  DBuf<unsigned> err;
+  cudaStream_t s;
+  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  CK(a.ensure((size_t)rows * P));
+  CK(g.ensure((size_t)P * P));
+  CK(a2.ensure((size_t)rows * P));
+  CK(part.ensure((size_t)rows * (P / 128)));
+  CK(err.ensure(1));
+  CK(cudaMemsetAsync(a.p, 0, (size_t)rows * P * 2, s));
+  CK(cudaMemsetAsync(g.p, 0, (size_t)P * P * 2, s));
+  CK(cudaMemsetAsync(a2.p, 0, (size_t)rows * P * 4, s));
+  CK(cudaMemsetAsync(err.p, 0, 4, s));
+  double best = 1e30;
+  int pick = 0;
+  double t[2] = {0, 0};
+  for (int sh = 0; sh < 2; ++sh) {
+    const int tbn = sh == 0 ? 256 : 128;
+    std::vector<int4> it;
+    for (int mt = 0; mt < rows / 128; ++mt)
+      for (int nt = 0; nt < P / tbn; ++nt) it.push_back(make_int4(mt, nt, 0, 128));
+    CK(items.ensure(it.size()));
+    CK(cudaMemcpyAsync(items.p, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float ms = 0;
+    for (int rep = 0; rep < 3; ++rep) {  // warm-up, then the best of two
+      cudaEventRecord(e0, s);
+      CK(launch_contract_pers(a.p, a.p, g.p, g.p, 1, rows, P, items.p, (int)it.size(), a2.p, part.p,
+                              err.p, sh, *grid, s));
+      cudaEventRecord(e1, s);
+      CK(cudaEventSynchronize(e1));
+      float m = 0;
+      cudaEventElapsedTime(&m, e0, e1);
+      if (rep == 1 || (rep == 2 && m < ms)) ms = m;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    t[sh] = ms;
+    if (ms < best) {
+      best = ms;
+      pick = sh;
+    }
+  }
+  unsigned herr = 0;
+  CK(cudaMemcpy(&herr, err.p, 4, cudaMemcpyDeviceToHost));
+  cudaStreamDestroy(s);
+  if (herr) return fail(UPCG_ERR_CUDA, "contraction autotune timed out (code %u)", herr);
+  (void)nvalid;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune[key] = pick;
+  g_tune_ms[key.rows] = {t[0], t[1]};
+  *shape = pick;
+  return UPCG_OK;
+}
+
 struct upcg_generator {
   // ---- configuration (defaults: include/UpcCrossSection.h:73-172,
   //      include/UpcGenerator.h:62-73, UpcGenerator() :30-40)
@@ -179,6 +278,7 @@ struct upcg_generator {
     return cudaSuccess;
   }
   DBuf<int> ntab, nq, ovf, tile_count, mirror, guide2, guidez;
+  DBuf<int4> fitems;
   DBuf<uint16_t> guidept;
   DBuf<unsigned int> work;
   DBuf<QagsStats> stats;
@@ -623,11 +723,11 @@ int upcg_generator::build_lumi() {
   // mirror rapidities (see LumiParams::mirror); chunks hold whole m-rows
   std::vector<int> mir(ny, -1);
   const double dy = (ymax - ymin) / ny;
-  for (int a = 0; a < ny; ++a) {
-    const double ya = ymin + dy * a;
-    for (int b = 0; b < ny; ++b) {
-      const double yb = ymin + dy * b;
-      if (b != a && std::fabs(ya + yb) <= 8 * 2.220446049250313e-16 * std::fabs(ya)) { mir[a] = b; break; }
+  for (int ia = 0; ia < ny; ++ia) {
+    const double ya = ymin + dy * ia;
+    for (int ib = 0; ib < ny; ++ib) {
+      const double yb = ymin + dy * ib;
+      if (ib != ia && std::fabs(ya + yb) <= 8 * 2.220446049250313e-16 * std::fabs(ya)) { mir[ia] = ib; break; }
     }
   }
   CK(mirror.ensure(ny));
@@ -661,7 +761,7 @@ int upcg_generator::build_lumi() {
     CK(fa2.ensure((size_t)chunk_pad * P));
     CK(ffar.ensure(2 * (size_t)chunk_pad));  // one float4 per cell
     CK(fsides.ensure((2 * (size_t)chunk * fast_side_bytes() + 7) / 8));
-    CK(fpart.ensure((size_t)chunk * (P / 256)));
+    CK(fpart.ensure((size_t)chunk_pad * (P / 128)));
     CK(ferr.ensure(1));
     CK(cudaMemsetAsync(ferr.p, 0, sizeof(unsigned), s));
   }
@@ -804,10 +904,24 @@ int upcg_generator::build_lumi() {
                              node_flux ? flux.p : nullptr, &ftab, fsides.p, fah.p, fal.p, fa2.p,
                              ffar.p, s));
       spans.push_back({4, {b, mark()}});
+      // persistent contraction over this chunk's (row tile, N tile) work list
+      int shape = 0, grid = 0;
+      {
+        const int rc = contract_plan(ncp, nc, P, &shape, &grid);
+        if (rc) return rc;
+      }
+      const int tbn = shape == 0 ? 256 : 128;
+      std::vector<int4> items;
+      for (int mt = 0; mt < ncp / 128; ++mt)
+        for (int nt = 0; nt < P / tbn; ++nt)
+          items.push_back(make_int4(mt, nt, 0, std::min(128, nc - mt * 128)));
+      CK(fitems.ensure(items.size()));
+      CK(mcpy(fitems.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
       b = mark();
-      CK(launch_contract(fah.p, fal.p, fgh.p, fgl.p, fa2.p, ncp, nc, P, fpart.p, ferr.p, s));
+      CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(),
+                              fa2.p, fpart.p, ferr.p, shape, grid, s));
       spans.push_back({3, {b, mark()}});
-      CK(launch_fast_finish(p, c0, nc, P / 256, c_far, fpart.p, ffar.p, lumi.p, s));
+      CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s));
     }
   }
   const int w1 = mark();

@@ -828,6 +828,220 @@ cudaError_t make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t c
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// 3-D bf16 tensor map over [planes][rows][cols] (cols contiguous), box =
+// box_rows x 64 x 1: the stacked survival kernels of several configurations.
+cudaError_t make_map3(CUtensorMap* m, const void* base, uint64_t planes, uint64_t rows,
+                      uint64_t cols, uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  cuuint64_t dims[3] = {cols, rows, planes};
+  cuuint64_t strides[2] = {cols * 2, rows * cols * 2};
+  cuuint32_t box[3] = {(cuuint32_t)BK, box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Work item of the persistent contraction: a 128-row tile of the stacked
+// operands, one N tile of the survival kernel, and the configuration whose
+// kernel plane it uses.
+struct PersItem {
+  int mtile, ntile, config, rows;  // rows: valid rows of the tile (<= 128)
+};
+
+struct PersArgs {
+  const PersItem* items;
+  int nitems, ktiles, P, ntiles;
+  const float* a2;   // [rows of all tiles][P]
+  float* partial;    // [rows][ntiles]
+  unsigned* err;
+};
+
+// Persistent form of k_contract: each CTA walks the work list (item
+// blockIdx.x, + gridDim.x, ...).  The k-stage ring and its phases run on
+// across items; the accumulator is double-buffered in TMEM (2 x TBN columns),
+// so the MMAs of one item overlap the epilogue of the previous one.
+// Template: TBN = N tile (256 or 128), TST = stages (2 or 3): the shapes the
+// autotuner picks from.
+template <int TBN, int TST>
+__global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant__ CUtensorMap tAh,
+                                                          const __grid_constant__ CUtensorMap tAl,
+                                                          const __grid_constant__ CUtensorMap tBh,
+                                                          const __grid_constant__ CUtensorMap tBl,
+                                                          PersArgs args) {
+  constexpr int kA = BM * BK * 2, kB = TBN * BK * 2, kStage = 2 * kA + 2 * kB;
+  constexpr uint32_t kCols = 2 * TBN;
+  constexpr uint32_t kId = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TBN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[TST], empty_bar[TST], accf[2], acce[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TST; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);  // one arrival per epilogue warp
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int nmine = args.nitems > (int)blockIdx.x
+                        ? (args.nitems - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                        : 0;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    int g = 0;  // k tiles issued by this CTA
+    bool ok = true;
+    for (int it = 0; it < nmine && ok; ++it) {
+      const PersItem w = args.items[blockIdx.x + it * gridDim.x];
+      for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+        const int s = g % TST;
+        if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 1u)) {
+          ok = false;
+          abort_flag = 1;
+          break;
+        }
+        if (abort_flag) {
+          ok = false;
+          break;
+        }
+        uint8_t* st = smem + s * kStage;
+        mbar_expect_tx(&full_bar[s], kStage);
+        const int x = kt * BK;
+        tma_load_2d(st, &tAh, &full_bar[s], x, w.mtile * BM);
+        tma_load_2d(st + kA, &tAl, &full_bar[s], x, w.mtile * BM);
+        tma_load_3d(st + 2 * kA, &tBh, &full_bar[s], x, w.ntile * TBN, w.config);
+        tma_load_3d(st + 2 * kA + kB, &tBl, &full_bar[s], x, w.ntile * TBN, w.config);
+      }
+    }
+    // the copies in flight land before the CTA exits
+    for (int q = (g > TST ? g - TST : 0); q < g; ++q)
+      mbar_wait(&full_bar[q % TST], (q / TST) & 1, args.err, 8u);
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    int g = 0;
+    bool ok = true;
+    for (int it = 0; it < nmine && ok; ++it) {
+      const int b = it & 1;
+      if (it >= 2 && !mbar_wait(&acce[b], ((it >> 1) & 1) ^ 1, args.err, 16u)) {
+        ok = false;
+        abort_flag = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t acc = tmem + (uint32_t)(b * TBN);
+      for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+        const int s = g % TST;
+        if (!mbar_wait(&full_bar[s], (g / TST) & 1, args.err, 2u)) {
+          ok = false;
+          abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t base = smem_u32(smem + s * kStage);
+        const uint32_t ah = base, al = base + kA, bh = base + 2 * kA, bl = base + 2 * kA + kB;
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) {
+          const uint32_t off = kk * 32;
+          const uint64_t dah = sw128_desc(ah + off), dal = sw128_desc(al + off);
+          const uint64_t dbh = sw128_desc(bh + off), dbl = sw128_desc(bl + off);
+          const uint32_t first = (kt > 0 || kk > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
+              "l"(dah), "l"(dbh), "r"(kId), "r"(first));
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
+              "l"(dah), "l"(dbl), "r"(kId), "r"(1u));
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
+              "l"(dal), "l"(dbh), "r"(kId), "r"(1u));
+        }
+        umma_commit(&empty_bar[s]);
+      }
+      if (ok) umma_commit(&accf[b]);
+    }
+  } else if (warp >= 2) {
+    // ---------------- epilogue: TMEM -> registers, row-dot with A2
+    const int quad = warp & 3;
+    for (int it = 0; it < nmine; ++it) {
+      const PersItem w = args.items[blockIdx.x + it * gridDim.x];
+      const int b = it & 1;
+      const bool ok = mbar_wait(&accf[b], (it >> 1) & 1, args.err, 4u);
+      tc_fence_after();
+      const int row = quad * 32 + lane;
+      const size_t grow = (size_t)w.mtile * BM + row;
+      float acc = 0.f;
+      if (ok) {
+        const float* a2 = args.a2 + grow * args.P + w.ntile * TBN;
+        for (int c0 = 0; c0 < TBN; c0 += 16) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TBN + c0), v);
+          if (row < w.rows) {
+            const float4* a4 = reinterpret_cast<const float4*>(a2 + c0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const float4 x = __ldg(a4 + q);
+              acc += v[4 * q] * x.x + v[4 * q + 1] * x.y + v[4 * q + 2] * x.z + v[4 * q + 3] * x.w;
+            }
+          }
+        }
+      }
+      if (row < w.rows) args.partial[grow * args.ntiles + w.ntile] = ok ? acc : 0.f;
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
+      if (!ok) break;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+  }
+}
+
+template <int TBN, int TST>
+constexpr int pers_smem() {
+  return TST * (2 * BM * BK * 2 + 2 * TBN * BK * 2) + 1024;
+}
+
 }  // namespace
 
 int fast_grid_points() { return 1024; }
@@ -854,6 +1068,48 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
   k_contract<<<grid, 192, kContractSmem, st>>>(tAh, tAl, tBh, tBl, args);
   return cudaGetLastError();
 }
+
+cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh, const void* gl,
+                                 int nconf, int rows_total, int P, const void* items, int nitems,
+                                 const float* a2, float* partial, unsigned* d_err, int shape,
+                                 int grid, cudaStream_t st) {
+  // shape 0: N tile 256, 2 stages; shape 1: N tile 128, 3 stages
+  const int tbn = shape == 0 ? 256 : 128;
+  if (P % tbn != 0 || P % BK != 0 || rows_total % BM != 0 || nitems <= 0 || grid <= 0)
+    return cudaErrorInvalidValue;
+  CUtensorMap tAh, tAl, tBh, tBl;
+  cudaError_t e;
+  if ((e = make_map(&tAh, ah, rows_total, P, BM)) != cudaSuccess) return e;
+  if ((e = make_map(&tAl, al, rows_total, P, BM)) != cudaSuccess) return e;
+  if ((e = make_map3(&tBh, gh, nconf, P, P, tbn)) != cudaSuccess) return e;
+  if ((e = make_map3(&tBl, gl, nconf, P, P, tbn)) != cudaSuccess) return e;
+  PersArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, a2, partial, d_err};
+  if (grid > nitems) grid = nitems;
+  if (shape == 0) {
+    static bool attr = false;
+    constexpr int sm = pers_smem<256, 2>();
+    if (!attr) {
+      e = cudaFuncSetAttribute(k_contract_pers<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    note_launch();
+    k_contract_pers<256, 2><<<grid, 192, sm, st>>>(tAh, tAl, tBh, tBl, args);
+  } else {
+    static bool attr = false;
+    constexpr int sm = pers_smem<128, 3>();
+    if (!attr) {
+      e = cudaFuncSetAttribute(k_contract_pers<128, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    note_launch();
+    k_contract_pers<128, 3><<<grid, 192, sm, st>>>(tAh, tAl, tBh, tBl, args);
+  }
+  return cudaGetLastError();
+}
+
+int contract_item_bytes() { return (int)sizeof(PersItem); }
 
 cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, const void* bl,
                                int M, int N, int K, float* out_f32, void* out_hi, void* out_lo,

@@ -153,6 +153,16 @@ size_t fast_side_bytes();
 cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, const void* bl,
                                int M, int N, int K, float* out_f32, void* out_hi, void* out_lo,
                                unsigned* d_err, cudaStream_t st);
+// Persistent contraction over a work list of {128-row tile of the stacked A,
+// N tile, configuration (plane of the stacked G), valid rows} items (int4
+// each, contract_item_bytes()); rows_total = rows of the stacked A (multiple
+// of 128).  shape 0 = 256-wide N tiles x 2 stages, 1 = 128-wide x 3 stages;
+// partial is [rows][P / tile width].
+cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh, const void* gl,
+                                 int nconf, int rows_total, int P, const void* items, int nitems,
+                                 const float* a2, float* partial, unsigned* d_err, int shape,
+                                 int grid, cudaStream_t st);
+int contract_item_bytes();
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
                             const float* a2, int ncells_pad, int ncells, int P, float* partial,
                             unsigned* d_err, cudaStream_t st);
