@@ -190,6 +190,23 @@ int upcg_generate_events_device(upcg_generator* g, int64_t n, upcg_event* out_de
  * upcg_generate_events. */
 int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted);
 
+/* ---- batched scans (no counterpart in the reference: one configuration per
+ * process there) ----------------------------------------------------------
+ * A scan builds the tables of n configurations (each a handle with its
+ * parameters set) with the fast form: per configuration the nuclear tables,
+ * its survival kernel and projection; ONE persistent tensor-core contraction
+ * over every configuration's tiles (uneven grid sizes in one work list; the
+ * tile shape picked by the library's autotuner); then per configuration the
+ * cross section and samplers.  The first upcg_scan_run initialises every
+ * handle, captures the whole sequence into a CUDA graph and replays it;
+ * later runs replay the graph.  After a run each handle is ready for events.
+ * The handles must outlive the scan and run on its stream from then on. */
+typedef struct upcg_scan upcg_scan;
+int upcg_scan_create(upcg_scan** out, upcg_generator* const* gens, int n);
+int upcg_scan_run(upcg_scan* sc, double* ms);
+int upcg_scan_info(const upcg_scan* sc, int* nitems, int* shape, int* rows_total, double* setup_ms);
+int upcg_scan_destroy(upcg_scan* sc);
+
 /* ---- learned flux surrogate (no counterpart in the reference) -------------
  * An MLP (inputs ln w, ln b, R, a, ln g; four hidden layers of 128 SiLU; BF16
  * weights, FP32 accumulation) for y = ln(Q_ff / Q_pt), the log-ratio of

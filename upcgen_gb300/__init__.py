@@ -40,7 +40,8 @@ ABI_SYMBOLS = [
     "upcg_mlp_create", "upcg_mlp_destroy", "upcg_mlp_box", "upcg_mlp_make_data",
     "upcg_mlp_get_data", "upcg_mlp_train", "upcg_mlp_gradients", "upcg_mlp_params",
     "upcg_mlp_set_params", "upcg_mlp_predict", "upcg_mlp_timings", "upcg_set_flux_surrogate",
-    "upcg_surrogate_rows",
+    "upcg_surrogate_rows", "upcg_scan_create", "upcg_scan_run", "upcg_scan_info",
+    "upcg_scan_destroy",
 ]
 
 
@@ -100,6 +101,9 @@ def load_library(path=None):
         "upcg_mlp_params": [vp, vp, sz], "upcg_mlp_set_params": [vp, vp, sz],
         "upcg_mlp_predict": [vp, vp, i, vp], "upcg_mlp_timings": [vp, dp, dp],
         "upcg_set_flux_surrogate": [vp, vp], "upcg_surrogate_rows": [vp, C.POINTER(i)],
+        "upcg_scan_create": [C.POINTER(vp), C.POINTER(vp), i], "upcg_scan_run": [vp, dp],
+        "upcg_scan_info": [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i), dp],
+        "upcg_scan_destroy": [vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -232,6 +236,35 @@ class FluxSurrogate:
         a, b = C.c_double(), C.c_double()
         _check(self._L.upcg_mlp_timings(self._h, C.byref(a), C.byref(b)))
         return {"labels_ms": a.value, "train_ms": b.value}
+
+
+class Scan:
+    """Batched table build of several configurations (upcg_scan_*): one
+    persistent tensor-core contraction over all of them, replayed from a
+    captured CUDA graph."""
+
+    def __init__(self, generators):
+        self._L = load_library()
+        self.generators = list(generators)  # kept alive with the scan
+        arr = (C.c_void_p * len(self.generators))(*[g._h.value for g in self.generators])
+        self._h = C.c_void_p()
+        _check(self._L.upcg_scan_create(C.byref(self._h), arr, len(self.generators)))
+
+    def run(self):
+        ms = C.c_double()
+        _check(self._L.upcg_scan_run(self._h, C.byref(ms)))
+        return ms.value
+
+    def info(self):
+        n, sh, rows, st = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        _check(self._L.upcg_scan_info(self._h, C.byref(n), C.byref(sh), C.byref(rows), C.byref(st)))
+        return {"items": n.value, "shape": ["256x2", "128x3"][sh.value], "rows": rows.value,
+                "setup_ms": st.value}
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.upcg_scan_destroy(self._h)
+            self._h = C.c_void_p()
 
 
 class UpcCrossSection:

@@ -224,6 +224,8 @@ int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid) {
   return UPCG_OK;
 }
 
+struct upcg_scan;
+
 struct upcg_generator {
   // ---- configuration (defaults: include/UpcCrossSection.h:73-172,
   //      include/UpcGenerator.h:62-73, UpcGenerator() :30-40)
@@ -246,6 +248,11 @@ struct upcg_generator {
   int row_lo = 0, row_hi = -1;  // m-rows of the luminosity this handle computes (-1: all)
   upcg_mlp* surrogate = nullptr;  // luminosity method 4: Q(w, b) rows from the MLP
   int surrogate_rows = 0;         // rows of the last Q table that came from it
+  bool cap = false;               // enqueue device work only (stream capture of a scan)
+  FastFluxTables ftab_last{};     // the fast form's flux tables of the last build
+  int nqn_last = 0;
+  int enqueue_scan_front(upcg_scan& sc, int ci);
+  int enqueue_scan_back(upcg_scan& sc, int ci);
   // ---- derived
   double mPart = 0;
   int partPDG = 0;
@@ -528,10 +535,12 @@ int upcg_generator::build_tables() {
   if (rc) return rc;
   cudaStream_t s = st();
   CK(side_streams());
-  cudaEvent_t t0, t1;
-  cudaEventCreate(&t0);
-  cudaEventCreate(&t1);
-  cudaEventRecord(t0, s);
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (!cap) {
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    cudaEventRecord(t0, s);
+  }
   factor = Z * Z * kAlpha / M_PI / M_PI / kHc / kHc;  // src/UpcCrossSection.cpp:120
   rho0 = ws_rho_host(R, a, A);
   // sigma_NN (PDG 2016 fit), src/UpcCrossSection.cpp:368-369
@@ -577,9 +586,11 @@ int upcg_generator::build_tables() {
   // spline at min(b, 20))
   CK(bu_tab.ensure(4 * kBreakupTabMax));
   CK(ntab.ensure(1));
-  CK(mcpy(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double),
-                     cudaMemcpyHostToDevice, side[1]));
-  CK(mcpy(ntab.p, &bu_nt, sizeof(int), cudaMemcpyHostToDevice, side[1]));
+  if (!cap) {  // a captured replay reuses the table uploaded by the set-up run
+    CK(mcpy(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double),
+                       cudaMemcpyHostToDevice, side[1]));
+    CK(mcpy(ntab.p, &bu_nt, sizeof(int), cudaMemcpyHostToDevice, side[1]));
+  }
   const double dbb = (1000. - 1e-6) / 1000000;
   brk_n = (int)((20. - 1e-6) / dbb) + 257;
   CK(brk_y.ensure(brk_n));
@@ -593,13 +604,15 @@ int upcg_generator::build_tables() {
   CK(cudaEventRecord(ev_join[1], side[1]));
   CK(cudaStreamWaitEvent(s, ev_join[0], 0));
   CK(cudaStreamWaitEvent(s, ev_join[1], 0));
-  cudaEventRecord(t1, s);
-  CK(cudaEventSynchronize(t1));
-  float ms = 0;
-  cudaEventElapsedTime(&ms, t0, t1);
-  timings[0] = ms;
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
+  if (!cap) {
+    cudaEventRecord(t1, s);
+    CK(cudaEventSynchronize(t1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    timings[0] = ms;
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+  }
   tables_ready = true;
   return UPCG_OK;
 }
@@ -868,6 +881,8 @@ int upcg_generator::build_lumi() {
     c_far = 0.;
     for (int q = 0; q < 5; ++q) c_far += P20 * 1. * p.wk[q];
     spans.push_back({4, {b, mark()}});
+    ftab_last = ftab;
+    nqn_last = nqn;
   }
   for (int c0 = cell_lo; c0 < cell_hi; c0 += chunk) {
     const int nc = std::min(chunk, cell_hi - c0);
@@ -951,10 +966,12 @@ int upcg_generator::build_xsec() {
   cudaStream_t s = st();
   const FoldParams f = fold_params();
   const int ncell = nm * ny;
-  cudaEvent_t t0, t1;
-  cudaEventCreate(&t0);
-  cudaEventCreate(&t1);
-  cudaEventRecord(t0, s);
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (!cap) {
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    cudaEventRecord(t0, s);
+  }
   CK(cs.ensure(ncell));
   CK(ratio.ensure(usePolarizedCS ? ncell : 1));
   CK(partial.ensure((ncell + 255) / 256 + 1));
@@ -988,6 +1005,10 @@ int upcg_generator::build_xsec() {
     CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
     const EventParams eg = event_params();  // with the guide buffers allocated
     CK(launch_guides(eg, cdf2.p, cdfz.p, ptcdf.p, guide2.p, guidez.p, guidept.p, s));
+  }
+  if (cap) {  // a captured replay leaves sigma_tot on the device (read after the replay)
+    xsec_ready = true;
+    return UPCG_OK;
   }
   CK(mcpy(&totCS, tot.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   cudaEventRecord(t1, s);
@@ -1096,6 +1117,72 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
   }
   *rejected = rej;
   return UPCG_OK;
+}
+
+// ---------------------------------------------------------------- scans ----
+// Many configurations in one captured graph: per configuration the table
+// chains, the survival kernel (one plane of a stacked G) and the projection
+// (rows of a stacked A), then ONE persistent contraction over the work list
+// of every configuration's tiles, then per configuration the finish, the
+// fold and the samplers.
+struct upcg_scan {
+  std::vector<upcg_generator*> gens;
+  DBuf<uint16_t> ah, al, gh, gl;
+  DBuf<float> a2, part;
+  DBuf<double> far, fc;
+  DBuf<int4> items;
+  DBuf<unsigned> err;
+  std::vector<int> row0, rows;
+  int rows_total = 0, nitems = 0, shape = 0, grid = 0, P = 0;
+  cudaStream_t s = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double setup_ms = 0, run_ms = 0;
+  ~upcg_scan() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+int upcg_generator::enqueue_scan_front(upcg_scan& sc, int ci) {
+  cudaStream_t s = st();
+  cap = true;
+  int rc = build_tables();
+  if (rc) {
+    cap = false;
+    return rc;
+  }
+  const LumiParams p = lumi_params();
+  const int P = sc.P;
+  const double fu0 = std::log(0.1), fh = (std::log(256.) - std::log(0.1)) / (P - 1);
+  const size_t plane = (size_t)P * P;
+  double* fc = sc.fc.p + 2 * ci;
+  CK(launch_far_consts(p, breakupMode != 1, fc, s));
+  CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, sc.gh.p + ci * plane,
+                   sc.gl.p + ci * plane, s, fc));
+  FastFluxTables ft = ftab_last;
+  CK(build_flux_tables(p, &ft, fqn.p, fwn.p, nqn_last, fH.p, fJ.p, fpartq.p, s, 0));
+  const size_t r0 = (size_t)sc.row0[ci];
+  CK(launch_fast_project(p, fu0, fh, P, 0, nm * ny, sc.rows[ci], flnm2.p, 0.0, nullptr, &ft,
+                         fsides.p, sc.ah.p + r0 * P, sc.al.p + r0 * P, sc.a2.p + r0 * P,
+                         sc.far.p + 2 * r0, s));
+  cap = false;
+  return UPCG_OK;
+}
+
+int upcg_generator::enqueue_scan_back(upcg_scan& sc, int ci) {
+  cudaStream_t s = st();
+  const LumiParams p = lumi_params();
+  const int ntiles = sc.P / (sc.shape == 0 ? 256 : 128);
+  const size_t r0 = (size_t)sc.row0[ci];
+  CK(launch_fast_finish(p, 0, nm * ny, ntiles, 0.0, sc.part.p + r0 * ntiles, sc.far.p + 2 * r0,
+                        lumi.p, s, sc.fc.p + 2 * ci));
+  lumi_ready = true;
+  cap = true;
+  const int rc = build_xsec();
+  cap = false;
+  return rc;
 }
 
 // ------------------------------------------------------------------ ABI ----
@@ -1840,6 +1927,150 @@ int upcg_mlp_timings(const upcg_mlp* h, double* labels_ms, double* train_ms) {
   if (!h) return fail(UPCG_ERR_ARG, "null handle");
   if (labels_ms) *labels_ms = h->labels_ms;
   if (train_ms) *train_ms = h->train_ms;
+  return UPCG_OK;
+}
+
+int upcg_scan_create(upcg_scan** out, upcg_generator* const* gens, int n) {
+  if (!out || !gens || n <= 0) return fail(UPCG_ERR_ARG, "bad argument");
+  for (int i = 0; i < n; ++i)
+    if (!gens[i]) return fail(UPCG_ERR_ARG, "null generator %d", i);
+  upcg_scan* sc = new (std::nothrow) upcg_scan();
+  if (!sc) return fail(UPCG_ERR_NOMEM, "out of host memory");
+  sc->gens.assign(gens, gens + n);
+  *out = sc;
+  return UPCG_OK;
+}
+
+int upcg_scan_destroy(upcg_scan* sc) {
+  delete sc;
+  return UPCG_OK;
+}
+
+namespace {
+int scan_setup(upcg_scan* sc) {
+  const int n = (int)sc->gens.size();
+  const auto t0 = std::chrono::steady_clock::now();
+  CK(cudaStreamCreateWithFlags(&sc->s, cudaStreamNonBlocking));
+  sc->P = fast_grid_points();
+  const int P = sc->P;
+  // one ordinary initialisation per configuration: allocations, static
+  // uploads, checks; the generators then run on the scan's stream
+  sc->row0.assign(n, 0);
+  sc->rows.assign(n, 0);
+  int64_t rows_total = 0;
+  for (int i = 0; i < n; ++i) {
+    upcg_generator* g = sc->gens[i];
+    g->lumiMethod = 1;
+    g->row_lo = 0;
+    g->row_hi = -1;
+    g->stream = sc->s;
+    g->invalidate();
+    int rc = upcg_init(g);
+    if (rc) return rc;
+    if (g->usePolarizedCS) return fail(UPCG_ERR_PROCESS, "scan: polarized configuration %d", i);
+    const int ncell = g->nm * g->ny;
+    CK(g->fsides.ensure((2 * (size_t)ncell * fast_side_bytes() + 7) / 8));
+    sc->row0[i] = (int)rows_total;
+    sc->rows[i] = (ncell + 127) / 128 * 128;
+    rows_total += sc->rows[i];
+  }
+  if (rows_total > (int64_t)1 << 30) return fail(UPCG_ERR_SIZE, "scan too large");
+  sc->rows_total = (int)rows_total;
+  const size_t plane = (size_t)P * P;
+  CK(sc->ah.ensure((size_t)rows_total * P));
+  CK(sc->al.ensure((size_t)rows_total * P));
+  CK(sc->a2.ensure((size_t)rows_total * P));
+  CK(sc->part.ensure((size_t)rows_total * (P / 128)));
+  CK(sc->far.ensure(2 * (size_t)rows_total));
+  CK(sc->gh.ensure(n * plane));
+  CK(sc->gl.ensure(n * plane));
+  CK(sc->fc.ensure(2 * (size_t)n));
+  CK(sc->err.ensure(1));
+  // tile shape from the autotuner, then the work list: per configuration its
+  // row tiles, the N tiles of a row tile adjacent (L2 reuse of A)
+  int rc = contract_plan(std::min(sc->rows_total, 131072), sc->rows_total, P, &sc->shape, &sc->grid);
+  if (rc) return rc;
+  const int tbn = sc->shape == 0 ? 256 : 128;
+  std::vector<int4> items;
+  for (int i = 0; i < n; ++i) {
+    const int ncell = sc->gens[i]->nm * sc->gens[i]->ny;
+    for (int mt = 0; mt < sc->rows[i] / 128; ++mt)
+      for (int nt = 0; nt < P / tbn; ++nt)
+        items.push_back(make_int4(sc->row0[i] / 128 + mt, nt, i, std::min(128, ncell - mt * 128)));
+  }
+  sc->nitems = (int)items.size();
+  CK(sc->items.ensure(items.size()));
+  CK(mcpy(sc->items.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, sc->s));
+  CK(cudaStreamSynchronize(sc->s));
+  // capture the whole scan
+  CK(cudaStreamBeginCapture(sc->s, cudaStreamCaptureModeThreadLocal));
+  auto abort_capture = [&](int code) {
+    cudaGraph_t gph = nullptr;
+    cudaStreamEndCapture(sc->s, &gph);
+    if (gph) cudaGraphDestroy(gph);
+    return code;
+  };
+  if (cudaMemsetAsync(sc->err.p, 0, sizeof(unsigned), sc->s) != cudaSuccess)
+    return abort_capture(fail(UPCG_ERR_CUDA, "scan: capture of the error word failed"));
+  for (int i = 0; i < n; ++i) {
+    rc = sc->gens[i]->enqueue_scan_front(*sc, i);
+    if (rc) return abort_capture(rc);
+  }
+  if (launch_contract_pers(sc->ah.p, sc->al.p, sc->gh.p, sc->gl.p, n, sc->rows_total, P, sc->items.p,
+                           sc->nitems, sc->a2.p, sc->part.p, sc->err.p, sc->shape, sc->grid,
+                           sc->s) != cudaSuccess)
+    return abort_capture(fail(UPCG_ERR_CUDA, "scan: contraction capture failed"));
+  for (int i = 0; i < n; ++i) {
+    rc = sc->gens[i]->enqueue_scan_back(*sc, i);
+    if (rc) return abort_capture(rc);
+  }
+  CK(cudaStreamEndCapture(sc->s, &sc->graph));
+  CK(cudaGraphInstantiate(&sc->exec, sc->graph, 0));
+  sc->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return UPCG_OK;
+}
+}  // namespace
+
+int upcg_scan_run(upcg_scan* sc, double* ms) {
+  if (!sc) return fail(UPCG_ERR_ARG, "null handle");
+  if (!sc->exec) {
+    const int rc = scan_setup(sc);
+    if (rc) return rc;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, sc->s);
+  CK(cudaGraphLaunch(sc->exec, sc->s));
+  cudaEventRecord(e1, sc->s);
+  CK(cudaEventSynchronize(e1));
+  float t = 0;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  sc->run_ms = t;
+  if (ms) *ms = t;
+  unsigned herr = 0;
+  CK(mcpy_sync(&herr, sc->err.p, sizeof herr, cudaMemcpyDeviceToHost));
+  if (herr) return fail(UPCG_ERR_CUDA, "scan contraction timed out (code %u)", herr);
+  for (upcg_generator* g : sc->gens) {
+    CK(mcpy_sync(&g->totCS, g->tot.p, sizeof(double), cudaMemcpyDeviceToHost));
+    g->fidCS = g->totCS;
+    g->next_cand = 0;
+    g->ev_batch.clear();
+    g->ev_flag.clear();
+    g->ev_pos = 0;
+    g->tables_ready = g->lumi_ready = g->xsec_ready = true;
+  }
+  return UPCG_OK;
+}
+
+int upcg_scan_info(const upcg_scan* sc, int* nitems, int* shape, int* rows_total, double* setup_ms) {
+  if (!sc) return fail(UPCG_ERR_ARG, "null handle");
+  if (nitems) *nitems = sc->nitems;
+  if (shape) *shape = sc->shape;
+  if (rows_total) *rows_total = sc->rows_total;
+  if (setup_ms) *setup_ms = sc->setup_ms;
   return UPCG_OK;
 }
 

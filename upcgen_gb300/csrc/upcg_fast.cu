@@ -322,6 +322,7 @@ struct GParams {
   int has_brk;
   float P20, cosk[5], wk[5];
   float u0, h;
+  const double* P20d;  // when set: P20 from the device (k_far_consts)
 };
 
 // G_pq = sum_k w_k P(min(b,20)) (b<20 ? G_AA(b) : 1), b^2 = r_p^2 + r_q^2 +
@@ -336,11 +337,12 @@ __global__ void k_fast_G(GParams gp, int P, __nv_bfloat16* __restrict__ gh,
   const int pp = blockIdx.y;
   if (q >= P) return;
   const float rp = expf(gp.u0 + pp * gp.h), rq = expf(gp.u0 + q * gp.h);
+  const float P20 = gp.P20d ? (float)__ldg(gp.P20d) : gp.P20;
   float g = 0.f;
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     const float bsq = rp * rp + rq * rq + 2.f * rp * rq * gp.cosk[k];
-    float v = gp.P20;
+    float v = P20;
     if (bsq < 400.f) {
       const float b = sqrtf(bsq);
       if (b < 20.f)
@@ -742,7 +744,19 @@ __global__ void __launch_bounds__(kProjThreads) k_fast_project(
   }
 }
 
+// P(20 fm) and c = P(20) sum_k w_k into out[0], out[1] (device-side, for
+// captured scans that may not read them back to the host)
+__global__ void k_far_consts(SplineU brk, int has_brk, LumiParams p, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double P20 = has_brk ? spline_eval(brk, 20.) : 1.;
+  double c = 0.;
+  for (int q = 0; q < 5; ++q) c += P20 * 1. * p.wk[q];
+  out[0] = P20;
+  out[1] = c;
+}
+
 __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, double c_far,
+                              const double* __restrict__ c_far_d,
                               const float* __restrict__ partial, const float4* __restrict__ far_term,
                               double* __restrict__ lumi) {
   const int lc = blockIdx.x * blockDim.x + threadIdx.x;
@@ -753,7 +767,8 @@ __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, d
   double t2 = 0.;
   for (int t = 0; t < ntiles; ++t) t2 += (double)partial[(size_t)lc * ntiles + t];
   const float4 f = far_term[lc];
-  const double s = exp((double)f.y + (double)f.z) * (c_far * (double)f.x + t2);
+  const double cf = c_far_d ? c_far_d[1] : c_far;
+  const double s = exp((double)f.y + (double)f.z) * (cf * (double)f.x + t2);
   lumi[cell] = 2 * kPi * kPi * M * s * p.dm * p.dy;
 }
 
@@ -1140,7 +1155,8 @@ cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, c
 }
 
 cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, double P20,
-                          float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st) {
+                          float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st,
+                          const double* P20d) {
   if (p.gaa.n - 1 > 200) return cudaErrorInvalidValue;
   GParams gp{};
   note_launch();
@@ -1159,6 +1175,7 @@ cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, doubl
   }
   gp.u0 = (float)u0;
   gp.h = (float)h;
+  gp.P20d = P20d;
   dim3 grid((P + 255) / 256, P);
   note_launch();
   k_fast_G<<<grid, 256, 0, st>>>(gp, P, (__nv_bfloat16*)gh, (__nv_bfloat16*)gl);
@@ -1242,12 +1259,19 @@ void flux_table_ktab_range(double* u0, double* u1) {
   *u1 = kKTabU1;
 }
 
+cudaError_t launch_far_consts(const LumiParams& p, int has_brk, double* d_out, cudaStream_t st) {
+  note_launch();
+  k_far_consts<<<1, 32, 0, st>>>(p.brk, has_brk, p, d_out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
                                double c_far, const float* partial, const void* far_term,
-                               double* lumi, cudaStream_t st) {
+                               double* lumi, cudaStream_t st, const double* c_far_d) {
   note_launch();
-  k_fast_finish<<<(ncells + 255) / 256, 256, 0, st>>>(p, cell0, ncells, ntiles, c_far, partial,
-                                                      static_cast<const float4*>(far_term), lumi);
+  k_fast_finish<<<(ncells + 255) / 256, 256, 0, st>>>(p, cell0, ncells, ntiles, c_far, c_far_d,
+                                                      partial, static_cast<const float4*>(far_term),
+                                                      lumi);
   return cudaGetLastError();
 }
 

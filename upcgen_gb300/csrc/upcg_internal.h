@@ -117,7 +117,10 @@ cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, doub
 int fast_grid_points();
 // d_gaa32 / d_brk32: FP32 copies of the G_AA and breakup splines' intervals
 cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, double P20,
-                          float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st);
+                          float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st,
+                          const double* P20d = nullptr);
+// P(20 fm) and the survival kernel beyond 20 fm into d_out[0..1]
+cudaError_t launch_far_consts(const LumiParams& p, int has_brk, double* d_out, cudaStream_t st);
 // Flux tables of the fast form: scaled K0/K1 on ln x, and Q(w, b) of the
 // form-factor flux on (ln w, ln b) (built by the Hankel product H.J).
 struct FastFluxTables {
@@ -168,7 +171,7 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
                             unsigned* d_err, cudaStream_t st);
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
                                double c_far, const float* partial, const void* far_term,
-                               double* lumi, cudaStream_t st);
+                               double* lumi, cudaStream_t st, const double* c_far_d = nullptr);
 cudaError_t contract_selftest(int ncells, int P, uint64_t seed, double* max_rel, double* ms);
 
 // fold + samplers
