@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <new>
 #include <atomic>
@@ -249,6 +250,11 @@ struct upcg_generator {
   upcg_mlp* surrogate = nullptr;  // luminosity method 4: Q(w, b) rows from the MLP
   int surrogate_rows = 0;         // rows of the last Q table that came from it
   bool cap = false;               // enqueue device work only (stream capture of a scan)
+  // scan: earlier configurations whose form factor / G_AA / breakup tables
+  // have the same inputs (their tables are copied, not rebuilt)
+  upcg_generator* ff_donor = nullptr;
+  upcg_generator* gaa_donor = nullptr;
+  upcg_generator* brk_donor = nullptr;
   FastFluxTables ftab_last{};     // the fast form's flux tables of the last build
   int nqn_last = 0;
   int enqueue_scan_front(upcg_scan& sc, int ci);
@@ -573,14 +579,25 @@ int upcg_generator::build_tables() {
   CK(gaa_coef.ensure(199));
   CK(ta_coef.ensure(199));
   CK(gaa_work.ensure(800));
-  CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s));
+  // in a captured scan, a configuration with the same inputs as an earlier one
+  // copies that one's tables instead of rebuilding them
+  if (cap && gaa_donor)
+    CK(cudaMemcpyAsync(gaa_coef.p, gaa_donor->gaa_coef.p, 199 * sizeof(double4),
+                       cudaMemcpyDeviceToDevice, s));
+  else
+    CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s));
   // form factor on 1e6 knots
   const double dq = (kQ2max - kQ2min) / kNQ2;
   CK(ff_y.ensure(kNQ2));
   CK(ff_c.ensure(kNQ2));
   CK(ff_coef.ensure(kNQ2 - 1));
-  CK(launch_formfac_values(ff_y.p, kNQ2, kQ2min, dq, rho0, R, a, side[0]));
-  CK(build_spline_uniform(ff_y.p, kNQ2, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
+  if (cap && ff_donor) {
+    CK(cudaMemcpyAsync(ff_coef.p, ff_donor->ff_coef.p, (size_t)(kNQ2 - 1) * sizeof(double4),
+                       cudaMemcpyDeviceToDevice, side[0]));
+  } else {
+    CK(launch_formfac_values(ff_y.p, kNQ2, kQ2min, dq, rho0, R, a, side[0]));
+    CK(build_spline_uniform(ff_y.p, kNQ2, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
+  }
   CK(cudaEventRecord(ev_join[0], side[0]));
   // breakup probability: knots up to 20 fm + margin (the path evaluates the
   // spline at min(b, 20))
@@ -596,7 +613,10 @@ int upcg_generator::build_tables() {
   CK(brk_y.ensure(brk_n));
   CK(brk_c.ensure(brk_n));
   CK(brk_coef.ensure(brk_n - 1));
-  if (breakupMode > 1) {
+  if (breakupMode > 1 && cap && brk_donor) {
+    CK(cudaMemcpyAsync(brk_coef.p, brk_donor->brk_coef.p, (size_t)(brk_n - 1) * sizeof(double4),
+                       cudaMemcpyDeviceToDevice, side[1]));
+  } else if (breakupMode > 1) {
     CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
                              1e-6, dbb, brk_y.p, side[1]));
     CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1]));
@@ -1975,6 +1995,27 @@ int scan_setup(upcg_scan* sc) {
     rows_total += sc->rows[i];
   }
   if (rows_total > (int64_t)1 << 30) return fail(UPCG_ERR_SIZE, "scan too large");
+  // table sharing: the form factor depends on (A, R, a), G_AA also on sqrt(s)
+  // (sigma_NN), the breakup spline on (sqrt(s), mode)
+  {
+    std::map<std::tuple<int, double, double>, upcg_generator*> ffk;
+    std::map<std::tuple<int, double, double, double>, upcg_generator*> gaak;
+    std::map<std::pair<double, int>, upcg_generator*> brkk;
+    for (upcg_generator* g : sc->gens) {
+      const auto kf = std::make_tuple(g->A, g->R, g->a);
+      const auto kg = std::make_tuple(g->A, g->R, g->a, g->sqrts);
+      const auto kb = std::make_pair(g->sqrts, g->breakupMode);
+      auto f = ffk.find(kf);
+      g->ff_donor = f == ffk.end() ? nullptr : f->second;
+      if (f == ffk.end()) ffk[kf] = g;
+      auto q = gaak.find(kg);
+      g->gaa_donor = q == gaak.end() ? nullptr : q->second;
+      if (q == gaak.end()) gaak[kg] = g;
+      auto b = brkk.find(kb);
+      g->brk_donor = b == brkk.end() ? nullptr : b->second;
+      if (b == brkk.end()) brkk[kb] = g;
+    }
+  }
   sc->rows_total = (int)rows_total;
   const size_t plane = (size_t)P * P;
   CK(sc->ah.ensure((size_t)rows_total * P));
