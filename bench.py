@@ -164,7 +164,7 @@ def cpu_baseline_sample(workload, seconds=15.0):
 # DRAM traffic per launch from one ncu capture of the c2 workload (65,536-cell
 # chunk; profiles/k_contract_c2.md, profiles/k_fast_project_c2.md), scaled by
 # cells for the other chunk: bytes per cell
-CONTRACT_DRAM_BYTES_PER_CELL = (460.295168e6 + 4.016384e6) / 55680  # read + write, one launch
+CONTRACT_DRAM_BYTES_PER_CELL = (404.828160e6 + 3.985408e6) / 55660  # read + write, one launch
 PROJECT_DRAM_BYTES_PER_CELL = (9.432832e6 + 394.498816e6) / 55680
 
 
@@ -338,7 +338,8 @@ def main():
                 "h2d_bytes_per_step": (h1 - h0) // args.e2e_steps,
                 "d2h_bytes_per_step": (d1 - d0) // args.e2e_steps,
                 "events": ev_h},
-        "roofline": {"kernel": "k_contract (tcgen05.mma kind::f16, 3xBF16)", "bound": "tensor",
+        "roofline": {"kernel": "k_contract_pers (persistent tcgen05.mma kind::f16, 3xBF16)",
+                     "bound": "tensor",
                      "achieved": achieved / nlaunch_contract * nlaunch_contract, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "note": f"algorithmic 2*cells*P^2 = {alg_flops:.3e} FLOP per table over "
