@@ -170,14 +170,17 @@ class Oracle:
         self.L.uo_nuc_cs_ym(self.h, _ptr(lumi), _ptr(lumi2), _ptr(cs), _ptr(ratio), C.byref(tot))
         return cs, tot.value, ratio
 
-    def generate(self, cs_ym, cs_zm, n, seed):
+    def generate(self, cs_ym, cs_zm, n, seed, ratio=None):
+        """Events; polarized: cs_zm = (scalar [nm][nz], pseudoscalar [nm][nz])
+        stacked, ratio = nuccs_s / nuccs_p [ny][nm] from nuc_cs_ym (the reference's threshold)."""
         rec = np.zeros((n, 12))
         mbin = np.zeros(n, dtype=np.int32)
         rej = C.c_int64()
         cs_ym = np.ascontiguousarray(cs_ym, dtype=np.float64)
         cs_zm = np.ascontiguousarray(cs_zm, dtype=np.float64)
-        rc = self.L.uo_generate(self.h, _ptr(cs_ym), _ptr(cs_zm), None, n, seed,
-                                _ptr(rec), C.byref(rej), _ptr(mbin))
+        rt = np.ascontiguousarray(ratio, dtype=np.float64) if ratio is not None else None
+        rc = self.L.uo_generate(self.h, _ptr(cs_ym), _ptr(cs_zm), _ptr(rt) if rt is not None else None,
+                                n, seed, _ptr(rec), C.byref(rej), _ptr(mbin))
         if rc != 0:
             raise RuntimeError(f"uo_generate failed: {rc}")
         return rec, rej.value, mbin

@@ -157,7 +157,11 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
                            double* rec, int64_t* rejected, int32_t* mbin_out) {
   using namespace uo;
   const Ctx& c = h->c;
-  if (c.usePolarizedCS) return -3;  // polarized z-sampling is not restated here
+  // polarized (src/UpcGenerator.cpp:686-692, 744-751): cs_zm holds the scalar
+  // [nm][nz] then the pseudoscalar [nm][nz] tables, ratio the nuccs_s / nuccs_p
+  // [ny][nm]; each mass bin has a scalar and a pseudoscalar z sampler
+  const bool pol = c.usePolarizedCS;
+  if (pol && !ratio) return -3;
   const int nm = c.nm, ny = c.ny, nz = c.nz;
   const double dm = (c.mmax - c.mmin) / nm, dz = (c.zmax - c.zmin) / nz,
                dy = (c.ymax - c.ymin) / ny;
@@ -168,14 +172,22 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
   // 2-D sampler over [ny][nm] (x = y-edges, y = m-edges), src/UpcGenerator.cpp:700
   std::vector<double> sum2 = gsl_cdf(cs_ym, (size_t)ny * nm);
   GslUniform rng2(seed);
-  std::vector<std::vector<double>> sumz;
-  std::vector<GslUniform> rngz;
+  std::vector<std::vector<double>> sumz, sumz2;
+  std::vector<GslUniform> rngz, rngz2;
   if (!c.ignoreCSZ) {
     sumz.reserve(nm);
     rngz.reserve(nm);
     for (int i = 0; i < nm; ++i) {
       sumz.push_back(gsl_cdf(cs_zm + (size_t)i * nz, nz));
       rngz.emplace_back(seed);
+    }
+    if (pol) {
+      sumz2.reserve(nm);
+      rngz2.reserve(nm);
+      for (int i = 0; i < nm; ++i) {
+        sumz2.push_back(gsl_cdf(cs_zm + (size_t)(nm + i) * nz, nz));
+        rngz2.emplace_back(seed);
+      }
     }
   }
   RootMT64 groot(seed);
@@ -195,11 +207,17 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
     int mBin = uo_sampler_bin(nm, em.front(), em.back(), mPair);
     double cost;
     if (!c.ignoreCSZ) {
-      double r = rngz[mBin]();
+      bool scalar = true;
+      if (pol) {
+        const int yBin = uo_sampler_bin(ny, ey.front(), ey.back(), yPair);
+        scalar = groot.uniform(0, 1) < ratio[(size_t)yBin * nm + mBin];
+      }
+      std::vector<double>& S = scalar ? sumz[mBin] : sumz2[mBin];
+      double r = scalar ? rngz[mBin]() : rngz2[mBin]();
       if (r == 1.0) r = 0.0;
-      long iz = gsl_find(sumz[mBin], r);
+      long iz = gsl_find(S, r);
       if (iz < 0) return -4;
-      double dl = (r - sumz[mBin][iz]) / (sumz[mBin][iz + 1] - sumz[mBin][iz]);
+      double dl = (r - S[iz]) / (S[iz + 1] - S[iz]);
       cost = ez[iz] + dl * (ez[iz + 1] - ez[iz]);
     } else {
       cost = groot.uniform(-1., 1.);

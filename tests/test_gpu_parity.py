@@ -129,6 +129,67 @@ def test_lumi_polarized(ug, oracle_mod):
     assert rel(s, rs) < TOL and rel(ps, rp) < TOL
 
 
+def _z_mixture_counts(mb, yb, ratio, ts, tp, group):
+    """Expected cos(theta) counts of polarized events: per event the scalar
+    table with probability min(ratio[yb][mb], 1) (the test Uniform(0,1) < ratio,
+    src/UpcGenerator.cpp:744-751), else the pseudoscalar one; table bins
+    summed in groups of `group`."""
+    ps = np.clip(ratio[yb, mb], 0.0, 1.0)
+    fs = ts / ts.sum(1, keepdims=True)
+    fp = tp / tp.sum(1, keepdims=True)
+    e = (ps[:, None] * fs[mb] + (1.0 - ps)[:, None] * fp[mb]).sum(0)
+    return e.reshape(-1, group).sum(1)
+
+
+def _gof(x, expect, lo, hi):
+    from scipy import stats
+    h, _ = np.histogram(x, np.linspace(lo, hi, len(expect) + 1))
+    return stats.chi2.sf(np.sum((h - expect) ** 2 / expect), len(expect) - 1)
+
+
+def test_events_polarized(ug, oracle_mod):
+    """USE_POLARIZED_CS sampling (src/UpcGenerator.cpp:686-692, 744-751): per
+    event the scalar or pseudoscalar z sampler of its mass bin, the scalar one
+    when Uniform(0,1) < polCSRatio = nuccs_s / nuccs_p.  Tau pairs near
+    threshold, where the two z shapes differ most.
+
+    m and y go against the oracle's events (two-sample chi2).  z goes against
+    the expected mixture given each event's bins: the reference seeds every z
+    sampler with the same seed, so its z draws repeat across mass bins and a
+    two-sample test against them has far fewer independent entries than
+    events; the product draws each candidate from its own Philox stream."""
+    p = dict(C1, PROC_ID=15, BREAKUP_MODE=2, USE_POLARIZED_CS=1, MMAX=8, BINS_M=21,
+             BINS_Y=13, NON_ZERO_GAM_PT=0)
+    g = _gen(ug, p)
+    o = _oracle(oracle_mod, p)
+    ls, lp = o.lumi_table(polarized=True)
+    cs, tot, ratio = o.nuc_cs_ym(ls, lp)
+    ts, tp = o.cs_zm_table(1), o.cs_zm_table(2)
+    n = 200000
+    rec, _, _ = o.generate(cs, np.concatenate([ts.ravel(), tp.ravel()]), n, 4321, ratio=ratio)
+    ev, rej, mb = g.generateEvents(3 * n, with_mbin=True)
+    assert rej == 0
+    assert g.totNuclX() == pytest.approx(tot, rel=1e-10)
+    for name, a, b, bins in (("m", ev["m"], rec[:, 0], np.linspace(3.56, 8, 22)),
+                             ("y", ev["y"], rec[:, 1], np.linspace(-6, 6, 14))):
+        pv = _chi2_two_sample(a, b, bins)
+        assert pv > 1e-4, f"{name}: chi2 p-value {pv:.2e}"
+    grid = g.grid()
+    # getBinX with the reference's truncation; checked against the oracle's
+    y = ev["y"].astype(np.float64)
+    yb = np.clip((np.trunc(13 * (y - grid["ymin"])) / (grid["ymax"] - grid["ymin"])).astype(np.int64),
+                 0, 12)
+    assert all(oracle_mod.sampler_bin(13, grid["ymin"], grid["ymax"], v) == b
+               for v, b in zip(y[:2000], yb[:2000]))
+    z = ev["z"].astype(np.float64)
+    pv = _gof(z, _z_mixture_counts(mb, yb, ratio, ts, tp, 2), -1.0, 1.0)
+    assert pv > 1e-4, f"z: chi2 p-value {pv:.2e}"
+    # the test has power: all-scalar, all-pseudoscalar and ratio read as a
+    # scalar fraction s / (s + p) are each rejected
+    for alt in (np.ones_like(ratio), np.zeros_like(ratio), ratio / (1.0 + ratio)):
+        assert _gof(z, _z_mixture_counts(mb, yb, alt, ts, tp, 2), -1.0, 1.0) < 1e-6
+
+
 def test_lumi_alp_other_nucleus(ug, oracle_mod):
     p = dict(C1, PROC_ID=51, ALP_MASS=1, ALP_WIDTH=0.01, NUCLEUS_Z=79, NUCLEUS_A=197,
              WS_R=6.38, WS_A=0.535, SQRTS=200, BREAKUP_MODE=4, BINS_M=21, BINS_Y=25)

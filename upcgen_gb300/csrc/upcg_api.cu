@@ -492,6 +492,9 @@ EventParams upcg_generator::event_params() const {
   e.gz_n = 128;
   e.gpt = guidept.p;
   e.gpt_n = 4096;
+  e.polarized = usePolarizedCS ? 1 : 0;
+  e.ratio = usePolarizedCS ? ratio.p : nullptr;
+  e.cdfz_ps = usePolarizedCS ? cdfz3.p : nullptr;
   return e;
 }
 
@@ -1019,7 +1022,7 @@ int upcg_generator::build_xsec() {
   CK(ptcdf.ensure((size_t)e.pt_ne * (e.pt_nbins + 1)));
   CK(ff32.ensure(kNQ2));
   CK(launch_photon_pt_tables(e, lumi_params().ff, ff32.p, ptcdf.p, s));
-  if (!usePolarizedCS) {
+  {
     CK(guide2.ensure(e.g2_n));
     CK(guidez.ensure((size_t)nm * e.gz_n));
     CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
@@ -1079,10 +1082,9 @@ __global__ void k_find_cut(const int* cnt, const int64_t* off, const uint32_t* m
 int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin,
                                       int64_t* rejected) {
   if (!xsec_ready) return fail(UPCG_ERR_STATE, "upcg_init has not run");
-  if (usePolarizedCS) return fail(UPCG_ERR_PROCESS, "polarized event sampling is not on this path");
   cudaStream_t s = st();
   const EventParams e = event_params();
-  const double* zc = ignoreCSZ ? cdf2.p : cdfz.p;
+  const double* zc = ignoreCSZ ? cdf2.p : (usePolarizedCS ? cdfz2.p : cdfz.p);
   int64_t rej = 0;
   if (!doPtCut && !doEtaCut) {
     CK(launch_events_write(e, cdf2.p, zc, ptcdf.p, next_cand, n, nullptr, nullptr, 0, n, out, mbin, s));
@@ -1581,7 +1583,6 @@ int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted) {
   // its accept flag (1 = passes the cuts, 0 = rejected), as generateEvent.
   if (!g || !ev || !accepted) return fail(UPCG_ERR_ARG, "null argument");
   if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "upcg_init has not run");
-  if (g->usePolarizedCS) return fail(UPCG_ERR_PROCESS, "polarized event sampling is not on this path");
   if (g->ev_pos >= g->ev_flag.size()) {
     const int64_t nb = 4096;
     DBuf<EventRecord> rec;
@@ -1589,7 +1590,7 @@ int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted) {
     CK(rec.ensure(nb));
     CK(flg.ensure(nb));
     const EventParams e = g->event_params();
-    const double* zc = g->ignoreCSZ ? g->cdf2.p : g->cdfz.p;
+    const double* zc = g->ignoreCSZ ? g->cdf2.p : (g->usePolarizedCS ? g->cdfz2.p : g->cdfz.p);
     CK(launch_events_all(e, g->cdf2.p, zc, g->ptcdf.p, g->next_cand, nb, rec.p, flg.p, g->st()));
     g->ev_batch.resize(nb);
     g->ev_flag.resize(nb);

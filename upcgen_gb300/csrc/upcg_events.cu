@@ -179,7 +179,20 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   const double rz = u53(r1.x, r1.y);
   if (!e.ignoreCSZ) {
     const double* cz = cdfz + (size_t)mb * (e.nz + 1);
-    const int iz = cdf_find_from(cz, e.nz, __ldg(e.gz + (size_t)mb * e.gz_n + (int)(rz * (double)e.gz_n)), rz);
+    int iz;
+    if (e.polarized) {
+      // scalar or pseudoscalar z sampler of this mass bin: the reference draws
+      // Uniform(0, 1) < polCSRatio[yBin][mBin] (getBinX of y, as getBinY)
+      const double yedge_hi = e.ymin + e.dy * e.ny;
+      int yb = (int)((double)(int)(e.ny * (c.y - e.ymin)) / (yedge_hi - e.ymin));
+      yb = yb < 0 ? 0 : (yb > e.ny - 1 ? e.ny - 1 : yb);
+      const uint4 r4 = philox4x32_10(make_uint4(clo, chi, 4u, 0x55504347u), key);
+      if (!(u53(r4.x, r4.y) < __ldg(e.ratio + (size_t)yb * e.nm + mb)))
+        cz = e.cdfz_ps + (size_t)mb * (e.nz + 1);
+      iz = cdf_find(cz, e.nz, rz);
+    } else {
+      iz = cdf_find_from(cz, e.nz, __ldg(e.gz + (size_t)mb * e.gz_n + (int)(rz * (double)e.gz_n)), rz);
+    }
     const double z0 = __ldg(cz + iz), z1 = __ldg(cz + iz + 1);
     const double dl = z1 > z0 ? (rz - z0) / (z1 - z0) : 0.;
     const double zlo = e.zmin + e.dz * iz, zhi = e.zmin + e.dz * (iz + 1);
@@ -495,7 +508,7 @@ cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const doub
   const int n2 = e.nm * e.ny;
   note_launch();
   k_guide_rows_d<<<(e.g2_n + 255) / 256, 256, 0, st>>>(d_cdf2, 1, n2, e.g2_n, d_g2);
-  if (!e.ignoreCSZ) {
+  if (!e.ignoreCSZ && !e.polarized) {  // polarized z: plain searches on two CDF sets
     const int64_t nz = (int64_t)e.nm * e.gz_n;
     note_launch();
     k_guide_rows_d<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(d_cdfz, e.nm, e.nz, e.gz_n, d_gz);

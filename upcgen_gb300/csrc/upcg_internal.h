@@ -214,6 +214,12 @@ struct EventParams {
   int gz_n;
   const uint16_t* gpt;  // photon-pT tables, gpt_n buckets per table
   int gpt_n;
+  // polarized cross section: the z CDFs passed to the kernels are the scalar
+  // ones, cdfz_ps the pseudoscalar ones, ratio[iy][im] the reference's
+  // nuccs_s / nuccs_p threshold (src/UpcCrossSection.cpp:658, UpcGenerator.cpp:744-751)
+  int polarized;
+  const double* ratio;
+  const double* cdfz_ps;
 };
 // guide tables (EventParams) of the built CDFs; d_g2 / d_gz / d_gpt sized
 // g2_n, nm * gz_n, pt_ne * gpt_n
