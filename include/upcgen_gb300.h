@@ -73,6 +73,13 @@ int upcg_set_lumi_file_directory(upcg_generator* g, const char* dir);
  * table (the reference's twoPhotonLumi.root is keyed by nothing,
  * src/UpcCrossSection.cpp:481-491); 0 (default): always compute */
 int upcg_set_lumi_cache(upcg_generator* g, int enable);
+/* The cache file of the current configuration (no counterpart in the
+ * reference, whose file is always twoPhotonLumi[Pol].root,
+ * src/UpcCrossSection.cpp:481-482): "<dir>/upcg_lumi_<16 hex>.bin", the hex
+ * digits a 64-bit FNV-1a hash of a key text naming every input of the table.
+ * last_hit (optional): 1 if the last upcg_init read the table from it, 0 if it
+ * computed the table, -1 if the cache was not used.  Host only. */
+int upcg_lumi_cache_file(upcg_generator* g, char* path, size_t len, int* last_hit);
 /* CUDA stream (cudaStream_t) for every launch of this handle; NULL = the
  * handle's own stream */
 int upcg_set_stream(upcg_generator* g, void* stream);

@@ -26,7 +26,7 @@ assert EVENT_DTYPE.itemsize == 48
 ABI_SYMBOLS = [
     "upcg_create", "upcg_destroy", "upcg_set_parameter", "upcg_config_from_file",
     "upcg_set_collision_system", "upcg_set_seed", "upcg_set_num_threads",
-    "upcg_set_debug_level", "upcg_set_lumi_file_directory", "upcg_set_lumi_cache",
+    "upcg_set_debug_level", "upcg_set_lumi_file_directory", "upcg_set_lumi_cache", "upcg_lumi_cache_file",
     "upcg_set_stream", "upcg_set_lumi_method", "upcg_init", "upcg_compute_nucl_xsection",
     "upcg_tot_nucl_x", "upcg_fid_nucl_x", "upcg_get_grid", "upcg_lumi_table",
     "upcg_lumi_table_device", "upcg_nuc_cs_ym", "upcg_cs_zm_table", "upcg_flux_point",
@@ -70,6 +70,7 @@ def load_library(path=None):
         "upcg_set_collision_system": [vp, C.c_float, i, i], "upcg_set_seed": [vp, C.c_long],
         "upcg_set_num_threads": [vp, i], "upcg_set_debug_level": [vp, i],
         "upcg_set_lumi_file_directory": [vp, cp], "upcg_set_lumi_cache": [vp, i],
+        "upcg_lumi_cache_file": [vp, cp, C.c_size_t, C.POINTER(C.c_int)],
         "upcg_set_stream": [vp, vp], "upcg_set_lumi_method": [vp, i], "upcg_init": [vp],
         "upcg_compute_nucl_xsection": [vp], "upcg_tot_nucl_x": [vp, dp],
         "upcg_fid_nucl_x": [vp, dp],
@@ -381,6 +382,15 @@ class UpcGenerator:
 
     def setLumiCache(self, enable):
         _check(self._L.upcg_set_lumi_cache(self._h, int(bool(enable))))
+
+    def lumiCacheFile(self):
+        """(path of this configuration's cache file, last_hit): last_hit 1 if
+        the last init read the table from it, 0 if it computed the table, -1
+        if the cache was not used."""
+        buf = C.create_string_buffer(4096)
+        hit = C.c_int()
+        _check(self._L.upcg_lumi_cache_file(self._h, buf, len(buf), C.byref(hit)))
+        return buf.value.decode(), hit.value
 
     def setStream(self, stream_handle):
         _check(self._L.upcg_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))

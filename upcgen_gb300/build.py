@@ -1,6 +1,7 @@
 """Build the CUDA library in-tree: ``upcgen_gb300/libupcgen_gb300.so``.
 
-Every translation unit under ``csrc/`` is compiled for sm_103a only
+Every translation unit under ``csrc/`` (``.cu`` kernels and host code, ``.cpp``
+host-only code) is compiled by nvcc for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), in parallel, and linked with
 nvcc into one shared library exporting the C ABI of ``include/upcgen_gb300.h``.
 No torch, no cmake: nvcc and the CUDA runtime only.
@@ -27,7 +28,7 @@ def nvcc():
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _headers():

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/upcgen_gb300.h"
+#include "upcg_cache.h"
 #include "upcg_internal.h"
 
 using namespace upcg;
@@ -245,6 +246,7 @@ struct upcg_generator {
   int numThreads = 1, debug = 0;
   std::string lumiDir = ".";
   bool lumiCache = false;
+  int lumi_cache_hit = -1;  // last init: 1 table read from the cache, 0 computed, -1 cache unused
   int lumiMethod = 0;
   int row_lo = 0, row_hi = -1;  // m-rows of the luminosity this handle computes (-1: all)
   upcg_mlp* surrogate = nullptr;  // luminosity method 4: Q(w, b) rows from the MLP
@@ -355,6 +357,11 @@ struct upcg_generator {
   int setup_process();
   int build_tables();
   int build_lumi();
+  int build_lumi_cached();
+  std::string lumi_cache_key() const;
+  bool lumi_cache_usable() const {
+    return lumiCache && lumiMethod != 4 && !cap && row_lo <= 0 && (row_hi < 0 || row_hi >= nm);
+  }
   int build_lumi_grid();
   int breakup_at_20(double* P20);
   int build_xsec();
@@ -739,6 +746,73 @@ int upcg_generator::build_lumi_grid() {
   CK(mcpy_sync(&herr, ferr.p, sizeof herr, cudaMemcpyDeviceToHost));
   if (herr) return fail(UPCG_ERR_CUDA, "tensor-core product timed out (code %u)", herr);
   lumi_ready = true;
+  return UPCG_OK;
+}
+
+// Revision of the table-producing code; part of every cache key, raised
+// whenever a change moves the values of any luminosity method.
+constexpr int kLumiAlgorithmRevision = 1;
+constexpr double kLumiLockTimeoutS = 600.;
+
+std::string upcg_generator::lumi_cache_key() const {
+  // every input of the table, doubles as exact hex floats
+  char buf[768];
+  snprintf(buf, sizeof buf,
+           "upcgen_gb300 two-photon luminosity L dm dy [nm][ny]; revision %d; method %d; "
+           "Z %d; A %d; R %a; a %a; sqrts %a; g1 %a; g2 %a; point flux %d; breakup mode %d; "
+           "polarized %d; m [%a, %a] bins %d; y [%a, %a] bins %d",
+           kLumiAlgorithmRevision, lumiMethod, Z, A, R, a, sqrts, g1, g2, isPoint ? 1 : 0,
+           breakupMode, usePolarizedCS ? 1 : 0, mmin, mmax, nm, ymin, ymax, ny);
+  return buf;
+}
+
+namespace {
+struct LockGuard {
+  std::string path;
+  bool held = false;
+  LockGuard(const std::string& p, double timeout) : path(p) {
+    held = lumi_lock_acquire(path, timeout) == 1;
+  }
+  ~LockGuard() {
+    if (held) lumi_lock_release(path);
+  }
+};
+}  // namespace
+
+int upcg_generator::build_lumi_cached() {
+  // src/UpcCrossSection.cpp:463-592 with a keyed cache file (upcg_cache.cpp)
+  const std::string key = lumi_cache_key();
+  const std::string path = lumiDir + "/" + lumi_cache_file_name(key);
+  const int ntab = usePolarizedCS ? 2 : 1;
+  const size_t ncell = (size_t)nm * ny;
+  const auto t0 = std::chrono::steady_clock::now();
+  LockGuard lock(path + ".lock", kLumiLockTimeoutS);
+  std::vector<double> host;
+  if (lumi_cache_read(path, key, ntab, nm, ny, host)) {
+    cudaStream_t s = st();
+    CK(lumi.ensure(ncell));
+    CK(mcpy(lumi.p, host.data(), ncell * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (usePolarizedCS) {
+      CK(lumi2.ensure(ncell));
+      CK(mcpy(lumi2.p, host.data() + ncell, ncell * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    for (int k = 1; k < 8; ++k) timings[k] = 0;
+    timings[1] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    lumi_cache_hit = 1;
+    lumi_ready = true;
+    return UPCG_OK;
+  }
+  const int rc = build_lumi();
+  if (rc) return rc;
+  lumi_cache_hit = 0;
+  if (!lock.held) return UPCG_OK;  // another process holds the file: compute only
+  host.resize((size_t)ntab * ncell);
+  CK(mcpy_sync(host.data(), lumi.p, ncell * sizeof(double), cudaMemcpyDeviceToHost));
+  if (usePolarizedCS)
+    CK(mcpy_sync(host.data() + ncell, lumi2.p, ncell * sizeof(double), cudaMemcpyDeviceToHost));
+  if (lumi_cache_write(path, key, ntab, nm, ny, host.data()) != 0 && debug > 0)
+    fprintf(stderr, "upcgen_gb300: could not write the luminosity cache %s\n", path.c_str());
   return UPCG_OK;
 }
 
@@ -1311,9 +1385,21 @@ int upcg_init(upcg_generator* g) {
   if (g->breakupMode < 1 || g->breakupMode > 4) return fail(UPCG_ERR_ARG, "BREAKUP_MODE must be 1..4");
   int rc = g->build_tables();
   if (rc) return rc;
-  rc = g->build_lumi();
+  g->lumi_cache_hit = -1;
+  rc = g->lumi_cache_usable() ? g->build_lumi_cached() : g->build_lumi();
   if (rc) return rc;
   return g->build_xsec();
+}
+
+int upcg_lumi_cache_file(upcg_generator* g, char* path, size_t len, int* last_hit) {
+  if (!g || !path || len == 0) return fail(UPCG_ERR_ARG, "null argument");
+  const int rc = g->setup_process();  // the key holds the derived mass range
+  if (rc) return rc;
+  const std::string p = g->lumiDir + "/" + lumi_cache_file_name(g->lumi_cache_key());
+  if (p.size() + 1 > len) return fail(UPCG_ERR_SIZE, "path needs %zu bytes", p.size() + 1);
+  std::memcpy(path, p.c_str(), p.size() + 1);
+  if (last_hit) *last_hit = g->lumi_cache_hit;
+  return UPCG_OK;
 }
 
 int upcg_compute_nucl_xsection(upcg_generator* g) {
