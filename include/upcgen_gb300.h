@@ -34,6 +34,7 @@ extern "C" {
 #define UPCG_ERR_NUMERIC (-5)   /* QAGS failure the reference would abort on */
 #define UPCG_ERR_NOMEM (-6)
 #define UPCG_ERR_SIZE (-7)      /* output buffer too small */
+#define UPCG_ERR_IO (-8)        /* file could not be opened or written */
 
 typedef struct upcg_generator upcg_generator;
 
@@ -191,6 +192,46 @@ int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t*
                          int64_t* rejected);
 int upcg_generate_events_device(upcg_generator* g, int64_t n, upcg_event* out_device,
                                 int32_t* mbin_device, int64_t* rejected);
+/* ---- event output (UpcGenerator::writeEvent / generateEvents' files,
+ * src/UpcGenerator.cpp:589-628, 834-926) ----------------------------------
+ * Particles per event as generateEvent lists them (:767-812): a lepton pair
+ * is 2 (pdg +-PDG, status 23, mother 0), an ALP 3 (the ALP: pdg 51, status
+ * 23, mother 0, momentum = the photons' sum; two photons: pdg 22, status 33,
+ * mother 1). */
+int upcg_particles_per_event(upcg_generator* g, int* n);
+/* Columns of the reference's ROOT tree "particles" (:842-853), one row per
+ * particle, row = event * particles_per_event + (particleID - 1). */
+typedef struct upcg_particle_columns {
+  int32_t* eventNumber;
+  int32_t* pdgCode;
+  int32_t* particleID;
+  int32_t* statusID;
+  int32_t* motherID;
+  double* px;
+  double* py;
+  double* pz;
+  double* e;
+} upcg_particle_columns;
+/* Device records -> device columns (every pointer device memory), eventNumber
+ * = first_event + index; one kernel on the handle's stream. */
+int upcg_event_particles_device(upcg_generator* g, const upcg_event* ev_device, int64_t n,
+                                int64_t first_event, const upcg_particle_columns* cols);
+/* HepMC3 ASCII of n host records as WriterHepMC writes them
+ * (include/UpcGenerator.h:192-242): "E", "U GEV MM" and "P" lines, numbers
+ * as setprecision(9); without the version / listing lines.  *len = the text's
+ * size; UPCG_ERR_SIZE when out is NULL or cap is smaller.  Host only. */
+int upcg_format_hepmc3(upcg_generator* g, const upcg_event* ev, int64_t n, int64_t first_event,
+                       char* out, size_t cap, size_t* len);
+/* generateEvents with file output: the next n accepted events to path.
+ * format 0: HepMC3 ASCII (the reference's events.hepmc, complete with the
+ * version and listing lines); 1: the particle columns (the reference's
+ * events.root tree) in a column file, converted to ROOT by
+ * upcgen_gb300/particles_to_root.C.  threads: host formatting threads
+ * (0 = every core).  Device generation of the next batch overlaps the file
+ * work of the current one.  Sets fidNuclX over the n events. */
+int upcg_write_events(upcg_generator* g, const char* path, int64_t n, int format, int threads,
+                      int64_t* rejected);
+
 /* UpcGenerator::generateEvent, src/UpcGenerator.cpp:715-832: one candidate.
  * Returns 1 (accepted) or 0 (rejected by the cuts) in *accepted and the
  * event in *ev; candidates are drawn from the same sequence as

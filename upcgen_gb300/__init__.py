@@ -27,6 +27,8 @@ ABI_SYMBOLS = [
     "upcg_create", "upcg_destroy", "upcg_set_parameter", "upcg_config_from_file",
     "upcg_set_collision_system", "upcg_set_seed", "upcg_set_num_threads",
     "upcg_set_debug_level", "upcg_set_lumi_file_directory", "upcg_set_lumi_cache", "upcg_lumi_cache_file",
+    "upcg_particles_per_event", "upcg_event_particles_device", "upcg_format_hepmc3",
+    "upcg_write_events",
     "upcg_set_stream", "upcg_set_lumi_method", "upcg_init", "upcg_compute_nucl_xsection",
     "upcg_tot_nucl_x", "upcg_fid_nucl_x", "upcg_get_grid", "upcg_lumi_table",
     "upcg_lumi_table_device", "upcg_nuc_cs_ym", "upcg_cs_zm_table", "upcg_flux_point",
@@ -71,6 +73,10 @@ def load_library(path=None):
         "upcg_set_num_threads": [vp, i], "upcg_set_debug_level": [vp, i],
         "upcg_set_lumi_file_directory": [vp, cp], "upcg_set_lumi_cache": [vp, i],
         "upcg_lumi_cache_file": [vp, cp, C.c_size_t, C.POINTER(C.c_int)],
+        "upcg_particles_per_event": [vp, C.POINTER(i)],
+        "upcg_event_particles_device": [vp, vp, i64, i64, vp],
+        "upcg_format_hepmc3": [vp, vp, i64, i64, vp, sz, C.POINTER(sz)],
+        "upcg_write_events": [vp, cp, i64, i, i, C.POINTER(i64)],
         "upcg_set_stream": [vp, vp], "upcg_set_lumi_method": [vp, i], "upcg_init": [vp],
         "upcg_compute_nucl_xsection": [vp], "upcg_tot_nucl_x": [vp, dp],
         "upcg_fid_nucl_x": [vp, dp],
@@ -473,6 +479,32 @@ class UpcGenerator:
         _check(self._L.upcg_generate_events(self._h, int(n), _p(out), _p(mb) if with_mbin else None,
                                             C.byref(rej)))
         return (out, rej.value, mb) if with_mbin else (out, rej.value)
+
+    def particlesPerEvent(self):
+        n = C.c_int()
+        _check(self._L.upcg_particles_per_event(self._h, C.byref(n)))
+        return n.value
+
+    def formatHepMC3(self, events, first_event=0):
+        """HepMC3 ASCII lines of host event records (no version / listing lines)."""
+        ev = np.ascontiguousarray(events, dtype=EVENT_DTYPE)
+        n = C.c_size_t()
+        rc = self._L.upcg_format_hepmc3(self._h, _p(ev), len(ev), int(first_event), None, 0, C.byref(n))
+        if rc not in (0, -7):
+            _check(rc)
+        buf = C.create_string_buffer(n.value + 1)
+        _check(self._L.upcg_format_hepmc3(self._h, _p(ev), len(ev), int(first_event), buf, len(buf),
+                                          C.byref(n)))
+        return buf.raw[:n.value].decode()
+
+    def writeEvents(self, path, n, format="hepmc", threads=0):
+        """generateEvents with file output (HepMC3 ASCII, or the particle
+        columns of the reference's ROOT tree); returns the rejected count."""
+        fmt = {"hepmc": 0, "columns": 1}.get(format, format)
+        rej = C.c_int64()
+        _check(self._L.upcg_write_events(self._h, str(path).encode(), int(n), int(fmt), int(threads),
+                                         C.byref(rej)))
+        return rej.value
 
     def generateEvent(self):
         """One candidate: (1 or 0, event record), as UpcGenerator::generateEvent."""

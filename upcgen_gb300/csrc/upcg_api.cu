@@ -39,11 +39,16 @@ unsigned long long launch_count() { return g_launches.load(std::memory_order_rel
 namespace {
 // host <-> device bytes the library has copied (upcg_copy_bytes)
 std::atomic<unsigned long long> g_h2d{0}, g_d2h{0};
+}  // namespace
 
+namespace upcg {
 void count_copy(size_t n, cudaMemcpyKind k) {
   if (k == cudaMemcpyHostToDevice) g_h2d.fetch_add(n, std::memory_order_relaxed);
   if (k == cudaMemcpyDeviceToHost) g_d2h.fetch_add(n, std::memory_order_relaxed);
 }
+}  // namespace upcg
+
+namespace {
 
 cudaError_t mcpy(void* dst, const void* src, size_t n, cudaMemcpyKind k, cudaStream_t s) {
   count_copy(n, k);
@@ -57,9 +62,10 @@ cudaError_t mcpy_sync(void* dst, const void* src, size_t n, cudaMemcpyKind k) {
 }  // namespace
 
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
 
+namespace upcg {
 int fail(int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -69,6 +75,9 @@ int fail(int code, const char* fmt, ...) {
   g_err = buf;
   return code;
 }
+}  // namespace upcg
+
+namespace {
 
 #define CK(call)                                                                         \
   do {                                                                                   \
@@ -413,6 +422,13 @@ int upcg_generator::set_param(const std::string& k, const std::string& v) {
 
 // Process-specific overrides of UpcGenerator::init (src/UpcGenerator.cpp:66-140)
 // and the lepton masses of UpcTwoPhotonDilep (src/UpcTwoPhotonDilep.cpp:29-44).
+namespace upcg {
+cudaStream_t handle_stream(upcg_generator* g) { return g->st(); }
+void set_fiducial(upcg_generator* g, int64_t n, int64_t rejected) {
+  g->fidCS = g->totCS * (double)n / (double)(n + rejected);  // src/UpcGenerator.cpp:889
+}
+}  // namespace upcg
+
 int upcg_generator::setup_process() {
   ignoreCSZ = false;
   if (procID == 51) {

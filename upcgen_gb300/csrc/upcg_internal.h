@@ -6,6 +6,8 @@
 
 #include "upcg_device.cuh"
 
+struct upcg_generator;
+
 namespace upcg {
 
 constexpr int kNb = 120;                // b-bins per side (include/UpcCrossSection.h:116-117)
@@ -45,6 +47,14 @@ struct QagsStats {
 // Every kernel launch of the library calls note_launch() first; the count
 // (upcg_kernel_launches) lets a caller see how many kernels a call issued.
 void note_launch();
+// the library's error status: records the message for upcg_last_error, returns code
+int fail(int code, const char* fmt, ...);
+// host <-> device byte counters of upcg_copy_bytes
+void count_copy(size_t n, cudaMemcpyKind k);
+// the CUDA stream a handle launches on
+cudaStream_t handle_stream(::upcg_generator* g);
+// fidNuclX after n accepted events with `rejected` rejections
+void set_fiducial(::upcg_generator* g, int64_t n, int64_t rejected);
 unsigned long long launch_count();
 
 // grid (precision) form of the luminosity, point flux: see upcg_grid.cu
