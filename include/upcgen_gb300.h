@@ -192,6 +192,25 @@ int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t*
                          int64_t* rejected);
 int upcg_generate_events_device(upcg_generator* g, int64_t n, upcg_event* out_device,
                                 int32_t* mbin_device, int64_t* rejected);
+/* ---- photonuclear path: coherent vector mesons (PROC_ID 443 J/psi, 100443
+ * psi(2S), 553 Upsilon(1S); DECAY_PDG 11, 13 or 2212; SHADOWING 0, the
+ * impulse approximation -- the other options need the reference's
+ * nuclear-shadowing tables and return UPCG_ERR_PROCESS).  upcg_init builds
+ * calcNucCrossSectionY's dsigma/dy on the y-bins (one mass bin at m_V) and
+ * the samplers of generateEvent's vector-meson branch. ---------------------
+ * calcPhotonFlux, src/UpcCrossSection.cpp:700-722: the photon flux of one
+ * nucleus integrated over b with the survival factors, at n (m, y) points */
+int upcg_photon_flux(upcg_generator* g, const double* m, const double* y, double* out, size_t n);
+/* UpcPhotoNuclearVM::calcCrossSectionY, src/UpcPhotoNuclearVM.cpp:340-381
+ * (impulse approximation), at n rapidities */
+int upcg_vm_cross_section_y(upcg_generator* g, const double* y, double* out, size_t n);
+/* calcNucCrossSectionY, src/UpcCrossSection.cpp:724-748: dsigma/dy [ny] at
+ * the left y-edges, the emitter ratio [ny] (optional) and sigma_tot (mb) */
+int upcg_nuc_cs_y(upcg_generator* g, double* cs, double* ratio, size_t ny, double* tot_mb);
+/* PDG code of the decay products of the configured process: DECAY_PDG for a
+ * vector meson, 22 for the ALP, 0 for a lepton pair */
+int upcg_decay_pdg(upcg_generator* g, int* pdg);
+
 /* ---- event output (UpcGenerator::writeEvent / generateEvents' files,
  * src/UpcGenerator.cpp:589-628, 834-926) ----------------------------------
  * Particles per event as generateEvent lists them (:767-812): a lepton pair

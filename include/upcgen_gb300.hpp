@@ -138,21 +138,26 @@ class UpcGenerator {
   // pairProduction (src/UpcGenerator.cpp:388-423): two leptons, status 23,
   // mother 0, charges sign1 = +-1, sign2 = -sign1; the ALP (status 23) and its
   // two decay photons (pdg 22, status 33, mother 1) as twoPartDecayUniform
-  // (:526-561).
+  // (:526-561); a vector meson and its two daughters likewise.
   void fill(const upcg_event& e, std::vector<int>& pdgs, std::vector<int>& statuses,
             std::vector<int>& mothers, std::vector<LorentzVector>& particles) {
-    int pdg = 0, charged = 0;
+    int pdg = 0, charged = 0, dpdg = 0;
     check(upcg_particle_pdg(h_, &pdg, &charged));
+    check(upcg_decay_pdg(h_, &dpdg));
     const LorentzVector a{e.p0[0], e.p0[1], e.p0[2], e.p0[3]};
     const LorentzVector b{e.p1[0], e.p1[1], e.p1[2], e.p1[3]};
-    if (pdg == 51) {
+    if (dpdg != 0) {  // ALP -> 2 photons; vector meson -> +-DECAY_PDG (twoPartDecayVM, :425-472)
       particles.push_back(LorentzVector{a.px + b.px, a.py + b.py, a.pz + b.pz, a.e + b.e});
       pdgs.push_back(pdg);
       statuses.push_back(23);
       mothers.push_back(0);
-      for (const LorentzVector& g : {a, b}) {
-        particles.push_back(g);
-        pdgs.push_back(22);
+      const int s1 = dpdg == 22 ? 1 : (e.sign > 0 ? 1 : -1);
+      const int s2 = dpdg == 22 ? 1 : -s1;
+      particles.push_back(a);
+      particles.push_back(b);
+      pdgs.push_back(s1 * dpdg);
+      pdgs.push_back(s2 * dpdg);
+      for (int k = 0; k < 2; ++k) {
         statuses.push_back(33);
         mothers.push_back(1);
       }

@@ -45,6 +45,9 @@ def lib():
         L.uo_two_photon_lumi.argtypes = [p, d, d]; L.uo_two_photon_lumi.restype = d
         L.uo_two_photon_lumi_pol.argtypes = [p, d, d, dp, dp]
         L.uo_cs_m.argtypes = [p, d, i]; L.uo_cs_m.restype = d
+        L.uo_photon_flux.argtypes = [p, d, d]; L.uo_photon_flux.restype = d
+        L.uo_vm_cs_y.argtypes = [p, d]; L.uo_vm_cs_y.restype = d
+        L.uo_nuc_cs_y.argtypes = [p, p, p, dp]
         L.uo_cs_zm.argtypes = [p, d, d, i]; L.uo_cs_zm.restype = d
         L.uo_lumi_table.argtypes = [p, p, p, i, i]
         L.uo_cs_zm_table.argtypes = [p, i, p]
@@ -141,6 +144,22 @@ class Oracle:
 
     def cs_m(self, m, flag=0):
         return self.L.uo_cs_m(self.h, m, flag)
+
+    def photon_flux(self, m, y):
+        """calcPhotonFlux (src/UpcCrossSection.cpp:700-722)."""
+        return self.L.uo_photon_flux(self.h, m, y)
+
+    def vm_cs_y(self, y):
+        """UpcPhotoNuclearVM::calcCrossSectionY in the impulse approximation."""
+        return self.L.uo_vm_cs_y(self.h, y)
+
+    def nuc_cs_y(self):
+        """calcNucCrossSectionY: (dsigma/dy [ny], emitter ratio [ny], sigma_tot)."""
+        ny = self.grid()["ny"]
+        cs, ratio, tot = np.zeros(ny), np.zeros(ny), C.c_double()
+        if self.L.uo_nuc_cs_y(self.h, _ptr(cs), _ptr(ratio), C.byref(tot)) != 0:
+            raise RuntimeError("uo_nuc_cs_y: not a vector-meson configuration")
+        return cs, ratio, tot.value
 
     def cs_zm(self, z, m, flag=0):
         return self.L.uo_cs_zm(self.h, z, m, flag)

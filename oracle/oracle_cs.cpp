@@ -28,6 +28,7 @@ namespace uo {
 const double kAlpha = 1.0 / 137.035999074;
 const double kHc = 0.1973269718;
 const double kMProt = 0.9382720813;
+const double kMNeut = 0.939565346;
 const double kMEl = 0.000510998946;
 const double kMMu = 0.1056583745;
 const double kMTau = 1.77686;
@@ -97,6 +98,8 @@ int Ctx::set_param(const std::string& k, const std::string& v) {
     else if (k == "USE_POLARIZED_CS") usePolarizedCS = std::stoi(v);
     else if (k == "SEED") seed = std::stol(v);
     else if (k == "ORACLE_FLUX_EPS") fluxEps = std::stod(v);
+    else if (k == "SHADOWING") shadowing = std::stoi(v);  // src/UpcGenerator.cpp:299-304
+    else if (k == "DECAY_PDG") dghtPDG = std::stoi(v);
     else return 1;  // accepted and ignored (PYTHIA_*, output flags, ...)
   } catch (...) {
     return -1;
@@ -124,7 +127,30 @@ int Ctx::setup_process() {
     if (mmin < mPart * 2.) mmin = mPart * 2.;
     return 0;
   }
-  return -1;  // light-by-light, dipion and vector mesons are not on this path
+  if (procID == 443 || procID == 100443 || procID == 553) {
+    // UpcPhotoNuclearVM::UpcPhotoNuclearVM (src/UpcPhotoNuclearVM.cpp:55-93)
+    // and the generator's settings for it (src/UpcGenerator.cpp:131-140)
+    isVM = true;
+    ignoreCSZ = true;
+    partPDG = procID;
+    isCharged = false;
+    vm_pw = 0.4;
+    if (procID == 443) { mPart = 3.0969; vm_c0 = 342.; vm_mu2 = 3.; }
+    if (procID == 100443) { mPart = 3.6861; vm_c0 = 56.8; vm_mu2 = 4.; }
+    if (procID == 553) { mPart = 9.3987; vm_c0 = 0.902; vm_pw = 0.447; vm_mu2 = 22.4; }
+    if (dghtPDG == 11) mDght = kMEl;
+    else if (dghtPDG == 13) mDght = kMMu;
+    else if (dghtPDG == 2212) mDght = kMProt;
+    else return -3;  // "Unsupported decay mode"
+    mmin = mPart - 1e-6;
+    mmax = mPart + 1e-6;
+    nm = 1;
+    // nuclear shadowing (options 1-4) needs the reference's EPS09 / LTA
+    // tables; the impulse approximation (0) is restated here
+    if (shadowing != 0) return -4;
+    return 0;
+  }
+  return -1;  // light-by-light and dipion are not on this path
 }
 
 double Ctx::cs_m(double m, int flag) const {
@@ -527,6 +553,7 @@ void Ctx::two_photon_lumi_pol(double M, double Y, double* ns, double* np) const 
 int Ctx::init_tables() {
   if (setup_process() != 0) return -2;
   factor = Z * Z * kAlpha / M_PI / M_PI / kHc / kHc;  // src/UpcCrossSection.cpp:120
+  mNucl = (Z * kMProt + (A - Z) * kMNeut) / A;         // src/UpcCrossSection.cpp:121
   rho0 = calc_ws_rho();
   prepare_gaa();
   prepare_form_fac();
@@ -605,6 +632,73 @@ void Ctx::nuc_cs_ym(const double* lumi, const double* lumi2, double* cs, double*
   *tot = total * 1e-6;
 }
 
+// ------------------------------------------------------ photonuclear path --
+// calcPhotonFlux (src/UpcCrossSection.cpp:700-722): the photon flux of one
+// nucleus integrated over b with the survival factors, 120 log b-bins.
+double Ctx::photon_flux(double M, double Y) const {
+  double k = M / 2. * std::exp(Y);
+  double bmin = isPoint ? 1 * R : 0.05 * R;
+  double bmax = std::max(5. * g1 * kHc / k, 5 * R);
+  double log_delta_b = (std::log(bmax) - std::log(bmin)) / nb1;
+  double sum = 0;
+  for (int i = 0; i < nb1; i++) {
+    double bl = bmin * std::exp(i * log_delta_b);
+    double bh = bmin * std::exp((i + 1) * log_delta_b);
+    double b = (bh + bl) / 2.;
+    double bu = 1.;
+    if (breakupMode != 1) bu = breakup.eval(b < 20. ? b : 20.);
+    double g = b < 20. ? gaa.eval(b) : 1.;
+    sum += bu * g * flux_form(b, k, nullptr) * b * (bh - bl);
+  }
+  return 2. * M_PI * k * sum;
+}
+
+// UpcPhotoNuclearVM::calcCrossSectionY (src/UpcPhotoNuclearVM.cpp:340-381) in
+// the impulse approximation (SHADOWING 0: cAcP2 = Rg = 1), with dsdt
+// (:42-53) and PhiA = TF1::Integral of calcFormFac^2 over [tmin, tmin + 1]
+// (converged here by QAGS at epsrel 1e-12).
+double Ctx::vm_cs_y(double y) const {
+  double w = mPart / 2. * std::exp(y);
+  double beamE = 0.5 * sqrts;
+  double Wgp2 = 4. * w * beamE;
+  double Wgp = std::sqrt(Wgp2);
+  const double wmin = kMProt + mPart;
+  double csGammaP = 0.;
+  if (Wgp > wmin)
+    csGammaP = vm_c0 * std::pow(1. - (wmin * wmin) / Wgp2, 1.5) * std::pow(Wgp2 * 1e-4, vm_pw);
+  double m2 = mPart * mPart;
+  double x = m2 / Wgp2;
+  double tmin = x * x * mNucl * mNucl;
+  double tmax = tmin + 1.;
+  auto f2 = [&](double t) {
+    double f = calc_form_fac(t);
+    return f * f;
+  };
+  QagsResult r = qags(f2, tmin, tmax, 0., 1e-12, 1000);
+  return csGammaP * r.result * 1e-6;
+}
+
+// calcNucCrossSectionY (src/UpcCrossSection.cpp:724-748): dsigma/dy at the
+// left edges of the y-bins, both photon emitters; ratio = emitter 1 / 2.
+void Ctx::nuc_cs_y(double* cs, double* ratio, double* tot) const {
+  const double dy = (ymax - ymin) / ny;
+  std::vector<double> u1(ny), u2(ny);
+  const int nthr = numThreads < 1 ? 1 : numThreads;
+#pragma omp parallel for num_threads(nthr) schedule(dynamic)
+  for (int iy = 0; iy < ny; iy++) {
+    double y = ymin + dy * iy;
+    u1[iy] = photon_flux(mPart, y) * vm_cs_y(y);
+    u2[iy] = photon_flux(mPart, -y) * vm_cs_y(-y);
+  }
+  double total = 0;
+  for (int iy = 0; iy < ny; iy++) {
+    cs[iy] = u1[iy] + u2[iy];
+    total += u1[iy] + u2[iy];
+    ratio[iy] = u1[iy] / u2[iy];
+  }
+  *tot = total * dy;
+}
+
 }  // namespace uo
 
 // ------------------------------------------------------------ C interface --
@@ -673,6 +767,13 @@ void uo_two_photon_lumi_pol(const uo_ctx* h, double m, double y, double* ls, dou
   h->c.two_photon_lumi_pol(m, y, ls, lp);
 }
 double uo_cs_m(const uo_ctx* h, double m, int flag) { return h->c.cs_m(m, flag); }
+double uo_photon_flux(const uo_ctx* h, double m, double y) { return h->c.photon_flux(m, y); }
+double uo_vm_cs_y(const uo_ctx* h, double y) { return h->c.vm_cs_y(y); }
+int uo_nuc_cs_y(const uo_ctx* h, double* cs, double* ratio, double* tot) {
+  if (!h->c.initialized || !h->c.isVM) return -1;
+  h->c.nuc_cs_y(cs, ratio, tot);
+  return 0;
+}
 double uo_cs_zm(const uo_ctx* h, double z, double m, int flag) { return h->c.cs_zm(z, m, flag); }
 int uo_lumi_table(uo_ctx* h, double* lumi, double* lumi2, int im_lo, int im_hi) {
   if (!h->c.initialized) return -1;

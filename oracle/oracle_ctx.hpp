@@ -22,6 +22,11 @@ struct Ctx {
   double mPart = 0;
   int partPDG = 0;
   bool isCharged = true, ignoreCSZ = false;
+  // vector-meson photoproduction (src/UpcPhotoNuclearVM.cpp:55-93): the
+  // reference's SHADOWING and DECAY_PDG keys, the meson's dsdt constants
+  bool isVM = false;
+  int shadowing = 0, dghtPDG = 0;
+  double mDght = 0, vm_c0 = 0, vm_pw = 0.4, vm_mu2 = 0, mNucl = 0;
   // grid
   double zmin = -1, zmax = 1, mmin = 3.56, mmax = 50., ymin = -6., ymax = 6.;
   int nz = 100, nm = 1001, ny = 121;
@@ -69,6 +74,10 @@ struct Ctx {
   void cs_zm_table(int flag, double* out) const;
   void nuc_cs_ym(const double* lumi, const double* lumi2, double* cs, double* ratio,
                  double* tot) const;
+  // photonuclear path (oracle_vm.cpp)
+  double photon_flux(double m, double y) const;
+  double vm_cs_y(double y) const;
+  void nuc_cs_y(double* cs, double* ratio, double* tot) const;
 };
 
 }  // namespace uo

@@ -162,6 +162,8 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
   // [ny][nm]; each mass bin has a scalar and a pseudoscalar z sampler
   const bool pol = c.usePolarizedCS;
   if (pol && !ratio) return -3;
+  // vector mesons: cs_ym is [ny][1], ratio the emitter ratio [ny] of nuc_cs_y
+  if (c.isVM && !ratio) return -3;
   const int nm = c.nm, ny = c.ny, nz = c.nz;
   const double dm = (c.mmax - c.mmin) / nm, dz = (c.zmax - c.zmin) / nz,
                dy = (c.ymax - c.ymin) / ny;
@@ -222,9 +224,34 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
     } else {
       cost = groot.uniform(-1., 1.);
     }
-    // getPairMomentum (src/UpcCrossSection.cpp:1053-1074)
     Vec4 pp;
-    if (!c.useNonzeroGamPt) {
+    if (c.isVM) {
+      // target pick (src/UpcGenerator.cpp:761-764): Uniform(0,1) < the y-bin's
+      // emitter ratio; getMomentumVM (src/UpcCrossSection.cpp:1076-1104)
+      const int yBin = uo_sampler_bin(ny, ey.front(), ey.back(), yPair);
+      const bool target = groot.uniform(0, 1) < ratio[yBin];
+      const double sign = target ? 1 : -1;
+      const double ePhot = mPair / 2 * std::exp(sign * yPair);
+      const double ePom = mPair / 2 * std::exp(-sign * yPair);
+      const double ptPhot = ptgen.sample(ePhot, groot);
+      const double phi1 = groot.uniform(0, 2 * M_PI);
+      const double phi2 = groot.uniform(0, 2 * M_PI);
+      const double tmin = (ePom * ePom) / (c.g1 * c.g1);
+      double ptPom;
+      while (true) {
+        ptPom = 32. * groot.uniform(0., 1.) * 0.1973269718 * c.R;
+        const double t2 = tmin + ptPom * ptPom;
+        const double ff = c.calc_form_fac(t2) / c.A;
+        const double test = groot.uniform(0., 1.);
+        if (test < ff * ff * ptPom) break;
+      }
+      const double px = ptPhot * std::cos(phi1) + ptPom * std::cos(phi2);
+      const double py = ptPhot * std::sin(phi1) + ptPom * std::sin(phi2);
+      const double pt = std::sqrt(px * px + py * py);
+      const double mt = std::sqrt(mPair * mPair + pt * pt);
+      pp = Vec4{px, py, mt * std::sinh(yPair), mt * std::cosh(yPair)};
+    } else if (!c.useNonzeroGamPt) {
+      // getPairMomentum (src/UpcCrossSection.cpp:1053-1074)
       double mt = mPair;
       pp = Vec4{0., 0., mt * std::sinh(yPair), mt * std::cosh(yPair)};
     } else {
@@ -244,7 +271,41 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
     double sign0 = 1;
     bool pass = true;
     const double bx = pp.x / pp.t, by = pp.y / pp.t, bz = pp.z / pp.t;
-    if (c.procID != 51) {
+    if (c.isVM) {
+      // cuts on the meson (the decay comes after checkKinCuts), then
+      // twoPartDecayVM (src/UpcGenerator.cpp:425-472)
+      if (c.doPtCut && pt_of(pp) < c.minPt) pass = false;
+      if (pass && c.doEtaCut) {
+        double e = eta_of(pp);
+        if (e < c.minEta || e > c.maxEta) pass = false;
+      }
+      if (pass) {
+        double theta, dndtheta = 0;
+        while (true) {
+          theta = M_PI * groot.uniform(0., 1.);
+          double test = groot.uniform(0., 1.);
+          const double ct = std::cos(theta);
+          if (c.dghtPDG == 11 || c.dghtPDG == 13) dndtheta = std::sin(theta) * (1. + ct * ct);
+          else if (c.dghtPDG == 2212) dndtheta = std::sin(theta) * (1. + 0.605 * ct * ct);
+          if (test < dndtheta) break;
+        }
+        sign0 = groot.uniform(-1, 1) > 0 ? 1 : -1;
+        double mag2 = pp.t * pp.t - (pp.x * pp.x + pp.y * pp.y + pp.z * pp.z);
+        double pMag = std::sqrt(mag2 / 4. - c.mDght * c.mDght);
+        double phi = groot.uniform(0., 2. * M_PI);
+        double vx = pMag * std::sin(theta) * std::cos(phi);
+        double vy = pMag * std::sin(theta) * std::sin(phi);
+        double vz = pMag * std::cos(theta);
+        d0 = set_vect_m(-vx, -vy, -vz, c.mDght);
+        d1 = set_vect_m(vx, vy, vz, c.mDght);
+        double pm = std::sqrt(pp.x * pp.x + pp.y * pp.y + pp.z * pp.z);
+        double u1 = pm > 0 ? pp.x / pm : 0, u2 = pm > 0 ? pp.y / pm : 0, u3 = pm > 0 ? pp.z / pm : 0;
+        rotate_uz(d0, u1, u2, u3);
+        rotate_uz(d1, u1, u2, u3);
+        boost(d0, bx, by, bz);
+        boost(d1, bx, by, bz);
+      }
+    } else if (c.procID != 51) {
       // pair production (src/UpcGenerator.cpp:769-776, 388-423)
       double mag2 = pp.t * pp.t - (pp.x * pp.x + pp.y * pp.y + pp.z * pp.z);
       double pMag = std::sqrt(mag2 / 4 - c.mPart * c.mPart);

@@ -82,6 +82,9 @@ int uo_nuc_cs_ym(const uo_ctx* h, const double* lumi, const double* lumi2,
  * rec[i*12 + ...] = m, y, z, charge-sign of particle 0, then px,py,pz,E of
  * the two final-state particles (ALP: the two decay photons).  Needs the cs
  * tables from uo_nuc_cs_ym / uo_cs_zm_table. */
+double uo_photon_flux(const uo_ctx* h, double m, double y);
+double uo_vm_cs_y(const uo_ctx* h, double y);
+int uo_nuc_cs_y(const uo_ctx* h, double* cs, double* ratio, double* tot);
 int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
                 const double* ratio, int64_t nevents, uint64_t seed,
                 double* rec, int64_t* rejected, int32_t* mbin);

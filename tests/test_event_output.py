@@ -30,12 +30,16 @@ def _records(ug, n, seed):
     return ev
 
 
-def _particles(e, pdg, charged):
+def _particles(e, pdg, charged, dpdg=0):
     """generateEvent's vectors for one record: (pdgs, statuses, mothers, momenta)."""
     a = [float(x) for x in e["p0"]]
     b = [float(x) for x in e["p1"]]
     if pdg == 51:
         return ([51, 22, 22], [23, 33, 33], [0, 1, 1],
+                [[a[i] + b[i] for i in range(4)], a, b])
+    if dpdg:  # vector meson: twoPartDecayVM's signed daughters
+        s1 = 1 if e["sign"] > 0 else -1
+        return ([pdg, s1 * dpdg, -s1 * dpdg], [23, 33, 33], [0, 1, 1],
                 [[a[i] + b[i] for i in range(4)], a, b])
     s1 = (1 if e["sign"] > 0 else -1) if charged else 1
     s2 = -s1 if charged else 1
@@ -47,10 +51,10 @@ def _mass(p):
     return -np.sqrt(-mm) if mm < 0 else np.sqrt(mm)
 
 
-def _hepmc_reference(events, pdg, charged, first):
+def _hepmc_reference(events, pdg, charged, first, dpdg=0):
     out = []
     for i, e in enumerate(events):
-        pdgs, sts, mos, ps = _particles(e, pdg, charged)
+        pdgs, sts, mos, ps = _particles(e, pdg, charged, dpdg)
         nv, last = -1, -1  # writeEvent's vertex count
         for m in mos:
             if m != last:
@@ -63,18 +67,20 @@ def _hepmc_reference(events, pdg, charged, first):
     return "".join(out)
 
 
-@pytest.mark.parametrize("proc,pdg,ppe", [(13, 13, 2), (15, 15, 2), (51, 51, 3)])
-def test_hepmc_text_matches_reference_writer(ug, proc, pdg, ppe):
-    g = ug.UpcGenerator({"PROC_ID": proc})
+@pytest.mark.parametrize("proc,pdg,ppe,dpdg", [(13, 13, 2, 0), (15, 15, 2, 0), (51, 51, 3, 0),
+                                               (443, 443, 3, 13), (553, 553, 3, 2212)])
+def test_hepmc_text_matches_reference_writer(ug, proc, pdg, ppe, dpdg):
+    g = ug.UpcGenerator({"PROC_ID": proc, "DECAY_PDG": dpdg})
     assert g.particlesPerEvent() == ppe
+    assert g.decayPDG() == (dpdg or (22 if proc == 51 else 0))
     ev = _records(ug, 20000, proc)
     text = g.formatHepMC3(ev, first_event=17)
-    assert text == _hepmc_reference(ev, pdg, True, 17)
+    assert text == _hepmc_reference(ev, pdg, True, 17, dpdg)
     events, rows = eo.read_hepmc3(text)
-    assert len(events) == 20000 and events[0] == (17, 1 if proc == 51 else 0, ppe)
+    assert len(events) == 20000 and events[0] == (17, 1 if ppe == 3 else 0, ppe)
     # 9 significant digits give back every float32 momentum exactly
     px = rows[:, 3].reshape(-1, ppe)
-    col = 1 if proc == 51 else 0
+    col = 1 if ppe == 3 else 0
     assert np.array_equal(px[:, col].astype(np.float32), ev["p0"][:, 0])
     assert g.formatHepMC3(ev[:0]) == ""
 
@@ -125,6 +131,19 @@ struct TTree {
 _MAIN = r"""int particles_to_root(const char*, const char*);
 int main(int, char** v) { return particles_to_root(v[1], v[2]); }
 """
+
+
+def test_vector_meson_configuration_errors(ug):
+    # src/UpcPhotoNuclearVM.cpp:80-87: the decay mode must be one the meson knows
+    with pytest.raises(ug.UpcgError, match="DECAY_PDG"):
+        ug.UpcGenerator({"PROC_ID": 443}).particlesPerEvent()
+    with pytest.raises(ug.UpcgError, match="SHADOWING"):
+        ug.UpcGenerator({"PROC_ID": 443, "DECAY_PDG": 13, "SHADOWING": 2}).particlesPerEvent()
+    # the generator's single mass bin around m_V (src/UpcGenerator.cpp:131-140)
+    g = ug.UpcGenerator({"PROC_ID": 553, "DECAY_PDG": 11, "BINS_M": 50})
+    g.particlesPerEvent()
+    gr = g.grid()
+    assert gr["nm"] == 1 and abs(gr["mmin"] - (9.3987 - 1e-6)) < 1e-12
 
 
 def test_particles_root_macro(tmp_path):

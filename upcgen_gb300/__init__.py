@@ -28,7 +28,8 @@ ABI_SYMBOLS = [
     "upcg_set_collision_system", "upcg_set_seed", "upcg_set_num_threads",
     "upcg_set_debug_level", "upcg_set_lumi_file_directory", "upcg_set_lumi_cache", "upcg_lumi_cache_file",
     "upcg_particles_per_event", "upcg_event_particles_device", "upcg_format_hepmc3",
-    "upcg_write_events",
+    "upcg_write_events", "upcg_photon_flux", "upcg_vm_cross_section_y", "upcg_nuc_cs_y",
+    "upcg_decay_pdg",
     "upcg_set_stream", "upcg_set_lumi_method", "upcg_init", "upcg_compute_nucl_xsection",
     "upcg_tot_nucl_x", "upcg_fid_nucl_x", "upcg_get_grid", "upcg_lumi_table",
     "upcg_lumi_table_device", "upcg_nuc_cs_ym", "upcg_cs_zm_table", "upcg_flux_point",
@@ -77,6 +78,8 @@ def load_library(path=None):
         "upcg_event_particles_device": [vp, vp, i64, i64, vp],
         "upcg_format_hepmc3": [vp, vp, i64, i64, vp, sz, C.POINTER(sz)],
         "upcg_write_events": [vp, cp, i64, i, i, C.POINTER(i64)],
+        "upcg_photon_flux": [vp, vp, vp, vp, sz], "upcg_vm_cross_section_y": [vp, vp, vp, sz],
+        "upcg_nuc_cs_y": [vp, vp, vp, sz, dp], "upcg_decay_pdg": [vp, C.POINTER(i)],
         "upcg_set_stream": [vp, vp], "upcg_set_lumi_method": [vp, i], "upcg_init": [vp],
         "upcg_compute_nucl_xsection": [vp], "upcg_tot_nucl_x": [vp, dp],
         "upcg_fid_nucl_x": [vp, dp],
@@ -479,6 +482,34 @@ class UpcGenerator:
         _check(self._L.upcg_generate_events(self._h, int(n), _p(out), _p(mb) if with_mbin else None,
                                             C.byref(rej)))
         return (out, rej.value, mb) if with_mbin else (out, rej.value)
+
+    # -- photonuclear path (vector mesons)
+    def calcPhotonFlux(self, m, y):
+        """UpcCrossSection::calcPhotonFlux at points (m, y)."""
+        m, y = np.broadcast_arrays(_arr(m), _arr(y))
+        m, y = np.ascontiguousarray(m), np.ascontiguousarray(y)
+        out = np.zeros(m.size)
+        _check(self._L.upcg_photon_flux(self._h, _p(m), _p(y), _p(out), m.size))
+        return out
+
+    def vmCrossSectionY(self, y):
+        """UpcPhotoNuclearVM::calcCrossSectionY (impulse approximation)."""
+        y = np.ascontiguousarray(_arr(y))
+        out = np.zeros(y.size)
+        _check(self._L.upcg_vm_cross_section_y(self._h, _p(y), _p(out), y.size))
+        return out
+
+    def nucCSY(self):
+        """calcNucCrossSectionY: (dsigma/dy [ny], emitter ratio [ny], sigma_tot mb)."""
+        ny = self.grid()["ny"]
+        cs, ratio, tot = np.zeros(ny), np.zeros(ny), C.c_double()
+        _check(self._L.upcg_nuc_cs_y(self._h, _p(cs), _p(ratio), ny, C.byref(tot)))
+        return cs, ratio, tot.value
+
+    def decayPDG(self):
+        n = C.c_int()
+        _check(self._L.upcg_decay_pdg(self._h, C.byref(n)))
+        return n.value
 
     def particlesPerEvent(self):
         n = C.c_int()

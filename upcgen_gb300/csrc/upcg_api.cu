@@ -245,6 +245,11 @@ struct upcg_generator {
   double sqrts = 5020., g1 = 0, g2 = 0, gtot = 0;
   int procID = 15;
   double aLep = 0, alpMass = 1., alpWidth = 0.010;
+  // vector mesons (src/UpcPhotoNuclearVM.cpp:55-93): the SHADOWING and
+  // DECAY_PDG keys and the meson's dsdt constants
+  bool isVM = false;
+  int shadowing = 0, dghtPDG = 0;
+  double mDght = 0, vm_c0 = 0, vm_pw = 0.4;
   double zmin = -1, zmax = 1, mmin = 3.56, mmax = 50., ymin = -6., ymax = 6.;
   int nz = 100, nm = 1001, ny = 121;
   bool isPoint = true, useNonzeroGamPt = true, usePolarizedCS = false;
@@ -281,7 +286,9 @@ struct upcg_generator {
   DBuf<double> ff_y, ff_c, brk_y, brk_c, lumi, lumi2, cs, ratio, cszm, cszm2, cszm3;
   DBuf<double> cdf2, cdfz, cdfz2, cdfz3, flux, partial, tot, gws, pts_a, pts_b, pts_c;
   DBuf<double4> ff_coef, gaa_coef, ta_coef, brk_coef;
-  DBuf<double> gaa_work, bu_tab, cdf_scratch;  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
+  DBuf<double> gaa_work, bu_tab, cdf_scratch;
+  DBuf<double> vm_m, vm_y, vm_b, vm_k, vm_w, vm_f, vm_flux, vm_s, pom_vals, pom_cdf;
+  DBuf<unsigned> vm_err;  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
   std::vector<double> bu_host;
   int bu_nt = 0;
   // side streams of the table set-up and their fork / join events
@@ -364,8 +371,20 @@ struct upcg_generator {
 
   int set_param(const std::string& k, const std::string& v);
   int setup_process();
+  // vector mesons: the decay-angle draws of the last events all ended
+  int vm_check() {
+    if (!isVM) return UPCG_OK;
+    unsigned n = 0;
+    const cudaError_t e = cudaMemcpyAsync(&n, vm_err.p, sizeof n, cudaMemcpyDeviceToHost, st());
+    if (e != cudaSuccess || cudaStreamSynchronize(st()) != cudaSuccess)
+      return fail(UPCG_ERR_CUDA, "reading the decay-angle error count failed");
+    if (n) return fail(UPCG_ERR_NUMERIC, "%u candidates ran out of decay-angle draws", n);
+    return UPCG_OK;
+  }
   int build_tables();
   int build_lumi();
+  int build_vm();
+  VmParams vm_params() const;
   int build_lumi_cached();
   std::string lumi_cache_key() const;
   bool lumi_cache_usable() const {
@@ -411,6 +430,8 @@ int upcg_generator::set_param(const std::string& k, const std::string& v) {
     else if (k == "BREAKUP_MODE") breakupMode = std::stoi(v);
     else if (k == "NON_ZERO_GAM_PT") useNonzeroGamPt = std::stoi(v);
     else if (k == "USE_POLARIZED_CS") usePolarizedCS = std::stoi(v);
+    else if (k == "SHADOWING") shadowing = std::stoi(v);  // src/UpcGenerator.cpp:299-304
+    else if (k == "DECAY_PDG") dghtPDG = std::stoi(v);
     else if (k == "SEED") seed = std::stol(v);
     else return UPCG_OK;  // keys of other paths: accepted and ignored
   } catch (...) {
@@ -431,6 +452,32 @@ void set_fiducial(upcg_generator* g, int64_t n, int64_t rejected) {
 
 int upcg_generator::setup_process() {
   ignoreCSZ = false;
+  isVM = false;
+  if (procID == 443 || procID == 100443 || procID == 553) {
+    // UpcPhotoNuclearVM::UpcPhotoNuclearVM (src/UpcPhotoNuclearVM.cpp:55-93)
+    // and the generator's settings for it (src/UpcGenerator.cpp:131-140)
+    isVM = true;
+    ignoreCSZ = true;
+    partPDG = procID;
+    isCharged = false;
+    vm_pw = 0.4;
+    if (procID == 443) { mPart = 3.0969; vm_c0 = 342.; }
+    if (procID == 100443) { mPart = 3.6861; vm_c0 = 56.8; }
+    if (procID == 553) { mPart = 9.3987; vm_c0 = 0.902; vm_pw = 0.447; }
+    if (dghtPDG == 11) mDght = kMEl;
+    else if (dghtPDG == 13) mDght = kMMu;
+    else if (dghtPDG == 2212) mDght = kMProt;
+    else return fail(UPCG_ERR_ARG, "DECAY_PDG %d: the vector mesons decay to 11, 13 or 2212", dghtPDG);
+    if (shadowing != 0)
+      return fail(UPCG_ERR_PROCESS,
+                  "SHADOWING %d needs the nuclear-shadowing tables (EPS09 / LTA); this path has the "
+                  "impulse approximation (SHADOWING 0)", shadowing);
+    if (usePolarizedCS) return fail(UPCG_ERR_PROCESS, "polarized cross section needs a dilepton process");
+    mmin = mPart - 1e-6;
+    mmax = mPart + 1e-6;
+    nm = 1;
+    return UPCG_OK;
+  }
   if (procID == 51) {
     ignoreCSZ = true;
     mmin = alpMass - 4. * alpWidth;
@@ -518,6 +565,13 @@ EventParams upcg_generator::event_params() const {
   e.polarized = usePolarizedCS ? 1 : 0;
   e.ratio = usePolarizedCS ? ratio.p : nullptr;
   e.cdfz_ps = usePolarizedCS ? cdfz3.p : nullptr;
+  e.vm = isVM ? 1 : 0;
+  e.vm_ratio = isVM ? ratio.p : nullptr;
+  e.pom_cdf = isVM ? pom_cdf.p : nullptr;
+  e.vm_g1 = g1;
+  e.mDght = (float)mDght;
+  e.dght_law = dghtPDG == 2212 ? 1 : 0;
+  e.vm_err = isVM ? vm_err.p : nullptr;
   return e;
 }
 
@@ -1075,6 +1129,81 @@ int upcg_generator::build_lumi() {
   return UPCG_OK;
 }
 
+VmParams upcg_generator::vm_params() const {
+  VmParams v{};
+  v.mPart = mPart;
+  v.sqrts = sqrts;
+  v.c0 = vm_c0;
+  v.pw = vm_pw;
+  v.wmin = kMProt + mPart;  // dsdt's threshold (src/UpcPhotoNuclearVM.cpp:89)
+  v.mNucl = (Z * kMProt + (A - Z) * kMNeut) / A;  // src/UpcCrossSection.cpp:121
+  v.rho0 = rho0;
+  v.R = R;
+  v.a = a;
+  std::vector<double> x, w;
+  gauss_legendre(16, x, w);
+  for (int j = 0; j < 16; ++j) {
+    v.glx[j] = x[j];
+    v.glw[j] = w[j];
+  }
+  return v;
+}
+
+// calcNucCrossSectionY (src/UpcCrossSection.cpp:724-748): per y-bin the photon
+// flux of either nucleus (calcPhotonFlux at m_V, +-y) times the meson's
+// dsigma/dy; the pomeron table of getMomentumVM.
+int upcg_generator::build_vm() {
+  cudaStream_t s = st();
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, s);
+  const int n2 = 2 * ny;
+  const double dy = (ymax - ymin) / ny;
+  std::vector<double> hm((size_t)n2, mPart), hy((size_t)n2);
+  for (int iy = 0; iy < ny; ++iy) {
+    hy[iy] = ymin + dy * iy;
+    hy[ny + iy] = -hy[iy];
+  }
+  CK(vm_m.ensure(n2));
+  CK(vm_y.ensure(n2));
+  CK(mcpy(vm_m.p, hm.data(), n2 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(mcpy(vm_y.p, hy.data(), n2 * sizeof(double), cudaMemcpyHostToDevice, s));
+  const size_t nn = (size_t)n2 * kNb;
+  CK(vm_b.ensure(nn));
+  CK(vm_k.ensure(nn));
+  CK(vm_w.ensure(nn));
+  CK(vm_f.ensure(nn));
+  CK(vm_flux.ensure(n2));
+  CK(vm_s.ensure(n2));
+  CK(stats.ensure(1));
+  CK(cudaMemsetAsync(stats.p, 0, sizeof(QagsStats), s));
+  CK(launch_photon_flux(lumi_params(), vm_m.p, vm_y.p, n2, vm_b.p, vm_k.p, vm_w.p, vm_f.p, vm_flux.p,
+                        stats.p, s));
+  const VmParams v = vm_params();
+  CK(launch_vm_cs_y(v, vm_y.p, n2, vm_s.p, s));
+  CK(cs.ensure(ny));
+  CK(ratio.ensure(ny));
+  CK(tot.ensure(1));
+  CK(launch_vm_fold(vm_flux.p, vm_s.p, ny, dy, cs.p, ratio.p, tot.p, s));
+  CK(pom_vals.ensure(kPomN));
+  CK(pom_cdf.ensure(kPomN + 1));
+  CK(launch_pom_table(v, pom_vals.p, pom_cdf.p, s));
+  CK(vm_err.ensure(1));
+  CK(cudaMemsetAsync(vm_err.p, 0, sizeof(unsigned), s));
+  cudaEventRecord(t1, s);
+  CK(cudaEventSynchronize(t1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  for (int k = 1; k < 8; ++k) timings[k] = 0;
+  timings[1] = ms;
+  CK(mcpy_sync(&last_stats, stats.p, sizeof(QagsStats), cudaMemcpyDeviceToHost));
+  lumi_ready = false;
+  return UPCG_OK;
+}
+
 int upcg_generator::build_xsec() {
   cudaStream_t s = st();
   const FoldParams f = fold_params();
@@ -1085,15 +1214,19 @@ int upcg_generator::build_xsec() {
     cudaEventCreate(&t1);
     cudaEventRecord(t0, s);
   }
-  CK(cs.ensure(ncell));
-  CK(ratio.ensure(usePolarizedCS ? ncell : 1));
-  CK(partial.ensure((ncell + 255) / 256 + 1));
-  CK(tot.ensure(1));
-  CK(launch_fold(f, lumi.p, usePolarizedCS ? lumi2.p : nullptr, cs.p, ratio.p, partial.p, tot.p, s));
+  if (!isVM) {  // vector mesons: cs, ratio and tot come from build_vm
+    CK(cs.ensure(ncell));
+    CK(ratio.ensure(usePolarizedCS ? ncell : 1));
+    CK(partial.ensure((ncell + 255) / 256 + 1));
+    CK(tot.ensure(1));
+    CK(launch_fold(f, lumi.p, usePolarizedCS ? lumi2.p : nullptr, cs.p, ratio.p, partial.p, tot.p, s));
+  }
   CK(cdf2.ensure((size_t)ncell + 1));
   CK(cdf_scratch.ensure(cdf_2d_scratch_doubles(ncell)));
   CK(launch_cdf_2d(cs.p, ncell, cdf2.p, cdf_scratch.p, s));
-  if (!usePolarizedCS) {
+  if (isVM) {
+    CK(cdfz.ensure(1));  // no z distribution (ignoreCSZ)
+  } else if (!usePolarizedCS) {
     CK(cszm.ensure((size_t)nm * nz));
     CK(launch_cs_zm(f, 0, cszm.p, s));
     CK(cdfz.ensure((size_t)nm * (nz + 1)));
@@ -1180,7 +1313,7 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     CK(launch_events_write(e, cdf2.p, zc, ptcdf.p, next_cand, n, nullptr, nullptr, 0, n, out, mbin, s));
     next_cand += (uint64_t)n;
     *rejected = 0;
-    return UPCG_OK;
+    return vm_check();
   }
   int64_t done = 0;
   const int64_t kMaxChunk = (int64_t)1 << 28;
@@ -1228,7 +1361,7 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     }
   }
   *rejected = rej;
-  return UPCG_OK;
+  return vm_check();
 }
 
 // ---------------------------------------------------------------- scans ----
@@ -1402,6 +1535,11 @@ int upcg_init(upcg_generator* g) {
   int rc = g->build_tables();
   if (rc) return rc;
   g->lumi_cache_hit = -1;
+  if (g->isVM) {  // photonuclear: calcNucCrossSectionY instead of the two-photon luminosity
+    rc = g->build_vm();
+    if (rc) return rc;
+    return g->build_xsec();
+  }
   rc = g->lumi_cache_usable() ? g->build_lumi_cached() : g->build_lumi();
   if (rc) return rc;
   return g->build_xsec();
@@ -1453,6 +1591,7 @@ int upcg_get_grid(const upcg_generator* g, double* mmin, double* mmax, int* nm, 
 
 int upcg_lumi_table(upcg_generator* g, double* out, size_t n, double* out2) {
   if (!g || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (g->isVM) return fail(UPCG_ERR_PROCESS, "PROC_ID %d has no two-photon luminosity", g->procID);
   if (!g->lumi_ready) return fail(UPCG_ERR_STATE, "luminosity not computed");
   const size_t need = (size_t)g->nm * g->ny;
   if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);
@@ -1793,6 +1932,65 @@ int upcg_set_candidate_offset(upcg_generator* g, uint64_t counter) {
   g->ev_batch.clear();
   g->ev_flag.clear();
   g->ev_pos = 0;
+  return UPCG_OK;
+}
+
+int upcg_decay_pdg(upcg_generator* g, int* pdg) {
+  if (!g || !pdg) return fail(UPCG_ERR_ARG, "null argument");
+  const int rc = g->setup_process();
+  if (rc) return rc;
+  *pdg = g->isVM ? g->dghtPDG : (g->procID == 51 ? 22 : 0);
+  return UPCG_OK;
+}
+
+int upcg_photon_flux(upcg_generator* g, const double* m, const double* y, double* out, size_t n) {
+  if (!g || !m || !y || !out) return fail(UPCG_ERR_ARG, "null argument");
+  if (n == 0) return UPCG_OK;
+  if (n > (size_t)(1 << 24)) return fail(UPCG_ERR_SIZE, "at most 2^24 points per call");
+  int rc = need_tables(g);
+  if (rc) return rc;
+  rc = points_in(g, m, y, n);
+  if (rc) return rc;
+  cudaStream_t s = g->st();
+  const size_t nn = n * kNb;
+  DBuf<double> b, k, w, f;
+  CK(b.ensure(nn));
+  CK(k.ensure(nn));
+  CK(w.ensure(nn));
+  CK(f.ensure(nn));
+  CK(g->stats.ensure(1));
+  CK(cudaMemsetAsync(g->stats.p, 0, sizeof(QagsStats), s));
+  CK(launch_photon_flux(g->lumi_params(), g->pts_a.p, g->pts_b.p, (int)n, b.p, k.p, w.p, f.p,
+                        g->pts_c.p, g->stats.p, s));
+  rc = points_out(g, out, n);
+  if (rc) return rc;
+  CK(mcpy_sync(&g->last_stats, g->stats.p, sizeof(QagsStats), cudaMemcpyDeviceToHost));
+  return UPCG_OK;
+}
+
+int upcg_vm_cross_section_y(upcg_generator* g, const double* y, double* out, size_t n) {
+  if (!g || !y || !out) return fail(UPCG_ERR_ARG, "null argument");
+  int rc = g->setup_process();
+  if (rc) return rc;
+  if (!g->isVM) return fail(UPCG_ERR_PROCESS, "PROC_ID %d is not a vector meson", g->procID);
+  if (n == 0) return UPCG_OK;
+  rc = need_tables(g);  // rho0 of the form factor
+  if (rc) return rc;
+  rc = points_in(g, y, nullptr, n);
+  if (rc) return rc;
+  CK(launch_vm_cs_y(g->vm_params(), g->pts_a.p, (int)n, g->pts_c.p, g->st()));
+  return points_out(g, out, n);
+}
+
+int upcg_nuc_cs_y(upcg_generator* g, double* cs, double* ratio, size_t ny, double* tot_mb) {
+  if (!g || !cs) return fail(UPCG_ERR_ARG, "null argument");
+  if (!g->isVM) return fail(UPCG_ERR_PROCESS, "PROC_ID %d is not a vector meson", g->procID);
+  if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "cross section not computed");
+  if (ny < (size_t)g->ny) return fail(UPCG_ERR_SIZE, "need %d doubles", g->ny);
+  CK(mcpy(cs, g->cs.p, g->ny * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  if (ratio) CK(mcpy(ratio, g->ratio.p, g->ny * sizeof(double), cudaMemcpyDeviceToHost, g->st()));
+  CK(cudaStreamSynchronize(g->st()));
+  if (tot_mb) *tot_mb = g->totCS;
   return UPCG_OK;
 }
 

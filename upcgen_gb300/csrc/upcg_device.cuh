@@ -23,6 +23,7 @@ namespace upcg {
 constexpr double kAlpha = 1.0 / 137.035999074;  // include/UpcPhysConstants.h:26-32
 constexpr double kHc = 0.1973269718;
 constexpr double kMProt = 0.9382720813;
+constexpr double kMNeut = 0.939565346;
 constexpr double kMEl = 0.000510998946;
 constexpr double kMMu = 0.1056583745;
 constexpr double kMTau = 1.77686;
@@ -94,6 +95,18 @@ __device__ __forceinline__ void bessel_k01(double x, double& k0, double& k1) {
 }
 
 // Abramowitz & Stegun 9.8.3 / 9.8.7 / 9.8.8 (TMath::BesselK1).
+// calcFormFac (src/UpcCrossSection.cpp:436-445): the Woods-Saxon form factor
+// (symmetrised-Fermi closed form), normalised to ~A at Q2 -> 0
+__device__ __forceinline__ double calc_form_fac(double Q2, double rho0, double R, double a) {
+  const double Q = sqrt(Q2) / kHc;
+  const double coshVal = cosh(kPi * Q * a);
+  const double sinhVal = sinh(kPi * Q * a);
+  double ff = 4 * kPi * kPi * rho0 * a * a * a / (Q * a * Q * a * sinhVal * sinhVal) *
+              (kPi * Q * a * coshVal * sin(Q * R) - Q * R * cos(Q * R) * sinhVal);
+  ff += 8 * kPi * rho0 * a * a * a * exp(-R / a) / (1 + Q * Q * a * a) / (1 + Q * Q * a * a);
+  return ff;
+}
+
 __device__ __forceinline__ double bessel_k1_as(double x) {
   if (x <= 0) return 0;
   if (x <= 2) {

@@ -151,6 +151,115 @@ __device__ __forceinline__ void boost_by(float vx, float vy, float vz, float ev,
   out[3] = (E * ev + pv) / M;
 }
 
+// TVector3::RotateUz: v from the frame whose z axis is the direction of p
+__device__ __forceinline__ void rotate_uz_f(float& vx, float& vy, float& vz, float px, float py,
+                                            float pz) {
+  const float pm = sqrtf(px * px + py * py + pz * pz);
+  if (!(pm > 0.f)) return;
+  const float u1 = px / pm, u2 = py / pm, u3 = pz / pm;
+  float up = u1 * u1 + u2 * u2;
+  if (up > 0.f) {
+    up = sqrtf(up);
+    const float x = (u1 * u3 * vx - u2 * vy + u1 * up * vz) / up;
+    const float yy = (u2 * u3 * vx + u1 * vy + u2 * up * vz) / up;
+    const float z = (u3 * u3 * vx - vx + u3 * up * vz) / up;
+    vx = x;
+    vy = yy;
+    vz = z;
+  } else if (u3 < 0.f) {
+    vx = -vx;
+    vz = -vz;
+  }
+}
+
+// Vector meson (src/UpcGenerator.cpp:761-764, 425-472; getMomentumVM,
+// src/UpcCrossSection.cpp:1076-1104): the emitter picked with the reference's
+// test Uniform(0,1) < ratio[yBin] (a ratio of the two emitters' dsigma/dy, not
+// a fraction), the photon pT from its spectrum, the pomeron pT by inverting
+// the F^2 table between tmin and the end, cuts on the meson, then the decay
+// angle theta with density min(sin theta (1 + c cos^2 theta), 1) on [0, pi]
+// (the reference's rejection test against a unit envelope).  Philox blocks:
+// 1 (azimuths), 2 (photon pT), 3 (decay azimuth, charges), 4 (emitter,
+// pomeron), 5.. (decay-angle tries, two per block).
+__device__ bool gen_vm(const EventParams& e, const float* __restrict__ pttab, Cand& c,
+                       uint32_t clo, uint32_t chi, uint2 key, uint4 r1, uint4 r2) {
+  const double yedge_hi = e.ymin + e.dy * e.ny;
+  int yb = (int)((double)(int)(e.ny * (c.y - e.ymin)) / (yedge_hi - e.ymin));
+  yb = yb < 0 ? 0 : (yb > e.ny - 1 ? e.ny - 1 : yb);
+  const uint4 r4 = philox4x32_10(make_uint4(clo, chi, 4u, 0x55504347u), key);
+  const bool target = u53(r4.x, r4.y) < __ldg(e.vm_ratio + yb);
+  const double sgn = target ? 1. : -1.;
+  const float m = (float)c.m, y = (float)c.y;
+  const float ptPhot = photon_pt(e, pttab, logf(0.5f * m) + (float)sgn * y, u24(r2.x), u24(r2.y));
+  // pomeron: t = tmin + ptPom^2 with density F(t)^2 on [tmin, end of table]
+  const double ePom = c.m / 2. * exp(-sgn * c.y);
+  const double tmin = (ePom * ePom) / (e.vm_g1 * e.vm_g1);
+  const double dq = kPomQmax / kPomN;
+  const double* __restrict__ G = e.pom_cdf;
+  int jm = (int)(sqrt(tmin) / dq);
+  jm = jm > kPomN - 1 ? kPomN - 1 : jm;
+  double ta = (jm * dq) * (jm * dq), tb = ((jm + 1) * dq) * ((jm + 1) * dq);
+  const double g0 = __ldg(G + jm), g1 = __ldg(G + jm + 1);
+  double gmin = g0 + (g1 - g0) * (tmin - ta) / (tb - ta);
+  gmin = gmin < 0. ? 0. : (gmin > 1. ? 1. : gmin);
+  const double u = gmin + u53(r4.z, r4.w) * (1. - gmin);
+  int lo = jm, hi = kPomN;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (u >= __ldg(G + mid)) lo = mid; else hi = mid;
+  }
+  const double c0 = __ldg(G + lo), c1 = __ldg(G + lo + 1);
+  ta = (lo * dq) * (lo * dq);
+  tb = ((lo + 1) * dq) * ((lo + 1) * dq);
+  double t = c1 > c0 ? ta + (u - c0) / (c1 - c0) * (tb - ta) : ta;
+  t = t < tmin ? tmin : t;
+  const float ptPom = (float)sqrt(t - tmin);
+  float s1, c1f, s2, c2f;
+  sincosf(kTwoPiF * u24(r1.z), &s1, &c1f);
+  sincosf(kTwoPiF * u24(r1.w), &s2, &c2f);
+  const float ppx = ptPhot * c1f + ptPom * c2f;
+  const float ppy = ptPhot * s1 + ptPom * s2;
+  const float mt = sqrtf(m * m + ppx * ppx + ppy * ppy);
+  const float ppz = mt * sinhf(y), pE = mt * coshf(y);
+  // checkKinCuts on the meson (the decay follows the cuts)
+  if (e.doPtCut && sqrtf(ppx * ppx + ppy * ppy) < (float)e.minPt) return false;
+  if (e.doEtaCut) {
+    const float et = eta_f(ppx, ppy, ppz);
+    if (et < (float)e.minEta || et > (float)e.maxEta) return false;
+  }
+  // twoPartDecayVM's angle: at most 32 tries (acceptance above 0.8 per try)
+  const float cc = e.dght_law ? 0.605f : 1.f;
+  float theta = 0.25f * kTwoPiF;
+  bool ok = false;
+  for (int blk = 0; blk < 16 && !ok; ++blk) {
+    const uint4 rr = philox4x32_10(make_uint4(clo, chi, 5u + (uint32_t)blk, 0x55504347u), key);
+    for (int tr = 0; tr < 2 && !ok; ++tr) {
+      const float th = 0.5f * kTwoPiF * u24(tr ? rr.z : rr.x);
+      const float test = u24(tr ? rr.w : rr.y);
+      float sth, cth;
+      sincosf(th, &sth, &cth);
+      if (test < sth * (1.f + cc * cth * cth)) {
+        theta = th;
+        ok = true;
+      }
+    }
+  }
+  if (!ok) atomicAdd(e.vm_err, 1u);
+  const uint4 r3 = philox4x32_10(make_uint4(clo, chi, 3u, 0x55504347u), key);
+  c.sign = (r3.y & 1u) ? 1.f : -1.f;
+  const float md = e.mDght;
+  const float pmag = sqrtf(fmaxf(m * m * 0.25f - md * md, 0.f));
+  float sp, cp, sth, cth;
+  sincosf(kTwoPiF * u24(r3.x), &sp, &cp);
+  sincosf(theta, &sth, &cth);
+  float vx = pmag * sth * cp, vy = pmag * sth * sp, vz = pmag * cth;
+  rotate_uz_f(vx, vy, vz, ppx, ppy, ppz);
+  const float ev = sqrtf(pmag * pmag + md * md);
+  boost_by(-vx, -vy, -vz, ev, ppx, ppy, ppz, pE, m, c.p0);
+  boost_by(vx, vy, vz, ev, ppx, ppy, ppz, pE, m, c.p1);
+  return true;
+}
+
 __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ cdf2,
                               const double* __restrict__ cdfz, const float* __restrict__ pttab,
                               uint64_t idx, Cand& c) {
@@ -200,6 +309,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   } else {
     c.z = -1. + 2. * rz;
   }
+  if (e.vm) return gen_vm(e, pttab, c, clo, chi, key, r1, r2);
   // pair momentum (getPairMomentum)
   const float m = (float)c.m, y = (float)c.y;
   float ppx = 0.f, ppy = 0.f, mt = m;
@@ -253,20 +363,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   const float st = sqrtf(fmaxf(1.f - ct * ct, 0.f));
   float vx = eph * st * cp, vy = eph * st * sp, vz = eph * ct;
   // RotateUz onto the ALP direction (a rotation of an isotropic decay)
-  const float pm = sqrtf(ppx * ppx + ppy * ppy + ppz * ppz);
-  if (pm > 0.f) {
-    const float u1 = ppx / pm, u2 = ppy / pm, u3 = ppz / pm;
-    float up = u1 * u1 + u2 * u2;
-    if (up > 0.f) {
-      up = sqrtf(up);
-      const float x = (u1 * u3 * vx - u2 * vy + u1 * up * vz) / up;
-      const float yy = (u2 * u3 * vx + u1 * vy + u2 * up * vz) / up;
-      const float z = (u3 * u3 * vx - vx + u3 * up * vz) / up;
-      vx = x; vy = yy; vz = z;
-    } else if (u3 < 0.f) {
-      vx = -vx; vz = -vz;
-    }
-  }
+  rotate_uz_f(vx, vy, vz, ppx, ppy, ppz);
   boost_by(-vx, -vy, -vz, eph, ppx, ppy, ppz, pE, m, c.p0);
   boost_by(vx, vy, vz, eph, ppx, ppy, ppz, pE, m, c.p1);
   c.sign = 1.f;
@@ -513,7 +610,7 @@ cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const doub
     note_launch();
     k_guide_rows_d<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(d_cdfz, e.nm, e.nz, e.gz_n, d_gz);
   }
-  if (e.useNonzeroGamPt) {
+  if (e.useNonzeroGamPt || e.vm) {  // vector mesons always draw a photon pT
     const int64_t np = (int64_t)e.pt_ne * e.gpt_n;
     note_launch();
     k_guide_rows_f<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(d_ptcdf, e.pt_ne, e.pt_nbins,

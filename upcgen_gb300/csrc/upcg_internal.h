@@ -230,6 +230,18 @@ struct EventParams {
   int polarized;
   const double* ratio;
   const double* cdfz_ps;
+  // vector mesons (getMomentumVM, twoPartDecayVM): the emitter ratio per
+  // y-bin, the pomeron table (kPomN + 1 cumulative values over q in
+  // [0, kPomQmax]), the beam gamma, the daughters' mass and angular law
+  // (0: 1 + cos^2, 1: 1 + 0.605 cos^2), a device counter of candidates whose
+  // decay-angle draw ran out of tries
+  int vm;
+  const double* vm_ratio;
+  const double* pom_cdf;
+  double vm_g1;
+  float mDght;
+  int dght_law;
+  unsigned* vm_err;
 };
 // guide tables (EventParams) of the built CDFs; d_g2 / d_gz / d_gpt sized
 // g2_n, nm * gz_n, pt_ne * gpt_n
@@ -259,6 +271,25 @@ cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* 
                                cudaStream_t st);
 cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
                               cudaStream_t st);
+
+// photonuclear path (upcg_photonuc.cu)
+constexpr int kPomN = 65536;       // cells of the pomeron table
+constexpr double kPomQmax = 2.0;   // its q range [0, kPomQmax] GeV
+struct VmParams {
+  double mPart, sqrts, c0, pw, wmin, mNucl;  // dsdt constants, wmin = m_p + m_V
+  double rho0, R, a;
+  double glx[16], glw[16];                   // 16-point Gauss-Legendre on [-1, 1]
+};
+// calcPhotonFlux at npts (m, y) points; d_b / d_k / d_w / d_flux: npts * kNb scratch
+cudaError_t launch_photon_flux(const LumiParams& p, const double* d_m, const double* d_y, int npts,
+                               double* d_b, double* d_k, double* d_w, double* d_flux, double* d_out,
+                               QagsStats* d_stats, cudaStream_t st);
+cudaError_t launch_vm_cs_y(const VmParams& v, const double* d_y, int n, double* d_out,
+                           cudaStream_t st);
+cudaError_t launch_vm_fold(const double* d_flux, const double* d_s, int ny, double dy, double* d_cs,
+                           double* d_ratio, double* d_tot, cudaStream_t st);
+// d_vals: kPomN scratch, d_cdf: kPomN + 1
+cudaError_t launch_pom_table(const VmParams& v, double* d_vals, double* d_cdf, cudaStream_t st);
 
 // learned flux surrogate (upcg_mlp.cu).  Box of the training points: ln w in
 // [lw_lo, lw_hi], ln b from ln(bf_lo R) to lb_hi, R, a uniform, g uniform.

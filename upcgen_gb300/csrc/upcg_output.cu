@@ -14,7 +14,10 @@
 // Particles per event follow generateEvent (src/UpcGenerator.cpp:767-812):
 // a lepton pair is two leptons (pdg +-PDG by the event's charge sign, status
 // 23, mother 0); an ALP is the ALP (pdg 51, status 23, mother 0, momentum =
-// the photons' sum) and its two photons (pdg 22, status 33, mother 1).
+// the photons' sum) and its two photons (pdg 22, status 33, mother 1); a
+// vector meson is the meson (status 23, mother 0, momentum = the daughters'
+// sum) and its two daughters (pdg +-DECAY_PDG by the event's sign, status 33,
+// mother 1; twoPartDecayVM, :425-472).
 //
 // upcg_write_events generates batches on the device while host threads format
 // and write the previous batch: the device work of batch k+1 overlaps the file
@@ -39,15 +42,20 @@ namespace {
 
 struct ProcOut {
   int pdg, charged, ppe;  // particles per event
+  int dpdg, dsigned;      // decay products (3-particle events), signed by the event's sign
 };
 
 int proc_out(upcg_generator* g, ProcOut* p) {
-  int pdg = 0, ch = 0;
-  const int rc = upcg_particle_pdg(g, &pdg, &ch);
+  int pdg = 0, ch = 0, d = 0;
+  int rc = upcg_particle_pdg(g, &pdg, &ch);
+  if (rc) return rc;
+  rc = upcg_decay_pdg(g, &d);
   if (rc) return rc;
   p->pdg = pdg;
   p->charged = ch;
-  p->ppe = pdg == 51 ? 3 : 2;
+  p->ppe = d != 0 ? 3 : 2;
+  p->dpdg = d;
+  p->dsigned = d != 22;
   return UPCG_OK;
 }
 
@@ -59,11 +67,11 @@ __global__ void k_event_columns(const float4* __restrict__ ev, int64_t n, int64_
   const float4 h = __ldg(ev + 3 * i), a = __ldg(ev + 3 * i + 1), b = __ldg(ev + 3 * i + 2);
   const int evn = (int)(first + i);
   const int64_t r = i * po.ppe;
-  if (po.pdg == 51) {
+  if (po.ppe == 3) {
     const double q[4] = {(double)a.x + (double)b.x, (double)a.y + (double)b.y,
                          (double)a.z + (double)b.z, (double)a.w + (double)b.w};
     c.eventNumber[r] = evn;
-    c.pdgCode[r] = 51;
+    c.pdgCode[r] = po.pdg;
     c.particleID[r] = 1;
     c.statusID[r] = 23;
     c.motherID[r] = 0;
@@ -72,11 +80,12 @@ __global__ void k_event_columns(const float4* __restrict__ ev, int64_t n, int64_
     c.pz[r] = q[2];
     c.e[r] = q[3];
     const float4 ph[2] = {a, b};
+    const int s1 = po.dsigned ? (h.w > 0.f ? 1 : -1) : 1;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const int64_t rk = r + 1 + k;
       c.eventNumber[rk] = evn;
-      c.pdgCode[rk] = 22;
+      c.pdgCode[rk] = (k == 0 ? s1 : (po.dsigned ? -s1 : 1)) * po.dpdg;
       c.particleID[rk] = 2 + k;
       c.statusID[rk] = 33;
       c.motherID[rk] = 1;
@@ -124,15 +133,17 @@ void append_particle(std::string& s, int id, int mother, int pdg, double px, dou
 // count of writeEvent: mother-id changes along the list, starting from -1)
 void append_event(std::string& s, int64_t evt, const EventRecord& r, const ProcOut& po) {
   char buf[96];
-  const int nvert = po.pdg == 51 ? 1 : 0;
+  const int nvert = po.ppe == 3 ? 1 : 0;
   const int k = snprintf(buf, sizeof buf, "E %lld %d %d\nU GEV MM\n", (long long)evt, nvert, po.ppe);
   s.append(buf, (size_t)k);
   const double a[4] = {r.p0[0], r.p0[1], r.p0[2], r.p0[3]};
   const double b[4] = {r.p1[0], r.p1[1], r.p1[2], r.p1[3]};
-  if (po.pdg == 51) {
-    append_particle(s, 1, 0, 51, a[0] + b[0], a[1] + b[1], a[2] + b[2], a[3] + b[3], 23);
-    append_particle(s, 2, 1, 22, a[0], a[1], a[2], a[3], 33);
-    append_particle(s, 3, 1, 22, b[0], b[1], b[2], b[3], 33);
+  if (po.ppe == 3) {
+    const int s1 = po.dsigned ? (r.sign > 0.f ? 1 : -1) : 1;
+    const int s2 = po.dsigned ? -s1 : 1;
+    append_particle(s, 1, 0, po.pdg, a[0] + b[0], a[1] + b[1], a[2] + b[2], a[3] + b[3], 23);
+    append_particle(s, 2, 1, s1 * po.dpdg, a[0], a[1], a[2], a[3], 33);
+    append_particle(s, 3, 1, s2 * po.dpdg, b[0], b[1], b[2], b[3], 33);
     return;
   }
   const int s1 = po.charged ? (r.sign > 0.f ? 1 : -1) : 1;

@@ -87,14 +87,7 @@ __global__ void k_formfac_values(double* __restrict__ out, int n, double x0, dou
                                  double rho0, double R, double a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double Q2 = x0 + i * h;
-  const double Q = sqrt(Q2) / kHc;
-  const double coshVal = cosh(kPi * Q * a);
-  const double sinhVal = sinh(kPi * Q * a);
-  double ff = 4 * kPi * kPi * rho0 * a * a * a / (Q * a * Q * a * sinhVal * sinhVal) *
-              (kPi * Q * a * coshVal * sin(Q * R) - Q * R * cos(Q * R) * sinhVal);
-  ff += 8 * kPi * rho0 * a * a * a * exp(-R / a) / (1 + Q * Q * a * a) / (1 + Q * Q * a * a);
-  out[i] = ff;
+  out[i] = calc_form_fac(x0 + i * h, rho0, R, a);
 }
 
 __device__ __forceinline__ double eval_u(const double4* coef, int n, double h, double x) {
@@ -354,13 +347,7 @@ __global__ void k_formfac_pts(const double* __restrict__ q2, double* __restrict_
                               double rho0, double R, double a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double Q = sqrt(q2[i]) / kHc;
-  const double coshVal = cosh(kPi * Q * a);
-  const double sinhVal = sinh(kPi * Q * a);
-  double ff = 4 * kPi * kPi * rho0 * a * a * a / (Q * a * Q * a * sinhVal * sinhVal) *
-              (kPi * Q * a * coshVal * sin(Q * R) - Q * R * cos(Q * R) * sinhVal);
-  ff += 8 * kPi * rho0 * a * a * a * exp(-R / a) / (1 + Q * Q * a * a) / (1 + Q * Q * a * a);
-  out[i] = ff;
+  out[i] = calc_form_fac(q2[i], rho0, R, a);
 }
 
 }  // namespace
