@@ -217,3 +217,48 @@ def test_reference_flux_quadrature_noise(oracle_mod):
     scale = fconv / (v / A) ** 2 * k  # the flux's constant factor
     assert scale == pytest.approx(82 ** 2 / 137.035999074 / np.pi ** 2 / hc ** 2, rel=1e-9)
     assert fref / fconv - 1 == pytest.approx(0.0527, abs=2e-3)
+
+
+VM = {"NUCLEUS_Z": 82, "NUCLEUS_A": 208, "WS_R": 6.68, "WS_A": 0.447, "SQRTS": 5020,
+      "PROC_ID": 443, "DECAY_PDG": 13, "FLUX_POINT": 0, "BREAKUP_MODE": 2, "BINS_Y": 9}
+
+
+def test_vm_cross_section_restatement(oracle_mod):
+    """UpcPhotoNuclearVM::calcCrossSectionY (src/UpcPhotoNuclearVM.cpp:42-53,
+    340-381, impulse approximation) recomputed with scipy's quad: dsdt closed
+    form times the integral of calcFormFac^2 over [tmin, tmin + 1]."""
+    o = oracle_mod.Oracle(VM)
+    o.init_tables()
+    mV, mp, mn = 3.0969, 0.9382720813, 0.939565346
+    mnucl = (82 * mp + 126 * mn) / 208
+    for y in (-4.0, -1.5, 0.0, 2.0, 5.0):
+        w = mV / 2 * np.exp(y)
+        W2 = 4 * w * 2510.0
+        wmin = mp + mV
+        cs = 342.0 * (1 - wmin ** 2 / W2) ** 1.5 * (W2 * 1e-4) ** 0.4 if np.sqrt(W2) > wmin else 0.0
+        tmin = (mV ** 2 / W2) ** 2 * mnucl ** 2
+        edges = np.linspace(np.sqrt(tmin), np.sqrt(tmin + 1), 41)
+        phi = sum(integrate.quad(lambda q: o.form_factor(q * q) ** 2 * 2 * q, a, b,
+                                 epsabs=0, epsrel=1e-13, limit=200)[0]
+                  for a, b in zip(edges[:-1], edges[1:]))
+        assert o.vm_cs_y(y) == pytest.approx(cs * phi * 1e-6, rel=1e-11)
+
+
+def test_photon_flux_restatement(oracle_mod):
+    """calcPhotonFlux (src/UpcCrossSection.cpp:700-722) as a Python loop over
+    the oracle's fluxForm, G_AA and breakup splines."""
+    o = oracle_mod.Oracle(VM)
+    o.init_tables()
+    R, g1, hc = 6.68, 5020 / (2 * 0.9382720813), 0.1973269718
+    for m, y in ((3.0969, -3.0), (3.0969, 0.5), (9.3987, 2.5)):
+        k = m / 2 * np.exp(y)
+        bmin, bmax = 0.05 * R, max(5 * g1 * hc / k, 5 * R)
+        ldb = (np.log(bmax) - np.log(bmin)) / 120
+        s = 0.0
+        for i in range(120):
+            bl, bh = bmin * np.exp(i * ldb), bmin * np.exp((i + 1) * ldb)
+            b = (bh + bl) / 2
+            bu = o.breakup_spline(min(b, 20.0))
+            ga = o.gaa(b) if b < 20 else 1.0
+            s += bu * ga * o.flux_form(b, k) * b * (bh - bl)
+        assert o.photon_flux(m, y) == pytest.approx(2 * np.pi * k * s, rel=1e-13)
