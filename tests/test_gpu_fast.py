@@ -94,6 +94,24 @@ def test_fast_light_nucleus(ug, oracle_mod):
     assert rel.max() < FAST_TOL and rtot < FAST_TOL
 
 
+@pytest.mark.parametrize("mode", [2, 3, 4])
+def test_fast_breakup_table_fp32(ug, mode):
+    """The fast form's breakup table comes from FP32 trapezoid sums: within
+    1e-5 of the FP64 table (the plain path's), absolutely and relative to
+    values above 1e-3."""
+    b = np.linspace(1e-6, 20.0, 4001)
+    vals = {}
+    for meth in ("plain", "fast"):
+        g = ug.UpcGenerator(dict(C1, BREAKUP_MODE=mode, BINS_M=3, BINS_Y=3))
+        g.setLumiMethod(meth)
+        g.init()
+        vals[meth] = g.nucProcessCS.spline("breakup", b)
+    d = np.abs(vals["fast"] - vals["plain"])
+    assert d.max() < 1e-5
+    big = np.abs(vals["plain"]) > 1e-3
+    assert (d[big] / np.abs(vals["plain"][big])).max() < 1e-5
+
+
 def test_fast_contraction_on_reference_fluxes(ug):
     """Method 2: the plain path's node fluxes (the reference's QAGS) through
     the projection and the tensor-core contraction -- isolates the

@@ -94,6 +94,10 @@ const double kX10pos[5] = {0.1488743389816312, 0.4333953941292472, 0.67940956829
                            0.8650633666889845, 0.9739065285171717};
 const double kQ2min = 1e-9, kQ2max = 2.;
 const int kNQ2 = 1000000;
+// the fast form's form-factor spline: 65,536 knots on the same range (a
+// cubic spline error below 1e-9 of F; the Q(w, b) table and the photon-pT
+// spectra are its only users there)
+const int kNQ2Fast = 65536;
 
 template <class T>
 struct DBuf {
@@ -269,6 +273,7 @@ struct upcg_generator {
   // scan: earlier configurations whose form factor / G_AA / breakup tables
   // have the same inputs (their tables are copied, not rebuilt)
   upcg_generator* ff_donor = nullptr;
+  int ff_n = kNQ2;  // knots of the form-factor spline (kNQ2Fast for methods 1 and 4)
   upcg_generator* gaa_donor = nullptr;
   upcg_generator* brk_donor = nullptr;
   FastFluxTables ftab_last{};     // the fast form's flux tables of the last build
@@ -319,7 +324,7 @@ struct upcg_generator {
   DBuf<EventRecord> evbuf;
   DBuf<uint16_t> fgh, fgl, fah, fal;  // fast form: bf16 hi/lo of G and of the projections
   DBuf<float> fa2, fpart;
-  DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq, fsides;
+  DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq, fsides, ffc;
   DBuf<float> fs32, fq32;
   DBuf<float4> fgaa32, fbrk32, ff32;
   // grid form: G, flux matrix, T = N G (bf16 hi/lo), Lg, row sums and tails
@@ -353,6 +358,7 @@ struct upcg_generator {
       if (ev_join[i]) cudaEventDestroy(ev_join[i]);
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_static) cudaEventDestroy(ev_static);
     if (own) cudaStreamDestroy(own);
   }
   void set_collision(float s, int z, int aa) {
@@ -384,6 +390,10 @@ struct upcg_generator {
   int build_tables();
   int build_lumi();
   int build_vm();
+  int enqueue_static_samplers(cudaStream_t ss);
+  int fork_static_samplers();
+  bool static_pending = false;   // static samplers enqueued on side[0], not yet joined
+  cudaEvent_t ev_static = nullptr;
   VmParams vm_params() const;
   int build_lumi_cached();
   std::string lumi_cache_key() const;
@@ -514,10 +524,10 @@ LumiParams upcg_generator::lumi_params() const {
   p.gaa = SplineU{gaa_coef.p, 0.0, dbg, 1.0 / dbg, 200};
   const double dbb = (1000. - 1e-6) / 1000000;
   p.brk = SplineU{brk_coef.p, 1e-6, dbb, 1.0 / dbb, brk_n};
-  const double dq = (kQ2max - kQ2min) / kNQ2;
-  p.ff = SplineU{ff_coef.p, kQ2min, dq, 1.0 / dq, kNQ2};
+  const double dq = (kQ2max - kQ2min) / ff_n;
+  p.ff = SplineU{ff_coef.p, kQ2min, dq, 1.0 / dq, ff_n};
   p.q2max = kQ2max;
-  p.q2clamp = kQ2max - dq;
+  p.q2clamp = kQ2max - (kQ2max - kQ2min) / kNQ2;  // the reference's clamp, Q2max - dQ2
   p.mirror = nullptr;
   return p;
 }
@@ -666,17 +676,18 @@ int upcg_generator::build_tables() {
                        cudaMemcpyDeviceToDevice, s));
   else
     CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s));
-  // form factor on 1e6 knots
-  const double dq = (kQ2max - kQ2min) / kNQ2;
-  CK(ff_y.ensure(kNQ2));
-  CK(ff_c.ensure(kNQ2));
-  CK(ff_coef.ensure(kNQ2 - 1));
-  if (cap && ff_donor) {
-    CK(cudaMemcpyAsync(ff_coef.p, ff_donor->ff_coef.p, (size_t)(kNQ2 - 1) * sizeof(double4),
+  // form factor on 1e6 knots (the reference's), 65,536 for the fast form
+  ff_n = (lumiMethod == 1 || lumiMethod == 4) ? kNQ2Fast : kNQ2;
+  const double dq = (kQ2max - kQ2min) / ff_n;
+  CK(ff_y.ensure(ff_n));
+  CK(ff_c.ensure(ff_n));
+  CK(ff_coef.ensure(ff_n - 1));
+  if (cap && ff_donor && ff_donor->ff_n == ff_n) {
+    CK(cudaMemcpyAsync(ff_coef.p, ff_donor->ff_coef.p, (size_t)(ff_n - 1) * sizeof(double4),
                        cudaMemcpyDeviceToDevice, side[0]));
   } else {
-    CK(launch_formfac_values(ff_y.p, kNQ2, kQ2min, dq, rho0, R, a, side[0]));
-    CK(build_spline_uniform(ff_y.p, kNQ2, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
+    CK(launch_formfac_values(ff_y.p, ff_n, kQ2min, dq, rho0, R, a, side[0]));
+    CK(build_spline_uniform(ff_y.p, ff_n, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
   }
   CK(cudaEventRecord(ev_join[0], side[0]));
   // breakup probability: knots up to 20 fm + margin (the path evaluates the
@@ -697,8 +708,10 @@ int upcg_generator::build_tables() {
     CK(cudaMemcpyAsync(brk_coef.p, brk_donor->brk_coef.p, (size_t)(brk_n - 1) * sizeof(double4),
                        cudaMemcpyDeviceToDevice, side[1]));
   } else if (breakupMode > 1) {
+    // the fast form (methods 1, 4; budget 1e-4) takes the FP32 sums (~1e-6)
+    const int brk_fp32 = (lumiMethod == 1 || lumiMethod == 4) ? 1 : 0;
     CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
-                             1e-6, dbb, brk_y.p, side[1]));
+                             1e-6, dbb, brk_y.p, side[1], brk_fp32));
     CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1]));
   }
   CK(cudaEventRecord(ev_join[1], side[1]));
@@ -960,22 +973,17 @@ int upcg_generator::build_lumi() {
   double c_far = 0.;
   if (fast) {
     const int b = mark();
-    // the breakup probability at 20 fm: the survival kernel beyond b = 20 fm
-    double P20 = 1.;
-    if (breakupMode != 1) {
-      const double x20 = 20.;
-      CK(pts_a.ensure(1));
-      CK(pts_c.ensure(1));
-      CK(mcpy(pts_a.p, &x20, sizeof x20, cudaMemcpyHostToDevice, s));
-      CK(launch_spline_eval(p.brk, pts_a.p, pts_c.p, 1, s));
-      CK(mcpy(&P20, pts_c.p, sizeof P20, cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-    }
+    // the breakup probability at 20 fm (the survival kernel beyond b = 20 fm)
+    // and c_far, on the device: no host round trip between the phases
+    CK(ffc.ensure(2));
+    CK(launch_far_consts(p, breakupMode != 1, ffc.p, s));
     CK(fgaa32.ensure(p.gaa.n));
     CK(fbrk32.ensure(breakupMode != 1 ? p.brk.n : 1));
-    CK(launch_fast_G(p, fu0, fh, P, P20, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s));
+    CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p));
     // flux tables: K0/K1 on ln x; Q(w, b) on 512 x 256 (ln w, ln b) points by
-    // 160 Gauss-Legendre panels of 16 points on q in [0, 10]
+    // 24 Gauss-Legendre panels of 16 points on q in [0, kQNodeMax] (panels of
+    // 1/16 GeV, two thirds of J1's shortest period, at b = 2R) and the
+    // closed-form rest to q = 10
     const int nk = flux_table_ktab_n();
     CK(fk1.ensure(nk));
     CK(fs32.ensure(nk));
@@ -989,12 +997,12 @@ int upcg_generator::build_lumi() {
     ftab.hw = (std::log(kmax) - ftab.lw0) / (ftab.nw - 1);
     ftab.lb0 = std::log(0.05 * R * 0.999);
     ftab.hb = (std::log(2. * R * 1.001) - ftab.lb0) / (ftab.nb - 1);
-    const int npan = 160, ngl = 16, nqn = npan * ngl;
+    const int npan = 24, ngl = 16, nqn = npan * ngl;
     if (!isPoint) {
       std::vector<double> gx, gw, qn(nqn), wn(nqn);
       gauss_legendre(ngl, gx, gw);
       for (int pa = 0; pa < npan; ++pa) {
-        const double lo = 10.0 * pa / npan, hi = 10.0 * (pa + 1) / npan;
+        const double lo = kQNodeMax * pa / npan, hi = kQNodeMax * (pa + 1) / npan;
         for (int j = 0; j < ngl; ++j) {
           qn[pa * ngl + j] = 0.5 * (hi - lo) * gx[j] + 0.5 * (hi + lo);
           wn[pa * ngl + j] = 0.5 * (hi - lo) * gw[j];
@@ -1045,8 +1053,6 @@ int upcg_generator::build_lumi() {
     for (int im = 0; im < nm; ++im) lnm2[im] = std::log((p.mmin + p.dm * im) / 2.);
     CK(flnm2.ensure(nm));
     CK(mcpy(flnm2.p, lnm2.data(), nm * sizeof(double), cudaMemcpyHostToDevice, s));
-    c_far = 0.;
-    for (int q = 0; q < 5; ++q) c_far += P20 * 1. * p.wk[q];
     spans.push_back({4, {b, mark()}});
     ftab_last = ftab;
     nqn_last = nqn;
@@ -1103,7 +1109,7 @@ int upcg_generator::build_lumi() {
       CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(),
                               fa2.p, fpart.p, ferr.p, shape, grid, s));
       spans.push_back({3, {b, mark()}});
-      CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s));
+      CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s, ffc.p));
     }
   }
   const int w1 = mark();
@@ -1204,6 +1210,53 @@ int upcg_generator::build_vm() {
   return UPCG_OK;
 }
 
+// The samplers that do not depend on the luminosity: the dsigma/dz tables
+// and their CDFs, the photon-pT spectra, their guide tables.  upcg_init
+// enqueues them on a side stream as soon as the nuclear tables exist, so that
+// they run beside the luminosity; build_xsec joins them.
+int upcg_generator::enqueue_static_samplers(cudaStream_t ss) {
+  const FoldParams f = fold_params();
+  if (isVM) {
+    CK(cdfz.ensure(1));  // no z distribution (ignoreCSZ)
+  } else if (!usePolarizedCS) {
+    CK(cszm.ensure((size_t)nm * nz));
+    CK(launch_cs_zm(f, 0, cszm.p, ss));
+    CK(cdfz.ensure((size_t)nm * (nz + 1)));
+    if (!ignoreCSZ) CK(launch_cdf_rows(cszm.p, nm, nz, cdfz.p, ss));
+  } else {
+    CK(cszm2.ensure((size_t)nm * nz));
+    CK(cszm3.ensure((size_t)nm * nz));
+    CK(launch_cs_zm(f, 1, cszm2.p, ss));
+    CK(launch_cs_zm(f, 2, cszm3.p, ss));
+    CK(cdfz2.ensure((size_t)nm * (nz + 1)));
+    CK(cdfz3.ensure((size_t)nm * (nz + 1)));
+    CK(launch_cdf_rows(cszm2.p, nm, nz, cdfz2.p, ss));
+    CK(launch_cdf_rows(cszm3.p, nm, nz, cdfz3.p, ss));
+  }
+  const EventParams e = event_params();
+  CK(ptcdf.ensure((size_t)e.pt_ne * (e.pt_nbins + 1)));
+  CK(ff32.ensure(ff_n));
+  CK(launch_photon_pt_tables(e, lumi_params().ff, ff32.p, ptcdf.p, ss));
+  CK(guidez.ensure((size_t)nm * e.gz_n));
+  CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
+  const EventParams eg = event_params();  // with the guide buffers allocated
+  CK(launch_guides(eg, nullptr, cdfz.p, ptcdf.p, nullptr, guidez.p, guidept.p, ss));
+  return UPCG_OK;
+}
+
+int upcg_generator::fork_static_samplers() {
+  cudaStream_t s = st();
+  CK(side_streams());
+  if (!ev_static) CK(cudaEventCreateWithFlags(&ev_static, cudaEventDisableTiming));
+  CK(cudaEventRecord(ev_fork, s));
+  CK(cudaStreamWaitEvent(side[0], ev_fork, 0));
+  const int rc = enqueue_static_samplers(side[0]);
+  if (rc) return rc;
+  CK(cudaEventRecord(ev_static, side[0]));
+  static_pending = true;
+  return UPCG_OK;
+}
+
 int upcg_generator::build_xsec() {
   cudaStream_t s = st();
   const FoldParams f = fold_params();
@@ -1224,33 +1277,18 @@ int upcg_generator::build_xsec() {
   CK(cdf2.ensure((size_t)ncell + 1));
   CK(cdf_scratch.ensure(cdf_2d_scratch_doubles(ncell)));
   CK(launch_cdf_2d(cs.p, ncell, cdf2.p, cdf_scratch.p, s));
-  if (isVM) {
-    CK(cdfz.ensure(1));  // no z distribution (ignoreCSZ)
-  } else if (!usePolarizedCS) {
-    CK(cszm.ensure((size_t)nm * nz));
-    CK(launch_cs_zm(f, 0, cszm.p, s));
-    CK(cdfz.ensure((size_t)nm * (nz + 1)));
-    if (!ignoreCSZ) CK(launch_cdf_rows(cszm.p, nm, nz, cdfz.p, s));
+  if (static_pending) {  // enqueued on a side stream before the luminosity
+    CK(cudaStreamWaitEvent(s, ev_static, 0));
+    static_pending = false;
   } else {
-    CK(cszm2.ensure((size_t)nm * nz));
-    CK(cszm3.ensure((size_t)nm * nz));
-    CK(launch_cs_zm(f, 1, cszm2.p, s));
-    CK(launch_cs_zm(f, 2, cszm3.p, s));
-    CK(cdfz2.ensure((size_t)nm * (nz + 1)));
-    CK(cdfz3.ensure((size_t)nm * (nz + 1)));
-    CK(launch_cdf_rows(cszm2.p, nm, nz, cdfz2.p, s));
-    CK(launch_cdf_rows(cszm3.p, nm, nz, cdfz3.p, s));
+    const int rc = enqueue_static_samplers(s);
+    if (rc) return rc;
   }
-  const EventParams e = event_params();
-  CK(ptcdf.ensure((size_t)e.pt_ne * (e.pt_nbins + 1)));
-  CK(ff32.ensure(kNQ2));
-  CK(launch_photon_pt_tables(e, lumi_params().ff, ff32.p, ptcdf.p, s));
   {
+    const EventParams e = event_params();
     CK(guide2.ensure(e.g2_n));
-    CK(guidez.ensure((size_t)nm * e.gz_n));
-    CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
-    const EventParams eg = event_params();  // with the guide buffers allocated
-    CK(launch_guides(eg, cdf2.p, cdfz.p, ptcdf.p, guide2.p, guidez.p, guidept.p, s));
+    const EventParams eg = event_params();  // with the guide buffer allocated
+    CK(launch_guides(eg, cdf2.p, nullptr, nullptr, guide2.p, nullptr, nullptr, s));
   }
   if (cap) {  // a captured replay leaves sigma_tot on the device (read after the replay)
     xsec_ready = true;
@@ -1540,8 +1578,16 @@ int upcg_init(upcg_generator* g) {
     if (rc) return rc;
     return g->build_xsec();
   }
-  rc = g->lumi_cache_usable() ? g->build_lumi_cached() : g->build_lumi();
+  rc = g->fork_static_samplers();  // beside the luminosity
   if (rc) return rc;
+  rc = g->lumi_cache_usable() ? g->build_lumi_cached() : g->build_lumi();
+  if (rc) {
+    if (g->static_pending) {  // leave no side-stream work behind a failed init
+      cudaStreamWaitEvent(g->st(), g->ev_static, 0);
+      g->static_pending = false;
+    }
+    return rc;
+  }
   return g->build_xsec();
 }
 

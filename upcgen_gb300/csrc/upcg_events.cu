@@ -602,15 +602,18 @@ cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const doub
                           const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
                           cudaStream_t st) {
   if (e.pt_nbins > 65535) return cudaErrorInvalidValue;
+  // each guide set is built when its buffer is given (null: skipped)
   const int n2 = e.nm * e.ny;
-  note_launch();
-  k_guide_rows_d<<<(e.g2_n + 255) / 256, 256, 0, st>>>(d_cdf2, 1, n2, e.g2_n, d_g2);
-  if (!e.ignoreCSZ && !e.polarized) {  // polarized z: plain searches on two CDF sets
+  if (d_g2) {
+    note_launch();
+    k_guide_rows_d<<<(e.g2_n + 255) / 256, 256, 0, st>>>(d_cdf2, 1, n2, e.g2_n, d_g2);
+  }
+  if (d_gz && !e.ignoreCSZ && !e.polarized) {  // polarized z: plain searches on two CDF sets
     const int64_t nz = (int64_t)e.nm * e.gz_n;
     note_launch();
     k_guide_rows_d<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(d_cdfz, e.nm, e.nz, e.gz_n, d_gz);
   }
-  if (e.useNonzeroGamPt || e.vm) {  // vector mesons always draw a photon pT
+  if (d_gpt && (e.useNonzeroGamPt || e.vm)) {  // vector mesons always draw a photon pT
     const int64_t np = (int64_t)e.pt_ne * e.gpt_n;
     note_launch();
     k_guide_rows_f<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(d_ptcdf, e.pt_ne, e.pt_nbins,

@@ -378,9 +378,9 @@ __global__ void k_ktab(double g, double* __restrict__ t1, float* __restrict__ t3
 }
 
 // Form-factor flux amplitude Q(w, b) = int_0^10 q^2 F(q^2 + w^2/g^2)/(q^2 + w^2/g^2)
-// J1(b q / hc) dq by composite Gauss-Legendre (the integrand of
-// src/UpcCrossSection.cpp:181-191, clamp at Q2max - dQ2 included), as the
-// FP64 product H[w][n] J[n][b].
+// J1(b q / hc) dq (the integrand of src/UpcCrossSection.cpp:181-191, clamp at
+// Q2max - dQ2 included): composite Gauss-Legendre on q in [0, kQNodeMax] as
+// the FP64 product H[w][n] J[n][b], the rest in closed form (k_dgemm_reduce).
 __global__ void k_qtab_H(LumiParams p, const double* __restrict__ qn, const double* __restrict__ wn,
                          int nq, double lw0, double hw, double* __restrict__ H) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -394,12 +394,21 @@ __global__ void k_qtab_H(LumiParams p, const double* __restrict__ qn, const doub
 }
 
 __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, double hb, int nb,
-                         double* __restrict__ J) {
+                         SplineU ff, double q2clamp, double* __restrict__ J,
+                         double* __restrict__ tail) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = blockIdx.y;
   if (j >= nb) return;
   const double b = exp(lb0 + j * hb);
   J[(size_t)n * nb + j] = j1(b * qn[n] / kHc);
+  // q in [kQNodeMax, 10]: q^2 + w^2/g^2 > Q2max, so the reference's integrand
+  // is F(Q2max - dQ2) q^2 / (q^2 + w^2/g^2) J1(b q / hc); with the
+  // q^2 / (q^2 + w^2/g^2) factor taken as 1 its integral is
+  // F_c hc / b (J0(b qc / hc) - J0(10 b / hc)).  The factor's departure,
+  // (w/g)^2 / qc^2 at most, is below 1e-2 for w < 0.2 g, where this part is
+  // itself ~1e-6 of Q; at larger w the flux is below 1e-10 of its peak.
+  if (n == 0)
+    tail[j] = spline_eval(ff, q2clamp) * kHc / b * (j0(b * kQNodeMax / kHc) - j0(b * 10. / kHc));
 }
 
 // Split-K FP64 product: Cp[s][M][N] = A[M][Ks] B[Ks][N] over the s-th slice
@@ -445,12 +454,15 @@ __global__ void __launch_bounds__(256) k_dgemm(const double* __restrict__ A,
 }
 
 // C = sum over the slices in order (FP64), and its FP32 copy
-__global__ void k_dgemm_reduce(const double* __restrict__ Cp, int nslice, size_t mn,
-                               double* __restrict__ C, float* __restrict__ C32) {
+// Sums the K slices and adds the closed-form part beyond kQNodeMax (k_qtab_J).
+__global__ void k_dgemm_reduce(const double* __restrict__ Cp, int nslice, size_t mn, int nb,
+                               const double* __restrict__ tail, double* __restrict__ C,
+                               float* __restrict__ C32) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= mn) return;
   double v = 0.;
   for (int z = 0; z < nslice; ++z) v += Cp[(size_t)z * mn + i];
+  v += __ldg(tail + (int)(i % (size_t)nb));
   C[i] = v;
   C32[i] = (float)v;
 }
@@ -1219,7 +1231,7 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
 
 size_t fast_side_bytes() { return sizeof(SideC); }
 
-int flux_table_part_doubles(int nw, int nb) { return 8 * nw * nb; }
+int flux_table_part_doubles(int nw, int nb) { return 8 * nw * nb + nb; }  // slices + tail
 
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
                               int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st,
@@ -1236,8 +1248,9 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
     note_launch();
     k_qtab_H<<<gh, 256, 0, st>>>(p, d_qn, d_wn, nq, lw, t->hw, d_H);
     dim3 gj((t->nb + 255) / 256, nq);
+    double* d_tail = d_part + (size_t)8 * t->nw * t->nb;
     note_launch();
-    k_qtab_J<<<gj, 256, 0, st>>>(d_qn, nq, t->lb0, t->hb, t->nb, d_J);
+    k_qtab_J<<<gj, 256, 0, st>>>(d_qn, nq, t->lb0, t->hb, t->nb, p.ff, p.q2clamp, d_J, d_tail);
     // K = nq split into nq / kslice slices; d_part holds them
     const int nslice = nq % (8 * 16) == 0 ? 8 : 1;
     const int kslice = nq / nslice;
@@ -1247,8 +1260,8 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
     const size_t mn = (size_t)rows * t->nb;
     const size_t off = (size_t)w_lo * t->nb;
     note_launch();
-    k_dgemm_reduce<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(d_part, nslice, mn, t->qt + off,
-                                                                 t->qt32 + off);
+    k_dgemm_reduce<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(d_part, nslice, mn, t->nb, d_tail,
+                                                                 t->qt + off, t->qt32 + off);
   }
   return cudaGetLastError();
 }

@@ -89,7 +89,8 @@ int breakup_energy_table(double gammatarg, double* ee, double* se);
 // d_tab = [ee | se | ln ee | 1/ee], each kBreakupTabMax long, nt entries used
 cudaError_t launch_breakup_values(const double* d_tab, int nt, double gammatarg, double omaxx,
                                   double zcon, int mode, int n, double x0, double h,
-                                  double* d_out, cudaStream_t st);
+                                  double* d_out, cudaStream_t st,
+                                  int fp32 = 0);
 cudaError_t launch_spline_eval(const SplineU& s, const double* d_x, double* d_y, int n,
                                cudaStream_t st);
 
@@ -271,6 +272,11 @@ cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* 
                                cudaStream_t st);
 cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
                               cudaStream_t st);
+
+// fast form's Q(w, b) table: Gauss-Legendre nodes cover q in [0, kQNodeMax]
+// GeV (beyond it q^2 > Q2max, where the reference's integrand holds the form
+// factor at its clamp value and the integral has a closed form)
+constexpr double kQNodeMax = 1.5;
 
 // photonuclear path (upcg_photonuc.cu)
 constexpr int kPomN = 65536;       // cells of the pomeron table

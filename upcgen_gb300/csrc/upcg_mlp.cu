@@ -403,9 +403,13 @@ __global__ void __launch_bounds__(kStepThreads) k_mlp_infer(const __nv_bfloat16*
   MlpSmemI& S = *reinterpret_cast<MlpSmemI*>(smem);
   __shared__ float u[NS][kIn], y[NS];
   for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) S.w1[i / kIn][i % kIn] = pb[oW1 + i];
+  // hidden weights: 16-byte loads (the offsets are multiples of 8 bf16)
+  static_assert(oW2 % 8 == 0 && oW3 % 8 == 0 && oW4 % 8 == 0 && (kAs * 2) % 16 == 0, "alignment");
   for (int l = 0; l < 3; ++l) {
     const int off = l == 0 ? oW2 : (l == 1 ? oW3 : oW4);
-    for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) S.w[l][i / kH][i % kH] = pb[off + i];
+    const uint4* src = reinterpret_cast<const uint4*>(pb + off);
+    for (int i = threadIdx.x; i < kH * (kH / 8); i += blockDim.x)
+      *reinterpret_cast<uint4*>(&S.w[l][i / (kH / 8)][(i % (kH / 8)) * 8]) = __ldg(src + i);
   }
   for (int i = threadIdx.x; i < kH; i += blockDim.x) {
     S.w5[i] = __bfloat162float(pb[oW5 + i]);
