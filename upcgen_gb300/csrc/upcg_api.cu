@@ -293,7 +293,9 @@ struct upcg_generator {
   DBuf<double4> ff_coef, gaa_coef, ta_coef, brk_coef;
   DBuf<double> gaa_work, bu_tab, cdf_scratch;
   DBuf<double> vm_m, vm_y, vm_b, vm_k, vm_w, vm_f, vm_flux, vm_s, pom_vals, pom_cdf;
-  DBuf<unsigned> vm_err;  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
+  DBuf<unsigned> vm_err;
+  DBuf<int> mbinlut;  // getBinY of int(nm (m - mmin)), see EventParams
+  int mbinlut_n = 0;  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
   std::vector<double> bu_host;
   int bu_nt = 0;
   // side streams of the table set-up and their fork / join events
@@ -359,6 +361,8 @@ struct upcg_generator {
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_static) cudaEventDestroy(ev_static);
+    for (auto e : ev_ft)
+      if (e) cudaEventDestroy(e);
     if (own) cudaStreamDestroy(own);
   }
   void set_collision(float s, int z, int aa) {
@@ -390,6 +394,9 @@ struct upcg_generator {
   int build_tables();
   int build_lumi();
   int build_vm();
+  int setup_flux_tables(cudaStream_t ss);
+  bool ftab_early = false;  // build_tables enqueued the flux tables
+  cudaEvent_t ev_ft[2] = {nullptr, nullptr};
   int enqueue_static_samplers(cudaStream_t ss);
   int fork_static_samplers();
   bool static_pending = false;   // static samplers enqueued on side[0], not yet joined
@@ -575,6 +582,9 @@ EventParams upcg_generator::event_params() const {
   e.polarized = usePolarizedCS ? 1 : 0;
   e.ratio = usePolarizedCS ? ratio.p : nullptr;
   e.cdfz_ps = usePolarizedCS ? cdfz3.p : nullptr;
+  e.medge_hi = mmin + (mmax - mmin) / nm * nm;  // binEdgesM.back() (src/UpcGenerator.cpp:677-678)
+  e.mbin_lut = mbinlut.p;
+  e.mbin_lut_n = mbinlut.p && mbinlut.n >= (size_t)mbinlut_n ? mbinlut_n : 0;
   e.vm = isVM ? 1 : 0;
   e.vm_ratio = isVM ? ratio.p : nullptr;
   e.pom_cdf = isVM ? pom_cdf.p : nullptr;
@@ -688,6 +698,18 @@ int upcg_generator::build_tables() {
   } else {
     CK(launch_formfac_values(ff_y.p, ff_n, kQ2min, dq, rho0, R, a, side[0]));
     CK(build_spline_uniform(ff_y.p, ff_n, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
+  }
+  ftab_early = false;
+  if (!cap && !isVM && (lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4)) {
+    // the fast form's flux tables need only the form factor: they run here,
+    // beside the breakup and G_AA chains
+    for (auto& e : ev_ft)
+      if (!e) CK(cudaEventCreate(&e));
+    CK(cudaEventRecord(ev_ft[0], side[0]));
+    const int frc = setup_flux_tables(side[0]);
+    if (frc) return frc;
+    CK(cudaEventRecord(ev_ft[1], side[0]));
+    ftab_early = true;
   }
   CK(cudaEventRecord(ev_join[0], side[0]));
   // breakup probability: knots up to 20 fm + margin (the path evaluates the
@@ -899,6 +921,82 @@ int upcg_generator::build_lumi_cached() {
   return UPCG_OK;
 }
 
+// The fast form's flux tables: K0/K1 on ln x and the Q(w, b) table (or its
+// surrogate rows), on stream ss; the result is in ftab_last.
+int upcg_generator::setup_flux_tables(cudaStream_t ss) {
+  const LumiParams p = lumi_params();
+  FastFluxTables ftab{};
+  // flux tables: K0/K1 on ln x; Q(w, b) on 512 x 256 (ln w, ln b) points by
+  // 24 Gauss-Legendre panels of 16 points on q in [0, kQNodeMax] (panels of
+  // 1/16 GeV, two thirds of J1's shortest period, at b = 2R) and the
+  // closed-form rest to q = 10
+  const int nk = flux_table_ktab_n();
+  CK(fk1.ensure(nk));
+  CK(fs32.ensure(nk));
+  ftab.st = fk1.p;
+  ftab.st32 = fs32.p;
+  ftab.nw = 512;
+  ftab.nb = 256;
+  const double ymx = std::max(std::fabs(ymin), std::fabs(ymax));
+  const double kmin = mmin / 2. * std::exp(-ymx) * 0.9, kmax = mmax / 2. * std::exp(ymx) * 1.1;
+  ftab.lw0 = std::log(kmin);
+  ftab.hw = (std::log(kmax) - ftab.lw0) / (ftab.nw - 1);
+  ftab.lb0 = std::log(0.05 * R * 0.999);
+  ftab.hb = (std::log(2. * R * 1.001) - ftab.lb0) / (ftab.nb - 1);
+  const int npan = 24, ngl = 16, nqn = npan * ngl;
+  if (!isPoint) {
+    std::vector<double> gx, gw, qn(nqn), wn(nqn);
+    gauss_legendre(ngl, gx, gw);
+    for (int pa = 0; pa < npan; ++pa) {
+      const double lo = kQNodeMax * pa / npan, hi = kQNodeMax * (pa + 1) / npan;
+      for (int j = 0; j < ngl; ++j) {
+        qn[pa * ngl + j] = 0.5 * (hi - lo) * gx[j] + 0.5 * (hi + lo);
+        wn[pa * ngl + j] = 0.5 * (hi - lo) * gw[j];
+      }
+    }
+    CK(fqn.ensure(nqn));
+    CK(fwn.ensure(nqn));
+    CK(fq.ensure((size_t)ftab.nw * ftab.nb));
+    CK(fq32.ensure((size_t)ftab.nw * ftab.nb));
+    CK(fH.ensure((size_t)ftab.nw * nqn));
+    CK(fJ.ensure((size_t)nqn * ftab.nb));
+    CK(mcpy(fqn.p, qn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, ss));
+    CK(mcpy(fwn.p, wn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, ss));
+    ftab.qt = fq.p;
+    ftab.qt32 = fq32.p;
+  }
+  // method 4: the rows inside the surrogate's box from the MLP (rows in
+  // blocks of 64), the others from the quadrature
+  int w_sur = 0;
+  const double gam = g1;
+  if (lumiMethod == 4 && !isPoint) {
+    const MlpBox& bx = surrogate->box;
+    const bool inside = R >= bx.R_lo && R <= bx.R_hi && a >= bx.a_lo && a <= bx.a_hi &&
+                        gam >= bx.g_lo && gam <= bx.g_hi && ftab.lw0 >= bx.lw_lo &&
+                        ftab.lb0 >= std::log(bx.bf_lo * R) &&
+                        ftab.lb0 + (ftab.nb - 1) * ftab.hb <= bx.lb_hi;
+    if (inside) {
+      const int nin = (int)std::floor((bx.lw_hi - ftab.lw0) / ftab.hw) + 1;
+      w_sur = std::max(0, std::min(ftab.nw, nin)) / 64 * 64;
+    }
+  }
+  if (!isPoint) CK(fpartq.ensure(flux_table_part_doubles(ftab.nw, ftab.nb)));
+  CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, ss, w_sur));
+  if (w_sur > 0) {
+    const int n = w_sur * ftab.nb;
+    CK(surrogate->tx.ensure((size_t)n * 5));
+    CK(surrogate->out.ensure(n));
+    CK(launch_mlp_table_inputs(surrogate->box, ftab, 0, w_sur, (float)R, (float)a, (float)gam,
+                               surrogate->tx.p, ss));
+    CK(launch_mlp_infer(surrogate->pb.p, surrogate->pf.p, surrogate->tx.p, n, surrogate->out.p, ss));
+    CK(launch_mlp_table_fill(ftab, 0, w_sur, gam, (double)A, surrogate->out.p, ss));
+  }
+  surrogate_rows = w_sur;
+  ftab_last = ftab;
+  nqn_last = nqn;
+  return UPCG_OK;
+}
+
 int upcg_generator::build_lumi() {
   if (lumiMethod == 3) return build_lumi_grid();
   cudaStream_t s = st();
@@ -927,18 +1025,23 @@ int upcg_generator::build_lumi() {
   CK(mcpy(mirror.p, mir.data(), ny * sizeof(int), cudaMemcpyHostToDevice, s));
   LumiParams p = lumi_params();
   p.mirror = mirror.p;
-  const int chunk = std::max(1, std::min(ncell, 65536) / ny) * ny;
-  CK(flux.ensure((size_t)chunk * 2 * kNb));
-  CK(nq.ensure((size_t)chunk * 2));
+  // 1: fast form (flux tables + tensor-core contraction); 2: the same
+  // contraction on the plain path's exact node fluxes (QAGS / K0,K1)
+  const bool fast = lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4;
+  const bool node_flux = lumiMethod == 2 || !fast;
+  // cells per chunk: the node-flux paths hold 1.9 KB of node fluxes per cell,
+  // the fast form 8 KB of contraction operands; its chunks are larger, so
+  // that a table needs fewer persistent contractions (2 GB at 2^18 cells)
+  const int chunk = std::max(1, std::min(ncell, node_flux ? 65536 : 262144) / ny) * ny;
+  if (node_flux) {
+    CK(flux.ensure((size_t)chunk * 2 * kNb));
+    CK(nq.ensure((size_t)chunk * 2));
+  }
   CK(work.ensure(1));
   CK(stats.ensure(1));
   const int ovf_cap = 1 << 20;
   CK(ovf.ensure(ovf_cap));
   CK(cudaMemsetAsync(stats.p, 0, sizeof(QagsStats), s));
-  // 1: fast form (flux tables + tensor-core contraction); 2: the same
-  // contraction on the plain path's exact node fluxes (QAGS / K0,K1)
-  const bool fast = lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4;
-  const bool node_flux = lumiMethod == 2 || !fast;
   if (lumiMethod == 4 && !surrogate)
     return fail(UPCG_ERR_STATE, "luminosity method 4 needs a surrogate (upcg_set_flux_surrogate)");
   if (fast && usePolarizedCS)
@@ -980,82 +1083,21 @@ int upcg_generator::build_lumi() {
     CK(fgaa32.ensure(p.gaa.n));
     CK(fbrk32.ensure(breakupMode != 1 ? p.brk.n : 1));
     CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p));
-    // flux tables: K0/K1 on ln x; Q(w, b) on 512 x 256 (ln w, ln b) points by
-    // 24 Gauss-Legendre panels of 16 points on q in [0, kQNodeMax] (panels of
-    // 1/16 GeV, two thirds of J1's shortest period, at b = 2R) and the
-    // closed-form rest to q = 10
-    const int nk = flux_table_ktab_n();
-    CK(fk1.ensure(nk));
-    CK(fs32.ensure(nk));
-    ftab.st = fk1.p;
-    ftab.st32 = fs32.p;
-    ftab.nw = 512;
-    ftab.nb = 256;
-    const double ymx = std::max(std::fabs(ymin), std::fabs(ymax));
-    const double kmin = mmin / 2. * std::exp(-ymx) * 0.9, kmax = mmax / 2. * std::exp(ymx) * 1.1;
-    ftab.lw0 = std::log(kmin);
-    ftab.hw = (std::log(kmax) - ftab.lw0) / (ftab.nw - 1);
-    ftab.lb0 = std::log(0.05 * R * 0.999);
-    ftab.hb = (std::log(2. * R * 1.001) - ftab.lb0) / (ftab.nb - 1);
-    const int npan = 24, ngl = 16, nqn = npan * ngl;
-    if (!isPoint) {
-      std::vector<double> gx, gw, qn(nqn), wn(nqn);
-      gauss_legendre(ngl, gx, gw);
-      for (int pa = 0; pa < npan; ++pa) {
-        const double lo = kQNodeMax * pa / npan, hi = kQNodeMax * (pa + 1) / npan;
-        for (int j = 0; j < ngl; ++j) {
-          qn[pa * ngl + j] = 0.5 * (hi - lo) * gx[j] + 0.5 * (hi + lo);
-          wn[pa * ngl + j] = 0.5 * (hi - lo) * gw[j];
-        }
-      }
-      CK(fqn.ensure(nqn));
-      CK(fwn.ensure(nqn));
-      CK(fq.ensure((size_t)ftab.nw * ftab.nb));
-      CK(fq32.ensure((size_t)ftab.nw * ftab.nb));
-      CK(fH.ensure((size_t)ftab.nw * nqn));
-      CK(fJ.ensure((size_t)nqn * ftab.nb));
-      CK(mcpy(fqn.p, qn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
-      CK(mcpy(fwn.p, wn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, s));
-      ftab.qt = fq.p;
-      ftab.qt32 = fq32.p;
+    // the flux tables, unless build_tables already enqueued them beside the
+    // breakup and G_AA chains
+    if (!ftab_early) {
+      const int ft0 = mark();
+      const int rc = setup_flux_tables(s);
+      if (rc) return rc;
+      spans.push_back({5, {ft0, mark()}});
     }
-    // method 4: the rows inside the surrogate's box from the MLP (rows in
-    // blocks of 64), the others from the quadrature
-    int w_sur = 0;
-    const double gam = g1;
-    if (lumiMethod == 4 && !isPoint) {
-      const MlpBox& bx = surrogate->box;
-      const bool inside = R >= bx.R_lo && R <= bx.R_hi && a >= bx.a_lo && a <= bx.a_hi &&
-                          gam >= bx.g_lo && gam <= bx.g_hi && ftab.lw0 >= bx.lw_lo &&
-                          ftab.lb0 >= std::log(bx.bf_lo * R) &&
-                          ftab.lb0 + (ftab.nb - 1) * ftab.hb <= bx.lb_hi;
-      if (inside) {
-        const int nin = (int)std::floor((bx.lw_hi - ftab.lw0) / ftab.hw) + 1;
-        w_sur = std::max(0, std::min(ftab.nw, nin)) / 64 * 64;
-      }
-    }
-    if (!isPoint) CK(fpartq.ensure(flux_table_part_doubles(ftab.nw, ftab.nb)));
-    const int ft0 = mark();  // flux-table build: quadrature rows + surrogate rows
-    CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, s, w_sur));
-    if (w_sur > 0) {
-      const int n = w_sur * ftab.nb;
-      CK(surrogate->tx.ensure((size_t)n * 5));
-      CK(surrogate->out.ensure(n));
-      CK(launch_mlp_table_inputs(surrogate->box, ftab, 0, w_sur, (float)R, (float)a, (float)gam,
-                                 surrogate->tx.p, s));
-      CK(launch_mlp_infer(surrogate->pb.p, surrogate->pf.p, surrogate->tx.p, n, surrogate->out.p, s));
-      CK(launch_mlp_table_fill(ftab, 0, w_sur, gam, (double)A, surrogate->out.p, s));
-    }
-    surrogate_rows = w_sur;
-    spans.push_back({5, {ft0, mark()}});
+    ftab = ftab_last;
     // ln(m/2) per mass row, and the survival kernel beyond b = 20 fm
     std::vector<double> lnm2(nm);
     for (int im = 0; im < nm; ++im) lnm2[im] = std::log((p.mmin + p.dm * im) / 2.);
     CK(flnm2.ensure(nm));
     CK(mcpy(flnm2.p, lnm2.data(), nm * sizeof(double), cudaMemcpyHostToDevice, s));
     spans.push_back({4, {b, mark()}});
-    ftab_last = ftab;
-    nqn_last = nqn;
   }
   for (int c0 = cell_lo; c0 < cell_hi; c0 += chunk) {
     const int nc = std::min(chunk, cell_hi - c0);
@@ -1123,6 +1165,12 @@ int upcg_generator::build_lumi() {
     cudaEventElapsedTime(&t, ev[sp.second.first], ev[sp.second.second]);
     timings[2 + sp.first] += t;  // [3] nodes [4] qags [5] band/contract [6] projection+G
   }
+  if (ftab_early && fast) {  // the flux tables ran beside the table chains
+    float t = 0;
+    cudaEventElapsedTime(&t, ev_ft[0], ev_ft[1]);
+    timings[7] = t;
+  }
+  ftab_early = false;
   for (auto e : ev) cudaEventDestroy(e);
   if (fast) {
     unsigned herr = 0;
@@ -1216,6 +1264,17 @@ int upcg_generator::build_vm() {
 // they run beside the luminosity; build_xsec joins them.
 int upcg_generator::enqueue_static_samplers(cudaStream_t ss) {
   const FoldParams f = fold_params();
+  {  // getBinY (include/UpcSampler.h:130-133) of every numerator int(nm (m - mmin))
+    const double lo = mmin, hi = mmin + (mmax - mmin) / nm * nm;
+    const double nmax = std::floor(nm * (hi - lo)) + 2;
+    mbinlut_n = nmax < (double)(1 << 22) ? (int)nmax : 0;
+    if (mbinlut_n > 0 && !cap) {  // a captured replay reuses the set-up run's table
+      std::vector<int> lut((size_t)mbinlut_n);
+      for (int n = 0; n < mbinlut_n; ++n) lut[n] = (int)((double)n / (hi - lo));
+      CK(mbinlut.ensure(mbinlut_n));
+      CK(mcpy(mbinlut.p, lut.data(), (size_t)mbinlut_n * sizeof(int), cudaMemcpyHostToDevice, ss));
+    }
+  }
   if (isVM) {
     CK(cdfz.ensure(1));  // no z distribution (ignoreCSZ)
   } else if (!usePolarizedCS) {

@@ -53,6 +53,19 @@ __device__ __forceinline__ float u24(uint32_t a) {  // [0, 1)
 
 constexpr float kTwoPiF = 6.28318530717958647692f;
 
+// num / den in FP32 for 0 <= num <= den (a CDF difference and its bin's
+// width): the fraction of the way through a bin, in [0, 1); 0 for an empty
+// bin.  Widths below 2^-100 are scaled up first (exact in FP64).
+__device__ __forceinline__ float frac_in_bin(double num, double den) {
+  if (!(den > 0.)) return 0.f;
+  if (den < 0x1p-100) {
+    num *= 0x1p100;
+    den *= 0x1p100;
+  }
+  const float f = (float)num / (float)den;
+  return f < 0.f ? 0.f : (f < 0x1.fffffep-1f ? f : 0x1.fffffep-1f);
+}
+
 // cdf[k] <= r < cdf[k+1] over n bins (the last non-empty bin if r >= cdf[n]).
 __device__ __forceinline__ int cdf_find(const double* __restrict__ cdf, int n, double r) {
   int lo = 0, hi = n;
@@ -273,15 +286,20 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   const double ra = u53(r0.x, r0.y), rb = u53(r0.z, r0.w);
   const int k = cdf_find_from(cdf2, n2, __ldg(e.g2 + (int)(ra * (double)e.g2_n)), ra);
   const int iy = k / e.nm, im = k - iy * e.nm;
+  // the position inside the bin, (r - c0) / (c1 - c0), in FP32: the event
+  // stores y in FP32, and GB300's FP64 pipe runs at 1/64 of the FP32 rate
   const double c0 = __ldg(cdf2 + k), c1 = __ldg(cdf2 + k + 1);
-  const double delta = c1 > c0 ? (ra - c0) / (c1 - c0) : 0.;
+  const float delta = frac_in_bin(ra - c0, c1 - c0);
   const double ylo = e.ymin + e.dy * iy, yhi = e.ymin + e.dy * (iy + 1);
   const double mlo = e.mmin + e.dm * im, mhi = e.mmin + e.dm * (im + 1);
-  c.y = ylo + delta * (yhi - ylo);
+  c.y = ylo + (double)delta * (yhi - ylo);
   c.m = mlo + rb * (mhi - mlo);
-  // getBinY (include/UpcSampler.h:130-133), the int() truncating the numerator
-  const double medge_hi = e.mmin + e.dm * e.nm;
-  int mb = (int)((double)(int)(e.nm * (c.m - e.mmin)) / (medge_hi - e.mmin));
+  // getBinY (include/UpcSampler.h:130-133), the int() truncating the numerator:
+  // int(n / (hi - lo)) of the integer n = int(nm (m - lo)) from a table made
+  // on the host with that FP64 division (no division per candidate)
+  const int nnum = (int)(e.nm * (c.m - e.mmin));
+  int mb = (nnum >= 0 && nnum < e.mbin_lut_n) ? __ldg(e.mbin_lut + nnum)
+                                              : (int)((double)nnum / (e.medge_hi - e.mmin));
   mb = mb < 0 ? 0 : (mb > e.nm - 1 ? e.nm - 1 : mb);
   c.mbin = mb;
   // z = cos(theta)
@@ -303,9 +321,8 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
       iz = cdf_find_from(cz, e.nz, __ldg(e.gz + (size_t)mb * e.gz_n + (int)(rz * (double)e.gz_n)), rz);
     }
     const double z0 = __ldg(cz + iz), z1 = __ldg(cz + iz + 1);
-    const double dl = z1 > z0 ? (rz - z0) / (z1 - z0) : 0.;
-    const double zlo = e.zmin + e.dz * iz, zhi = e.zmin + e.dz * (iz + 1);
-    c.z = zlo + dl * (zhi - zlo);
+    const float dl = frac_in_bin(rz - z0, z1 - z0);
+    c.z = (double)fmaf((float)e.dz, (float)iz + dl, (float)e.zmin);
   } else {
     c.z = -1. + 2. * rz;
   }

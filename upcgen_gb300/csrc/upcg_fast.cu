@@ -592,7 +592,7 @@ __global__ void k_fast_sides(LumiParams p, FastGrid fg, FluxTabs ft, int cell0, 
   out[t] = c;
 }
 
-__global__ void __launch_bounds__(kProjThreads) k_fast_project(
+__global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
     LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
     const SideC* __restrict__ sides, const double* __restrict__ flux_nodes,
     __nv_bfloat16* __restrict__ ah, __nv_bfloat16* __restrict__ al, float* __restrict__ a2,

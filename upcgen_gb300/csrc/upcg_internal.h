@@ -236,6 +236,10 @@ struct EventParams {
   // [0, kPomQmax]), the beam gamma, the daughters' mass and angular law
   // (0: 1 + cos^2, 1: 1 + 0.605 cos^2), a device counter of candidates whose
   // decay-angle draw ran out of tries
+  // getBinY's int(n / (mmax_edge - mmin)) for n < mbin_lut_n, and that edge
+  int mbin_lut_n;
+  const int* mbin_lut;
+  double medge_hi;
   int vm;
   const double* vm_ratio;
   const double* pom_cdf;
