@@ -295,6 +295,7 @@ struct upcg_generator {
   DBuf<double> vm_m, vm_y, vm_b, vm_k, vm_w, vm_f, vm_flux, vm_s, pom_vals, pom_cdf;
   DBuf<unsigned> vm_err;
   DBuf<int> mbinlut;  // getBinY of int(nm (m - mmin)), see EventParams
+  DBuf<uint64_t> cdf2fx, cdfzfx;  // fixed-point CDF copies (EventParams)
   int mbinlut_n = 0;  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
   std::vector<double> bu_host;
   int bu_nt = 0;
@@ -571,12 +572,19 @@ EventParams upcg_generator::event_params() const {
   e.pt_width = 6. * kHc / R / 5000;
   e.pt_c0 = (float)(2. * std::log(gtot) + e.pt_lne0);
   e.pt_inv_dlne = (float)(1. / e.pt_dlne);
-  int g2n = 1;
-  while (g2n < nm * ny) g2n <<= 1;
+  int g2n = 1, g2b = 0;
+  while (g2n < nm * ny) {
+    g2n <<= 1;
+    ++g2b;
+  }
   e.g2 = guide2.p;
   e.g2_n = g2n;
+  e.g2_bits = g2b;
   e.gz = guidez.p;
   e.gz_n = 128;
+  e.gz_bits = 7;
+  e.cdf2fx = cdf2fx.p;
+  e.cdfzfx = cdfzfx.p;
   e.gpt = guidept.p;
   e.gpt_n = 4096;
   e.polarized = usePolarizedCS ? 1 : 0;
@@ -1298,8 +1306,10 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss) {
   CK(launch_photon_pt_tables(e, lumi_params().ff, ff32.p, ptcdf.p, ss));
   CK(guidez.ensure((size_t)nm * e.gz_n));
   CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
+  CK(cdfzfx.ensure((size_t)nm * (nz + 1)));
   const EventParams eg = event_params();  // with the guide buffers allocated
-  CK(launch_guides(eg, nullptr, cdfz.p, ptcdf.p, nullptr, guidez.p, guidept.p, ss));
+  CK(launch_guides(eg, nullptr, cdfz.p, ptcdf.p, nullptr, guidez.p, guidept.p, ss, nullptr,
+                   cdfzfx.p));
   return UPCG_OK;
 }
 
@@ -1346,8 +1356,10 @@ int upcg_generator::build_xsec() {
   {
     const EventParams e = event_params();
     CK(guide2.ensure(e.g2_n));
+    CK(cdf2fx.ensure((size_t)ncell + 1));
     const EventParams eg = event_params();  // with the guide buffer allocated
-    CK(launch_guides(eg, cdf2.p, nullptr, nullptr, guide2.p, nullptr, nullptr, s));
+    CK(launch_guides(eg, cdf2.p, nullptr, nullptr, guide2.p, nullptr, nullptr, s, cdf2fx.p,
+                     nullptr));
   }
   if (cap) {  // a captured replay leaves sigma_tot on the device (read after the replay)
     xsec_ready = true;

@@ -66,6 +66,44 @@ __device__ __forceinline__ float frac_in_bin(double num, double den) {
   return f < 0.f ? 0.f : (f < 0x1.fffffep-1f ? f : 0x1.fffffep-1f);
 }
 
+// The (y, m) and z CDFs are also held in 64-bit fixed point (value * 2^64,
+// 1 saturating to 2^64 - 1) and searched with a 64-bit uniform r: integer
+// compares instead of FP64 ones, which on this part run at 1/64 of the FP32
+// rate.  The bin is the largest k with cdf[k] <= r, as before.
+__device__ __forceinline__ int cdf_find_from_fx(const uint64_t* __restrict__ cdf, int n, int k,
+                                                uint64_t r) {
+#pragma unroll 1
+  for (int s = 0; s < 8; ++s) {
+    if (k + 1 >= n || __ldg(cdf + k + 1) > r) return k;
+    ++k;
+  }
+  int hi = n;
+  while (hi - k > 1) {
+    const int mid = (k + hi) >> 1;
+    if (r >= __ldg(cdf + mid)) k = mid; else hi = mid;
+  }
+  return k;
+}
+
+__device__ __forceinline__ int cdf_find_fx(const uint64_t* __restrict__ cdf, int n, uint64_t r) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (r >= __ldg(cdf + mid)) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// num / den for fixed-point num <= den: both scaled so that den has its top
+// bit set, then their top 32 bits divided in FP32; [0, 1), 0 for den = 0
+__device__ __forceinline__ float frac_fx(uint64_t num, uint64_t den) {
+  if (den == 0) return 0.f;
+  if (num >= den) return 0x1.fffffep-1f;
+  const int s = __clzll((long long)den);
+  const float f = (float)(uint32_t)((num << s) >> 32) / (float)(uint32_t)((den << s) >> 32);
+  return f < 0x1.fffffep-1f ? f : 0x1.fffffep-1f;
+}
+
 // cdf[k] <= r < cdf[k+1] over n bins (the last non-empty bin if r >= cdf[n]).
 __device__ __forceinline__ int cdf_find(const double* __restrict__ cdf, int n, double r) {
   int lo = 0, hi = n;
@@ -283,17 +321,17 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   const uint4 r2 = philox4x32_10(make_uint4(clo, chi, 2u, 0x55504347u), key);
   // (y, m): gsl_histogram2d_pdf_sample with r1 for the bin and y, r2 for m
   const int n2 = e.ny * e.nm;
-  const double ra = u53(r0.x, r0.y), rb = u53(r0.z, r0.w);
-  const int k = cdf_find_from(cdf2, n2, __ldg(e.g2 + (int)(ra * (double)e.g2_n)), ra);
+  const uint64_t ra = ((uint64_t)r0.x << 32) | r0.y;
+  const double rb = u53(r0.z, r0.w);
+  const int k = cdf_find_from_fx(e.cdf2fx, n2, __ldg(e.g2 + (int)(ra >> (64 - e.g2_bits))), ra);
   const int iy = k / e.nm, im = k - iy * e.nm;
-  // the position inside the bin, (r - c0) / (c1 - c0), in FP32: the event
-  // stores y in FP32, and GB300's FP64 pipe runs at 1/64 of the FP32 rate
-  const double c0 = __ldg(cdf2 + k), c1 = __ldg(cdf2 + k + 1);
-  const float delta = frac_in_bin(ra - c0, c1 - c0);
-  const double ylo = e.ymin + e.dy * iy, yhi = e.ymin + e.dy * (iy + 1);
+  // the position inside the bin, (r - c0) / (c1 - c0), in FP32 (the event
+  // stores y in FP32); m in FP64, for getBinY
+  const float delta = frac_fx(ra - __ldg(e.cdf2fx + k), __ldg(e.cdf2fx + k + 1) - __ldg(e.cdf2fx + k));
+  c.y = (double)fmaf((float)iy + delta, (float)e.dy, (float)e.ymin);
   const double mlo = e.mmin + e.dm * im, mhi = e.mmin + e.dm * (im + 1);
-  c.y = ylo + (double)delta * (yhi - ylo);
   c.m = mlo + rb * (mhi - mlo);
+  (void)cdf2;
   // getBinY (include/UpcSampler.h:130-133), the int() truncating the numerator:
   // int(n / (hi - lo)) of the integer n = int(nm (m - lo)) from a table made
   // on the host with that FP64 division (no division per candidate)
@@ -303,28 +341,30 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   mb = mb < 0 ? 0 : (mb > e.nm - 1 ? e.nm - 1 : mb);
   c.mbin = mb;
   // z = cos(theta)
-  const double rz = u53(r1.x, r1.y);
-  if (!e.ignoreCSZ) {
+  if (!e.ignoreCSZ && !e.polarized) {
+    const uint64_t rz = ((uint64_t)r1.x << 32) | r1.y;
+    const uint64_t* cz = e.cdfzfx + (size_t)mb * (e.nz + 1);
+    const int iz = cdf_find_from_fx(
+        cz, e.nz, __ldg(e.gz + (size_t)mb * e.gz_n + (int)(rz >> (64 - e.gz_bits))), rz);
+    const float dl = frac_fx(rz - __ldg(cz + iz), __ldg(cz + iz + 1) - __ldg(cz + iz));
+    c.z = (double)fmaf((float)e.dz, (float)iz + dl, (float)e.zmin);
+  } else if (!e.ignoreCSZ) {
+    // polarized: the scalar or pseudoscalar z sampler of this mass bin; the
+    // reference draws Uniform(0, 1) < polCSRatio[yBin][mBin] (getBinX of y, as getBinY)
+    const double rz = u53(r1.x, r1.y);
     const double* cz = cdfz + (size_t)mb * (e.nz + 1);
-    int iz;
-    if (e.polarized) {
-      // scalar or pseudoscalar z sampler of this mass bin: the reference draws
-      // Uniform(0, 1) < polCSRatio[yBin][mBin] (getBinX of y, as getBinY)
-      const double yedge_hi = e.ymin + e.dy * e.ny;
-      int yb = (int)((double)(int)(e.ny * (c.y - e.ymin)) / (yedge_hi - e.ymin));
-      yb = yb < 0 ? 0 : (yb > e.ny - 1 ? e.ny - 1 : yb);
-      const uint4 r4 = philox4x32_10(make_uint4(clo, chi, 4u, 0x55504347u), key);
-      if (!(u53(r4.x, r4.y) < __ldg(e.ratio + (size_t)yb * e.nm + mb)))
-        cz = e.cdfz_ps + (size_t)mb * (e.nz + 1);
-      iz = cdf_find(cz, e.nz, rz);
-    } else {
-      iz = cdf_find_from(cz, e.nz, __ldg(e.gz + (size_t)mb * e.gz_n + (int)(rz * (double)e.gz_n)), rz);
-    }
+    const double yedge_hi = e.ymin + e.dy * e.ny;
+    int yb = (int)((double)(int)(e.ny * (c.y - e.ymin)) / (yedge_hi - e.ymin));
+    yb = yb < 0 ? 0 : (yb > e.ny - 1 ? e.ny - 1 : yb);
+    const uint4 r4 = philox4x32_10(make_uint4(clo, chi, 4u, 0x55504347u), key);
+    if (!(u53(r4.x, r4.y) < __ldg(e.ratio + (size_t)yb * e.nm + mb)))
+      cz = e.cdfz_ps + (size_t)mb * (e.nz + 1);
+    const int iz = cdf_find(cz, e.nz, rz);
     const double z0 = __ldg(cz + iz), z1 = __ldg(cz + iz + 1);
     const float dl = frac_in_bin(rz - z0, z1 - z0);
     c.z = (double)fmaf((float)e.dz, (float)iz + dl, (float)e.zmin);
   } else {
-    c.z = -1. + 2. * rz;
+    c.z = -1. + 2. * (double)u24(r1.x);
   }
   if (e.vm) return gen_vm(e, pttab, c, clo, chi, key, r1, r2);
   // pair momentum (getPairMomentum)
@@ -556,6 +596,25 @@ __global__ void k_guide_rows_d(const double* __restrict__ cdf, int rows, int len
   guide[t] = cdf_find(cdf + (size_t)r * (len + 1), len, (double)j / (double)K);
 }
 
+// fixed-point copy of a CDF (see cdf_find_from_fx)
+__global__ void k_cdf_fixed(const double* __restrict__ cdf, int64_t n, uint64_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = cdf[i];
+  out[i] = v >= 1. ? ~0ull : (v > 0. ? (uint64_t)(v * 18446744073709551616.0) : 0ull);
+}
+
+// guide[r][j]: the bin of r_j = j 2^(64 - bits) in fixed-point CDF row r
+__global__ void k_guide_rows_fx(const uint64_t* __restrict__ cdf, int rows, int len, int bits,
+                                int* __restrict__ guide) {
+  const int64_t K = (int64_t)1 << bits;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)rows * K) return;
+  const int r = (int)(t >> bits);
+  const uint64_t j = (uint64_t)(t - ((int64_t)r << bits));
+  guide[t] = cdf_find_fx(cdf + (size_t)r * (len + 1), len, j << (64 - bits));
+}
+
 __global__ void k_guide_rows_f(const float* __restrict__ cdf, int rows, int len, int K,
                                uint16_t* __restrict__ guide) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -617,18 +676,28 @@ cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* 
 
 cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                           const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
-                          cudaStream_t st) {
+                          cudaStream_t st, uint64_t* d_cdf2fx, uint64_t* d_cdfzfx) {
   if (e.pt_nbins > 65535) return cudaErrorInvalidValue;
-  // each guide set is built when its buffer is given (null: skipped)
+  if (e.g2_n != (1 << e.g2_bits) || e.gz_n != (1 << e.gz_bits)) return cudaErrorInvalidValue;
+  // each guide set is built when its buffer is given (null: skipped), with
+  // the fixed-point copy of its CDF
   const int n2 = e.nm * e.ny;
   if (d_g2) {
+    if (!d_cdf2fx) return cudaErrorInvalidValue;
     note_launch();
-    k_guide_rows_d<<<(e.g2_n + 255) / 256, 256, 0, st>>>(d_cdf2, 1, n2, e.g2_n, d_g2);
+    k_cdf_fixed<<<(unsigned)((n2 + 1 + 255) / 256), 256, 0, st>>>(d_cdf2, n2 + 1, d_cdf2fx);
+    note_launch();
+    k_guide_rows_fx<<<(e.g2_n + 255) / 256, 256, 0, st>>>(d_cdf2fx, 1, n2, e.g2_bits, d_g2);
   }
   if (d_gz && !e.ignoreCSZ && !e.polarized) {  // polarized z: plain searches on two CDF sets
+    if (!d_cdfzfx) return cudaErrorInvalidValue;
+    const int64_t nzc = (int64_t)e.nm * (e.nz + 1);
+    note_launch();
+    k_cdf_fixed<<<(unsigned)((nzc + 255) / 256), 256, 0, st>>>(d_cdfz, nzc, d_cdfzfx);
     const int64_t nz = (int64_t)e.nm * e.gz_n;
     note_launch();
-    k_guide_rows_d<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(d_cdfz, e.nm, e.nz, e.gz_n, d_gz);
+    k_guide_rows_fx<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(d_cdfzfx, e.nm, e.nz, e.gz_bits,
+                                                                  d_gz);
   }
   if (d_gpt && (e.useNonzeroGamPt || e.vm)) {  // vector mesons always draw a photon pT
     const int64_t np = (int64_t)e.pt_ne * e.gpt_n;

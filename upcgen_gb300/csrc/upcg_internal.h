@@ -240,6 +240,11 @@ struct EventParams {
   int mbin_lut_n;
   const int* mbin_lut;
   double medge_hi;
+  // 64-bit fixed-point copies of the (y, m) CDF and the z CDFs, searched with
+  // the guides g2 / gz (2^g2_bits, 2^gz_bits buckets per row)
+  const uint64_t* cdf2fx;
+  const uint64_t* cdfzfx;
+  int g2_bits, gz_bits;
   int vm;
   const double* vm_ratio;
   const double* pom_cdf;
@@ -252,7 +257,8 @@ struct EventParams {
 // g2_n, nm * gz_n, pt_ne * gpt_n
 cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                           const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
-                          cudaStream_t st);
+                          cudaStream_t st, uint64_t* d_cdf2fx = nullptr,
+                          uint64_t* d_cdfzfx = nullptr);
 struct EventRecord {  // 48 bytes
   float m, y, z, sign;
   float p0[4];
