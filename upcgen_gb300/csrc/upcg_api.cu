@@ -362,6 +362,7 @@ struct upcg_generator {
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_static) cudaEventDestroy(ev_static);
+    if (hstat) cudaFreeHost(hstat);
     for (auto e : ev_ft)
       if (e) cudaEventDestroy(e);
     if (own) cudaStreamDestroy(own);
@@ -395,8 +396,26 @@ struct upcg_generator {
   int build_tables();
   int build_lumi();
   int build_vm();
-  int setup_flux_tables(cudaStream_t ss);
+  int setup_flux_tables(cudaStream_t ss, int with_ktab = 1);
   bool ftab_early = false;  // build_tables enqueued the flux tables
+  bool ftab_early_done = false;  // ... and build_lumi used them (deferred timing)
+  // upcg_init enqueues tables, luminosity and cross section with one host
+  // synchronisation at its end: the phases' timing events, the contraction's
+  // error word, the QAGS statistics and sigma_tot are collected then
+  // (complete_deferred); other callers of the phases synchronise per phase
+  bool defer = false;
+  struct HostStatus {
+    unsigned herr, pad;
+    QagsStats stats;
+    double tot;
+  };
+  HostStatus* hstat = nullptr;  // pinned
+  cudaEvent_t tab_ev[2] = {nullptr, nullptr}, xs_ev[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> lumi_ev;
+  std::vector<std::pair<int, std::pair<int, int>>> lumi_spans;
+  int lumi_w0 = 0, lumi_w1 = 0;
+  bool tab_pending = false, lumi_pending = false, lumi_fast = false, xs_pending = false;
+  int complete_deferred(int rc);
   cudaEvent_t ev_ft[2] = {nullptr, nullptr};
   int enqueue_static_samplers(cudaStream_t ss);
   int fork_static_samplers();
@@ -713,8 +732,12 @@ int upcg_generator::build_tables() {
     // beside the breakup and G_AA chains
     for (auto& e : ev_ft)
       if (!e) CK(cudaEventCreate(&e));
+    // the point-flux table on the main stream, after the G_AA chain
+    CK(fk1.ensure(flux_table_ktab_n()));
+    CK(fs32.ensure(flux_table_ktab_n()));
+    CK(launch_ktab(g1, fk1.p, fs32.p, s));
     CK(cudaEventRecord(ev_ft[0], side[0]));
-    const int frc = setup_flux_tables(side[0]);
+    const int frc = setup_flux_tables(side[0], 0);
     if (frc) return frc;
     CK(cudaEventRecord(ev_ft[1], side[0]));
     ftab_early = true;
@@ -749,12 +772,18 @@ int upcg_generator::build_tables() {
   CK(cudaStreamWaitEvent(s, ev_join[1], 0));
   if (!cap) {
     cudaEventRecord(t1, s);
-    CK(cudaEventSynchronize(t1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, t0, t1);
-    timings[0] = ms;
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
+    if (defer) {
+      tab_ev[0] = t0;
+      tab_ev[1] = t1;
+      tab_pending = true;
+    } else {
+      CK(cudaEventSynchronize(t1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, t0, t1);
+      timings[0] = ms;
+      cudaEventDestroy(t0);
+      cudaEventDestroy(t1);
+    }
   }
   tables_ready = true;
   return UPCG_OK;
@@ -921,6 +950,7 @@ int upcg_generator::build_lumi_cached() {
   lumi_cache_hit = 0;
   if (!lock.held) return UPCG_OK;  // another process holds the file: compute only
   host.resize((size_t)ntab * ncell);
+  CK(cudaStreamSynchronize(st()));  // build_lumi may have left its work in flight
   CK(mcpy_sync(host.data(), lumi.p, ncell * sizeof(double), cudaMemcpyDeviceToHost));
   if (usePolarizedCS)
     CK(mcpy_sync(host.data() + ncell, lumi2.p, ncell * sizeof(double), cudaMemcpyDeviceToHost));
@@ -931,13 +961,16 @@ int upcg_generator::build_lumi_cached() {
 
 // The fast form's flux tables: K0/K1 on ln x and the Q(w, b) table (or its
 // surrogate rows), on stream ss; the result is in ftab_last.
-int upcg_generator::setup_flux_tables(cudaStream_t ss) {
+int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab) {
   const LumiParams p = lumi_params();
   FastFluxTables ftab{};
   // flux tables: K0/K1 on ln x; Q(w, b) on 512 x 256 (ln w, ln b) points by
-  // 24 Gauss-Legendre panels of 16 points on q in [0, kQNodeMax] (panels of
-  // 1/16 GeV, two thirds of J1's shortest period, at b = 2R) and the
-  // closed-form rest to q = 10
+  // 16 Gauss-Legendre panels of 16 points on q in [0, kQNodeMax] (panels of
+  // 3/32 GeV, one period of J1(b q / hc) at b = 2R for Pb) and the
+  // closed-form rest to q = 10.  With 8 panels the fast form's cells move by
+  // up to 1.3e-4 from the converged quadrature (the kink of the clamped form
+  // factor and the q -> 0 end inside wider panels); with 16, as with 24, they
+  // stay within 1e-4.
   const int nk = flux_table_ktab_n();
   CK(fk1.ensure(nk));
   CK(fs32.ensure(nk));
@@ -951,7 +984,7 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss) {
   ftab.hw = (std::log(kmax) - ftab.lw0) / (ftab.nw - 1);
   ftab.lb0 = std::log(0.05 * R * 0.999);
   ftab.hb = (std::log(2. * R * 1.001) - ftab.lb0) / (ftab.nb - 1);
-  const int npan = 24, ngl = 16, nqn = npan * ngl;
+  const int npan = 16, ngl = 16, nqn = npan * ngl;
   if (!isPoint) {
     std::vector<double> gx, gw, qn(nqn), wn(nqn);
     gauss_legendre(ngl, gx, gw);
@@ -989,7 +1022,7 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss) {
     }
   }
   if (!isPoint) CK(fpartq.ensure(flux_table_part_doubles(ftab.nw, ftab.nb)));
-  CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, ss, w_sur));
+  CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, ss, w_sur, with_ktab));
   if (w_sur > 0) {
     const int n = w_sur * ftab.nb;
     CK(surrogate->tx.ensure((size_t)n * 5));
@@ -1002,6 +1035,52 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss) {
   surrogate_rows = w_sur;
   ftab_last = ftab;
   nqn_last = nqn;
+  return UPCG_OK;
+}
+
+int upcg_generator::complete_deferred(int rc) {
+  defer = false;
+  const cudaError_t se = cudaStreamSynchronize(st());
+  auto elapsed = [](cudaEvent_t a, cudaEvent_t b) {
+    float t = 0;
+    cudaEventElapsedTime(&t, a, b);
+    return t;
+  };
+  if (tab_pending) {
+    timings[0] = elapsed(tab_ev[0], tab_ev[1]);
+    cudaEventDestroy(tab_ev[0]);
+    cudaEventDestroy(tab_ev[1]);
+    tab_pending = false;
+  }
+  bool herr = false;
+  if (lumi_pending) {
+    timings[1] = elapsed(lumi_ev[lumi_w0], lumi_ev[lumi_w1]);
+    for (int k = 3; k < 8; ++k) timings[k] = 0;
+    for (auto& sp : lumi_spans)
+      timings[2 + sp.first] += elapsed(lumi_ev[sp.second.first], lumi_ev[sp.second.second]);
+    if (lumi_fast && ev_ft[0] && ftab_early_done) timings[7] = elapsed(ev_ft[0], ev_ft[1]);
+    for (auto e : lumi_ev) cudaEventDestroy(e);
+    lumi_ev.clear();
+    lumi_spans.clear();
+    last_stats = hstat->stats;
+    herr = lumi_fast && hstat->herr != 0;
+    lumi_pending = false;
+  }
+  ftab_early_done = false;
+  if (xs_pending) {
+    timings[2] = elapsed(xs_ev[0], xs_ev[1]);
+    cudaEventDestroy(xs_ev[0]);
+    cudaEventDestroy(xs_ev[1]);
+    totCS = hstat->tot;
+    fidCS = totCS;
+    xs_pending = false;
+  }
+  if (rc) return rc;
+  if (se != cudaSuccess) return fail(UPCG_ERR_CUDA, "upcg_init: %s", cudaGetErrorString(se));
+  if (herr) {
+    xsec_ready = false;
+    return fail(UPCG_ERR_CUDA, "tensor-core contraction timed out (code %u)", hstat->herr);
+  }
   return UPCG_OK;
 }
 
@@ -1163,6 +1242,20 @@ int upcg_generator::build_lumi() {
     }
   }
   const int w1 = mark();
+  if (defer) {  // collected by complete_deferred
+    lumi_ev = std::move(ev);
+    lumi_spans = std::move(spans);
+    lumi_w0 = w0;
+    lumi_w1 = w1;
+    lumi_fast = fast;
+    ftab_early_done = ftab_early && fast;
+    ftab_early = false;
+    if (fast) CK(mcpy(&hstat->herr, ferr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(mcpy(&hstat->stats, stats.p, sizeof(QagsStats), cudaMemcpyDeviceToHost, s));
+    lumi_pending = true;
+    lumi_ready = true;
+    return UPCG_OK;
+  }
   CK(cudaEventSynchronize(ev[w1]));
   float ms = 0;
   cudaEventElapsedTime(&ms, ev[w0], ev[w1]);
@@ -1179,6 +1272,7 @@ int upcg_generator::build_lumi() {
     timings[7] = t;
   }
   ftab_early = false;
+  ftab_early_done = false;
   for (auto e : ev) cudaEventDestroy(e);
   if (fast) {
     unsigned herr = 0;
@@ -1362,6 +1456,19 @@ int upcg_generator::build_xsec() {
                      nullptr));
   }
   if (cap) {  // a captured replay leaves sigma_tot on the device (read after the replay)
+    xsec_ready = true;
+    return UPCG_OK;
+  }
+  if (defer) {  // collected by complete_deferred
+    CK(mcpy(&hstat->tot, tot.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    cudaEventRecord(t1, s);
+    xs_ev[0] = t0;
+    xs_ev[1] = t1;
+    xs_pending = true;
+    next_cand = 0;
+    ev_batch.clear();
+    ev_flag.clear();
+    ev_pos = 0;
     xsec_ready = true;
     return UPCG_OK;
   }
@@ -1641,25 +1748,28 @@ int upcg_init(upcg_generator* g) {
     return fail(UPCG_ERR_CUDA, "no CUDA device visible");
   if (g->nm < 1 || g->ny < 1 || g->nz < 1) return fail(UPCG_ERR_ARG, "empty grid");
   if (g->breakupMode < 1 || g->breakupMode > 4) return fail(UPCG_ERR_ARG, "BREAKUP_MODE must be 1..4");
+  if (!g->hstat && cudaMallocHost(&g->hstat, sizeof(upcg_generator::HostStatus)) != cudaSuccess)
+    return fail(UPCG_ERR_CUDA, "pinned status block");
+  g->defer = true;  // one host synchronisation, at the end (complete_deferred)
   int rc = g->build_tables();
-  if (rc) return rc;
+  if (rc) return g->complete_deferred(rc);
   g->lumi_cache_hit = -1;
   if (g->isVM) {  // photonuclear: calcNucCrossSectionY instead of the two-photon luminosity
     rc = g->build_vm();
-    if (rc) return rc;
-    return g->build_xsec();
+    if (rc) return g->complete_deferred(rc);
+    return g->complete_deferred(g->build_xsec());
   }
   rc = g->fork_static_samplers();  // beside the luminosity
-  if (rc) return rc;
+  if (rc) return g->complete_deferred(rc);
   rc = g->lumi_cache_usable() ? g->build_lumi_cached() : g->build_lumi();
   if (rc) {
     if (g->static_pending) {  // leave no side-stream work behind a failed init
       cudaStreamWaitEvent(g->st(), g->ev_static, 0);
       g->static_pending = false;
     }
-    return rc;
+    return g->complete_deferred(rc);
   }
-  return g->build_xsec();
+  return g->complete_deferred(g->build_xsec());
 }
 
 int upcg_lumi_cache_file(upcg_generator* g, char* path, size_t len, int* last_hit) {

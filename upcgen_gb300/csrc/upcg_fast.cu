@@ -1233,11 +1233,19 @@ size_t fast_side_bytes() { return sizeof(SideC); }
 
 int flux_table_part_doubles(int nw, int nb) { return 8 * nw * nb + nb; }  // slices + tail
 
+cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream) {
+  note_launch();
+  k_ktab<<<(kKTabN + 255) / 256, 256, 0, stream>>>(g1, st, st32);
+  return cudaGetLastError();
+}
+
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
                               int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st,
-                              int w_lo) {
-  note_launch();
-  k_ktab<<<(kKTabN + 255) / 256, 256, 0, st>>>(p.g1, t->st, t->st32);
+                              int w_lo, int with_ktab) {
+  if (with_ktab) {
+    note_launch();
+    k_ktab<<<(kKTabN + 255) / 256, 256, 0, st>>>(p.g1, t->st, t->st32);
+  }
   // Q rows [w_lo, nw) by the quadrature (w_lo a multiple of 64; the rows below
   // come from elsewhere)
   const int rows = t->nw - w_lo;

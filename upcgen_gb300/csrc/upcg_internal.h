@@ -150,7 +150,10 @@ int flux_table_part_doubles(int nw, int nb);
 // point-flux table, and the Q(w, b) rows [w_lo, nw) by the Hankel quadrature
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
                               int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st,
-                              int w_lo = 0);
+                              int w_lo = 0,
+                              int with_ktab = 1);
+// the point-flux table S(ln x) of the fast form (k_ktab) alone
+cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream);
 // lnm2[im] = ln(m_im / 2); c_far = P(20 fm) sum_k w_k, the survival kernel
 // wherever every azimuth has b >= 20 fm
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
