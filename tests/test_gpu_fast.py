@@ -73,6 +73,14 @@ def test_fast_config1_full_grid(ug, oracle_mod):
     assert rtot < FAST_TOL
     t = g.timings()
     assert t["contract_ms"] > 0
+    # one cell of each mirror pair y_j = -y_i (i + j = 61 on this grid; left
+    # edges equal and opposite to 8 ulps) is computed and the other copied:
+    # L(m, -y) = L(m, y).  Pairs whose edges miss the 8-ulp match are both
+    # computed and agree to the fast form's rounding.
+    lumi = g.lumiTable()
+    a, b = lumi[:, 1:], lumi[:, 1:][:, ::-1]
+    assert np.allclose(a, b, rtol=2e-5, atol=0)
+    assert np.mean(np.all(a == b, axis=0)) > 0.8
 
 
 @pytest.mark.parametrize("mode", [2, 3, 4])

@@ -316,7 +316,7 @@ struct upcg_generator {
     if (!ev_fork) return cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
     return cudaSuccess;
   }
-  DBuf<int> ntab, nq, ovf, tile_count, mirror, guide2, guidez;
+  DBuf<int> ntab, nq, ovf, tile_count, mirror, guide2, guidez, frep;
   DBuf<int4> fitems;
   DBuf<uint16_t> guidept;
   DBuf<unsigned int> work;
@@ -1186,8 +1186,24 @@ int upcg_generator::build_lumi() {
     CK(mcpy(flnm2.p, lnm2.data(), nm * sizeof(double), cudaMemcpyHostToDevice, s));
     spans.push_back({4, {b, mark()}});
   }
-  for (int c0 = cell_lo; c0 < cell_hi; c0 += chunk) {
-    const int nc = std::min(chunk, cell_hi - c0);
+  // the fast form on table fluxes computes one cell of each pair of mirror
+  // rapidities: L(m, -y) = L(m, y) (the photons swap and the survival kernel
+  // is symmetric), with equal beams
+  const bool use_map = fast && !node_flux && g1 == g2;
+  int row_lo = cell_lo, row_hi = cell_hi, n_rep = 0;
+  if (use_map) {
+    std::vector<int> rm;
+    for (int iy = 0; iy < ny; ++iy)
+      if (mir[iy] < 0 || iy < mir[iy]) rm.push_back(iy);
+    n_rep = (int)rm.size();
+    for (int j = 0; j < n_rep; ++j) rm.push_back(mir[rm[j]]);
+    CK(frep.ensure(2 * (size_t)n_rep));
+    CK(mcpy(frep.p, rm.data(), rm.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    row_lo = 0;
+    row_hi = (r1 - r0) * n_rep;
+  }
+  for (int c0 = row_lo; c0 < row_hi; c0 += chunk) {
+    const int nc = std::min(chunk, row_hi - c0);
     int b = 0;
     if (node_flux) {
       b = mark();
@@ -1219,7 +1235,7 @@ int upcg_generator::build_lumi() {
       b = mark();
       CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, flnm2.p, c_far,
                              node_flux ? flux.p : nullptr, &ftab, fsides.p, fah.p, fal.p, fa2.p,
-                             ffar.p, s));
+                             ffar.p, s, use_map ? frep.p : nullptr, n_rep, r0));
       spans.push_back({4, {b, mark()}});
       // persistent contraction over this chunk's (row tile, N tile) work list
       int shape = 0, grid = 0;
@@ -1238,7 +1254,9 @@ int upcg_generator::build_lumi() {
       CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(),
                               fa2.p, fpart.p, ferr.p, shape, grid, s));
       spans.push_back({3, {b, mark()}});
-      CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s, ffc.p));
+      CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s, ffc.p,
+                            use_map ? frep.p : nullptr, use_map ? frep.p + n_rep : nullptr, n_rep,
+                            r0));
     }
   }
   const int w1 = mark();

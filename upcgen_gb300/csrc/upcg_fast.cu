@@ -315,7 +315,18 @@ struct FastGrid {
   const double* lnm2;   // ln(m_im / 2)
   double ln5ghc1, ln5ghc2, ln5R, lnbmin, ln2R, ln_rnear, lnghc, lnc_pt, lnc_ff;
   double c_far;         // G where every azimuth has b >= 20 fm: P(20) sum_k w_k
+  // rows -> cells: null, row = cell; else row r is cell (m0 + r / n_rep_y,
+  // rep_y[r % n_rep_y]) -- one cell of each pair of mirror rapidities
+  // (L(m, -y) = L(m, y): the two photons swap and G is symmetric)
+  const int* rep_y;
+  int n_rep_y, m0;
 };
+
+__device__ __forceinline__ int fast_cell(const FastGrid& fg, int ny, int row) {
+  if (!fg.rep_y) return row;
+  const int q = row / fg.n_rep_y;
+  return (fg.m0 + q) * ny + __ldg(fg.rep_y + (row - q * fg.n_rep_y));
+}
 
 struct GParams {
   SplineF gaa, brk;
@@ -540,7 +551,7 @@ __global__ void k_fast_sides(LumiParams p, FastGrid fg, FluxTabs ft, int cell0, 
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 2 * ncells) return;
   const int lc = t >> 1, side = t & 1;
-  const int cell = cell0 + lc;
+  const int cell = fast_cell(fg, p.ny, cell0 + lc);
   const int im = cell / p.ny, iy = cell - (cell / p.ny) * p.ny;
   const double Y = p.ymin + p.dy * iy;
   const double lnk = fg.lnm2[im] + (side ? -Y : Y);  // k = m/2 e^{+-y} (:224-225)
@@ -615,7 +626,7 @@ __global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
     }
     return;
   }
-  const int cell = cell0 + lc;
+  const int cell = fast_cell(fg, p.ny, cell0 + lc);
   const int im = cell / p.ny, iy = cell - (cell / p.ny) * p.ny;
   if (tid < 2) sc[tid] = sides[2 * lc + tid];
   for (int q = 4 * tid; q < 2 * kMaxP; q += 4 * kProjThreads)
@@ -770,10 +781,10 @@ __global__ void k_far_consts(SplineU brk, int has_brk, LumiParams p, double* __r
 __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, double c_far,
                               const double* __restrict__ c_far_d,
                               const float* __restrict__ partial, const float4* __restrict__ far_term,
-                              double* __restrict__ lumi) {
+                              double* __restrict__ lumi, FastGrid fg, const int* __restrict__ rep_mir) {
   const int lc = blockIdx.x * blockDim.x + threadIdx.x;
   if (lc >= ncells) return;
-  const int cell = cell0 + lc;
+  const int cell = fast_cell(fg, p.ny, cell0 + lc);
   const int im = cell / p.ny;
   const double M = p.mmin + p.dm * im;
   double t2 = 0.;
@@ -781,7 +792,12 @@ __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, d
   const float4 f = far_term[lc];
   const double cf = c_far_d ? c_far_d[1] : c_far;
   const double s = exp((double)f.y + (double)f.z) * (cf * (double)f.x + t2);
-  lumi[cell] = 2 * kPi * kPi * M * s * p.dm * p.dy;
+  const double v = 2 * kPi * kPi * M * s * p.dm * p.dy;
+  lumi[cell] = v;
+  if (fg.rep_y) {  // the mirror rapidity's cell
+    const int j = (cell0 + lc) % fg.n_rep_y, iym = __ldg(rep_mir + j);
+    if (iym >= 0) lumi[im * p.ny + iym] = v;
+  }
 }
 
 // reference contraction in FP64 for the self-test
@@ -1197,8 +1213,13 @@ cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, doubl
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
                                 const double* flux_nodes, const FastFluxTables* t, void* d_sides,
-                                void* ah, void* al, float* a2, void* far_term, cudaStream_t st) {
+                                void* ah, void* al, float* a2, void* far_term, cudaStream_t st,
+                                const int* rep_y, int n_rep_y, int m0) {
+  if (rep_y && (flux_nodes || n_rep_y <= 0)) return cudaErrorInvalidValue;
   FastGrid fg{P, u0, h, 1.0 / h, 250.};
+  fg.rep_y = rep_y;
+  fg.n_rep_y = n_rep_y;
+  fg.m0 = m0;
   fg.lnm2 = lnm2;
   fg.ln5ghc1 = std::log(5. * p.g1 * kHc);
   fg.ln5ghc2 = std::log(5. * p.g2 * kHc);
@@ -1288,11 +1309,17 @@ cudaError_t launch_far_consts(const LumiParams& p, int has_brk, double* d_out, c
 
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
                                double c_far, const float* partial, const void* far_term,
-                               double* lumi, cudaStream_t st, const double* c_far_d) {
+                               double* lumi, cudaStream_t st, const double* c_far_d,
+                               const int* rep_y, const int* rep_mir, int n_rep_y, int m0) {
+  FastGrid fg{};
+  fg.rep_y = rep_y;
+  fg.n_rep_y = n_rep_y;
+  fg.m0 = m0;
+  if (rep_y && (!rep_mir || n_rep_y <= 0)) return cudaErrorInvalidValue;
   note_launch();
   k_fast_finish<<<(ncells + 255) / 256, 256, 0, st>>>(p, cell0, ncells, ntiles, c_far, c_far_d,
                                                       partial, static_cast<const float4*>(far_term),
-                                                      lumi);
+                                                      lumi, fg, rep_mir);
   return cudaGetLastError();
 }
 

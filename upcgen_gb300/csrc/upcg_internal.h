@@ -156,10 +156,15 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
 cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream);
 // lnm2[im] = ln(m_im / 2); c_far = P(20 fm) sum_k w_k, the survival kernel
 // wherever every azimuth has b >= 20 fm
+// rep_y (optional, n_rep_y entries): rows map to cells (m0 + r / n_rep_y,
+// rep_y[r % n_rep_y]) -- one of each pair of mirror rapidities, whose
+// luminosities are equal; launch_fast_finish then also writes the mirror cell
+// rep_mir[r % n_rep_y] (-1: none).  Without it row r is cell r.
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
                                 const double* flux_nodes, const FastFluxTables* t, void* d_sides,
-                                void* ah, void* al, float* a2, void* far_term, cudaStream_t st);
+                                void* ah, void* al, float* a2, void* far_term, cudaStream_t st,
+                                const int* rep_y = nullptr, int n_rep_y = 0, int m0 = 0);
 // bytes of the per-(cell, photon) constants (d_sides holds 2 per cell);
 // far_term holds one float4 per cell
 size_t fast_side_bytes();
@@ -185,7 +190,9 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
                             unsigned* d_err, cudaStream_t st);
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
                                double c_far, const float* partial, const void* far_term,
-                               double* lumi, cudaStream_t st, const double* c_far_d = nullptr);
+                               double* lumi, cudaStream_t st, const double* c_far_d = nullptr,
+                               const int* rep_y = nullptr, const int* rep_mir = nullptr,
+                               int n_rep_y = 0, int m0 = 0);
 cudaError_t contract_selftest(int ncells, int P, uint64_t seed, double* max_rel, double* ms);
 
 // fold + samplers
