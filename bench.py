@@ -164,8 +164,10 @@ def cpu_baseline_sample(workload, seconds=15.0):
 # DRAM traffic per launch from one ncu capture of the c2 workload (65,536-cell
 # chunk; profiles/k_contract_c2.md, profiles/k_fast_project_c2.md), scaled by
 # cells for the other chunk: bytes per cell
-CONTRACT_DRAM_BYTES_PER_CELL = (404.828160e6 + 3.985408e6) / 55660  # read + write, one launch
-PROJECT_DRAM_BYTES_PER_CELL = (9.432832e6 + 394.498816e6) / 55680
+# DRAM bytes per contraction row (read + write) and per projected row, from
+# the ncu captures in profiles/k_contract_c2.md and profiles/k_fast_project_c2.md
+CONTRACT_DRAM_BYTES_PER_CELL = (521.124608e6 + 4.506880e6) / 63063
+PROJECT_DRAM_BYTES_PER_CELL = (10.690816e6 + 457.163520e6) / 63063
 
 
 def main():
@@ -311,12 +313,15 @@ def main():
 
     pk_vals, pk_kind = peaks()
     P = FAST_GRID_P
-    cells_pad = (cells + 127) // 128 * 128
-    alg_flops = 2.0 * cells_pad * P * P  # A1 (cells x P) . G (P x P), per table
+    # the contraction's rows: one cell of each mirror-rapidity pair (the other
+    # is a copy); one launch covers up to 2^18 rows
+    rows = fast.contractRows()
+    rows_pad = (rows + 127) // 128 * 128
+    nlaunch_contract = max(1, -(-rows // 262144))
+    alg_flops = 2.0 * rows_pad * P * P  # A1 (rows x P) . G (P x P), per table
     achieved = alg_flops / (ms_contract * 1e-3) / 1e12
     peak = pk_vals.get("bf16_tflops", 1900.0)
-    nlaunch_contract = 2 if args.workload == "c2" else 1
-    traffic = (CONTRACT_DRAM_BYTES_PER_CELL * cells / nlaunch_contract
+    traffic = (CONTRACT_DRAM_BYTES_PER_CELL * rows / nlaunch_contract
                if CONTRACT_DRAM_BYTES_PER_CELL else None)
     ph = runs[-1][3]
     line = {
@@ -342,16 +347,17 @@ def main():
                      "bound": "tensor",
                      "achieved": achieved / nlaunch_contract * nlaunch_contract, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-                     "note": f"algorithmic 2*cells*P^2 = {alg_flops:.3e} FLOP per table over "
-                             f"{nlaunch_contract} launches (the hi/lo split issues it 3x); "
+                     "note": f"algorithmic 2*rows*P^2 = {alg_flops:.3e} FLOP per table over "
+                             f"{nlaunch_contract} launch(es), rows = {rows} computed cells (one of "
+                             f"each mirror-rapidity pair; the hi/lo split issues it 3x); "
                              f"peak = {pk_kind} bf16 burst; traffic = DRAM bytes per launch "
                              f"(profiles/k_contract_c2.md)"},
         "roofline_projection": {
             "kernel": "k_fast_sides + k_fast_project", "bound": "hbm",
-            "achieved": 8.0 * P * cells / (ms_project * 1e-3) / 1e9 if ms_project else None,
+            "achieved": 8.0 * P * rows / (ms_project * 1e-3) / 1e9 if ms_project else None,
             "peak": pk_vals.get("hbm_gbs", 6800.0), "unit": "GB/s",
-            "traffic": PROJECT_DRAM_BYTES_PER_CELL * cells / nlaunch_contract,
-            "note": "algorithmic bytes = the 8 KB per cell of contraction operands written "
+            "traffic": PROJECT_DRAM_BYTES_PER_CELL * rows / nlaunch_contract,
+            "note": "algorithmic bytes = the 8 KB per computed cell (row) of contraction operands written "
                     "(A1 bf16 hi + lo, A2 fp32); project_ms also holds the G and flux-table builds; "
                     "traffic = DRAM bytes per launch (profiles/k_fast_project_c2.md)"},
         "gpu_launches": n_launch,

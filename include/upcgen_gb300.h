@@ -332,6 +332,10 @@ int upcg_kernel_launches(uint64_t* n);
 /* host-to-device and device-to-host bytes the library has copied in this
  * process so far (all handles) */
 int upcg_copy_bytes(uint64_t* h2d, uint64_t* d2h);
+/* Rows of the last fast-form luminosity's contraction: the cells computed,
+ * one of each pair of mirror rapidities (L(m, -y) = L(m, y), copied to the
+ * other); 0 when the last luminosity was not the fast form */
+int upcg_contract_rows(const upcg_generator* g, int64_t* rows);
 const char* upcg_last_error(void);
 const char* upcg_version(void);
 

@@ -296,7 +296,8 @@ struct upcg_generator {
   DBuf<unsigned> vm_err;
   DBuf<int> mbinlut;  // getBinY of int(nm (m - mmin)), see EventParams
   DBuf<uint64_t> cdf2fx, cdfzfx;  // fixed-point CDF copies (EventParams)
-  int mbinlut_n = 0;  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
+  int mbinlut_n = 0;
+  int64_t contract_rows = 0;  // rows of the last fast-form contraction  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
   std::vector<double> bu_host;
   int bu_nt = 0;
   // side streams of the table set-up and their fork / join events
@@ -1202,6 +1203,7 @@ int upcg_generator::build_lumi() {
     row_lo = 0;
     row_hi = (r1 - r0) * n_rep;
   }
+  contract_rows = fast ? (int64_t)(row_hi - row_lo) : 0;
   for (int c0 = row_lo; c0 < row_hi; c0 += chunk) {
     const int nc = std::min(chunk, row_hi - c0);
     int b = 0;
@@ -2245,6 +2247,12 @@ int upcg_particle_pdg(upcg_generator* g, int* pdg, int* charged) {
   if (rc) return rc;
   *pdg = g->partPDG;
   if (charged) *charged = g->isCharged ? 1 : 0;
+  return UPCG_OK;
+}
+
+int upcg_contract_rows(const upcg_generator* g, int64_t* rows) {
+  if (!g || !rows) return fail(UPCG_ERR_ARG, "null argument");
+  *rows = g->contract_rows;
   return UPCG_OK;
 }
 
