@@ -41,7 +41,24 @@ WORKLOADS = {
            "MMIN": 3.56, "MMAX": 50, "BINS_M": 201, "YMIN": -6, "YMAX": 6, "BINS_Y": 61,
            "ZMIN": -1, "ZMAX": 1, "BINS_Z": 100, "SEED": 1},
 }
-EVENTS = {"c2": 10_000_000, "c1": 100_000}
+EVENTS = {"c2": 10_000_000, "c1": 100_000, "c5": 1_000_000_000}
+
+
+def c5_configs():
+    """The batched scan: Pb, Au, Xe, O x sqrt(s) 200/5020/5360/5440 GeV x
+    breakup modes 1-4, ALP (M = 1 GeV, width 0.01), m-bins cycling through
+    201/501/1001, 121 y-bins."""
+    nuclei = [(82, 208, 6.68, 0.447), (79, 197, 6.38, 0.535), (54, 129, 5.36, 0.59),
+              (8, 16, 2.608, 0.513)]
+    out, k = [], 0
+    for z, a, r, d in nuclei:
+        for sq in (200, 5020, 5360, 5440):
+            for mode in (1, 2, 3, 4):
+                out.append({"NUCLEUS_Z": z, "NUCLEUS_A": a, "WS_R": r, "WS_A": d, "SQRTS": sq,
+                            "PROC_ID": 51, "ALP_MASS": 1, "ALP_WIDTH": 0.01, "BREAKUP_MODE": mode,
+                            "BINS_M": (201, 501, 1001)[k % 3], "BINS_Y": 121, "SEED": 1 + k})
+                k += 1
+    return out
 METRIC = "gamma-gamma lumi (m,y) cells/s"
 FAST_GRID_P = 1024  # radial grid of the fast form (csrc/upcg_fast.cu)
 
@@ -170,13 +187,53 @@ CONTRACT_DRAM_BYTES_PER_CELL = (521.124608e6 + 4.506880e6) / 63063
 PROJECT_DRAM_BYTES_PER_CELL = (10.690816e6 + 457.163520e6) / 63063
 
 
+def run_scan(args, ug, torch):
+    """C5: 64 configurations in one captured scan (upcg_scan_*), replayed;
+    then 1e9 events over them into one device buffer.  A step is one replay
+    (every configuration's tables, one persistent contraction, samplers)."""
+    import ctypes as C
+    cfgs = c5_configs()
+    gens = [ug.UpcGenerator(c) for c in cfgs]
+    scan = ug.Scan(gens)
+    setup_first = scan.run()
+    for _ in range(args.warmup):
+        scan.run()
+    torch.cuda.synchronize()
+    ms = [scan.run() for _ in range(args.steps)]
+    cells = sum(g.grid()["nm"] * g.grid()["ny"] for g in gens)
+    ms_step = float(np.mean(ms))
+    nev = args.events if args.events is not None else EVENTS["c5"]
+    per = nev // len(gens)
+    buf = torch.empty(max(per, 1) * 48, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for g in gens:
+        r = C.c_int64()
+        ug._check(g._L.upcg_generate_events_device(g._h, per, C.c_void_p(buf.data_ptr()), None,
+                                                   C.byref(r)))
+    torch.cuda.synchronize()
+    t_ev = time.perf_counter() - t0
+    info = scan.info()
+    print(json.dumps({
+        "metric": METRIC, "value": cells / (ms_step * 1e-3), "unit": "cells/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+bf16x3",
+        "data": "synthetic (the workload is a parameter set)",
+        "config": {"workload": f"c5: {len(gens)} ALP configurations, {cells} (m,y) cells, one "
+                               f"captured scan per step; {per * len(gens)} events",
+                   "rows": info["rows"], "items": info["items"], "shape": info["shape"],
+                   "setup_and_first_run_ms": info["setup_ms"] + setup_first},
+        "events_per_s": per * len(gens) / t_ev, "events_wall_s": t_ev,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c5"])
     ap.add_argument("--events", type=int, default=None)
     ap.add_argument("--ref-rows", type=int, default=None)
     ap.add_argument("--plain-steps", type=int, default=None)
@@ -196,6 +253,10 @@ def main():
     import upcgen_gb300 as ug
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.workload == "c5":
+        if rank == 0:
+            run_scan(args, ug, torch)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

@@ -297,7 +297,8 @@ struct upcg_generator {
   DBuf<int> mbinlut;  // getBinY of int(nm (m - mmin)), see EventParams
   DBuf<uint64_t> cdf2fx, cdfzfx;  // fixed-point CDF copies (EventParams)
   int mbinlut_n = 0;
-  int64_t contract_rows = 0;  // rows of the last fast-form contraction  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
+  int64_t contract_rows = 0;  // rows of the last fast-form contraction
+  int fast_nrep = 0;          // rapidity bins per m-row the fast form computes (frep), 0: all  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
   std::vector<double> bu_host;
   int bu_nt = 0;
   // side streams of the table set-up and their fork / join events
@@ -1204,6 +1205,7 @@ int upcg_generator::build_lumi() {
     row_hi = (r1 - r0) * n_rep;
   }
   contract_rows = fast ? (int64_t)(row_hi - row_lo) : 0;
+  fast_nrep = use_map ? n_rep : 0;
   for (int c0 = row_lo; c0 < row_hi; c0 += chunk) {
     const int nc = std::min(chunk, row_hi - c0);
     int b = 0;
@@ -1645,9 +1647,10 @@ int upcg_generator::enqueue_scan_front(upcg_scan& sc, int ci) {
   FastFluxTables ft = ftab_last;
   CK(build_flux_tables(p, &ft, fqn.p, fwn.p, nqn_last, fH.p, fJ.p, fpartq.p, s, 0));
   const size_t r0 = (size_t)sc.row0[ci];
-  CK(launch_fast_project(p, fu0, fh, P, 0, nm * ny, sc.rows[ci], flnm2.p, 0.0, nullptr, &ft,
+  const int nrows = nm * (fast_nrep > 0 ? fast_nrep : ny);
+  CK(launch_fast_project(p, fu0, fh, P, 0, nrows, sc.rows[ci], flnm2.p, 0.0, nullptr, &ft,
                          fsides.p, sc.ah.p + r0 * P, sc.al.p + r0 * P, sc.a2.p + r0 * P,
-                         sc.far.p + 2 * r0, s));
+                         sc.far.p + 2 * r0, s, fast_nrep > 0 ? frep.p : nullptr, fast_nrep, 0));
   cap = false;
   return UPCG_OK;
 }
@@ -1657,8 +1660,10 @@ int upcg_generator::enqueue_scan_back(upcg_scan& sc, int ci) {
   const LumiParams p = lumi_params();
   const int ntiles = sc.P / (sc.shape == 0 ? 256 : 128);
   const size_t r0 = (size_t)sc.row0[ci];
-  CK(launch_fast_finish(p, 0, nm * ny, ntiles, 0.0, sc.part.p + r0 * ntiles, sc.far.p + 2 * r0,
-                        lumi.p, s, sc.fc.p + 2 * ci));
+  const int nrows = nm * (fast_nrep > 0 ? fast_nrep : ny);
+  CK(launch_fast_finish(p, 0, nrows, ntiles, 0.0, sc.part.p + r0 * ntiles, sc.far.p + 2 * r0,
+                        lumi.p, s, sc.fc.p + 2 * ci, fast_nrep > 0 ? frep.p : nullptr,
+                        fast_nrep > 0 ? frep.p + fast_nrep : nullptr, fast_nrep, 0));
   lumi_ready = true;
   cap = true;
   const int rc = build_xsec();
@@ -2542,7 +2547,8 @@ int scan_setup(upcg_scan* sc) {
     int rc = upcg_init(g);
     if (rc) return rc;
     if (g->usePolarizedCS) return fail(UPCG_ERR_PROCESS, "scan: polarized configuration %d", i);
-    const int ncell = g->nm * g->ny;
+    // its rows: one cell of each mirror-rapidity pair (the map upcg_init made)
+    const int ncell = g->nm * (g->fast_nrep > 0 ? g->fast_nrep : g->ny);
     CK(g->fsides.ensure((2 * (size_t)ncell * fast_side_bytes() + 7) / 8));
     sc->row0[i] = (int)rows_total;
     sc->rows[i] = (ncell + 127) / 128 * 128;
@@ -2588,7 +2594,8 @@ int scan_setup(upcg_scan* sc) {
   const int tbn = sc->shape == 0 ? 256 : 128;
   std::vector<int4> items;
   for (int i = 0; i < n; ++i) {
-    const int ncell = sc->gens[i]->nm * sc->gens[i]->ny;
+    const upcg_generator* g = sc->gens[i];
+    const int ncell = g->nm * (g->fast_nrep > 0 ? g->fast_nrep : g->ny);
     for (int mt = 0; mt < sc->rows[i] / 128; ++mt)
       for (int nt = 0; nt < P / tbn; ++nt)
         items.push_back(make_int4(sc->row0[i] / 128 + mt, nt, i, std::min(128, ncell - mt * 128)));
