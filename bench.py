@@ -237,7 +237,7 @@ def main():
     ap.add_argument("--events", type=int, default=None)
     ap.add_argument("--ref-rows", type=int, default=None)
     ap.add_argument("--plain-steps", type=int, default=None)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
 

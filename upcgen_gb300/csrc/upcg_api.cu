@@ -297,6 +297,8 @@ struct upcg_generator {
   DBuf<int> mbinlut;  // getBinY of int(nm (m - mmin)), see EventParams
   DBuf<uint64_t> cdf2fx, cdfzfx;  // fixed-point CDF copies (EventParams)
   int mbinlut_n = 0;
+  std::vector<int> mbinlut_host;  // its host copy and (lo, hi) edges
+  double mbinlut_key[2] = {0., 0.};
   int64_t contract_rows = 0;  // rows of the last fast-form contraction
   int fast_nrep = 0;          // rapidity bins per m-row the fast form computes (frep), 0: all  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
   std::vector<double> bu_host;
@@ -330,6 +332,8 @@ struct upcg_generator {
   DBuf<uint16_t> fgh, fgl, fah, fal;  // fast form: bf16 hi/lo of G and of the projections
   DBuf<float> fa2, fpart;
   DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq, fsides, ffc;
+  DBuf<double> fk01;        // ln K0 + x, ln K1 + x on the K table's x grid (any gamma)
+  bool fk01_ready = false;
   DBuf<float> fs32, fq32;
   DBuf<float4> fgaa32, fbrk32, ff32;
   // grid form: G, flux matrix, T = N G (bf16 hi/lo), Lg, row sums and tails
@@ -381,7 +385,21 @@ struct upcg_generator {
     if (!own) cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking);
     return own;
   }
-  void invalidate() { tables_ready = lumi_ready = xsec_ready = false; }
+  void invalidate() {
+    tables_ready = lumi_ready = xsec_ready = false;
+    up_cache.clear();
+  }
+  // Small host-computed tables uploaded at every init (grids, node sets, the
+  // breakup energy table, work lists): skipped when the bytes for the same
+  // device buffer are unchanged.  A buffer only moves when it must grow, and
+  // then its new contents are larger, so a size match means the same buffer.
+  std::map<const void*, std::vector<char>> up_cache;
+  cudaError_t upload(void* dst, const void* src, size_t n, cudaStream_t ss) {
+    std::vector<char>& c = up_cache[dst];
+    if (!cap && c.size() == n && std::memcmp(c.data(), src, n) == 0) return cudaSuccess;
+    c.assign(static_cast<const char*>(src), static_cast<const char*>(src) + n);
+    return mcpy(dst, src, n, cudaMemcpyHostToDevice, ss);
+  }
 
   int set_param(const std::string& k, const std::string& v);
   int setup_process();
@@ -737,7 +755,9 @@ int upcg_generator::build_tables() {
     // the point-flux table on the main stream, after the G_AA chain
     CK(fk1.ensure(flux_table_ktab_n()));
     CK(fs32.ensure(flux_table_ktab_n()));
-    CK(launch_ktab(g1, fk1.p, fs32.p, s));
+    CK(fk01.ensure(2 * (size_t)flux_table_ktab_n()));
+    CK(launch_ktab(g1, fk1.p, fs32.p, s, fk01.p, fk01_ready ? 1 : 0));
+    fk01_ready = true;
     CK(cudaEventRecord(ev_ft[0], side[0]));
     const int frc = setup_flux_tables(side[0], 0);
     if (frc) return frc;
@@ -750,9 +770,8 @@ int upcg_generator::build_tables() {
   CK(bu_tab.ensure(4 * kBreakupTabMax));
   CK(ntab.ensure(1));
   if (!cap) {  // a captured replay reuses the table uploaded by the set-up run
-    CK(mcpy(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double),
-                       cudaMemcpyHostToDevice, side[1]));
-    CK(mcpy(ntab.p, &bu_nt, sizeof(int), cudaMemcpyHostToDevice, side[1]));
+    CK(upload(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double), side[1]));
+    CK(upload(ntab.p, &bu_nt, sizeof(int), side[1]));
   }
   const double dbb = (1000. - 1e-6) / 1000000;
   brk_n = (int)((20. - 1e-6) / dbb) + 257;
@@ -763,7 +782,9 @@ int upcg_generator::build_tables() {
     CK(cudaMemcpyAsync(brk_coef.p, brk_donor->brk_coef.p, (size_t)(brk_n - 1) * sizeof(double4),
                        cudaMemcpyDeviceToDevice, side[1]));
   } else if (breakupMode > 1) {
-    // the fast form (methods 1, 4; budget 1e-4) takes the FP32 sums (~1e-6)
+    // the fast form (methods 1, 4; budget 1e-4) takes the FP32 sums (~1e-6);
+    // the reference's sum steps where an energy crosses omax(b), so every
+    // knot is summed (an interpolated table smears those steps to 1.5e-5)
     const int brk_fp32 = (lumiMethod == 1 || lumiMethod == 4) ? 1 : 0;
     CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
                              1e-6, dbb, brk_y.p, side[1], brk_fp32));
@@ -1003,8 +1024,8 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab) {
     CK(fq32.ensure((size_t)ftab.nw * ftab.nb));
     CK(fH.ensure((size_t)ftab.nw * nqn));
     CK(fJ.ensure((size_t)nqn * ftab.nb));
-    CK(mcpy(fqn.p, qn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, ss));
-    CK(mcpy(fwn.p, wn.data(), nqn * sizeof(double), cudaMemcpyHostToDevice, ss));
+    CK(upload(fqn.p, qn.data(), nqn * sizeof(double), ss));
+    CK(upload(fwn.p, wn.data(), nqn * sizeof(double), ss));
     ftab.qt = fq.p;
     ftab.qt32 = fq32.p;
   }
@@ -1111,7 +1132,7 @@ int upcg_generator::build_lumi() {
     }
   }
   CK(mirror.ensure(ny));
-  CK(mcpy(mirror.p, mir.data(), ny * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(upload(mirror.p, mir.data(), ny * sizeof(int), s));
   LumiParams p = lumi_params();
   p.mirror = mirror.p;
   // 1: fast form (flux tables + tensor-core contraction); 2: the same
@@ -1185,7 +1206,7 @@ int upcg_generator::build_lumi() {
     std::vector<double> lnm2(nm);
     for (int im = 0; im < nm; ++im) lnm2[im] = std::log((p.mmin + p.dm * im) / 2.);
     CK(flnm2.ensure(nm));
-    CK(mcpy(flnm2.p, lnm2.data(), nm * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(upload(flnm2.p, lnm2.data(), nm * sizeof(double), s));
     spans.push_back({4, {b, mark()}});
   }
   // the fast form on table fluxes computes one cell of each pair of mirror
@@ -1200,7 +1221,7 @@ int upcg_generator::build_lumi() {
     n_rep = (int)rm.size();
     for (int j = 0; j < n_rep; ++j) rm.push_back(mir[rm[j]]);
     CK(frep.ensure(2 * (size_t)n_rep));
-    CK(mcpy(frep.p, rm.data(), rm.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(upload(frep.p, rm.data(), rm.size() * sizeof(int), s));
     row_lo = 0;
     row_hi = (r1 - r0) * n_rep;
   }
@@ -1253,7 +1274,7 @@ int upcg_generator::build_lumi() {
         for (int nt = 0; nt < P / tbn; ++nt)
           items.push_back(make_int4(mt, nt, 0, std::min(128, nc - mt * 128)));
       CK(fitems.ensure(items.size()));
-      CK(mcpy(fitems.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+      CK(upload(fitems.p, items.data(), items.size() * sizeof(int4), s));
       b = mark();
       CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(),
                               fa2.p, fpart.p, ferr.p, shape, grid, s));
@@ -1393,10 +1414,14 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss) {
     const double nmax = std::floor(nm * (hi - lo)) + 2;
     mbinlut_n = nmax < (double)(1 << 22) ? (int)nmax : 0;
     if (mbinlut_n > 0 && !cap) {  // a captured replay reuses the set-up run's table
-      std::vector<int> lut((size_t)mbinlut_n);
-      for (int n = 0; n < mbinlut_n; ++n) lut[n] = (int)((double)n / (hi - lo));
+      if ((int)mbinlut_host.size() != mbinlut_n || mbinlut_key[0] != lo || mbinlut_key[1] != hi) {
+        mbinlut_host.resize((size_t)mbinlut_n);
+        for (int n = 0; n < mbinlut_n; ++n) mbinlut_host[n] = (int)((double)n / (hi - lo));
+        mbinlut_key[0] = lo;
+        mbinlut_key[1] = hi;
+      }
       CK(mbinlut.ensure(mbinlut_n));
-      CK(mcpy(mbinlut.p, lut.data(), (size_t)mbinlut_n * sizeof(int), cudaMemcpyHostToDevice, ss));
+      CK(upload(mbinlut.p, mbinlut_host.data(), (size_t)mbinlut_n * sizeof(int), ss));
     }
   }
   if (isVM) {

@@ -388,6 +388,28 @@ __global__ void k_ktab(double g, double* __restrict__ t1, float* __restrict__ t3
   t32[i] = (float)v;
 }
 
+// The same table from cached Bessel logs: lk = ln K + x on the fixed x grid
+// (independent of g), S = 2 lk1 + ln(1 + e^{2 (lk0 - lk1)} / g^2).
+__global__ void k_k01_logs(double2* __restrict__ lk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kKTabN) return;
+  const double h = (kKTabU1 - kKTabU0) / (kKTabN - 1);
+  const double x = exp(kKTabU0 + i * h);
+  double K0, K1;
+  bessel_k01(x, K0, K1);
+  lk[i] = make_double2(log(K0) + x, log(K1) + x);
+}
+
+__global__ void k_ktab_logs(double g, const double2* __restrict__ lk, double* __restrict__ t1,
+                            float* __restrict__ t32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kKTabN) return;
+  const double2 l = lk[i];
+  const double v = 2. * l.y + log1p(exp(2. * (l.x - l.y)) / (g * g));
+  t1[i] = v;
+  t32[i] = (float)v;
+}
+
 // Form-factor flux amplitude Q(w, b) = int_0^10 q^2 F(q^2 + w^2/g^2)/(q^2 + w^2/g^2)
 // J1(b q / hc) dq (the integrand of src/UpcCrossSection.cpp:181-191, clamp at
 // Q2max - dQ2 included): composite Gauss-Legendre on q in [0, kQNodeMax] as
@@ -1254,9 +1276,20 @@ size_t fast_side_bytes() { return sizeof(SideC); }
 
 int flux_table_part_doubles(int nw, int nb) { return 8 * nw * nb + nb; }  // slices + tail
 
-cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream) {
+cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream, void* d_lk,
+                        int lk_ready) {
+  if (!d_lk) {
+    note_launch();
+    k_ktab<<<(kKTabN + 255) / 256, 256, 0, stream>>>(g1, st, st32);
+    return cudaGetLastError();
+  }
+  double2* lk = static_cast<double2*>(d_lk);
+  if (!lk_ready) {
+    note_launch();
+    k_k01_logs<<<(kKTabN + 255) / 256, 256, 0, stream>>>(lk);
+  }
   note_launch();
-  k_ktab<<<(kKTabN + 255) / 256, 256, 0, stream>>>(g1, st, st32);
+  k_ktab_logs<<<(kKTabN + 255) / 256, 256, 0, stream>>>(g1, lk, st, st32);
   return cudaGetLastError();
 }
 

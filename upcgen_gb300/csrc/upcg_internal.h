@@ -87,6 +87,7 @@ cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaCo
 // calcBreakupProb's energy / cross-section table (host); returns its length
 int breakup_energy_table(double gammatarg, double* ee, double* se);
 // d_tab = [ee | se | ln ee | 1/ee], each kBreakupTabMax long, nt entries used
+// fp32: the fast form's table, FP32 sums (~1e-6 of the FP64 ones)
 cudaError_t launch_breakup_values(const double* d_tab, int nt, double gammatarg, double omaxx,
                                   double zcon, int mode, int n, double x0, double h,
                                   double* d_out, cudaStream_t st,
@@ -152,8 +153,11 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
                               int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st,
                               int w_lo = 0,
                               int with_ktab = 1);
-// the point-flux table S(ln x) of the fast form (k_ktab) alone
-cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream);
+// the point-flux table S(ln x) of the fast form alone; with d_lk (2 * N
+// doubles, flux_table_ktab_n() points) from cached Bessel logs, computed
+// there first unless lk_ready
+cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream,
+                        void* d_lk = nullptr, int lk_ready = 0);
 // lnm2[im] = ln(m_im / 2); c_far = P(20 fm) sum_k w_k, the survival kernel
 // wherever every azimuth has b >= 20 fm
 // rep_y (optional, n_rep_y entries): rows map to cells (m0 + r / n_rep_y,
