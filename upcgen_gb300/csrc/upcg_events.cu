@@ -429,7 +429,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
 
 constexpr int kTile = 256;
 
-__global__ void __launch_bounds__(kTile) k_events_flags(EventParams e, const double* __restrict__ cdf2,
+__global__ void __launch_bounds__(kTile, 5) k_events_flags(EventParams e, const double* __restrict__ cdf2,
                                                         const double* __restrict__ cdfz,
                                                         const float* __restrict__ pttab,
                                                         uint64_t cand0, int64_t ncand,
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(kTile) k_events_flags(EventParams e, const dou
   if (threadIdx.x == 0) tile_count[blockIdx.x] = cnt;
 }
 
-__global__ void __launch_bounds__(kTile) k_events_write(EventParams e, const double* __restrict__ cdf2,
+__global__ void __launch_bounds__(kTile, 5) k_events_write(EventParams e, const double* __restrict__ cdf2,
                                                         const double* __restrict__ cdfz,
                                                         const float* __restrict__ pttab,
                                                         uint64_t cand0, int64_t ncand,
@@ -505,29 +505,57 @@ __global__ void __launch_bounds__(kTile) k_events_write(EventParams e, const dou
   if (mbin) mbin[slot] = c.mbin;
 }
 
-// Exclusive scan of the tile counts (one CTA; tiles per chunk <= 2^20) and the total.
-__global__ void k_scan_tiles(const int* __restrict__ cnt, int64_t* __restrict__ off, int n,
-                             int64_t* __restrict__ total) {
-  __shared__ int64_t red[1024];
-  const int t = threadIdx.x;
-  const int chunk = (n + 1023) / 1024;
-  const int lo = t * chunk, hi = min(lo + chunk, n);
-  int64_t s = 0;
-  for (int i = lo; i < hi; ++i) s += cnt[i];
-  red[t] = s;
-  __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    const int64_t add = t >= o ? red[t - o] : 0;
+// Exclusive scan of the tile counts (one CTA; tiles per chunk <= 2^20) and the
+// total: 8192 counts per round, loaded coalesced into shared memory; each
+// thread sums 8 consecutive ones, a warp-shuffle scan and a scan of the 32
+// warp totals give the thread's offset, and a carry runs across rounds.
+constexpr int kScanThreads = 1024, kScanPer = 8;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* __restrict__ cnt,
+                                                            int64_t* __restrict__ off, int n,
+                                                            int64_t* __restrict__ total) {
+  __shared__ int s_cnt[kScanThreads * kScanPer];
+  __shared__ int64_t s_warp[kScanThreads / 32];
+  __shared__ int64_t s_carry;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) s_carry = 0;
+  for (int base = 0; base < n; base += kScanThreads * kScanPer) {
+    for (int j = t; j < kScanThreads * kScanPer; j += kScanThreads)
+      s_cnt[j] = base + j < n ? __ldg(cnt + base + j) : 0;
     __syncthreads();
-    red[t] += add;
+    int64_t mine = 0;
+#pragma unroll
+    for (int i = 0; i < kScanPer; ++i) mine += s_cnt[t * kScanPer + i];
+    int64_t inc = mine;  // inclusive scan within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t v = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += v;
+    }
+    if (lane == 31) s_warp[w] = inc;
+    __syncthreads();
+    if (w == 0) {  // scan of the warp totals
+      int64_t x = s_warp[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t v = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += v;
+      }
+      s_warp[lane] = x;  // inclusive
+    }
+    __syncthreads();
+    int64_t run = s_carry + (w > 0 ? s_warp[w - 1] : 0) + inc - mine;
+#pragma unroll
+    for (int i = 0; i < kScanPer; ++i) {
+      const int j = base + t * kScanPer + i;
+      if (j < n) off[j] = run;
+      run += s_cnt[t * kScanPer + i];
+    }
+    __syncthreads();
+    if (t == 0) s_carry += s_warp[31];
     __syncthreads();
   }
-  int64_t run = t > 0 ? red[t - 1] : 0;
-  for (int i = lo; i < hi; ++i) {
-    off[i] = run;
-    run += cnt[i];
-  }
-  if (t == 1023) *total = red[1023];
+  if (t == 0) *total = s_carry;
 }
 
 // Photon pT spectra: dN/dpT ~ F(pT^2 + e)^2 pT^3 / (pT^2 + e)^2 on 5000 bins of
@@ -746,7 +774,7 @@ cudaError_t launch_events_write(const EventParams& e, const double* d_cdf2, cons
 cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
                               cudaStream_t st) {
   note_launch();
-  k_scan_tiles<<<1, 1024, 0, st>>>(d_count, d_off, n, d_total);
+  k_scan_tiles<<<1, kScanThreads, 0, st>>>(d_count, d_off, n, d_total);
   return cudaGetLastError();
 }
 
