@@ -95,6 +95,31 @@ def test_fast_form_factor_flux(ug, oracle_mod):
     assert rel.max() < FAST_TOL and rtot < FAST_TOL
 
 
+@pytest.mark.parametrize("flux_point", [1, 0])
+def test_fast_polarized(ug, oracle_mod, flux_point):
+    """USE_POLARIZED_CS in the fast form: the scalar and pseudoscalar survival
+    kernels (b^2 = b1^2 + b2^2 - 2 b1 b2 cos phi, weights cos^2 / sin^2 phi;
+    src/UpcCrossSection.cpp:274-335) in two contractions of the same operands;
+    both tables within 1e-4 of the (converged) oracle."""
+    p = dict(C1, PROC_ID=13, BREAKUP_MODE=2, USE_POLARIZED_CS=1, FLUX_POINT=flux_point,
+             BINS_M=21, BINS_Y=25)
+    g = ug.UpcGenerator(p)
+    g.setLumiMethod("fast")
+    g.init()
+    s, ps = g.lumiTable(polarized=True)
+    o = oracle_mod.Oracle(dict(p, ORACLE_FLUX_EPS=1e-10) if not flux_point else p,
+                          threads=os.cpu_count())
+    o.init_tables()
+    rs, rp = o.lumi_table(polarized=True)
+    for a, b in ((s, rs), (ps, rp)):
+        big = np.abs(b) >= 1e-5 * np.abs(b).max()
+        assert (np.abs(a - b)[big] / np.abs(b[big])).max() < FAST_TOL
+    # sigma and the scalar / pseudoscalar ratio of the fold
+    _, tot = g.nucCSYM()
+    _, rtot, _ = o.nuc_cs_ym(rs, rp)
+    assert abs(tot / rtot - 1) < FAST_TOL
+
+
 def test_fast_light_nucleus(ug, oracle_mod):
     p = dict(C1, PROC_ID=51, ALP_MASS=1, ALP_WIDTH=0.01, NUCLEUS_Z=8, NUCLEUS_A=16,
              WS_R=2.608, WS_A=0.513, SQRTS=5360, BREAKUP_MODE=3, BINS_M=21, BINS_Y=25)

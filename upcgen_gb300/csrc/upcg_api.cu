@@ -333,6 +333,9 @@ struct upcg_generator {
   DBuf<float> fa2, fpart;
   DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq, fsides, ffc;
   DBuf<double> fk01;        // ln K0 + x, ln K1 + x on the K table's x grid (any gamma)
+  DBuf<double> ffc2;        // polarized: the pseudoscalar far constants
+  DBuf<uint16_t> fgh2, fgl2;  // polarized: the pseudoscalar survival kernel (bf16 hi/lo)
+  DBuf<float> fpart2;
   bool fk01_ready = false;
   DBuf<float> fs32, fq32;
   DBuf<float4> fgaa32, fbrk32, ff32;
@@ -1154,8 +1157,6 @@ int upcg_generator::build_lumi() {
   CK(cudaMemsetAsync(stats.p, 0, sizeof(QagsStats), s));
   if (lumiMethod == 4 && !surrogate)
     return fail(UPCG_ERR_STATE, "luminosity method 4 needs a surrogate (upcg_set_flux_surrogate)");
-  if (fast && usePolarizedCS)
-    return fail(UPCG_ERR_ARG, "the fast form covers the unpolarized luminosity");
   const int P = fast_grid_points();
   const double fu0 = std::log(0.1), fh = (std::log(256.) - std::log(0.1)) / (P - 1);
   const int chunk_pad = (chunk + 127) / 128 * 128;
@@ -1189,10 +1190,29 @@ int upcg_generator::build_lumi() {
     // the breakup probability at 20 fm (the survival kernel beyond b = 20 fm)
     // and c_far, on the device: no host round trip between the phases
     CK(ffc.ensure(2));
-    CK(launch_far_consts(p, breakupMode != 1, ffc.p, s));
     CK(fgaa32.ensure(p.gaa.n));
     CK(fbrk32.ensure(breakupMode != 1 ? p.brk.n : 1));
-    CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p));
+    if (!usePolarizedCS) {
+      CK(launch_far_consts(p, breakupMode != 1, ffc.p, s));
+      CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p));
+    } else {
+      // calcTwoPhotonLumiPol (src/UpcCrossSection.cpp:274-335): b^2 = b1^2 + b2^2
+      // - 2 b1 b2 cos(phi), weights w cos^2(phi) (scalar) and w sin^2(phi)
+      // (pseudoscalar): two survival kernels and two far constants
+      LumiParams ps = p, pp = p;
+      for (int q = 0; q < 5; ++q) {
+        ps.cosk[q] = pp.cosk[q] = -p.cosk[q];
+        ps.wk[q] = p.wk[q] * p.cosk[q] * p.cosk[q];
+        pp.wk[q] = p.wk[q] * p.sink[q] * p.sink[q];
+      }
+      CK(ffc2.ensure(2));
+      CK(fgh2.ensure((size_t)P * P));
+      CK(fgl2.ensure((size_t)P * P));
+      CK(launch_far_consts(ps, breakupMode != 1, ffc.p, s));
+      CK(launch_far_consts(pp, breakupMode != 1, ffc2.p, s));
+      CK(launch_fast_G(ps, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p));
+      CK(launch_fast_G(pp, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh2.p, fgl2.p, s, ffc2.p));
+    }
     // the flux tables, unless build_tables already enqueued them beside the
     // breakup and G_AA chains
     if (!ftab_early) {
@@ -1278,10 +1298,19 @@ int upcg_generator::build_lumi() {
       b = mark();
       CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(),
                               fa2.p, fpart.p, ferr.p, shape, grid, s));
+      if (usePolarizedCS) {  // the same operands against the pseudoscalar kernel
+        CK(fpart2.ensure(fpart.n));
+        CK(launch_contract_pers(fah.p, fal.p, fgh2.p, fgl2.p, 1, ncp, P, fitems.p,
+                                (int)items.size(), fa2.p, fpart2.p, ferr.p, shape, grid, s));
+      }
       spans.push_back({3, {b, mark()}});
       CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s, ffc.p,
                             use_map ? frep.p : nullptr, use_map ? frep.p + n_rep : nullptr, n_rep,
                             r0));
+      if (usePolarizedCS)
+        CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart2.p, ffar.p, lumi2.p, s, ffc2.p,
+                              use_map ? frep.p : nullptr, use_map ? frep.p + n_rep : nullptr,
+                              n_rep, r0));
     }
   }
   const int w1 = mark();
