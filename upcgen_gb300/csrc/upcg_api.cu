@@ -329,6 +329,8 @@ struct upcg_generator {
   DBuf<uint32_t> mask;
   DBuf<int64_t> tile_off, total;
   DBuf<EventRecord> evbuf;
+  DBuf<EventRecord> evstage;  // pass 1's accepted records, 256 slots per candidate tile
+  DBuf<int32_t> evstage_mbin;
   DBuf<uint16_t> fgh, fgl, fah, fal;  // fast form: bf16 hi/lo of G and of the projections
   DBuf<float> fa2, fpart;
   DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq, fsides, ffc;
@@ -1608,7 +1610,9 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     return vm_check();
   }
   int64_t done = 0;
-  const int64_t kMaxChunk = (int64_t)1 << 28;
+  // pass 1 stages the accepted records (48 bytes per candidate slot), so a
+  // chunk holds at most 2^26 candidates: 3.2 GB of staging
+  const int64_t kMaxChunk = (int64_t)1 << 26;
   // the reference's loop never ends when the cuts reject everything
   // (src/UpcGenerator.cpp:840-889); this one gives up after 2^34 candidates
   // in a row without an accepted event
@@ -1623,10 +1627,13 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     CK(tile_count.ensure(tiles));
     CK(tile_off.ensure(tiles + 1));
     CK(total.ensure(2));
-    CK(launch_events_flags(e, cdf2.p, zc, ptcdf.p, next_cand, nc, mask.p, tile_count.p, s));
+    CK(evstage.ensure((size_t)nc));
+    if (mbin) CK(evstage_mbin.ensure((size_t)nc));
+    CK(launch_events_flags(e, cdf2.p, zc, ptcdf.p, next_cand, nc, mask.p, tile_count.p, s,
+                           evstage.p, mbin ? evstage_mbin.p : nullptr));
     CK(launch_scan_tiles(tile_count.p, tile_off.p, tiles, total.p, s));
-    CK(launch_events_write(e, cdf2.p, zc, ptcdf.p, next_cand, nc, mask.p, tile_off.p, done, n,
-                           out, mbin, s));
+    CK(launch_events_copy(evstage.p, mbin ? evstage_mbin.p : nullptr, tile_count.p, tile_off.p,
+                          tiles, done, n, out, mbin, s));
     int64_t acc = 0;
     CK(mcpy(&acc, total.p, sizeof acc, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));

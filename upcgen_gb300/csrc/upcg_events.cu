@@ -429,28 +429,82 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
 
 constexpr int kTile = 256;
 
-__global__ void __launch_bounds__(kTile, 5) k_events_flags(EventParams e, const double* __restrict__ cdf2,
+__device__ __forceinline__ EventRecord to_record(const Cand& c) {
+  EventRecord rec;
+  rec.m = (float)c.m;
+  rec.y = (float)c.y;
+  rec.z = (float)c.z;
+  rec.sign = c.sign;
+  for (int q = 0; q < 4; ++q) {
+    rec.p0[q] = c.p0[q];
+    rec.p1[q] = c.p1[q];
+  }
+  return rec;
+}
+
+// Pass 1: every candidate of a 256-candidate tile, its accept bit and the
+// tile's count; with stage, the accepted records also go to the tile's 256
+// staging slots in candidate order (pass 2 then copies instead of
+// regenerating).
+__global__ void __launch_bounds__(kTile, 4) k_events_flags(EventParams e, const double* __restrict__ cdf2,
                                                         const double* __restrict__ cdfz,
                                                         const float* __restrict__ pttab,
                                                         uint64_t cand0, int64_t ncand,
                                                         uint32_t* __restrict__ mask,
-                                                        int* __restrict__ tile_count) {
-  __shared__ int cnt;
-  if (threadIdx.x == 0) cnt = 0;
-  __syncthreads();
+                                                        int* __restrict__ tile_count,
+                                                        EventRecord* __restrict__ stage,
+                                                        int32_t* __restrict__ stage_mbin) {
+  __shared__ int s_pre[kTile / 32 + 1];
   const int64_t local = (int64_t)blockIdx.x * kTile + threadIdx.x;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   bool ok = false;
-  if (local < ncand) {
-    Cand c;
-    ok = gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)local, c);
-  }
+  Cand c;
+  if (local < ncand) ok = gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)local, c);
   const unsigned bal = __ballot_sync(0xffffffffu, ok);
-  if ((threadIdx.x & 31) == 0) {
-    mask[(size_t)blockIdx.x * (kTile / 32) + (threadIdx.x >> 5)] = bal;
-    atomicAdd(&cnt, __popc(bal));
+  if (lane == 0) {
+    mask[(size_t)blockIdx.x * (kTile / 32) + w] = bal;
+    s_pre[w + 1] = __popc(bal);
   }
   __syncthreads();
-  if (threadIdx.x == 0) tile_count[blockIdx.x] = cnt;
+  if (threadIdx.x == 0) {
+    s_pre[0] = 0;
+    for (int q = 0; q < kTile / 32; ++q) s_pre[q + 1] += s_pre[q];
+    tile_count[blockIdx.x] = s_pre[kTile / 32];
+  }
+  __syncthreads();
+  if (stage && ok) {
+    const int rank = s_pre[w] + __popc(bal & ((1u << lane) - 1u));
+    const size_t slot = (size_t)blockIdx.x * kTile + rank;
+    stage[slot] = to_record(c);
+    if (stage_mbin) stage_mbin[slot] = c.mbin;
+  }
+}
+
+// Pass 2 from the staging slots: tile t's accepted records to their output
+// slots out_base + tile_off[t] + r (below nmax); 3 float4 per record.
+__global__ void k_events_copy(const EventRecord* __restrict__ stage,
+                              const int32_t* __restrict__ stage_mbin,
+                              const int* __restrict__ tile_count,
+                              const int64_t* __restrict__ tile_off, int64_t out_base,
+                              int64_t nmax, EventRecord* __restrict__ out,
+                              int32_t* __restrict__ mbin) {
+  const int tile = blockIdx.x;
+  const int64_t base = out_base + tile_off[tile];
+  if (base >= nmax) return;
+  const int cnt = tile_count[tile];
+  const int64_t lim = nmax - base < cnt ? nmax - base : cnt;
+  if ((reinterpret_cast<uintptr_t>(out) & 15) == 0) {  // 48-byte records: 3 float4 each
+    const float4* src = reinterpret_cast<const float4*>(stage + (size_t)tile * kTile);
+    float4* dst = reinterpret_cast<float4*>(out + base);
+    for (int i = threadIdx.x; i < 3 * lim; i += blockDim.x) dst[i] = __ldg(src + i);
+  } else {
+    const float* src = reinterpret_cast<const float*>(stage + (size_t)tile * kTile);
+    float* dst = reinterpret_cast<float*>(out + base);
+    for (int i = threadIdx.x; i < 12 * lim; i += blockDim.x) dst[i] = __ldg(src + i);
+  }
+  if (mbin)
+    for (int i = threadIdx.x; i < lim; i += blockDim.x)
+      mbin[base + i] = __ldg(stage_mbin + (size_t)tile * kTile + i);
 }
 
 __global__ void __launch_bounds__(kTile, 5) k_events_write(EventParams e, const double* __restrict__ cdf2,
@@ -495,13 +549,7 @@ __global__ void __launch_bounds__(kTile, 5) k_events_write(EventParams e, const 
   if (slot >= nmax) return;
   Cand c;
   gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)local, c);
-  EventRecord rec;
-  rec.m = (float)c.m;
-  rec.y = (float)c.y;
-  rec.z = (float)c.z;
-  rec.sign = c.sign;
-  for (int q = 0; q < 4; ++q) { rec.p0[q] = c.p0[q]; rec.p1[q] = c.p1[q]; }
-  out[slot] = rec;
+  out[slot] = to_record(c);
   if (mbin) mbin[slot] = c.mbin;
 }
 
@@ -750,11 +798,22 @@ cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, flo
 
 cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                                 const float* d_ptcdf, uint64_t cand0, int64_t ncand,
-                                uint32_t* d_mask, int* d_tile_count, cudaStream_t st) {
+                                uint32_t* d_mask, int* d_tile_count, cudaStream_t st,
+                                EventRecord* d_stage, int32_t* d_stage_mbin) {
   const int64_t tiles = (ncand + kTile - 1) / kTile;
   note_launch();
   k_events_flags<<<(unsigned)tiles, kTile, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, ncand,
-                                                   d_mask, d_tile_count);
+                                                   d_mask, d_tile_count, d_stage, d_stage_mbin);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_events_copy(const EventRecord* d_stage, const int32_t* d_stage_mbin,
+                               const int* d_tile_count, const int64_t* d_tile_off, int64_t tiles,
+                               int64_t out_base, int64_t nmax, EventRecord* d_out, int32_t* d_mbin,
+                               cudaStream_t st) {
+  note_launch();
+  k_events_copy<<<(unsigned)tiles, kTile, 0, st>>>(d_stage, d_stage_mbin, d_tile_count, d_tile_off,
+                                                   out_base, nmax, d_out, d_mbin);
   return cudaGetLastError();
 }
 
