@@ -89,7 +89,11 @@ int upcg_set_stream(upcg_generator* g, void* stream);
  * the converged quadrature), 2 = the fast form's contraction on the plain
  * path's node fluxes (diagnostic), 3 = grid form (point flux): fixed
  * 4096-energy x 2048-radius grids, L = N G N^T as two tensor-core products
- * (its own quadrature: the difference to the reference is stated by the tests) */
+ * (its own quadrature: the difference to the reference is stated by the tests),
+ * 4 = the fast form with the form-factor flux rows inside the learned
+ * surrogate's box from the surrogate (upcg_set_flux_surrogate).  With
+ * USE_POLARIZED_CS the fast form (1, 4) builds the scalar and pseudoscalar
+ * tables of calcTwoPhotonLumiPol from the same operands. */
 int upcg_set_lumi_method(upcg_generator* g, int method);
 
 /* ---- initialisation (UpcGenerator::init) ------------------------------ */
@@ -192,6 +196,11 @@ int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t*
                          int64_t* rejected);
 int upcg_generate_events_device(upcg_generator* g, int64_t n, upcg_event* out_device,
                                 int32_t* mbin_device, int64_t* rejected);
+/* Page-locked host memory for event buffers (the caller owns it; free with
+ * upcg_host_free): upcg_generate_events into such a buffer copies at the
+ * link's rate instead of through the driver's pageable staging. */
+int upcg_host_alloc(size_t bytes, void** out);
+int upcg_host_free(void* p);
 /* ---- photonuclear path: coherent vector mesons (PROC_ID 443 J/psi, 100443
  * psi(2S), 553 Upsilon(1S); DECAY_PDG 11, 13 or 2212; SHADOWING 0, the
  * impulse approximation -- the other options need the reference's

@@ -85,3 +85,20 @@ def test_empty_and_bad_path(ug, tmp_path):
     assert path.read_text() == HEAD + TAIL
     with pytest.raises(ug.UpcgError):
         g.writeEvents(tmp_path / "no" / "such" / "dir.hepmc", 10)
+
+
+def test_pinned_out_buffer(ug):
+    """generateEvents into a page-locked array (upcg_host_alloc) gives the
+    events of a pageable one; a short or mistyped out is refused."""
+    g, ref = _pair(ug, dict(C2S, BINS_M=51, BINS_Y=25))
+    n = 20000
+    buf = ug.pinned_array(n + 5, ug.EVENT_DTYPE)
+    ev, rej = g.generateEvents(n, out=buf)
+    ev_ref, rej_ref = ref.generateEvents(n)
+    assert rej == rej_ref and ev.base is not None
+    assert np.array_equal(buf[:n].view(np.uint8), ev_ref.view(np.uint8))
+    with pytest.raises(ValueError):
+        g.generateEvents(n + 6, out=buf)
+    with pytest.raises(ValueError):
+        g.generateEvents(10, out=np.zeros(10, dtype=np.float32))
+    del ev, buf  # frees the page-locked block

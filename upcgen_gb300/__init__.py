@@ -36,6 +36,7 @@ ABI_SYMBOLS = [
     "upcg_flux_form", "upcg_form_factor", "upcg_breakup_prob", "upcg_eval_spline",
     "upcg_two_photon_lumi", "upcg_cs_m", "upcg_generate_events",
     "upcg_generate_events_device", "upcg_generate_event", "upcg_philox",
+    "upcg_host_alloc", "upcg_host_free",
     "upcg_last_timings", "upcg_qags_stats", "upcg_last_error", "upcg_version",
     "upcg_selftest_contract", "upcg_fast_flux_table", "upcg_kernel_launches",
     "upcg_flux_form_device_noalloc", "upcg_copy_bytes", "upcg_particle_pdg",
@@ -93,6 +94,7 @@ def load_library(path=None):
         "upcg_cs_m": [vp, vp, i, vp, sz], "upcg_generate_events": [vp, i64, vp, vp, C.POINTER(i64)],
         "upcg_generate_events_device": [vp, i64, vp, vp, C.POINTER(i64)],
         "upcg_generate_event": [vp, vp, C.POINTER(i)], "upcg_philox": [u64, u64, sz, vp],
+        "upcg_host_alloc": [sz, C.POINTER(vp)], "upcg_host_free": [vp],
         "upcg_last_timings": [vp, dp, sz],
         "upcg_qags_stats": [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)],
         "upcg_last_error": [], "upcg_version": [],
@@ -160,6 +162,32 @@ def copy_bytes():
     a, b = C.c_uint64(), C.c_uint64()
     _check(L.upcg_copy_bytes(C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+class _PinnedBlock:
+    """Page-locked host bytes from upcg_host_alloc, freed with the last view."""
+
+    def __init__(self, nbytes):
+        self._L = load_library()
+        self.ptr = C.c_void_p()
+        _check(self._L.upcg_host_alloc(int(nbytes), C.byref(self.ptr)))
+        self.nbytes = int(nbytes)
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and self.ptr.value:
+            self._L.upcg_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+
+def pinned_array(shape, dtype):
+    """A numpy array in page-locked host memory (e.g. the out= buffer of
+    generateEvents); the memory lives as long as the array or a view of it."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape))
+    blk = _PinnedBlock(max(n * dtype.itemsize, 1))
+    buf = (C.c_char * blk.nbytes).from_address(blk.ptr.value)
+    buf._upcg_block = blk  # keeps the block alive while numpy holds the buffer
+    return np.frombuffer(buf, dtype=dtype, count=n).reshape(shape)
 
 
 def philox(seed, counter0, n):
@@ -475,9 +503,16 @@ class UpcGenerator:
         _check(self._L.upcg_cs_zm_table(self._h, int(flag), _p(out), out.size))
         return out
 
-    def generateEvents(self, n, with_mbin=False):
-        """The accepted-event loop; returns (events, rejected[, mbin])."""
-        out = np.zeros(int(n), dtype=EVENT_DTYPE)
+    def generateEvents(self, n, with_mbin=False, out=None):
+        """The accepted-event loop; returns (events, rejected[, mbin]).  out:
+        a caller's EVENT_DTYPE array of at least n records (pinned_array for
+        the fastest copy); the events are its first n."""
+        if out is None:
+            out = np.zeros(int(n), dtype=EVENT_DTYPE)
+        else:
+            if out.dtype != EVENT_DTYPE or not out.flags.c_contiguous or out.size < int(n):
+                raise ValueError("out must be a C-contiguous EVENT_DTYPE array of at least n records")
+            out = out[:int(n)]
         mb = np.zeros(int(n), dtype=np.int32) if with_mbin else None
         rej = C.c_int64()
         _check(self._L.upcg_generate_events(self._h, int(n), _p(out), _p(mb) if with_mbin else None,

@@ -306,6 +306,8 @@ struct upcg_generator {
   // side streams of the table set-up and their fork / join events
   cudaStream_t side[2] = {nullptr, nullptr};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  // host event output: generation done / slot copied out (side[1] copies)
+  cudaEvent_t ev_gen = nullptr, ev_out[3] = {nullptr, nullptr, nullptr};
   cudaError_t side_streams() {
     for (int i = 0; i < 2; ++i) {
       if (!side[i]) {
@@ -372,6 +374,9 @@ struct upcg_generator {
       if (ev_join[i]) cudaEventDestroy(ev_join[i]);
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_gen) cudaEventDestroy(ev_gen);
+    for (auto e : ev_out)
+      if (e) cudaEventDestroy(e);
     if (ev_static) cudaEventDestroy(ev_static);
     if (hstat) cudaFreeHost(hstat);
     for (auto e : ev_ft)
@@ -2116,19 +2121,61 @@ int upcg_generate_events_device(upcg_generator* g, int64_t n, upcg_event* out_de
   return UPCG_OK;
 }
 
+// Host output in slices of 2^21 events through a ring of 3 device slots: the
+// copy of slice k to the host (on side[1]) overlaps the generation of slice
+// k+1; a slot is reused once its copy has finished.  The slices take the
+// candidate sequence in order, so the events are those of one device call.
 int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t* mbin,
                          int64_t* rejected) {
   if (!g || !out || !rejected || n < 0) return fail(UPCG_ERR_ARG, "bad argument");
   if (n == 0) { *rejected = 0; return UPCG_OK; }
-  CK(g->evbuf.ensure((size_t)n));
-  if (mbin) CK(g->mbinbuf.ensure((size_t)n));
-  int rc = upcg_generate_events_device(g, n, reinterpret_cast<upcg_event*>(g->evbuf.p),
-                                       mbin ? g->mbinbuf.p : nullptr, rejected);
+  if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "upcg_init has not run");
+  const int64_t chunk = std::min<int64_t>(n, (int64_t)1 << 21);
+  const int nslot = n > chunk ? 3 : 1;
+  CK(g->evbuf.ensure((size_t)chunk * nslot));
+  if (mbin) CK(g->mbinbuf.ensure((size_t)chunk * nslot));
+  CK(g->side_streams());
+  if (!g->ev_gen) CK(cudaEventCreateWithFlags(&g->ev_gen, cudaEventDisableTiming));
+  for (auto& e : g->ev_out)
+    if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaStream_t s = g->st(), cs = g->side[1];
+  auto* rec = reinterpret_cast<EventRecord*>(out);
+  int64_t rej = 0;
+  int rc = UPCG_OK;
+  for (int64_t off = 0, k = 0; off < n; off += chunk, ++k) {
+    const int slot = (int)(k % nslot);
+    const int64_t c = std::min(chunk, n - off);
+    if (k >= nslot) CK(cudaStreamWaitEvent(s, g->ev_out[slot], 0));
+    EventRecord* dv = g->evbuf.p + (size_t)slot * chunk;
+    int32_t* dm = mbin ? g->mbinbuf.p + (size_t)slot * chunk : nullptr;
+    int64_t r = 0;
+    rc = g->gen_events_device(c, dv, dm, &r);
+    if (rc) break;
+    rej += r;
+    CK(cudaEventRecord(g->ev_gen, s));
+    CK(cudaStreamWaitEvent(cs, g->ev_gen, 0));
+    CK(mcpy(rec + off, dv, (size_t)c * sizeof(EventRecord), cudaMemcpyDeviceToHost, cs));
+    if (mbin) CK(mcpy(mbin + off, dm, (size_t)c * sizeof(int32_t), cudaMemcpyDeviceToHost, cs));
+    CK(cudaEventRecord(g->ev_out[slot], cs));
+  }
+  CK(cudaStreamSynchronize(cs));
+  CK(cudaStreamSynchronize(s));
   if (rc) return rc;
-  CK(mcpy(out, g->evbuf.p, (size_t)n * sizeof(EventRecord), cudaMemcpyDeviceToHost, g->st()));
-  if (mbin)
-    CK(mcpy(mbin, g->mbinbuf.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, g->st()));
-  CK(cudaStreamSynchronize(g->st()));
+  *rejected = rej;
+  g->fidCS = g->totCS * (double)n / (double)(n + rej);  // src/UpcGenerator.cpp:889
+  return UPCG_OK;
+}
+
+int upcg_host_alloc(size_t bytes, void** out) {
+  if (!out) return fail(UPCG_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (bytes == 0) return UPCG_OK;
+  CK(cudaMallocHost(out, bytes));
+  return UPCG_OK;
+}
+
+int upcg_host_free(void* p) {
+  if (p) CK(cudaFreeHost(p));
   return UPCG_OK;
 }
 
