@@ -298,6 +298,9 @@ struct upcg_generator {
   DBuf<uint64_t> cdf2fx, cdfzfx;  // fixed-point CDF copies (EventParams)
   int mbinlut_n = 0;
   std::vector<int> mbinlut_host;  // its host copy and (lo, hi) edges
+  DBuf<double2> medges;  // per mass bin (mmin + dm im, bin width), EventParams::medges
+  std::vector<double2> medges_host;
+  bool medges_ok = false;
   double mbinlut_key[2] = {0., 0.};
   int64_t contract_rows = 0;  // rows of the last fast-form contraction
   int fast_nrep = 0;          // rapidity bins per m-row the fast form computes (frep), 0: all  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
@@ -619,6 +622,11 @@ EventParams upcg_generator::event_params() const {
   e.pt_lne0 = std::log(kmin * kmin / (gtot * gtot));
   e.pt_dlne = (std::log(kmax * kmax / (gtot * gtot)) - e.pt_lne0) / (e.pt_ne - 1);
   e.pt_width = 6. * kHc / R / 5000;
+  e.f_dy = (float)e.dy; e.f_ymin = (float)e.ymin; e.f_dz = (float)e.dz; e.f_zmin = (float)e.zmin;
+  e.f_minPt = (float)e.minPt; e.f_minEta = (float)e.minEta; e.f_maxEta = (float)e.maxEta;
+  e.f_ptw = (float)e.pt_width;
+  e.nm_d = (double)nm;
+  e.medges = medges.p && medges.n >= (size_t)nm && medges_ok ? medges.p : nullptr;
   e.pt_c0 = (float)(2. * std::log(gtot) + e.pt_lne0);
   e.pt_inv_dlne = (float)(1. / e.pt_dlne);
   int g2n = 1, g2b = 0;
@@ -1458,6 +1466,17 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss) {
       }
       CK(mbinlut.ensure(mbinlut_n));
       CK(upload(mbinlut.p, mbinlut_host.data(), (size_t)mbinlut_n * sizeof(int), ss));
+    }
+    if (!cap) {  // the gsl histogram's mass edges mmin + dm i (src/UpcGenerator.cpp:677-678)
+      const double dmv = (mmax - mmin) / nm;
+      medges_host.resize((size_t)nm);
+      for (int i = 0; i < nm; ++i) {
+        const double a = mmin + dmv * i, b = mmin + dmv * (i + 1);
+        medges_host[i] = make_double2(a, b - a);
+      }
+      CK(medges.ensure((size_t)nm));
+      CK(upload(medges.p, medges_host.data(), (size_t)nm * sizeof(double2), ss));
+      medges_ok = true;
     }
   }
   if (isVM) {

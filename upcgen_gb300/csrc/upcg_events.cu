@@ -170,14 +170,15 @@ __device__ float photon_pt(const EventParams& e, const float* __restrict__ tabs,
   const int ib = cdf_find_from_f(I, e.pt_nbins,
                                  __ldg(e.gpt + (size_t)i * e.gpt_n + (int)(u * (float)e.gpt_n)), u);
   const float lo = __ldg(I + ib), hi = __ldg(I + ib + 1);
-  const float w = (float)e.pt_width;
+  const float w = e.f_ptw;
   float x = ib * w;
   if (hi > lo) x += w * (u - lo) / (hi - lo);
   return x;
 }
 
 struct Cand {
-  double m, y, z;
+  double m;  // FP64 for getBinY; y and z are drawn in FP32 (the record's type)
+  float y, z;
   float sign;
   float p0[4], p1[4];
   int mbin;
@@ -240,7 +241,7 @@ __device__ bool gen_vm(const EventParams& e, const float* __restrict__ pttab, Ca
   const uint4 r4 = philox4x32_10(make_uint4(clo, chi, 4u, 0x55504347u), key);
   const bool target = u53(r4.x, r4.y) < __ldg(e.vm_ratio + yb);
   const double sgn = target ? 1. : -1.;
-  const float m = (float)c.m, y = (float)c.y;
+  const float m = (float)c.m, y = c.y;
   const float ptPhot = photon_pt(e, pttab, logf(0.5f * m) + (float)sgn * y, u24(r2.x), u24(r2.y));
   // pomeron: t = tmin + ptPom^2 with density F(t)^2 on [tmin, end of table]
   const double ePom = c.m / 2. * exp(-sgn * c.y);
@@ -273,10 +274,10 @@ __device__ bool gen_vm(const EventParams& e, const float* __restrict__ pttab, Ca
   const float mt = sqrtf(m * m + ppx * ppx + ppy * ppy);
   const float ppz = mt * sinhf(y), pE = mt * coshf(y);
   // checkKinCuts on the meson (the decay follows the cuts)
-  if (e.doPtCut && sqrtf(ppx * ppx + ppy * ppy) < (float)e.minPt) return false;
+  if (e.doPtCut && sqrtf(ppx * ppx + ppy * ppy) < e.f_minPt) return false;
   if (e.doEtaCut) {
     const float et = eta_f(ppx, ppy, ppz);
-    if (et < (float)e.minEta || et > (float)e.maxEta) return false;
+    if (et < e.f_minEta || et > e.f_maxEta) return false;
   }
   // twoPartDecayVM's angle: at most 32 tries (acceptance above 0.8 per try)
   const float cc = e.dght_law ? 0.605f : 1.f;
@@ -328,14 +329,22 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   // the position inside the bin, (r - c0) / (c1 - c0), in FP32 (the event
   // stores y in FP32); m in FP64, for getBinY
   const float delta = frac_fx(ra - __ldg(e.cdf2fx + k), __ldg(e.cdf2fx + k + 1) - __ldg(e.cdf2fx + k));
-  c.y = (double)fmaf((float)iy + delta, (float)e.dy, (float)e.ymin);
-  const double mlo = e.mmin + e.dm * im, mhi = e.mmin + e.dm * (im + 1);
-  c.m = mlo + rb * (mhi - mlo);
+  c.y = fmaf((float)iy + delta, e.f_dy, e.f_ymin);
+  double mlo, mw;  // the mass bin's lower edge and width
+  if (e.medges) {
+    const double2 me = __ldg(e.medges + im);
+    mlo = me.x;
+    mw = me.y;
+  } else {
+    mlo = e.mmin + e.dm * im;
+    mw = (e.mmin + e.dm * (im + 1)) - mlo;
+  }
+  c.m = mlo + rb * mw;
   (void)cdf2;
   // getBinY (include/UpcSampler.h:130-133), the int() truncating the numerator:
   // int(n / (hi - lo)) of the integer n = int(nm (m - lo)) from a table made
   // on the host with that FP64 division (no division per candidate)
-  const int nnum = (int)(e.nm * (c.m - e.mmin));
+  const int nnum = (int)(e.nm_d * (c.m - e.mmin));
   int mb = (nnum >= 0 && nnum < e.mbin_lut_n) ? __ldg(e.mbin_lut + nnum)
                                               : (int)((double)nnum / (e.medge_hi - e.mmin));
   mb = mb < 0 ? 0 : (mb > e.nm - 1 ? e.nm - 1 : mb);
@@ -347,7 +356,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
     const int iz = cdf_find_from_fx(
         cz, e.nz, __ldg(e.gz + (size_t)mb * e.gz_n + (int)(rz >> (64 - e.gz_bits))), rz);
     const float dl = frac_fx(rz - __ldg(cz + iz), __ldg(cz + iz + 1) - __ldg(cz + iz));
-    c.z = (double)fmaf((float)e.dz, (float)iz + dl, (float)e.zmin);
+    c.z = fmaf(e.f_dz, (float)iz + dl, e.f_zmin);
   } else if (!e.ignoreCSZ) {
     // polarized: the scalar or pseudoscalar z sampler of this mass bin; the
     // reference draws Uniform(0, 1) < polCSRatio[yBin][mBin] (getBinX of y, as getBinY)
@@ -362,13 +371,13 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
     const int iz = cdf_find(cz, e.nz, rz);
     const double z0 = __ldg(cz + iz), z1 = __ldg(cz + iz + 1);
     const float dl = frac_in_bin(rz - z0, z1 - z0);
-    c.z = (double)fmaf((float)e.dz, (float)iz + dl, (float)e.zmin);
+    c.z = fmaf(e.f_dz, (float)iz + dl, e.f_zmin);
   } else {
-    c.z = -1. + 2. * (double)u24(r1.x);
+    c.z = -1.f + 2.f * u24(r1.x);
   }
   if (e.vm) return gen_vm(e, pttab, c, clo, chi, key, r1, r2);
   // pair momentum (getPairMomentum)
-  const float m = (float)c.m, y = (float)c.y;
+  const float m = (float)c.m, y = c.y;
   float ppx = 0.f, ppy = 0.f, mt = m;
   if (e.useNonzeroGamPt) {
     // ln k1,2 = ln(m/2) +- y
@@ -388,7 +397,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   if (e.procID != 51) {
     // pairProduction: back-to-back leptons, |p| = sqrt(M^2/4 - m_l^2), boosted
     const float pmag = sqrtf(fmaxf(m * m * 0.25f - e.mPart * e.mPart, 0.f));
-    const float cz = (float)c.z;
+    const float cz = c.z;
     const float sz = sqrtf(fmaxf(1.f - cz * cz, 0.f));
     float sp, cp;
     sincosf(kTwoPiF * u24(r3.x), &sp, &cp);
@@ -397,21 +406,22 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
     boost_by(vx, vy, vz, ev, ppx, ppy, ppz, pE, m, c.p0);
     boost_by(-vx, -vy, -vz, ev, ppx, ppy, ppz, pE, m, c.p1);
     c.sign = (r3.y & 1u) ? 1.f : -1.f;
+#pragma unroll
     for (int q = 0; q < 2; ++q) {
       const float* pp = q ? c.p1 : c.p0;
-      if (e.doPtCut && sqrtf(pp[0] * pp[0] + pp[1] * pp[1]) < (float)e.minPt) return false;
+      if (e.doPtCut && sqrtf(pp[0] * pp[0] + pp[1] * pp[1]) < e.f_minPt) return false;
       if (e.doEtaCut) {
         const float et = eta_f(pp[0], pp[1], pp[2]);
-        if (et < (float)e.minEta || et > (float)e.maxEta) return false;
+        if (et < e.f_minEta || et > e.f_maxEta) return false;
       }
     }
     return true;
   }
   // ALP: cuts on the ALP, then the isotropic two-photon decay
-  if (e.doPtCut && sqrtf(ppx * ppx + ppy * ppy) < (float)e.minPt) return false;
+  if (e.doPtCut && sqrtf(ppx * ppx + ppy * ppy) < e.f_minPt) return false;
   if (e.doEtaCut) {
     const float et = eta_f(ppx, ppy, ppz);
-    if (et < (float)e.minEta || et > (float)e.maxEta) return false;
+    if (et < e.f_minEta || et > e.f_maxEta) return false;
   }
   const float eph = 0.5f * m;
   float sp, cp;
@@ -432,8 +442,8 @@ constexpr int kTile = 256;
 __device__ __forceinline__ EventRecord to_record(const Cand& c) {
   EventRecord rec;
   rec.m = (float)c.m;
-  rec.y = (float)c.y;
-  rec.z = (float)c.z;
+  rec.y = c.y;
+  rec.z = c.z;
   rec.sign = c.sign;
   for (int q = 0; q < 4; ++q) {
     rec.p0[q] = c.p0[q];
@@ -710,8 +720,8 @@ __global__ void k_events_all(EventParams e, const double* __restrict__ cdf2,
   const bool ok = gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)i, c);
   EventRecord rec;
   rec.m = (float)c.m;
-  rec.y = (float)c.y;
-  rec.z = (float)c.z;
+  rec.y = c.y;
+  rec.z = c.z;
   rec.sign = c.sign;
   for (int q = 0; q < 4; ++q) { rec.p0[q] = c.p0[q]; rec.p1[q] = c.p1[q]; }
   out[i] = rec;

@@ -224,6 +224,11 @@ struct EventParams {
   double mmin, mmax, dm, ymin, dy, zmin, dz;
   int ignoreCSZ, procID, useNonzeroGamPt, doPtCut, doEtaCut;
   double minPt, minEta, maxEta;
+  // FP32 copies of the values the per-candidate FP32 code uses (a conversion
+  // from FP64 runs on the 1/64-rate FP64 pipe), nm as a double
+  float f_dy, f_ymin, f_dz, f_zmin, f_minPt, f_minEta, f_maxEta, f_ptw;
+  double nm_d;
+  const double2* medges;  // per mass bin: lower edge mmin + dm im, width (or null)
   float mPart;
   int partPDG;
   uint64_t seed;
