@@ -1653,11 +1653,11 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     CK(total.ensure(2));
     CK(evstage.ensure((size_t)nc));
     if (mbin) CK(evstage_mbin.ensure((size_t)nc));
-    CK(launch_events_flags(e, cdf2.p, zc, ptcdf.p, next_cand, nc, mask.p, tile_count.p, s,
-                           evstage.p, mbin ? evstage_mbin.p : nullptr));
-    CK(launch_scan_tiles(tile_count.p, tile_off.p, tiles, total.p, s));
-    CK(launch_events_copy(evstage.p, mbin ? evstage_mbin.p : nullptr, tile_count.p, tile_off.p,
-                          tiles, done, n, out, mbin, s));
+    CK(launch_events_flags(e, cdf2.p, zc, ptcdf.p, next_cand, nc, mask.p, s, evstage.p,
+                           mbin ? evstage_mbin.p : nullptr));
+    CK(launch_scan_tiles(nullptr, mask.p, tile_off.p, tiles, total.p, s));
+    CK(launch_events_copy(evstage.p, mbin ? evstage_mbin.p : nullptr, mask.p, tile_off.p, tiles,
+                          done, n, out, mbin, s));
     int64_t acc = 0;
     CK(mcpy(&acc, total.p, sizeof acc, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));

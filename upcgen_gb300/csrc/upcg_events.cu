@@ -452,69 +452,65 @@ __device__ __forceinline__ EventRecord to_record(const Cand& c) {
   return rec;
 }
 
-// Pass 1: every candidate of a 256-candidate tile, its accept bit and the
-// tile's count; with stage, the accepted records also go to the tile's 256
-// staging slots in candidate order (pass 2 then copies instead of
-// regenerating).
+// Pass 1, persistent: warp-tile wt (32 candidates; wt = 8 t + w is warp w
+// of the 256-candidate tile t) -> its accept word mask[wt]; with stage, its
+// accepted records to stage[32 wt + rank] in candidate order.  Every warp
+// runs its warp-tiles on its own (no block barrier), so warps that draw cheap
+// candidates never wait for the slow ones of their block.
 __global__ void __launch_bounds__(kTile, 4) k_events_flags(EventParams e, const double* __restrict__ cdf2,
                                                         const double* __restrict__ cdfz,
                                                         const float* __restrict__ pttab,
-                                                        uint64_t cand0, int64_t ncand,
+                                                        uint64_t cand0, int64_t ncand, int64_t nwt,
                                                         uint32_t* __restrict__ mask,
-                                                        int* __restrict__ tile_count,
                                                         EventRecord* __restrict__ stage,
                                                         int32_t* __restrict__ stage_mbin) {
-  __shared__ int s_pre[kTile / 32 + 1];
-  const int64_t local = (int64_t)blockIdx.x * kTile + threadIdx.x;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  bool ok = false;
-  Cand c;
-  if (local < ncand) ok = gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)local, c);
-  const unsigned bal = __ballot_sync(0xffffffffu, ok);
-  if (lane == 0) {
-    mask[(size_t)blockIdx.x * (kTile / 32) + w] = bal;
-    s_pre[w + 1] = __popc(bal);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_pre[0] = 0;
-    for (int q = 0; q < kTile / 32; ++q) s_pre[q + 1] += s_pre[q];
-    tile_count[blockIdx.x] = s_pre[kTile / 32];
-  }
-  __syncthreads();
-  if (stage && ok) {
-    const int rank = s_pre[w] + __popc(bal & ((1u << lane) - 1u));
-    const size_t slot = (size_t)blockIdx.x * kTile + rank;
-    stage[slot] = to_record(c);
-    if (stage_mbin) stage_mbin[slot] = c.mbin;
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (kTile / 32);
+  for (int64_t wt = (int64_t)blockIdx.x * (kTile / 32) + (threadIdx.x >> 5); wt < nwt; wt += nwarps) {
+    const int64_t local = wt * 32 + lane;
+    bool ok = false;
+    Cand c;
+    if (local < ncand) ok = gen_candidate(e, cdf2, cdfz, pttab, cand0 + (uint64_t)local, c);
+    const unsigned bal = __ballot_sync(0xffffffffu, ok);
+    if (lane == 0) mask[wt] = bal;
+    if (stage && ok) {
+      const size_t slot = (size_t)wt * 32 + __popc(bal & ((1u << lane) - 1u));
+      stage[slot] = to_record(c);
+      if (stage_mbin) stage_mbin[slot] = c.mbin;
+    }
   }
 }
 
-// Pass 2 from the staging slots: tile t's accepted records to their output
-// slots out_base + tile_off[t] + r (below nmax); 3 float4 per record.
+// Pass 2 from the staging slots: tile t's accepted records to out_base +
+// tile_off[t] + r (below nmax), r counted over the tile's 8 warp-tiles in
+// order; one thread per record (3 float4 when out is 16-byte aligned).
 __global__ void k_events_copy(const EventRecord* __restrict__ stage,
                               const int32_t* __restrict__ stage_mbin,
-                              const int* __restrict__ tile_count,
+                              const uint32_t* __restrict__ mask,
                               const int64_t* __restrict__ tile_off, int64_t out_base,
                               int64_t nmax, EventRecord* __restrict__ out,
                               int32_t* __restrict__ mbin) {
-  const int tile = blockIdx.x;
+  const int64_t tile = blockIdx.x;
   const int64_t base = out_base + tile_off[tile];
   if (base >= nmax) return;
-  const int cnt = tile_count[tile];
-  const int64_t lim = nmax - base < cnt ? nmax - base : cnt;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int before = 0;
+  for (int q = 0; q < w; ++q) before += __popc(__ldg(mask + tile * (kTile / 32) + q));
+  const int cnt = __popc(__ldg(mask + tile * (kTile / 32) + w));
+  if (lane >= cnt) return;
+  const int64_t slot = base + before + lane;
+  if (slot >= nmax) return;
+  const size_t src = (size_t)(tile * (kTile / 32) + w) * 32 + lane;
   if ((reinterpret_cast<uintptr_t>(out) & 15) == 0) {  // 48-byte records: 3 float4 each
-    const float4* src = reinterpret_cast<const float4*>(stage + (size_t)tile * kTile);
-    float4* dst = reinterpret_cast<float4*>(out + base);
-    for (int i = threadIdx.x; i < 3 * lim; i += blockDim.x) dst[i] = __ldg(src + i);
+    const float4* a = reinterpret_cast<const float4*>(stage + src);
+    float4* b = reinterpret_cast<float4*>(out + slot);
+    b[0] = __ldg(a);
+    b[1] = __ldg(a + 1);
+    b[2] = __ldg(a + 2);
   } else {
-    const float* src = reinterpret_cast<const float*>(stage + (size_t)tile * kTile);
-    float* dst = reinterpret_cast<float*>(out + base);
-    for (int i = threadIdx.x; i < 12 * lim; i += blockDim.x) dst[i] = __ldg(src + i);
+    out[slot] = stage[src];
   }
-  if (mbin)
-    for (int i = threadIdx.x; i < lim; i += blockDim.x)
-      mbin[base + i] = __ldg(stage_mbin + (size_t)tile * kTile + i);
+  if (mbin) mbin[slot] = __ldg(stage_mbin + src);
 }
 
 __global__ void __launch_bounds__(kTile, 5) k_events_write(EventParams e, const double* __restrict__ cdf2,
@@ -564,12 +560,13 @@ __global__ void __launch_bounds__(kTile, 5) k_events_write(EventParams e, const 
 }
 
 // Exclusive scan of the tile counts (one CTA; tiles per chunk <= 2^20) and the
-// total: 8192 counts per round, loaded coalesced into shared memory; each
+// total, the counts given or taken from the accept words: 8192 counts per round, loaded coalesced into shared memory; each
 // thread sums 8 consecutive ones, a warp-shuffle scan and a scan of the 32
 // warp totals give the thread's offset, and a carry runs across rounds.
 constexpr int kScanThreads = 1024, kScanPer = 8;
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* __restrict__ cnt,
+                                                            const uint32_t* __restrict__ mask,
                                                             int64_t* __restrict__ off, int n,
                                                             int64_t* __restrict__ total) {
   __shared__ int s_cnt[kScanThreads * kScanPer];
@@ -578,8 +575,21 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* __restri
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   if (t == 0) s_carry = 0;
   for (int base = 0; base < n; base += kScanThreads * kScanPer) {
-    for (int j = t; j < kScanThreads * kScanPer; j += kScanThreads)
-      s_cnt[j] = base + j < n ? __ldg(cnt + base + j) : 0;
+    if (mask) {  // a tile's count: the set bits of its 8 accept words (32 bytes)
+      for (int j = t; j < kScanThreads * kScanPer; j += kScanThreads) {
+        int v = 0;
+        if (base + j < n) {
+          const uint4* m4 = reinterpret_cast<const uint4*>(mask + (size_t)(base + j) * 8);
+          const uint4 a = __ldg(m4), b = __ldg(m4 + 1);
+          v = __popc(a.x) + __popc(a.y) + __popc(a.z) + __popc(a.w) + __popc(b.x) + __popc(b.y) +
+              __popc(b.z) + __popc(b.w);
+        }
+        s_cnt[j] = v;
+      }
+    } else {
+      for (int j = t; j < kScanThreads * kScanPer; j += kScanThreads)
+        s_cnt[j] = base + j < n ? __ldg(cnt + base + j) : 0;
+    }
     __syncthreads();
     int64_t mine = 0;
 #pragma unroll
@@ -808,21 +818,39 @@ cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, flo
 
 cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                                 const float* d_ptcdf, uint64_t cand0, int64_t ncand,
-                                uint32_t* d_mask, int* d_tile_count, cudaStream_t st,
-                                EventRecord* d_stage, int32_t* d_stage_mbin) {
+                                uint32_t* d_mask, cudaStream_t st, EventRecord* d_stage,
+                                int32_t* d_stage_mbin) {
+  // one resident wave: SMs x the blocks of k_events_flags an SM holds
+  static int waves[64] = {0};
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!waves[dev]) {
+    int sms = 0, per = 0;
+    err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (err != cudaSuccess) return err;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_events_flags, kTile, 0);
+    if (err != cudaSuccess) return err;
+    waves[dev] = std::max(1, sms * std::max(1, per));
+  }
   const int64_t tiles = (ncand + kTile - 1) / kTile;
+  const int64_t nwt = tiles * (kTile / 32);
+  const int64_t grid = std::min<int64_t>(tiles, waves[dev]);
+  if (grid <= 0) return cudaSuccess;
   note_launch();
-  k_events_flags<<<(unsigned)tiles, kTile, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, ncand,
-                                                   d_mask, d_tile_count, d_stage, d_stage_mbin);
+  k_events_flags<<<(unsigned)grid, kTile, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, ncand, nwt,
+                                                  d_mask, d_stage, d_stage_mbin);
   return cudaGetLastError();
 }
 
 cudaError_t launch_events_copy(const EventRecord* d_stage, const int32_t* d_stage_mbin,
-                               const int* d_tile_count, const int64_t* d_tile_off, int64_t tiles,
+                               const uint32_t* d_mask, const int64_t* d_tile_off, int64_t tiles,
                                int64_t out_base, int64_t nmax, EventRecord* d_out, int32_t* d_mbin,
                                cudaStream_t st) {
+  if (tiles <= 0) return cudaSuccess;
   note_launch();
-  k_events_copy<<<(unsigned)tiles, kTile, 0, st>>>(d_stage, d_stage_mbin, d_tile_count, d_tile_off,
+  k_events_copy<<<(unsigned)tiles, kTile, 0, st>>>(d_stage, d_stage_mbin, d_mask, d_tile_off,
                                                    out_base, nmax, d_out, d_mbin);
   return cudaGetLastError();
 }
@@ -840,10 +868,10 @@ cudaError_t launch_events_write(const EventParams& e, const double* d_cdf2, cons
   return cudaGetLastError();
 }
 
-cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
-                              cudaStream_t st) {
+cudaError_t launch_scan_tiles(const int* d_count, const uint32_t* d_mask, int64_t* d_off, int n,
+                              int64_t* d_total, cudaStream_t st) {
   note_launch();
-  k_scan_tiles<<<1, kScanThreads, 0, st>>>(d_count, d_off, n, d_total);
+  k_scan_tiles<<<1, kScanThreads, 0, st>>>(d_count, d_mask, d_off, n, d_total);
   return cudaGetLastError();
 }
 

@@ -288,11 +288,11 @@ cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, flo
                                     float* d_cdf, cudaStream_t st);
 cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                                 const float* d_ptcdf, uint64_t cand0, int64_t ncand,
-                                uint32_t* d_mask, int* d_tile_count, cudaStream_t st,
-                                EventRecord* d_stage = nullptr, int32_t* d_stage_mbin = nullptr);
+                                uint32_t* d_mask, cudaStream_t st, EventRecord* d_stage = nullptr,
+                                int32_t* d_stage_mbin = nullptr);
 // pass 2 from pass 1's staging slots (launch_events_flags with d_stage)
 cudaError_t launch_events_copy(const EventRecord* d_stage, const int32_t* d_stage_mbin,
-                               const int* d_tile_count, const int64_t* d_tile_off, int64_t tiles,
+                               const uint32_t* d_mask, const int64_t* d_tile_off, int64_t tiles,
                                int64_t out_base, int64_t nmax, EventRecord* d_out, int32_t* d_mbin,
                                cudaStream_t st);
 cudaError_t launch_events_write(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
@@ -305,8 +305,8 @@ cudaError_t launch_events_all(const EventParams& e, const double* d_cdf2, const 
                               uint8_t* d_flag, cudaStream_t st);
 cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* d_out,
                                cudaStream_t st);
-cudaError_t launch_scan_tiles(const int* d_count, int64_t* d_off, int n, int64_t* d_total,
-                              cudaStream_t st);
+cudaError_t launch_scan_tiles(const int* d_count, const uint32_t* d_mask, int64_t* d_off, int n,
+                              int64_t* d_total, cudaStream_t st);
 
 // fast form's Q(w, b) table: Gauss-Legendre nodes cover q in [0, kQNodeMax]
 // GeV (beyond it q^2 > Q2max, where the reference's integrand holds the form
