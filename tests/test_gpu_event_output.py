@@ -88,9 +88,20 @@ def test_empty_and_bad_path(ug, tmp_path):
 
 
 def test_pinned_out_buffer(ug):
-    """generateEvents into a page-locked array (upcg_host_alloc) gives the
-    events of a pageable one; a short or mistyped out is refused."""
+    """generateEvents, lumiTable and nucCSYM into page-locked arrays
+    (upcg_host_alloc) give what they give into pageable ones; an out of the
+    wrong size or type is refused."""
     g, ref = _pair(ug, dict(C2S, BINS_M=51, BINS_Y=25))
+    lum = ug.pinned_array((51, 25), np.float64)
+    csh = ug.pinned_array((25, 51), np.float64)
+    assert g.lumiTable(out=lum) is lum and np.array_equal(lum, ref.lumiTable())
+    cs, tot = g.nucCSYM(out=csh)
+    cs_ref, tot_ref = ref.nucCSYM()
+    assert cs is csh and np.array_equal(cs, cs_ref) and tot == tot_ref
+    with pytest.raises(ValueError):
+        g.lumiTable(out=np.zeros((25, 51)))
+    with pytest.raises(ValueError):
+        g.nucCSYM(out=np.zeros((25, 51), dtype=np.float32))
     n = 20000
     buf = ug.pinned_array(n + 5, ug.EVENT_DTYPE)
     ev, rej = g.generateEvents(n, out=buf)

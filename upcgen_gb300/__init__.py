@@ -140,6 +140,16 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
+def _out_array(out, shape, dtype=np.float64):
+    """A fresh zeroed array, or the caller's after checking it fits."""
+    if out is None:
+        return np.zeros(shape, dtype=dtype)
+    if out.dtype != dtype or out.shape != tuple(shape) or not out.flags.c_contiguous \
+            or not out.flags.writeable:
+        raise ValueError(f"out must be a writeable C-contiguous {np.dtype(dtype)} array of shape {tuple(shape)}")
+    return out
+
+
 def selftest_contract(ncells, P, seed=1):
     """Tensor-core contraction vs FP64 on random data: (max rel err, ms)."""
     L = load_library()
@@ -483,16 +493,20 @@ class UpcGenerator:
         return dict(mmin=v[0].value, mmax=v[1].value, nm=n[0].value, ymin=v[2].value,
                     ymax=v[3].value, ny=n[1].value, zmin=v[4].value, zmax=v[5].value, nz=n[2].value)
 
-    def lumiTable(self, polarized=False):
+    def lumiTable(self, polarized=False, out=None, out2=None):
+        """L dm dy [nm][ny] (and the pseudoscalar table when polarized); out /
+        out2: a caller's float64 arrays of that shape (pinned_array for the
+        fastest copy)."""
         g = self.grid()
-        out = np.zeros((g["nm"], g["ny"]))
-        out2 = np.zeros_like(out) if polarized else None
+        out = _out_array(out, (g["nm"], g["ny"]))
+        out2 = _out_array(out2, (g["nm"], g["ny"])) if polarized else None
         _check(self._L.upcg_lumi_table(self._h, _p(out), out.size, _p(out2) if polarized else None))
         return (out, out2) if polarized else out
 
-    def nucCSYM(self):
+    def nucCSYM(self, out=None):
+        """(dsigma [ny][nm], sigma_tot mb); out: a caller's float64 [ny][nm] array."""
         g = self.grid()
-        out = np.zeros((g["ny"], g["nm"]))
+        out = _out_array(out, (g["ny"], g["nm"]))
         tot = C.c_double()
         _check(self._L.upcg_nuc_cs_ym(self._h, _p(out), out.size, C.byref(tot)))
         return out, tot.value
