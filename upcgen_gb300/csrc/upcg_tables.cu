@@ -321,6 +321,8 @@ __global__ void __launch_bounds__(256) k_breakup_values(const double* __restrict
 // near se / ee instead of up to 1e35 at b -> 0) in FP32, the warp sum and the
 // 1/beta^2 in FP64; relative error ~1e-6, at 1/64 of the FP64 pipe's cost per
 // term.
+constexpr int kBreakupThreads = 256;
+
 __device__ __forceinline__ float bessel_k1_as_f(float x) {  // bessel_k1_as, x > 2
   const float y = 2.f / x;
   return (expf(-x) * rsqrtf(x)) *
@@ -328,72 +330,100 @@ __device__ __forceinline__ float bessel_k1_as_f(float x) {  // bessel_k1_as, x >
           y * (-0.780353e-2f + y * (0.325614e-2f + y * (-0.68245e-3f)))))));
 }
 
+// A block takes 32 consecutive b: warp 0 computes their FP64 prologue (beta,
+// ln(beta/2), omax) and epilogue (1/beta^2, the mode formula) one b per lane,
+// so that each FP64 instruction serves 32 b (a warp FP64 instruction costs the
+// same with 1 useful lane as with 32); the 8 warps share the 32 FP32 sums
+// over the energy table, 4 b each.  Same arithmetic, in the same order, as
+// one warp per b.
 __global__ void __launch_bounds__(256) k_breakup_values_f(const double* __restrict__ tab, int nt,
                                                           int n, double x0, double h, int mode,
                                                           double gammatarg, double omaxx,
                                                           double zcon, double* __restrict__ out) {
   extern __shared__ float s_tabf[];  // ee | se | ln ee | 1/ee
+  __shared__ float s_beta[32], s_lnhb[32], s_omax[32];
+  __shared__ double s_sum[32];
+  __shared__ unsigned s_run;
   for (int i = threadIdx.x; i < 4 * nt; i += blockDim.x) {
     const int part = i / nt, j = i - part * nt;
     s_tabf[i] = (float)tab[part * kBreakupTabMax + j];
   }
-  __syncthreads();
   const float* see = s_tabf;
   const float* sse = s_tabf + nt;
   const float* slne = s_tabf + 2 * nt;
   const float* sinv = s_tabf + 3 * nt;
-  const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
-  const double b = x0 + i * h;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const double hbarcmev = 197.3269718, o0 = 7.4;
-  const double beta_d = b / ((hbarcmev) * gammatarg);
-  const float beta = (float)beta_d;
-  const float ln_half_beta = (float)log(0.5 * beta_d);
-  // g_k = beta^2 f_k = se_k ee_k (beta K1(ee_k beta))^2
-  auto g = [&](int k) {
-    const float x = see[k] * beta;
-    float bk1;  // beta K1(x)
-    if (x > 2.f) {
-      bk1 = beta * bessel_k1_as_f(x);
-    } else {
-      const float y = x * x * 0.25f;
-      const float u = x * x * (1.f / 14.0625f);
-      const float i1 = x * (0.5f + u * (0.87890594f + u * (0.51498869f + u * (0.15084934f +
-                       u * (0.2658733e-1f + u * (0.301532e-2f + u * 0.32411e-3f))))));
-      bk1 = beta * (slne[k] + ln_half_beta) * i1 +
-            sinv[k] * (1.f + y * (0.15443144f + y * (-0.67278579f + y * (-0.18156897f +
-            y * (-0.1919402e-1f + y * (-0.110404e-2f + y * (-0.4686e-4f)))))));
+  for (int i0 = blockIdx.x * 32; i0 < n; i0 += gridDim.x * 32) {
+    if (w == 0) {  // FP64 prologue, b = i0 + lane
+      const int ib = i0 + lane;
+      const double b = x0 + ib * h;
+      const double beta_d = b / ((hbarcmev) * gammatarg);
+      const double omax = fmin(omaxx, 4. * gammatarg * (hbarcmev) / b);
+      s_beta[lane] = (float)beta_d;
+      s_lnhb[lane] = (float)log(0.5 * beta_d);
+      s_omax[lane] = (float)omax;
+      const unsigned run = __ballot_sync(0xffffffffu, ib < n && !(omax < o0));
+      if (lane == 0) s_run = run;
     }
-    return sse[k] * see[k] * bk1 * bk1;
-  };
-  const double omax = fmin(omaxx, 4. * gammatarg * (hbarcmev) / b);
-  double p = 0.;
-  if (!(omax < o0)) {
-    const float omaxf = (float)omax;
-    float part = 0.f;
-    float carry = lane == 31 ? g(1) : 0.f;
-    for (int k0 = 2; k0 < nt; k0 += 32) {
-      const int k = k0 + lane;
-      const bool in = k < nt && see[k] < omaxf;
-      const float gk = in ? g(k) : 0.f;
-      float gm = __shfl_up_sync(0xffffffffu, gk, 1);
-      const float c = __shfl_sync(0xffffffffu, carry, 31);
-      if (lane == 0) gm = c;
-      if (in) part += (see[k] - see[k - 1]) * .5f * (gm + gk);
-      carry = gk;
-      if (!__any_sync(0xffffffffu, in)) break;
-    }
-    double sum = (double)part;
+    __syncthreads();
+    const unsigned run = s_run;
+    for (int jb = w; jb < 32; jb += kBreakupThreads / 32) {
+      if (!((run >> jb) & 1u)) continue;
+      const float beta = s_beta[jb], ln_half_beta = s_lnhb[jb], omaxf = s_omax[jb];
+      // g_k = beta^2 f_k = se_k ee_k (beta K1(ee_k beta))^2
+      auto g = [&](int k) {
+        const float x = see[k] * beta;
+        float bk1;  // beta K1(x)
+        if (x > 2.f) {
+          bk1 = beta * bessel_k1_as_f(x);
+        } else {
+          const float y = x * x * 0.25f;
+          const float u = x * x * (1.f / 14.0625f);
+          const float i1 = x * (0.5f + u * (0.87890594f + u * (0.51498869f + u * (0.15084934f +
+                           u * (0.2658733e-1f + u * (0.301532e-2f + u * 0.32411e-3f))))));
+          bk1 = beta * (slne[k] + ln_half_beta) * i1 +
+                sinv[k] * (1.f + y * (0.15443144f + y * (-0.67278579f + y * (-0.18156897f +
+                y * (-0.1919402e-1f + y * (-0.110404e-2f + y * (-0.4686e-4f)))))));
+        }
+        return sse[k] * see[k] * bk1 * bk1;
+      };
+      float part = 0.f;
+      float carry = lane == 31 ? g(1) : 0.f;
+      for (int k0 = 2; k0 < nt; k0 += 32) {
+        const int k = k0 + lane;
+        const bool in = k < nt && see[k] < omaxf;
+        const float gk = in ? g(k) : 0.f;
+        float gm = __shfl_up_sync(0xffffffffu, gk, 1);
+        const float c = __shfl_sync(0xffffffffu, carry, 31);
+        if (lane == 0) gm = c;
+        if (in) part += (see[k] - see[k - 1]) * .5f * (gm + gk);
+        carry = gk;
+        if (!__any_sync(0xffffffffu, in)) break;
+      }
+      double sum = (double)part;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    const double pxn = zcon * sum / (beta_d * beta_d);
-    if (mode == 1) p = 1.;
-    if (mode == 2) p = (1 - exp(-1 * pxn)) * (1 - exp(-1 * pxn));
-    if (mode == 3) p = exp(-2 * pxn);
-    if (mode == 4) p = 2. * exp(-pxn) * (1. - exp(-pxn));
-  }
-  if (lane == 0) out[i] = p;
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) s_sum[jb] = sum;
+    }
+    __syncthreads();
+    if (w == 0) {  // FP64 epilogue
+      const int ib = i0 + lane;
+      if (ib < n) {
+        double p = 0.;
+        if ((run >> lane) & 1u) {
+          const double b = x0 + ib * h;
+          const double beta_d = b / ((hbarcmev) * gammatarg);
+          const double pxn = zcon * s_sum[lane] / (beta_d * beta_d);
+          if (mode == 1) p = 1.;
+          if (mode == 2) p = (1 - exp(-1 * pxn)) * (1 - exp(-1 * pxn));
+          if (mode == 3) p = exp(-2 * pxn);
+          if (mode == 4) p = 2. * exp(-pxn) * (1. - exp(-pxn));
+        }
+        out[ib] = p;
+      }
+    }
+    __syncthreads();  // s_* are rewritten by the next group
   }
 }
 
@@ -516,10 +546,11 @@ cudaError_t launch_breakup_values(const double* d_tab, int nt, double gammatarg,
   if (nt > kBreakupTabMax) return cudaErrorInvalidValue;
   // 8 warps per block, each over several b: 4 blocks per SM of 152
   const unsigned blocks = (unsigned)std::min<size_t>(((size_t)n * 32 + 255) / 256, 608);
-  if (fp32) {
+  if (fp32) {  // 32 b per block
+    const unsigned bf = (unsigned)std::min<size_t>(((size_t)n + 31) / 32, 152 * 16);
     note_launch();
-    k_breakup_values_f<<<blocks, 256, 4 * sizeof(float) * nt, st>>>(d_tab, nt, n, x0, h, mode,
-                                                                   gammatarg, omaxx, zcon, d_out);
+    k_breakup_values_f<<<bf, kBreakupThreads, 4 * sizeof(float) * nt, st>>>(
+        d_tab, nt, n, x0, h, mode, gammatarg, omaxx, zcon, d_out);
     return cudaGetLastError();
   }
   const size_t smem = 4 * sizeof(double) * nt;
