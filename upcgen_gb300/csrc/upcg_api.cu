@@ -1535,7 +1535,7 @@ int upcg_generator::build_xsec() {
   if (!isVM) {  // vector mesons: cs, ratio and tot come from build_vm
     CK(cs.ensure(ncell));
     CK(ratio.ensure(usePolarizedCS ? ncell : 1));
-    CK(partial.ensure((ncell + 255) / 256 + 1));
+    CK(partial.ensure(fold_partial_doubles(nm, ny)));
     CK(tot.ensure(1));
     CK(launch_fold(f, lumi.p, usePolarizedCS ? lumi2.p : nullptr, cs.p, ratio.p, partial.p, tot.p, s));
   }

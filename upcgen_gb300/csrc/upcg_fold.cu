@@ -99,9 +99,26 @@ __global__ void k_cs_m_pts(FoldParams f, const double* __restrict__ m, double* _
 
 constexpr int kFoldThreads = 256;
 
+// sigma(m) of every mass row, once per row rather than once per cell: the FP64
+// cross section runs on the 1/64-rate pipe, which a warp of cells of one row
+// would occupy 32 times for one value.  Polarized: scalar in csm[0, nm),
+// pseudoscalar in csm[nm, 2 nm).
+__global__ void k_cs_m_rows(FoldParams f, double* __restrict__ csm) {
+  const int im = blockIdx.x * blockDim.x + threadIdx.x;
+  if (im >= f.nm) return;
+  const double m = f.mmin + f.dm * im;
+  if (!f.polarized) {
+    csm[im] = cs_m(f, m, 0);
+  } else {
+    csm[im] = cs_m(f, m, 1);
+    csm[f.nm + im] = cs_m(f, m, 2);
+  }
+}
+
 // cs[iy][im] and one partial sum of cs per block (fixed order).
 __global__ void __launch_bounds__(kFoldThreads) k_fold(FoldParams f, const double* __restrict__ lumi,
                                                        const double* __restrict__ lumi2,
+                                                       const double* __restrict__ csm,
                                                        double* __restrict__ cs,
                                                        double* __restrict__ ratio,
                                                        double* __restrict__ partial) {
@@ -111,13 +128,12 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold(FoldParams f, const doubl
   double v = 0.;
   if (i < n) {
     const int im = i / f.ny, iy = i - im * f.ny;
-    const double m = f.mmin + f.dm * im;
     const size_t co = (size_t)iy * f.nm + im;
     if (!f.polarized) {
-      v = cs_m(f, m, 0) * lumi[i];
+      v = __ldg(csm + im) * lumi[i];
     } else {
-      const double s = lumi[i] * cs_m(f, m, 1);
-      const double p = lumi2[i] * cs_m(f, m, 2);
+      const double s = lumi[i] * __ldg(csm + im);
+      const double p = lumi2[i] * __ldg(csm + f.nm + im);
       v = (s + p) * 1e7;
       ratio[co] = s / p;
     }
@@ -281,13 +297,20 @@ cudaError_t launch_cs_m_points(const FoldParams& f, const double* d_m, double* d
   return cudaGetLastError();
 }
 
+int fold_partial_doubles(int nm, int ny) {
+  return ((int64_t)nm * ny + kFoldThreads - 1) / kFoldThreads + 1 + 2 * nm;
+}
+
 cudaError_t launch_fold(const FoldParams& f, const double* d_lumi, const double* d_lumi2,
                         double* d_cs, double* d_ratio, double* d_partial, double* d_tot,
                         cudaStream_t st) {
   const int n = f.nm * f.ny;
   const int blocks = (n + kFoldThreads - 1) / kFoldThreads;
+  double* csm = d_partial + blocks + 1;  // fold_partial_doubles: the blocks' sums, then sigma(m)
   note_launch();
-  k_fold<<<blocks, kFoldThreads, 0, st>>>(f, d_lumi, d_lumi2, d_cs, d_ratio, d_partial);
+  k_cs_m_rows<<<(f.nm + 127) / 128, 128, 0, st>>>(f, csm);
+  note_launch();
+  k_fold<<<blocks, kFoldThreads, 0, st>>>(f, d_lumi, d_lumi2, csm, d_cs, d_ratio, d_partial);
   note_launch();
   k_reduce_total<<<1, 1024, 0, st>>>(d_partial, blocks, 1e-6, d_tot);
   return cudaGetLastError();

@@ -207,6 +207,8 @@ struct FoldParams {
   double mPart, aLep, alpWidth;
 };
 cudaError_t launch_cs_zm(const FoldParams& f, int flag, double* d_out, cudaStream_t st);
+// doubles of launch_fold's d_partial: the per-block sums, then sigma(m) per row
+int fold_partial_doubles(int nm, int ny);
 cudaError_t launch_fold(const FoldParams& f, const double* d_lumi, const double* d_lumi2,
                         double* d_cs, double* d_ratio, double* d_partial, double* d_tot,
                         cudaStream_t st);
