@@ -821,22 +821,24 @@ cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, cons
                                 uint32_t* d_mask, cudaStream_t st, EventRecord* d_stage,
                                 int32_t* d_stage_mbin) {
   // one resident wave: SMs x the blocks of k_events_flags an SM holds
-  static int waves[64] = {0};
+  static std::atomic<int> waves[64] = {};  // per device id, 0 until measured
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return err;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!waves[dev]) {
+  int wave = waves[dev].load(std::memory_order_relaxed);
+  if (!wave) {
     int sms = 0, per = 0;
     err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (err != cudaSuccess) return err;
     err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_events_flags, kTile, 0);
     if (err != cudaSuccess) return err;
-    waves[dev] = std::max(1, sms * std::max(1, per));
+    wave = std::max(1, sms * std::max(1, per));
+    waves[dev].store(wave, std::memory_order_relaxed);
   }
   const int64_t tiles = (ncand + kTile - 1) / kTile;
   const int64_t nwt = tiles * (kTile / 32);
-  const int64_t grid = std::min<int64_t>(tiles, waves[dev]);
+  const int64_t grid = std::min<int64_t>(tiles, wave);
   if (grid <= 0) return cudaSuccess;
   note_launch();
   k_events_flags<<<(unsigned)grid, kTile, 0, st>>>(e, d_cdf2, d_cdfz, d_ptcdf, cand0, ncand, nwt,

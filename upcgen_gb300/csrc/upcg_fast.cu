@@ -1121,11 +1121,10 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
   if ((e = make_map(&tAl, al, ncells_pad, P, BM)) != cudaSuccess) return e;
   if ((e = make_map(&tBh, gh, P, P, BN)) != cudaSuccess) return e;
   if ((e = make_map(&tBl, gl, P, P, BN)) != cudaSuccess) return e;
-  static bool attr = false;
-  if (!attr) {
-    e = cudaFuncSetAttribute(k_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
-    if (e != cudaSuccess) return e;
-    attr = true;
+  static std::atomic<uint64_t> attr{0};  // devices with the limit raised
+  {
+    const cudaError_t ea = smem_attr_once(attr, k_contract, kContractSmem);
+    if (ea != cudaSuccess) return ea;
   }
   ContractArgs args{P / BK, ncells, P, P / BN, a2, partial, d_err, nullptr, nullptr, nullptr, 0};
   dim3 grid(P / BN, ncells_pad / BM);
@@ -1151,22 +1150,20 @@ cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh,
   PersArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, a2, partial, d_err};
   if (grid > nitems) grid = nitems;
   if (shape == 0) {
-    static bool attr = false;
+    static std::atomic<uint64_t> attr{0};  // devices with the limit raised
     constexpr int sm = pers_smem<256, 2>();
-    if (!attr) {
-      e = cudaFuncSetAttribute(k_contract_pers<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-      if (e != cudaSuccess) return e;
-      attr = true;
+    {
+      const cudaError_t ea = smem_attr_once(attr, k_contract_pers<256, 2>, sm);
+      if (ea != cudaSuccess) return ea;
     }
     note_launch();
     k_contract_pers<256, 2><<<grid, 192, sm, st>>>(tAh, tAl, tBh, tBl, args);
   } else {
-    static bool attr = false;
+    static std::atomic<uint64_t> attr{0};  // devices with the limit raised
     constexpr int sm = pers_smem<128, 3>();
-    if (!attr) {
-      e = cudaFuncSetAttribute(k_contract_pers<128, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-      if (e != cudaSuccess) return e;
-      attr = true;
+    {
+      const cudaError_t ea = smem_attr_once(attr, k_contract_pers<128, 3>, sm);
+      if (ea != cudaSuccess) return ea;
     }
     note_launch();
     k_contract_pers<128, 3><<<grid, 192, sm, st>>>(tAh, tAl, tBh, tBl, args);
@@ -1190,11 +1187,10 @@ cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, c
   if ((e = make_map(&tAl, al, Mpad, K, BM)) != cudaSuccess) return e;
   if ((e = make_map(&tBh, bh, N, K, BN)) != cudaSuccess) return e;
   if ((e = make_map(&tBl, bl, N, K, BN)) != cudaSuccess) return e;
-  static bool attr = false;
-  if (!attr) {
-    e = cudaFuncSetAttribute(k_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, kContractSmem);
-    if (e != cudaSuccess) return e;
-    attr = true;
+  static std::atomic<uint64_t> attr{0};  // devices with the limit raised
+  {
+    const cudaError_t ea = smem_attr_once(attr, k_contract, kContractSmem);
+    if (ea != cudaSuccess) return ea;
   }
   ContractArgs args{K / BK, M, K, N / BN, nullptr, nullptr, d_err, out_f32,
                     static_cast<__nv_bfloat16*>(out_hi), static_cast<__nv_bfloat16*>(out_lo), N};

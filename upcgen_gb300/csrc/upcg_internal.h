@@ -4,11 +4,29 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "upcg_device.cuh"
 
 struct upcg_generator;
 
 namespace upcg {
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per device for one
+// kernel; done holds a bit per device id (< 64), so handles on several
+// devices, from several threads, each see the limit raised on theirs
+template <typename Kernel>
+inline cudaError_t smem_attr_once(std::atomic<uint64_t>& done, Kernel kernel, int bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  const uint64_t bit = 1ull << dev;
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 
 constexpr int kNb = 120;                // b-bins per side (include/UpcCrossSection.h:116-117)
 constexpr int kBreakupTabMax = 1024;    // capacity of the photo-neutron energy table

@@ -550,12 +550,10 @@ cudaError_t launch_mlp_labels(const MlpBox& bx, uint64_t seed, uint64_t i0, int 
 cudaError_t launch_mlp_step(const void* pb, const float* pf, const float* xs, const float* ys,
                             const float* ws, const int* idx, int nbatch, float inv_wsum,
                             float* part, float* lossp, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)mlp_step_smem());
-    if (e != cudaSuccess) return e;
-    attr = true;
+  static std::atomic<uint64_t> attr{0};  // devices with the limit raised
+  {
+    const cudaError_t ea = smem_attr_once(attr, k_mlp_step, (int)mlp_step_smem());
+    if (ea != cudaSuccess) return ea;
   }
   const int ctas = (nbatch + kStepSamples - 1) / kStepSamples;
   note_launch();
@@ -583,12 +581,10 @@ cudaError_t launch_mlp_to_bf16(const float* pf, void* pb, cudaStream_t st) {
 
 cudaError_t launch_mlp_infer(const void* pb, const float* pf, const float* xs, int n, float* out,
                              cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)mlp_infer_smem());
-    if (e != cudaSuccess) return e;
-    attr = true;
+  static std::atomic<uint64_t> attr{0};  // devices with the limit raised
+  {
+    const cudaError_t ea = smem_attr_once(attr, k_mlp_infer, (int)mlp_infer_smem());
+    if (ea != cudaSuccess) return ea;
   }
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);

@@ -554,13 +554,10 @@ cudaError_t launch_breakup_values(const double* d_tab, int nt, double gammatarg,
     return cudaGetLastError();
   }
   const size_t smem = 4 * sizeof(double) * nt;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_breakup_values,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(4 * sizeof(double) * kBreakupTabMax));
-    if (e != cudaSuccess) return e;
-    attr = true;
+  static std::atomic<uint64_t> attr{0};  // devices with the limit raised
+  {
+    const cudaError_t ea = smem_attr_once(attr, k_breakup_values, (int)(4 * sizeof(double) * kBreakupTabMax));
+    if (ea != cudaSuccess) return ea;
   }
   note_launch();
   k_breakup_values<<<blocks, 256, smem, st>>>(d_tab, nt, n, x0, h, mode, gammatarg, omaxx, zcon,
