@@ -325,7 +325,7 @@ struct upcg_generator {
     if (!ev_fork) return cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
     return cudaSuccess;
   }
-  DBuf<int> ntab, nq, ovf, tile_count, mirror, guide2, guidez, frep;
+  DBuf<int> ntab, nq, ovf, mirror, guide2, guidez, frep;
   DBuf<int4> fitems;
   DBuf<uint16_t> guidept;
   DBuf<unsigned int> work;
@@ -1593,8 +1593,10 @@ int upcg_generator::build_xsec() {
 
 namespace {
 // Candidate index of the need-th accepted candidate (need >= 1) of a chunk.
-__global__ void k_find_cut(const int* cnt, const int64_t* off, const uint32_t* mask, int ntiles,
-                           int64_t need, int64_t* out) {
+// The candidate index of the need-th accepted candidate of a chunk, from the
+// tiles' output offsets and accept words (-1 if the chunk holds fewer).
+__global__ void k_find_cut(const int64_t* off, const uint32_t* mask, int ntiles, int64_t need,
+                           int64_t* out) {
   if (threadIdx.x != 0) return;
   int lo = 0, hi = ntiles;  // last tile with off <= need-1
   while (hi - lo > 1) {
@@ -1616,7 +1618,6 @@ __global__ void k_find_cut(const int* cnt, const int64_t* off, const uint32_t* m
     rem -= pc;
   }
   *out = -1;
-  (void)cnt;
 }
 }  // namespace
 
@@ -1648,7 +1649,6 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     nc = (nc + 255) / 256 * 256;
     const int tiles = (int)(nc / 256);
     CK(mask.ensure((size_t)tiles * 8));
-    CK(tile_count.ensure(tiles));
     CK(tile_off.ensure(tiles + 1));
     CK(total.ensure(2));
     CK(evstage.ensure((size_t)nc));
@@ -1668,7 +1668,7 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
     if (acc >= need) {
       CK(cudaMemsetAsync(total.p + 1, 0xff, sizeof(int64_t), s));
       note_launch();
-      k_find_cut<<<1, 32, 0, s>>>(tile_count.p, tile_off.p, mask.p, tiles, need, total.p + 1);
+      k_find_cut<<<1, 32, 0, s>>>(tile_off.p, mask.p, tiles, need, total.p + 1);
       CK(cudaGetLastError());
       int64_t cut = -1;
       CK(mcpy(&cut, total.p + 1, sizeof cut, cudaMemcpyDeviceToHost, s));
