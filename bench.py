@@ -124,6 +124,12 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+def workload_name(workload, params, nm, ny, nev):
+    """The config.workload string both arms print for a single-table workload."""
+    return (f"{workload}: Pb-Pb {nm}x{ny} (m,y) cells, FLUX_POINT {params['FLUX_POINT']}, "
+            f"BREAKUP_MODE {params['BREAKUP_MODE']}, PROC_ID {params['PROC_ID']}, {nev} events")
+
+
 def run_reference(args):
     """CPU restatement of the reference on all host threads, bounded sample."""
     from oracle.oracle import Oracle
@@ -150,7 +156,10 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "sample": sample},
+            "config": {"workload": workload_name(args.workload, params, g["nm"], g["ny"],
+                                                 args.events if args.events is not None
+                                                 else EVENTS[args.workload]),
+                       "sample": sample},
             "init_tables_s": t_init,
             "cpu_baseline": {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
                              "sample": sample},
@@ -401,9 +410,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_tab,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+bf16x3",
         "data": "synthetic (the workload is a parameter set)",
-        "config": {"workload": f"{args.workload}: Pb-Pb {g0['nm']}x{g0['ny']} (m,y) cells, "
-                               f"FLUX_POINT {params['FLUX_POINT']}, BREAKUP_MODE {params['BREAKUP_MODE']}, "
-                               f"PROC_ID {params['PROC_ID']}, {nev} events",
+        "config": {"workload": workload_name(args.workload, params, g0["nm"], g0["ny"], nev),
                    "lumi_method": "fast form (tcgen05 3xBF16 contraction)",
                    "l2": "flushed (256 MB write) before each timed phase"},
         "fast_vs_plain": fvp,
