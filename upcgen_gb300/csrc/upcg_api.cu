@@ -2161,25 +2161,34 @@ int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t*
   auto* rec = reinterpret_cast<EventRecord*>(out);
   int64_t rej = 0;
   int rc = UPCG_OK;
+  // on an error the loop stops, and both streams are drained before returning:
+  // no copy into the caller's buffers outlives the call
+  cudaError_t ce = cudaSuccess;
   for (int64_t off = 0, k = 0; off < n; off += chunk, ++k) {
     const int slot = (int)(k % nslot);
     const int64_t c = std::min(chunk, n - off);
-    if (k >= nslot) CK(cudaStreamWaitEvent(s, g->ev_out[slot], 0));
+    if (k >= nslot) ce = cudaStreamWaitEvent(s, g->ev_out[slot], 0);
+    if (ce != cudaSuccess) break;
     EventRecord* dv = g->evbuf.p + (size_t)slot * chunk;
     int32_t* dm = mbin ? g->mbinbuf.p + (size_t)slot * chunk : nullptr;
     int64_t r = 0;
     rc = g->gen_events_device(c, dv, dm, &r);
     if (rc) break;
     rej += r;
-    CK(cudaEventRecord(g->ev_gen, s));
-    CK(cudaStreamWaitEvent(cs, g->ev_gen, 0));
-    CK(mcpy(rec + off, dv, (size_t)c * sizeof(EventRecord), cudaMemcpyDeviceToHost, cs));
-    if (mbin) CK(mcpy(mbin + off, dm, (size_t)c * sizeof(int32_t), cudaMemcpyDeviceToHost, cs));
-    CK(cudaEventRecord(g->ev_out[slot], cs));
+    ce = cudaEventRecord(g->ev_gen, s);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(cs, g->ev_gen, 0);
+    if (ce == cudaSuccess)
+      ce = mcpy(rec + off, dv, (size_t)c * sizeof(EventRecord), cudaMemcpyDeviceToHost, cs);
+    if (ce == cudaSuccess && mbin)
+      ce = mcpy(mbin + off, dm, (size_t)c * sizeof(int32_t), cudaMemcpyDeviceToHost, cs);
+    if (ce == cudaSuccess) ce = cudaEventRecord(g->ev_out[slot], cs);
+    if (ce != cudaSuccess) break;
   }
-  CK(cudaStreamSynchronize(cs));
-  CK(cudaStreamSynchronize(s));
+  const cudaError_t e_cs = cudaStreamSynchronize(cs), e_s = cudaStreamSynchronize(s);
   if (rc) return rc;
+  if (ce == cudaSuccess) ce = e_cs != cudaSuccess ? e_cs : e_s;
+  if (ce != cudaSuccess)
+    return fail(UPCG_ERR_CUDA, "event output to the host: %s", cudaGetErrorString(ce));
   *rejected = rej;
   g->fidCS = g->totCS * (double)n / (double)(n + rej);  // src/UpcGenerator.cpp:889
   return UPCG_OK;
