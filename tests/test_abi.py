@@ -65,6 +65,32 @@ def test_compute_without_gpu_fails_loudly(ug):
         g.init()
 
 
+def test_output_arrays_checked_on_the_host(ug):
+    """The caller-owned out= arrays of generateEvents / lumiTable / nucCSYM
+    are checked before any library call; page-locked memory needs a GPU."""
+    import numpy as np
+    import torch
+    a = ug._out_array(None, (3, 4))
+    assert a.shape == (3, 4) and a.dtype == np.float64 and not a.any()
+    b = np.zeros((3, 4))
+    assert ug._out_array(b, (3, 4)) is b
+    for bad in (np.zeros((4, 3)), np.zeros((3, 4), dtype=np.float32), np.zeros((3, 8))[:, ::2]):
+        with pytest.raises(ValueError):
+            ug._out_array(bad, (3, 4))
+    ro = np.zeros((3, 4))
+    ro.flags.writeable = False
+    with pytest.raises(ValueError):
+        ug._out_array(ro, (3, 4))
+    g = ug.UpcGenerator({"BINS_M": 3, "BINS_Y": 3})
+    with pytest.raises(ValueError):
+        g.generateEvents(10, out=np.zeros(10, dtype=np.float32))
+    with pytest.raises(ValueError):
+        g.generateEvents(10, out=np.zeros(5, dtype=ug.EVENT_DTYPE))
+    if not torch.cuda.is_available():
+        with pytest.raises(ug.UpcgError):
+            ug.pinned_array(16, ug.EVENT_DTYPE)
+
+
 FACADE_PROGRAM = r"""
 #include <cstdio>
 #include "upcgen_gb300.hpp"
