@@ -7,8 +7,9 @@
 //
 // Differences from the reference's classes:
 //   * errors throw upcgen_gb300::Error (the reference exits the process);
-//   * generateEvents() does not write ROOT/HepMC files; generateEvents(n)
-//     returns the accepted events, and eventRecords(n) the raw 48-byte records;
+//   * generateEvents(n) returns the accepted events and eventRecords(n) the
+//     raw 48-byte records; writeEvents(path, n, format) writes them as the
+//     reference's HepMC3 text or as the particles tree's columns;
 //   * setSeed() seeds the Philox event stream (the reference reseeds gRandom).
 #ifndef UPCGEN_GB300_HPP_
 #define UPCGEN_GB300_HPP_
@@ -105,6 +106,16 @@ class UpcGenerator {
     return accepted;
   }
   const std::vector<Particle>& getParticles() const { return genParticles_; }
+
+  // The reference's generateEvents with its file output (src/UpcGenerator.cpp:
+  // 834-926): n events to path, format 0 = HepMC3 text (events.hepmc), 1 = the
+  // particles tree as a column file (events.root via particles_to_root.C);
+  // threads formatting on the host (0 = every core).  Returns the rejected count.
+  int64_t writeEvents(const std::string& path, int64_t n, int format = 0, int threads = 0) {
+    int64_t rej = 0;
+    check(upcg_write_events(h_, path.c_str(), n, format, threads, &rej));
+    return rej;
+  }
 
   // The first n accepted events of the candidate sequence (the reference's
   // loop without the file output); *rejected gets the rejected count.

@@ -108,7 +108,13 @@ int main() {
   } catch (const Error& e) {
     thrown = e.code() == UPCG_ERR_ARG;
   }
-  std::printf("%d %d %d\n", pdg, charged, thrown);
+  int bad_format = 0;  // writeEvents: formats 0 (HepMC3) and 1 (columns) only
+  try {
+    gen.writeEvents("events.out", 1, 7);
+  } catch (const Error& e) {
+    bad_format = e.code() == UPCG_ERR_ARG;
+  }
+  std::printf("%d %d %d %d\n", pdg, charged, thrown, bad_format);
   return 0;
 }
 """
@@ -132,4 +138,4 @@ def test_cpp_facade_compiles_and_configures(ug, tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stderr
-    assert out.stdout.split() == ["13", "1", "1"]
+    assert out.stdout.split() == ["13", "1", "1", "1"]
