@@ -126,6 +126,8 @@ int upcg_set_lumi_table(upcg_generator* g, const double* table, size_t n, const 
 /* start the candidate sequence of the event entries at this Philox counter
  * (after upcg_init, which resets it to 0): disjoint ranges per shard */
 int upcg_set_candidate_offset(upcg_generator* g, uint64_t counter);
+/* the Philox counter the next event entry starts at */
+int upcg_get_candidate_offset(const upcg_generator* g, uint64_t* counter);
 
 /* ---- tables ------------------------------------------------------------ */
 /* hD2LDMDY of prepareTwoPhotonLumi (src/UpcCrossSection.cpp:506-571):
@@ -227,6 +229,11 @@ int upcg_decay_pdg(upcg_generator* g, int* pdg);
  * 23, mother 0, momentum = the photons' sum; two photons: pdg 22, status 33,
  * mother 1). */
 int upcg_particles_per_event(upcg_generator* g, int* n);
+/* NEVENTS, USE_ROOT_OUTPUT and USE_HEPMC_OUTPUT as configured: the event
+ * count and the files of the reference's generateEvents() (src/UpcGenerator.cpp:
+ * 185-187, 284-289, 834-926) */
+int upcg_event_output_config(const upcg_generator* g, int64_t* nevents, int* use_root,
+                             int* use_hepmc);
 /* Columns of the reference's ROOT tree "particles" (:842-853), one row per
  * particle, row = event * particles_per_event + (particleID - 1). */
 typedef struct upcg_particle_columns {

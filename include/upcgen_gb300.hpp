@@ -7,9 +7,10 @@
 //
 // Differences from the reference's classes:
 //   * errors throw upcgen_gb300::Error (the reference exits the process);
-//   * generateEvents(n) returns the accepted events and eventRecords(n) the
-//     raw 48-byte records; writeEvents(path, n, format) writes them as the
-//     reference's HepMC3 text or as the particles tree's columns;
+//   * generateEvents() writes NEVENTS events as the reference does, with the
+//     particles tree as a column file (events.cols) in place of events.root;
+//     generateEvents(n) returns the accepted events and eventRecords(n) the
+//     raw 48-byte records; writeEvents(path, n, format) writes one file;
 //   * setSeed() seeds the Philox event stream (the reference reseeds gRandom).
 #ifndef UPCGEN_GB300_HPP_
 #define UPCGEN_GB300_HPP_
@@ -115,6 +116,22 @@ class UpcGenerator {
     int64_t rej = 0;
     check(upcg_write_events(h_, path.c_str(), n, format, threads, &rej));
     return rej;
+  }
+
+  // The reference's generateEvents() itself: NEVENTS events to events.hepmc
+  // (USE_HEPMC_OUTPUT) and to the particles tree's column file events.cols
+  // (USE_ROOT_OUTPUT), in the working directory, the same events in both.
+  void generateEvents() {
+    int64_t n = 0;
+    int use_root = 0, use_hepmc = 0;
+    check(upcg_event_output_config(h_, &n, &use_root, &use_hepmc));
+    uint64_t c0 = 0;
+    check(upcg_get_candidate_offset(h_, &c0));
+    if (use_hepmc) writeEvents("events.hepmc", n, 0);
+    if (use_root) {
+      if (use_hepmc) check(upcg_set_candidate_offset(h_, c0));
+      writeEvents("events.cols", n, 1);
+    }
   }
 
   // The first n accepted events of the candidate sequence (the reference's

@@ -65,6 +65,23 @@ def test_compute_without_gpu_fails_loudly(ug):
         g.init()
 
 
+def test_event_output_config(ug, tmp_path):
+    """NEVENTS, USE_ROOT_OUTPUT, USE_HEPMC_OUTPUT (src/UpcGenerator.cpp:185-187,
+    284-289) from a parameter file; they leave the tables valid."""
+    p = tmp_path / "parameters.in"
+    p.write_text("NEVENTS 12345\nUSE_HEPMC_OUTPUT 1\nBINS_M 5\n")
+    g = ug.UpcGenerator()
+    assert g.eventOutputConfig() == (1000, 0, 0)  # the reference's defaults
+    g.setParFile(str(p))
+    g.configGeneratorFromFile()
+    assert g.eventOutputConfig() == (12345, 0, 1)
+    g.setParameterValue("USE_ROOT_OUTPUT", "1")
+    assert g.eventOutputConfig() == (12345, 1, 1)
+    assert g.candidateOffset() == 0
+    with pytest.raises(ug.UpcgError):
+        g.setParameterValue("NEVENTS", "lots")
+
+
 def test_output_arrays_checked_on_the_host(ug):
     """The caller-owned out= arrays of generateEvents / lumiTable / nucCSYM
     are checked before any library call; page-locked memory needs a GPU."""
@@ -114,6 +131,7 @@ int main() {
   } catch (const Error& e) {
     bad_format = e.code() == UPCG_ERR_ARG;
   }
+  gen.generateEvents();  // no USE_*_OUTPUT set: the reference writes no file either
   std::printf("%d %d %d %d\n", pdg, charged, thrown, bad_format);
   return 0;
 }

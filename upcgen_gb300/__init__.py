@@ -41,6 +41,7 @@ ABI_SYMBOLS = [
     "upcg_selftest_contract", "upcg_fast_flux_table", "upcg_kernel_launches",
     "upcg_flux_form_device_noalloc", "upcg_copy_bytes", "upcg_particle_pdg",
     "upcg_set_row_range", "upcg_set_lumi_table", "upcg_set_candidate_offset",
+    "upcg_get_candidate_offset", "upcg_event_output_config",
     "upcg_mlp_create", "upcg_mlp_destroy", "upcg_mlp_box", "upcg_mlp_make_data",
     "upcg_mlp_get_data", "upcg_mlp_train", "upcg_mlp_gradients", "upcg_mlp_params",
     "upcg_mlp_set_params", "upcg_mlp_predict", "upcg_mlp_timings", "upcg_set_flux_surrogate",
@@ -106,6 +107,8 @@ def load_library(path=None):
         "upcg_particle_pdg": [vp, C.POINTER(i), C.POINTER(i)],
         "upcg_set_row_range": [vp, i, i], "upcg_set_lumi_table": [vp, vp, sz, vp],
         "upcg_set_candidate_offset": [vp, u64],
+        "upcg_get_candidate_offset": [vp, C.POINTER(u64)],
+        "upcg_event_output_config": [vp, C.POINTER(i64), C.POINTER(i), C.POINTER(i)],
         "upcg_mlp_create": [C.POINTER(vp), u64], "upcg_mlp_destroy": [vp],
         "upcg_mlp_box": [vp, vp, sz], "upcg_mlp_make_data": [vp, i64, u64],
         "upcg_mlp_get_data": [vp, i64, i64, vp, vp, vp],
@@ -584,6 +587,35 @@ class UpcGenerator:
         _check(self._L.upcg_format_hepmc3(self._h, _p(ev), len(ev), int(first_event), buf, len(buf),
                                           C.byref(n)))
         return buf.raw[:n.value].decode()
+
+    def eventOutputConfig(self):
+        """(NEVENTS, USE_ROOT_OUTPUT, USE_HEPMC_OUTPUT) as configured."""
+        n, r, h = C.c_int64(), C.c_int(), C.c_int()
+        _check(self._L.upcg_event_output_config(self._h, C.byref(n), C.byref(r), C.byref(h)))
+        return n.value, r.value, h.value
+
+    def candidateOffset(self):
+        """The Philox counter the next event entry starts at."""
+        c = C.c_uint64()
+        _check(self._L.upcg_get_candidate_offset(self._h, C.byref(c)))
+        return c.value
+
+    def generateEventFiles(self, directory="."):
+        """The reference's generateEvents() (src/UpcGenerator.cpp:834-926):
+        NEVENTS events to events.hepmc (USE_HEPMC_OUTPUT) and to the particles
+        tree's column file events.cols (USE_ROOT_OUTPUT; particles_to_root.C
+        makes events.root); both files hold the same events.  Returns the
+        rejected count, or None when no output is configured."""
+        n, use_root, use_hepmc = self.eventOutputConfig()
+        c0 = self.candidateOffset()
+        rej = None
+        if use_hepmc:
+            rej = self.writeEvents(os.path.join(directory, "events.hepmc"), n, "hepmc")
+        if use_root:
+            if use_hepmc:
+                self.setCandidateOffset(c0)
+            rej = self.writeEvents(os.path.join(directory, "events.cols"), n, "columns")
+        return rej
 
     def writeEvents(self, path, n, format="hepmc", threads=0):
         """generateEvents with file output (HepMC3 ASCII, or the particle

@@ -261,6 +261,7 @@ struct upcg_generator {
   bool doPtCut = false, doEtaCut = false;
   double minPt = 0, minEta = 0, maxEta = 0;
   long seed = 0, nEvents = 1000;
+  int useROOTOut = 0, useHepMCOut = 0;  // generateEvents' files (src/UpcGenerator.cpp:284-289)
   int numThreads = 1, debug = 0;
   std::string lumiDir = ".";
   bool lumiCache = false;
@@ -472,8 +473,11 @@ struct upcg_generator {
 int upcg_generator::set_param(const std::string& k, const std::string& v) {
   // src/UpcGenerator.cpp:183-305
   try {
-    if (k == "NEVENTS") nEvents = std::stol(v);
-    else if (k == "SQRTS") { sqrts = std::stod(v); g1 = g2 = sqrts / (2. * kMProt); }
+    // keys of the event loop alone: no table depends on them
+    if (k == "NEVENTS") { nEvents = std::stol(v); return UPCG_OK; }
+    if (k == "USE_ROOT_OUTPUT") { useROOTOut = std::stoi(v); return UPCG_OK; }
+    if (k == "USE_HEPMC_OUTPUT") { useHepMCOut = std::stoi(v); return UPCG_OK; }
+    if (k == "SQRTS") { sqrts = std::stod(v); g1 = g2 = sqrts / (2. * kMProt); }
     else if (k == "PROC_ID") procID = std::stoi(v);
     else if (k == "LEP_A") aLep = std::stod(v);
     else if (k == "ALP_MASS") alpMass = std::stod(v);
@@ -2320,6 +2324,21 @@ int upcg_set_candidate_offset(upcg_generator* g, uint64_t counter) {
   g->ev_batch.clear();
   g->ev_flag.clear();
   g->ev_pos = 0;
+  return UPCG_OK;
+}
+
+int upcg_event_output_config(const upcg_generator* g, int64_t* nevents, int* use_root,
+                             int* use_hepmc) {
+  if (!g || !nevents || !use_root || !use_hepmc) return fail(UPCG_ERR_ARG, "null argument");
+  *nevents = g->nEvents;
+  *use_root = g->useROOTOut;
+  *use_hepmc = g->useHepMCOut;
+  return UPCG_OK;
+}
+
+int upcg_get_candidate_offset(const upcg_generator* g, uint64_t* counter) {
+  if (!g || !counter) return fail(UPCG_ERR_ARG, "null argument");
+  *counter = g->next_cand;
   return UPCG_OK;
 }
 
