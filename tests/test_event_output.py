@@ -168,3 +168,22 @@ def test_particles_root_macro(tmp_path):
         v = line.split()
         assert [int(x) for x in v[:5]] == [int(cols[c][r_]) for c in eo.COLUMNS[:5]]
         assert [float.fromhex(x) for x in v[5:]] == [float(cols[c][r_]) for c in eo.COLUMNS[5:]]
+
+
+@pytest.mark.parametrize("proc,dpdg", [(13, 0), (15, 0), (51, 0), (443, 13), (553, 2212)])
+def test_particle_lists(ug, proc, dpdg):
+    """particlesOf / getParticles against the restatement of generateEvent's
+    lists above and against the HepMC3 text of the same records."""
+    g = ug.UpcGenerator({"PROC_ID": proc, "DECAY_PDG": dpdg})
+    assert g.getParticles() == []
+    ev = _records(ug, 300, proc + 1)
+    events, rows = eo.read_hepmc3(g.formatHepMC3(ev))
+    ppe = g.particlesPerEvent()
+    pdg = 51 if proc == 51 else proc
+    for k, e in enumerate(ev):
+        got = g.particlesOf(e)
+        pdgs, sts, mos, ps = _particles(e, pdg, True, dpdg)
+        assert [p[0] for p in got] == pdgs
+        assert [p[1] for p in got] == sts and [p[2] for p in got] == mos
+        assert all(tuple(q) == tuple(r) for (_, _, _, q), r in zip(got, ps))
+        assert [int(x) for x in rows[k * ppe:(k + 1) * ppe, 2]] == pdgs

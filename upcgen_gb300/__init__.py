@@ -631,7 +631,38 @@ class UpcGenerator:
         ev = np.zeros(1, dtype=EVENT_DTYPE)
         acc = C.c_int()
         _check(self._L.upcg_generate_event(self._h, _p(ev), C.byref(acc)))
+        self._last_record = ev[0]
         return acc.value, ev[0]
+
+    def particlePDG(self):
+        """(PDG code of the final state, whether it is charged)."""
+        p, q = C.c_int(), C.c_int()
+        _check(self._L.upcg_particle_pdg(self._h, C.byref(p), C.byref(q)))
+        return p.value, bool(q.value)
+
+    def particlesOf(self, rec):
+        """generateEvent's particle lists for one record (src/UpcGenerator.cpp:
+        767-812): [(pdg, status, mother, (px, py, pz, e))].  A lepton pair: two
+        leptons, status 23, mother 0, opposite charges by the record's sign; an
+        ALP or a vector meson: the parent (status 23, momentum = the daughters'
+        sum) and its two daughters (status 33, mother 1)."""
+        pdg, charged = self.particlePDG()
+        a = tuple(float(x) for x in rec["p0"])
+        b = tuple(float(x) for x in rec["p1"])
+        s1 = 1 if rec["sign"] > 0 else -1
+        if self.particlesPerEvent() == 3:
+            dpdg = self.decayPDG()
+            d1, d2 = (22, 22) if dpdg == 22 else (s1 * dpdg, -s1 * dpdg)
+            parent = tuple(a[i] + b[i] for i in range(4))
+            return [(pdg, 23, 0, parent), (d1, 33, 1, a), (d2, 33, 1, b)]
+        if not charged:
+            return [(pdg, 23, 0, a), (pdg, 23, 0, b)]
+        return [(s1 * pdg, 23, 0, a), (-s1 * pdg, 23, 0, b)]
+
+    def getParticles(self):
+        """The particles of the last generateEvent (UpcGenerator::getParticles)."""
+        rec = getattr(self, "_last_record", None)
+        return [] if rec is None else self.particlesOf(rec)
 
     def timings(self):
         v = (C.c_double * 8)()
