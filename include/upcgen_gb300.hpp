@@ -235,6 +235,42 @@ class UpcCrossSection {
     check(upcg_two_photon_lumi(h_, m.data(), y.data(), out.data(), nullptr, m.size()));
     return out;
   }
+  // calcTwoPhotonLumiPol (src/UpcCrossSection.cpp:274-335): the scalar
+  // luminosity into the result, the pseudoscalar one into *ps
+  std::vector<double> calcTwoPhotonLumiPol(const std::vector<double>& m,
+                                           const std::vector<double>& y, std::vector<double>* ps) {
+    if (m.size() != y.size()) throw Error(UPCG_ERR_ARG, "m and y differ in length");
+    if (!ps) throw Error(UPCG_ERR_ARG, "no pseudoscalar output");
+    std::vector<double> out(m.size());
+    ps->assign(m.size(), 0.);
+    check(upcg_two_photon_lumi(h_, m.data(), y.data(), out.data(), ps->data(), m.size()));
+    return out;
+  }
+  // the elementary process's sigma(m) (flag 0 unpolarized, 1 scalar, 2
+  // pseudoscalar; src/UpcTwoPhotonDilep.cpp:46-122, src/UpcTwoPhotonALP.cpp:28-33)
+  std::vector<double> calcCrossSectionM(const std::vector<double>& m, int flag = 0) {
+    std::vector<double> out(m.size());
+    check(upcg_cs_m(h_, m.data(), flag, out.data(), m.size()));
+    return out;
+  }
+  // fillCrossSectionZM (src/UpcCrossSection.cpp:337-362): [nm][nz]
+  std::vector<double> fillCrossSectionZM(size_t n, int flag = 0) {
+    std::vector<double> out(n);
+    check(upcg_cs_zm_table(h_, flag, out.data(), n));
+    return out;
+  }
+  // calcPhotonFlux (src/UpcCrossSection.cpp:700-722) at points (m, y)
+  std::vector<double> calcPhotonFlux(const std::vector<double>& m, const std::vector<double>& y) {
+    return pts2(m, y, &upcg_photon_flux);
+  }
+  // calcNucCrossSectionY (src/UpcCrossSection.cpp:724-748): dsigma/dy [ny],
+  // the emitter ratio into *ratio (may be null), the total (mb) into *tot_mb
+  std::vector<double> calcNucCrossSectionY(size_t ny, std::vector<double>* ratio, double* tot_mb) {
+    std::vector<double> out(ny);
+    if (ratio) ratio->assign(ny, 0.);
+    check(upcg_nuc_cs_y(h_, out.data(), ratio ? ratio->data() : nullptr, ny, tot_mb));
+    return out;
+  }
   // hD2LDMDY of prepareTwoPhotonLumi: [nm][ny], L dm dy
   std::vector<double> lumiTable(size_t n) {
     std::vector<double> out(n);

@@ -384,6 +384,20 @@ class UpcCrossSection:
         _check(self._g._L.upcg_cs_m(self._g._h, _p(m), int(flag), _p(out), out.size))
         return out
 
+    def fillCrossSectionZM(self, flag=0):  # src/UpcCrossSection.cpp:337-362, [nm][nz]
+        return self._g.crossSectionZM(flag)
+
+    def calcNucCrossSectionYM(self, out=None):  # src/UpcCrossSection.cpp:594-698
+        """(dsigma [ny][nm] in nb, sigma_tot in mb)."""
+        return self._g.nucCSYM(out=out)
+
+    def calcPhotonFlux(self, m, y):  # src/UpcCrossSection.cpp:700-722
+        return self._g.calcPhotonFlux(m, y)
+
+    def calcNucCrossSectionY(self):  # src/UpcCrossSection.cpp:724-748
+        """(dsigma/dy [ny], emitter ratio [ny], sigma_tot mb) of a vector meson."""
+        return self._g.nucCSY()
+
 
 class UpcGenerator:
     """Mirror of upcgen's UpcGenerator (include/UpcGenerator.h:55-128)."""
