@@ -132,7 +132,15 @@ int main() {
     bad_format = e.code() == UPCG_ERR_ARG;
   }
   gen.generateEvents();  // no USE_*_OUTPUT set: the reference writes no file either
-  std::printf("%d %d %d %d\n", pdg, charged, thrown, bad_format);
+  int not_vm = 0;  // calcNucCrossSectionY is the photonuclear path's
+  try {
+    UpcCrossSection cs(gen);
+    double tot = 0;
+    cs.calcNucCrossSectionY(5, nullptr, &tot);
+  } catch (const Error& e) {
+    not_vm = e.code() == UPCG_ERR_PROCESS;
+  }
+  std::printf("%d %d %d %d %d\n", pdg, charged, thrown, bad_format, not_vm);
   return 0;
 }
 """
@@ -156,4 +164,4 @@ def test_cpp_facade_compiles_and_configures(ug, tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stderr
-    assert out.stdout.split() == ["13", "1", "1", "1"]
+    assert out.stdout.split() == ["13", "1", "1", "1", "1"]
