@@ -123,6 +123,11 @@ int upcg_set_row_range(upcg_generator* g, int im0, int im1);
  * pseudoscalar one in table2 when polarized) and build the cross section and
  * samplers from it (upcg_compute_nucl_xsection) */
 int upcg_set_lumi_table(upcg_generator* g, const double* table, size_t n, const double* table2);
+/* the same from device memory of the handle's GPU (a table all-gathered
+ * on the device); the copies run on the handle's stream, which is
+ * synchronised before the call returns */
+int upcg_set_lumi_table_device(upcg_generator* g, const double* table_device, size_t n,
+                               const double* table2_device);
 /* start the candidate sequence of the event entries at this Philox counter
  * (after upcg_init, which resets it to 0): disjoint ranges per shard */
 int upcg_set_candidate_offset(upcg_generator* g, uint64_t counter);
@@ -149,9 +154,10 @@ int upcg_flux_point(upcg_generator* g, const double* b, const double* k, double*
 int upcg_flux_form(upcg_generator* g, const double* b, const double* k, double* out, size_t n);
 /* No counterpart in the reference.  upcg_flux_form on DEVICE buffers without
  * any device-memory allocation: for callers that may not allocate once they
- * run -- code inside a larger CUDA stream capture, where an allocation would
- * break or serialise the capture, and applications whose memory pool owns all
- * HBM after start-up, where a driver allocation fails or evicts the pool.
+ * run -- applications whose memory pool takes all of HBM at start-up, where a
+ * driver allocation later fails or forces the pool to give memory back, and
+ * hosts that grant a library a fixed device budget at start and forbid
+ * cudaMalloc afterwards.
  * The QAGS scratch lives in 2.6 MB of static device memory of the library
  * (64 warp workspaces and one statistics word); nothing is allocated here.
  *   - n <= UPCG_NOALLOC_MAX_POINTS, else UPCG_ERR_SIZE;
@@ -266,6 +272,12 @@ int upcg_format_hepmc3(upcg_generator* g, const upcg_event* ev, int64_t n, int64
  * work of the current one.  Sets fidNuclX over the n events. */
 int upcg_write_events(upcg_generator* g, const char* path, int64_t n, int format, int threads,
                       int64_t* rejected);
+/* The loop of the reference's generateEvents() with no file configured
+ * (USE_ROOT_OUTPUT 0 and USE_HEPMC_OUTPUT 0, src/UpcGenerator.cpp:866-889):
+ * the next n accepted events are drawn on the device and dropped, so that the
+ * candidate sequence advances, *rejected counts the rejected candidates and
+ * fidNuclX = totNuclX n / (n + rejected), as after the reference's loop. */
+int upcg_run_events(upcg_generator* g, int64_t n, int64_t* rejected);
 
 /* UpcGenerator::generateEvent, src/UpcGenerator.cpp:715-832: one candidate.
  * Returns 1 (accepted) or 0 (rejected by the cuts) in *accepted and the

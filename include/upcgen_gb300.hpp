@@ -120,11 +120,18 @@ class UpcGenerator {
 
   // The reference's generateEvents() itself: NEVENTS events to events.hepmc
   // (USE_HEPMC_OUTPUT) and to the particles tree's column file events.cols
-  // (USE_ROOT_OUTPUT), in the working directory, the same events in both.
+  // (USE_ROOT_OUTPUT, on unless set to 0), in the working directory, the same
+  // events in both.  With neither file the loop still runs: the events are
+  // drawn and dropped, and fidNuclX() is set as after the reference's loop.
   void generateEvents() {
     int64_t n = 0;
     int use_root = 0, use_hepmc = 0;
     check(upcg_event_output_config(h_, &n, &use_root, &use_hepmc));
+    if (!use_root && !use_hepmc) {
+      int64_t rej = 0;
+      check(upcg_run_events(h_, n, &rej));
+      return;
+    }
     uint64_t c0 = 0;
     check(upcg_get_candidate_offset(h_, &c0));
     if (use_hepmc) writeEvents("events.hepmc", n, 0);

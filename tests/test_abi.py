@@ -71,12 +71,14 @@ def test_event_output_config(ug, tmp_path):
     p = tmp_path / "parameters.in"
     p.write_text("NEVENTS 12345\nUSE_HEPMC_OUTPUT 1\nBINS_M 5\n")
     g = ug.UpcGenerator()
-    assert g.eventOutputConfig() == (1000, 0, 0)  # the reference's defaults
+    # the reference's defaults: NEVENTS 1000, useROOTOut true, useHepMCOut
+    # false (include/UpcGenerator.h:135-136)
+    assert g.eventOutputConfig() == (1000, 1, 0)
     g.setParFile(str(p))
     g.configGeneratorFromFile()
-    assert g.eventOutputConfig() == (12345, 0, 1)
-    g.setParameterValue("USE_ROOT_OUTPUT", "1")
     assert g.eventOutputConfig() == (12345, 1, 1)
+    g.setParameterValue("USE_ROOT_OUTPUT", "0")
+    assert g.eventOutputConfig() == (12345, 0, 1)
     assert g.candidateOffset() == 0
     with pytest.raises(ug.UpcgError):
         g.setParameterValue("NEVENTS", "lots")
@@ -131,7 +133,14 @@ int main() {
   } catch (const Error& e) {
     bad_format = e.code() == UPCG_ERR_ARG;
   }
-  gen.generateEvents();  // no USE_*_OUTPUT set: the reference writes no file either
+  // no file configured: the loop still needs the tables of init()
+  gen.setParameterValue("USE_ROOT_OUTPUT", "0");
+  int no_init = 0;
+  try {
+    gen.generateEvents();
+  } catch (const Error& e) {
+    no_init = e.code() == UPCG_ERR_STATE;
+  }
   int not_vm = 0;  // calcNucCrossSectionY is the photonuclear path's
   try {
     UpcCrossSection cs(gen);
@@ -140,7 +149,7 @@ int main() {
   } catch (const Error& e) {
     not_vm = e.code() == UPCG_ERR_PROCESS;
   }
-  std::printf("%d %d %d %d %d\n", pdg, charged, thrown, bad_format, not_vm);
+  std::printf("%d %d %d %d %d %d\n", pdg, charged, thrown, bad_format, not_vm, no_init);
   return 0;
 }
 """
@@ -164,4 +173,4 @@ def test_cpp_facade_compiles_and_configures(ug, tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stderr
-    assert out.stdout.split() == ["13", "1", "1", "1", "1"]
+    assert out.stdout.split() == ["13", "1", "1", "1", "1", "1"]

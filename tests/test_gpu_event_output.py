@@ -113,3 +113,31 @@ def test_pinned_out_buffer(ug):
     with pytest.raises(ValueError):
         g.generateEvents(10, out=np.zeros(10, dtype=np.float32))
     del ev, buf  # frees the page-locked block
+
+
+@pytest.mark.parametrize("flags", [(1, 1), (0, 0)], ids=["both-files", "no-file"])
+def test_generate_event_files(ug, tmp_path, monkeypatch, flags):
+    """The reference's generateEvents() (src/UpcGenerator.cpp:834-926) from the
+    parameter keys: with USE_HEPMC_OUTPUT and USE_ROOT_OUTPUT both files hold
+    the events generateEvents(n) gives for the same seed (the candidate
+    sequence is rewound between them); with neither the loop still runs, so
+    fidNuclX, the rejected count and the next candidate match."""
+    use_root, use_hepmc = flags
+    monkeypatch.chdir(tmp_path)
+    n = 1000
+    params = dict(C2S, NEVENTS=n, USE_ROOT_OUTPUT=use_root, USE_HEPMC_OUTPUT=use_hepmc)
+    g, ref = _pair(ug, params)
+    rej = g.generateEventFiles()
+    ev, rej_ref = ref.generateEvents(n)
+    assert rej == rej_ref
+    assert g.fidNuclX() == ref.fidNuclX()
+    assert g.fidNuclX() == g.totNuclX() * n / (n + rej_ref)
+    assert g.candidateOffset() == ref.candidateOffset()
+    if use_hepmc:
+        assert (tmp_path / "events.hepmc").read_text() == HEAD + ref.formatHepMC3(ev, 0) + TAIL
+    if use_root:
+        c = eo.read_particle_columns(tmp_path / "events.cols")
+        p0 = ev["p0"].astype(np.float64)
+        assert np.array_equal(c["px"][0::2], p0[:, 0]) and np.array_equal(c["e"][0::2], p0[:, 3])
+    if not use_root and not use_hepmc:
+        assert not (tmp_path / "events.hepmc").exists() and not (tmp_path / "events.cols").exists()

@@ -105,3 +105,23 @@ def test_cache_off_by_default(ug, tmp_path):
     g.init()
     assert g.lumiCacheFile()[1] == -1
     assert os.listdir(tmp_path) == []
+
+
+def test_lock_of_another_host(ug, tmp_path, monkeypatch):
+    """A lock written by a process of another host (a shared luminosity
+    directory) cannot be checked from here: it is left alone, and at the end
+    of the wait the generator computes the table without writing the file."""
+    monkeypatch.setenv("UPCG_LUMI_LOCK_TIMEOUT", "0.3")
+    probe = ug.UpcGenerator(dict(C1))
+    probe.setLumiFileDirectory(str(tmp_path))
+    fname, _ = probe.lumiCacheFile()
+    with open(fname + ".lock", "w") as f:
+        f.write("some-other-host 1\n")
+    g = _gen(ug, C1, tmp_path)
+    assert g.lumiCacheFile()[1] == 0
+    assert not os.path.exists(fname)
+    assert open(fname + ".lock").read() == "some-other-host 1\n"
+    os.unlink(fname + ".lock")
+    g2 = _gen(ug, C1, tmp_path)
+    assert np.array_equal(g2.lumiTable(), g.lumiTable())
+    assert os.path.exists(fname) and not os.path.exists(fname + ".lock")

@@ -65,3 +65,37 @@ def test_gloo_two_ranks_gather_equals_single(tmp_path):
     got = np.load(out)
     assert got.shape == ref.shape
     assert np.array_equal(got, ref)
+
+
+def _rank_main_pol(rank, world, port, out_path):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from oracle.oracle import Oracle
+    o = Oracle(dict(SMALL, USE_POLARIZED_CS=1), threads=1)
+    o.init_tables()
+    nm = o.grid()["nm"]
+    im0, im1 = shard.row_range(nm, rank, world)
+    s, p = o.lumi_table(im0, im1, polarized=True)
+    full = [shard.gather_rows(t, nm, rank, world) for t in (s, p)]
+    if rank == 0:
+        np.save(out_path, np.stack(full))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_gloo_two_ranks_polarized_pair(tmp_path):
+    """Polarized configurations shard both tables (scalar and pseudoscalar,
+    calcTwoPhotonLumiPol, src/UpcCrossSection.cpp:274-335)."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    from oracle.oracle import Oracle
+    out = str(tmp_path / "pol.npy")
+    mp.start_processes(_rank_main_pol, args=(2, _free_port(), out), nprocs=2, start_method="spawn",
+                       join=True)
+    o = Oracle(dict(SMALL, USE_POLARIZED_CS=1), threads=1)
+    o.init_tables()
+    s, p = o.lumi_table(polarized=True)
+    got = np.load(out)
+    assert np.array_equal(got[0], s) and np.array_equal(got[1], p)

@@ -28,7 +28,7 @@ ABI_SYMBOLS = [
     "upcg_set_collision_system", "upcg_set_seed", "upcg_set_num_threads",
     "upcg_set_debug_level", "upcg_set_lumi_file_directory", "upcg_set_lumi_cache", "upcg_lumi_cache_file",
     "upcg_particles_per_event", "upcg_event_particles_device", "upcg_format_hepmc3",
-    "upcg_write_events", "upcg_photon_flux", "upcg_vm_cross_section_y", "upcg_nuc_cs_y",
+    "upcg_write_events", "upcg_run_events", "upcg_photon_flux", "upcg_vm_cross_section_y", "upcg_nuc_cs_y",
     "upcg_decay_pdg", "upcg_contract_rows",
     "upcg_set_stream", "upcg_set_lumi_method", "upcg_init", "upcg_compute_nucl_xsection",
     "upcg_tot_nucl_x", "upcg_fid_nucl_x", "upcg_get_grid", "upcg_lumi_table",
@@ -40,7 +40,7 @@ ABI_SYMBOLS = [
     "upcg_last_timings", "upcg_qags_stats", "upcg_last_error", "upcg_version",
     "upcg_selftest_contract", "upcg_fast_flux_table", "upcg_kernel_launches",
     "upcg_flux_form_device_noalloc", "upcg_copy_bytes", "upcg_particle_pdg",
-    "upcg_set_row_range", "upcg_set_lumi_table", "upcg_set_candidate_offset",
+    "upcg_set_row_range", "upcg_set_lumi_table", "upcg_set_lumi_table_device", "upcg_set_candidate_offset",
     "upcg_get_candidate_offset", "upcg_event_output_config",
     "upcg_mlp_create", "upcg_mlp_destroy", "upcg_mlp_box", "upcg_mlp_make_data",
     "upcg_mlp_get_data", "upcg_mlp_train", "upcg_mlp_gradients", "upcg_mlp_params",
@@ -80,6 +80,7 @@ def load_library(path=None):
         "upcg_event_particles_device": [vp, vp, i64, i64, vp],
         "upcg_format_hepmc3": [vp, vp, i64, i64, vp, sz, C.POINTER(sz)],
         "upcg_write_events": [vp, cp, i64, i, i, C.POINTER(i64)],
+        "upcg_run_events": [vp, i64, C.POINTER(i64)],
         "upcg_photon_flux": [vp, vp, vp, vp, sz], "upcg_vm_cross_section_y": [vp, vp, vp, sz],
         "upcg_nuc_cs_y": [vp, vp, vp, sz, dp], "upcg_decay_pdg": [vp, C.POINTER(i)],
         "upcg_contract_rows": [vp, C.POINTER(i64)],
@@ -106,6 +107,7 @@ def load_library(path=None):
         "upcg_copy_bytes": [C.POINTER(u64), C.POINTER(u64)],
         "upcg_particle_pdg": [vp, C.POINTER(i), C.POINTER(i)],
         "upcg_set_row_range": [vp, i, i], "upcg_set_lumi_table": [vp, vp, sz, vp],
+        "upcg_set_lumi_table_device": [vp, vp, sz, vp],
         "upcg_set_candidate_offset": [vp, u64],
         "upcg_get_candidate_offset": [vp, C.POINTER(u64)],
         "upcg_event_output_config": [vp, C.POINTER(i64), C.POINTER(i), C.POINTER(i)],
@@ -472,6 +474,19 @@ class UpcGenerator:
         t2 = _arr(table2).ravel() if table2 is not None else None
         _check(self._L.upcg_set_lumi_table(self._h, _p(t), t.size, _p(t2) if t2 is not None else None))
 
+    def setLumiTableDevice(self, ptr, n, ptr2=None):
+        """Install a full table from device memory (raw device pointers to
+        n float64 each; upcg_set_lumi_table_device)."""
+        _check(self._L.upcg_set_lumi_table_device(self._h, C.c_void_p(ptr), int(n),
+                                                  C.c_void_p(ptr2) if ptr2 else None))
+
+    def lumiTableDevicePtrs(self):
+        """(device pointer of the table, of the pseudoscalar table or 0):
+        valid until the next init on this generator."""
+        a, b = C.c_void_p(), C.c_void_p()
+        _check(self._L.upcg_lumi_table_device(self._h, C.byref(a), C.byref(b)))
+        return a.value or 0, b.value or 0
+
     def setFluxSurrogate(self, surrogate):
         self._surrogate = surrogate  # kept alive with the generator
         _check(self._L.upcg_set_flux_surrogate(self._h, surrogate._h if surrogate else None))
@@ -617,10 +632,17 @@ class UpcGenerator:
     def generateEventFiles(self, directory="."):
         """The reference's generateEvents() (src/UpcGenerator.cpp:834-926):
         NEVENTS events to events.hepmc (USE_HEPMC_OUTPUT) and to the particles
-        tree's column file events.cols (USE_ROOT_OUTPUT; particles_to_root.C
-        makes events.root); both files hold the same events.  Returns the
-        rejected count, or None when no output is configured."""
+        tree's column file events.cols (USE_ROOT_OUTPUT, on unless set to 0;
+        particles_to_root.C makes events.root); both files hold the same
+        events.  With neither file configured the loop still runs (the events
+        are drawn and dropped), so the candidate sequence, the rejected count
+        and fidNuclX end where the reference's do.  Returns the rejected
+        count."""
         n, use_root, use_hepmc = self.eventOutputConfig()
+        if not use_root and not use_hepmc:
+            rej = C.c_int64()
+            _check(self._L.upcg_run_events(self._h, int(n), C.byref(rej)))
+            return rej.value
         c0 = self.candidateOffset()
         rej = None
         if use_hepmc:

@@ -261,7 +261,9 @@ struct upcg_generator {
   bool doPtCut = false, doEtaCut = false;
   double minPt = 0, minEta = 0, maxEta = 0;
   long seed = 0, nEvents = 1000;
-  int useROOTOut = 0, useHepMCOut = 0;  // generateEvents' files (src/UpcGenerator.cpp:284-289)
+  // generateEvents' files: the reference writes the particles tree unless
+  // USE_ROOT_OUTPUT says 0 (include/UpcGenerator.h:135-136, src/UpcGenerator.cpp:284-289)
+  int useROOTOut = 1, useHepMCOut = 0;
   int numThreads = 1, debug = 0;
   std::string lumiDir = ".";
   bool lumiCache = false;
@@ -940,6 +942,14 @@ int upcg_generator::build_lumi_grid() {
 // whenever a change moves the values of any luminosity method.
 constexpr int kLumiAlgorithmRevision = 1;
 constexpr double kLumiLockTimeoutS = 600.;
+// the wait for another process's lock: kLumiLockTimeoutS, or UPCG_LUMI_LOCK_TIMEOUT seconds
+double lumi_lock_timeout() {
+  if (const char* env = getenv("UPCG_LUMI_LOCK_TIMEOUT")) {
+    const double t = atof(env);
+    if (t >= 0) return t;
+  }
+  return kLumiLockTimeoutS;
+}
 
 std::string upcg_generator::lumi_cache_key() const {
   // every input of the table, doubles as exact hex floats
@@ -973,7 +983,7 @@ int upcg_generator::build_lumi_cached() {
   const int ntab = usePolarizedCS ? 2 : 1;
   const size_t ncell = (size_t)nm * ny;
   const auto t0 = std::chrono::steady_clock::now();
-  LockGuard lock(path + ".lock", kLumiLockTimeoutS);
+  LockGuard lock(path + ".lock", lumi_lock_timeout());
   std::vector<double> host;
   if (lumi_cache_read(path, key, ntab, nm, ny, host)) {
     cudaStream_t s = st();
@@ -2198,6 +2208,26 @@ int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t*
   return UPCG_OK;
 }
 
+int upcg_run_events(upcg_generator* g, int64_t n, int64_t* rejected) {
+  if (!g || !rejected || n < 0) return fail(UPCG_ERR_ARG, "bad argument");
+  if (n == 0) { *rejected = 0; return UPCG_OK; }
+  if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "upcg_init has not run");
+  // slices of 2^21 events through one device slot, in candidate order
+  const int64_t chunk = std::min<int64_t>(n, (int64_t)1 << 21);
+  CK(g->evbuf.ensure((size_t)chunk));
+  int64_t rej = 0;
+  for (int64_t off = 0; off < n; off += chunk) {
+    int64_t r = 0;
+    const int rc = g->gen_events_device(std::min(chunk, n - off), g->evbuf.p, nullptr, &r);
+    if (rc) return rc;
+    rej += r;
+  }
+  CK(cudaStreamSynchronize(g->st()));
+  *rejected = rej;
+  g->fidCS = g->totCS * (double)n / (double)(n + rej);  // src/UpcGenerator.cpp:889
+  return UPCG_OK;
+}
+
 int upcg_host_alloc(size_t bytes, void** out) {
   if (!out) return fail(UPCG_ERR_ARG, "null argument");
   *out = nullptr;
@@ -2296,7 +2326,9 @@ int upcg_set_row_range(upcg_generator* g, int im0, int im1) {
   return UPCG_OK;
 }
 
-int upcg_set_lumi_table(upcg_generator* g, const double* table, size_t n, const double* table2) {
+namespace {
+int set_lumi_table(upcg_generator* g, const double* table, size_t n, const double* table2,
+                   cudaMemcpyKind kind) {
   if (!g || !table) return fail(UPCG_ERR_ARG, "null argument");
   const size_t ncell = (size_t)g->nm * g->ny;
   if (n != ncell) return fail(UPCG_ERR_SIZE, "table has %zu cells, the grid %zu", n, ncell);
@@ -2307,14 +2339,24 @@ int upcg_set_lumi_table(upcg_generator* g, const double* table, size_t n, const 
   }
   cudaStream_t s = g->st();
   CK(g->lumi.ensure(ncell));
-  CK(mcpy(g->lumi.p, table, ncell * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(mcpy(g->lumi.p, table, ncell * sizeof(double), kind, s));
   if (g->usePolarizedCS) {
     CK(g->lumi2.ensure(ncell));
-    CK(mcpy(g->lumi2.p, table2, ncell * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(mcpy(g->lumi2.p, table2, ncell * sizeof(double), kind, s));
   }
   CK(cudaStreamSynchronize(s));
   g->lumi_ready = true;
   return g->build_xsec();
+}
+}  // namespace
+
+int upcg_set_lumi_table(upcg_generator* g, const double* table, size_t n, const double* table2) {
+  return set_lumi_table(g, table, n, table2, cudaMemcpyHostToDevice);
+}
+
+int upcg_set_lumi_table_device(upcg_generator* g, const double* table_device, size_t n,
+                               const double* table2_device) {
+  return set_lumi_table(g, table_device, n, table2_device, cudaMemcpyDeviceToDevice);
 }
 
 int upcg_set_candidate_offset(upcg_generator* g, uint64_t counter) {

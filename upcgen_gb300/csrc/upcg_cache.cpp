@@ -9,8 +9,11 @@
 // limit.  Here the file name carries a 64-bit FNV-1a hash of a key text that
 // spells out every input of the table (exact hex-float values), the file
 // repeats the full key and a checksum of the payload, and the lock wait is
-// bounded: a lock whose process is gone is removed, and a lock still held at
-// the limit lets this generator compute without writing.
+// bounded.  A lock names its owner as "<host> <pid>": a lock of this host
+// whose process is gone is taken over (renamed away, never unlinked blind), a
+// lock of another host is waited for, a lock still held at the limit lets
+// this generator compute without writing, and a generator removes the lock
+// only while it still names it.  Temporary files carry the host and pid too.
 //
 // File layout (host byte order, every field 8-byte aligned):
 //   char  magic[8]   = "UPCGLUM1"
@@ -28,6 +31,7 @@
 #include <unistd.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -65,18 +69,58 @@ double now_s() {
   return ts.tv_sec + 1e-9 * ts.tv_nsec;
 }
 
-// a lock file holds the decimal pid of its owner; false if that process is gone
-bool lock_owner_alive(const std::string& lock) {
-  FILE* f = fopen(lock.c_str(), "r");
-  if (!f) return true;  // vanished or unreadable: let the caller retry
-  long pid = 0;
-  const int got = fscanf(f, "%ld", &pid);
+// This process as a lock owner: "<host> <pid>" (host name reduced to
+// [A-Za-z0-9.-], so that it is one token).
+std::string owner_id() {
+  char host[256] = {0};
+  if (gethostname(host, sizeof host - 1) != 0) host[0] = 0;
+  std::string h;
+  for (const char* c = host; *c; ++c)
+    h += ((*c >= 'a' && *c <= 'z') || (*c >= 'A' && *c <= 'Z') || (*c >= '0' && *c <= '9') ||
+          *c == '.' || *c == '-')
+             ? *c
+             : '_';
+  if (h.empty()) h = "unknown-host";
+  return h + " " + std::to_string((long)getpid());
+}
+
+std::string host_of(const std::string& id) { return id.substr(0, id.find(' ')); }
+
+bool read_text(const std::string& path, std::string& out) {
+  FILE* f = fopen(path.c_str(), "r");
+  if (!f) return false;
+  char buf[512];
+  const size_t n = fread(buf, 1, sizeof buf - 1, f);
   fclose(f);
-  if (got != 1 || pid <= 0) {
-    // no pid yet: being written, unless its owner died between create and write
+  out.assign(buf, n);
+  while (!out.empty() && (out.back() == '\n' || out.back() == '\r')) out.pop_back();
+  return true;
+}
+
+// A lock file holds "<host> <pid>" of its owner (a bare "<pid>" is read as a
+// lock of this host).  False only when the owner is known to be gone: a lock
+// of this host whose process no longer exists, or one left without an owner
+// for more than 10 s.  A lock of another host (a shared luminosity
+// directory) counts as alive: its process cannot be checked from here, so
+// the waiter's time limit decides.  *content gets the text judged.
+bool lock_owner_alive(const std::string& lock, std::string* content) {
+  std::string txt;
+  if (!read_text(lock, txt)) return true;  // vanished or unreadable: let the caller retry
+  *content = txt;
+  std::string host = host_of(owner_id()), pid_s = txt;
+  const size_t sp = txt.find(' ');
+  if (sp != std::string::npos) {
+    host = txt.substr(0, sp);
+    pid_s = txt.substr(sp + 1);
+  }
+  char* end = nullptr;
+  const long pid = pid_s.empty() ? 0 : strtol(pid_s.c_str(), &end, 10);
+  if (pid <= 0 || (end && *end)) {
+    // no owner yet: being written, unless its owner died between create and write
     struct stat st{};
     return stat(lock.c_str(), &st) != 0 || time(nullptr) - st.st_mtime < 10;
   }
+  if (host != host_of(owner_id())) return true;
   return !(kill((pid_t)pid, 0) != 0 && errno == ESRCH);
 }
 
@@ -121,7 +165,9 @@ int lumi_cache_write(const std::string& path, const std::string& key, int ntab, 
                      const double* data) {
   // write a private temporary file, then rename it over the target: readers
   // see either the old file or the complete new one
-  const std::string tmp = path + ".tmp." + std::to_string((long)getpid());
+  std::string id = owner_id();
+  id[id.find(' ')] = '.';
+  const std::string tmp = path + ".tmp." + id;
   FILE* f = fopen(tmp.c_str(), "wb");
   if (!f) return -1;
   const size_t n = (size_t)ntab * nm * ny;
@@ -142,18 +188,34 @@ int lumi_cache_write(const std::string& path, const std::string& key, int ntab, 
 
 int lumi_lock_acquire(const std::string& lock, double timeout_s) {
   const double t0 = now_s();
+  const std::string me = owner_id();
   for (;;) {
     const int fd = open(lock.c_str(), O_CREAT | O_EXCL | O_WRONLY, 0644);
     if (fd >= 0) {
-      const std::string pid = std::to_string((long)getpid()) + "\n";
-      const ssize_t w = write(fd, pid.data(), pid.size());
+      const std::string line = me + "\n";
+      const ssize_t w = write(fd, line.data(), line.size());
       (void)w;
       close(fd);
       return 1;
     }
     if (errno != EEXIST) return 0;  // directory not writable: run without a lock
-    if (!lock_owner_alive(lock)) {
-      unlink(lock.c_str());  // its owner died while holding it
+    std::string dead;
+    if (!lock_owner_alive(lock, &dead)) {
+      // Take the dead lock out of the way by renaming it to a name of our own
+      // (of two waiters only one rename finds it).  If what was moved is not
+      // the text judged dead, a new owner took the lock meanwhile: put it
+      // back (link fails if yet another lock is there) and drop the copy.
+      std::string grave_id = me;
+      grave_id[grave_id.find(' ')] = '.';
+      const std::string grave = lock + ".stale." + grave_id;
+      if (rename(lock.c_str(), grave.c_str()) == 0) {
+        std::string moved;
+        if (read_text(grave, moved) && moved != dead) {
+          const int rl = link(grave.c_str(), lock.c_str());
+          (void)rl;
+        }
+        unlink(grave.c_str());
+      }
       continue;
     }
     if (now_s() - t0 > timeout_s) return 0;
@@ -161,6 +223,10 @@ int lumi_lock_acquire(const std::string& lock, double timeout_s) {
   }
 }
 
-void lumi_lock_release(const std::string& lock) { unlink(lock.c_str()); }
+// Removes the lock only while it still names this process.
+void lumi_lock_release(const std::string& lock) {
+  std::string txt;
+  if (read_text(lock, txt) && txt == owner_id()) unlink(lock.c_str());
+}
 
 }  // namespace upcg

@@ -15,10 +15,11 @@ int lumi_cache_read(const std::string& path, const std::string& key, int ntab, i
 // 0 on success; written to a temporary file and renamed over path
 int lumi_cache_write(const std::string& path, const std::string& key, int ntab, int nm, int ny,
                      const double* data);
-// 1 when this process holds the lock file, 0 when it could not be had within
-// timeout_s (or the directory refuses it); a lock whose owner process is gone
-// is removed
+// 1 when this process holds the lock file ("<host> <pid>"), 0 when it could
+// not be had within timeout_s (or the directory refuses it); a lock of this
+// host whose owner process is gone is taken over, one of another host waited for
 int lumi_lock_acquire(const std::string& lock, double timeout_s);
+// removes the lock file if it still names this process
 void lumi_lock_release(const std::string& lock);
 
 }  // namespace upcg
