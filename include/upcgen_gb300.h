@@ -284,6 +284,12 @@ int upcg_run_events(upcg_generator* g, int64_t n, int64_t* rejected);
  * event in *ev; candidates are drawn from the same sequence as
  * upcg_generate_events. */
 int upcg_generate_event(upcg_generator* g, upcg_event* ev, int* accepted);
+/* The event kernels' bin functions on given values, as the sampler of
+ * include/UpcSampler.h:124-134 computes them: axis 0 = getBinY of the
+ * (y, m) sampler for masses x (the z sampler and the polarized ratio are
+ * picked with it), axis 1 = getBinX for rapidities x (the polarized pick);
+ * out[i] = the bin, clamped to the grid.  Needs upcg_init. */
+int upcg_sampler_bins(upcg_generator* g, const double* x, size_t n, int axis, int32_t* out);
 
 /* ---- batched scans (no counterpart in the reference: one configuration per
  * process there) ----------------------------------------------------------

@@ -281,14 +281,51 @@ def test_events_sequence_and_bins(ug, oracle_mod):
     b, rb = g.generateEvents(13000)
     assert ra + rb == rej_all
     assert np.array_equal(np.concatenate([a, b]).view(np.uint8), ev_all.view(np.uint8))
-    # getBinY with the reference's truncation, on the stored masses away from
-    # the truncation boundaries
+    # the bins the event kernel used are the bins of the (FP32-stored) masses
+    # wherever the FP32 rounding does not cross a bin edge
+    assert mb.min() >= 0 and mb.max() <= 20
     grid = g.grid()
-    x = 21 * (ev_all["m"].astype(np.float64) - grid["mmin"])
-    ok = np.abs(x - np.round(x)) > 1e-3
-    lo, hi = grid["mmin"], grid["mmin"] + (grid["mmax"] - grid["mmin"]) / 21 * 21
-    ref = np.array([oracle_mod.sampler_bin(21, lo, hi, float(m)) for m in ev_all["m"][ok]])
-    assert np.array_equal(mb[ok], ref)
+    m32 = ev_all["m"].astype(np.float64)
+    dm = (grid["mmax"] - grid["mmin"]) / 21
+    far = np.abs((m32 - grid["mmin"]) / dm - np.round((m32 - grid["mmin"]) / dm)) > 1e-5
+    assert np.array_equal(g.samplerBins(m32[far], "m"), mb[far])
+
+
+def _edge_values(lo, n, d):
+    """Bin edges lo + d i (binEdgesM / binEdgesY, src/UpcGenerator.cpp:677-684),
+    the points where int(n (x - lo)) steps (x = lo + k / n), and 1 and 2 ulps
+    on both sides of each, inside [lo, hi)."""
+    hi = lo + d * n
+    k_max = int(n * (hi - lo)) + 1
+    base = np.concatenate([lo + d * np.arange(n + 1), lo + np.arange(k_max + 1) / n])
+    vals = [base]
+    for direction in (np.inf, -np.inf):
+        x = base
+        for _ in range(2):
+            x = np.nextafter(x, direction)
+            vals.append(x)
+    v = np.unique(np.concatenate(vals))
+    return v[(v >= lo) & (v < hi)], hi
+
+
+@pytest.mark.parametrize("nm,ny", [(201, 61), (1001, 121), (21, 13)])
+def test_sampler_bins_bit_exact_at_edges(ug, oracle_mod, nm, ny):
+    """getBinY / getBinX of the (y, m) sampler (include/UpcSampler.h:124-134,
+    the int() truncating the numerator) as the event kernel computes them,
+    on every bin edge, every step of the truncated numerator and 1-2 ulps on
+    both sides of each: no mismatch with the oracle's restatement."""
+    p = dict(C2S, BINS_M=nm, BINS_Y=ny, FLUX_POINT=1, DO_PT_CUT=0, DO_ETA_CUT=0)
+    g = _gen(ug, p)
+    grid = g.grid()
+    for axis, lo, n, top in (("m", grid["mmin"], nm, grid["mmax"]),
+                             ("y", grid["ymin"], ny, grid["ymax"])):
+        d = (top - lo) / n
+        x, hi = _edge_values(lo, n, d)
+        got = g.samplerBins(x, axis)
+        ref = np.array([oracle_mod.sampler_bin(n, lo, hi, float(v)) for v in x])
+        assert np.all((ref >= 0) & (ref < n))
+        bad = np.flatnonzero(got != ref)
+        assert bad.size == 0, (axis, bad.size, x[bad[:5]], got[bad[:5]], ref[bad[:5]])
 
 
 def test_generate_event_single(ug):

@@ -28,7 +28,7 @@ ABI_SYMBOLS = [
     "upcg_set_collision_system", "upcg_set_seed", "upcg_set_num_threads",
     "upcg_set_debug_level", "upcg_set_lumi_file_directory", "upcg_set_lumi_cache", "upcg_lumi_cache_file",
     "upcg_particles_per_event", "upcg_event_particles_device", "upcg_format_hepmc3",
-    "upcg_write_events", "upcg_run_events", "upcg_photon_flux", "upcg_vm_cross_section_y", "upcg_nuc_cs_y",
+    "upcg_write_events", "upcg_run_events", "upcg_sampler_bins", "upcg_photon_flux", "upcg_vm_cross_section_y", "upcg_nuc_cs_y",
     "upcg_decay_pdg", "upcg_contract_rows",
     "upcg_set_stream", "upcg_set_lumi_method", "upcg_init", "upcg_compute_nucl_xsection",
     "upcg_tot_nucl_x", "upcg_fid_nucl_x", "upcg_get_grid", "upcg_lumi_table",
@@ -81,6 +81,7 @@ def load_library(path=None):
         "upcg_format_hepmc3": [vp, vp, i64, i64, vp, sz, C.POINTER(sz)],
         "upcg_write_events": [vp, cp, i64, i, i, C.POINTER(i64)],
         "upcg_run_events": [vp, i64, C.POINTER(i64)],
+        "upcg_sampler_bins": [vp, vp, sz, i, vp],
         "upcg_photon_flux": [vp, vp, vp, vp, sz], "upcg_vm_cross_section_y": [vp, vp, vp, sz],
         "upcg_nuc_cs_y": [vp, vp, vp, sz, dp], "upcg_decay_pdg": [vp, C.POINTER(i)],
         "upcg_contract_rows": [vp, C.POINTER(i64)],
@@ -661,6 +662,14 @@ class UpcGenerator:
         _check(self._L.upcg_write_events(self._h, str(path).encode(), int(n), int(fmt), int(threads),
                                          C.byref(rej)))
         return rej.value
+
+    def samplerBins(self, x, axis="m"):
+        """The event kernels' getBinY (axis "m") / getBinX (axis "y") of the
+        (y, m) sampler on the values x (include/UpcSampler.h:124-134)."""
+        x = _arr(x).ravel()
+        out = np.zeros(x.size, dtype=np.int32)
+        _check(self._L.upcg_sampler_bins(self._h, _p(x), x.size, {"m": 0, "y": 1}[axis], _p(out)))
+        return out
 
     def generateEvent(self):
         """One candidate: (1 or 0, event record), as UpcGenerator::generateEvent."""

@@ -2208,6 +2208,22 @@ int upcg_generate_events(upcg_generator* g, int64_t n, upcg_event* out, int32_t*
   return UPCG_OK;
 }
 
+int upcg_sampler_bins(upcg_generator* g, const double* x, size_t n, int axis, int32_t* out) {
+  if (!g || !x || !out || axis < 0 || axis > 1) return fail(UPCG_ERR_ARG, "bad argument");
+  if (n == 0) return UPCG_OK;
+  if (n > (size_t)INT32_MAX) return fail(UPCG_ERR_SIZE, "too many values");
+  if (!g->xsec_ready) return fail(UPCG_ERR_STATE, "upcg_init has not run");
+  CK(g->pts_a.ensure(n));
+  CK(g->pts_c.ensure((n + 1) / 2));  // n ints
+  cudaStream_t s = g->st();
+  CK(mcpy(g->pts_a.p, x, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  int* d_out = reinterpret_cast<int*>(g->pts_c.p);
+  CK(launch_sampler_bins(g->event_params(), g->pts_a.p, (int)n, axis, d_out, s));
+  CK(mcpy(out, d_out, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return UPCG_OK;
+}
+
 int upcg_run_events(upcg_generator* g, int64_t n, int64_t* rejected) {
   if (!g || !rejected || n < 0) return fail(UPCG_ERR_ARG, "bad argument");
   if (n == 0) { *rejected = 0; return UPCG_OK; }

@@ -312,6 +312,26 @@ __device__ bool gen_vm(const EventParams& e, const float* __restrict__ pttab, Ca
   return true;
 }
 
+// getBinY of the (y, m) sampler (include/UpcSampler.h:130-133) for the mass:
+// int(nBinsY (m - lo)) / (hi - lo), the int() truncating the numerator, then
+// the return's truncation.  The quotient comes from a table made on the host
+// with that FP64 division for every integer numerator (no FP64 division per
+// candidate); clamped to the mass bins.
+__device__ __forceinline__ int sampler_mbin(const EventParams& e, double m) {
+  const int nnum = (int)(e.nm_d * (m - e.mmin));
+  const int mb = (nnum >= 0 && nnum < e.mbin_lut_n) ? __ldg(e.mbin_lut + nnum)
+                                                    : (int)((double)nnum / (e.medge_hi - e.mmin));
+  return mb < 0 ? 0 : (mb > e.nm - 1 ? e.nm - 1 : mb);
+}
+
+// getBinX of the (y, m) sampler for the rapidity (include/UpcSampler.h:124-128),
+// clamped to the rapidity bins
+__device__ __forceinline__ int sampler_ybin(const EventParams& e, double y) {
+  const double yedge_hi = e.ymin + e.dy * e.ny;
+  const int yb = (int)((double)(int)(e.ny * (y - e.ymin)) / (yedge_hi - e.ymin));
+  return yb < 0 ? 0 : (yb > e.ny - 1 ? e.ny - 1 : yb);
+}
+
 __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ cdf2,
                               const double* __restrict__ cdfz, const float* __restrict__ pttab,
                               uint64_t idx, Cand& c) {
@@ -341,13 +361,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
   }
   c.m = mlo + rb * mw;
   (void)cdf2;
-  // getBinY (include/UpcSampler.h:130-133), the int() truncating the numerator:
-  // int(n / (hi - lo)) of the integer n = int(nm (m - lo)) from a table made
-  // on the host with that FP64 division (no division per candidate)
-  const int nnum = (int)(e.nm_d * (c.m - e.mmin));
-  int mb = (nnum >= 0 && nnum < e.mbin_lut_n) ? __ldg(e.mbin_lut + nnum)
-                                              : (int)((double)nnum / (e.medge_hi - e.mmin));
-  mb = mb < 0 ? 0 : (mb > e.nm - 1 ? e.nm - 1 : mb);
+  const int mb = sampler_mbin(e, c.m);
   c.mbin = mb;
   // z = cos(theta)
   if (!e.ignoreCSZ && !e.polarized) {
@@ -362,9 +376,7 @@ __device__ bool gen_candidate(const EventParams& e, const double* __restrict__ c
     // reference draws Uniform(0, 1) < polCSRatio[yBin][mBin] (getBinX of y, as getBinY)
     const double rz = u53(r1.x, r1.y);
     const double* cz = cdfz + (size_t)mb * (e.nz + 1);
-    const double yedge_hi = e.ymin + e.dy * e.ny;
-    int yb = (int)((double)(int)(e.ny * (c.y - e.ymin)) / (yedge_hi - e.ymin));
-    yb = yb < 0 ? 0 : (yb > e.ny - 1 ? e.ny - 1 : yb);
+    const int yb = sampler_ybin(e, (double)c.y);
     const uint4 r4 = philox4x32_10(make_uint4(clo, chi, 4u, 0x55504347u), key);
     if (!(u53(r4.x, r4.y) < __ldg(e.ratio + (size_t)yb * e.nm + mb)))
       cz = e.cdfz_ps + (size_t)mb * (e.nz + 1);
@@ -874,6 +886,25 @@ cudaError_t launch_scan_tiles(const int* d_count, const uint32_t* d_mask, int64_
                               int64_t* d_total, cudaStream_t st) {
   note_launch();
   k_scan_tiles<<<1, kScanThreads, 0, st>>>(d_count, d_mask, d_off, n, d_total);
+  return cudaGetLastError();
+}
+
+// The event kernels' bin functions on given values (axis 0: sampler_mbin of
+// m, axis 1: sampler_ybin of y), for bit-exact checks against getBinY/getBinX.
+namespace {
+__global__ void k_sampler_bins(EventParams e, const double* __restrict__ x, int n, int axis,
+                               int* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = axis == 0 ? sampler_mbin(e, x[i]) : sampler_ybin(e, x[i]);
+}
+}  // namespace
+
+cudaError_t launch_sampler_bins(const EventParams& e, const double* d_x, int n, int axis,
+                                int* d_out, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  note_launch();
+  k_sampler_bins<<<(n + 255) / 256, 256, 0, st>>>(e, d_x, n, axis, d_out);
   return cudaGetLastError();
 }
 

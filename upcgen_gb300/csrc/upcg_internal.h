@@ -315,6 +315,8 @@ cudaError_t launch_events_copy(const EventRecord* d_stage, const int32_t* d_stag
                                const uint32_t* d_mask, const int64_t* d_tile_off, int64_t tiles,
                                int64_t out_base, int64_t nmax, EventRecord* d_out, int32_t* d_mbin,
                                cudaStream_t st);
+cudaError_t launch_sampler_bins(const EventParams& e, const double* d_x, int n, int axis,
+                                int* d_out, cudaStream_t st);
 cudaError_t launch_events_write(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                                 const float* d_ptcdf, uint64_t cand0, int64_t ncand,
                                 const uint32_t* d_mask, const int64_t* d_tile_off,
