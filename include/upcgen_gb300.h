@@ -91,8 +91,11 @@ int upcg_set_stream(upcg_generator* g, void* stream);
  * 4096-energy x 2048-radius grids, L = N G N^T as two tensor-core products
  * (its own quadrature: the difference to the reference is stated by the tests),
  * 4 = the fast form with the form-factor flux rows inside the learned
- * surrogate's box from the surrogate (upcg_set_flux_surrogate).  With
- * USE_POLARIZED_CS the fast form (1, 4) builds the scalar and pseudoscalar
+ * surrogate's box from the surrogate (upcg_set_flux_surrogate), 5 = the fast
+ * form with the projection and the contraction as two kernels (dense operands
+ * through device memory; the same table as 1 up to FP32 summation order --
+ * methods 1, 2 and 4 build the contraction's operands inside it).  With
+ * USE_POLARIZED_CS the fast form (1, 4, 5) builds the scalar and pseudoscalar
  * tables of calcTwoPhotonLumiPol from the same operands. */
 int upcg_set_lumi_method(upcg_generator* g, int method);
 

@@ -464,7 +464,8 @@ class UpcGenerator:
         _check(self._L.upcg_set_stream(self._h, C.c_void_p(int(stream_handle) if stream_handle else 0)))
 
     def setLumiMethod(self, method):
-        _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1, "hybrid": 2, "grid": 3, "surrogate": 4}.get(method, method)))
+        _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1, "hybrid": 2, "grid": 3, "surrogate": 4,
+                                                                 "staged": 5}.get(method, method)))
 
     # -- sharding over m-rows (upcgen_gb300.shard)
     def setRowRange(self, im0, im1=-1):

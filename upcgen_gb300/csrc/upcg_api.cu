@@ -147,9 +147,11 @@ namespace {
 // tile shapes (256-wide x 2 stages, 128-wide x 3 stages) on synthetic
 // operands of that size, once per process and device, and keeps the faster.
 struct TuneKey {
-  int dev, rows, P;
+  int dev, rows, P, fused;
   bool operator<(const TuneKey& o) const {
-    return dev != o.dev ? dev < o.dev : (rows != o.rows ? rows < o.rows : P < o.P);
+    if (dev != o.dev) return dev < o.dev;
+    if (rows != o.rows) return rows < o.rows;
+    return P != o.P ? P < o.P : fused < o.fused;
   }
 };
 std::mutex g_tune_mu;
@@ -163,13 +165,15 @@ int tune_bucket(int rows) {  // power-of-two buckets of the row count
 }
 }  // namespace
 
-// shape and grid for `rows_pad` stacked rows (nvalid of them valid) at P
-int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid) {
+// shape and grid for `rows_pad` stacked rows (nvalid of them valid) at P, for
+// the staged contraction (fused = 0, dense operands) or the fused one (node
+// lists; timed on synthetic lists shaped like form-factor rows)
+int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid, int fused) {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   *grid = sms;
-  const TuneKey key{dev, tune_bucket(rows_pad), P};
+  const TuneKey key{dev, tune_bucket(rows_pad), P, fused ? 1 : 0};
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tune.find(key);
@@ -181,20 +185,25 @@ int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid) {
   // synthetic operands of the bucket's size, timed with events on a private stream
   const int rows = key.rows;
   DBuf<uint16_t> a, g;
-  DBuf<float> a2, part;
+  DBuf<float> a2, part, nodes;
   DBuf<int4> items;
   DBuf<unsigned> err;
   cudaStream_t s;
   CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  CK(a.ensure((size_t)rows * P));
   CK(g.ensure((size_t)P * P));
-  CK(a2.ensure((size_t)rows * P));
   CK(part.ensure((size_t)rows * (P / 128)));
   CK(err.ensure(1));
-  CK(cudaMemsetAsync(a.p, 0, (size_t)rows * P * 2, s));
   CK(cudaMemsetAsync(g.p, 0, (size_t)P * P * 2, s));
-  CK(cudaMemsetAsync(a2.p, 0, (size_t)rows * P * 4, s));
   CK(cudaMemsetAsync(err.p, 0, 4, s));
+  if (fused) {
+    CK(nodes.ensure((size_t)rows * fast_node_floats_per_row()));
+    CK(launch_fill_nodes_synthetic(nodes.p, rows, s));
+  } else {
+    CK(a.ensure((size_t)rows * P));
+    CK(a2.ensure((size_t)rows * P));
+    CK(cudaMemsetAsync(a.p, 0, (size_t)rows * P * 2, s));
+    CK(cudaMemsetAsync(a2.p, 0, (size_t)rows * P * 4, s));
+  }
   double best = 1e30;
   int pick = 0;
   double t[2] = {0, 0};
@@ -211,8 +220,12 @@ int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid) {
     float ms = 0;
     for (int rep = 0; rep < 3; ++rep) {  // warm-up, then the best of two
       cudaEventRecord(e0, s);
-      CK(launch_contract_pers(a.p, a.p, g.p, g.p, 1, rows, P, items.p, (int)it.size(), a2.p, part.p,
-                              err.p, sh, *grid, s));
+      if (fused)
+        CK(launch_contract_fused(g.p, g.p, 1, rows, P, items.p, (int)it.size(), nodes.p, part.p,
+                                 err.p, sh, *grid, s));
+      else
+        CK(launch_contract_pers(a.p, a.p, g.p, g.p, 1, rows, P, items.p, (int)it.size(), a2.p,
+                                part.p, err.p, sh, *grid, s));
       cudaEventRecord(e1, s);
       CK(cudaEventSynchronize(e1));
       float m = 0;
@@ -340,7 +353,7 @@ struct upcg_generator {
   DBuf<EventRecord> evstage;  // pass 1's accepted records, 256 slots per candidate tile
   DBuf<int32_t> evstage_mbin;
   DBuf<uint16_t> fgh, fgl, fah, fal;  // fast form: bf16 hi/lo of G and of the projections
-  DBuf<float> fa2, fpart;
+  DBuf<float> fa2, fpart, fnodes;
   DBuf<double> ffar, fk1, fq, fqn, fwn, fH, fJ, flnm2, fpartq, fsides, ffc;
   DBuf<double> fk01;        // ln K0 + x, ln K1 + x on the K table's x grid (any gamma)
   DBuf<double> ffc2;        // polarized: the pseudoscalar far constants
@@ -758,7 +771,7 @@ int upcg_generator::build_tables() {
   else
     CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s));
   // form factor on 1e6 knots (the reference's), 65,536 for the fast form
-  ff_n = (lumiMethod == 1 || lumiMethod == 4) ? kNQ2Fast : kNQ2;
+  ff_n = (lumiMethod == 1 || lumiMethod == 4 || lumiMethod == 5) ? kNQ2Fast : kNQ2;
   const double dq = (kQ2max - kQ2min) / ff_n;
   CK(ff_y.ensure(ff_n));
   CK(ff_c.ensure(ff_n));
@@ -771,7 +784,8 @@ int upcg_generator::build_tables() {
     CK(build_spline_uniform(ff_y.p, ff_n, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
   }
   ftab_early = false;
-  if (!cap && !isVM && (lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4)) {
+  if (!cap && !isVM &&
+      (lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4 || lumiMethod == 5)) {
     // the fast form's flux tables need only the form factor: they run here,
     // beside the breakup and G_AA chains
     for (auto& e : ev_ft)
@@ -809,7 +823,7 @@ int upcg_generator::build_tables() {
     // the fast form (methods 1, 4; budget 1e-4) takes the FP32 sums (~1e-6);
     // the reference's sum steps where an energy crosses omax(b), so every
     // knot is summed (an interpolated table smears those steps to 1.5e-5)
-    const int brk_fp32 = (lumiMethod == 1 || lumiMethod == 4) ? 1 : 0;
+    const int brk_fp32 = (lumiMethod == 1 || lumiMethod == 4 || lumiMethod == 5) ? 1 : 0;
     CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
                              1e-6, dbb, brk_y.p, side[1], brk_fp32));
     CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1]));
@@ -1168,9 +1182,13 @@ int upcg_generator::build_lumi() {
   LumiParams p = lumi_params();
   p.mirror = mirror.p;
   // 1: fast form (flux tables + tensor-core contraction); 2: the same
-  // contraction on the plain path's exact node fluxes (QAGS / K0,K1)
-  const bool fast = lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4;
+  // contraction on the plain path's exact node fluxes (QAGS / K0,K1); 5: the
+  // fast form with the projection and the contraction as two kernels (dense
+  // operands through HBM), the others fold the projection into the
+  // contraction (node lists, k_contract_fused)
+  const bool fast = lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4 || lumiMethod == 5;
   const bool node_flux = lumiMethod == 2 || !fast;
+  const bool staged = lumiMethod == 5;
   // cells per chunk: the node-flux paths hold 1.9 KB of node fluxes per cell,
   // the fast form 8 KB of contraction operands; its chunks are larger, so
   // that a table needs fewer persistent contractions (2 GB at 2^18 cells)
@@ -1192,9 +1210,13 @@ int upcg_generator::build_lumi() {
   if (fast) {
     CK(fgh.ensure((size_t)P * P));
     CK(fgl.ensure((size_t)P * P));
-    CK(fah.ensure((size_t)chunk_pad * P));
-    CK(fal.ensure((size_t)chunk_pad * P));
-    CK(fa2.ensure((size_t)chunk_pad * P));
+    if (staged) {
+      CK(fah.ensure((size_t)chunk_pad * P));
+      CK(fal.ensure((size_t)chunk_pad * P));
+      CK(fa2.ensure((size_t)chunk_pad * P));
+    } else {
+      CK(fnodes.ensure((size_t)chunk_pad * fast_node_floats_per_row()));
+    }
     CK(ffar.ensure(2 * (size_t)chunk_pad));  // one float4 per cell
     CK(fsides.ensure((2 * (size_t)chunk * fast_side_bytes() + 7) / 8));
     CK(fpart.ensure((size_t)chunk_pad * (P / 128)));
@@ -1309,12 +1331,13 @@ int upcg_generator::build_lumi() {
       b = mark();
       CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, flnm2.p, c_far,
                              node_flux ? flux.p : nullptr, &ftab, fsides.p, fah.p, fal.p, fa2.p,
-                             ffar.p, s, use_map ? frep.p : nullptr, n_rep, r0));
+                             ffar.p, s, use_map ? frep.p : nullptr, n_rep, r0,
+                             staged ? nullptr : fnodes.p));
       spans.push_back({4, {b, mark()}});
       // persistent contraction over this chunk's (row tile, N tile) work list
       int shape = 0, grid = 0;
       {
-        const int rc = contract_plan(ncp, nc, P, &shape, &grid);
+        const int rc = contract_plan(ncp, nc, P, &shape, &grid, staged ? 0 : 1);
         if (rc) return rc;
       }
       const int tbn = shape == 0 ? 256 : 128;
@@ -1325,12 +1348,20 @@ int upcg_generator::build_lumi() {
       CK(fitems.ensure(items.size()));
       CK(upload(fitems.p, items.data(), items.size() * sizeof(int4), s));
       b = mark();
-      CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(),
-                              fa2.p, fpart.p, ferr.p, shape, grid, s));
+      if (staged)
+        CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p,
+                                (int)items.size(), fa2.p, fpart.p, ferr.p, shape, grid, s));
+      else
+        CK(launch_contract_fused(fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(), fnodes.p,
+                                 fpart.p, ferr.p, shape, grid, s));
       if (usePolarizedCS) {  // the same operands against the pseudoscalar kernel
         CK(fpart2.ensure(fpart.n));
-        CK(launch_contract_pers(fah.p, fal.p, fgh2.p, fgl2.p, 1, ncp, P, fitems.p,
-                                (int)items.size(), fa2.p, fpart2.p, ferr.p, shape, grid, s));
+        if (staged)
+          CK(launch_contract_pers(fah.p, fal.p, fgh2.p, fgl2.p, 1, ncp, P, fitems.p,
+                                  (int)items.size(), fa2.p, fpart2.p, ferr.p, shape, grid, s));
+        else
+          CK(launch_contract_fused(fgh2.p, fgl2.p, 1, ncp, P, fitems.p, (int)items.size(),
+                                   fnodes.p, fpart2.p, ferr.p, shape, grid, s));
       }
       spans.push_back({3, {b, mark()}});
       CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s, ffc.p,
@@ -1709,8 +1740,8 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
 // fold and the samplers.
 struct upcg_scan {
   std::vector<upcg_generator*> gens;
-  DBuf<uint16_t> ah, al, gh, gl;
-  DBuf<float> a2, part;
+  DBuf<uint16_t> gh, gl;
+  DBuf<float> nodes, part;  // node lists of every configuration's rows (stacked)
   DBuf<double> far, fc;
   DBuf<int4> items;
   DBuf<unsigned> err;
@@ -1748,8 +1779,9 @@ int upcg_generator::enqueue_scan_front(upcg_scan& sc, int ci) {
   const size_t r0 = (size_t)sc.row0[ci];
   const int nrows = nm * (fast_nrep > 0 ? fast_nrep : ny);
   CK(launch_fast_project(p, fu0, fh, P, 0, nrows, sc.rows[ci], flnm2.p, 0.0, nullptr, &ft,
-                         fsides.p, sc.ah.p + r0 * P, sc.al.p + r0 * P, sc.a2.p + r0 * P,
-                         sc.far.p + 2 * r0, s, fast_nrep > 0 ? frep.p : nullptr, fast_nrep, 0));
+                         fsides.p, nullptr, nullptr, nullptr, sc.far.p + 2 * r0, s,
+                         fast_nrep > 0 ? frep.p : nullptr, fast_nrep, 0,
+                         sc.nodes.p + r0 * fast_node_floats_per_row()));
   cap = false;
   return UPCG_OK;
 }
@@ -1859,7 +1891,7 @@ int upcg_set_stream(upcg_generator* g, void* stream) {
 }
 
 int upcg_set_lumi_method(upcg_generator* g, int method) {
-  if (!g || method < 0 || method > 4) return fail(UPCG_ERR_ARG, "bad luminosity method");
+  if (!g || method < 0 || method > 5) return fail(UPCG_ERR_ARG, "bad luminosity method");
   if (method != g->lumiMethod) g->invalidate();
   g->lumiMethod = method;
   return UPCG_OK;
@@ -2791,9 +2823,7 @@ int scan_setup(upcg_scan* sc) {
   }
   sc->rows_total = (int)rows_total;
   const size_t plane = (size_t)P * P;
-  CK(sc->ah.ensure((size_t)rows_total * P));
-  CK(sc->al.ensure((size_t)rows_total * P));
-  CK(sc->a2.ensure((size_t)rows_total * P));
+  CK(sc->nodes.ensure((size_t)rows_total * fast_node_floats_per_row()));
   CK(sc->part.ensure((size_t)rows_total * (P / 128)));
   CK(sc->far.ensure(2 * (size_t)rows_total));
   CK(sc->gh.ensure(n * plane));
@@ -2802,7 +2832,8 @@ int scan_setup(upcg_scan* sc) {
   CK(sc->err.ensure(1));
   // tile shape from the autotuner, then the work list: per configuration its
   // row tiles, the N tiles of a row tile adjacent (L2 reuse of A)
-  int rc = contract_plan(std::min(sc->rows_total, 131072), sc->rows_total, P, &sc->shape, &sc->grid);
+  int rc = contract_plan(std::min(sc->rows_total, 131072), sc->rows_total, P, &sc->shape,
+                         &sc->grid, 1);
   if (rc) return rc;
   const int tbn = sc->shape == 0 ? 256 : 128;
   std::vector<int4> items;
@@ -2831,9 +2862,9 @@ int scan_setup(upcg_scan* sc) {
     rc = sc->gens[i]->enqueue_scan_front(*sc, i);
     if (rc) return abort_capture(rc);
   }
-  if (launch_contract_pers(sc->ah.p, sc->al.p, sc->gh.p, sc->gl.p, n, sc->rows_total, P, sc->items.p,
-                           sc->nitems, sc->a2.p, sc->part.p, sc->err.p, sc->shape, sc->grid,
-                           sc->s) != cudaSuccess)
+  if (launch_contract_fused(sc->gh.p, sc->gl.p, n, sc->rows_total, P, sc->items.p, sc->nitems,
+                            sc->nodes.p, sc->part.p, sc->err.p, sc->shape, sc->grid,
+                            sc->s) != cudaSuccess)
     return abort_capture(fail(UPCG_ERR_CUDA, "scan: contraction capture failed"));
   for (int i = 0; i < n; ++i) {
     rc = sc->gens[i]->enqueue_scan_back(*sc, i);

@@ -531,6 +531,7 @@ struct FluxTabs {
 // keep full precision; the scale returns in FP64 in k_fast_finish.
 constexpr int kProjThreads = 256;
 constexpr int kMaxP = 1024;  // radial grid points (the projection's shared-memory row)
+constexpr int kNodeStride = 128;  // floats per (row, side) of a node list: header [4], weights [120], pad
 
 struct SideC {
   float lnb0, ld;   // ln b_i = lnb0 + i ld
@@ -625,42 +626,38 @@ __global__ void k_fast_sides(LumiParams p, FastGrid fg, FluxTabs ft, int cell0, 
   out[t] = c;
 }
 
-__global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
-    LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
-    const SideC* __restrict__ sides, const double* __restrict__ flux_nodes,
-    __nv_bfloat16* __restrict__ ah, __nv_bfloat16* __restrict__ al, float* __restrict__ a2,
-    float4* __restrict__ far_term) {
-  __shared__ SideC sc[2];
-  __shared__ float s_an[2][kNb];   // a_i / max near a (near nodes), 0 beyond
-  __shared__ float s_t[2][kNb];    // radial-grid coordinate of near node i
-  __shared__ float s_qk[2][256];   // Q(k_side, b_j) on the table's b grid
-  __shared__ float s_red[3][2][kProjThreads / 32];
-  __shared__ float s_lamax[2];
-  __shared__ __align__(16) float s_row[2][kMaxP];  // A_side on the radial grid
-  const int lc = blockIdx.x;
+// Shared memory of the per-row node-weight stage.
+struct ProjSmem {
+  SideC sc[2];
+  float an[2][kNb];  // a_i / max near a (near nodes), 0 beyond
+  float t[2][kNb];   // radial-grid coordinate of near node i
+  float qk[2][256];  // Q(k_side, b_j) on the table's b grid
+  float red[3][2][kProjThreads / 32];
+  float lamax[2];
+};
+
+// The node weights of one row (cell): per side ln a_i of every node in FP32
+// log space (point flux from the S(ln x) table, form-factor flux from the Q
+// row of the photon energy, or the plain path's node fluxes), normalised by
+// the side's largest near-node weight.  On return (after a block barrier)
+// sm.an / sm.t hold the near nodes' weights and grid coordinates, `an`/`near`
+// this thread's node, and far_term[lc] the far part and the two ln scales.
+// Every thread of the block calls it.
+__device__ __forceinline__ void proj_weights(const LumiParams& p, const FluxTabs& ft, int lc,
+                                             int iy, const SideC* __restrict__ sides,
+                                             const double* __restrict__ flux_nodes, ProjSmem& sm,
+                                             float4* __restrict__ far_term, float& an_out,
+                                             bool& near_out) {
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const size_t row = (size_t)lc * fg.P;
-  if (lc >= ncells) {  // padding rows of the last 128-cell tile
-    for (int q = tid; q < fg.P; q += kProjThreads) {
-      ah[row + q] = __float2bfloat16(0.f);
-      al[row + q] = __float2bfloat16(0.f);
-      a2[row + q] = 0.f;
-    }
-    return;
-  }
-  const int cell = fast_cell(fg, p.ny, cell0 + lc);
-  const int im = cell / p.ny, iy = cell - (cell / p.ny) * p.ny;
-  if (tid < 2) sc[tid] = sides[2 * lc + tid];
-  for (int q = 4 * tid; q < 2 * kMaxP; q += 4 * kProjThreads)
-    *reinterpret_cast<float4*>(&s_row[0][0] + q) = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (tid < 2) sm.sc[tid] = sides[2 * lc + tid];
   __syncthreads();
   if (!p.isPoint && ft.q32 && !flux_nodes) {  // the photon energy's Q row
     for (int j = tid; j < 2 * ft.nb; j += kProjThreads) {
       const int side = j / ft.nb, jj = j - side * ft.nb;
-      const SideC& c = sc[side];
+      const SideC& c = sm.sc[side];
       const float* q = ft.q32 + (size_t)c.iw * ft.nb + jj;
-      s_qk[side][jj] = c.ww[0] * __ldg(q) + c.ww[1] * __ldg(q + ft.nb) +
-                       c.ww[2] * __ldg(q + 2 * ft.nb) + c.ww[3] * __ldg(q + 3 * ft.nb);
+      sm.qk[side][jj] = c.ww[0] * __ldg(q) + c.ww[1] * __ldg(q + ft.nb) +
+                        c.ww[2] * __ldg(q + 2 * ft.nb) + c.ww[3] * __ldg(q + 3 * ft.nb);
     }
     __syncthreads();
   }
@@ -670,7 +667,7 @@ __global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
   float la = -INFINITY;
   bool near = false;
   if (node) {
-    const SideC& c = sc[side];
+    const SideC& c = sm.sc[side];
     const float lnb = fmaf((float)i, c.ld, c.lnb0);
     near = i < c.n_near;
     if (flux_nodes) {  // the plain path's node fluxes (QAGS / K0, K1)
@@ -691,11 +688,11 @@ __global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
     } else {  // form-factor flux: N = factor Q^2 / (A^2 k)
       float w[4];
       const int j0 = lag4f(fmaf((float)i, c.tbd, c.tb0), ft.nb, w);
-      const float Q = w[0] * s_qk[side][j0] + w[1] * s_qk[side][j0 + 1] +
-                      w[2] * s_qk[side][j0 + 2] + w[3] * s_qk[side][j0 + 3];
+      const float Q = w[0] * sm.qk[side][j0] + w[1] * sm.qk[side][j0 + 1] +
+                      w[2] * sm.qk[side][j0 + 2] + w[3] * sm.qk[side][j0 + 3];
       if (Q != 0.f) la = c.lnc_ff + 2.f * logf(fabsf(Q)) + 2.f * lnb + c.lnw0;
     }
-    if (near) s_t[side][i] = fmaf((float)i, c.tgd, c.tg0);
+    if (near) sm.t[side][i] = fmaf((float)i, c.tgd, c.tg0);
   }
   // each side's largest near-node ln a
   {
@@ -707,22 +704,22 @@ __global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
       m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
     }
     if (lane == 0) {
-      s_red[0][0][wid] = m0;
-      s_red[0][1][wid] = m1;
+      sm.red[0][0][wid] = m0;
+      sm.red[0][1][wid] = m1;
     }
     __syncthreads();
     if (tid < 2) {
       float m = -INFINITY;
-      for (int w = 0; w < kProjThreads / 32; ++w) m = fmaxf(m, s_red[0][tid][w]);
-      s_lamax[tid] = m == -INFINITY ? 0.f : m;  // a side without flux: all weights 0
+      for (int w = 0; w < kProjThreads / 32; ++w) m = fmaxf(m, sm.red[0][tid][w]);
+      sm.lamax[tid] = m == -INFINITY ? 0.f : m;  // a side without flux: all weights 0
     }
     __syncthreads();
   }
   // normalised weights; near and far sums per side (fixed order)
   float an = 0.f;
   if (node) {
-    an = la == -INFINITY ? 0.f : expf(la - s_lamax[side]);
-    s_an[side][i] = near ? an : 0.f;
+    an = la == -INFINITY ? 0.f : expf(la - sm.lamax[side]);
+    sm.an[side][i] = near ? an : 0.f;
   }
   {
     float v[4] = {0.f, 0.f, 0.f, 0.f};  // near0, near1, far0, far1
@@ -732,24 +729,71 @@ __global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
     if (lane == 0) {
-      s_red[1][0][wid] = v[0];
-      s_red[1][1][wid] = v[1];
-      s_red[2][0][wid] = v[2];
-      s_red[2][1][wid] = v[3];
+      sm.red[1][0][wid] = v[0];
+      sm.red[1][1][wid] = v[1];
+      sm.red[2][0][wid] = v[2];
+      sm.red[2][1][wid] = v[3];
     }
   }
   __syncthreads();
+  if (tid == 0) {
+    float S[4] = {0.f, 0.f, 0.f, 0.f};  // near0, near1, far0, far1
+    for (int w = 0; w < kProjThreads / 32; ++w) {
+      S[0] += sm.red[1][0][w];
+      S[1] += sm.red[1][1][w];
+      S[2] += sm.red[2][0][w];
+      S[3] += sm.red[2][1][w];
+    }
+    // G = c wherever one node is far: (S1far S2 + S1near S2far), normalised;
+    // the two ln scales; k_fast_finish combines them in FP64
+    far_term[lc] = make_float4(S[2] * (S[1] + S[3]) + S[0] * S[3], sm.lamax[0], sm.lamax[1], 0.f);
+  }
+  an_out = an;
+  near_out = near;
+}
+
+// Staged projection: one CTA per row writes the dense contraction operands
+// A1 (bf16 hi / lo) and A2 (FP32) on the radial grid, 8 KB per row, for
+// k_contract_pers to read back.
+__global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
+    LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
+    const SideC* __restrict__ sides, const double* __restrict__ flux_nodes,
+    __nv_bfloat16* __restrict__ ah, __nv_bfloat16* __restrict__ al, float* __restrict__ a2,
+    float4* __restrict__ far_term) {
+  __shared__ ProjSmem sm;
+  __shared__ __align__(16) float s_row[2][kMaxP];  // A_side on the radial grid
+  const int lc = blockIdx.x;
+  const int tid = threadIdx.x;
+  const size_t row = (size_t)lc * fg.P;
+  if (lc >= ncells) {  // padding rows of the last 128-cell tile
+    for (int q = tid; q < fg.P; q += kProjThreads) {
+      ah[row + q] = __float2bfloat16(0.f);
+      al[row + q] = __float2bfloat16(0.f);
+      a2[row + q] = 0.f;
+    }
+    return;
+  }
+  const int cell = fast_cell(fg, p.ny, cell0 + lc);
+  const int iy = cell - (cell / p.ny) * p.ny;
+  for (int q = 4 * tid; q < 2 * kMaxP; q += 4 * kProjThreads)
+    *reinterpret_cast<float4*>(&s_row[0][0] + q) = make_float4(0.f, 0.f, 0.f, 0.f);
+  float an;
+  bool near;
+  proj_weights(p, ft, lc, iy, sides, flux_nodes, sm, far_term, an, near);
+  const int side = tid / kNb, i = tid - side * kNb;
+  const bool node = tid < 2 * kNb;
+  (void)an;
   // scatter onto the radial grid: A_side[p0_i + m] += an_i phi_m(s_i).  Nodes
   // i = r (mod np) go in pass r, np = ceil(4.5 / spacing): within a pass the
   // 4-point stencils are disjoint, so no atomics and a fixed summation order.
-  const int np = (int)ceilf(4.5f * fmaxf(sc[0].inv_tgd, sc[1].inv_tgd));
+  const int np = (int)ceilf(4.5f * fmaxf(sm.sc[0].inv_tgd, sm.sc[1].inv_tgd));
   for (int pass = 0; pass < np; ++pass) {
     if (node && near && i % np == pass) {
-      const float t = s_t[side][i];
+      const float t = sm.t[side][i];
       const int p0 = (int)floorf(t) - 1;  // in [0, P-4]: the host checks the grid's span
       const float s = t - (float)p0;
       const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
-      const float a = s_an[side][i];
+      const float a = sm.an[side][i];
       float* r = &s_row[side][p0];
       r[0] = fmaf(a, -s1 * s2 * s3 * (1.f / 6.f), r[0]);
       r[1] = fmaf(a, s * s2 * s3 * 0.5f, r[1]);
@@ -775,17 +819,36 @@ __global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
     *reinterpret_cast<uint2*>(al + row + q) = lv;
     *reinterpret_cast<float4*>(a2 + row + q) = *reinterpret_cast<const float4*>(&s_row[1][q]);
   }
-  if (tid == 0) {
-    float S[4] = {0.f, 0.f, 0.f, 0.f};  // near0, near1, far0, far1
-    for (int w = 0; w < kProjThreads / 32; ++w) {
-      S[0] += s_red[1][0][w];
-      S[1] += s_red[1][1][w];
-      S[2] += s_red[2][0][w];
-      S[3] += s_red[2][1][w];
-    }
-    // G = c wherever one node is far: (S1far S2 + S1near S2far), normalised;
-    // the two ln scales; k_fast_finish combines them in FP64
-    far_term[lc] = make_float4(S[2] * (S[1] + S[3]) + S[0] * S[3], s_lamax[0], s_lamax[1], 0.f);
+}
+
+// Node lists for the fused contraction: per row and side kNodeStride floats,
+// [0] the radial-grid coordinate of node 0 (tg0), [1] the spacing (tgd), [2]
+// the near-node count (int bits), [3] unused, [4 + i] the normalised weight
+// of near node i.  Padding rows get a count of 0.
+__global__ void __launch_bounds__(kProjThreads, 8) k_fast_nodes(
+    LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
+    const SideC* __restrict__ sides, const double* __restrict__ flux_nodes,
+    float* __restrict__ nodes, float4* __restrict__ far_term) {
+  __shared__ ProjSmem sm;
+  const int lc = blockIdx.x;
+  const int tid = threadIdx.x;
+  float* out = nodes + (size_t)lc * 2 * kNodeStride;
+  if (lc >= ncells) {
+    if (tid < 2)
+      *reinterpret_cast<float4*>(out + tid * kNodeStride) = make_float4(0.f, 1.f, 0.f, 0.f);
+    return;
+  }
+  const int cell = fast_cell(fg, p.ny, cell0 + lc);
+  const int iy = cell - (cell / p.ny) * p.ny;
+  float an;
+  bool near;
+  proj_weights(p, ft, lc, iy, sides, flux_nodes, sm, far_term, an, near);
+  const int side = tid / kNb, i = tid - side * kNb;
+  if (tid < 2 * kNb) out[side * kNodeStride + 4 + i] = near ? an : 0.f;
+  if (tid < 2) {
+    const SideC& c = sm.sc[tid];
+    *reinterpret_cast<float4*>(out + tid * kNodeStride) =
+        make_float4(c.tg0, c.tgd, __int_as_float(c.n_near), 0.f);
   }
 }
 
@@ -1102,6 +1165,338 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
   }
 }
 
+// ---------------------------------------------------- fused contraction --
+// k_contract_fused: the persistent contraction with the projection folded in.
+// The A1 operand (side 0 on the radial grid, bf16 hi / lo) is built in shared
+// memory by builder warps from the row's node list, stage by stage, instead
+// of being read by TMA from an 8 KB-per-row array; the A2 row-dot of the
+// epilogue gathers the accumulator at side 1's node stencils instead of
+// reading a dense A2 row.  Only the survival kernel G still comes by TMA.
+// Per CTA (448 threads):
+//   warp 0       TMA producer of the G tiles (B operand);
+//   warp 1       TMEM allocation and the single-thread tcgen05.mma issuer;
+//   warps 2-5    epilogue: TMEM -> registers -> the gathered row-dot;
+//   warps 6-13   A1 builders: two threads per row, 32 columns of a stage each.
+// A stage is complete when the TMA transaction bytes have landed and the 8
+// builder warps have arrived (full barrier of count 9); the builders write
+// generic-proxy shared memory and fence it to the async proxy before they
+// arrive.  A builder stages its 32 FP32 values in its own row of the stage's
+// hi (first half) or lo (second half) tile, reads them back after the
+// partner thread has read its half, and overwrites both rows with the bf16
+// pair in the SWIZZLE_128B K-major layout the MMA descriptors expect.
+constexpr int kBuildWarps = 8;
+constexpr int kFusedThreads = (6 + kBuildWarps) * 32;
+
+__device__ __forceinline__ int node_p0(float tg0, float tgd, int i) {
+  return (int)floorf(fmaf((float)i, tgd, tg0)) - 1;
+}
+
+// 4-point Lagrange weights of a node at fractional offset s from its first
+// stencil point (the projection's formula)
+__device__ __forceinline__ void lag4_weights(float s, float w[4]) {
+  const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
+  w[0] = -s1 * s2 * s3 * (1.f / 6.f);
+  w[1] = s * s2 * s3 * 0.5f;
+  w[2] = -s * s1 * s3 * 0.5f;
+  w[3] = s * s1 * s2 * (1.f / 6.f);
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+struct FusedArgs {
+  const PersItem* items;
+  int nitems, ktiles, P, ntiles;
+  const float* nodes;  // [rows][2][kNodeStride] (k_fast_nodes)
+  float* partial;      // [rows][ntiles]
+  unsigned* err;
+};
+
+template <int TBN, int TST>
+__global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
+    const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl,
+    FusedArgs args) {
+  constexpr int kA = BM * BK * 2, kB = TBN * BK * 2, kStage = 2 * kA + 2 * kB;
+  constexpr uint32_t kCols = 2 * TBN;
+  constexpr uint32_t kId = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TBN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[TST], empty_bar[TST], accf[2], acce[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  __shared__ float ep_scr[4][32][17];  // epilogue: one 16-column accumulator chunk per thread
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TST; ++s) {
+      mbar_init(&full_bar[s], 1 + kBuildWarps);
+      mbar_init(&empty_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);  // one arrival per epilogue warp
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int nmine = args.nitems > (int)blockIdx.x
+                        ? (args.nitems - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                        : 0;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer: the G tiles
+      int g = 0;
+      bool ok = true;
+      for (int it = 0; it < nmine && ok; ++it) {
+        const PersItem w = args.items[blockIdx.x + it * gridDim.x];
+        for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+          const int s = g % TST;
+          if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 1u)) {
+            ok = false;
+            abort_flag = 1;
+            break;
+          }
+          if (abort_flag) {
+            ok = false;
+            break;
+          }
+          uint8_t* st = smem + s * kStage;
+          mbar_expect_tx(&full_bar[s], 2 * kB);
+          const int x = kt * BK;
+          tma_load_3d(st + 2 * kA, &tBh, &full_bar[s], x, w.ntile * TBN, w.config);
+          tma_load_3d(st + 2 * kA + kB, &tBl, &full_bar[s], x, w.ntile * TBN, w.config);
+        }
+      }
+      // the copies in flight land before the CTA exits
+      for (int q = (g > TST ? g - TST : 0); q < g; ++q)
+        mbar_wait(&full_bar[q % TST], (q / TST) & 1, args.err, 8u);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      int g = 0;
+      bool ok = true;
+      for (int it = 0; it < nmine && ok; ++it) {
+        const int b = it & 1;
+        if (it >= 2 && !mbar_wait(&acce[b], ((it >> 1) & 1) ^ 1, args.err, 16u)) {
+          ok = false;
+          abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * TBN);
+        for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+          const int s = g % TST;
+          if (!mbar_wait(&full_bar[s], (g / TST) & 1, args.err, 2u)) {
+            ok = false;
+            abort_flag = 1;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t base = smem_u32(smem + s * kStage);
+          const uint32_t ah = base, al = base + kA, bh = base + 2 * kA, bl = base + 2 * kA + kB;
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            const uint32_t off = kk * 32;
+            const uint64_t dah = sw128_desc(ah + off), dal = sw128_desc(al + off);
+            const uint64_t dbh = sw128_desc(bh + off), dbl = sw128_desc(bl + off);
+            const uint32_t first = (kt > 0 || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
+                "l"(dah), "l"(dbh), "r"(kId), "r"(first));
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
+                "l"(dah), "l"(dbl), "r"(kId), "r"(1u));
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
+                "l"(dal), "l"(dbh), "r"(kId), "r"(1u));
+          }
+          umma_commit(&empty_bar[s]);
+        }
+        if (ok) umma_commit(&accf[b]);
+      }
+    }
+  } else if (warp < 6) {
+    // ---------------- epilogue: TMEM -> registers, row-dot gathered at side 1's nodes
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    float* scr = &ep_scr[warp - 2][lane][0];
+    for (int it = 0; it < nmine; ++it) {
+      const PersItem w = args.items[blockIdx.x + it * gridDim.x];
+      const int b = it & 1;
+      const bool ok = mbar_wait(&accf[b], (it >> 1) & 1, args.err, 4u);
+      tc_fence_after();
+      const size_t grow = (size_t)w.mtile * BM + row;
+      const float* nd = args.nodes + (grow * 2 + 1) * kNodeStride;
+      float tg0 = 0.f, tgd = 1.f;
+      int nn = 0;
+      if (row < w.rows) {
+        const float4 hd = __ldg(reinterpret_cast<const float4*>(nd));
+        tg0 = hd.x;
+        tgd = hd.y;
+        nn = __float_as_int(hd.z);
+      }
+      int cur = 0;  // first node whose stencil may reach the current columns
+      float acc = 0.f;
+      if (ok) {
+        for (int c0 = 0; c0 < TBN; c0 += 16) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TBN + c0), v);
+          const int lo = w.ntile * TBN + c0, hi = lo + 15;
+          while (cur < nn && node_p0(tg0, tgd, cur) + 3 < lo) ++cur;
+          if (cur < nn && node_p0(tg0, tgd, cur) <= hi) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) scr[j] = v[j];
+            for (int i = cur; i < nn; ++i) {
+              const float t = fmaf((float)i, tgd, tg0);
+              const int p0 = (int)floorf(t) - 1;
+              if (p0 > hi) break;
+              float wl[4];
+              lag4_weights(t - (float)p0, wl);
+              const float a = __ldg(nd + 4 + i);
+#pragma unroll
+              for (int m = 0; m < 4; ++m) {
+                const int c = p0 + m - lo;
+                if ((unsigned)c < 16u) acc = fmaf(a * wl[m], scr[c], acc);
+              }
+            }
+          }
+        }
+      }
+      if (row < w.rows) args.partial[grow * args.ntiles + w.ntile] = ok ? acc : 0.f;
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
+      if (!ok) break;
+    }
+  } else {
+    // ---------------- A1 builders: row r, columns 32h .. 32h+31 of each stage
+    const int r = (warp - 6) * 16 + (lane >> 1);
+    const int h = lane & 1;
+    const uint32_t roff = (uint32_t)((r >> 3) * 1024 + (r & 7) * 128);
+    const int sw = r & 7;
+    int g = 0;
+    bool ok = true;
+    for (int it = 0; it < nmine && ok; ++it) {
+      const PersItem w = args.items[blockIdx.x + it * gridDim.x];
+      const size_t grow = (size_t)w.mtile * BM + r;
+      const float* nd = args.nodes + grow * 2 * kNodeStride;  // side 0
+      float tg0 = 0.f, tgd = 1.f;
+      int nn = 0;
+      if (r < w.rows) {
+        const float4 hd = __ldg(reinterpret_cast<const float4*>(nd));
+        tg0 = hd.x;
+        tgd = hd.y;
+        nn = __float_as_int(hd.z);
+      }
+      int cur = 0;
+      for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+        const int s = g % TST;
+        if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 32u)) {
+          ok = false;
+          abort_flag = 1;
+        }
+        ok = __all_sync(0xffffffffu, ok && !abort_flag);  // the warp leaves together
+        if (!ok) break;
+        uint8_t* st = smem + s * kStage;
+        float* stg = reinterpret_cast<float*>(st + (h ? kA : 0) + roff);  // own 32 floats
+        const int c_lo = kt * BK + 32 * h, c_hi = c_lo + 31;
+        while (cur < nn && node_p0(tg0, tgd, cur) + 3 < c_lo) ++cur;
+        float v[32];
+        if (cur < nn && node_p0(tg0, tgd, cur) <= c_hi) {
+          // FP32 staging in the own row, 16-byte chunks XOR-swizzled by row
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            *reinterpret_cast<float4*>(stg + ((q ^ sw) << 2)) = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int i = cur; i < nn; ++i) {
+            const float t = fmaf((float)i, tgd, tg0);
+            const int p0 = (int)floorf(t) - 1;
+            if (p0 > c_hi) break;
+            float wl[4];
+            lag4_weights(t - (float)p0, wl);
+            const float a = __ldg(nd + 4 + i);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+              const int c = p0 + m - c_lo;
+              if ((unsigned)c < 32u) {
+                float* e = stg + ((((c >> 2) ^ sw) << 2) | (c & 3));
+                *e = fmaf(a, wl[m], *e);
+              }
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float4 x = *reinterpret_cast<const float4*>(stg + ((q ^ sw) << 2));
+            v[4 * q] = x.x;
+            v[4 * q + 1] = x.y;
+            v[4 * q + 2] = x.z;
+            v[4 * q + 3] = x.w;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = 0.f;
+        }
+        __syncwarp();  // the partner thread has read its staging (in this row's other half)
+        // bf16 hi / lo of the 32 values: chunks 4h .. 4h+3 of the 128-byte row
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          uint32_t hw[4], lw[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float x0 = v[8 * q + 2 * e], x1 = v[8 * q + 2 * e + 1];
+            const __nv_bfloat162 hh = __floats2bfloat162_rn(x0, x1);
+            const float2 f = __bfloat1622float2(hh);
+            const __nv_bfloat162 ll = __floats2bfloat162_rn(x0 - f.x, x1 - f.y);
+            hw[e] = *reinterpret_cast<const uint32_t*>(&hh);
+            lw[e] = *reinterpret_cast<const uint32_t*>(&ll);
+          }
+          const uint32_t ch = (uint32_t)(((4 * h + q) ^ sw) << 4);
+          *reinterpret_cast<uint4*>(st + roff + ch) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          *reinterpret_cast<uint4*>(st + kA + roff + ch) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&full_bar[s]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+  }
+}
+
+// Synthetic node lists for the autotuner: every row and side with 120 near
+// nodes spread like a form-factor row (spacing 5 - 5.6 grid points from 157).
+__global__ void k_fill_nodes_synthetic(float* __restrict__ nodes, int rows) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= rows * 2) return;
+  float* o = nodes + (size_t)t * kNodeStride;
+  o[0] = 157.f + (float)(t % 61) * 0.5f;
+  o[1] = 5.f + (float)(t % 7) * 0.1f;
+  o[2] = __int_as_float(kNb);
+  o[3] = 0.f;
+  for (int i = 0; i < kNb; ++i) o[4 + i] = 1.f / (1.f + (float)i);
+}
+
 template <int TBN, int TST>
 constexpr int pers_smem() {
   return TST * (2 * BM * BK * 2 + 2 * TBN * BK * 2) + 1024;
@@ -1173,6 +1568,52 @@ cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh,
 
 int contract_item_bytes() { return (int)sizeof(PersItem); }
 
+cudaError_t launch_contract_fused(const void* gh, const void* gl, int nconf, int rows_total, int P,
+                                  const void* items, int nitems, const float* nodes,
+                                  float* partial, unsigned* d_err, int shape, int grid,
+                                  cudaStream_t st) {
+  // shape 0: N tile 256, 2 stages; shape 1: N tile 128, 3 stages
+  const int tbn = shape == 0 ? 256 : 128;
+  if (P % tbn != 0 || P % BK != 0 || P > kMaxP || rows_total % BM != 0 || nitems <= 0 ||
+      grid <= 0 || !nodes)
+    return cudaErrorInvalidValue;
+  CUtensorMap tBh, tBl;
+  cudaError_t e;
+  if ((e = make_map3(&tBh, gh, nconf, P, P, tbn)) != cudaSuccess) return e;
+  if ((e = make_map3(&tBl, gl, nconf, P, P, tbn)) != cudaSuccess) return e;
+  FusedArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, nodes, partial,
+                 d_err};
+  if (grid > nitems) grid = nitems;
+  if (shape == 0) {
+    static std::atomic<uint64_t> attr{0};  // devices with the limit raised
+    constexpr int sm = pers_smem<256, 2>();
+    {
+      const cudaError_t ea = smem_attr_once(attr, k_contract_fused<256, 2>, sm);
+      if (ea != cudaSuccess) return ea;
+    }
+    note_launch();
+    k_contract_fused<256, 2><<<grid, kFusedThreads, sm, st>>>(tBh, tBl, args);
+  } else {
+    static std::atomic<uint64_t> attr{0};  // devices with the limit raised
+    constexpr int sm = pers_smem<128, 3>();
+    {
+      const cudaError_t ea = smem_attr_once(attr, k_contract_fused<128, 3>, sm);
+      if (ea != cudaSuccess) return ea;
+    }
+    note_launch();
+    k_contract_fused<128, 3><<<grid, kFusedThreads, sm, st>>>(tBh, tBl, args);
+  }
+  return cudaGetLastError();
+}
+
+int fast_node_floats_per_row() { return 2 * kNodeStride; }
+
+cudaError_t launch_fill_nodes_synthetic(float* nodes, int rows, cudaStream_t st) {
+  note_launch();
+  k_fill_nodes_synthetic<<<(2 * rows + 255) / 256, 256, 0, st>>>(nodes, rows);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, const void* bl,
                                int M, int N, int K, float* out_f32, void* out_hi, void* out_lo,
                                unsigned* d_err, cudaStream_t st) {
@@ -1232,8 +1673,9 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
                                 const double* flux_nodes, const FastFluxTables* t, void* d_sides,
                                 void* ah, void* al, float* a2, void* far_term, cudaStream_t st,
-                                const int* rep_y, int n_rep_y, int m0) {
+                                const int* rep_y, int n_rep_y, int m0, float* nodes) {
   if (rep_y && (flux_nodes || n_rep_y <= 0)) return cudaErrorInvalidValue;
+  if (!nodes && !(ah && al && a2)) return cudaErrorInvalidValue;
   FastGrid fg{P, u0, h, 1.0 / h, 250.};
   fg.rep_y = rep_y;
   fg.n_rep_y = n_rep_y;
@@ -1262,9 +1704,14 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
   note_launch();
   k_fast_sides<<<(2 * ncells + 255) / 256, 256, 0, st>>>(p, fg, ft, cell0, ncells, sides);
   note_launch();
-  k_fast_project<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, sides, flux_nodes,
-                                                        (__nv_bfloat16*)ah, (__nv_bfloat16*)al,
-                                                        a2, static_cast<float4*>(far_term));
+  if (nodes)  // node lists for k_contract_fused
+    k_fast_nodes<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, sides, flux_nodes,
+                                                      nodes, static_cast<float4*>(far_term));
+  else  // dense operands for k_contract_pers
+    k_fast_project<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, sides,
+                                                        flux_nodes, (__nv_bfloat16*)ah,
+                                                        (__nv_bfloat16*)al, a2,
+                                                        static_cast<float4*>(far_term));
   return cudaGetLastError();
 }
 

@@ -182,11 +182,24 @@ cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream,
 // rep_y[r % n_rep_y]) -- one of each pair of mirror rapidities, whose
 // luminosities are equal; launch_fast_finish then also writes the mirror cell
 // rep_mir[r % n_rep_y] (-1: none).  Without it row r is cell r.
+// With nodes set the rows' node lists (fast_node_floats_per_row() floats per
+// row) are written for launch_contract_fused and ah / al / a2 are not used;
+// without it the dense operands of launch_contract_pers are.
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
                                 const double* flux_nodes, const FastFluxTables* t, void* d_sides,
                                 void* ah, void* al, float* a2, void* far_term, cudaStream_t st,
-                                const int* rep_y = nullptr, int n_rep_y = 0, int m0 = 0);
+                                const int* rep_y = nullptr, int n_rep_y = 0, int m0 = 0,
+                                float* nodes = nullptr);
+int fast_node_floats_per_row();
+// The persistent contraction with the projection folded in (k_contract_fused):
+// the same work list and partial sums as launch_contract_pers, the A1 operand
+// built in shared memory and the A2 row-dot gathered from the node lists.
+cudaError_t launch_contract_fused(const void* gh, const void* gl, int nconf, int rows_total, int P,
+                                  const void* items, int nitems, const float* nodes,
+                                  float* partial, unsigned* d_err, int shape, int grid,
+                                  cudaStream_t st);
+cudaError_t launch_fill_nodes_synthetic(float* nodes, int rows, cudaStream_t st);
 // bytes of the per-(cell, photon) constants (d_sides holds 2 per cell);
 // far_term holds one float4 per cell
 size_t fast_side_bytes();
