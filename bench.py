@@ -130,8 +130,73 @@ def workload_name(workload, params, nm, ny, nev):
             f"BREAKUP_MODE {params['BREAKUP_MODE']}, PROC_ID {params['PROC_ID']}, {nev} events")
 
 
+def row_blocks(nm, nblocks, block):
+    """`nblocks` blocks of `block` consecutive m-rows spread evenly over the
+    mass range (low, middle and top masses; the quadrature cost grows with
+    the mass)."""
+    if nblocks * block >= nm:
+        return [(0, nm)]
+    starts = np.linspace(0, nm - block, nblocks).round().astype(int)
+    return [(int(a), int(a) + block) for a in starts]
+
+
+def cpu_lumi_sample(o, blocks):
+    """Luminosity rows of the blocks on every host thread; (seconds, cells)."""
+    ny = o.grid()["ny"]
+    t0 = time.perf_counter()
+    for a, b in blocks:
+        o.lumi_table(a, b)
+    return time.perf_counter() - t0, sum(b - a for a, b in blocks) * ny
+
+
+def cpu_phases(params, threads, blocks, n_events, lumi=None):
+    """The CPU restatement's phases, each timed on its own: init (form factor,
+    G_AA and breakup splines: src/UpcCrossSection.cpp:364-461), the luminosity
+    on a row sample (:221-271, 463-592, OpenMP over m-rows), the fold and the
+    samplers (:337-362, 594-698; UpcSampler.h:37-142), and event generation
+    single-threaded as in the reference (src/UpcGenerator.cpp:715-926).
+    `lumi` (the full table) feeds the fold; without it the sampled rows are
+    tiled over the grid (the fold's cost does not depend on the values)."""
+    from oracle.oracle import Oracle
+    o = Oracle(params, threads=threads)
+    t0 = time.perf_counter()
+    o.init_tables()
+    t_init = time.perf_counter() - t0
+    g = o.grid()
+    t_lumi, cells = cpu_lumi_sample(o, blocks)
+    if lumi is None:
+        rows = np.concatenate([o.lumi_table(a, b) for a, b in blocks[:1]])
+        lumi = np.resize(rows, (g["nm"], g["ny"]))
+    o1 = Oracle(params, threads=1)
+    o1.init_tables()
+    t0 = time.perf_counter()
+    cs, tot, ratio = o1.nuc_cs_ym(lumi)
+    zm = o1.cs_zm_table()
+    t1 = time.perf_counter()
+    o1.generate(cs, zm, 1, 1)  # builds the samplers (and draws one event)
+    t_samp = time.perf_counter() - t1
+    t_fold = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _, rej, _ = o1.generate(cs, zm, n_events, 1)
+    t_ev = time.perf_counter() - t0 - t_samp
+    return {
+        "init_s": t_init,
+        "lumi_cells_per_s": cells / t_lumi, "lumi_sample_cells": cells, "lumi_sample_s": t_lumi,
+        "lumi_full_table_s_est": t_lumi * g["nm"] * g["ny"] / cells,
+        "fold_and_samplers_s": t_fold,
+        "events_per_s_1_thread": n_events / max(t_ev, 1e-9),
+        "events_sample": n_events, "events_rejected": rej,
+        "threads_lumi": threads, "threads_fold_events": 1,
+        "sample": f"luminosity rows {blocks} (all {g['ny']} y-bins), FP64 on {threads} threads; "
+                  f"fold + samplers on the full {g['nm']}x{g['ny']} grid; {n_events} events "
+                  f"single-threaded",
+    }
+
+
 def run_reference(args):
-    """CPU restatement of the reference on all host threads, bounded sample."""
+    """CPU restatement of the reference on all host threads, bounded sample:
+    each step computes 4 blocks of m-rows (as many rows per block as host
+    threads) spread over the mass range."""
     from oracle.oracle import Oracle
     params = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
@@ -140,18 +205,22 @@ def run_reference(args):
     o.init_tables()
     t_init = time.perf_counter() - t0
     g = o.grid()
-    # sample: the first R m-rows (all rapidities), ~10-30 s of CPU work
-    rows = args.ref_rows or (64 if args.workload == "c2" else g["nm"])
+    # blocks as wide as the thread count (the OpenMP slicing is over m-rows)
+    width = max(4, threads)
+    if args.ref_rows:
+        blocks = row_blocks(g["nm"], max(1, args.ref_rows // width), min(width, args.ref_rows))
+    else:
+        blocks = row_blocks(g["nm"], 4, width) if args.workload == "c2" else [(0, g["nm"])]
     for _ in range(min(args.warmup, 1)):
         o.lumi_table(0, 1)
     times = []
     for _ in range(args.steps):
-        t0 = time.perf_counter()
-        o.lumi_table(0, rows)
-        times.append(time.perf_counter() - t0)
-    cells = rows * g["ny"]
+        dt, cells = cpu_lumi_sample(o, blocks)
+        times.append(dt)
     v = cells / float(np.mean(times))
-    sample = f"first {rows} of {g['nm']} m-rows x {g['ny']} y-bins = {cells} cells per step"
+    sample = (f"m-row blocks {blocks} of {g['nm']} x {g['ny']} y-bins = {cells} cells per step "
+              f"(spread over the mass range)")
+    phases = cpu_phases(params, threads, blocks[:2], 20000 if args.workload == "c2" else 100000)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
@@ -161,30 +230,24 @@ def run_reference(args):
                                                  else EVENTS[args.workload]),
                        "sample": sample},
             "init_tables_s": t_init,
+            "cpu_phases": phases,
             "cpu_baseline": {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def cpu_baseline_sample(workload, seconds=15.0):
-    from oracle.oracle import Oracle
+def cpu_baseline_sample(workload, lumi=None):
+    """The GPU arm's CPU leg: the restatement's phases on this host (about
+    15 s), cells/s of the luminosity sample as the headline figure."""
     params = WORKLOADS[workload]
     threads = os.cpu_count() or 1
-    o = Oracle(params, threads=threads)
-    o.init_tables()
-    g = o.grid()
-    rows, dt = 2, 0.0
-    while True:
-        t0 = time.perf_counter()
-        o.lumi_table(0, rows)
-        dt = time.perf_counter() - t0
-        if dt > seconds / 4 or rows >= g["nm"]:
-            break
-        rows = min(g["nm"], rows * 4)
-    cells = rows * g["ny"]
-    return {"value": cells / dt, "unit": "cells/s", "cores": threads, "kind": "port",
-            "sample": f"{cells} cells (first {rows} of {g['nm']} m-rows, low masses), one pass"}
+    from oracle.oracle import Oracle
+    nm = Oracle(params, threads=1).grid()["nm"]
+    blocks = row_blocks(nm, 8, max(4, threads)) if workload == "c2" else [(0, nm)]
+    ph = cpu_phases(params, threads, blocks, 20000 if workload == "c2" else 100000, lumi)
+    return {"value": ph["lumi_cells_per_s"], "unit": "cells/s", "cores": threads, "kind": "port",
+            "sample": ph["sample"], "phases": ph}
 
 
 # DRAM traffic per launch from one ncu capture of the c2 workload (65,536-cell
@@ -447,7 +510,7 @@ def main():
         line["roofline_projection"]["frac"] = (line["roofline_projection"]["achieved"] /
                                                line["roofline_projection"]["peak"])
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(args.workload)
+        line["cpu_baseline"] = cpu_baseline_sample(args.workload, lf if pk > 0 else None)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

@@ -5,8 +5,15 @@
 * ``build_ref()`` compiles the two translation units of the reference that build
   without ROOT/GSL -- ``src/UpcTwoPhotonDilep.cpp`` and ``src/UpcTwoPhotonALP.cpp``
   -- together with ``ref_shim.cpp`` into ``oracle/_ref/libupcref_elem.so``, when
-  the reference sources are present.  The rest of the reference needs ROOT and
-  GSL and is not buildable here.
+  the reference sources are present.
+* ``build_ref_cs()`` compiles the reference's ``src/UpcCrossSection.cpp`` and the
+  process classes it creates (``UpcTwoPhotonDilep``, ``UpcTwoPhotonALP``,
+  ``UpcTwoPhotonDipion``, ``UpcTwoPhotonLbyL``, ``UpcPhotoNuclearVM``) where they
+  lie, against the GSL / ROOT stand-ins of ``refshim/`` (whose luminosity-path
+  calls are the oracle's own restated primitives), with ``ref_cs_shim.cpp``
+  into ``oracle/_ref/libupcref_cs.so``.  This pins the oracle's restatement of
+  calcTwoPhotonLumi, fluxForm, calcBreakupProb, prepareGAA, calcPhotonFlux ...
+  to the reference's own source text.
 
 ``-ffp-contract=off`` keeps the x86 and aarch64 builds bit-identical (gcc
 contracts a*b+c into FMAs by default on aarch64).
@@ -61,6 +68,34 @@ def build_ref(force=False):
     return REF_SO
 
 
+REF_CS_SO = os.path.join(REF_DIR, "libupcref_cs.so")
+_REF_CS_UNITS = ["UpcCrossSection.cpp", "UpcTwoPhotonDilep.cpp", "UpcTwoPhotonALP.cpp",
+                 "UpcTwoPhotonDipion.cpp", "UpcTwoPhotonLbyL.cpp", "UpcPhotoNuclearVM.cpp"]
+
+
+def build_ref_cs(force=False):
+    """Compile the reference's UpcCrossSection against refshim/; None if the
+    reference sources are absent (the prebuilt library is used if present)."""
+    src = os.path.join(REFERENCE_ROOT, "src")
+    inc = os.path.join(REFERENCE_ROOT, "include")
+    units = [os.path.join(src, u) for u in _REF_CS_UNITS]
+    if not all(os.path.exists(u) for u in units):
+        return REF_CS_SO if os.path.exists(REF_CS_SO) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    shim_dir = os.path.join(HERE, "refshim")
+    shim = os.path.join(HERE, "ref_cs_shim.cpp")
+    deps = units + [shim, os.path.join(HERE, "oracle_num.hpp")]
+    deps += [os.path.join(shim_dir, f) for f in os.listdir(shim_dir) if f.endswith(".h")]
+    if force or _stale(REF_CS_SO, deps):
+        cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+               "-w", '-DCROSS_SEC_DIR="/nonexistent"', "-I", shim_dir, "-I", inc, *units, shim,
+               "-lpthread", "-o", REF_CS_SO + ".tmp"]
+        subprocess.run(cmd, check=True)
+        os.replace(REF_CS_SO + ".tmp", REF_CS_SO)
+    return REF_CS_SO
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref_cs(force=True))

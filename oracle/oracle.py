@@ -242,6 +242,93 @@ def sampler_bin(nbins, lo, hi, x):
     return lib().uo_sampler_bin(nbins, lo, hi, x)
 
 
+_ref_cs = None
+
+
+def ref_cs_lib():
+    """The reference's own UpcCrossSection (src/UpcCrossSection.cpp compiled
+    against oracle/refshim/), or None when the reference sources are absent."""
+    global _ref_cs
+    if _ref_cs is None:
+        so = _build.build_ref_cs()
+        if so is None:
+            return None
+        L = C.CDLL(so)
+        d, i = C.c_double, C.c_int
+        L.uref_cs_init.argtypes = [i, i, d, d, d, i, i, i, d, d, d, d, i, d, d, i, i]
+        L.uref_cs_init.restype = i
+        for name, args in (("uref_cs_flux_point", [d, d]), ("uref_cs_flux_form", [d, d]),
+                           ("uref_cs_form_factor", [d]), ("uref_cs_breakup_prob", [d, i]),
+                           ("uref_cs_gaa_spline", [d]), ("uref_cs_breakup_spline", [d]),
+                           ("uref_cs_lumi", [d, d]), ("uref_cs_photon_flux", [d, d]),
+                           ("uref_cs_rho0", [])):
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = d
+        L.uref_cs_lumi_pol.argtypes = [d, d, C.POINTER(d), C.POINTER(d)]
+        L.uref_cs_lumi_pol.restype = None
+        _ref_cs = L
+    return _ref_cs
+
+
+class RefCrossSection:
+    """One configuration of the reference's own UpcCrossSection:
+    UpcCrossSection::init without the luminosity file, then its member
+    functions point by point.  Like the reference, one configuration per
+    process: its nucleus and splines are globals, and calcBreakupProb builds
+    its photo-neutron tables once per process, for the Lorentz factor of its
+    first call (src/UpcCrossSection.cpp:774-898) -- use a fresh process for
+    each configuration."""
+
+    def __init__(self, params):
+        L = ref_cs_lib()
+        if L is None:
+            raise RuntimeError("reference sources not present")
+        p = dict({"NUCLEUS_Z": 82, "NUCLEUS_A": 208, "WS_R": 6.68, "WS_A": 0.447, "SQRTS": 5020,
+                  "FLUX_POINT": 1, "BREAKUP_MODE": 1, "PROC_ID": 15, "ALP_MASS": 1.0,
+                  "ALP_WIDTH": 0.01, "MMIN": 3.56, "MMAX": 50, "BINS_M": 1001, "YMIN": -6,
+                  "YMAX": 6, "BINS_Y": 121, "USE_POLARIZED_CS": 0}, **params)
+        self.L = L
+        L.uref_cs_init(int(p["NUCLEUS_Z"]), int(p["NUCLEUS_A"]), float(p["WS_R"]),
+                       float(p["WS_A"]), float(p["SQRTS"]), int(p["FLUX_POINT"]),
+                       int(p["BREAKUP_MODE"]), int(p["PROC_ID"]), float(p["ALP_MASS"]),
+                       float(p["ALP_WIDTH"]), float(p["MMIN"]), float(p["MMAX"]),
+                       int(p["BINS_M"]), float(p["YMIN"]), float(p["YMAX"]), int(p["BINS_Y"]),
+                       int(p["USE_POLARIZED_CS"]))
+
+    def rho0(self):
+        return self.L.uref_cs_rho0()
+
+    def flux_point(self, b, k):
+        return self.L.uref_cs_flux_point(b, k)
+
+    def flux_form(self, b, k):
+        return self.L.uref_cs_flux_form(b, k)
+
+    def form_factor(self, q2):
+        return self.L.uref_cs_form_factor(q2)
+
+    def breakup_prob(self, b, mode):
+        return self.L.uref_cs_breakup_prob(b, mode)
+
+    def gaa_spline(self, b):
+        return self.L.uref_cs_gaa_spline(b)
+
+    def breakup_spline(self, b):
+        return self.L.uref_cs_breakup_spline(b)
+
+    def two_photon_lumi(self, m, y):
+        return self.L.uref_cs_lumi(m, y)
+
+    def two_photon_lumi_pol(self, m, y):
+        s, q = C.c_double(), C.c_double()
+        self.L.uref_cs_lumi_pol(m, y, C.byref(s), C.byref(q))
+        return s.value, q.value
+
+    def photon_flux(self, m, y):
+        return self.L.uref_cs_photon_flux(m, y)
+
+
 _ref = None
 
 

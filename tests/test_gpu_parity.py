@@ -340,3 +340,64 @@ def test_generate_event_single(ug):
     g = _gen(ug, p)
     flags = [g.generateEvent()[0] for _ in range(3000)]
     assert set(flags) <= {0, 1} and 0 < sum(flags) < 3000
+
+
+def _ref_cs_fixture():
+    import json
+    with open(os.path.join(os.path.dirname(__file__), "golden", "ref_cs.json")) as f:
+        return json.load(f)["configs"]
+
+
+def _close(got, ref, rtol, atol=0.0):
+    got, ref = np.asarray(got, dtype=float), np.asarray(ref, dtype=float)
+    return np.all(np.abs(got - ref) <= rtol * np.abs(ref) + atol), np.max(
+        np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300))
+
+
+@pytest.mark.parametrize("name", ["pb_point_mode1", "pb_point_mode2", "pb_point_mode3",
+                                  "pb_point_mode4", "pb_form_mode2", "pb_form_mode2_pol",
+                                  "au200_form_mode4", "o16_form_mode3_alp"])
+def test_plain_path_vs_reference_source(ug, name):
+    """The plain FP64 GPU path against values of the reference's own
+    UpcCrossSection (src/UpcCrossSection.cpp compiled from source against the
+    oracle's primitives; tests/golden/make_ref_cs.py): luminosity cells at the
+    grid's mass and rapidity edges (calcTwoPhotonLumi / Pol, <= 1e-10), the
+    fluxes (fluxPoint <= 1e-12, fluxForm's QAGS <= 1e-9), the form factor, the
+    G_AA and breakup splines and the breakup probability (<= 1e-12), and
+    calcPhotonFlux (<= 1e-10)."""
+    e = _ref_cs_fixture()[name]
+    g = ug.UpcGenerator(e["params"])
+    g.setLumiMethod("plain")
+    cs = g.nucProcessCS
+    bk = np.array(e["flux_point"])
+    ok, r = _close(cs.fluxPoint(bk[:, 0], bk[:, 1]), bk[:, 2], 1e-12, 1e-300)
+    assert ok, ("fluxPoint", r)
+    bk = np.array(e["flux_form"])
+    ok, r = _close(cs.fluxForm(bk[:, 0], bk[:, 1]), bk[:, 2], 1e-9, 1e-300)
+    assert ok, ("fluxForm", r)
+    q = np.array(e["form_factor"])
+    ok, r = _close(cs.calcFormFac(q[:, 0]), q[:, 1], 1e-12)
+    assert ok, ("calcFormFac", r)
+    gs = np.array(e["gaa_spline"])
+    ok, r = _close(cs.spline("gaa", gs[:, 0]), gs[:, 1], 1e-12, 1e-15)
+    assert ok, ("G_AA spline", r)
+    bp = np.array(e["breakup_prob"])
+    ok, r = _close(cs.calcBreakupProb(bp[:, 0], e["params"]["BREAKUP_MODE"]), bp[:, 1], 1e-12, 1e-15)
+    assert ok, ("calcBreakupProb", r)
+    if "breakup_spline" in e:
+        bs = np.array(e["breakup_spline"])
+        ok, r = _close(cs.spline("breakup", bs[:, 0]), bs[:, 1], 1e-12, 1e-15)
+        assert ok, ("breakup spline", r)
+    if "lumi" in e:
+        c = np.array(e["lumi"])
+        ok, r = _close(cs.calcTwoPhotonLumi(c[:, 2], c[:, 3]), c[:, 4], 1e-10, 1e-300)
+        assert ok, ("calcTwoPhotonLumi", r)
+    else:
+        c = np.array(e["lumi_pol"])
+        s, p = cs.calcTwoPhotonLumiPol(c[:, 2], c[:, 3])
+        for got, ref in ((s, c[:, 4]), (p, c[:, 5])):
+            ok, r = _close(got, ref, 1e-10, 1e-300)
+            assert ok, ("calcTwoPhotonLumiPol", r)
+    pf = np.array(e["photon_flux"])
+    ok, r = _close(cs.calcPhotonFlux(pf[:, 0], pf[:, 1]), pf[:, 2], 1e-10, 1e-300)
+    assert ok, ("calcPhotonFlux", r)

@@ -1,9 +1,18 @@
 """Pins of the CPU oracle (no GPU).
 
-The reference cannot be built here (ROOT/GSL), so the oracle is pinned
+ROOT and GSL are not installed, so the reference cannot be built with its own
+build system.  The oracle is pinned
 (1) against the reference's own elementary cross sections, compiled from its
-sources (golden ref_elem.json, bit for bit), (2) primitive by primitive against
-scipy, and (3) against the independent numpy/scipy restatement in
+sources (golden ref_elem.json, bit for bit);
+(2) against the reference's own UpcCrossSection -- src/UpcCrossSection.cpp
+compiled where it lies against the GSL / ROOT stand-ins of oracle/refshim/,
+whose spline, QAGS and Bessel calls are the oracle's own primitives -- on
+rho0, G_AA, the form factor, both fluxes, the breakup probability and its
+spline, the luminosity cells (unpolarized and polarized, grid edges included)
+and the photonuclear flux, bit for bit (golden ref_cs.json, and the live
+build when the reference sources are present);
+(3) primitive by primitive against scipy; and
+(4) against the independent numpy/scipy restatement in
 tests/golden/make_golden.py (golden numpy_restatement.json).
 """
 import json
@@ -47,6 +56,74 @@ def test_live_reference_elementary(oracle_mod):
         assert o.cs_m(m, 0) == L.uref_dilep_cs_m(15, 0.0, m, 0)
         for z in np.linspace(-0.99, 0.99, 9):
             assert o.cs_zm(z, m, 0) == L.uref_dilep_cs_zm(15, 0.0, z, m, 0)
+
+
+def _check_ref_cs(oracle_mod, e, ref=None):
+    """The oracle against one configuration of ref_cs.json (bit for bit);
+    `ref`: the live reference build, checked at the same points as well."""
+    p = e["params"]
+    o = oracle_mod.Oracle(p, threads=4)
+    o.init_tables()
+    mode = p["BREAKUP_MODE"]
+    got = {"rho0": o.rho0()}
+    assert o.rho0() == e["rho0"]
+    for b, v in e["gaa_spline"]:
+        assert o.gaa(b) == v, ("gaa", b)
+    for q2, v in e["form_factor"]:
+        assert o.form_factor(q2) == v, ("ff", q2)
+    for b, k, v in e["flux_point"]:
+        assert o.flux_point(b, k) == v, ("flux_point", b, k)
+    for b, k, v in e["flux_form"]:
+        assert o.flux_form(b, k) == v, ("flux_form", b, k)
+    for b, v in e["breakup_prob"]:
+        assert o.breakup_prob(b, mode) == v, ("breakup", b)
+    for b, v in e.get("breakup_spline", []):
+        assert o.breakup_spline(b) == v, ("breakup spline", b)
+    for im, iy, m, y, v in e.get("lumi", []):
+        assert o.two_photon_lumi(m, y) == v, ("lumi", im, iy)
+    for im, iy, m, y, vs, vp in e.get("lumi_pol", []):
+        assert o.two_photon_lumi_pol(m, y) == (vs, vp), ("lumi pol", im, iy)
+    for m, y, v in e["photon_flux"]:
+        assert o.photon_flux(m, y) == v, ("photon flux", m, y)
+    if ref is not None:
+        assert ref.rho0() == got["rho0"]
+        for im, iy, m, y, v in e.get("lumi", []):
+            assert ref.two_photon_lumi(m, y) == v
+        for im, iy, m, y, vs, vp in e.get("lumi_pol", []):
+            assert ref.two_photon_lumi_pol(m, y) == (vs, vp)
+
+
+@pytest.mark.parametrize("name", ["pb_point_mode1", "pb_point_mode2", "pb_point_mode3",
+                                  "pb_point_mode4", "pb_form_mode2", "pb_form_mode2_pol",
+                                  "au200_form_mode4", "o16_form_mode3_alp"])
+def test_oracle_bit_exact_vs_reference_cross_section(oracle_mod, name):
+    """The oracle equals the reference's own UpcCrossSection (compiled from
+    src/UpcCrossSection.cpp; tests/golden/make_ref_cs.py) bit for bit:
+    calcWSRho, prepareGAA, calcFormFac, fluxPoint, fluxForm (QAGS at 1e-4),
+    calcBreakupProb / prepareBreakupProb, calcTwoPhotonLumi(Pol) on cells at
+    the grid's edges, calcPhotonFlux."""
+    _check_ref_cs(oracle_mod, load("ref_cs.json")["configs"][name])
+
+
+def _live_check(name):
+    from oracle import oracle
+    e = load("ref_cs.json")["configs"][name]
+    _check_ref_cs(oracle, e, oracle.RefCrossSection(e["params"]))
+    return True
+
+
+@pytest.mark.parametrize("name", ["pb_form_mode2", "au200_form_mode4"])
+def test_live_reference_cross_section(oracle_mod, name):
+    """The same against a live build of the reference's sources (skipped where
+    they are absent): the fixture is what the reference's code computes today.
+    Each configuration runs in a fresh process, as the reference needs
+    (calcBreakupProb builds its tables once per process)."""
+    if oracle_mod.ref_cs_lib() is None:
+        pytest.skip("reference sources not present on this machine")
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(1, mp_context=mp.get_context("spawn")) as ex:
+        assert ex.submit(_live_check, name).result()
 
 
 def test_bessel_k_vs_scipy(oracle_mod):

@@ -1406,6 +1406,10 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
         nn = __float_as_int(hd.z);
       }
       int cur = 0;
+      // node stencils 4.5 or more grid points apart never share a column
+      // (first points floor(t_i) - 1 at least 4 apart after rounding; always
+      // so for the form-factor flux, where b_max / b_min >= 100 gives >= 5)
+      const bool disjoint = tgd >= 4.5f;
       for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
         const int s = g % TST;
         if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 32u)) {
@@ -1424,19 +1428,49 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
 #pragma unroll
           for (int q = 0; q < 8; ++q)
             *reinterpret_cast<float4*>(stg + ((q ^ sw) << 2)) = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (int i = cur; i < nn; ++i) {
-            const float t = fmaf((float)i, tgd, tg0);
-            const int p0 = (int)floorf(t) - 1;
-            if (p0 > c_hi) break;
-            float wl[4];
-            lag4_weights(t - (float)p0, wl);
-            const float a = __ldg(nd + 4 + i);
+          if (disjoint) {
+            // stencils at least 4 points apart: every column gets at most one
+            // node's value, stored without reading the staging back; two
+            // nodes per iteration (independent loads and stores)
+            for (int i = cur; i < nn; i += 2) {
+              const float t0 = fmaf((float)i, tgd, tg0);
+              const int q0 = (int)floorf(t0) - 1;
+              if (q0 > c_hi) break;
+              const bool two = i + 1 < nn;
+              const float t1 = fmaf((float)(i + 1), tgd, tg0);
+              const int q1 = (int)floorf(t1) - 1;
+              const float a0 = __ldg(nd + 4 + i);
+              const float a1 = two ? __ldg(nd + 5 + i) : 0.f;
+              float w0[4], w1[4];
+              lag4_weights(t0 - (float)q0, w0);
+              lag4_weights(t1 - (float)q1, w1);
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-              const int c = p0 + m - c_lo;
-              if ((unsigned)c < 32u) {
-                float* e = stg + ((((c >> 2) ^ sw) << 2) | (c & 3));
-                *e = fmaf(a, wl[m], *e);
+              for (int m = 0; m < 4; ++m) {
+                const int c = q0 + m - c_lo;
+                if ((unsigned)c < 32u) stg[(((c >> 2) ^ sw) << 2) | (c & 3)] = a0 * w0[m];
+              }
+              if (!two || q1 > c_hi) break;
+#pragma unroll
+              for (int m = 0; m < 4; ++m) {
+                const int c = q1 + m - c_lo;
+                if ((unsigned)c < 32u) stg[(((c >> 2) ^ sw) << 2) | (c & 3)] = a1 * w1[m];
+              }
+            }
+          } else {
+            for (int i = cur; i < nn; ++i) {
+              const float t = fmaf((float)i, tgd, tg0);
+              const int p0 = (int)floorf(t) - 1;
+              if (p0 > c_hi) break;
+              float wl[4];
+              lag4_weights(t - (float)p0, wl);
+              const float a = __ldg(nd + 4 + i);
+#pragma unroll
+              for (int m = 0; m < 4; ++m) {
+                const int c = p0 + m - c_lo;
+                if ((unsigned)c < 32u) {
+                  float* e = stg + ((((c >> 2) ^ sw) << 2) | (c & 3));
+                  *e = fmaf(a, wl[m], *e);
+                }
               }
             }
           }
