@@ -259,22 +259,86 @@ CONTRACT_DRAM_BYTES_PER_CELL = (521.124608e6 + 4.506880e6) / 63063
 PROJECT_DRAM_BYTES_PER_CELL = (10.690816e6 + 457.163520e6) / 63063
 
 
-def run_scan(args, ug, torch):
-    """C5: 64 configurations in one captured scan (upcg_scan_*), replayed;
-    then 1e9 events over them into one device buffer.  A step is one replay
-    (every configuration's tables, one persistent contraction, samplers)."""
+def c2_parity(fast, tot_fast, plain=None):
+    """The full 1001 x 121 table against the committed oracle fixture
+    (tests/golden/c2_lumi.npz): the fast form against the converged flux
+    quadrature and against the reference's own quadrature (QAGS at 1e-4), the
+    plain path against the reference's quadrature; every cell."""
+    path = os.path.join(ROOT, "tests", "golden", "c2_lumi.npz")
+    if not os.path.exists(path):
+        return None
+    d = np.load(path)
+    conv, ref = d["conv"], d["ref"]
+    mx = conv.max()
+
+    def stats(a, b):
+        rel = np.abs(a / b - 1)
+        out = {}
+        for name, thr in (("above_1e-4_of_max", 1e-4), ("above_1e-5_of_max", 1e-5), ("all", 0.0)):
+            m = conv >= thr * mx
+            out[name] = {"cells": int(m.sum()), "max_rel": float(rel[m].max()),
+                         "median_rel": float(np.median(rel[m])),
+                         "cells_rel_above_1e-4": int((rel[m] > 1e-4).sum())}
+        return out
+
+    res = {"fixture": "tests/golden/c2_lumi.npz (oracle: ref = QAGS 1e-4 as the reference, "
+                      "conv = converged flux integral)",
+           "fast_vs_converged": stats(fast, conv),
+           "fast_vs_reference_quadrature": stats(fast, ref),
+           "reference_quadrature_vs_converged": stats(ref, conv),
+           "fast_sigma_tot_vs_converged": abs(tot_fast / float(d["sigma_tot_conv"]) - 1),
+           "fast_sigma_tot_vs_reference_quadrature": abs(tot_fast / float(d["sigma_tot_ref"]) - 1)}
+    if plain is not None:
+        res["plain_vs_reference_quadrature_max_rel"] = float(np.max(np.abs(plain / ref - 1)))
+    return res
+
+
+def event_file_rates(gen, n_cols=10_000_000, n_hepmc=2_000_000):
+    """generateEvents with file output (src/UpcGenerator.cpp:589-628, 834-926):
+    the particle-tree columns (n_cols events) and HepMC3 text (n_hepmc events)
+    written to a temporary directory, wall clock through the API; each file
+    is removed afterwards."""
+    import shutil
+    import tempfile
+    out = {}
+    d = tempfile.mkdtemp(prefix="upcg_bench_")
+    try:
+        for fmt, n, name in (("columns", n_cols, "events.cols"), ("hepmc", n_hepmc, "events.hepmc")):
+            path = os.path.join(d, name)
+            gen.writeEvents(path, 1000, fmt)  # the writer's buffers and threads
+            t0 = time.perf_counter()
+            gen.writeEvents(path, n, fmt)
+            dt = time.perf_counter() - t0
+            size = os.path.getsize(path)
+            os.remove(path)
+            out[fmt] = {"events": n, "events_per_s": n / dt, "file_gb_per_s": size / dt / 1e9,
+                        "file_bytes": size}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    out["host_threads"] = os.cpu_count()
+    out["note"] = ("device generation of batch k+1 overlaps the host's formatting and writing of "
+                   "batch k; HepMC3 text is formatted on every host core")
+    return out
+
+
+def scan_c5(ug, torch, steps, warmup, nev):
+    """C5: the 64 ALP configurations built by one captured scan (upcg_scan_*),
+    replayed; then nev events over them into one device buffer.  A step is one
+    replay (every configuration's tables, one persistent contraction, the
+    samplers)."""
     import ctypes as C
     cfgs = c5_configs()
     gens = [ug.UpcGenerator(c) for c in cfgs]
     scan = ug.Scan(gens)
+    t0 = time.perf_counter()
     setup_first = scan.run()
-    for _ in range(args.warmup):
+    setup_wall = time.perf_counter() - t0
+    for _ in range(warmup):
         scan.run()
     torch.cuda.synchronize()
-    ms = [scan.run() for _ in range(args.steps)]
+    ms = [scan.run() for _ in range(steps)]
     cells = sum(g.grid()["nm"] * g.grid()["ny"] for g in gens)
     ms_step = float(np.mean(ms))
-    nev = args.events if args.events is not None else EVENTS["c5"]
     per = nev // len(gens)
     buf = torch.empty(max(per, 1) * 48, dtype=torch.uint8, device="cuda")
     torch.cuda.synchronize()
@@ -286,16 +350,31 @@ def run_scan(args, ug, torch):
     torch.cuda.synchronize()
     t_ev = time.perf_counter() - t0
     info = scan.info()
+    return {"configurations": len(gens), "cells": cells, "ms_per_replay": ms_step,
+            "cells_per_s": cells / (ms_step * 1e-3), "replays": steps,
+            "rows": info["rows"], "items": info["items"], "shape": info["shape"],
+            "setup_and_first_run_s": setup_wall, "first_run_ms": setup_first,
+            "events": per * len(gens), "events_per_s": per * len(gens) / t_ev,
+            "events_wall_s": t_ev,
+            "note": "64 ALP configurations (Pb, Au, Xe, O x sqrt(s) 200/5020/5360/5440 GeV x "
+                    "breakup modes 1-4; m-bins 201/501/1001, 121 y-bins), one captured graph "
+                    "per replay; events without cuts, device buffer"}
+
+
+def run_scan(args, ug, torch):
+    """--workload c5: the scan as the line's own workload."""
+    nev = args.events if args.events is not None else EVENTS["c5"]
+    r = scan_c5(ug, torch, args.steps, args.warmup, nev)
     print(json.dumps({
-        "metric": METRIC, "value": cells / (ms_step * 1e-3), "unit": "cells/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "metric": METRIC, "value": r["cells_per_s"], "unit": "cells/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_replay"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+bf16x3",
         "data": "synthetic (the workload is a parameter set)",
-        "config": {"workload": f"c5: {len(gens)} ALP configurations, {cells} (m,y) cells, one "
-                               f"captured scan per step; {per * len(gens)} events",
-                   "rows": info["rows"], "items": info["items"], "shape": info["shape"],
-                   "setup_and_first_run_ms": info["setup_ms"] + setup_first},
-        "events_per_s": per * len(gens) / t_ev, "events_wall_s": t_ev,
+        "config": {"workload": f"c5: {r['configurations']} ALP configurations, {r['cells']} (m,y) "
+                               f"cells, one captured scan per step; {r['events']} events",
+                   "rows": r["rows"], "items": r["items"], "shape": r["shape"],
+                   "setup_and_first_run_s": r["setup_and_first_run_s"]},
+        "events_per_s": r["events_per_s"], "events_wall_s": r["events_wall_s"],
     }))
 
 
@@ -311,6 +390,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=None)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-scan", action="store_true", help="skip the 64-configuration scan")
+    ap.add_argument("--no-files", action="store_true", help="skip the event-file output timing")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -334,8 +415,12 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     params = dict(WORKLOADS[args.workload])
-    params["SEED"] = 1 + rank  # independent replicas: weak scaling over ranks
-    nev = args.events if args.events is not None else EVENTS[args.workload]
+    # N > 1: one table split over the ranks by m-rows (the reference's OpenMP
+    # m-slices, src/UpcCrossSection.cpp:537-538), all-gathered over NCCL on the
+    # device; every rank builds the replicated samplers and draws its share of
+    # the events from its own Philox counter range (upcgen_gb300/shard.py)
+    nev_total = args.events if args.events is not None else EVENTS[args.workload]
+    nev = nev_total // world + (1 if rank < nev_total % world else 0)
     stream = torch.cuda.Stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     evbuf = torch.empty(max(nev, 1) * 48, dtype=torch.uint8, device="cuda")
@@ -358,9 +443,19 @@ def main():
     def step(gen, with_events):
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         flush_l2()
-        s0.record(stream)
-        gen.init()
-        s1.record(stream)
+        if world > 1:
+            # the sharded build synchronises with the host (the all-gather runs
+            # on torch's stream): timed by the host clock between barriers
+            from upcgen_gb300 import shard
+            barrier()
+            t0 = time.perf_counter()
+            shard.sharded_init(gen, rank, world)
+            torch.cuda.synchronize()
+            tab_ms = 1e3 * (time.perf_counter() - t0)
+        else:
+            s0.record(stream)
+            gen.init()
+            s1.record(stream)
         ev_ms, rej = None, None
         if with_events and nev:
             flush_l2()
@@ -373,11 +468,19 @@ def main():
             stream.synchronize()
             ev_ms, rej = e0.elapsed_time(e1), r.value
         stream.synchronize()
-        return s0.elapsed_time(s1), ev_ms, rej, gen.timings()
+        if world == 1:
+            tab_ms = s0.elapsed_time(s1)
+        return tab_ms, ev_ms, rej, gen.timings()
 
     fast = make("fast")
     g0 = fast.grid()
     cells = g0["nm"] * g0["ny"]
+    # the cold first init of a process (one configuration per process, as the
+    # reference's main runs): allocations, static uploads, the contraction
+    # autotuner, every table; host wall clock, init returns synchronised
+    t0 = time.perf_counter()
+    fast.init()
+    cold_init_ms = 1e3 * (time.perf_counter() - t0)
     for _ in range(args.warmup):
         step(fast, True)
     barrier()
@@ -397,32 +500,34 @@ def main():
         t = torch.tensor([ms_tab, ms_ev or 0.0, ms_contract], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_tab, ms_ev, ms_contract = float(t[0]), float(t[1]) or None, float(t[2])
-    value = world * cells / (ms_tab * 1e-3)
+    # one table per step whatever the rank count: its cells over the slowest
+    # rank's time (strong scaling for N > 1)
+    value = cells / (ms_tab * 1e-3)
 
     # the plain FP64 path on the same workload (the reference's quadrature)
     pk = args.plain_steps if args.plain_steps is not None else (2 if args.workload == "c2" else args.steps)
     fvp = None
     pruns = []
+    lf = fast.lumiTable()
+    _, tot_f = fast.nucCSYM()
     if pk > 0:
         plain = make("plain")
         step(plain, False)
         pruns = [step(plain, False) for _ in range(pk)]
         ms_plain = float(np.mean([r[0] for r in pruns]))
-        lf, lp = fast.lumiTable(), plain.lumiTable()
-        _, tot_f = fast.nucCSYM()
+        lp = plain.lumiTable()
         _, tot_p = plain.nucCSYM()
         big = np.abs(lp) >= 1e-5 * np.abs(lp).max()
         rel = np.abs(lf - lp)[big] / np.abs(lp[big])
         fvp = {"max_rel_err_cells_above_1e-5_of_max": float(rel.max()),
                "median_rel_err": float(np.median(rel)),
                "sigma_tot_rel_err": abs(tot_f / tot_p - 1),
-               "note": "vs the plain path, i.e. the reference's own QAGS at 1e-4, which is off by "
-                       "up to 1.2e-1 on those cells; against a converged quadrature the fast form "
-                       "stays within 5.1e-5 (tests/test_gpu_fast.py)",
+               "note": "vs the plain path, i.e. the reference's own QAGS at 1e-4; see parity",
                "plain_ms_per_step": ms_plain,
                "plain_cells_per_s": cells / (ms_plain * 1e-3),
                "speedup": ms_plain / ms_tab}
         del plain
+    parity = c2_parity(lf, tot_f, lp if pk > 0 else None) if args.workload == "c2" else None
 
     # end to end through the public API, host buffers: init, then the
     # luminosity table, sigma(y, m) and its total copied to the host, into
@@ -471,13 +576,14 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_tab,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+bf16x3",
+        "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f64+bf16x3",
         "data": "synthetic (the workload is a parameter set)",
         "config": {"workload": workload_name(args.workload, params, g0["nm"], g0["ny"], nev),
                    "lumi_method": "fast form (tcgen05 3xBF16 contraction)",
                    "l2": "flushed (256 MB write) before each timed phase"},
         "fast_vs_plain": fvp,
-        "events_per_s": world * nev / (ms_ev * 1e-3) if nev else None,
+        "parity": parity,
+        "events_per_s": nev_total / (ms_ev * 1e-3) if nev else None,
         "ms_events": ms_ev, "rejected_per_step": runs[-1][2],
         "sigma_tot_mb": tot,
         "phases_ms": ph, "plain_phases_ms": pruns[-1][3] if pruns else None,
@@ -503,14 +609,20 @@ def main():
             "note": "algorithmic bytes = the 8 KB per computed cell (row) of contraction operands written "
                     "(A1 bf16 hi + lo, A2 fp32); project_ms also holds the G and flux-table builds; "
                     "traffic = DRAM bytes per launch (profiles/k_fast_project_c2.md)"},
+        "cold_first_init_ms": cold_init_ms,
         "gpu_launches": n_launch,
         "clocks": clk,
     }
     if line["roofline_projection"]["achieved"]:
         line["roofline_projection"]["frac"] = (line["roofline_projection"]["achieved"] /
                                                line["roofline_projection"]["peak"])
+    if rank == 0 and args.workload == "c2" and not args.no_files:
+        line["event_files"] = event_file_rates(fast)
+    if rank == 0 and args.workload == "c2" and not args.no_scan:
+        # the batched scan (C5) of the same run, beside the headline table
+        line["c5_scan"] = scan_c5(ug, torch, steps=5, warmup=2, nev=EVENTS["c5"])
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(args.workload, lf if pk > 0 else None)
+        line["cpu_baseline"] = cpu_baseline_sample(args.workload, lf)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

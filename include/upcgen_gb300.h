@@ -89,14 +89,19 @@ int upcg_set_stream(upcg_generator* g, void* stream);
  * the converged quadrature), 2 = the fast form's contraction on the plain
  * path's node fluxes (diagnostic), 3 = grid form (point flux): fixed
  * 4096-energy x 2048-radius grids, L = N G N^T as two tensor-core products
- * (its own quadrature: the difference to the reference is stated by the tests),
+ * (its own quadrature: the difference to the reference is stated by the tests)
+ * in the three-term bf16 split, 7 = the same grid form with TF32 products
+ * (tcgen05 kind::tf32, one product per k step),
  * 4 = the fast form with the form-factor flux rows inside the learned
- * surrogate's box from the surrogate (upcg_set_flux_surrogate), 5 = the fast
- * form with the projection and the contraction as two kernels (dense operands
- * through device memory; the same table as 1 up to FP32 summation order --
- * methods 1, 2 and 4 build the contraction's operands inside it).  With
- * USE_POLARIZED_CS the fast form (1, 4, 5) builds the scalar and pseudoscalar
- * tables of calcTwoPhotonLumiPol from the same operands. */
+ * surrogate's box from the surrogate (upcg_set_flux_surrogate).  Methods 5
+ * and 6 are the fast form with other operand paths, for comparison: 1, 2 and
+ * 4 write the contraction's dense A1 rows and side 1's node lists (the
+ * epilogue gathers the A2 row-dot at the node stencils); 5 writes both
+ * operands dense (A2 read back by the epilogue); 6 writes node lists only and
+ * builds A1 in the contraction's shared memory.  All three give the same
+ * table up to FP32 summation order.  With USE_POLARIZED_CS the fast form (1,
+ * 4, 5, 6) builds the scalar and pseudoscalar tables of calcTwoPhotonLumiPol
+ * from the same operands. */
 int upcg_set_lumi_method(upcg_generator* g, int method);
 
 /* ---- initialisation (UpcGenerator::init) ------------------------------ */

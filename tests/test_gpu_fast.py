@@ -189,24 +189,53 @@ def test_grid_form_config3(ug, oracle_mod):
     dict(C1, PROC_ID=15, FLUX_POINT=0, BREAKUP_MODE=2, BINS_M=41, BINS_Y=25),
     dict(C1, PROC_ID=13, BREAKUP_MODE=2, USE_POLARIZED_CS=1, FLUX_POINT=0, BINS_M=21, BINS_Y=25),
 ], ids=["point-201x61", "form-xnxn", "form-polarized"])
-def test_fused_contraction_equals_staged(ug, params):
-    """The fused contraction (operands built in shared memory from the rows'
-    node lists) against the staged one (dense operands written by the
-    projection kernel and read back by TMA): the same bf16 hi / lo operands
-    and survival kernel, so the tables differ only by the FP32 summation order
-    of the row-dot (<= 2e-6 relative on cells above 1e-12 of the maximum)."""
+@pytest.mark.parametrize("other", ["staged", "fused"])
+def test_operand_paths_agree(ug, params, other):
+    """The fast form's three operand paths on the same bf16 hi / lo operands and
+    survival kernel: the default (dense A1 through TMA, the A2 row-dot gathered
+    at side 1's node stencils), "staged" (both operands dense, A2 read back)
+    and "fused" (A1 built in shared memory from the node lists).  The tables
+    differ only by the FP32 summation order of the row-dot (<= 2e-6 relative
+    on cells above 1e-12 of the maximum)."""
     out = {}
     pol = params.get("USE_POLARIZED_CS", 0)
-    for meth in ("fast", "staged"):
+    for meth in ("fast", other):
         g = ug.UpcGenerator(params)
         g.setLumiMethod(meth)
         g.init()
         out[meth] = g.lumiTable(polarized=bool(pol))
         out[meth + "_tot"] = g.nucCSYM()[1]
-    pairs = zip(out["fast"], out["staged"]) if pol else [(out["fast"], out["staged"])]
+    pairs = zip(out["fast"], out[other]) if pol else [(out["fast"], out[other])]
     for a, b in pairs:
         big = np.abs(b) >= 1e-12 * np.abs(b).max()
         assert np.all((a == 0) == (b == 0))
         rel = np.abs(a[big] / b[big] - 1)
         assert rel.max() <= 2e-6, rel.max()
-    assert abs(out["fast_tot"] / out["staged_tot"] - 1) <= 1e-6
+    assert abs(out["fast_tot"] / out[other + "_tot"] - 1) <= 1e-6
+
+
+def test_grid_form_tf32_arm(ug, oracle_mod):
+    """Luminosity method 7: the grid form with its two products on tcgen05
+    kind::tf32 (FP32 operands, 10 mantissa bits kept, FP32 accumulation)
+    instead of the three-term bf16 split.  It carries the grid form's own
+    quadrature difference (as method 3) plus the TF32 rounding; both are
+    stated here against the oracle, beside the bf16x3 arm on the same table."""
+    p = dict(C1, BREAKUP_MODE=2)
+    o = oracle_mod.Oracle(p, threads=os.cpu_count())
+    o.init_tables()
+    ref = o.lumi_table()
+    big = np.abs(ref) >= 1e-5 * np.abs(ref).max()
+    out = {}
+    for meth in ("grid", "grid-tf32"):
+        g = ug.UpcGenerator(p)
+        g.setLumiMethod(meth)
+        g.init()
+        lumi = g.lumiTable()
+        out[meth] = (np.abs(lumi / ref - 1)[big], g.nucCSYM()[1], g.timings()["contract_ms"])
+    rel32, tot32, _ = out["grid-tf32"]
+    rel16, tot16, _ = out["grid"]
+    _, rtot, _ = o.nuc_cs_ym(ref)
+    assert rel32.max() < 1e-2 and np.median(rel32) < 3e-3, (rel32.max(), np.median(rel32))
+    assert abs(tot32 / rtot - 1) < 2e-3
+    # the TF32 rounding on top of the grid quadrature's difference
+    assert np.median(rel32) < 3 * np.median(rel16) + 1e-3

@@ -282,6 +282,8 @@ struct upcg_generator {
   bool lumiCache = false;
   int lumi_cache_hit = -1;  // last init: 1 table read from the cache, 0 computed, -1 cache unused
   int lumiMethod = 0;
+  // the fast form's tables (65,536-knot form factor, FP32 breakup sums): methods 1, 4, 5, 6
+  bool fast_tables() const { return lumiMethod == 1 || lumiMethod == 4 || lumiMethod == 5 || lumiMethod == 6; }
   int row_lo = 0, row_hi = -1;  // m-rows of the luminosity this handle computes (-1: all)
   upcg_mlp* surrogate = nullptr;  // luminosity method 4: Q(w, b) rows from the MLP
   int surrogate_rows = 0;         // rows of the last Q table that came from it
@@ -365,6 +367,7 @@ struct upcg_generator {
   // grid form: G, flux matrix, T = N G (bf16 hi/lo), Lg, row sums and tails
   DBuf<uint16_t> gg_h, gg_l, gn_h, gn_l, gt_h, gt_l;
   DBuf<float> g_lg;
+  DBuf<float> g_n32, g_g32, g_t32;  // grid form, TF32 arm: FP32 N, G and T = N G
   DBuf<double> g_rowsum, g_tail;
   DBuf<unsigned> ferr;
   DBuf<int32_t> mbinbuf;
@@ -771,7 +774,7 @@ int upcg_generator::build_tables() {
   else
     CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s));
   // form factor on 1e6 knots (the reference's), 65,536 for the fast form
-  ff_n = (lumiMethod == 1 || lumiMethod == 4 || lumiMethod == 5) ? kNQ2Fast : kNQ2;
+  ff_n = fast_tables() ? kNQ2Fast : kNQ2;
   const double dq = (kQ2max - kQ2min) / ff_n;
   CK(ff_y.ensure(ff_n));
   CK(ff_c.ensure(ff_n));
@@ -784,8 +787,7 @@ int upcg_generator::build_tables() {
     CK(build_spline_uniform(ff_y.p, ff_n, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
   }
   ftab_early = false;
-  if (!cap && !isVM &&
-      (lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4 || lumiMethod == 5)) {
+  if (!cap && !isVM && (lumiMethod == 2 || fast_tables())) {
     // the fast form's flux tables need only the form factor: they run here,
     // beside the breakup and G_AA chains
     for (auto& e : ev_ft)
@@ -823,7 +825,7 @@ int upcg_generator::build_tables() {
     // the fast form (methods 1, 4; budget 1e-4) takes the FP32 sums (~1e-6);
     // the reference's sum steps where an energy crosses omax(b), so every
     // knot is summed (an interpolated table smears those steps to 1.5e-5)
-    const int brk_fp32 = (lumiMethod == 1 || lumiMethod == 4 || lumiMethod == 5) ? 1 : 0;
+    const int brk_fp32 = fast_tables() ? 1 : 0;
     CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
                              1e-6, dbb, brk_y.p, side[1], brk_fp32));
     CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1]));
@@ -928,10 +930,23 @@ int upcg_generator::build_lumi_grid() {
   cudaEventRecord(ev[1], s);
   CK(ferr.ensure(1));
   CK(cudaMemsetAsync(ferr.p, 0, sizeof(unsigned), s));
-  CK(launch_gemm_bf16x3(gn_h.p, gn_l.p, gg_h.p, gg_l.p, nw, nr, nr, nullptr, gt_h.p, gt_l.p,
-                        ferr.p, s));
-  CK(launch_gemm_bf16x3(gt_h.p, gt_l.p, gn_h.p, gn_l.p, nw, nw, nr, g_lg.p, nullptr, nullptr,
-                        ferr.p, s));
+  if (lumiMethod == 7) {
+    // TF32 arm: FP32 operands (the hi / lo pairs summed), one kind::tf32
+    // product per k step instead of the three bf16 ones
+    CK(g_n32.ensure(nwp * nr));
+    CK(g_g32.ensure((size_t)nr * nr));
+    CK(g_t32.ensure(nwp * nr));
+    CK(launch_pair_to_f32(gn_h.p, gn_l.p, nwp * nr, g_n32.p, s));
+    CK(launch_pair_to_f32(gg_h.p, gg_l.p, (size_t)nr * nr, g_g32.p, s));
+    cudaEventRecord(ev[1], s);
+    CK(launch_gemm_tf32(g_n32.p, g_g32.p, nw, nr, nr, g_t32.p, ferr.p, s));
+    CK(launch_gemm_tf32(g_t32.p, g_n32.p, nw, nw, nr, g_lg.p, ferr.p, s));
+  } else {
+    CK(launch_gemm_bf16x3(gn_h.p, gn_l.p, gg_h.p, gg_l.p, nw, nr, nr, nullptr, gt_h.p, gt_l.p,
+                          ferr.p, s));
+    CK(launch_gemm_bf16x3(gt_h.p, gt_l.p, gn_h.p, gn_l.p, nw, nw, nr, g_lg.p, nullptr, nullptr,
+                          ferr.p, s));
+  }
   cudaEventRecord(ev[2], s);
   CK(launch_grid_cells(p, gf, g_lg.p, g_rowsum.p, g_tail.p, lumi.p, s));
   cudaEventRecord(ev[3], s);
@@ -1154,7 +1169,7 @@ int upcg_generator::complete_deferred(int rc) {
 }
 
 int upcg_generator::build_lumi() {
-  if (lumiMethod == 3) return build_lumi_grid();
+  if (lumiMethod == 3 || lumiMethod == 7) return build_lumi_grid();
   cudaStream_t s = st();
   const int ncell = nm * ny;
   CK(lumi.ensure(ncell));
@@ -1182,13 +1197,14 @@ int upcg_generator::build_lumi() {
   LumiParams p = lumi_params();
   p.mirror = mirror.p;
   // 1: fast form (flux tables + tensor-core contraction); 2: the same
-  // contraction on the plain path's exact node fluxes (QAGS / K0,K1); 5: the
-  // fast form with the projection and the contraction as two kernels (dense
-  // operands through HBM), the others fold the projection into the
-  // contraction (node lists, k_contract_fused)
-  const bool fast = lumiMethod == 1 || lumiMethod == 2 || lumiMethod == 4 || lumiMethod == 5;
+  // contraction on the plain path's exact node fluxes (QAGS / K0,K1).  The
+  // contraction's operands: methods 1, 2, 4 write the dense A1 rows and side
+  // 1's node lists (the epilogue gathers the A2 row-dot at the node
+  // stencils); 5 writes both dense rows (A2 read back by the epilogue); 6
+  // writes node lists only and builds A1 in shared memory (k_contract_fused)
+  const bool fast = lumiMethod == 2 || fast_tables();
   const bool node_flux = lumiMethod == 2 || !fast;
-  const bool staged = lumiMethod == 5;
+  const bool staged = lumiMethod == 5, fused = lumiMethod == 6;
   // cells per chunk: the node-flux paths hold 1.9 KB of node fluxes per cell,
   // the fast form 8 KB of contraction operands; its chunks are larger, so
   // that a table needs fewer persistent contractions (2 GB at 2^18 cells)
@@ -1210,14 +1226,13 @@ int upcg_generator::build_lumi() {
   if (fast) {
     CK(fgh.ensure((size_t)P * P));
     CK(fgl.ensure((size_t)P * P));
-    if (staged) {
+    if (!fused) {
       CK(fah.ensure((size_t)chunk_pad * P));
       CK(fal.ensure((size_t)chunk_pad * P));
-      CK(fa2.ensure((size_t)chunk_pad * P));
-    } else {
-      CK(fnodes.ensure((size_t)chunk_pad * fast_node_floats_per_row()));
     }
-    CK(ffar.ensure(2 * (size_t)chunk_pad));  // one float4 per cell
+    if (staged) CK(fa2.ensure((size_t)chunk_pad * P));
+    else CK(fnodes.ensure((size_t)chunk_pad * fast_node_floats_per_row()));
+    CK(ffar.ensure(4 * (size_t)chunk_pad));  // per row and side: (ln scale, near, far) float4
     CK(fsides.ensure((2 * (size_t)chunk * fast_side_bytes() + 7) / 8));
     CK(fpart.ensure((size_t)chunk_pad * (P / 128)));
     CK(ferr.ensure(1));
@@ -1330,14 +1345,15 @@ int upcg_generator::build_lumi() {
       const int ncp = (nc + 127) / 128 * 128;
       b = mark();
       CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, flnm2.p, c_far,
-                             node_flux ? flux.p : nullptr, &ftab, fsides.p, fah.p, fal.p, fa2.p,
-                             ffar.p, s, use_map ? frep.p : nullptr, n_rep, r0,
-                             staged ? nullptr : fnodes.p));
+                             node_flux ? flux.p : nullptr, &ftab, fsides.p,
+                             fused ? nullptr : fah.p, fused ? nullptr : fal.p,
+                             staged ? fa2.p : nullptr, ffar.p, s, use_map ? frep.p : nullptr, n_rep,
+                             r0, staged ? nullptr : fnodes.p));
       spans.push_back({4, {b, mark()}});
       // persistent contraction over this chunk's (row tile, N tile) work list
       int shape = 0, grid = 0;
       {
-        const int rc = contract_plan(ncp, nc, P, &shape, &grid, staged ? 0 : 1);
+        const int rc = contract_plan(ncp, nc, P, &shape, &grid, fused ? 1 : 0);
         if (rc) return rc;
       }
       const int tbn = shape == 0 ? 256 : 128;
@@ -1348,20 +1364,22 @@ int upcg_generator::build_lumi() {
       CK(fitems.ensure(items.size()));
       CK(upload(fitems.p, items.data(), items.size() * sizeof(int4), s));
       b = mark();
-      if (staged)
-        CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p,
-                                (int)items.size(), fa2.p, fpart.p, ferr.p, shape, grid, s));
-      else
+      if (fused)
         CK(launch_contract_fused(fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(), fnodes.p,
                                  fpart.p, ferr.p, shape, grid, s));
+      else
+        CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p,
+                                (int)items.size(), staged ? fa2.p : nullptr, fpart.p, ferr.p,
+                                shape, grid, s, staged ? nullptr : fnodes.p));
       if (usePolarizedCS) {  // the same operands against the pseudoscalar kernel
         CK(fpart2.ensure(fpart.n));
-        if (staged)
-          CK(launch_contract_pers(fah.p, fal.p, fgh2.p, fgl2.p, 1, ncp, P, fitems.p,
-                                  (int)items.size(), fa2.p, fpart2.p, ferr.p, shape, grid, s));
-        else
+        if (fused)
           CK(launch_contract_fused(fgh2.p, fgl2.p, 1, ncp, P, fitems.p, (int)items.size(),
                                    fnodes.p, fpart2.p, ferr.p, shape, grid, s));
+        else
+          CK(launch_contract_pers(fah.p, fal.p, fgh2.p, fgl2.p, 1, ncp, P, fitems.p,
+                                  (int)items.size(), staged ? fa2.p : nullptr, fpart2.p, ferr.p,
+                                  shape, grid, s, staged ? nullptr : fnodes.p));
       }
       spans.push_back({3, {b, mark()}});
       CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s, ffc.p,
@@ -1740,8 +1758,8 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
 // fold and the samplers.
 struct upcg_scan {
   std::vector<upcg_generator*> gens;
-  DBuf<uint16_t> gh, gl;
-  DBuf<float> nodes, part;  // node lists of every configuration's rows (stacked)
+  DBuf<uint16_t> ah, al, gh, gl;  // stacked A1 rows (bf16 hi / lo), survival kernels
+  DBuf<float> nodes, part;        // side 1's node lists of every configuration's rows
   DBuf<double> far, fc;
   DBuf<int4> items;
   DBuf<unsigned> err;
@@ -1779,8 +1797,8 @@ int upcg_generator::enqueue_scan_front(upcg_scan& sc, int ci) {
   const size_t r0 = (size_t)sc.row0[ci];
   const int nrows = nm * (fast_nrep > 0 ? fast_nrep : ny);
   CK(launch_fast_project(p, fu0, fh, P, 0, nrows, sc.rows[ci], flnm2.p, 0.0, nullptr, &ft,
-                         fsides.p, nullptr, nullptr, nullptr, sc.far.p + 2 * r0, s,
-                         fast_nrep > 0 ? frep.p : nullptr, fast_nrep, 0,
+                         fsides.p, sc.ah.p + r0 * P, sc.al.p + r0 * P, nullptr,
+                         sc.far.p + 4 * r0, s, fast_nrep > 0 ? frep.p : nullptr, fast_nrep, 0,
                          sc.nodes.p + r0 * fast_node_floats_per_row()));
   cap = false;
   return UPCG_OK;
@@ -1792,7 +1810,7 @@ int upcg_generator::enqueue_scan_back(upcg_scan& sc, int ci) {
   const int ntiles = sc.P / (sc.shape == 0 ? 256 : 128);
   const size_t r0 = (size_t)sc.row0[ci];
   const int nrows = nm * (fast_nrep > 0 ? fast_nrep : ny);
-  CK(launch_fast_finish(p, 0, nrows, ntiles, 0.0, sc.part.p + r0 * ntiles, sc.far.p + 2 * r0,
+  CK(launch_fast_finish(p, 0, nrows, ntiles, 0.0, sc.part.p + r0 * ntiles, sc.far.p + 4 * r0,
                         lumi.p, s, sc.fc.p + 2 * ci, fast_nrep > 0 ? frep.p : nullptr,
                         fast_nrep > 0 ? frep.p + fast_nrep : nullptr, fast_nrep, 0));
   lumi_ready = true;
@@ -1891,7 +1909,7 @@ int upcg_set_stream(upcg_generator* g, void* stream) {
 }
 
 int upcg_set_lumi_method(upcg_generator* g, int method) {
-  if (!g || method < 0 || method > 5) return fail(UPCG_ERR_ARG, "bad luminosity method");
+  if (!g || method < 0 || method > 7) return fail(UPCG_ERR_ARG, "bad luminosity method");
   if (method != g->lumiMethod) g->invalidate();
   g->lumiMethod = method;
   return UPCG_OK;
@@ -2823,9 +2841,11 @@ int scan_setup(upcg_scan* sc) {
   }
   sc->rows_total = (int)rows_total;
   const size_t plane = (size_t)P * P;
+  CK(sc->ah.ensure((size_t)rows_total * P));
+  CK(sc->al.ensure((size_t)rows_total * P));
   CK(sc->nodes.ensure((size_t)rows_total * fast_node_floats_per_row()));
   CK(sc->part.ensure((size_t)rows_total * (P / 128)));
-  CK(sc->far.ensure(2 * (size_t)rows_total));
+  CK(sc->far.ensure(4 * (size_t)rows_total));
   CK(sc->gh.ensure(n * plane));
   CK(sc->gl.ensure(n * plane));
   CK(sc->fc.ensure(2 * (size_t)n));
@@ -2833,7 +2853,7 @@ int scan_setup(upcg_scan* sc) {
   // tile shape from the autotuner, then the work list: per configuration its
   // row tiles, the N tiles of a row tile adjacent (L2 reuse of A)
   int rc = contract_plan(std::min(sc->rows_total, 131072), sc->rows_total, P, &sc->shape,
-                         &sc->grid, 1);
+                         &sc->grid, 0);
   if (rc) return rc;
   const int tbn = sc->shape == 0 ? 256 : 128;
   std::vector<int4> items;
@@ -2862,9 +2882,9 @@ int scan_setup(upcg_scan* sc) {
     rc = sc->gens[i]->enqueue_scan_front(*sc, i);
     if (rc) return abort_capture(rc);
   }
-  if (launch_contract_fused(sc->gh.p, sc->gl.p, n, sc->rows_total, P, sc->items.p, sc->nitems,
-                            sc->nodes.p, sc->part.p, sc->err.p, sc->shape, sc->grid,
-                            sc->s) != cudaSuccess)
+  if (launch_contract_pers(sc->ah.p, sc->al.p, sc->gh.p, sc->gl.p, n, sc->rows_total, P,
+                           sc->items.p, sc->nitems, nullptr, sc->part.p, sc->err.p, sc->shape,
+                           sc->grid, sc->s, sc->nodes.p) != cudaSuccess)
     return abort_capture(fail(UPCG_ERR_CUDA, "scan: contraction capture failed"));
   for (int i = 0; i < n; ++i) {
     rc = sc->gens[i]->enqueue_scan_back(*sc, i);

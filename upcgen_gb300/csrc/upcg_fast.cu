@@ -306,6 +306,124 @@ __global__ void __launch_bounds__(192, 1) k_contract(const __grid_constant__ CUt
   }
 }
 
+// ------------------------------------------------------------ TF32 product --
+// k_gemm_tf32: D = A B^T on tcgen05 kind::tf32, one product per k step (no
+// hi / lo split: TF32 keeps 10 mantissa bits of each FP32 operand), FP32
+// accumulation in TMEM, FP32 store epilogue.  A [Mpad][K], B [N][K] FP32 with
+// K contiguous; 128-byte rows of 32 elements in SWIZZLE_128B boxes, so the
+// shared-memory layout, the descriptors and the 32-byte step per MMA (K = 8)
+// are those of the bf16 kernels.  One CTA per 128 x 256 tile, 4 stages;
+// warps 0 (TMA), 1 (MMA), 2-5 (epilogue), every wait bounded.
+constexpr int kT32K = 32;                 // elements per 128-byte row
+constexpr int kT32A = BM * 128;           // 16 KB
+constexpr int kT32B = BN * 128;           // 32 KB
+constexpr int kT32Stages = 4;
+constexpr int kT32Smem = kT32Stages * (kT32A + kT32B) + 1024;
+// instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major
+constexpr uint32_t kIdescTf32 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                ((uint32_t)(BM >> 4) << 24);
+
+__global__ void __launch_bounds__(192, 1) k_gemm_tf32(const __grid_constant__ CUtensorMap tA,
+                                                      const __grid_constant__ CUtensorMap tB,
+                                                      int ktiles, int M, int ldo, float* out,
+                                                      unsigned* err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[kT32Stages], empty_bar[kT32Stages], done_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nt = blockIdx.x, mt = blockIdx.y;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kT32Stages; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&done_bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  if (warp == 0 && lane == 0) {
+    int issued = 0;
+    for (int kt = 0; kt < ktiles; ++kt) {
+      const int s = kt % kT32Stages;
+      const uint32_t ph = (kt / kT32Stages) & 1;
+      if (kt >= kT32Stages && !mbar_wait(&empty_bar[s], ph ^ 1, err, 1u)) {
+        abort_flag = 1;
+        break;
+      }
+      if (abort_flag) break;
+      uint8_t* st = smem + s * (kT32A + kT32B);
+      mbar_expect_tx(&full_bar[s], kT32A + kT32B);
+      const int x = kt * kT32K;
+      tma_load_2d(st, &tA, &full_bar[s], x, mt * BM);
+      tma_load_2d(st + kT32A, &tB, &full_bar[s], x, nt * BN);
+      issued = kt + 1;
+    }
+    for (int kt = (issued > kT32Stages ? issued - kT32Stages : 0); kt < issued; ++kt)
+      mbar_wait(&full_bar[kt % kT32Stages], (kt / kT32Stages) & 1, err, 8u);
+  } else if (warp == 1 && lane == 0) {
+    for (int kt = 0; kt < ktiles; ++kt) {
+      const int s = kt % kT32Stages;
+      if (!mbar_wait(&full_bar[s], (kt / kT32Stages) & 1, err, 2u)) {
+        abort_flag = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a = smem_u32(smem + s * (kT32A + kT32B)), b = a + kT32A;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {  // 8 TF32 (32 bytes) along K per MMA
+        const uint64_t da = sw128_desc(a + kk * 32), db = sw128_desc(b + kk * 32);
+        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(kIdescTf32), "r"(acc));
+      }
+      umma_commit(&empty_bar[s]);
+    }
+    umma_commit(&done_bar);
+  } else if (warp >= 2) {
+    const bool ok = mbar_wait(&done_bar, 0, err, 4u);
+    tc_fence_after();
+    const int quad = warp & 3;
+    const int row = mt * BM + quad * 32 + lane;
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      if (ok) tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, v);
+      if (!ok || row >= M) continue;
+      float4* d = reinterpret_cast<float4*>(out + (size_t)row * ldo + nt * BN + c0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) d[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+  }
+}
+
+// FP32 value of a bf16 hi / lo pair (the operands of the TF32 products)
+__global__ void k_pair_to_f32(const __nv_bfloat16* __restrict__ hi, const __nv_bfloat16* __restrict__ lo,
+                              size_t n, float* __restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = __bfloat162float(hi[i]) + __bfloat162float(lo[i]);
+}
+
 // --------------------------------------------------------------- grids ---
 struct FastGrid {
   int P;
@@ -529,7 +647,6 @@ struct FluxTabs {
 // a_i = N(b_i, k) b_i (bh - bl)_i.  Each side is normalised by its largest
 // near-node weight, so cells whose luminosity lies far below FP32's range
 // keep full precision; the scale returns in FP64 in k_fast_finish.
-constexpr int kProjThreads = 256;
 constexpr int kMaxP = 1024;  // radial grid points (the projection's shared-memory row)
 constexpr int kNodeStride = 128;  // floats per (row, side) of a node list: header [4], weights [120], pad
 
@@ -626,55 +743,69 @@ __global__ void k_fast_sides(LumiParams p, FastGrid fg, FluxTabs ft, int cell0, 
   out[t] = c;
 }
 
-// Shared memory of the per-row node-weight stage.
-struct ProjSmem {
-  SideC sc[2];
-  float an[2][kNb];  // a_i / max near a (near nodes), 0 beyond
-  float t[2][kNb];   // radial-grid coordinate of near node i
-  float qk[2][256];  // Q(k_side, b_j) on the table's b grid
-  float red[3][2][kProjThreads / 32];
-  float lamax[2];
-};
+// One warp per (row, side): the side's 120 nodes, lane l taking nodes l,
+// l + 32, l + 64, l + 96.  Per node ln a_i in FP32 log space (point flux from
+// the S(ln x) table; form-factor flux from the Q(w, b) table read at the node,
+// 4 x 4 Lagrange weights in ln w and ln b; or the plain path's node fluxes),
+// then the side's largest near-node ln a (warp maximum), the normalised
+// weights an_i = a_i / max near a and the near / far sums (warp sums).  Per
+// side the warp writes either its node list (kNodeStride floats: [0] tg0, [1]
+// tgd, [2] the near count as int bits, [4 + i] an_i of the near nodes) or its
+// dense row on the radial grid (A_side[p0_i + m] += an_i phi_m(s_i); side 0 as
+// a bf16 hi / lo pair, side 1 in FP32), and side_part[row][side] = (ln scale,
+// near sum, far sum).  No block barrier: rows are independent warps.
+constexpr int kWeightWarps = 8;
 
-// The node weights of one row (cell): per side ln a_i of every node in FP32
-// log space (point flux from the S(ln x) table, form-factor flux from the Q
-// row of the photon energy, or the plain path's node fluxes), normalised by
-// the side's largest near-node weight.  On return (after a block barrier)
-// sm.an / sm.t hold the near nodes' weights and grid coordinates, `an`/`near`
-// this thread's node, and far_term[lc] the far part and the two ln scales.
-// Every thread of the block calls it.
-__device__ __forceinline__ void proj_weights(const LumiParams& p, const FluxTabs& ft, int lc,
-                                             int iy, const SideC* __restrict__ sides,
-                                             const double* __restrict__ flux_nodes, ProjSmem& sm,
-                                             float4* __restrict__ far_term, float& an_out,
-                                             bool& near_out) {
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  if (tid < 2) sm.sc[tid] = sides[2 * lc + tid];
-  __syncthreads();
-  if (!p.isPoint && ft.q32 && !flux_nodes) {  // the photon energy's Q row
-    for (int j = tid; j < 2 * ft.nb; j += kProjThreads) {
-      const int side = j / ft.nb, jj = j - side * ft.nb;
-      const SideC& c = sm.sc[side];
-      const float* q = ft.q32 + (size_t)c.iw * ft.nb + jj;
-      sm.qk[side][jj] = c.ww[0] * __ldg(q) + c.ww[1] * __ldg(q + ft.nb) +
-                        c.ww[2] * __ldg(q + 2 * ft.nb) + c.ww[3] * __ldg(q + 3 * ft.nb);
+__global__ void __launch_bounds__(kWeightWarps * 32) k_fast_weights(
+    LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells, int nrows_pad,
+    const SideC* __restrict__ sides, const double* __restrict__ flux_nodes, int dense_mask,
+    __nv_bfloat16* __restrict__ ah, __nv_bfloat16* __restrict__ al, float* __restrict__ a2,
+    float* __restrict__ nodes, float4* __restrict__ side_part) {
+  __shared__ __align__(16) float s_row[kWeightWarps][kMaxP];  // a dense row per warp
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * kWeightWarps + warp;
+  const int lc = gw >> 1, side = gw & 1;
+  if (lc >= nrows_pad) return;  // whole warps leave; nothing below waits for others
+  const bool dense = (dense_mask >> side) & 1;
+  const int P = fg.P;
+  if (lc >= ncells) {  // padding rows of the last 128-row tile
+    if (lane == 0) side_part[2 * lc + side] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!dense) {
+      if (lane == 0)
+        *reinterpret_cast<float4*>(nodes + ((size_t)lc * 2 + side) * kNodeStride) =
+            make_float4(0.f, 1.f, 0.f, 0.f);
+    } else {
+      const size_t row = (size_t)lc * P;
+      for (int q = 4 * lane; q < P; q += 128) {
+        if (side == 0) {
+          *reinterpret_cast<uint2*>(ah + row + q) = make_uint2(0u, 0u);
+          *reinterpret_cast<uint2*>(al + row + q) = make_uint2(0u, 0u);
+        } else {
+          *reinterpret_cast<float4*>(a2 + row + q) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
     }
-    __syncthreads();
+    return;
   }
-  // ln a_i, one node per thread
-  const int side = tid / kNb, i = tid - side * kNb;
-  const bool node = tid < 2 * kNb;
-  float la = -INFINITY;
-  bool near = false;
-  if (node) {
-    const SideC& c = sm.sc[side];
+  const int cell = fast_cell(fg, p.ny, cell0 + lc);
+  const int iy = cell - (cell / p.ny) * p.ny;
+  const SideC c = sides[2 * lc + side];
+  // ln a_i of this lane's nodes
+  float la[4];
+  bool nr[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int i = lane + 32 * j;
+    la[j] = -INFINITY;
+    nr[j] = false;
+    if (i >= kNb) continue;
     const float lnb = fmaf((float)i, c.ld, c.lnb0);
-    near = i < c.n_near;
+    nr[j] = i < c.n_near;
     if (flux_nodes) {  // the plain path's node fluxes (QAGS / K0, K1)
       const bool mir = side == 1 && p.mirror != nullptr && p.mirror[iy] >= 0;
       const double f = mir ? flux_nodes[((size_t)(lc + p.mirror[iy] - iy) * 2) * kNb + i]
                            : flux_nodes[((size_t)lc * 2 + side) * kNb + i];
-      if (f > 0.) la = (float)log(f) + 2.f * lnb + c.lnw0;
+      if (f > 0.) la[j] = (float)log(f) + 2.f * lnb + c.lnw0;
     } else if (i >= c.n_form) {  // point flux: ln N = ln(factor k/g^2) + S - 2x
       const float tk = fmaf((float)i, c.tkd, c.tk0);
       if (tk <= (float)(kKTabN - 1)) {  // x <= 300; beyond, the flux is taken as zero
@@ -682,129 +813,93 @@ __device__ __forceinline__ void proj_weights(const LumiParams& p, const FluxTabs
         const int i0 = lag4f(tk, kKTabN, w);
         const float S = w[0] * __ldg(ft.s32 + i0) + w[1] * __ldg(ft.s32 + i0 + 1) +
                         w[2] * __ldg(ft.s32 + i0 + 2) + w[3] * __ldg(ft.s32 + i0 + 3);
+        // x up to 300 enters as e^{-2x}: its relative error is multiplied by
+        // 2x, so x takes the accurate expf (not the approximate __expf)
         const float x = expf(lnb + c.lnxk);
-        la = c.lnc_pt + S - 2.f * x + 2.f * lnb + c.lnw0;
+        la[j] = c.lnc_pt + S - 2.f * x + 2.f * lnb + c.lnw0;
       }
-    } else {  // form-factor flux: N = factor Q^2 / (A^2 k)
-      float w[4];
-      const int j0 = lag4f(fmaf((float)i, c.tbd, c.tb0), ft.nb, w);
-      const float Q = w[0] * sm.qk[side][j0] + w[1] * sm.qk[side][j0 + 1] +
-                      w[2] * sm.qk[side][j0 + 2] + w[3] * sm.qk[side][j0 + 3];
-      if (Q != 0.f) la = c.lnc_ff + 2.f * logf(fabsf(Q)) + 2.f * lnb + c.lnw0;
-    }
-    if (near) sm.t[side][i] = fmaf((float)i, c.tgd, c.tg0);
-  }
-  // each side's largest near-node ln a
-  {
-    float m0 = (node && near && side == 0) ? la : -INFINITY;
-    float m1 = (node && near && side == 1) ? la : -INFINITY;
+    } else {  // form-factor flux: N = factor Q^2 / (A^2 k), Q from the table at (k, b_i)
+      float wb[4];
+      const int j0 = lag4f(fmaf((float)i, c.tbd, c.tb0), ft.nb, wb);
+      const float* q = ft.q32 + (size_t)c.iw * ft.nb + j0;
+      float Q = 0.f;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
-      m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+      for (int r = 0; r < 4; ++r) {
+        const float* qr = q + (size_t)r * ft.nb;
+        Q = fmaf(c.ww[r],
+                 wb[0] * __ldg(qr) + wb[1] * __ldg(qr + 1) + wb[2] * __ldg(qr + 2) +
+                     wb[3] * __ldg(qr + 3),
+                 Q);
+      }
+      if (Q != 0.f) la[j] = c.lnc_ff + 2.f * __logf(fabsf(Q)) + 2.f * lnb + c.lnw0;
     }
-    if (lane == 0) {
-      sm.red[0][0][wid] = m0;
-      sm.red[0][1][wid] = m1;
-    }
-    __syncthreads();
-    if (tid < 2) {
-      float m = -INFINITY;
-      for (int w = 0; w < kProjThreads / 32; ++w) m = fmaxf(m, sm.red[0][tid][w]);
-      sm.lamax[tid] = m == -INFINITY ? 0.f : m;  // a side without flux: all weights 0
-    }
-    __syncthreads();
   }
-  // normalised weights; near and far sums per side (fixed order)
-  float an = 0.f;
-  if (node) {
-    an = la == -INFINITY ? 0.f : expf(la - sm.lamax[side]);
-    sm.an[side][i] = near ? an : 0.f;
-  }
-  {
-    float v[4] = {0.f, 0.f, 0.f, 0.f};  // near0, near1, far0, far1
-    if (node) v[(near ? 0 : 2) + side] = an;
+  // the side's largest near-node ln a
+  float m = -INFINITY;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+  for (int j = 0; j < 4; ++j)
+    if (nr[j]) m = fmaxf(m, la[j]);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
-    if (lane == 0) {
-      sm.red[1][0][wid] = v[0];
-      sm.red[1][1][wid] = v[1];
-      sm.red[2][0][wid] = v[2];
-      sm.red[2][1][wid] = v[3];
-    }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (m == -INFINITY) m = 0.f;  // a side without flux: all weights 0
+  float an[4], sn = 0.f, sf = 0.f;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    an[j] = la[j] == -INFINITY ? 0.f : __expf(la[j] - m);
+    if (nr[j]) sn += an[j];
+    else sf += an[j];
   }
-  __syncthreads();
-  if (tid == 0) {
-    float S[4] = {0.f, 0.f, 0.f, 0.f};  // near0, near1, far0, far1
-    for (int w = 0; w < kProjThreads / 32; ++w) {
-      S[0] += sm.red[1][0][w];
-      S[1] += sm.red[1][1][w];
-      S[2] += sm.red[2][0][w];
-      S[3] += sm.red[2][1][w];
-    }
-    // G = c wherever one node is far: (S1far S2 + S1near S2far), normalised;
-    // the two ln scales; k_fast_finish combines them in FP64
-    far_term[lc] = make_float4(S[2] * (S[1] + S[3]) + S[0] * S[3], sm.lamax[0], sm.lamax[1], 0.f);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sn += __shfl_xor_sync(0xffffffffu, sn, o);
+    sf += __shfl_xor_sync(0xffffffffu, sf, o);
   }
-  an_out = an;
-  near_out = near;
-}
-
-// Staged projection: one CTA per row writes the dense contraction operands
-// A1 (bf16 hi / lo) and A2 (FP32) on the radial grid, 8 KB per row, for
-// k_contract_pers to read back.
-__global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
-    LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
-    const SideC* __restrict__ sides, const double* __restrict__ flux_nodes,
-    __nv_bfloat16* __restrict__ ah, __nv_bfloat16* __restrict__ al, float* __restrict__ a2,
-    float4* __restrict__ far_term) {
-  __shared__ ProjSmem sm;
-  __shared__ __align__(16) float s_row[2][kMaxP];  // A_side on the radial grid
-  const int lc = blockIdx.x;
-  const int tid = threadIdx.x;
-  const size_t row = (size_t)lc * fg.P;
-  if (lc >= ncells) {  // padding rows of the last 128-cell tile
-    for (int q = tid; q < fg.P; q += kProjThreads) {
-      ah[row + q] = __float2bfloat16(0.f);
-      al[row + q] = __float2bfloat16(0.f);
-      a2[row + q] = 0.f;
+  if (lane == 0) side_part[2 * lc + side] = make_float4(m, sn, sf, 0.f);
+  if (!dense) {
+    float* out = nodes + ((size_t)lc * 2 + side) * kNodeStride;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = lane + 32 * j;
+      if (i < kNb) out[4 + i] = nr[j] ? an[j] : 0.f;
     }
+    if (lane == 0)
+      *reinterpret_cast<float4*>(out) = make_float4(c.tg0, c.tgd, __int_as_float(c.n_near), 0.f);
     return;
   }
-  const int cell = fast_cell(fg, p.ny, cell0 + lc);
-  const int iy = cell - (cell / p.ny) * p.ny;
-  for (int q = 4 * tid; q < 2 * kMaxP; q += 4 * kProjThreads)
-    *reinterpret_cast<float4*>(&s_row[0][0] + q) = make_float4(0.f, 0.f, 0.f, 0.f);
-  float an;
-  bool near;
-  proj_weights(p, ft, lc, iy, sides, flux_nodes, sm, far_term, an, near);
-  const int side = tid / kNb, i = tid - side * kNb;
-  const bool node = tid < 2 * kNb;
-  (void)an;
-  // scatter onto the radial grid: A_side[p0_i + m] += an_i phi_m(s_i).  Nodes
-  // i = r (mod np) go in pass r, np = ceil(4.5 / spacing): within a pass the
-  // 4-point stencils are disjoint, so no atomics and a fixed summation order.
-  const int np = (int)ceilf(4.5f * fmaxf(sm.sc[0].inv_tgd, sm.sc[1].inv_tgd));
-  for (int pass = 0; pass < np; ++pass) {
-    if (node && near && i % np == pass) {
-      const float t = sm.t[side][i];
-      const int p0 = (int)floorf(t) - 1;  // in [0, P-4]: the host checks the grid's span
-      const float s = t - (float)p0;
-      const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
-      const float a = sm.an[side][i];
-      float* r = &s_row[side][p0];
-      r[0] = fmaf(a, -s1 * s2 * s3 * (1.f / 6.f), r[0]);
-      r[1] = fmaf(a, s * s2 * s3 * 0.5f, r[1]);
-      r[2] = fmaf(a, -s * s1 * s3 * 0.5f, r[2]);
-      r[3] = fmaf(a, s * s1 * s2 * (1.f / 6.f), r[3]);
+  // dense row: A_side[p0_i + m] += an_i phi_m(s_i).  Nodes i = r (mod np) go
+  // in pass r, np = ceil(4.5 / spacing): within a pass the 4-point stencils
+  // are disjoint, so no atomics and a fixed summation order.
+  float* row = s_row[warp];
+  for (int q = 4 * lane; q < P; q += 128)
+    *reinterpret_cast<float4*>(row + q) = make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncwarp();
+  const int np = (int)ceilf(4.5f * c.inv_tgd);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int i = lane + 32 * j;
+    for (int pass = 0; pass < np; ++pass) {
+      if (i < kNb && nr[j] && i % np == pass) {
+        const float t = fmaf((float)i, c.tgd, c.tg0);
+        const int p0 = (int)floorf(t) - 1;  // in [0, P-4]: the host checks the grid's span
+        const float s = t - (float)p0;
+        const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
+        const float a = an[j];
+        float* r = row + p0;
+        r[0] = fmaf(a, -s1 * s2 * s3 * (1.f / 6.f), r[0]);
+        r[1] = fmaf(a, s * s2 * s3 * 0.5f, r[1]);
+        r[2] = fmaf(a, -s * s1 * s3 * 0.5f, r[2]);
+        r[3] = fmaf(a, s * s1 * s2 * (1.f / 6.f), r[3]);
+      }
+      __syncwarp();
     }
-    __syncthreads();
   }
-  // 4 grid points per thread: bf16 hi / lo of side 0, FP32 of side 1
-  for (int q = 4 * tid; q < fg.P; q += 4 * kProjThreads) {
-    const float4 x = *reinterpret_cast<const float4*>(&s_row[0][q]);
+  const size_t base = (size_t)lc * P;
+  for (int q = 4 * lane; q < P; q += 128) {
+    const float4 x = *reinterpret_cast<const float4*>(row + q);
+    if (side == 1) {
+      *reinterpret_cast<float4*>(a2 + base + q) = x;
+      continue;
+    }
     const __nv_bfloat162 h01 = __floats2bfloat162_rn(x.x, x.y);
     const __nv_bfloat162 h23 = __floats2bfloat162_rn(x.z, x.w);
     const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
@@ -815,40 +910,8 @@ __global__ void __launch_bounds__(kProjThreads, 8) k_fast_project(
     hv.y = *reinterpret_cast<const uint32_t*>(&h23);
     lv.x = *reinterpret_cast<const uint32_t*>(&l01);
     lv.y = *reinterpret_cast<const uint32_t*>(&l23);
-    *reinterpret_cast<uint2*>(ah + row + q) = hv;
-    *reinterpret_cast<uint2*>(al + row + q) = lv;
-    *reinterpret_cast<float4*>(a2 + row + q) = *reinterpret_cast<const float4*>(&s_row[1][q]);
-  }
-}
-
-// Node lists for the fused contraction: per row and side kNodeStride floats,
-// [0] the radial-grid coordinate of node 0 (tg0), [1] the spacing (tgd), [2]
-// the near-node count (int bits), [3] unused, [4 + i] the normalised weight
-// of near node i.  Padding rows get a count of 0.
-__global__ void __launch_bounds__(kProjThreads, 8) k_fast_nodes(
-    LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells,
-    const SideC* __restrict__ sides, const double* __restrict__ flux_nodes,
-    float* __restrict__ nodes, float4* __restrict__ far_term) {
-  __shared__ ProjSmem sm;
-  const int lc = blockIdx.x;
-  const int tid = threadIdx.x;
-  float* out = nodes + (size_t)lc * 2 * kNodeStride;
-  if (lc >= ncells) {
-    if (tid < 2)
-      *reinterpret_cast<float4*>(out + tid * kNodeStride) = make_float4(0.f, 1.f, 0.f, 0.f);
-    return;
-  }
-  const int cell = fast_cell(fg, p.ny, cell0 + lc);
-  const int iy = cell - (cell / p.ny) * p.ny;
-  float an;
-  bool near;
-  proj_weights(p, ft, lc, iy, sides, flux_nodes, sm, far_term, an, near);
-  const int side = tid / kNb, i = tid - side * kNb;
-  if (tid < 2 * kNb) out[side * kNodeStride + 4 + i] = near ? an : 0.f;
-  if (tid < 2) {
-    const SideC& c = sm.sc[tid];
-    *reinterpret_cast<float4*>(out + tid * kNodeStride) =
-        make_float4(c.tg0, c.tgd, __int_as_float(c.n_near), 0.f);
+    *reinterpret_cast<uint2*>(ah + base + q) = hv;
+    *reinterpret_cast<uint2*>(al + base + q) = lv;
   }
 }
 
@@ -863,9 +926,12 @@ __global__ void k_far_consts(SplineU brk, int has_brk, LumiParams p, double* __r
   out[1] = c;
 }
 
+// L = 2 pi^2 M dm dy e^{ln scale0 + ln scale1} (c (S0far S1 + S0near S1far) +
+// sum over the N tiles of the contraction's partial row-dots), per row; the
+// side sums and scales come from k_fast_weights (side_part[row][side]).
 __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, double c_far,
                               const double* __restrict__ c_far_d,
-                              const float* __restrict__ partial, const float4* __restrict__ far_term,
+                              const float* __restrict__ partial, const float4* __restrict__ side_part,
                               double* __restrict__ lumi, FastGrid fg, const int* __restrict__ rep_mir) {
   const int lc = blockIdx.x * blockDim.x + threadIdx.x;
   if (lc >= ncells) return;
@@ -874,9 +940,10 @@ __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, d
   const double M = p.mmin + p.dm * im;
   double t2 = 0.;
   for (int t = 0; t < ntiles; ++t) t2 += (double)partial[(size_t)lc * ntiles + t];
-  const float4 f = far_term[lc];
+  const float4 s0 = side_part[2 * lc], s1 = side_part[2 * lc + 1];  // (ln scale, near, far)
+  const float far = s0.z * (s1.y + s1.z) + s0.y * s1.z;
   const double cf = c_far_d ? c_far_d[1] : c_far;
-  const double s = exp((double)f.y + (double)f.z) * (cf * (double)f.x + t2);
+  const double s = exp((double)s0.x + (double)s1.x) * (cf * (double)far + t2);
   const double v = 2 * kPi * kPi * M * s * p.dm * p.dy;
   lumi[cell] = v;
   if (fg.rep_y) {  // the mirror rapidity's cell
@@ -972,6 +1039,22 @@ cudaError_t make_map3(CUtensorMap* m, const void* base, uint64_t planes, uint64_
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// 2-D FP32 tensor map, rows x cols (cols contiguous), box = box_rows x 32
+// (128-byte rows, SWIZZLE_128B as the bf16 maps).
+cudaError_t make_map_f32(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols,
+                         uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * 4};
+  cuuint32_t box[2] = {(cuuint32_t)kT32K, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
                                             int x, int y, int z) {
   asm volatile(
@@ -995,10 +1078,42 @@ struct PersItem {
 struct PersArgs {
   const PersItem* items;
   int nitems, ktiles, P, ntiles;
-  const float* a2;   // [rows of all tiles][P]
-  float* partial;    // [rows][ntiles]
+  const float* a2;     // [rows of all tiles][P], or nullptr:
+  const float* nodes;  // side 1's node lists [rows][2][kNodeStride] (k_fast_weights)
+  float* partial;      // [rows][ntiles]
   unsigned* err;
 };
+
+// The epilogue's row-dot of one 16-column accumulator chunk v (columns lo ..
+// lo + 15 of the radial grid) with side 1's dense row, gathered at its node
+// stencils: sum_i an_i sum_m phi_m(s_i) v[p0_i + m - lo].  `cur` walks the
+// nodes forward across the chunks of a row; scr is the thread's own 16-float
+// scratch for the dynamically indexed reads.
+__device__ __forceinline__ float gather_dot16(const float* v, int lo, float tg0, float tgd,
+                                              int nn, const float* __restrict__ an, int& cur,
+                                              float* scr, float acc) {
+  const int hi = lo + 15;
+  while (cur < nn && (int)floorf(fmaf((float)cur, tgd, tg0)) - 1 + 3 < lo) ++cur;
+  if (cur >= nn || (int)floorf(fmaf((float)cur, tgd, tg0)) - 1 > hi) return acc;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) scr[j] = v[j];
+  for (int i = cur; i < nn; ++i) {
+    const float t = fmaf((float)i, tgd, tg0);
+    const int p0 = (int)floorf(t) - 1;
+    if (p0 > hi) break;
+    const float s = t - (float)p0;
+    const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
+    const float w[4] = {-s1 * s2 * s3 * (1.f / 6.f), s * s2 * s3 * 0.5f, -s * s1 * s3 * 0.5f,
+                        s * s1 * s2 * (1.f / 6.f)};
+    const float a = __ldg(an + i);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int c = p0 + m - lo;
+      if ((unsigned)c < 16u) acc = fmaf(a * w[m], scr[c], acc);
+    }
+  }
+  return acc;
+}
 
 // Persistent form of k_contract: each CTA walks the work list (item
 // blockIdx.x, + gridDim.x, ...).  The k-stage ring and its phases run on
@@ -1020,6 +1135,7 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
   __shared__ __align__(8) uint64_t full_bar[TST], empty_bar[TST], accf[2], acce[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
+  __shared__ float ep_scr[4][32][17];  // gathered row-dot: one accumulator chunk per thread
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1135,7 +1251,24 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
       const int row = quad * 32 + lane;
       const size_t grow = (size_t)w.mtile * BM + row;
       float acc = 0.f;
-      if (ok) {
+      if (ok && !args.a2) {  // side 1 from its node list
+        const float* nd = args.nodes + (grow * 2 + 1) * kNodeStride;
+        float tg0 = 0.f, tgd = 1.f;
+        int nn = 0;
+        if (row < w.rows) {
+          const float4 hd = __ldg(reinterpret_cast<const float4*>(nd));
+          tg0 = hd.x;
+          tgd = hd.y;
+          nn = __float_as_int(hd.z);
+        }
+        int cur = 0;
+        float* scr = &ep_scr[warp - 2][lane][0];
+        for (int c0 = 0; c0 < TBN; c0 += 16) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TBN + c0), v);
+          acc = gather_dot16(v, w.ntile * TBN + c0, tg0, tgd, nn, nd + 4, cur, scr, acc);
+        }
+      } else if (ok) {
         const float* a2 = args.a2 + grow * args.P + w.ntile * TBN;
         for (int c0 = 0; c0 < TBN; c0 += 16) {
           float v[16];
@@ -1358,25 +1491,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
         for (int c0 = 0; c0 < TBN; c0 += 16) {
           float v[16];
           tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TBN + c0), v);
-          const int lo = w.ntile * TBN + c0, hi = lo + 15;
-          while (cur < nn && node_p0(tg0, tgd, cur) + 3 < lo) ++cur;
-          if (cur < nn && node_p0(tg0, tgd, cur) <= hi) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) scr[j] = v[j];
-            for (int i = cur; i < nn; ++i) {
-              const float t = fmaf((float)i, tgd, tg0);
-              const int p0 = (int)floorf(t) - 1;
-              if (p0 > hi) break;
-              float wl[4];
-              lag4_weights(t - (float)p0, wl);
-              const float a = __ldg(nd + 4 + i);
-#pragma unroll
-              for (int m = 0; m < 4; ++m) {
-                const int c = p0 + m - lo;
-                if ((unsigned)c < 16u) acc = fmaf(a * wl[m], scr[c], acc);
-              }
-            }
-          }
+          acc = gather_dot16(v, w.ntile * TBN + c0, tg0, tgd, nn, nd + 4, cur, scr, acc);
         }
       }
       if (row < w.rows) args.partial[grow * args.ntiles + w.ntile] = ok ? acc : 0.f;
@@ -1565,10 +1680,11 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
 cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh, const void* gl,
                                  int nconf, int rows_total, int P, const void* items, int nitems,
                                  const float* a2, float* partial, unsigned* d_err, int shape,
-                                 int grid, cudaStream_t st) {
+                                 int grid, cudaStream_t st, const float* nodes) {
   // shape 0: N tile 256, 2 stages; shape 1: N tile 128, 3 stages
   const int tbn = shape == 0 ? 256 : 128;
-  if (P % tbn != 0 || P % BK != 0 || rows_total % BM != 0 || nitems <= 0 || grid <= 0)
+  if (P % tbn != 0 || P % BK != 0 || rows_total % BM != 0 || nitems <= 0 || grid <= 0 ||
+      (!a2 && !nodes))
     return cudaErrorInvalidValue;
   CUtensorMap tAh, tAl, tBh, tBl;
   cudaError_t e;
@@ -1576,7 +1692,8 @@ cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh,
   if ((e = make_map(&tAl, al, rows_total, P, BM)) != cudaSuccess) return e;
   if ((e = make_map3(&tBh, gh, nconf, P, P, tbn)) != cudaSuccess) return e;
   if ((e = make_map3(&tBl, gl, nconf, P, P, tbn)) != cudaSuccess) return e;
-  PersArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, a2, partial, d_err};
+  PersArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, a2, nodes,
+                partial, d_err};
   if (grid > nitems) grid = nitems;
   if (shape == 0) {
     static std::atomic<uint64_t> attr{0};  // devices with the limit raised
@@ -1675,6 +1792,34 @@ cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, c
   return cudaGetLastError();
 }
 
+cudaError_t launch_gemm_tf32(const float* a, const float* b, int M, int N, int K, float* out,
+                             unsigned* d_err, cudaStream_t st) {
+  // A [M_pad][K], B [N][K] FP32 (K contiguous); D = A B^T into out [M][N]
+  if (M <= 0 || N % BN != 0 || K % kT32K != 0 || !out) return cudaErrorInvalidValue;
+  const int Mpad = (M + BM - 1) / BM * BM;
+  CUtensorMap tA, tB;
+  cudaError_t e;
+  if ((e = make_map_f32(&tA, a, Mpad, K, BM)) != cudaSuccess) return e;
+  if ((e = make_map_f32(&tB, b, N, K, BN)) != cudaSuccess) return e;
+  static std::atomic<uint64_t> attr{0};  // devices with the limit raised
+  {
+    const cudaError_t ea = smem_attr_once(attr, k_gemm_tf32, kT32Smem);
+    if (ea != cudaSuccess) return ea;
+  }
+  dim3 grid(N / BN, Mpad / BM);
+  note_launch();
+  k_gemm_tf32<<<grid, 192, kT32Smem, st>>>(tA, tB, K / kT32K, M, N, out, d_err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_to_f32(const void* hi, const void* lo, size_t n, float* out,
+                               cudaStream_t st) {
+  note_launch();
+  k_pair_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+      static_cast<const __nv_bfloat16*>(hi), static_cast<const __nv_bfloat16*>(lo), n, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, double P20,
                           float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st,
                           const double* P20d) {
@@ -1706,10 +1851,14 @@ cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, doubl
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
                                 const double* flux_nodes, const FastFluxTables* t, void* d_sides,
-                                void* ah, void* al, float* a2, void* far_term, cudaStream_t st,
+                                void* ah, void* al, float* a2, void* side_part, cudaStream_t st,
                                 const int* rep_y, int n_rep_y, int m0, float* nodes) {
   if (rep_y && (flux_nodes || n_rep_y <= 0)) return cudaErrorInvalidValue;
-  if (!nodes && !(ah && al && a2)) return cudaErrorInvalidValue;
+  // side 0: dense A1 (bf16 hi / lo) when ah and al are given, side 1: dense A2
+  // (FP32) when a2 is; a side without a dense row writes its node list
+  const int dense_mask = ((ah && al) ? 1 : 0) | (a2 ? 2 : 0);
+  if (dense_mask != 3 && !nodes) return cudaErrorInvalidValue;
+  if ((ah != nullptr) != (al != nullptr)) return cudaErrorInvalidValue;
   FastGrid fg{P, u0, h, 1.0 / h, 250.};
   fg.rep_y = rep_y;
   fg.n_rep_y = n_rep_y;
@@ -1726,26 +1875,20 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
   fg.lnc_ff = std::log(p.factor / ((double)p.A * p.A));
   fg.c_far = c_far;
   FluxTabs ft{};
-  if (P != kMaxP || P % (4 * kProjThreads) != 0) return cudaErrorInvalidValue;
+  if (P != kMaxP || P % 128 != 0 || ncells_pad % kWeightWarps != 0) return cudaErrorInvalidValue;
   // every near node's 4-point stencil inside the grid: b_min >= r_1, b <= r_near < r_{P-3}
   if (std::log(p.isPoint ? p.R : 0.05 * p.R) < u0 + h || std::log(250.) > u0 + (P - 4) * h)
     return cudaErrorInvalidValue;
   if (t) {
-    if (t->nb > 256) return cudaErrorInvalidValue;  // s_qk holds one Q row
     ft = FluxTabs{t->st32, t->qt32, t->nw, t->nb, t->lw0, 1. / t->hw, t->lb0, 1. / t->hb};
   }
   SideC* sides = static_cast<SideC*>(d_sides);
   note_launch();
   k_fast_sides<<<(2 * ncells + 255) / 256, 256, 0, st>>>(p, fg, ft, cell0, ncells, sides);
   note_launch();
-  if (nodes)  // node lists for k_contract_fused
-    k_fast_nodes<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, sides, flux_nodes,
-                                                      nodes, static_cast<float4*>(far_term));
-  else  // dense operands for k_contract_pers
-    k_fast_project<<<ncells_pad, kProjThreads, 0, st>>>(p, fg, ft, cell0, ncells, sides,
-                                                        flux_nodes, (__nv_bfloat16*)ah,
-                                                        (__nv_bfloat16*)al, a2,
-                                                        static_cast<float4*>(far_term));
+  k_fast_weights<<<2 * ncells_pad / kWeightWarps, kWeightWarps * 32, 0, st>>>(
+      p, fg, ft, cell0, ncells, ncells_pad, sides, flux_nodes, dense_mask, (__nv_bfloat16*)ah,
+      (__nv_bfloat16*)al, a2, nodes, static_cast<float4*>(side_part));
   return cudaGetLastError();
 }
 
@@ -1818,7 +1961,7 @@ cudaError_t launch_far_consts(const LumiParams& p, int has_brk, double* d_out, c
 }
 
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
-                               double c_far, const float* partial, const void* far_term,
+                               double c_far, const float* partial, const void* side_part,
                                double* lumi, cudaStream_t st, const double* c_far_d,
                                const int* rep_y, const int* rep_mir, int n_rep_y, int m0) {
   FastGrid fg{};
@@ -1828,7 +1971,7 @@ cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int n
   if (rep_y && (!rep_mir || n_rep_y <= 0)) return cudaErrorInvalidValue;
   note_launch();
   k_fast_finish<<<(ncells + 255) / 256, 256, 0, st>>>(p, cell0, ncells, ntiles, c_far, c_far_d,
-                                                      partial, static_cast<const float4*>(far_term),
+                                                      partial, static_cast<const float4*>(side_part),
                                                       lumi, fg, rep_mir);
   return cudaGetLastError();
 }

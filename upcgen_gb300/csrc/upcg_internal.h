@@ -182,13 +182,16 @@ cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream,
 // rep_y[r % n_rep_y]) -- one of each pair of mirror rapidities, whose
 // luminosities are equal; launch_fast_finish then also writes the mirror cell
 // rep_mir[r % n_rep_y] (-1: none).  Without it row r is cell r.
-// With nodes set the rows' node lists (fast_node_floats_per_row() floats per
-// row) are written for launch_contract_fused and ah / al / a2 are not used;
-// without it the dense operands of launch_contract_pers are.
+// Per side the rows are written either dense on the radial grid -- side 0 as
+// the A1 bf16 hi / lo pair when ah and al are given, side 1 as the FP32 A2 row
+// when a2 is -- or as node lists (fast_node_floats_per_row() floats per row,
+// both sides) in nodes.  side_part gets (ln scale, near sum, far sum) per row
+// and side (2 float4 per row, for launch_fast_finish).  ncells_pad: a
+// multiple of 128.
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
                                 const double* flux_nodes, const FastFluxTables* t, void* d_sides,
-                                void* ah, void* al, float* a2, void* far_term, cudaStream_t st,
+                                void* ah, void* al, float* a2, void* side_part, cudaStream_t st,
                                 const int* rep_y = nullptr, int n_rep_y = 0, int m0 = 0,
                                 float* nodes = nullptr);
 int fast_node_floats_per_row();
@@ -200,8 +203,7 @@ cudaError_t launch_contract_fused(const void* gh, const void* gl, int nconf, int
                                   float* partial, unsigned* d_err, int shape, int grid,
                                   cudaStream_t st);
 cudaError_t launch_fill_nodes_synthetic(float* nodes, int rows, cudaStream_t st);
-// bytes of the per-(cell, photon) constants (d_sides holds 2 per cell);
-// far_term holds one float4 per cell
+// bytes of the per-(cell, photon) constants (d_sides holds 2 per cell)
 size_t fast_side_bytes();
 // General product on tcgen05, three-term bf16 split with FP32 accumulation:
 // D[M][N] = A B^T for A [ceil128(M)][K], B [N][K] (K contiguous, bf16 hi/lo
@@ -210,21 +212,29 @@ size_t fast_side_bytes();
 cudaError_t launch_gemm_bf16x3(const void* ah, const void* al, const void* bh, const void* bl,
                                int M, int N, int K, float* out_f32, void* out_hi, void* out_lo,
                                unsigned* d_err, cudaStream_t st);
+// The same product on tcgen05 kind::tf32 (one product per k step, FP32
+// operands A [ceil128(M)][K], B [N][K], K % 32 == 0, N % 256 == 0) into out.
+cudaError_t launch_gemm_tf32(const float* a, const float* b, int M, int N, int K, float* out,
+                             unsigned* d_err, cudaStream_t st);
+// out[i] = hi[i] + lo[i] (FP32) of a bf16 hi / lo pair
+cudaError_t launch_pair_to_f32(const void* hi, const void* lo, size_t n, float* out,
+                               cudaStream_t st);
 // Persistent contraction over a work list of {128-row tile of the stacked A,
 // N tile, configuration (plane of the stacked G), valid rows} items (int4
 // each, contract_item_bytes()); rows_total = rows of the stacked A (multiple
 // of 128).  shape 0 = 256-wide N tiles x 2 stages, 1 = 128-wide x 3 stages;
-// partial is [rows][P / tile width].
+// partial is [rows][P / tile width].  The row-dot of the epilogue takes the
+// dense A2 rows, or with a2 == nullptr side 1's node lists in nodes.
 cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh, const void* gl,
                                  int nconf, int rows_total, int P, const void* items, int nitems,
                                  const float* a2, float* partial, unsigned* d_err, int shape,
-                                 int grid, cudaStream_t st);
+                                 int grid, cudaStream_t st, const float* nodes = nullptr);
 int contract_item_bytes();
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
                             const float* a2, int ncells_pad, int ncells, int P, float* partial,
                             unsigned* d_err, cudaStream_t st);
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
-                               double c_far, const float* partial, const void* far_term,
+                               double c_far, const float* partial, const void* side_part,
                                double* lumi, cudaStream_t st, const double* c_far_d = nullptr,
                                const int* rep_y = nullptr, const int* rep_mir = nullptr,
                                int n_rep_y = 0, int m0 = 0);
