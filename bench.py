@@ -392,6 +392,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-scan", action="store_true", help="skip the 64-configuration scan")
     ap.add_argument("--no-files", action="store_true", help="skip the event-file output timing")
+    ap.add_argument("--lumi-method", default="fast",
+                    help="the fast form's operand path for the timed build: fast, gather or fused")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -472,7 +474,7 @@ def main():
             tab_ms = s0.elapsed_time(s1)
         return tab_ms, ev_ms, rej, gen.timings()
 
-    fast = make("fast")
+    fast = make(args.lumi_method)
     g0 = fast.grid()
     cells = g0["nm"] * g0["ny"]
     # the cold first init of a process (one configuration per process, as the
@@ -579,7 +581,7 @@ def main():
         "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f64+bf16x3",
         "data": "synthetic (the workload is a parameter set)",
         "config": {"workload": workload_name(args.workload, params, g0["nm"], g0["ny"], nev),
-                   "lumi_method": "fast form (tcgen05 3xBF16 contraction)",
+                   "lumi_method": f"{args.lumi_method} (tcgen05 3xBF16 contraction)",
                    "l2": "flushed (256 MB write) before each timed phase"},
         "fast_vs_plain": fvp,
         "parity": parity,

@@ -95,11 +95,11 @@ int upcg_set_stream(upcg_generator* g, void* stream);
  * 4 = the fast form with the form-factor flux rows inside the learned
  * surrogate's box from the surrogate (upcg_set_flux_surrogate).  Methods 5
  * and 6 are the fast form with other operand paths, for comparison: 1, 2 and
- * 4 write the contraction's dense A1 rows and side 1's node lists (the
- * epilogue gathers the A2 row-dot at the node stencils); 5 writes both
- * operands dense (A2 read back by the epilogue); 6 writes node lists only and
- * builds A1 in the contraction's shared memory.  All three give the same
- * table up to FP32 summation order.  With USE_POLARIZED_CS the fast form (1,
+ * 4 write both contraction operands dense on the radial grid (A1 read by
+ * TMA, A2 by the epilogue); 5 writes the dense A1 rows and side 1's node
+ * lists (the epilogue gathers the A2 row-dot at the node stencils); 6 writes
+ * node lists only and builds A1 in the contraction's shared memory.  All
+ * three give the same table up to FP32 summation order.  With USE_POLARIZED_CS the fast form (1,
  * 4, 5, 6) builds the scalar and pseudoscalar tables of calcTwoPhotonLumiPol
  * from the same operands. */
 int upcg_set_lumi_method(upcg_generator* g, int method);

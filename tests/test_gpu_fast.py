@@ -189,12 +189,13 @@ def test_grid_form_config3(ug, oracle_mod):
     dict(C1, PROC_ID=15, FLUX_POINT=0, BREAKUP_MODE=2, BINS_M=41, BINS_Y=25),
     dict(C1, PROC_ID=13, BREAKUP_MODE=2, USE_POLARIZED_CS=1, FLUX_POINT=0, BINS_M=21, BINS_Y=25),
 ], ids=["point-201x61", "form-xnxn", "form-polarized"])
-@pytest.mark.parametrize("other", ["staged", "fused"])
+@pytest.mark.parametrize("other", ["gather", "fused"])
 def test_operand_paths_agree(ug, params, other):
     """The fast form's three operand paths on the same bf16 hi / lo operands and
-    survival kernel: the default (dense A1 through TMA, the A2 row-dot gathered
-    at side 1's node stencils), "staged" (both operands dense, A2 read back)
-    and "fused" (A1 built in shared memory from the node lists).  The tables
+    survival kernel: the default (both operands dense on the radial grid, A1
+    through TMA, A2 read by the epilogue), "gather" (the A2 row-dot gathered at
+    side 1's node stencils) and "fused" (A1 built in shared memory from the
+    node lists).  The tables
     differ only by the FP32 summation order of the row-dot (<= 2e-6 relative
     on cells above 1e-12 of the maximum)."""
     out = {}

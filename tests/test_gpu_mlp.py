@@ -188,3 +188,50 @@ def test_training_and_surrogate_luminosity(ug):
     cs.fluxForm(bq[sel], kq[sel])
     t_quad = (time.perf_counter() - t0) * n / max(int(sel.sum()), 1)
     assert t_net * 20 < t_quad, (t_net, t_quad)
+
+
+SURR_CONFIGS = [  # (Z, A, R, a, sqrt(s)): nuclei and energies of the batched scan inside the box
+    (82, 208, 6.68, 0.447, 5020.0), (79, 197, 6.38, 0.535, 200.0), (54, 129, 5.36, 0.59, 5360.0),
+    (82, 208, 6.68, 0.447, 5440.0)]
+
+
+def test_surrogate_against_the_qtable_it_replaces(ug, oracle_mod):
+    """What the network gains over the method without it.  In the fast form
+    the form-factor flux comes from the Q(w, b) table, rebuilt per
+    configuration by an FP64 Gauss-Legendre product (luminosity method 1);
+    method 4 takes the rows inside the network's box from the network
+    instead.  Per configuration (Pb, Au, Xe; sqrt(s) 200 - 5440 GeV) both
+    tables are held against the oracle with the flux integral converged, and
+    the flux-table build time of both is compared.  The bounds state the
+    measured outcome: the quadrature's tables meet 1e-4, the network's miss
+    it (median ~1e-3), at about the same flux-table time."""
+    s = _trained(ug)
+    for z, a_n, r, d, sq in SURR_CONFIGS:
+        p = {"NUCLEUS_Z": z, "NUCLEUS_A": a_n, "WS_R": r, "WS_A": d, "SQRTS": sq,
+             "PROC_ID": 15, "FLUX_POINT": 0, "BREAKUP_MODE": 2, "MMIN": 3.56, "MMAX": 50,
+             "BINS_M": 21, "YMIN": -6, "YMAX": 6, "BINS_Y": 25}
+        o = oracle_mod.Oracle(dict(p, ORACLE_FLUX_EPS=1e-10), threads=os.cpu_count())
+        o.init_tables()
+        ref = o.lumi_table()
+        big = np.abs(ref) >= 1e-5 * np.abs(ref).max()
+        res = {}
+        for meth in ("fast", "surrogate"):
+            g = ug.UpcGenerator(p)
+            if meth == "surrogate":
+                g.setFluxSurrogate(s)
+            g.setLumiMethod(meth)
+            times = []
+            for _ in range(4):
+                g.init()
+                times.append(g.timings()["fluxtab_ms"])
+            res[meth] = (np.abs(g.lumiTable() / ref - 1)[big], float(np.median(times[1:])),
+                         g.surrogateRows() if meth == "surrogate" else 0)
+        qrel, qt, _ = res["fast"]
+        srel, st, rows = res["surrogate"]
+        print(f"surrogate Z={z} sqrt(s)={sq}: rows {rows}, quadrature max {qrel.max():.2e} "
+              f"median {np.median(qrel):.2e} {qt:.4f} ms; network max {srel.max():.2e} "
+              f"median {np.median(srel):.2e} {st:.4f} ms")
+        assert rows > 0, (z, sq)
+        assert qrel.max() < 1e-4, (z, sq, qrel.max())
+        assert np.median(srel) < 5e-3 and srel.max() < 5e-2, (z, sq, np.median(srel), srel.max())
+        assert st < 3 * qt + 0.05, (z, sq, st, qt)

@@ -375,8 +375,11 @@ def test_plain_path_vs_reference_source(ug, name):
     bk = np.array(e["flux_form"])
     ok, r = _close(cs.fluxForm(bk[:, 0], bk[:, 1]), bk[:, 2], 1e-9, 1e-300)
     assert ok, ("fluxForm", r)
+    # the analytic form factor cancels to ~(qR)^2 at small q: the CPU's and the
+    # GPU's sin / sinh differ by ulps, so it is held to 1e-9 of F(0), as the
+    # oracle comparison of the full Q^2 range
     q = np.array(e["form_factor"])
-    ok, r = _close(cs.calcFormFac(q[:, 0]), q[:, 1], 1e-12)
+    ok, r = _close(cs.calcFormFac(q[:, 0]), q[:, 1], 1e-12, 1e-9 * abs(q[0, 1]))
     assert ok, ("calcFormFac", r)
     gs = np.array(e["gaa_spline"])
     ok, r = _close(cs.spline("gaa", gs[:, 0]), gs[:, 1], 1e-12, 1e-15)

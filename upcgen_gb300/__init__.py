@@ -465,7 +465,7 @@ class UpcGenerator:
 
     def setLumiMethod(self, method):
         _check(self._L.upcg_set_lumi_method(self._h, {"plain": 0, "fast": 1, "hybrid": 2, "grid": 3, "surrogate": 4,
-                                                                 "staged": 5, "fused": 6,
+                                                                 "gather": 5, "fused": 6,
                                                                  "grid-tf32": 7}.get(method, method)))
 
     # -- sharding over m-rows (upcgen_gb300.shard)

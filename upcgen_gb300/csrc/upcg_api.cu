@@ -1198,13 +1198,14 @@ int upcg_generator::build_lumi() {
   p.mirror = mirror.p;
   // 1: fast form (flux tables + tensor-core contraction); 2: the same
   // contraction on the plain path's exact node fluxes (QAGS / K0,K1).  The
-  // contraction's operands: methods 1, 2, 4 write the dense A1 rows and side
-  // 1's node lists (the epilogue gathers the A2 row-dot at the node
-  // stencils); 5 writes both dense rows (A2 read back by the epilogue); 6
-  // writes node lists only and builds A1 in shared memory (k_contract_fused)
+  // contraction's operands: methods 1, 2, 4 write both rows dense on the
+  // radial grid (A1 bf16 hi / lo through TMA, A2 FP32 read by the epilogue:
+  // the fastest on GB300); 5 writes the dense A1 rows and side 1's node lists
+  // (the epilogue gathers the A2 row-dot at the node stencils); 6 writes node
+  // lists only and builds A1 in shared memory (k_contract_fused)
   const bool fast = lumiMethod == 2 || fast_tables();
   const bool node_flux = lumiMethod == 2 || !fast;
-  const bool staged = lumiMethod == 5, fused = lumiMethod == 6;
+  const bool fused = lumiMethod == 6, staged = lumiMethod != 5 && !fused;  // staged: dense A2
   // cells per chunk: the node-flux paths hold 1.9 KB of node fluxes per cell,
   // the fast form 8 KB of contraction operands; its chunks are larger, so
   // that a table needs fewer persistent contractions (2 GB at 2^18 cells)
@@ -1759,7 +1760,7 @@ int upcg_generator::gen_events_device(int64_t n, EventRecord* out, int32_t* mbin
 struct upcg_scan {
   std::vector<upcg_generator*> gens;
   DBuf<uint16_t> ah, al, gh, gl;  // stacked A1 rows (bf16 hi / lo), survival kernels
-  DBuf<float> nodes, part;        // side 1's node lists of every configuration's rows
+  DBuf<float> a2, part;           // stacked A2 rows (FP32), partial row-dots
   DBuf<double> far, fc;
   DBuf<int4> items;
   DBuf<unsigned> err;
@@ -1797,9 +1798,8 @@ int upcg_generator::enqueue_scan_front(upcg_scan& sc, int ci) {
   const size_t r0 = (size_t)sc.row0[ci];
   const int nrows = nm * (fast_nrep > 0 ? fast_nrep : ny);
   CK(launch_fast_project(p, fu0, fh, P, 0, nrows, sc.rows[ci], flnm2.p, 0.0, nullptr, &ft,
-                         fsides.p, sc.ah.p + r0 * P, sc.al.p + r0 * P, nullptr,
-                         sc.far.p + 4 * r0, s, fast_nrep > 0 ? frep.p : nullptr, fast_nrep, 0,
-                         sc.nodes.p + r0 * fast_node_floats_per_row()));
+                         fsides.p, sc.ah.p + r0 * P, sc.al.p + r0 * P, sc.a2.p + r0 * P,
+                         sc.far.p + 4 * r0, s, fast_nrep > 0 ? frep.p : nullptr, fast_nrep, 0));
   cap = false;
   return UPCG_OK;
 }
@@ -2843,7 +2843,7 @@ int scan_setup(upcg_scan* sc) {
   const size_t plane = (size_t)P * P;
   CK(sc->ah.ensure((size_t)rows_total * P));
   CK(sc->al.ensure((size_t)rows_total * P));
-  CK(sc->nodes.ensure((size_t)rows_total * fast_node_floats_per_row()));
+  CK(sc->a2.ensure((size_t)rows_total * P));
   CK(sc->part.ensure((size_t)rows_total * (P / 128)));
   CK(sc->far.ensure(4 * (size_t)rows_total));
   CK(sc->gh.ensure(n * plane));
@@ -2883,8 +2883,8 @@ int scan_setup(upcg_scan* sc) {
     if (rc) return abort_capture(rc);
   }
   if (launch_contract_pers(sc->ah.p, sc->al.p, sc->gh.p, sc->gl.p, n, sc->rows_total, P,
-                           sc->items.p, sc->nitems, nullptr, sc->part.p, sc->err.p, sc->shape,
-                           sc->grid, sc->s, sc->nodes.p) != cudaSuccess)
+                           sc->items.p, sc->nitems, sc->a2.p, sc->part.p, sc->err.p, sc->shape,
+                           sc->grid, sc->s) != cudaSuccess)
     return abort_capture(fail(UPCG_ERR_CUDA, "scan: contraction capture failed"));
   for (int i = 0; i < n; ++i) {
     rc = sc->gens[i]->enqueue_scan_back(*sc, i);
