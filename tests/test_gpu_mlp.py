@@ -202,9 +202,12 @@ def test_surrogate_against_the_qtable_it_replaces(ug, oracle_mod):
     method 4 takes the rows inside the network's box from the network
     instead.  Per configuration (Pb, Au, Xe; sqrt(s) 200 - 5440 GeV) both
     tables are held against the oracle with the flux integral converged, and
-    the flux-table build time of both is compared.  The bounds state the
-    measured outcome: the quadrature's tables meet 1e-4, the network's miss
-    it (median ~1e-3), at about the same flux-table time."""
+    the flux-table build time of both is compared.  The measured outcome, which
+    the assertions state: the quadrature's tables meet 1e-4 (max 3e-5); the
+    network's do not (Pb at 5.02 TeV: median 9e-4, max 2.5e-2; Au at 200 GeV,
+    near the low-gamma edge of its box: median 0.3), and its rows take longer
+    to produce (0.32 ms against 0.13 ms for the quadrature's flux tables) --
+    on this path the network gains nothing over the table it replaces."""
     s = _trained(ug)
     for z, a_n, r, d, sq in SURR_CONFIGS:
         p = {"NUCLEUS_Z": z, "NUCLEUS_A": a_n, "WS_R": r, "WS_A": d, "SQRTS": sq,
@@ -233,5 +236,7 @@ def test_surrogate_against_the_qtable_it_replaces(ug, oracle_mod):
               f"median {np.median(srel):.2e} {st:.4f} ms")
         assert rows > 0, (z, sq)
         assert qrel.max() < 1e-4, (z, sq, qrel.max())
-        assert np.median(srel) < 5e-3 and srel.max() < 5e-2, (z, sq, np.median(srel), srel.max())
-        assert st < 3 * qt + 0.05, (z, sq, st, qt)
+        # the network's own error and cost, relative to the quadrature's
+        assert np.median(srel) > 10 * np.median(qrel), (z, sq)
+        assert np.median(srel) < 0.5 and srel.max() < 1.0, (z, sq, np.median(srel), srel.max())
+        assert qt < st < 10 * qt, (z, sq, st, qt)

@@ -364,7 +364,7 @@ def test_plain_path_vs_reference_source(ug, name):
     grid's mass and rapidity edges (calcTwoPhotonLumi / Pol, <= 1e-10), the
     fluxes (fluxPoint <= 1e-12, fluxForm's QAGS <= 1e-9), the form factor, the
     G_AA and breakup splines and the breakup probability (<= 1e-12), and
-    calcPhotonFlux (<= 1e-10)."""
+    calcPhotonFlux (<= 1e-10 above 1e-12 of its peak)."""
     e = _ref_cs_fixture()[name]
     g = ug.UpcGenerator(e["params"])
     g.setLumiMethod("plain")
@@ -401,6 +401,10 @@ def test_plain_path_vs_reference_source(ug, name):
         for got, ref in ((s, c[:, 4]), (p, c[:, 5])):
             ok, r = _close(got, ref, 1e-10, 1e-300)
             assert ok, ("calcTwoPhotonLumiPol", r)
+    # the photon flux wherever it is above 1e-12 of its peak (beyond the
+    # gamma hc / b cut-off both sums cancel to roundoff; the reference's own
+    # value there can be negative: its natural G_AA spline rings below zero)
     pf = np.array(e["photon_flux"])
-    ok, r = _close(cs.calcPhotonFlux(pf[:, 0], pf[:, 1]), pf[:, 2], 1e-10, 1e-300)
+    ok, r = _close(cs.calcPhotonFlux(pf[:, 0], pf[:, 1]), pf[:, 2], 1e-10,
+                   1e-12 * np.abs(pf[:, 2]).max())
     assert ok, ("calcPhotonFlux", r)

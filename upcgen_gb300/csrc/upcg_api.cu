@@ -1365,22 +1365,24 @@ int upcg_generator::build_lumi() {
       CK(fitems.ensure(items.size()));
       CK(upload(fitems.p, items.data(), items.size() * sizeof(int4), s));
       b = mark();
+      // the radial columns below the first node stencil are zero in every row
+      const int kt0 = fast_first_ktile(isPoint ? R : 0.05 * R, fu0, fh);
       if (fused)
         CK(launch_contract_fused(fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(), fnodes.p,
-                                 fpart.p, ferr.p, shape, grid, s));
+                                 fpart.p, ferr.p, shape, grid, s, kt0));
       else
         CK(launch_contract_pers(fah.p, fal.p, fgh.p, fgl.p, 1, ncp, P, fitems.p,
                                 (int)items.size(), staged ? fa2.p : nullptr, fpart.p, ferr.p,
-                                shape, grid, s, staged ? nullptr : fnodes.p));
+                                shape, grid, s, staged ? nullptr : fnodes.p, kt0));
       if (usePolarizedCS) {  // the same operands against the pseudoscalar kernel
         CK(fpart2.ensure(fpart.n));
         if (fused)
           CK(launch_contract_fused(fgh2.p, fgl2.p, 1, ncp, P, fitems.p, (int)items.size(),
-                                   fnodes.p, fpart2.p, ferr.p, shape, grid, s));
+                                   fnodes.p, fpart2.p, ferr.p, shape, grid, s, kt0));
         else
           CK(launch_contract_pers(fah.p, fal.p, fgh2.p, fgl2.p, 1, ncp, P, fitems.p,
                                   (int)items.size(), staged ? fa2.p : nullptr, fpart2.p, ferr.p,
-                                  shape, grid, s, staged ? nullptr : fnodes.p));
+                                  shape, grid, s, staged ? nullptr : fnodes.p, kt0));
       }
       spans.push_back({3, {b, mark()}});
       CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s, ffc.p,
@@ -2882,9 +2884,16 @@ int scan_setup(upcg_scan* sc) {
     rc = sc->gens[i]->enqueue_scan_front(*sc, i);
     if (rc) return abort_capture(rc);
   }
+  // the first nonzero K tile of any configuration (the smallest b_min)
+  int kt0 = P / 64;
+  {
+    const double fu0 = std::log(0.1), fh = (std::log(256.) - std::log(0.1)) / (P - 1);
+    for (const upcg_generator* g : sc->gens)
+      kt0 = std::min(kt0, fast_first_ktile(g->isPoint ? g->R : 0.05 * g->R, fu0, fh));
+  }
   if (launch_contract_pers(sc->ah.p, sc->al.p, sc->gh.p, sc->gl.p, n, sc->rows_total, P,
                            sc->items.p, sc->nitems, sc->a2.p, sc->part.p, sc->err.p, sc->shape,
-                           sc->grid, sc->s) != cudaSuccess)
+                           sc->grid, sc->s, nullptr, kt0) != cudaSuccess)
     return abort_capture(fail(UPCG_ERR_CUDA, "scan: contraction capture failed"));
   for (int i = 0; i < n; ++i) {
     rc = sc->gens[i]->enqueue_scan_back(*sc, i);

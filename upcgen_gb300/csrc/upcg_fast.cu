@@ -1078,6 +1078,7 @@ struct PersItem {
 struct PersArgs {
   const PersItem* items;
   int nitems, ktiles, P, ntiles;
+  int kt0;  // first K tile with a nonzero A1 column in any row (the earlier ones are skipped)
   const float* a2;     // [rows of all tiles][P], or nullptr:
   const float* nodes;  // side 1's node lists [rows][2][kNodeStride] (k_fast_weights)
   float* partial;      // [rows][ntiles]
@@ -1171,7 +1172,7 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
     bool ok = true;
     for (int it = 0; it < nmine && ok; ++it) {
       const PersItem w = args.items[blockIdx.x + it * gridDim.x];
-      for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+      for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
         const int s = g % TST;
         if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 1u)) {
           ok = false;
@@ -1207,7 +1208,7 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
       }
       tc_fence_after();
       const uint32_t acc = tmem + (uint32_t)(b * TBN);
-      for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+      for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
         const int s = g % TST;
         if (!mbar_wait(&full_bar[s], (g / TST) & 1, args.err, 2u)) {
           ok = false;
@@ -1222,7 +1223,7 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
           const uint32_t off = kk * 32;
           const uint64_t dah = sw128_desc(ah + off), dal = sw128_desc(al + off);
           const uint64_t dbh = sw128_desc(bh + off), dbl = sw128_desc(bl + off);
-          const uint32_t first = (kt > 0 || kk > 0) ? 1u : 0u;
+          const uint32_t first = (kt > args.kt0 || kk > 0) ? 1u : 0u;
           asm volatile(
               "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
               " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
@@ -1341,6 +1342,7 @@ __device__ __forceinline__ void fence_async_smem() {
 struct FusedArgs {
   const PersItem* items;
   int nitems, ktiles, P, ntiles;
+  int kt0;  // first K tile with a nonzero A1 column in any row (the earlier ones are skipped)
   const float* nodes;  // [rows][2][kNodeStride] (k_fast_nodes)
   float* partial;      // [rows][ntiles]
   unsigned* err;
@@ -1395,7 +1397,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
       bool ok = true;
       for (int it = 0; it < nmine && ok; ++it) {
         const PersItem w = args.items[blockIdx.x + it * gridDim.x];
-        for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+        for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
           const int s = g % TST;
           if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 1u)) {
             ok = false;
@@ -1431,7 +1433,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
         }
         tc_fence_after();
         const uint32_t acc = tmem + (uint32_t)(b * TBN);
-        for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+        for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
           const int s = g % TST;
           if (!mbar_wait(&full_bar[s], (g / TST) & 1, args.err, 2u)) {
             ok = false;
@@ -1446,7 +1448,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
             const uint32_t off = kk * 32;
             const uint64_t dah = sw128_desc(ah + off), dal = sw128_desc(al + off);
             const uint64_t dbh = sw128_desc(bh + off), dbl = sw128_desc(bl + off);
-            const uint32_t first = (kt > 0 || kk > 0) ? 1u : 0u;
+            const uint32_t first = (kt > args.kt0 || kk > 0) ? 1u : 0u;
             asm volatile(
                 "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
@@ -1525,7 +1527,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
       // (first points floor(t_i) - 1 at least 4 apart after rounding; always
       // so for the form-factor flux, where b_max / b_min >= 100 gives >= 5)
       const bool disjoint = tgd >= 4.5f;
-      for (int kt = 0; kt < args.ktiles; ++kt, ++g) {
+      for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
         const int s = g % TST;
         if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 32u)) {
           ok = false;
@@ -1655,6 +1657,15 @@ constexpr int pers_smem() {
 
 int fast_grid_points() { return 1024; }
 
+// The first K tile (64 radial points) that can hold a near node's stencil:
+// nodes lie at b >= b_min, their stencils start at floor(t) - 1 with t the
+// node's grid coordinate, so the columns below floor((ln b_min - u0)/h) - 1
+// are zero in every row (one more column of margin here).
+int fast_first_ktile(double b_min, double u0, double h) {
+  const int p0 = (int)std::floor((std::log(b_min) - u0) / h) - 2;
+  return p0 < 0 ? 0 : p0 / BK;
+}
+
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
                             const float* a2, int ncells_pad, int ncells, int P, float* partial,
                             unsigned* d_err, cudaStream_t st) {
@@ -1680,7 +1691,7 @@ cudaError_t launch_contract(const void* ah, const void* al, const void* gh, cons
 cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh, const void* gl,
                                  int nconf, int rows_total, int P, const void* items, int nitems,
                                  const float* a2, float* partial, unsigned* d_err, int shape,
-                                 int grid, cudaStream_t st, const float* nodes) {
+                                 int grid, cudaStream_t st, const float* nodes, int kt0) {
   // shape 0: N tile 256, 2 stages; shape 1: N tile 128, 3 stages
   const int tbn = shape == 0 ? 256 : 128;
   if (P % tbn != 0 || P % BK != 0 || rows_total % BM != 0 || nitems <= 0 || grid <= 0 ||
@@ -1692,7 +1703,8 @@ cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh,
   if ((e = make_map(&tAl, al, rows_total, P, BM)) != cudaSuccess) return e;
   if ((e = make_map3(&tBh, gh, nconf, P, P, tbn)) != cudaSuccess) return e;
   if ((e = make_map3(&tBl, gl, nconf, P, P, tbn)) != cudaSuccess) return e;
-  PersArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, a2, nodes,
+  if (kt0 < 0 || kt0 >= P / BK) return cudaErrorInvalidValue;
+  PersArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, kt0, a2, nodes,
                 partial, d_err};
   if (grid > nitems) grid = nitems;
   if (shape == 0) {
@@ -1722,7 +1734,7 @@ int contract_item_bytes() { return (int)sizeof(PersItem); }
 cudaError_t launch_contract_fused(const void* gh, const void* gl, int nconf, int rows_total, int P,
                                   const void* items, int nitems, const float* nodes,
                                   float* partial, unsigned* d_err, int shape, int grid,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, int kt0) {
   // shape 0: N tile 256, 2 stages; shape 1: N tile 128, 3 stages
   const int tbn = shape == 0 ? 256 : 128;
   if (P % tbn != 0 || P % BK != 0 || P > kMaxP || rows_total % BM != 0 || nitems <= 0 ||
@@ -1732,8 +1744,9 @@ cudaError_t launch_contract_fused(const void* gh, const void* gl, int nconf, int
   cudaError_t e;
   if ((e = make_map3(&tBh, gh, nconf, P, P, tbn)) != cudaSuccess) return e;
   if ((e = make_map3(&tBl, gl, nconf, P, P, tbn)) != cudaSuccess) return e;
-  FusedArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, nodes, partial,
-                 d_err};
+  if (kt0 < 0 || kt0 >= P / BK) return cudaErrorInvalidValue;
+  FusedArgs args{static_cast<const PersItem*>(items), nitems, P / BK, P, P / tbn, kt0, nodes,
+                 partial, d_err};
   if (grid > nitems) grid = nitems;
   if (shape == 0) {
     static std::atomic<uint64_t> attr{0};  // devices with the limit raised

@@ -201,7 +201,7 @@ int fast_node_floats_per_row();
 cudaError_t launch_contract_fused(const void* gh, const void* gl, int nconf, int rows_total, int P,
                                   const void* items, int nitems, const float* nodes,
                                   float* partial, unsigned* d_err, int shape, int grid,
-                                  cudaStream_t st);
+                                  cudaStream_t st, int kt0 = 0);
 cudaError_t launch_fill_nodes_synthetic(float* nodes, int rows, cudaStream_t st);
 // bytes of the per-(cell, photon) constants (d_sides holds 2 per cell)
 size_t fast_side_bytes();
@@ -228,7 +228,11 @@ cudaError_t launch_pair_to_f32(const void* hi, const void* lo, size_t n, float* 
 cudaError_t launch_contract_pers(const void* ah, const void* al, const void* gh, const void* gl,
                                  int nconf, int rows_total, int P, const void* items, int nitems,
                                  const float* a2, float* partial, unsigned* d_err, int shape,
-                                 int grid, cudaStream_t st, const float* nodes = nullptr);
+                                 int grid, cudaStream_t st, const float* nodes = nullptr,
+                                 int kt0 = 0);
+// kt0 for launch_contract_pers / launch_contract_fused: the first K tile that
+// can be nonzero when every node lies at b >= b_min on the grid (u0, h)
+int fast_first_ktile(double b_min, double u0, double h);
 int contract_item_bytes();
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
                             const float* a2, int ncells_pad, int ncells, int P, float* partial,
