@@ -10,9 +10,12 @@ One step = the complete table build of UpcGenerator::init on the GPU: nuclear
 tables (form factor, G_AA, breakup), the 121,121-cell luminosity, the nuclear
 cross section and the sampling CDFs.  It is timed with CUDA events on the
 library's stream, after a 256 MB L2 flush.  `value` is cells / s of the fast
-form (tensor-core contraction, checked here against the plain FP64 path to
-<= 1e-4); the plain FP64 path is timed in the same run.  The 1e7-event
-sampling is a second timed phase (events_per_s).
+form (tensor-core contraction); `parity` compares its table, every cell,
+with the committed oracle fixture (the converged flux integral and the
+reference's own quadrature), and the plain FP64 path is timed in the same run.
+The 1e7-event sampling is a second timed phase (events_per_s).  Extra keys:
+the CPU restatement's phases (cpu_baseline), the 64-configuration batched
+scan (c5_scan) and the event-file rates (event_files).
 
 --impl reference times the CPU restatement of the reference (oracle/, C++ with
 OpenMP on every host core) on a bounded sample of the same workload.
@@ -250,13 +253,11 @@ def cpu_baseline_sample(workload, lumi=None):
             "sample": ph["sample"], "phases": ph}
 
 
-# DRAM traffic per launch from one ncu capture of the c2 workload (65,536-cell
-# chunk; profiles/k_contract_c2.md, profiles/k_fast_project_c2.md), scaled by
-# cells for the other chunk: bytes per cell
-# DRAM bytes per contraction row (read + write) and per projected row, from
-# the ncu captures in profiles/k_contract_c2.md and profiles/k_fast_project_c2.md
-CONTRACT_DRAM_BYTES_PER_CELL = (521.124608e6 + 4.506880e6) / 63063
-PROJECT_DRAM_BYTES_PER_CELL = (10.690816e6 + 457.163520e6) / 63063
+# DRAM bytes per launch (read + write) per computed row, from one ncu capture
+# of each kernel on the c2 table (63,063 rows, one launch each): the
+# contraction reads the dense operands and G once; k_fast_weights writes them
+CONTRACT_DRAM_BYTES_PER_ROW = (488.194816e6 + 4.231936e6) / 63063
+WEIGHTS_DRAM_BYTES_PER_ROW = (10.727424e6 + 456.903936e6) / 63063
 
 
 def c2_parity(fast, tot_fast, plain=None):
@@ -572,8 +573,7 @@ def main():
     alg_flops = 2.0 * rows_pad * P * P  # A1 (rows x P) . G (P x P), per table
     achieved = alg_flops / (ms_contract * 1e-3) / 1e12
     peak = pk_vals.get("bf16_tflops", 1900.0)
-    traffic = (CONTRACT_DRAM_BYTES_PER_CELL * rows / nlaunch_contract
-               if CONTRACT_DRAM_BYTES_PER_CELL else None)
+    traffic = CONTRACT_DRAM_BYTES_PER_ROW * rows / nlaunch_contract
     ph = runs[-1][3]
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
@@ -602,22 +602,24 @@ def main():
                              f"{nlaunch_contract} launch(es), rows = {rows} computed cells (one of "
                              f"each mirror-rapidity pair; the hi/lo split issues it 3x); "
                              f"peak = {pk_kind} bf16 burst; traffic = DRAM bytes per launch "
-                             f"(profiles/k_contract_c2.md)"},
-        "roofline_projection": {
-            "kernel": "k_fast_sides + k_fast_project", "bound": "hbm",
+                             f"from an ncu capture, scaled by rows"},
+        "roofline_weights": {
+            "kernel": "k_fast_G + k_fast_sides + k_fast_weights (the projection phase)",
+            "bound": "hbm",
             "achieved": 8.0 * P * rows / (ms_project * 1e-3) / 1e9 if ms_project else None,
             "peak": pk_vals.get("hbm_gbs", 6800.0), "unit": "GB/s",
-            "traffic": PROJECT_DRAM_BYTES_PER_CELL * rows / nlaunch_contract,
-            "note": "algorithmic bytes = the 8 KB per computed cell (row) of contraction operands written "
-                    "(A1 bf16 hi + lo, A2 fp32); project_ms also holds the G and flux-table builds; "
-                    "traffic = DRAM bytes per launch (profiles/k_fast_project_c2.md)"},
+            "traffic": WEIGHTS_DRAM_BYTES_PER_ROW * rows / nlaunch_contract,
+            "note": "algorithmic bytes = the 8 KB per computed row of dense contraction operands "
+                    "written (A1 bf16 hi + lo, A2 FP32) over the phase's time, which also holds "
+                    f"the survival kernel G and the side constants; peak = {pk_kind} copy rate; "
+                    "traffic = k_fast_weights' DRAM bytes per launch from an ncu capture"},
         "cold_first_init_ms": cold_init_ms,
         "gpu_launches": n_launch,
         "clocks": clk,
     }
-    if line["roofline_projection"]["achieved"]:
-        line["roofline_projection"]["frac"] = (line["roofline_projection"]["achieved"] /
-                                               line["roofline_projection"]["peak"])
+    if line["roofline_weights"]["achieved"]:
+        line["roofline_weights"]["frac"] = (line["roofline_weights"]["achieved"] /
+                                            line["roofline_weights"]["peak"])
     if rank == 0 and args.workload == "c2" and not args.no_files:
         line["event_files"] = event_file_rates(fast)
     if rank == 0 and args.workload == "c2" and not args.no_scan:
