@@ -240,3 +240,36 @@ def test_grid_form_tf32_arm(ug, oracle_mod):
     assert abs(tot32 / rtot - 1) < 2e-3
     # the TF32 rounding on top of the grid quadrature's difference
     assert np.median(rel32) < 3 * np.median(rel16) + 1e-3
+
+
+def test_fast_flux_table_vs_converged_quadrature(ug, oracle_mod):
+    """The Q(w, b) table of the fast form (256 Gauss-Legendre nodes on q <= 1.5
+    GeV as a double-float product H J on the FP32 pipe, the clamped tail in
+    closed form) against the oracle's fluxForm integrated to convergence, at
+    table nodes with w < 0.05 gamma (where the tail's closed form holds) and
+    |Q| above 1e-3 of its row's largest: N = factor Q^2 / (A^2 k)."""
+    p = dict(C1, PROC_ID=15, FLUX_POINT=0, BREAKUP_MODE=2, BINS_M=21, BINS_Y=13)
+    g = ug.UpcGenerator(p)
+    g.setLumiMethod("fast")
+    g.init()
+    q, (lw0, hw, lb0, hb) = g.fastFluxTable()
+    o = oracle_mod.Oracle(dict(p, ORACLE_FLUX_EPS=1e-10), threads=os.cpu_count())
+    o.init_tables()
+    gam = o.gamma()
+    fac = 82 * 82 / 137.035999074 / np.pi ** 2 / 0.1973269718 ** 2
+    rng = np.random.default_rng(5)
+    rows = [i for i in range(512) if np.exp(lw0 + i * hw) < 0.05 * gam]
+    checked = 0
+    for i in rng.choice(rows, 24, replace=False):
+        k = float(np.exp(lw0 + i * hw))
+        row = q[i]
+        for j in rng.choice(256, 8, replace=False):
+            if abs(row[j]) < 1e-3 * np.abs(row).max():
+                continue
+            b = float(np.exp(lb0 + j * hb))
+            if b > 2 * 6.68:  # fluxForm takes the point flux beyond 2R
+                continue
+            qref = np.sqrt(o.flux_form(b, k) * 208 * 208 * k / fac)
+            assert abs(abs(row[j]) / qref - 1) < 2e-5, (i, j, k, b, row[j], qref)
+            checked += 1
+    assert checked > 100

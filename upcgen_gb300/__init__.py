@@ -490,6 +490,14 @@ class UpcGenerator:
         _check(self._L.upcg_lumi_table_device(self._h, C.byref(a), C.byref(b)))
         return a.value or 0, b.value or 0
 
+    def fastFluxTable(self):
+        """The fast form's form-factor flux amplitude table Q[512][256] on
+        (ln w, ln b) and its grid (ln w0, h_w, ln b0, h_b)."""
+        out = np.zeros((512, 256))
+        grid = np.zeros(4)
+        _check(self._L.upcg_fast_flux_table(self._h, _p(out), out.size, _p(grid)))
+        return out, tuple(grid)
+
     def setFluxSurrogate(self, surrogate):
         self._surrogate = surrogate  # kept alive with the generator
         _check(self._L.upcg_set_flux_surrogate(self._h, surrogate._h if surrogate else None))

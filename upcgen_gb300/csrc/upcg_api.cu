@@ -969,7 +969,7 @@ int upcg_generator::build_lumi_grid() {
 
 // Revision of the table-producing code; part of every cache key, raised
 // whenever a change moves the values of any luminosity method.
-constexpr int kLumiAlgorithmRevision = 1;
+constexpr int kLumiAlgorithmRevision = 2;
 constexpr double kLumiLockTimeoutS = 600.;
 // the wait for another process's lock: kLumiLockTimeoutS, or UPCG_LUMI_LOCK_TIMEOUT seconds
 double lumi_lock_timeout() {
@@ -2365,7 +2365,7 @@ int upcg_qags_stats(const upcg_generator* g, uint64_t* failures, uint64_t* max_i
 
 int upcg_fast_flux_table(upcg_generator* g, double* out, size_t n, double* grid) {
   if (!g || !out || !grid) return fail(UPCG_ERR_ARG, "null argument");
-  if (!g->lumi_ready || (g->lumiMethod != 1 && g->lumiMethod != 4) || g->isPoint || !g->fq.p)
+  if (!g->lumi_ready || !g->fast_tables() || g->isPoint || !g->fq.p)
     return fail(UPCG_ERR_STATE, "no fast-form flux table (fast method, FLUX_POINT 0, after init)");
   const size_t need = (size_t)512 * 256;
   if (n < need) return fail(UPCG_ERR_SIZE, "need %zu doubles", need);

@@ -531,7 +531,8 @@ __global__ void k_ktab_logs(double g, const double2* __restrict__ lk, double* __
 // Form-factor flux amplitude Q(w, b) = int_0^10 q^2 F(q^2 + w^2/g^2)/(q^2 + w^2/g^2)
 // J1(b q / hc) dq (the integrand of src/UpcCrossSection.cpp:181-191, clamp at
 // Q2max - dQ2 included): composite Gauss-Legendre on q in [0, kQNodeMax] as
-// the FP64 product H[w][n] J[n][b], the rest in closed form (k_dgemm_reduce).
+// the product H[w][n] J[n][b] (k_qtab_product, double-float), the rest in
+// closed form (k_dgemm_reduce).
 __global__ void k_qtab_H(LumiParams p, const double* __restrict__ qn, const double* __restrict__ wn,
                          int nq, double lw0, double hw, double* __restrict__ H) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -562,46 +563,75 @@ __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, doub
     tail[j] = spline_eval(ff, q2clamp) * kHc / b * (j0(b * kQNodeMax / kHc) - j0(b * 10. / kHc));
 }
 
-// Split-K FP64 product: Cp[s][M][N] = A[M][Ks] B[Ks][N] over the s-th slice
-// of K (kslice columns; M, N multiples of 64, kslice of 16), 64x64 tiles.
-// The 512 x 256 table is 32 tiles, a fifth of the SMs; the K slices give the
-// rest of the machine work.
-__global__ void __launch_bounds__(256) k_dgemm(const double* __restrict__ A,
-                                               const double* __restrict__ B,
-                                               double* __restrict__ Cp, int M, int N, int K,
-                                               int kslice) {
-  __shared__ double sa[16][64 + 1], sb[16][64 + 1];
+// Split-K product Cp[s][M][N] = A[M][Ks] B[Ks][N] over the s-th slice of K
+// (kslice columns; M, N multiples of 64, kslice of 16), 64 x 64 tiles, in
+// double-float arithmetic: the FP64 operands enter shared memory as float
+// pairs (hi + lo), each product is split exactly (hi = a_h b_h, its rounding
+// error by an FMA, plus the cross terms), and the sum is a compensated
+// (hi, lo) pair.  About 2^-44 relative to the terms' size -- FP64-grade for a
+// Hankel sum whose terms cancel -- on the FP32 pipe, which this part runs at
+// 64x its FP64 rate.  The 512 x 256 table is 32 tiles, a fifth of the SMs;
+// the K slices give the rest of the machine work.
+__device__ __forceinline__ void df_split(double x, float& h, float& l) {
+  h = (float)x;
+  l = (float)(x - (double)h);
+}
+
+__global__ void __launch_bounds__(256) k_qtab_product(const double* __restrict__ A,
+                                                      const double* __restrict__ B,
+                                                      double* __restrict__ Cp, int M, int N, int K,
+                                                      int kslice) {
+  __shared__ float sah[16][64 + 1], sal[16][64 + 1], sbh[16][64 + 1], sbl[16][64 + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
   const int kb = blockIdx.z * kslice, ke = kb + kslice;
   double* C = Cp + (size_t)blockIdx.z * M * N;
-  double acc[4][4] = {};
+  float sh[4][4] = {}, sl[4][4] = {};  // the sums as (hi, lo) pairs
   for (int k0 = kb; k0 < ke; k0 += 16) {
     for (int e = threadIdx.x; e < 16 * 64; e += 256) {
       const int r = e >> 4, c = e & 15;  // A tile: 64 rows x 16 cols
-      sa[c][r] = A[(size_t)(m0 + r) * K + k0 + c];
+      df_split(A[(size_t)(m0 + r) * K + k0 + c], sah[c][r], sal[c][r]);
       const int rb = e >> 6, cb = e & 63;  // B tile: 16 rows x 64 cols
-      sb[rb][cb] = B[(size_t)(k0 + rb) * N + n0 + cb];
+      df_split(B[(size_t)(k0 + rb) * N + n0 + cb], sbh[rb][cb], sbl[rb][cb]);
     }
     __syncthreads();
-#pragma unroll
+#pragma unroll 4
     for (int kk = 0; kk < 16; ++kk) {
-      double a[4], b[4];
+      float ah[4], al[4], bh[4], bl[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = sa[kk][ty * 4 + i];
+      for (int i = 0; i < 4; ++i) {
+        ah[i] = sah[kk][ty * 4 + i];
+        al[i] = sal[kk][ty * 4 + i];
+      }
 #pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = sb[kk][tx * 4 + j];
+      for (int j = 0; j < 4; ++j) {
+        bh[j] = sbh[kk][tx * 4 + j];
+        bl[j] = sbl[kk][tx * 4 + j];
+      }
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) {
+          // __fmul_rn / __fadd_rn / __fsub_rn: no contraction into FMAs, which
+          // would break the error-free transformations
+          const float p = __fmul_rn(ah[i], bh[j]);
+          float e = fmaf(ah[i], bh[j], -p);  // the exact rounding error of p
+          e = fmaf(ah[i], bl[j], fmaf(al[i], bh[j], e));
+          // two-sum of the running hi part and p; the errors gather in lo
+          const float t = __fadd_rn(sh[i][j], p);
+          const float v = __fsub_rn(t, sh[i][j]);
+          const float err = __fadd_rn(__fsub_rn(sh[i][j], __fsub_rn(t, v)), __fsub_rn(p, v));
+          sl[i][j] = __fadd_rn(sl[i][j], __fadd_rn(err, e));
+          sh[i][j] = t;
+        }
     }
     __syncthreads();
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) C[(size_t)(m0 + ty * 4 + i) * N + n0 + tx * 4 + j] = acc[i][j];
+    for (int j = 0; j < 4; ++j)
+      C[(size_t)(m0 + ty * 4 + i) * N + n0 + tx * 4 + j] = (double)sh[i][j] + (double)sl[i][j];
 }
 
 // C = sum over the slices in order (FP64), and its FP32 copy
@@ -756,7 +786,7 @@ __global__ void k_fast_sides(LumiParams p, FastGrid fg, FluxTabs ft, int cell0, 
 // near sum, far sum).  No block barrier: rows are independent warps.
 constexpr int kWeightWarps = 8;
 
-__global__ void __launch_bounds__(kWeightWarps * 32) k_fast_weights(
+__global__ void __launch_bounds__(kWeightWarps * 32, 6) k_fast_weights(
     LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells, int nrows_pad,
     const SideC* __restrict__ sides, const double* __restrict__ flux_nodes, int dense_mask,
     __nv_bfloat16* __restrict__ ah, __nv_bfloat16* __restrict__ al, float* __restrict__ a2,
@@ -1951,7 +1981,7 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
     const int kslice = nq / nslice;
     dim3 gg(t->nb / 64, rows / 64, nslice);
     note_launch();
-    k_dgemm<<<gg, 256, 0, st>>>(d_H, d_J, d_part, rows, t->nb, nq, kslice);
+    k_qtab_product<<<gg, 256, 0, st>>>(d_H, d_J, d_part, rows, t->nb, nq, kslice);
     const size_t mn = (size_t)rows * t->nb;
     const size_t off = (size_t)w_lo * t->nb;
     note_launch();
