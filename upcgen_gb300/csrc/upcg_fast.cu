@@ -786,7 +786,7 @@ __global__ void k_fast_sides(LumiParams p, FastGrid fg, FluxTabs ft, int cell0, 
 // near sum, far sum).  No block barrier: rows are independent warps.
 constexpr int kWeightWarps = 8;
 
-__global__ void __launch_bounds__(kWeightWarps * 32, 6) k_fast_weights(
+__global__ void __launch_bounds__(kWeightWarps * 32) k_fast_weights(
     LumiParams p, FastGrid fg, FluxTabs ft, int cell0, int ncells, int nrows_pad,
     const SideC* __restrict__ sides, const double* __restrict__ flux_nodes, int dense_mask,
     __nv_bfloat16* __restrict__ ah, __nv_bfloat16* __restrict__ al, float* __restrict__ a2,
