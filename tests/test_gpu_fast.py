@@ -233,9 +233,12 @@ def test_grid_form_tf32_arm(ug, oracle_mod):
         g.init()
         lumi = g.lumiTable()
         out[meth] = (np.abs(lumi / ref - 1)[big], g.nucCSYM()[1], g.timings()["contract_ms"])
-    rel32, tot32, _ = out["grid-tf32"]
-    rel16, tot16, _ = out["grid"]
+    rel32, tot32, t32 = out["grid-tf32"]
+    rel16, tot16, t16 = out["grid"]
     _, rtot, _ = o.nuc_cs_ym(ref)
+    print(f"grid form vs oracle: bf16x3 max {rel16.max():.2e} median {np.median(rel16):.2e} "
+          f"sigma {tot16 / rtot - 1:.2e} products {t16:.4f} ms; tf32 max {rel32.max():.2e} "
+          f"median {np.median(rel32):.2e} sigma {tot32 / rtot - 1:.2e} products {t32:.4f} ms")
     assert rel32.max() < 1e-2 and np.median(rel32) < 3e-3, (rel32.max(), np.median(rel32))
     assert abs(tot32 / rtot - 1) < 2e-3
     # the TF32 rounding on top of the grid quadrature's difference

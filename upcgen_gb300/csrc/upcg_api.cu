@@ -470,8 +470,19 @@ struct upcg_generator {
   int complete_deferred(int rc);
   cudaEvent_t ev_ft[2] = {nullptr, nullptr};
   int enqueue_static_samplers(cudaStream_t ss);
+  // the main stream waits for the form factor + flux-table chain (once)
+  cudaError_t join_flux_tables() {
+    if (!ff_join_pending) return cudaSuccess;
+    ff_join_pending = false;
+    return cudaStreamWaitEvent(st(), ev_join[0], 0);
+  }
   int fork_static_samplers();
   bool static_pending = false;   // static samplers enqueued on side[0], not yet joined
+  // the form factor + flux-table chain (side[0], ev_join[0]) not yet joined
+  // into the main stream: the fast form joins it only where the projection
+  // first reads the flux tables, so that the survival kernel and the side
+  // constants run beside that chain
+  bool ff_join_pending = false;
   cudaEvent_t ev_static = nullptr;
   VmParams vm_params() const;
   int build_lumi_cached();
@@ -831,7 +842,9 @@ int upcg_generator::build_tables() {
     CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1]));
   }
   CK(cudaEventRecord(ev_join[1], side[1]));
-  CK(cudaStreamWaitEvent(s, ev_join[0], 0));
+  // only inside upcg_init (defer), whose luminosity step joins the chain
+  ff_join_pending = defer && ftab_early && fast_tables() && !usePolarizedCS;
+  if (!ff_join_pending) CK(cudaStreamWaitEvent(s, ev_join[0], 0));
   CK(cudaStreamWaitEvent(s, ev_join[1], 0));
   if (!cap) {
     cudaEventRecord(t1, s);
@@ -1124,6 +1137,7 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab) {
 
 int upcg_generator::complete_deferred(int rc) {
   defer = false;
+  join_flux_tables();  // no side-stream work left behind on any path
   const cudaError_t se = cudaStreamSynchronize(st());
   auto elapsed = [](cudaEvent_t a, cudaEvent_t b) {
     float t = 0;
@@ -1345,11 +1359,21 @@ int upcg_generator::build_lumi() {
     } else {
       const int ncp = (nc + 127) / 128 * 128;
       b = mark();
+      int part = 0;
+      if (ff_join_pending) {  // the side constants beside the flux-table chain, then join it
+        CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, flnm2.p, c_far,
+                               node_flux ? flux.p : nullptr, &ftab, fsides.p,
+                               fused ? nullptr : fah.p, fused ? nullptr : fal.p,
+                               staged ? fa2.p : nullptr, ffar.p, s, use_map ? frep.p : nullptr,
+                               n_rep, r0, staged ? nullptr : fnodes.p, 1));
+        CK(join_flux_tables());
+        part = 2;
+      }
       CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, flnm2.p, c_far,
                              node_flux ? flux.p : nullptr, &ftab, fsides.p,
                              fused ? nullptr : fah.p, fused ? nullptr : fal.p,
                              staged ? fa2.p : nullptr, ffar.p, s, use_map ? frep.p : nullptr, n_rep,
-                             r0, staged ? nullptr : fnodes.p));
+                             r0, staged ? nullptr : fnodes.p, part));
       spans.push_back({4, {b, mark()}});
       // persistent contraction over this chunk's (row tile, N tile) work list
       int shape = 0, grid = 0;
@@ -1938,6 +1962,8 @@ int upcg_init(upcg_generator* g) {
   rc = g->fork_static_samplers();  // beside the luminosity
   if (rc) return g->complete_deferred(rc);
   rc = g->lumi_cache_usable() ? g->build_lumi_cached() : g->build_lumi();
+  if (const cudaError_t je = g->join_flux_tables(); je != cudaSuccess && !rc)
+    rc = fail(UPCG_ERR_CUDA, "upcg_init: %s", cudaGetErrorString(je));
   if (rc) {
     if (g->static_pending) {  // leave no side-stream work behind a failed init
       cudaStreamWaitEvent(g->st(), g->ev_static, 0);

@@ -1895,8 +1895,9 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
                                 const double* flux_nodes, const FastFluxTables* t, void* d_sides,
                                 void* ah, void* al, float* a2, void* side_part, cudaStream_t st,
-                                const int* rep_y, int n_rep_y, int m0, float* nodes) {
+                                const int* rep_y, int n_rep_y, int m0, float* nodes, int part) {
   if (rep_y && (flux_nodes || n_rep_y <= 0)) return cudaErrorInvalidValue;
+  if (part < 0 || part > 2) return cudaErrorInvalidValue;
   // side 0: dense A1 (bf16 hi / lo) when ah and al are given, side 1: dense A2
   // (FP32) when a2 is; a side without a dense row writes its node list
   const int dense_mask = ((ah && al) ? 1 : 0) | (a2 ? 2 : 0);
@@ -1926,8 +1927,11 @@ cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P,
     ft = FluxTabs{t->st32, t->qt32, t->nw, t->nb, t->lw0, 1. / t->hw, t->lb0, 1. / t->hb};
   }
   SideC* sides = static_cast<SideC*>(d_sides);
-  note_launch();
-  k_fast_sides<<<(2 * ncells + 255) / 256, 256, 0, st>>>(p, fg, ft, cell0, ncells, sides);
+  if (part != 2) {
+    note_launch();
+    k_fast_sides<<<(2 * ncells + 255) / 256, 256, 0, st>>>(p, fg, ft, cell0, ncells, sides);
+  }
+  if (part == 1) return cudaGetLastError();
   note_launch();
   k_fast_weights<<<2 * ncells_pad / kWeightWarps, kWeightWarps * 32, 0, st>>>(
       p, fg, ft, cell0, ncells, ncells_pad, sides, flux_nodes, dense_mask, (__nv_bfloat16*)ah,

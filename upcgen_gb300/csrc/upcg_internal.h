@@ -187,13 +187,15 @@ cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream,
 // when a2 is -- or as node lists (fast_node_floats_per_row() floats per row,
 // both sides) in nodes.  side_part gets (ln scale, near sum, far sum) per row
 // and side (2 float4 per row, for launch_fast_finish).  ncells_pad: a
-// multiple of 128.
+// multiple of 128.  part: 0 both kernels, 1 the side constants only (they
+// read no table values: they may run before the flux tables are ready), 2 the
+// weights only (on side constants computed by a part-1 call).
 cudaError_t launch_fast_project(const LumiParams& p, double u0, double h, int P, int cell0,
                                 int ncells, int ncells_pad, const double* lnm2, double c_far,
                                 const double* flux_nodes, const FastFluxTables* t, void* d_sides,
                                 void* ah, void* al, float* a2, void* side_part, cudaStream_t st,
                                 const int* rep_y = nullptr, int n_rep_y = 0, int m0 = 0,
-                                float* nodes = nullptr);
+                                float* nodes = nullptr, int part = 0);
 int fast_node_floats_per_row();
 // The persistent contraction with the projection folded in (k_contract_fused):
 // the same work list and partial sums as launch_contract_pers, the A1 operand
