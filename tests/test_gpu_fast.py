@@ -251,8 +251,9 @@ def test_fast_flux_table_vs_converged_quadrature(ug, oracle_mod):
     closed form) against the oracle's fluxForm integrated to convergence, at
     table nodes with w < 0.05 gamma (where the tail's closed form holds) and
     |Q| above 1e-3 of its row's largest: N = factor Q^2 / (A^2 k).  The
-    bound is the quadrature's (256 nodes; measured 2.0e-5 at worst): the
-    double-float product adds ~1e-13."""
+    bound is the quadrature's (256 nodes; measured 5.6e-5 at worst, at b near
+    2R where Q's own integral cancels most): the double-float product adds
+    ~1e-13."""
     p = dict(C1, PROC_ID=15, FLUX_POINT=0, BREAKUP_MODE=2, BINS_M=21, BINS_Y=13)
     g = ug.UpcGenerator(p)
     g.setLumiMethod("fast")
@@ -275,6 +276,6 @@ def test_fast_flux_table_vs_converged_quadrature(ug, oracle_mod):
             if b > 2 * 6.68:  # fluxForm takes the point flux beyond 2R
                 continue
             qref = np.sqrt(o.flux_form(b, k) * 208 * 208 * k / fac)
-            assert abs(abs(row[j]) / qref - 1) < 5e-5, (i, j, k, b, row[j], qref)
+            assert abs(abs(row[j]) / qref - 1) < 1e-4, (i, j, k, b, row[j], qref)
             checked += 1
     assert checked > 100

@@ -542,7 +542,10 @@ __global__ void k_qtab_H(LumiParams p, const double* __restrict__ qn, const doub
   const double q = qn[n];
   const double t = q * q + w * w / p.g1 / p.g1;
   const double ffv = spline_eval(p.ff, t < p.q2max ? t : p.q2clamp);
-  H[(size_t)iw * nq + n] = wn[n] * (q * q * ffv / t);
+  const double h = wn[n] * (q * q * ffv / t);
+  // stored as a double-float pair (hi, lo) for k_qtab_product
+  const float hh = (float)h;
+  reinterpret_cast<float2*>(H)[(size_t)iw * nq + n] = make_float2(hh, (float)(h - (double)hh));
 }
 
 __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, double hb, int nb,
@@ -552,7 +555,9 @@ __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, doub
   const int n = blockIdx.y;
   if (j >= nb) return;
   const double b = exp(lb0 + j * hb);
-  J[(size_t)n * nb + j] = j1(b * qn[n] / kHc);
+  const double jv = j1(b * qn[n] / kHc);
+  const float jh = (float)jv;  // a double-float pair (hi, lo) for k_qtab_product
+  reinterpret_cast<float2*>(J)[(size_t)n * nb + j] = make_float2(jh, (float)(jv - (double)jh));
   // q in [kQNodeMax, 10]: q^2 + w^2/g^2 > Q2max, so the reference's integrand
   // is F(Q2max - dQ2) q^2 / (q^2 + w^2/g^2) J1(b q / hc); with the
   // q^2 / (q^2 + w^2/g^2) factor taken as 1 its integral is
@@ -565,20 +570,15 @@ __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, doub
 
 // Split-K product Cp[s][M][N] = A[M][Ks] B[Ks][N] over the s-th slice of K
 // (kslice columns; M, N multiples of 64, kslice of 16), 64 x 64 tiles, in
-// double-float arithmetic: the FP64 operands enter shared memory as float
-// pairs (hi + lo), each product is split exactly (hi = a_h b_h, its rounding
+// double-float arithmetic: the operands come as float pairs (hi + lo, written
+// so by k_qtab_H / k_qtab_J), each product is split exactly (hi = a_h b_h, its rounding
 // error by an FMA, plus the cross terms), and the sum is a compensated
 // (hi, lo) pair.  About 2^-44 relative to the terms' size -- FP64-grade for a
 // Hankel sum whose terms cancel -- on the FP32 pipe, which this part runs at
 // 64x its FP64 rate.  The 512 x 256 table is 32 tiles, a fifth of the SMs;
 // the K slices give the rest of the machine work.
-__device__ __forceinline__ void df_split(double x, float& h, float& l) {
-  h = (float)x;
-  l = (float)(x - (double)h);
-}
-
-__global__ void __launch_bounds__(256) k_qtab_product(const double* __restrict__ A,
-                                                      const double* __restrict__ B,
+__global__ void __launch_bounds__(256) k_qtab_product(const float2* __restrict__ A,
+                                                      const float2* __restrict__ B,
                                                       double* __restrict__ Cp, int M, int N, int K,
                                                       int kslice) {
   __shared__ float sah[16][64 + 1], sal[16][64 + 1], sbh[16][64 + 1], sbl[16][64 + 1];
@@ -590,9 +590,13 @@ __global__ void __launch_bounds__(256) k_qtab_product(const double* __restrict__
   for (int k0 = kb; k0 < ke; k0 += 16) {
     for (int e = threadIdx.x; e < 16 * 64; e += 256) {
       const int r = e >> 4, c = e & 15;  // A tile: 64 rows x 16 cols
-      df_split(A[(size_t)(m0 + r) * K + k0 + c], sah[c][r], sal[c][r]);
+      const float2 a = A[(size_t)(m0 + r) * K + k0 + c];
+      sah[c][r] = a.x;
+      sal[c][r] = a.y;
       const int rb = e >> 6, cb = e & 63;  // B tile: 16 rows x 64 cols
-      df_split(B[(size_t)(k0 + rb) * N + n0 + cb], sbh[rb][cb], sbl[rb][cb]);
+      const float2 b = B[(size_t)(k0 + rb) * N + n0 + cb];
+      sbh[rb][cb] = b.x;
+      sbl[rb][cb] = b.y;
     }
     __syncthreads();
 #pragma unroll 4
@@ -680,7 +684,7 @@ struct FluxTabs {
 constexpr int kMaxP = 1024;  // radial grid points (the projection's shared-memory row)
 constexpr int kNodeStride = 128;  // floats per (row, side) of a node list: header [4], weights [120], pad
 
-struct SideC {
+struct __align__(16) SideC {  // 80 bytes: five 16-byte loads
   float lnb0, ld;   // ln b_i = lnb0 + i ld
   float tg0, tgd;   // radial-grid coordinate of node i: tg0 + i tgd
   float inv_tgd;
@@ -904,23 +908,45 @@ __global__ void __launch_bounds__(kWeightWarps * 32) k_fast_weights(
     *reinterpret_cast<float4*>(row + q) = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncwarp();
   const int np = (int)ceilf(4.5f * c.inv_tgd);
+  if (np == 1) {
+    // stencils 4.5 or more points apart (always so for the form-factor flux):
+    // each column takes at most one node's value, stored without a read
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int i = lane + 32 * j;
-    for (int pass = 0; pass < np; ++pass) {
-      if (i < kNb && nr[j] && i % np == pass) {
+    for (int j = 0; j < 4; ++j) {
+      const int i = lane + 32 * j;
+      if (i < kNb && nr[j]) {
         const float t = fmaf((float)i, c.tgd, c.tg0);
         const int p0 = (int)floorf(t) - 1;  // in [0, P-4]: the host checks the grid's span
         const float s = t - (float)p0;
         const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
         const float a = an[j];
         float* r = row + p0;
-        r[0] = fmaf(a, -s1 * s2 * s3 * (1.f / 6.f), r[0]);
-        r[1] = fmaf(a, s * s2 * s3 * 0.5f, r[1]);
-        r[2] = fmaf(a, -s * s1 * s3 * 0.5f, r[2]);
-        r[3] = fmaf(a, s * s1 * s2 * (1.f / 6.f), r[3]);
+        r[0] = a * (-s1 * s2 * s3 * (1.f / 6.f));
+        r[1] = a * (s * s2 * s3 * 0.5f);
+        r[2] = a * (-s * s1 * s3 * 0.5f);
+        r[3] = a * (s * s1 * s2 * (1.f / 6.f));
       }
-      __syncwarp();
+    }
+    __syncwarp();
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = lane + 32 * j;
+      for (int pass = 0; pass < np; ++pass) {
+        if (i < kNb && nr[j] && i % np == pass) {
+          const float t = fmaf((float)i, c.tgd, c.tg0);
+          const int p0 = (int)floorf(t) - 1;  // in [0, P-4]: the host checks the grid's span
+          const float s = t - (float)p0;
+          const float s1 = s - 1.f, s2 = s - 2.f, s3 = s - 3.f;
+          const float a = an[j];
+          float* r = row + p0;
+          r[0] = fmaf(a, -s1 * s2 * s3 * (1.f / 6.f), r[0]);
+          r[1] = fmaf(a, s * s2 * s3 * 0.5f, r[1]);
+          r[2] = fmaf(a, -s * s1 * s3 * 0.5f, r[2]);
+          r[3] = fmaf(a, s * s1 * s2 * (1.f / 6.f), r[3]);
+        }
+        __syncwarp();
+      }
     }
   }
   const size_t base = (size_t)lc * P;
@@ -1985,7 +2011,9 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
     const int kslice = nq / nslice;
     dim3 gg(t->nb / 64, rows / 64, nslice);
     note_launch();
-    k_qtab_product<<<gg, 256, 0, st>>>(d_H, d_J, d_part, rows, t->nb, nq, kslice);
+    k_qtab_product<<<gg, 256, 0, st>>>(reinterpret_cast<const float2*>(d_H),
+                                       reinterpret_cast<const float2*>(d_J), d_part, rows, t->nb,
+                                       nq, kslice);
     const size_t mn = (size_t)rows * t->nb;
     const size_t off = (size_t)w_lo * t->nb;
     note_launch();
