@@ -247,13 +247,15 @@ def test_grid_form_tf32_arm(ug, oracle_mod):
 
 def test_fast_flux_table_vs_converged_quadrature(ug, oracle_mod):
     """The Q(w, b) table of the fast form (256 Gauss-Legendre nodes on q <= 1.5
-    GeV as a double-float product H J on the FP32 pipe, the clamped tail in
-    closed form) against the oracle's fluxForm integrated to convergence, at
-    table nodes with w < 0.05 gamma (where the tail's closed form holds) and
-    |Q| above 1e-3 of its row's largest: N = factor Q^2 / (A^2 k).  The
-    bound is the quadrature's (256 nodes; measured 5.6e-5 at worst, at b near
-    2R where Q's own integral cancels most): the double-float product adds
-    ~1e-13."""
+    GeV, three panels of them in ln q below 0.094 GeV, as a double-float
+    product H J on the FP32 pipe, the clamped tail in closed form) against the
+    oracle's fluxForm integrated to convergence, at table nodes with w < 0.05
+    gamma (where the tail's closed form holds) and |Q| above 1e-3 of its
+    row's largest: N = factor Q^2 / (A^2 k).  The node layout integrates to
+    7e-7 of the converged integral at worst over these w and b (measured here
+    5e-8 on the sampled nodes; uniform panels from q = 0 missed the
+    integrand's turn-on at q ~ w / gamma by up to 1e-4 near b = 2R); the
+    double-float product adds ~1e-13."""
     p = dict(C1, PROC_ID=15, FLUX_POINT=0, BREAKUP_MODE=2, BINS_M=21, BINS_Y=13)
     g = ug.UpcGenerator(p)
     g.setLumiMethod("fast")
@@ -265,7 +267,7 @@ def test_fast_flux_table_vs_converged_quadrature(ug, oracle_mod):
     fac = 82 * 82 / 137.035999074 / np.pi ** 2 / 0.1973269718 ** 2
     rng = np.random.default_rng(5)
     rows = [i for i in range(512) if np.exp(lw0 + i * hw) < 0.05 * gam]
-    checked = 0
+    worst = []
     for i in rng.choice(rows, 24, replace=False):
         k = float(np.exp(lw0 + i * hw))
         row = q[i]
@@ -276,6 +278,7 @@ def test_fast_flux_table_vs_converged_quadrature(ug, oracle_mod):
             if b > 2 * 6.68:  # fluxForm takes the point flux beyond 2R
                 continue
             qref = np.sqrt(o.flux_form(b, k) * 208 * 208 * k / fac)
-            assert abs(abs(row[j]) / qref - 1) < 1e-4, (i, j, k, b, row[j], qref)
-            checked += 1
-    assert checked > 100
+            worst.append((abs(abs(row[j]) / qref - 1), i, j, k, b))
+    print("Q table vs converged fluxForm: worst", max(worst))
+    assert len(worst) > 100
+    assert max(worst)[0] < 1e-6, max(worst)

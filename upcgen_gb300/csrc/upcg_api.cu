@@ -324,13 +324,15 @@ struct upcg_generator {
   int fast_nrep = 0;          // rapidity bins per m-row the fast form computes (frep), 0: all  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
   std::vector<double> bu_host;
   int bu_nt = 0;
-  // side streams of the table set-up and their fork / join events
-  cudaStream_t side[2] = {nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  // side streams of the table set-up (form factor, breakup, the
+  // luminosity-independent samplers) and their fork / join events; ev_ff:
+  // the form-factor spline is complete (side[0])
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr}, ev_ff = nullptr;
   // host event output: generation done / slot copied out (side[1] copies)
   cudaEvent_t ev_gen = nullptr, ev_out[3] = {nullptr, nullptr, nullptr};
   cudaError_t side_streams() {
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 3; ++i) {
       if (!side[i]) {
         cudaError_t e = cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking);
         if (e != cudaSuccess) return e;
@@ -339,6 +341,10 @@ struct upcg_generator {
         cudaError_t e = cudaEventCreateWithFlags(&ev_join[i], cudaEventDisableTiming);
         if (e != cudaSuccess) return e;
       }
+    }
+    if (!ev_ff) {
+      cudaError_t e = cudaEventCreateWithFlags(&ev_ff, cudaEventDisableTiming);
+      if (e != cudaSuccess) return e;
     }
     if (!ev_fork) return cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
     return cudaSuccess;
@@ -391,11 +397,12 @@ struct upcg_generator {
     set_collision(5020.f, 82, 208);
   }
   ~upcg_generator() {
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 3; ++i) {
       if (side[i]) cudaStreamDestroy(side[i]);
       if (ev_join[i]) cudaEventDestroy(ev_join[i]);
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_ff) cudaEventDestroy(ev_ff);
     if (ev_gen) cudaEventDestroy(ev_gen);
     for (auto e : ev_out)
       if (e) cudaEventDestroy(e);
@@ -469,7 +476,7 @@ struct upcg_generator {
   bool tab_pending = false, lumi_pending = false, lumi_fast = false, xs_pending = false;
   int complete_deferred(int rc);
   cudaEvent_t ev_ft[2] = {nullptr, nullptr};
-  int enqueue_static_samplers(cudaStream_t ss);
+  int enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_ready = nullptr);
   // the main stream waits for the form factor + flux-table chain (once)
   cudaError_t join_flux_tables() {
     if (!ff_join_pending) return cudaSuccess;
@@ -477,7 +484,7 @@ struct upcg_generator {
     return cudaStreamWaitEvent(st(), ev_join[0], 0);
   }
   int fork_static_samplers();
-  bool static_pending = false;   // static samplers enqueued on side[0], not yet joined
+  bool static_pending = false;   // static samplers enqueued on side[2], not yet joined
   // the form factor + flux-table chain (side[0], ev_join[0]) not yet joined
   // into the main stream: the fast form joins it only where the projection
   // first reads the flux tables, so that the survival kernel and the side
@@ -774,6 +781,8 @@ int upcg_generator::build_tables() {
   CK(cudaEventRecord(ev_fork, s));
   CK(cudaStreamWaitEvent(side[0], ev_fork, 0));
   CK(cudaStreamWaitEvent(side[1], ev_fork, 0));
+  // side[2] (the luminosity-independent samplers, fork_static_samplers) starts here too
+  CK(cudaStreamWaitEvent(side[2], ev_fork, 0));
   CK(gaa_coef.ensure(199));
   CK(ta_coef.ensure(199));
   CK(gaa_work.ensure(800));
@@ -797,6 +806,7 @@ int upcg_generator::build_tables() {
     CK(launch_formfac_values(ff_y.p, ff_n, kQ2min, dq, rho0, R, a, side[0]));
     CK(build_spline_uniform(ff_y.p, ff_n, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
   }
+  CK(cudaEventRecord(ev_ff, side[0]));
   ftab_early = false;
   if (!cap && !isVM && (lumiMethod == 2 || fast_tables())) {
     // the fast form's flux tables need only the form factor: they run here,
@@ -982,7 +992,7 @@ int upcg_generator::build_lumi_grid() {
 
 // Revision of the table-producing code; part of every cache key, raised
 // whenever a change moves the values of any luminosity method.
-constexpr int kLumiAlgorithmRevision = 2;
+constexpr int kLumiAlgorithmRevision = 3;
 constexpr double kLumiLockTimeoutS = 600.;
 // the wait for another process's lock: kLumiLockTimeoutS, or UPCG_LUMI_LOCK_TIMEOUT seconds
 double lumi_lock_timeout() {
@@ -1081,15 +1091,30 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab) {
   ftab.hw = (std::log(kmax) - ftab.lw0) / (ftab.nw - 1);
   ftab.lb0 = std::log(0.05 * R * 0.999);
   ftab.hb = (std::log(2. * R * 1.001) - ftab.lb0) / (ftab.nb - 1);
-  const int npan = 16, ngl = 16, nqn = npan * ngl;
+  // Q(w, b) nodes on q in [0, kQNodeMax]: the integrand q^2 F / (q^2 + e^2)
+  // J1(b q / hc), e = w / gamma, turns on at q ~ e, anywhere from 1e-6 to 0.05
+  // GeV over the table's rows, so [1e-7, q1] is taken in ln q (three panels:
+  // smooth there for every e; below 1e-7 the integrand's share is < 1e-14),
+  // [q1, kQNodeMax] in 13 uniform panels (J1 at b = 2R has ~1.3 periods per
+  // panel).  16 Gauss-Legendre nodes per panel; against the integral
+  // converged to 1e-10, 7e-7 at worst over the table's w < 0.05 gamma and b
+  // (uniform panels from q = 0 were 1e-4 off at e ~ 5e-4 GeV, b ~ 2R).
+  const int nlogp = 3, npan = 16, ngl = 16, nqn = npan * ngl;
   if (!isPoint) {
     std::vector<double> gx, gw, qn(nqn), wn(nqn);
     gauss_legendre(ngl, gx, gw);
+    const double q0 = 1e-7, q1 = kQNodeMax / npan;
+    const double u0 = std::log(q0), du = (std::log(q1) - u0) / nlogp;
+    const double hq = (kQNodeMax - q1) / (npan - nlogp);
     for (int pa = 0; pa < npan; ++pa) {
-      const double lo = kQNodeMax * pa / npan, hi = kQNodeMax * (pa + 1) / npan;
+      const bool lg = pa < nlogp;
+      const double lo = lg ? u0 + du * pa : q1 + hq * (pa - nlogp);
+      const double hi = lg ? u0 + du * (pa + 1) : q1 + hq * (pa - nlogp + 1);
       for (int j = 0; j < ngl; ++j) {
-        qn[pa * ngl + j] = 0.5 * (hi - lo) * gx[j] + 0.5 * (hi + lo);
-        wn[pa * ngl + j] = 0.5 * (hi - lo) * gw[j];
+        const double x = 0.5 * (hi - lo) * gx[j] + 0.5 * (hi + lo);
+        const double wx = 0.5 * (hi - lo) * gw[j];
+        qn[pa * ngl + j] = lg ? std::exp(x) : x;
+        wn[pa * ngl + j] = lg ? wx * std::exp(x) : wx;  // dq = q du
       }
     }
     CK(fqn.ensure(nqn));
@@ -1541,7 +1566,7 @@ int upcg_generator::build_vm() {
 // and their CDFs, the photon-pT spectra, their guide tables.  upcg_init
 // enqueues them on a side stream as soon as the nuclear tables exist, so that
 // they run beside the luminosity; build_xsec joins them.
-int upcg_generator::enqueue_static_samplers(cudaStream_t ss) {
+int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_ready) {
   const FoldParams f = fold_params();
   {  // getBinY (include/UpcSampler.h:130-133) of every numerator int(nm (m - mmin))
     const double lo = mmin, hi = mmin + (mmax - mmin) / nm * nm;
@@ -1589,6 +1614,7 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss) {
   const EventParams e = event_params();
   CK(ptcdf.ensure((size_t)e.pt_ne * (e.pt_nbins + 1)));
   CK(ff32.ensure(ff_n));
+  if (ff_ready) CK(cudaStreamWaitEvent(ss, ff_ready, 0));  // the pT spectra read the form factor
   CK(launch_photon_pt_tables(e, lumi_params().ff, ff32.p, ptcdf.p, ss));
   CK(guidez.ensure((size_t)nm * e.gz_n));
   CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
@@ -1599,15 +1625,16 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss) {
   return UPCG_OK;
 }
 
+// On side[2], which build_tables forked at its start: the samplers need
+// nothing of the luminosity and, of the tables, only the form factor
+// (ev_ff), so they run beside the table chains, whose small grids leave most
+// SMs idle, and are done before the weights and the contraction fill the GPU.
 int upcg_generator::fork_static_samplers() {
-  cudaStream_t s = st();
   CK(side_streams());
   if (!ev_static) CK(cudaEventCreateWithFlags(&ev_static, cudaEventDisableTiming));
-  CK(cudaEventRecord(ev_fork, s));
-  CK(cudaStreamWaitEvent(side[0], ev_fork, 0));
-  const int rc = enqueue_static_samplers(side[0]);
+  const int rc = enqueue_static_samplers(side[2], ev_ff);
   if (rc) return rc;
-  CK(cudaEventRecord(ev_static, side[0]));
+  CK(cudaEventRecord(ev_static, side[2]));
   static_pending = true;
   return UPCG_OK;
 }

@@ -340,7 +340,8 @@ cudaError_t launch_cdf_2d(const double* d_w, int64_t n, double* d_cdf, double* d
 cudaError_t launch_cdf_rows(const double* d_w, int rows, int len, double* d_cdf,
                             cudaStream_t st) {
   note_launch();
-  k_cdf_rows<<<(rows + 127) / 128, 128, 0, st>>>(d_w, rows, len, d_cdf);
+  // one thread per row, FP64-bound: 32-thread blocks spread the rows over the SMs
+  k_cdf_rows<<<(rows + 31) / 32, 32, 0, st>>>(d_w, rows, len, d_cdf);
   return cudaGetLastError();
 }
 
