@@ -145,6 +145,30 @@ def test_fast_breakup_table_fp32(ug, mode):
     assert (d[big] / np.abs(vals["plain"][big])).max() < 1e-5
 
 
+@pytest.mark.parametrize("nucleus", [(82, 208, 6.68, 0.447), (79, 197, 6.38, 0.535), (8, 16, 2.608, 0.513)])
+def test_fast_gaa_table_fp32_integrands(ug, nucleus):
+    """The fast form's G_AA spline (T_A and G_AA integrands in FP32, sums in
+    FP64) against the plain path's FP64 one: within 2e-6 absolutely and 2e-5
+    relative to values above 1e-3 (Pb-Pb measured 6.4e-7 and 6.9e-6, the
+    relative figure where G_AA = exp(-sigma T_AA) ~ 1e-3 multiplies T_AA's
+    error by sigma T_AA ~ 7; G_AA is in [0, 1] and the fast form's budget is
+    1e-4)."""
+    z, a_, r, d = nucleus
+    b = np.linspace(0.0, 20.0, 2001)
+    vals = {}
+    for meth in ("plain", "fast"):
+        g = ug.UpcGenerator(dict(C1, NUCLEUS_Z=z, NUCLEUS_A=a_, WS_R=r, WS_A=d, BINS_M=3, BINS_Y=3))
+        g.setLumiMethod(meth)
+        g.init()
+        vals[meth] = g.nucProcessCS.spline("gaa", b)
+    diff = np.abs(vals["fast"] - vals["plain"])
+    big = np.abs(vals["plain"]) > 1e-3
+    rel = diff[big] / np.abs(vals["plain"][big])
+    print("G_AA fp32 integrands:", nucleus, "abs", diff.max(), "rel", rel.max())
+    assert diff.max() < 2e-6
+    assert rel.max() < 2e-5
+
+
 def test_fast_contraction_on_reference_fluxes(ug):
     """Method 2: the plain path's node fluxes (the reference's QAGS) through
     the projection and the tensor-core contraction -- isolates the

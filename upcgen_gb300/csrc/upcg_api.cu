@@ -307,7 +307,7 @@ struct upcg_generator {
   // ---- device state
   cudaStream_t own = nullptr, stream = nullptr;
   DBuf<double> ff_y, ff_c, brk_y, brk_c, lumi, lumi2, cs, ratio, cszm, cszm2, cszm3;
-  DBuf<double> cdf2, cdfz, cdfz2, cdfz3, flux, partial, tot, gws, pts_a, pts_b, pts_c;
+  DBuf<double> cdf2, cdfz, cdfz2, cdfz3, flux, csm, tot, gws, pts_a, pts_b, pts_c;
   DBuf<double4> ff_coef, gaa_coef, ta_coef, brk_coef;
   DBuf<double> gaa_work, bu_tab, cdf_scratch;
   DBuf<double> vm_m, vm_y, vm_b, vm_k, vm_w, vm_f, vm_flux, vm_s, pom_vals, pom_cdf;
@@ -329,12 +329,20 @@ struct upcg_generator {
   // the form-factor spline is complete (side[0])
   cudaStream_t side[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr}, ev_ff = nullptr;
+  cudaEvent_t ev_ktab = nullptr;  // the point-flux table (side[2]) is complete
+  cudaEvent_t ev_qj = nullptr;    // the Q table's Bessel part (side[2]) is complete
   // host event output: generation done / slot copied out (side[1] copies)
   cudaEvent_t ev_gen = nullptr, ev_out[3] = {nullptr, nullptr, nullptr};
   cudaError_t side_streams() {
+    int least = 0, greatest = 0;
+    cudaError_t pe = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (pe != cudaSuccess) return pe;
     for (int i = 0; i < 3; ++i) {
       if (!side[i]) {
-        cudaError_t e = cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking);
+        // the table chains feed the luminosity: their blocks go first; the
+        // luminosity-independent samplers (side[2]) fill the SMs they leave
+        const int prio = i < 2 ? greatest : least;
+        cudaError_t e = cudaStreamCreateWithPriority(&side[i], cudaStreamNonBlocking, prio);
         if (e != cudaSuccess) return e;
       }
       if (!ev_join[i]) {
@@ -342,9 +350,11 @@ struct upcg_generator {
         if (e != cudaSuccess) return e;
       }
     }
-    if (!ev_ff) {
-      cudaError_t e = cudaEventCreateWithFlags(&ev_ff, cudaEventDisableTiming);
-      if (e != cudaSuccess) return e;
+    for (cudaEvent_t* ev : {&ev_ff, &ev_ktab}) {
+      if (!*ev) {
+        cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+      }
     }
     if (!ev_fork) return cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
     return cudaSuccess;
@@ -369,7 +379,7 @@ struct upcg_generator {
   DBuf<float> fpart2;
   bool fk01_ready = false;
   DBuf<float> fs32, fq32;
-  DBuf<float4> fgaa32, fbrk32, ff32;
+  DBuf<float4> fgaa32, fbrk32, ff32, fta32;
   // grid form: G, flux matrix, T = N G (bf16 hi/lo), Lg, row sums and tails
   DBuf<uint16_t> gg_h, gg_l, gn_h, gn_l, gt_h, gt_l;
   DBuf<float> g_lg;
@@ -403,6 +413,8 @@ struct upcg_generator {
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_ff) cudaEventDestroy(ev_ff);
+    if (ev_ktab) cudaEventDestroy(ev_ktab);
+    if (ev_qj) cudaEventDestroy(ev_qj);
     if (ev_gen) cudaEventDestroy(ev_gen);
     for (auto e : ev_out)
       if (e) cudaEventDestroy(e);
@@ -455,8 +467,30 @@ struct upcg_generator {
   int build_tables();
   int build_lumi();
   int build_vm();
-  int setup_flux_tables(cudaStream_t ss, int with_ktab = 1);
+  // js: the stream of the table's Bessel part (and of the node uploads)
+  int setup_flux_tables(cudaStream_t ss, int with_ktab = 1, cudaStream_t js = nullptr);
   bool ftab_early = false;  // build_tables enqueued the flux tables
+  // build_tables wrote the FP32 copies of the G_AA and breakup splines
+  // (fgaa32, fbrk32) beside their FP64 coefficients
+  bool g32_ready = false;
+  bool herr_copy_pending = false;  // the contraction's error word, copied in complete_deferred
+  // per-N-tile K ranges of the delta survival kernel (delta_tile_ranges),
+  // kept for the last (P, N tile, azimuth set)
+  std::vector<std::pair<int, int>> dkr;
+  int dkr_key[3] = {0, 0, -1};
+  const std::vector<std::pair<int, int>>& delta_ranges(int P, double u0, double h, int tbn,
+                                                       const LumiParams& p, bool negated) {
+    if (dkr_key[0] != P || dkr_key[1] != tbn || dkr_key[2] != (negated ? 1 : 0)) {
+      double ck[5];
+      for (int q = 0; q < 5; ++q) ck[q] = negated ? -p.cosk[q] : p.cosk[q];
+      delta_tile_ranges(P, u0, h, ck, 5, tbn, kContractBK, dkr);
+      dkr_key[0] = P;
+      dkr_key[1] = tbn;
+      dkr_key[2] = negated ? 1 : 0;
+    }
+    return dkr;
+  }
+  bool lumi_stats = true;          // the deferred luminosity copied its QAGS statistics
   bool ftab_early_done = false;  // ... and build_lumi used them (deferred timing)
   // upcg_init enqueues tables, luminosity and cross section with one host
   // synchronisation at its end: the phases' timing events, the contraction's
@@ -786,13 +820,23 @@ int upcg_generator::build_tables() {
   CK(gaa_coef.ensure(199));
   CK(ta_coef.ensure(199));
   CK(gaa_work.ensure(800));
+  // the survival kernel of the fast forms reads FP32 copies of the G_AA and
+  // breakup splines: written here by the spline kernels themselves
+  const bool want32 = !cap && !isVM && (lumiMethod == 2 || fast_tables());
+  g32_ready = false;
+  if (want32) CK(fgaa32.ensure(200));
   // in a captured scan, a configuration with the same inputs as an earlier one
   // copies that one's tables instead of rebuilding them
-  if (cap && gaa_donor)
+  if (cap && gaa_donor) {
     CK(cudaMemcpyAsync(gaa_coef.p, gaa_donor->gaa_coef.p, 199 * sizeof(double4),
                        cudaMemcpyDeviceToDevice, s));
-  else
-    CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s));
+  } else {
+    // the fast forms (budget 1e-4) evaluate the T_A / G_AA integrands in FP32
+    const bool gaa_f = !isVM && fast_tables();
+    if (gaa_f) CK(fta32.ensure(199));
+    CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s,
+                  want32 ? fgaa32.p : nullptr, gaa_f ? fta32.p : nullptr));
+  }
   // form factor on 1e6 knots (the reference's), 65,536 for the fast form
   ff_n = fast_tables() ? kNQ2Fast : kNQ2;
   const double dq = (kQ2max - kQ2min) / ff_n;
@@ -813,14 +857,15 @@ int upcg_generator::build_tables() {
     // beside the breakup and G_AA chains
     for (auto& e : ev_ft)
       if (!e) CK(cudaEventCreate(&e));
-    // the point-flux table on the main stream, after the G_AA chain
+    // the point-flux table on side[2], ahead of the samplers there
     CK(fk1.ensure(flux_table_ktab_n()));
     CK(fs32.ensure(flux_table_ktab_n()));
     CK(fk01.ensure(2 * (size_t)flux_table_ktab_n()));
-    CK(launch_ktab(g1, fk1.p, fs32.p, s, fk01.p, fk01_ready ? 1 : 0));
+    CK(launch_ktab(g1, fk1.p, fs32.p, side[2], fk01.p, fk01_ready ? 1 : 0));
+    CK(cudaEventRecord(ev_ktab, side[2]));
     fk01_ready = true;
     CK(cudaEventRecord(ev_ft[0], side[0]));
-    const int frc = setup_flux_tables(side[0], 0);
+    const int frc = setup_flux_tables(side[0], 0, side[2]);
     if (frc) return frc;
     CK(cudaEventRecord(ev_ft[1], side[0]));
     ftab_early = true;
@@ -843,19 +888,23 @@ int upcg_generator::build_tables() {
     CK(cudaMemcpyAsync(brk_coef.p, brk_donor->brk_coef.p, (size_t)(brk_n - 1) * sizeof(double4),
                        cudaMemcpyDeviceToDevice, side[1]));
   } else if (breakupMode > 1) {
+    if (want32) CK(fbrk32.ensure(brk_n));
     // the fast form (methods 1, 4; budget 1e-4) takes the FP32 sums (~1e-6);
     // the reference's sum steps where an energy crosses omax(b), so every
     // knot is summed (an interpolated table smears those steps to 1.5e-5)
     const int brk_fp32 = fast_tables() ? 1 : 0;
     CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
                              1e-6, dbb, brk_y.p, side[1], brk_fp32));
-    CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1]));
+    CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1],
+                            want32 ? fbrk32.p : nullptr));
   }
+  g32_ready = want32;
   CK(cudaEventRecord(ev_join[1], side[1]));
   // only inside upcg_init (defer), whose luminosity step joins the chain
   ff_join_pending = defer && ftab_early && fast_tables() && !usePolarizedCS;
   if (!ff_join_pending) CK(cudaStreamWaitEvent(s, ev_join[0], 0));
   CK(cudaStreamWaitEvent(s, ev_join[1], 0));
+  if (ftab_early) CK(cudaStreamWaitEvent(s, ev_ktab, 0));
   if (!cap) {
     cudaEventRecord(t1, s);
     if (defer) {
@@ -1068,16 +1117,12 @@ int upcg_generator::build_lumi_cached() {
 
 // The fast form's flux tables: K0/K1 on ln x and the Q(w, b) table (or its
 // surrogate rows), on stream ss; the result is in ftab_last.
-int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab) {
+int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab, cudaStream_t js) {
   const LumiParams p = lumi_params();
   FastFluxTables ftab{};
   // flux tables: K0/K1 on ln x; Q(w, b) on 512 x 256 (ln w, ln b) points by
-  // 16 Gauss-Legendre panels of 16 points on q in [0, kQNodeMax] (panels of
-  // 3/32 GeV, one period of J1(b q / hc) at b = 2R for Pb) and the
-  // closed-form rest to q = 10.  With 8 panels the fast form's cells move by
-  // up to 1.3e-4 from the converged quadrature (the kink of the clamped form
-  // factor and the q -> 0 end inside wider panels); with 16, as with 24, they
-  // stay within 1e-4.
+  // a Gauss-Legendre product on q in [0, kQNodeMax] (nodes below) and the
+  // closed-form rest to q = 10.
   const int nk = flux_table_ktab_n();
   CK(fk1.ensure(nk));
   CK(fs32.ensure(nk));
@@ -1123,8 +1168,8 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab) {
     CK(fq32.ensure((size_t)ftab.nw * ftab.nb));
     CK(fH.ensure((size_t)ftab.nw * nqn));
     CK(fJ.ensure((size_t)nqn * ftab.nb));
-    CK(upload(fqn.p, qn.data(), nqn * sizeof(double), ss));
-    CK(upload(fwn.p, wn.data(), nqn * sizeof(double), ss));
+    CK(upload(fqn.p, qn.data(), nqn * sizeof(double), js ? js : ss));
+    CK(upload(fwn.p, wn.data(), nqn * sizeof(double), js ? js : ss));
     ftab.qt = fq.p;
     ftab.qt32 = fq32.p;
   }
@@ -1144,7 +1189,9 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab) {
     }
   }
   if (!isPoint) CK(fpartq.ensure(flux_table_part_doubles(ftab.nw, ftab.nb)));
-  CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, ss, w_sur, with_ktab));
+  if (js && !ev_qj) CK(cudaEventCreateWithFlags(&ev_qj, cudaEventDisableTiming));
+  CK(build_flux_tables(p, &ftab, fqn.p, fwn.p, nqn, fH.p, fJ.p, fpartq.p, ss, w_sur, with_ktab, js,
+                       js ? ev_qj : nullptr));
   if (w_sur > 0) {
     const int n = w_sur * ftab.nb;
     CK(surrogate->tx.ensure((size_t)n * 5));
@@ -1163,6 +1210,10 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab) {
 int upcg_generator::complete_deferred(int rc) {
   defer = false;
   join_flux_tables();  // no side-stream work left behind on any path
+  if (herr_copy_pending) {
+    mcpy(&hstat->herr, ferr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st());
+    herr_copy_pending = false;
+  }
   const cudaError_t se = cudaStreamSynchronize(st());
   auto elapsed = [](cudaEvent_t a, cudaEvent_t b) {
     float t = 0;
@@ -1185,7 +1236,7 @@ int upcg_generator::complete_deferred(int rc) {
     for (auto e : lumi_ev) cudaEventDestroy(e);
     lumi_ev.clear();
     lumi_spans.clear();
-    last_stats = hstat->stats;
+    last_stats = lumi_stats ? hstat->stats : QagsStats{};
     herr = lumi_fast && hstat->herr != 0;
     lumi_pending = false;
   }
@@ -1257,7 +1308,8 @@ int upcg_generator::build_lumi() {
   CK(stats.ensure(1));
   const int ovf_cap = 1 << 20;
   CK(ovf.ensure(ovf_cap));
-  CK(cudaMemsetAsync(stats.p, 0, sizeof(QagsStats), s));
+  // the QAGS statistics: zero unless a path with node fluxes fills them
+  if (node_flux) CK(cudaMemsetAsync(stats.p, 0, sizeof(QagsStats), s));
   if (lumiMethod == 4 && !surrogate)
     return fail(UPCG_ERR_STATE, "luminosity method 4 needs a surrogate (upcg_set_flux_surrogate)");
   const int P = fast_grid_points();
@@ -1276,7 +1328,8 @@ int upcg_generator::build_lumi() {
     CK(fsides.ensure((2 * (size_t)chunk * fast_side_bytes() + 7) / 8));
     CK(fpart.ensure((size_t)chunk_pad * (P / 128)));
     CK(ferr.ensure(1));
-    CK(cudaMemsetAsync(ferr.p, 0, sizeof(unsigned), s));
+    // the single-configuration survival kernel resets the error word itself
+    if (!g32_ready || usePolarizedCS) CK(cudaMemsetAsync(ferr.p, 0, sizeof(unsigned), s));
   }
   // phase timers: 0 whole, 1 nodes, 2 qags, 3 band / contraction, 4 projection + G
   std::vector<cudaEvent_t> ev;
@@ -1298,9 +1351,15 @@ int upcg_generator::build_lumi() {
     CK(ffc.ensure(2));
     CK(fgaa32.ensure(p.gaa.n));
     CK(fbrk32.ensure(breakupMode != 1 ? p.brk.n : 1));
-    if (!usePolarizedCS) {
+    if (!usePolarizedCS && g32_ready) {
+      // the FP32 spline copies come from build_tables; k_fast_G also writes
+      // the far constants and resets the error word
+      CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, nullptr, 0, ffc.p,
+                       ferr.p, 1));
+    } else if (!usePolarizedCS) {
       CK(launch_far_consts(p, breakupMode != 1, ffc.p, s));
-      CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p));
+      CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p, 1, nullptr,
+                       nullptr, 1));
     } else {
       // calcTwoPhotonLumiPol (src/UpcCrossSection.cpp:274-335): b^2 = b1^2 + b2^2
       // - 2 b1 b2 cos(phi), weights w cos^2(phi) (scalar) and w sin^2(phi)
@@ -1316,8 +1375,10 @@ int upcg_generator::build_lumi() {
       CK(fgl2.ensure((size_t)P * P));
       CK(launch_far_consts(ps, breakupMode != 1, ffc.p, s));
       CK(launch_far_consts(pp, breakupMode != 1, ffc2.p, s));
-      CK(launch_fast_G(ps, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p));
-      CK(launch_fast_G(pp, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh2.p, fgl2.p, s, ffc2.p));
+      CK(launch_fast_G(ps, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p, 1, nullptr,
+                       nullptr, 1));
+      CK(launch_fast_G(pp, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh2.p, fgl2.p, s, ffc2.p, 1,
+                       nullptr, nullptr, 1));
     }
     // the flux tables, unless build_tables already enqueued them beside the
     // breakup and G_AA chains
@@ -1407,15 +1468,23 @@ int upcg_generator::build_lumi() {
         if (rc) return rc;
       }
       const int tbn = shape == 0 ? 256 : 128;
+      // each N tile multiplies only the K tiles where G - c can be nonzero
+      // (the polarized kernels' azimuths are the negated ones)
+      const std::vector<std::pair<int, int>>& kr = delta_ranges(P, fu0, fh, tbn, p,
+                                                                usePolarizedCS);
       std::vector<int4> items;
       for (int mt = 0; mt < ncp / 128; ++mt)
         for (int nt = 0; nt < P / tbn; ++nt)
-          items.push_back(make_int4(mt, nt, 0, std::min(128, nc - mt * 128)));
+          items.push_back(make_int4(mt, nt, 0, pack_item(std::min(128, nc - mt * 128),
+                                                         kr[nt].first, kr[nt].second)));
+      // the radial columns below the first node stencil are zero in every row
+      const int kt0 = fast_first_ktile(isPoint ? R : 0.05 * R, fu0, fh);
+      // items of unequal work: every CTA meets every N tile
+      grid = std::min(grid, (int)items.size());
+      rotate_rounds(items, grid);
       CK(fitems.ensure(items.size()));
       CK(upload(fitems.p, items.data(), items.size() * sizeof(int4), s));
       b = mark();
-      // the radial columns below the first node stencil are zero in every row
-      const int kt0 = fast_first_ktile(isPoint ? R : 0.05 * R, fu0, fh);
       if (fused)
         CK(launch_contract_fused(fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(), fnodes.p,
                                  fpart.p, ferr.p, shape, grid, s, kt0));
@@ -1436,11 +1505,11 @@ int upcg_generator::build_lumi() {
       spans.push_back({3, {b, mark()}});
       CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart.p, ffar.p, lumi.p, s, ffc.p,
                             use_map ? frep.p : nullptr, use_map ? frep.p + n_rep : nullptr, n_rep,
-                            r0));
+                            r0, 1));
       if (usePolarizedCS)
         CK(launch_fast_finish(p, c0, nc, P / tbn, c_far, fpart2.p, ffar.p, lumi2.p, s, ffc2.p,
                               use_map ? frep.p : nullptr, use_map ? frep.p + n_rep : nullptr,
-                              n_rep, r0));
+                              n_rep, r0, 1));
     }
   }
   const int w1 = mark();
@@ -1452,8 +1521,9 @@ int upcg_generator::build_lumi() {
     lumi_fast = fast;
     ftab_early_done = ftab_early && fast;
     ftab_early = false;
-    if (fast) CK(mcpy(&hstat->herr, ferr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    CK(mcpy(&hstat->stats, stats.p, sizeof(QagsStats), cudaMemcpyDeviceToHost, s));
+    herr_copy_pending = fast;  // copied at the end (complete_deferred)
+    lumi_stats = node_flux;
+    if (node_flux) CK(mcpy(&hstat->stats, stats.p, sizeof(QagsStats), cudaMemcpyDeviceToHost, s));
     lumi_pending = true;
     lumi_ready = true;
     return UPCG_OK;
@@ -1481,7 +1551,8 @@ int upcg_generator::build_lumi() {
     CK(mcpy_sync(&herr, ferr.p, sizeof herr, cudaMemcpyDeviceToHost));
     if (herr) return fail(UPCG_ERR_CUDA, "tensor-core contraction timed out (code %u)", herr);
   }
-  CK(mcpy(&last_stats, stats.p, sizeof last_stats, cudaMemcpyDeviceToHost, s));
+  if (node_flux) CK(mcpy(&last_stats, stats.p, sizeof last_stats, cudaMemcpyDeviceToHost, s));
+  else last_stats = QagsStats{};
   CK(cudaStreamSynchronize(s));
   lumi_ready = true;
   return UPCG_OK;
@@ -1594,6 +1665,10 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_read
       medges_ok = true;
     }
   }
+  if (!isVM) {  // sigma(m) per m-row for the fold (build_xsec)
+    CK(csm.ensure(usePolarizedCS ? 2 * (size_t)nm : (size_t)nm));
+    CK(launch_cs_m_rows(f, csm.p, ss));
+  }
   if (isVM) {
     CK(cdfz.ensure(1));  // no z distribution (ignoreCSZ)
   } else if (!usePolarizedCS) {
@@ -1649,16 +1724,13 @@ int upcg_generator::build_xsec() {
     cudaEventCreate(&t1);
     cudaEventRecord(t0, s);
   }
-  if (!isVM) {  // vector mesons: cs, ratio and tot come from build_vm
-    CK(cs.ensure(ncell));
-    CK(ratio.ensure(usePolarizedCS ? ncell : 1));
-    CK(partial.ensure(fold_partial_doubles(nm, ny)));
-    CK(tot.ensure(1));
-    CK(launch_fold(f, lumi.p, usePolarizedCS ? lumi2.p : nullptr, cs.p, ratio.p, partial.p, tot.p, s));
-  }
   CK(cdf2.ensure((size_t)ncell + 1));
+  CK(cdf2fx.ensure((size_t)ncell + 1));
   CK(cdf_scratch.ensure(cdf_2d_scratch_doubles(ncell)));
-  CK(launch_cdf_2d(cs.p, ncell, cdf2.p, cdf_scratch.p, s));
+  if (isVM) {  // vector mesons: cs, ratio and tot come from build_vm
+    CK(launch_cdf_2d(cs.p, ncell, cdf2.p, cdf_scratch.p, s));
+  }
+  // the luminosity-independent samplers (sigma(m) among them) before the fold
   if (static_pending) {  // enqueued on a side stream before the luminosity
     CK(cudaStreamWaitEvent(s, ev_static, 0));
     static_pending = false;
@@ -1666,13 +1738,22 @@ int upcg_generator::build_xsec() {
     const int rc = enqueue_static_samplers(s);
     if (rc) return rc;
   }
+  if (!isVM) {
+    CK(cs.ensure(ncell));
+    CK(ratio.ensure(usePolarizedCS ? ncell : 1));
+    CK(tot.ensure(1));
+    CK(launch_fold_cdf(f, lumi.p, usePolarizedCS ? lumi2.p : nullptr, csm.p, cs.p, ratio.p,
+                       cdf_scratch.p, tot.p, cdf2.p, cdf2fx.p, s));
+  }
   {
     const EventParams e = event_params();
     CK(guide2.ensure(e.g2_n));
-    CK(cdf2fx.ensure((size_t)ncell + 1));
     const EventParams eg = event_params();  // with the guide buffer allocated
-    CK(launch_guides(eg, cdf2.p, nullptr, nullptr, guide2.p, nullptr, nullptr, s, cdf2fx.p,
-                     nullptr));
+    if (isVM)
+      CK(launch_guides(eg, cdf2.p, nullptr, nullptr, guide2.p, nullptr, nullptr, s, cdf2fx.p,
+                       nullptr));
+    else
+      CK(launch_guide2_fx(eg, cdf2fx.p, guide2.p, s));
   }
   if (cap) {  // a captured replay leaves sigma_tot on the device (read after the replay)
     xsec_ready = true;
@@ -1845,7 +1926,7 @@ int upcg_generator::enqueue_scan_front(upcg_scan& sc, int ci) {
   double* fc = sc.fc.p + 2 * ci;
   CK(launch_far_consts(p, breakupMode != 1, fc, s));
   CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, sc.gh.p + ci * plane,
-                   sc.gl.p + ci * plane, s, fc));
+                   sc.gl.p + ci * plane, s, fc, 1, nullptr, nullptr, 1));
   FastFluxTables ft = ftab_last;
   CK(build_flux_tables(p, &ft, fqn.p, fwn.p, nqn_last, fH.p, fJ.p, fpartq.p, s, 0));
   const size_t r0 = (size_t)sc.row0[ci];
@@ -1865,7 +1946,7 @@ int upcg_generator::enqueue_scan_back(upcg_scan& sc, int ci) {
   const int nrows = nm * (fast_nrep > 0 ? fast_nrep : ny);
   CK(launch_fast_finish(p, 0, nrows, ntiles, 0.0, sc.part.p + r0 * ntiles, sc.far.p + 4 * r0,
                         lumi.p, s, sc.fc.p + 2 * ci, fast_nrep > 0 ? frep.p : nullptr,
-                        fast_nrep > 0 ? frep.p + fast_nrep : nullptr, fast_nrep, 0));
+                        fast_nrep > 0 ? frep.p + fast_nrep : nullptr, fast_nrep, 0, 1));
   lumi_ready = true;
   cap = true;
   const int rc = build_xsec();
@@ -2911,15 +2992,34 @@ int scan_setup(upcg_scan* sc) {
                          &sc->grid, 0);
   if (rc) return rc;
   const int tbn = sc->shape == 0 ? 256 : 128;
+  // the K tiles where the delta survival kernels can be nonzero (the same
+  // radial grid and azimuths for every configuration)
+  std::vector<std::pair<int, int>> kr;
+  {
+    const double fu0 = std::log(0.1), fh = (std::log(256.) - std::log(0.1)) / (P - 1);
+    kr = sc->gens[0]->delta_ranges(P, fu0, fh, tbn, sc->gens[0]->lumi_params(), false);
+  }
   std::vector<int4> items;
   for (int i = 0; i < n; ++i) {
     const upcg_generator* g = sc->gens[i];
     const int ncell = g->nm * (g->fast_nrep > 0 ? g->fast_nrep : g->ny);
     for (int mt = 0; mt < sc->rows[i] / 128; ++mt)
       for (int nt = 0; nt < P / tbn; ++nt)
-        items.push_back(make_int4(sc->row0[i] / 128 + mt, nt, i, std::min(128, ncell - mt * 128)));
+        items.push_back(make_int4(sc->row0[i] / 128 + mt, nt, i,
+                                  pack_item(std::min(128, ncell - mt * 128), kr[nt].first,
+                                            kr[nt].second)));
   }
   sc->nitems = (int)items.size();
+  // the first nonzero K tile of any configuration (the smallest b_min)
+  int kt0 = P / kContractBK;
+  {
+    const double fu0 = std::log(0.1), fh = (std::log(256.) - std::log(0.1)) / (P - 1);
+    for (const upcg_generator* g : sc->gens)
+      kt0 = std::min(kt0, fast_first_ktile(g->isPoint ? g->R : 0.05 * g->R, fu0, fh));
+  }
+  // items of unequal work: every CTA meets every N tile
+  sc->grid = std::min(sc->grid, (int)items.size());
+  rotate_rounds(items, sc->grid);
   CK(sc->items.ensure(items.size()));
   CK(mcpy(sc->items.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, sc->s));
   CK(cudaStreamSynchronize(sc->s));
@@ -2936,13 +3036,6 @@ int scan_setup(upcg_scan* sc) {
   for (int i = 0; i < n; ++i) {
     rc = sc->gens[i]->enqueue_scan_front(*sc, i);
     if (rc) return abort_capture(rc);
-  }
-  // the first nonzero K tile of any configuration (the smallest b_min)
-  int kt0 = P / 64;
-  {
-    const double fu0 = std::log(0.1), fh = (std::log(256.) - std::log(0.1)) / (P - 1);
-    for (const upcg_generator* g : sc->gens)
-      kt0 = std::min(kt0, fast_first_ktile(g->isPoint ? g->R : 0.05 * g->R, fu0, fh));
   }
   if (launch_contract_pers(sc->ah.p, sc->al.p, sc->gh.p, sc->gl.p, n, sc->rows_total, P,
                            sc->items.p, sc->nitems, sc->a2.p, sc->part.p, sc->err.p, sc->shape,

@@ -216,4 +216,9 @@ __constant__ static double kWg[5] = {
     0.219086362515982043995534934228163, 0.269266719309996355091226921569469,
     0.295524224714752870173892994651338};
 
+// A CDF value in [0, 1] as 64-bit fixed point (1 and above: all ones)
+__device__ __forceinline__ uint64_t cdf_to_fx(double v) {
+  return v >= 1. ? ~0ull : (v > 0. ? (uint64_t)(v * 18446744073709551616.0) : 0ull);
+}
+
 }  // namespace upcg

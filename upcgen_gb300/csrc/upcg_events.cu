@@ -708,8 +708,7 @@ __global__ void k_guide_rows_d(const double* __restrict__ cdf, int rows, int len
 __global__ void k_cdf_fixed(const double* __restrict__ cdf, int64_t n, uint64_t* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double v = cdf[i];
-  out[i] = v >= 1. ? ~0ull : (v > 0. ? (uint64_t)(v * 18446744073709551616.0) : 0ull);
+  out[i] = cdf_to_fx(cdf[i]);
 }
 
 // guide[r][j]: the bin of r_j = j 2^(64 - bits) in fixed-point CDF row r
@@ -729,6 +728,28 @@ __global__ void k_guide_rows_f(const float* __restrict__ cdf, int rows, int len,
   if (t >= (int64_t)rows * K) return;
   const int r = (int)(t / K), j = (int)(t - (int64_t)r * K);
   guide[t] = (uint16_t)cdf_find_f(cdf + (size_t)r * (len + 1), len, (float)j / (float)K);
+}
+
+// The same guide entries, one CTA per row: the row's CDF entries [0, len) --
+// all that cdf_find_f reads -- staged in shared memory, then the same binary
+// search for each of the K points (the global-memory form's searches are
+// chains of dependent L2 reads).
+__global__ void __launch_bounds__(256) k_guide_rows_fs(const float* __restrict__ cdf, int len,
+                                                       int K, uint16_t* __restrict__ guide) {
+  extern __shared__ float sc[];
+  const float* src = cdf + (size_t)blockIdx.x * (len + 1);
+  for (int i = threadIdx.x; i < len; i += blockDim.x) sc[i] = src[i];
+  __syncthreads();
+  uint16_t* g = guide + (size_t)blockIdx.x * K;
+  for (int j = threadIdx.x; j < K; j += blockDim.x) {
+    const float u = (float)j / (float)K;
+    int lo = 0, hi = len;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (u >= sc[mid]) lo = mid; else hi = mid;
+    }
+    g[j] = (uint16_t)lo;
+  }
 }
 
 // Every candidate of [cand0, cand0 + n) with its accept flag (single-event API).
@@ -782,6 +803,14 @@ cudaError_t launch_philox_dump(uint64_t seed, uint64_t c0, int64_t n, uint32_t* 
   return cudaGetLastError();
 }
 
+cudaError_t launch_guide2_fx(const EventParams& e, const uint64_t* d_cdf2fx, int* d_g2,
+                             cudaStream_t st) {
+  if (e.g2_n != (1 << e.g2_bits)) return cudaErrorInvalidValue;
+  note_launch();
+  k_guide_rows_fx<<<(e.g2_n + 255) / 256, 256, 0, st>>>(d_cdf2fx, 1, e.nm * e.ny, e.g2_bits, d_g2);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                           const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
                           cudaStream_t st, uint64_t* d_cdf2fx, uint64_t* d_cdfzfx) {
@@ -808,10 +837,15 @@ cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const doub
                                                                   d_gz);
   }
   if (d_gpt && (e.useNonzeroGamPt || e.vm)) {  // vector mesons always draw a photon pT
-    const int64_t np = (int64_t)e.pt_ne * e.gpt_n;
+    const size_t smem = sizeof(float) * (size_t)e.pt_nbins;
     note_launch();
-    k_guide_rows_f<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(d_ptcdf, e.pt_ne, e.pt_nbins,
-                                                                 e.gpt_n, d_gpt);
+    if (smem <= 48 * 1024) {
+      k_guide_rows_fs<<<e.pt_ne, 256, smem, st>>>(d_ptcdf, e.pt_nbins, e.gpt_n, d_gpt);
+    } else {
+      const int64_t np = (int64_t)e.pt_ne * e.gpt_n;
+      k_guide_rows_f<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(d_ptcdf, e.pt_ne, e.pt_nbins,
+                                                                   e.gpt_n, d_gpt);
+    }
   }
   return cudaGetLastError();
 }

@@ -34,6 +34,7 @@ namespace upcg {
 namespace {
 
 constexpr int BM = 128, BN = 256, BK = 64;
+static_assert(BK == kContractBK, "K tile of the work items");
 constexpr int kStages = 2;
 constexpr int kATile = BM * BK * 2;  // 16 KB
 constexpr int kBTile = BN * BK * 2;  // 32 KB
@@ -452,6 +453,16 @@ struct GParams {
   float P20, cosk[5], wk[5];
   float u0, h;
   const double* P20d;  // when set: P20 from the device (k_far_consts)
+  // when far_out is set, each block takes P20 from the FP64 breakup spline
+  // itself, and block (0, 0) writes k_far_consts' pair (P20, P20 sum_k w_k)
+  // to far_out and resets the contraction's error word err0
+  SplineU brk64;
+  double wkd[5];
+  double* far_out;
+  unsigned* err0;
+  // delta: store G - P20 sum_k w_k (zero wherever all five azimuths reach
+  // b >= 20 fm); k_fast_finish adds the constant's share back in FP64
+  int delta;
 };
 
 // G_pq = sum_k w_k P(min(b,20)) (b<20 ? G_AA(b) : 1), b^2 = r_p^2 + r_q^2 +
@@ -460,13 +471,25 @@ struct GParams {
 __global__ void k_fast_G(GParams gp, int P, __nv_bfloat16* __restrict__ gh,
                          __nv_bfloat16* __restrict__ gl) {
   __shared__ float4 sg[200];
+  __shared__ float sP20;
   for (int i = threadIdx.x; i < gp.gaa.n - 1 && i < 200; i += blockDim.x) sg[i] = gp.gaa.coef[i];
+  if (gp.far_out && threadIdx.x == 0) {  // k_far_consts' arithmetic
+    const double P20 = gp.has_brk ? spline_eval(gp.brk64, 20.) : 1.;
+    sP20 = (float)P20;
+    if (blockIdx.x == 0 && blockIdx.y == 0) {
+      double c = 0.;
+      for (int k = 0; k < 5; ++k) c += P20 * 1. * gp.wkd[k];
+      gp.far_out[0] = P20;
+      gp.far_out[1] = c;
+      if (gp.err0) *gp.err0 = 0u;
+    }
+  }
   __syncthreads();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int pp = blockIdx.y;
   if (q >= P) return;
   const float rp = expf(gp.u0 + pp * gp.h), rq = expf(gp.u0 + q * gp.h);
-  const float P20 = gp.P20d ? (float)__ldg(gp.P20d) : gp.P20;
+  const float P20 = gp.far_out ? sP20 : (gp.P20d ? (float)__ldg(gp.P20d) : gp.P20);
   float g = 0.f;
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
@@ -477,7 +500,7 @@ __global__ void k_fast_G(GParams gp, int P, __nv_bfloat16* __restrict__ gh,
       if (b < 20.f)
         v = (gp.has_brk ? spline_eval_f(gp.brk, gp.brk.coef, b) : 1.f) * spline_eval_f(gp.gaa, sg, b);
     }
-    g += v * gp.wk[k];
+    g += (gp.delta ? v - P20 : v) * gp.wk[k];
   }
   const __nv_bfloat16 hi = __float2bfloat16(g);
   const __nv_bfloat16 lo = __float2bfloat16(g - __bfloat162float(hi));
@@ -534,9 +557,23 @@ __global__ void k_ktab_logs(double g, const double2* __restrict__ lk, double* __
 // the product H[w][n] J[n][b] (k_qtab_product, double-float), the rest in
 // closed form (k_dgemm_reduce).
 __global__ void k_qtab_H(LumiParams p, const double* __restrict__ qn, const double* __restrict__ wn,
-                         int nq, double lw0, double hw, double* __restrict__ H) {
+                         int nq, double lw0, double hw, double* __restrict__ H, double lb0,
+                         double hb, int nb, double* __restrict__ tail) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   const int iw = blockIdx.y;
+  // q in [kQNodeMax, 10]: q^2 + w^2/g^2 > Q2max, so the reference's integrand
+  // is F(Q2max - dQ2) q^2 / (q^2 + w^2/g^2) J1(b q / hc); with the
+  // q^2 / (q^2 + w^2/g^2) factor taken as 1 its integral is
+  // F_c hc / b (J0(b qc / hc) - J0(10 b / hc)).  The factor's departure,
+  // (w/g)^2 / qc^2 at most, is below 1e-2 for w < 0.2 g, where this part is
+  // itself ~1e-6 of Q; at larger w the flux is below 1e-10 of its peak.
+  if (blockIdx.x == 0 && iw == 0) {
+    const double fc = spline_eval(p.ff, p.q2clamp) * kHc;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+      const double b = exp(lb0 + j * hb);
+      tail[j] = fc / b * (j0(b * kQNodeMax / kHc) - j0(b * 10. / kHc));
+    }
+  }
   if (n >= nq) return;
   const double w = exp(lw0 + iw * hw);
   const double q = qn[n];
@@ -548,9 +585,10 @@ __global__ void k_qtab_H(LumiParams p, const double* __restrict__ qn, const doub
   reinterpret_cast<float2*>(H)[(size_t)iw * nq + n] = make_float2(hh, (float)(h - (double)hh));
 }
 
+// J1(b q_n / hc) on the table's (node, b) grid: it needs no form factor, so
+// it can run before the form-factor chain is done
 __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, double hb, int nb,
-                         SplineU ff, double q2clamp, double* __restrict__ J,
-                         double* __restrict__ tail) {
+                         double* __restrict__ J) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = blockIdx.y;
   if (j >= nb) return;
@@ -558,14 +596,6 @@ __global__ void k_qtab_J(const double* __restrict__ qn, int nq, double lb0, doub
   const double jv = j1(b * qn[n] / kHc);
   const float jh = (float)jv;  // a double-float pair (hi, lo) for k_qtab_product
   reinterpret_cast<float2*>(J)[(size_t)n * nb + j] = make_float2(jh, (float)(jv - (double)jh));
-  // q in [kQNodeMax, 10]: q^2 + w^2/g^2 > Q2max, so the reference's integrand
-  // is F(Q2max - dQ2) q^2 / (q^2 + w^2/g^2) J1(b q / hc); with the
-  // q^2 / (q^2 + w^2/g^2) factor taken as 1 its integral is
-  // F_c hc / b (J0(b qc / hc) - J0(10 b / hc)).  The factor's departure,
-  // (w/g)^2 / qc^2 at most, is below 1e-2 for w < 0.2 g, where this part is
-  // itself ~1e-6 of Q; at larger w the flux is below 1e-10 of its peak.
-  if (n == 0)
-    tail[j] = spline_eval(ff, q2clamp) * kHc / b * (j0(b * kQNodeMax / kHc) - j0(b * 10. / kHc));
 }
 
 // Split-K product Cp[s][M][N] = A[M][Ks] B[Ks][N] over the s-th slice of K
@@ -988,7 +1018,8 @@ __global__ void k_far_consts(SplineU brk, int has_brk, LumiParams p, double* __r
 __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, double c_far,
                               const double* __restrict__ c_far_d,
                               const float* __restrict__ partial, const float4* __restrict__ side_part,
-                              double* __restrict__ lumi, FastGrid fg, const int* __restrict__ rep_mir) {
+                              double* __restrict__ lumi, FastGrid fg, const int* __restrict__ rep_mir,
+                              int delta) {
   const int lc = blockIdx.x * blockDim.x + threadIdx.x;
   if (lc >= ncells) return;
   const int cell = fast_cell(fg, p.ny, cell0 + lc);
@@ -997,9 +1028,15 @@ __global__ void k_fast_finish(LumiParams p, int cell0, int ncells, int ntiles, d
   double t2 = 0.;
   for (int t = 0; t < ntiles; ++t) t2 += (double)partial[(size_t)lc * ntiles + t];
   const float4 s0 = side_part[2 * lc], s1 = side_part[2 * lc + 1];  // (ln scale, near, far)
-  const float far = s0.z * (s1.y + s1.z) + s0.y * s1.z;
+  // the constant part of the survival kernel, c (S0 S1 - S0near S1near) --
+  // or, when the contraction took G - c (delta), c S0 S1
+  double far;
+  if (delta)
+    far = ((double)s0.y + (double)s0.z) * ((double)s1.y + (double)s1.z);
+  else
+    far = (double)(s0.z * (s1.y + s1.z) + s0.y * s1.z);
   const double cf = c_far_d ? c_far_d[1] : c_far;
-  const double s = exp((double)s0.x + (double)s1.x) * (cf * (double)far + t2);
+  const double s = exp((double)s0.x + (double)s1.x) * (cf * far + t2);
   const double v = 2 * kPi * kPi * M * s * p.dm * p.dy;
   lumi[cell] = v;
   if (fg.rep_y) {  // the mirror rapidity's cell
@@ -1127,9 +1164,31 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // Work item of the persistent contraction: a 128-row tile of the stacked
 // operands, one N tile of the survival kernel, and the configuration whose
 // kernel plane it uses.
+// One work item: an M tile of rows x an N tile of the radial grid.  pack:
+// bits 0-7 the tile's valid rows (<= 128); bits 8-15 / 16-23 the item's K
+// tiles [lo, hi), hi = 0 for all of them -- the K tiles where the survival
+// kernel's N tile is nonzero (the delta form, G - c, is zero on the others).
 struct PersItem {
-  int mtile, ntile, config, rows;  // rows: valid rows of the tile (<= 128)
+  int mtile, ntile, config, pack;
 };
+
+__device__ __forceinline__ int item_rows(const PersItem& w) { return w.pack & 0xff; }
+
+// The K tiles an item multiplies: its own range within [kt0, ktiles) (kt0:
+// the first K tile with a nonzero A1 column in any row).  An empty range keeps
+// the single tile kt0, whose product is zero -- its A1 or its survival tile
+// is -- so that every item has an accumulator to read.
+struct KRange {
+  int lo, hi;
+};
+__device__ __forceinline__ KRange item_krange(const PersItem& w, int kt0, int ktiles) {
+  const int e = (w.pack >> 16) & 0xff;
+  if (e == 0) return {kt0, ktiles};
+  const int a = (w.pack >> 8) & 0xff;
+  KRange r{a > kt0 ? a : kt0, e < ktiles ? e : ktiles};
+  if (r.lo >= r.hi) r = {kt0, kt0 + 1};
+  return r;
+}
 
 struct PersArgs {
   const PersItem* items;
@@ -1218,6 +1277,8 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
+  // this CTA's items: blockIdx.x, + gridDim.x, ... (nmine of them)
+  const int i0 = blockIdx.x, istep = gridDim.x;
   const int nmine = args.nitems > (int)blockIdx.x
                         ? (args.nitems - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
                         : 0;
@@ -1227,8 +1288,9 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
     int g = 0;  // k tiles issued by this CTA
     bool ok = true;
     for (int it = 0; it < nmine && ok; ++it) {
-      const PersItem w = args.items[blockIdx.x + it * gridDim.x];
-      for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
+      const PersItem w = args.items[i0 + it * istep];
+      const KRange kr = item_krange(w, args.kt0, args.ktiles);
+      for (int kt = kr.lo; kt < kr.hi; ++kt, ++g) {
         const int s = g % TST;
         if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 1u)) {
           ok = false;
@@ -1264,7 +1326,9 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
       }
       tc_fence_after();
       const uint32_t acc = tmem + (uint32_t)(b * TBN);
-      for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
+      const PersItem w = args.items[i0 + it * istep];
+      const KRange kr = item_krange(w, args.kt0, args.ktiles);
+      for (int kt = kr.lo; kt < kr.hi; ++kt, ++g) {
         const int s = g % TST;
         if (!mbar_wait(&full_bar[s], (g / TST) & 1, args.err, 2u)) {
           ok = false;
@@ -1279,7 +1343,7 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
           const uint32_t off = kk * 32;
           const uint64_t dah = sw128_desc(ah + off), dal = sw128_desc(al + off);
           const uint64_t dbh = sw128_desc(bh + off), dbl = sw128_desc(bl + off);
-          const uint32_t first = (kt > args.kt0 || kk > 0) ? 1u : 0u;
+          const uint32_t first = (kt > kr.lo || kk > 0) ? 1u : 0u;
           asm volatile(
               "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
               " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
@@ -1300,19 +1364,33 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
   } else if (warp >= 2) {
     // ---------------- epilogue: TMEM -> registers, row-dot with A2
     const int quad = warp & 3;
+    constexpr int kPf = 4;  // A2 chunks (16 floats) in flight ahead of the row-dot
     for (int it = 0; it < nmine; ++it) {
-      const PersItem w = args.items[blockIdx.x + it * gridDim.x];
+      const PersItem w = args.items[i0 + it * istep];
       const int b = it & 1;
-      const bool ok = mbar_wait(&accf[b], (it >> 1) & 1, args.err, 4u);
-      tc_fence_after();
       const int row = quad * 32 + lane;
       const size_t grow = (size_t)w.mtile * BM + row;
+      const bool vrow = row < item_rows(w);
+      // the row's first A2 chunks are requested before the accumulator is
+      // ready (they do not depend on it), the later ones kPf chunks ahead
+      const float4* a4 =
+          args.a2 ? reinterpret_cast<const float4*>(args.a2 + grow * args.P + w.ntile * TBN)
+                  : nullptr;
+      float4 xq[kPf][4];
+      if (a4 && vrow) {
+#pragma unroll
+        for (int c = 0; c < kPf; ++c)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) xq[c][q] = __ldg(a4 + 4 * c + q);
+      }
+      const bool ok = mbar_wait(&accf[b], (it >> 1) & 1, args.err, 4u);
+      tc_fence_after();
       float acc = 0.f;
       if (ok && !args.a2) {  // side 1 from its node list
         const float* nd = args.nodes + (grow * 2 + 1) * kNodeStride;
         float tg0 = 0.f, tgd = 1.f;
         int nn = 0;
-        if (row < w.rows) {
+        if (row < item_rows(w)) {
           const float4 hd = __ldg(reinterpret_cast<const float4*>(nd));
           tg0 = hd.x;
           tgd = hd.y;
@@ -1326,21 +1404,25 @@ __global__ void __launch_bounds__(192, 1) k_contract_pers(const __grid_constant_
           acc = gather_dot16(v, w.ntile * TBN + c0, tg0, tgd, nn, nd + 4, cur, scr, acc);
         }
       } else if (ok) {
-        const float* a2 = args.a2 + grow * args.P + w.ntile * TBN;
-        for (int c0 = 0; c0 < TBN; c0 += 16) {
+#pragma unroll
+        for (int c = 0; c < TBN / 16; ++c) {
           float v[16];
-          tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TBN + c0), v);
-          if (row < w.rows) {
-            const float4* a4 = reinterpret_cast<const float4*>(a2 + c0);
+          tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TBN + 16 * c), v);
+          if (vrow) {
+            const int sl = c % kPf;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-              const float4 x = __ldg(a4 + q);
+              const float4 x = xq[sl][q];
               acc += v[4 * q] * x.x + v[4 * q + 1] * x.y + v[4 * q + 2] * x.z + v[4 * q + 3] * x.w;
+            }
+            if (c + kPf < TBN / 16) {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) xq[sl][q] = __ldg(a4 + 4 * (c + kPf) + q);
             }
           }
         }
       }
-      if (row < w.rows) args.partial[grow * args.ntiles + w.ntile] = ok ? acc : 0.f;
+      if (vrow) args.partial[grow * args.ntiles + w.ntile] = ok ? acc : 0.f;
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[b]);
@@ -1442,6 +1524,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
+  // this CTA's items: blockIdx.x, + gridDim.x, ... (nmine of them)
+  const int i0 = blockIdx.x, istep = gridDim.x;
   const int nmine = args.nitems > (int)blockIdx.x
                         ? (args.nitems - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
                         : 0;
@@ -1452,8 +1536,9 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
       int g = 0;
       bool ok = true;
       for (int it = 0; it < nmine && ok; ++it) {
-        const PersItem w = args.items[blockIdx.x + it * gridDim.x];
-        for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
+        const PersItem w = args.items[i0 + it * istep];
+        const KRange kr = item_krange(w, args.kt0, args.ktiles);
+        for (int kt = kr.lo; kt < kr.hi; ++kt, ++g) {
           const int s = g % TST;
           if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 1u)) {
             ok = false;
@@ -1489,7 +1574,9 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
         }
         tc_fence_after();
         const uint32_t acc = tmem + (uint32_t)(b * TBN);
-        for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
+        const PersItem w = args.items[i0 + it * istep];
+        const KRange kr = item_krange(w, args.kt0, args.ktiles);
+        for (int kt = kr.lo; kt < kr.hi; ++kt, ++g) {
           const int s = g % TST;
           if (!mbar_wait(&full_bar[s], (g / TST) & 1, args.err, 2u)) {
             ok = false;
@@ -1504,7 +1591,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
             const uint32_t off = kk * 32;
             const uint64_t dah = sw128_desc(ah + off), dal = sw128_desc(al + off);
             const uint64_t dbh = sw128_desc(bh + off), dbl = sw128_desc(bl + off);
-            const uint32_t first = (kt > args.kt0 || kk > 0) ? 1u : 0u;
+            const uint32_t first = (kt > kr.lo || kk > 0) ? 1u : 0u;
             asm volatile(
                 "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
@@ -1529,7 +1616,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
     const int row = quad * 32 + lane;
     float* scr = &ep_scr[warp - 2][lane][0];
     for (int it = 0; it < nmine; ++it) {
-      const PersItem w = args.items[blockIdx.x + it * gridDim.x];
+      const PersItem w = args.items[i0 + it * istep];
       const int b = it & 1;
       const bool ok = mbar_wait(&accf[b], (it >> 1) & 1, args.err, 4u);
       tc_fence_after();
@@ -1537,7 +1624,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
       const float* nd = args.nodes + (grow * 2 + 1) * kNodeStride;
       float tg0 = 0.f, tgd = 1.f;
       int nn = 0;
-      if (row < w.rows) {
+      if (row < item_rows(w)) {
         const float4 hd = __ldg(reinterpret_cast<const float4*>(nd));
         tg0 = hd.x;
         tgd = hd.y;
@@ -1552,7 +1639,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
           acc = gather_dot16(v, w.ntile * TBN + c0, tg0, tgd, nn, nd + 4, cur, scr, acc);
         }
       }
-      if (row < w.rows) args.partial[grow * args.ntiles + w.ntile] = ok ? acc : 0.f;
+      if (row < item_rows(w)) args.partial[grow * args.ntiles + w.ntile] = ok ? acc : 0.f;
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[b]);
@@ -1567,12 +1654,12 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
     int g = 0;
     bool ok = true;
     for (int it = 0; it < nmine && ok; ++it) {
-      const PersItem w = args.items[blockIdx.x + it * gridDim.x];
+      const PersItem w = args.items[i0 + it * istep];
       const size_t grow = (size_t)w.mtile * BM + r;
       const float* nd = args.nodes + grow * 2 * kNodeStride;  // side 0
       float tg0 = 0.f, tgd = 1.f;
       int nn = 0;
-      if (r < w.rows) {
+      if (r < item_rows(w)) {
         const float4 hd = __ldg(reinterpret_cast<const float4*>(nd));
         tg0 = hd.x;
         tgd = hd.y;
@@ -1583,7 +1670,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_contract_fused(
       // (first points floor(t_i) - 1 at least 4 apart after rounding; always
       // so for the form-factor flux, where b_max / b_min >= 100 gives >= 5)
       const bool disjoint = tgd >= 4.5f;
-      for (int kt = args.kt0; kt < args.ktiles; ++kt, ++g) {
+      const KRange kr = item_krange(w, args.kt0, args.ktiles);
+      for (int kt = kr.lo; kt < kr.hi; ++kt, ++g) {
         const int s = g % TST;
         if (g >= TST && !mbar_wait(&empty_bar[s], ((g / TST) & 1) ^ 1, args.err, 32u)) {
           ok = false;
@@ -1720,6 +1808,55 @@ int fast_grid_points() { return 1024; }
 int fast_first_ktile(double b_min, double u0, double h) {
   const int p0 = (int)std::floor((std::log(b_min) - u0) / h) - 2;
   return p0 < 0 ? 0 : p0 / BK;
+}
+
+// For azimuth cosine c, b^2 = rp^2 + rq^2 + 2 rp rq c < T holds for rq in
+// (-rp c - d, -rp c + d), d = sqrt(T - rp^2 (1 - c^2)): per grid row p the
+// columns q of that interval (one column of margin each side), per tile pair
+// the union over p and the azimuths.  T = 400 (1 + 1e-3) covers the FP32
+// radii and b^2 of k_fast_G.
+void delta_tile_ranges(int P, double u0, double h, const double* cosk, int ncos, int tbn, int bk,
+                       std::vector<std::pair<int, int>>& out) {
+  const int nt = P / tbn;
+  std::vector<int> lo(nt, 1 << 30), hi(nt, -1);
+  const double T = 400. * (1. + 1e-3);
+  for (int p = 0; p < P; ++p) {
+    const double rp = std::exp(u0 + p * h);
+    for (int k = 0; k < ncos; ++k) {
+      const double c = cosk[k];
+      const double disc = T - rp * rp * (1. - c * c);
+      if (disc < 0.) continue;
+      const double d = std::sqrt(disc), rm = -rp * c - d, rpl = -rp * c + d;
+      if (rpl <= 0.) continue;
+      int q0 = rm > 0. ? (int)std::floor((std::log(rm) - u0) / h) - 1 : 0;
+      int q1 = (int)std::ceil((std::log(rpl) - u0) / h) + 1;
+      q0 = std::max(q0, 0);
+      q1 = std::min(q1, P - 1);
+      for (int t = q0 / tbn; q0 <= q1 && t <= q1 / tbn; ++t) {
+        lo[t] = std::min(lo[t], p / bk);
+        hi[t] = std::max(hi[t], p / bk + 1);
+      }
+    }
+  }
+  out.resize(nt);
+  for (int t = 0; t < nt; ++t)
+    out[t] = hi[t] < 0 ? std::make_pair(P / bk, P / bk) : std::make_pair(lo[t], hi[t]);
+}
+
+// CTA b takes items b, b + grid, ...: the grid items of one round run side by
+// side, and the list keeps the N tiles of a row tile adjacent, so that a
+// round's CTAs share their row tiles' A reads in L2.  With items of unequal
+// work (their K ranges per N tile) a CTA would meet the same N tile in every
+// round; rotating round r by r positions deals each CTA every N tile in turn.
+void rotate_rounds(std::vector<int4>& items, int grid) {
+  const int n = (int)items.size();
+  if (grid < 2 || n < 2) return;
+  std::vector<int4> out(items.size());
+  for (int r0 = 0, r = 0; r0 < n; r0 += grid, ++r) {
+    const int m = std::min(grid, n - r0);
+    for (int b = 0; b < m; ++b) out[r0 + b] = items[r0 + (b + r) % m];
+  }
+  items.swap(out);
 }
 
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
@@ -1891,18 +2028,28 @@ cudaError_t launch_pair_to_f32(const void* hi, const void* lo, size_t n, float* 
 
 cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, double P20,
                           float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st,
-                          const double* P20d) {
+                          const double* P20d, int convert, double* far_out, unsigned* err0,
+                          int delta) {
   if (p.gaa.n - 1 > 200) return cudaErrorInvalidValue;
   GParams gp{};
-  note_launch();
-  k_coef_f32<<<(p.gaa.n - 1 + 255) / 256, 256, 0, st>>>(p.gaa.coef, d_gaa32, p.gaa.n - 1);
+  if (convert) {
+    note_launch();
+    k_coef_f32<<<(p.gaa.n - 1 + 255) / 256, 256, 0, st>>>(p.gaa.coef, d_gaa32, p.gaa.n - 1);
+  }
   gp.gaa = SplineF{d_gaa32, (float)p.gaa.x0, (float)p.gaa.h, (float)p.gaa.inv_h, p.gaa.n};
   gp.has_brk = p.breakupMode != 1;
   if (gp.has_brk) {
-    note_launch();
-    k_coef_f32<<<(p.brk.n - 1 + 255) / 256, 256, 0, st>>>(p.brk.coef, d_brk32, p.brk.n - 1);
+    if (convert) {
+      note_launch();
+      k_coef_f32<<<(p.brk.n - 1 + 255) / 256, 256, 0, st>>>(p.brk.coef, d_brk32, p.brk.n - 1);
+    }
     gp.brk = SplineF{d_brk32, (float)p.brk.x0, (float)p.brk.h, (float)p.brk.inv_h, p.brk.n};
   }
+  gp.brk64 = p.brk;
+  for (int k = 0; k < 5; ++k) gp.wkd[k] = p.wk[k];
+  gp.far_out = far_out;
+  gp.err0 = err0;
+  gp.delta = delta;
   gp.P20 = (float)P20;
   for (int k = 0; k < 5; ++k) {
     gp.cosk[k] = (float)p.cosk[k];
@@ -1988,7 +2135,7 @@ cudaError_t launch_ktab(double g1, double* st, float* st32, cudaStream_t stream,
 
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
                               int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st,
-                              int w_lo, int with_ktab) {
+                              int w_lo, int with_ktab, cudaStream_t js, cudaEvent_t ev_j) {
   if (with_ktab) {
     note_launch();
     k_ktab<<<(kKTabN + 255) / 256, 256, 0, st>>>(p.g1, t->st, t->st32);
@@ -1999,13 +2146,20 @@ cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_
   if (!p.isPoint && rows > 0) {
     if (w_lo % 64 != 0) return cudaErrorInvalidValue;
     const double lw = t->lw0 + w_lo * t->hw;
-    dim3 gh((nq + 255) / 256, rows);
-    note_launch();
-    k_qtab_H<<<gh, 256, 0, st>>>(p, d_qn, d_wn, nq, lw, t->hw, d_H);
+    // J on js when given (ev_j recorded there, joined before H), else on st
     dim3 gj((t->nb + 255) / 256, nq);
+    note_launch();
+    k_qtab_J<<<gj, 256, 0, js ? js : st>>>(d_qn, nq, t->lb0, t->hb, t->nb, d_J);
+    if (js) {
+      cudaError_t e = cudaEventRecord(ev_j, js);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_j, 0);
+      if (e != cudaSuccess) return e;
+    }
+    dim3 gh((nq + 255) / 256, rows);
     double* d_tail = d_part + (size_t)8 * t->nw * t->nb;
     note_launch();
-    k_qtab_J<<<gj, 256, 0, st>>>(d_qn, nq, t->lb0, t->hb, t->nb, p.ff, p.q2clamp, d_J, d_tail);
+    k_qtab_H<<<gh, 256, 0, st>>>(p, d_qn, d_wn, nq, lw, t->hw, d_H, t->lb0, t->hb, t->nb,
+                                 d_tail);
     // K = nq split into nq / kslice slices; d_part holds them
     const int nslice = nq % (8 * 16) == 0 ? 8 : 1;
     const int kslice = nq / nslice;
@@ -2038,7 +2192,8 @@ cudaError_t launch_far_consts(const LumiParams& p, int has_brk, double* d_out, c
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
                                double c_far, const float* partial, const void* side_part,
                                double* lumi, cudaStream_t st, const double* c_far_d,
-                               const int* rep_y, const int* rep_mir, int n_rep_y, int m0) {
+                               const int* rep_y, const int* rep_mir, int n_rep_y, int m0,
+                               int delta) {
   FastGrid fg{};
   fg.rep_y = rep_y;
   fg.n_rep_y = n_rep_y;
@@ -2047,7 +2202,7 @@ cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int n
   note_launch();
   k_fast_finish<<<(ncells + 255) / 256, 256, 0, st>>>(p, cell0, ncells, ntiles, c_far, c_far_d,
                                                       partial, static_cast<const float4*>(side_part),
-                                                      lumi, fg, rep_mir);
+                                                      lumi, fg, rep_mir, delta);
   return cudaGetLastError();
 }
 

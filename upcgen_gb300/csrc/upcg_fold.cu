@@ -97,7 +97,6 @@ __global__ void k_cs_m_pts(FoldParams f, const double* __restrict__ m, double* _
   if (i < n) out[i] = cs_m(f, m[i], flag);
 }
 
-constexpr int kFoldThreads = 256;
 
 // sigma(m) of every mass row, once per row rather than once per cell: the FP64
 // cross section runs on the 1/64-rate pipe, which a warp of cells of one row
@@ -113,53 +112,6 @@ __global__ void k_cs_m_rows(FoldParams f, double* __restrict__ csm) {
     csm[im] = cs_m(f, m, 1);
     csm[f.nm + im] = cs_m(f, m, 2);
   }
-}
-
-// cs[iy][im] and one partial sum of cs per block (fixed order).
-__global__ void __launch_bounds__(kFoldThreads) k_fold(FoldParams f, const double* __restrict__ lumi,
-                                                       const double* __restrict__ lumi2,
-                                                       const double* __restrict__ csm,
-                                                       double* __restrict__ cs,
-                                                       double* __restrict__ ratio,
-                                                       double* __restrict__ partial) {
-  __shared__ double red[kFoldThreads];
-  const int n = f.nm * f.ny;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = im*ny + iy
-  double v = 0.;
-  if (i < n) {
-    const int im = i / f.ny, iy = i - im * f.ny;
-    const size_t co = (size_t)iy * f.nm + im;
-    if (!f.polarized) {
-      v = __ldg(csm + im) * lumi[i];
-    } else {
-      const double s = lumi[i] * __ldg(csm + im);
-      const double p = lumi2[i] * __ldg(csm + f.nm + im);
-      v = (s + p) * 1e7;
-      ratio[co] = s / p;
-    }
-    cs[co] = v;
-  }
-  red[threadIdx.x] = v;
-  __syncthreads();
-  for (int s = kFoldThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
-}
-
-__global__ void k_reduce_total(const double* __restrict__ partial, int n, double scale,
-                               double* __restrict__ out) {
-  __shared__ double red[1024];
-  double v = 0.;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) v += partial[i];
-  red[threadIdx.x] = v;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *out = red[0] * scale;
 }
 
 // Normalised cumulative sum of n weights (gsl_histogram_pdf_init:
@@ -263,20 +215,153 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf_write(const double* __restr
   }
 }
 
-// One thread per row, exactly the sequential GSL recurrence (running mean).
+// Row-wise normalised cumulative sums (gsl_histogram_pdf_init per row:
+// cdf[0] = 0, cdf[i+1] = cdf[i] + (w_i / mean) / len), one warp per row: the
+// mean as the row's sum / len, the terms (w_i / mean) / len by all lanes, and
+// their running sum by a warp scan.  Only the summation order (and the mean's
+// rounding) differs from the sequential recurrence (relative 1e-16).
 __global__ void k_cdf_rows(const double* __restrict__ w, int rows, int len,
                            double* __restrict__ cdf) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
+  const int r = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= rows) return;  // the whole warp: r is the same for its lanes
   const double* x = w + (size_t)r * len;
   double* c = cdf + (size_t)r * (len + 1);
-  double mean = 0;
-  for (int i = 0; i < len; i++) mean += (x[i] - mean) / ((double)(i + 1));
-  double s = 0;
-  c[0] = 0;
-  for (int i = 0; i < len; i++) {
-    s += (x[i] / mean) / len;
-    c[i + 1] = s;
+  double sum = 0.;
+  for (int i = lane; i < len; i += 32) sum += x[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  const double mean = sum / (double)len;
+  if (lane == 0) c[0] = 0.;
+  double run = 0.;
+  for (int i0 = 0; i0 < len; i0 += 32) {
+    const int i = i0 + lane;
+    double t = i < len ? (x[i] / mean) / (double)len : 0.;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double u = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += u;
+    }
+    t += run;
+    if (i < len) c[i + 1] = t;
+    run = __shfl_sync(0xffffffffu, t, 31);
+  }
+}
+
+// The two-photon cross section's fold and its sampling CDF in three launches
+// (the samplers' cell order co = iy * nm + im, tiles of kCdfTile cells):
+//   k_fold_tiles     cs[co] = sigma(m) L (calcNucCrossSectionYM,
+//                    src/UpcCrossSection.cpp:594-698; the polarized ratio),
+//                    and each tile's sum of cs;
+//   k_cdf_top_total  exclusive offsets of the tile sums, the total (sigma_tot
+//                    = total * scale) and 1 / total;
+//   k_cdf_write_fx   cdf[i + 1] = (w_0 + ... + w_i) / total per tile from its
+//                    offset, with the fixed-point copy of every entry.
+// The CDF is gsl_histogram2d_pdf_init's, (w_i / mean) / n summed, up to the
+// rounding of the normalisation: the sum is taken first and scaled once.
+__global__ void __launch_bounds__(kCdfThreads) k_fold_tiles(FoldParams f,
+                                                           const double* __restrict__ lumi,
+                                                           const double* __restrict__ lumi2,
+                                                           const double* __restrict__ csm,
+                                                           double* __restrict__ cs,
+                                                           double* __restrict__ ratio,
+                                                           double* __restrict__ part) {
+  __shared__ double red[kCdfThreads / 32];
+  const int64_t n = (int64_t)f.nm * f.ny;
+  const int64_t base = (int64_t)blockIdx.x * kCdfTile;
+  double loc = 0.;
+#pragma unroll
+  for (int k = 0; k < kCdfItems; ++k) {
+    const int64_t co = base + (int64_t)k * kCdfThreads + threadIdx.x;
+    if (co < n) {
+      const int iy = (int)(co / f.nm), im = (int)(co - (int64_t)iy * f.nm);
+      const size_t i = (size_t)im * f.ny + iy;
+      double v;
+      if (!f.polarized) {
+        v = __ldg(csm + im) * lumi[i];
+      } else {
+        const double sc = lumi[i] * __ldg(csm + im);
+        const double ps = lumi2[i] * __ldg(csm + f.nm + im);
+        v = (sc + ps) * 1e7;
+        ratio[co] = sc / ps;
+      }
+      cs[co] = v;
+      loc += v;
+    }
+  }
+  const double sum = block_sum(loc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = sum;
+}
+
+__global__ void __launch_bounds__(1024) k_cdf_top_total(double* __restrict__ part, int ntiles,
+                                                        double scale, double* __restrict__ tot,
+                                                        double* __restrict__ inv) {
+  __shared__ double sh[1024];
+  const int t = threadIdx.x;
+  const int per = (ntiles + 1023) / 1024;
+  const int lo = t * per, hi = lo + per < ntiles ? lo + per : ntiles;
+  double loc = 0.;
+  for (int i = lo; i < hi; ++i) loc += part[i];
+  sh[t] = loc;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
+    const double add = t >= off ? sh[t - off] : 0.;
+    __syncthreads();
+    sh[t] += add;
+    __syncthreads();
+  }
+  if (t == 0) {
+    *tot = sh[1023] * scale;
+    *inv = 1. / sh[1023];
+  }
+  double run = t > 0 ? sh[t - 1] : 0.;
+  for (int i = lo; i < hi; ++i) {
+    const double v = part[i];
+    part[i] = run;
+    run += v;
+  }
+}
+
+__global__ void __launch_bounds__(kCdfThreads) k_cdf_write_fx(const double* __restrict__ w,
+                                                             int64_t n,
+                                                             const double* __restrict__ inv_p,
+                                                             const double* __restrict__ off,
+                                                             double* __restrict__ cdf,
+                                                             uint64_t* __restrict__ cdffx) {
+  __shared__ double sh[kCdfThreads];
+  const int t = threadIdx.x;
+  const int64_t base = (int64_t)blockIdx.x * kCdfTile + (int64_t)t * kCdfItems;
+  const double inv = *inv_p;
+  double v[kCdfItems];
+  double loc = 0.;
+#pragma unroll
+  for (int k = 0; k < kCdfItems; ++k) {
+    const int64_t i = base + k;
+    v[k] = i < n ? w[i] : 0.;
+    loc += v[k];
+  }
+  sh[t] = loc;
+  __syncthreads();
+  for (int o = 1; o < kCdfThreads; o <<= 1) {
+    const double add = t >= o ? sh[t - o] : 0.;
+    __syncthreads();
+    sh[t] += add;
+    __syncthreads();
+  }
+  double run = off[blockIdx.x] + (t > 0 ? sh[t - 1] : 0.);
+  if (blockIdx.x == 0 && t == 0) {
+    cdf[0] = 0.;
+    cdffx[0] = 0ull;
+  }
+#pragma unroll
+  for (int k = 0; k < kCdfItems; ++k) {
+    const int64_t i = base + k;
+    run += v[k];
+    if (i < n) {
+      const double c = run * inv;
+      cdf[i + 1] = c;
+      cdffx[i + 1] = cdf_to_fx(c);
+    }
   }
 }
 
@@ -297,22 +382,25 @@ cudaError_t launch_cs_m_points(const FoldParams& f, const double* d_m, double* d
   return cudaGetLastError();
 }
 
-int fold_partial_doubles(int nm, int ny) {
-  return ((int64_t)nm * ny + kFoldThreads - 1) / kFoldThreads + 1 + 2 * nm;
+cudaError_t launch_cs_m_rows(const FoldParams& f, double* d_csm, cudaStream_t st) {
+  note_launch();
+  k_cs_m_rows<<<(f.nm + 127) / 128, 128, 0, st>>>(f, d_csm);
+  return cudaGetLastError();
 }
 
-cudaError_t launch_fold(const FoldParams& f, const double* d_lumi, const double* d_lumi2,
-                        double* d_cs, double* d_ratio, double* d_partial, double* d_tot,
-                        cudaStream_t st) {
-  const int n = f.nm * f.ny;
-  const int blocks = (n + kFoldThreads - 1) / kFoldThreads;
-  double* csm = d_partial + blocks + 1;  // fold_partial_doubles: the blocks' sums, then sigma(m)
+cudaError_t launch_fold_cdf(const FoldParams& f, const double* d_lumi, const double* d_lumi2,
+                            const double* d_csm, double* d_cs, double* d_ratio, double* d_scratch,
+                            double* d_tot, double* d_cdf, uint64_t* d_cdffx, cudaStream_t st) {
+  const int64_t n = (int64_t)f.nm * f.ny;
+  const int ntiles = (int)((n + kCdfTile - 1) / kCdfTile);
+  double* part = d_scratch;  // cdf_2d_scratch_doubles(n): tile sums | 1 / total
+  double* inv = d_scratch + ntiles + 1;
   note_launch();
-  k_cs_m_rows<<<(f.nm + 127) / 128, 128, 0, st>>>(f, csm);
+  k_fold_tiles<<<ntiles, kCdfThreads, 0, st>>>(f, d_lumi, d_lumi2, d_csm, d_cs, d_ratio, part);
   note_launch();
-  k_fold<<<blocks, kFoldThreads, 0, st>>>(f, d_lumi, d_lumi2, csm, d_cs, d_ratio, d_partial);
+  k_cdf_top_total<<<1, 1024, 0, st>>>(part, ntiles, 1e-6, d_tot, inv);
   note_launch();
-  k_reduce_total<<<1, 1024, 0, st>>>(d_partial, blocks, 1e-6, d_tot);
+  k_cdf_write_fx<<<ntiles, kCdfThreads, 0, st>>>(d_cs, n, inv, part, d_cdf, d_cdffx);
   return cudaGetLastError();
 }
 
@@ -340,8 +428,8 @@ cudaError_t launch_cdf_2d(const double* d_w, int64_t n, double* d_cdf, double* d
 cudaError_t launch_cdf_rows(const double* d_w, int rows, int len, double* d_cdf,
                             cudaStream_t st) {
   note_launch();
-  // one thread per row, FP64-bound: 32-thread blocks spread the rows over the SMs
-  k_cdf_rows<<<(rows + 31) / 32, 32, 0, st>>>(d_w, rows, len, d_cdf);
+  // one warp per row, four rows per block
+  k_cdf_rows<<<(rows + 3) / 4, 128, 0, st>>>(d_w, rows, len, d_cdf);
   return cudaGetLastError();
 }
 

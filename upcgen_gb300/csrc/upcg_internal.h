@@ -2,6 +2,9 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <utility>
+#include <vector>
 #include <stdint.h>
 
 #include <atomic>
@@ -93,15 +96,19 @@ cudaError_t launch_grid_cells(const LumiParams& p, const GridForm& gf, const flo
                               const double* rowsum, const double* tail, double* lumi,
                               cudaStream_t st);
 
-// tables
+// tables; d_coef32 (optional): an FP32 copy of the coefficients, (float) of each
 cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
-                                 double4* d_coef, cudaStream_t st);
+                                 double4* d_coef, cudaStream_t st, float4* d_coef32 = nullptr);
 cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, double rho0,
                                   double R, double a, cudaStream_t st);
 // G_AA spline (199 intervals into d_coef); d_ta_coef: 199 intervals of the
 // T_A spline; d_work: 800 doubles of scratch
+// d_coef32: FP32 copy of the G_AA coefficients; d_ta32 (199 float4): the fast
+// form's variant -- T_A and G_AA integrands in FP32 (sums in FP64), the T_A
+// spline's FP32 copy written there
 cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaConsts& k,
-                       double4* d_coef, double4* d_ta_coef, double* d_work, cudaStream_t st);
+                       double4* d_coef, double4* d_ta_coef, double* d_work, cudaStream_t st,
+                       float4* d_coef32 = nullptr, float4* d_ta32 = nullptr);
 // calcBreakupProb's energy / cross-section table (host); returns its length
 int breakup_energy_table(double gammatarg, double* ee, double* se);
 // d_tab = [ee | se | ln ee | 1/ee], each kBreakupTabMax long, nt entries used
@@ -146,9 +153,14 @@ cudaError_t launch_formfac_points(const double* d_q2, double* d_out, int n, doub
 // fast form (tensor-core contraction), upcg_fast.cu
 int fast_grid_points();
 // d_gaa32 / d_brk32: FP32 copies of the G_AA and breakup splines' intervals
+// convert = 0: the FP32 coefficient copies d_gaa32 / d_brk32 are already
+// written (build_spline_uniform's coef32); far_out: P(20 fm) and the far
+// constant computed by the kernel itself into far_out[0..1] (k_far_consts
+// skipped), and *err0 reset to 0
 cudaError_t launch_fast_G(const LumiParams& p, double u0, double h, int P, double P20,
                           float4* d_gaa32, float4* d_brk32, void* gh, void* gl, cudaStream_t st,
-                          const double* P20d = nullptr);
+                          const double* P20d = nullptr, int convert = 1, double* far_out = nullptr,
+                          unsigned* err0 = nullptr, int delta = 0);
 // P(20 fm) and the survival kernel beyond 20 fm into d_out[0..1]
 cudaError_t launch_far_consts(const LumiParams& p, int has_brk, double* d_out, cudaStream_t st);
 // Flux tables of the fast form: scaled K0/K1 on ln x, and Q(w, b) of the
@@ -166,11 +178,13 @@ int flux_table_ktab_n();
 void flux_table_ktab_range(double* u0, double* u1);
 // d_part: flux_table_part_doubles(nw, nb) doubles of split-K scratch
 int flux_table_part_doubles(int nw, int nb);
-// point-flux table, and the Q(w, b) rows [w_lo, nw) by the Hankel quadrature
+// point-flux table, and the Q(w, b) rows [w_lo, nw) by the Hankel quadrature;
+// js: a stream for the Bessel part J (with d_qn written in its order), whose
+// completion ev_j is recorded there and joined into st before the rest
 cudaError_t build_flux_tables(const LumiParams& p, FastFluxTables* t, double* d_qn, double* d_wn,
                               int nq, double* d_H, double* d_J, double* d_part, cudaStream_t st,
-                              int w_lo = 0,
-                              int with_ktab = 1);
+                              int w_lo = 0, int with_ktab = 1, cudaStream_t js = nullptr,
+                              cudaEvent_t ev_j = nullptr);
 // the point-flux table S(ln x) of the fast form alone; with d_lk (2 * N
 // doubles, flux_table_ktab_n() points) from cached Bessel logs, computed
 // there first unless lk_ready
@@ -204,6 +218,10 @@ cudaError_t launch_contract_fused(const void* gh, const void* gl, int nconf, int
                                   const void* items, int nitems, const float* nodes,
                                   float* partial, unsigned* d_err, int shape, int grid,
                                   cudaStream_t st, int kt0 = 0);
+// the persistent contractions' work list for grid CTAs (CTA b: items b,
+// b + grid, ...), each round's items rotated by its index so that every CTA
+// meets every N tile (items of unequal K ranges); in place
+void rotate_rounds(std::vector<int4>& items, int grid);
 cudaError_t launch_fill_nodes_synthetic(float* nodes, int rows, cudaStream_t st);
 // bytes of the per-(cell, photon) constants (d_sides holds 2 per cell)
 size_t fast_side_bytes();
@@ -239,11 +257,21 @@ int contract_item_bytes();
 cudaError_t launch_contract(const void* ah, const void* al, const void* gh, const void* gl,
                             const float* a2, int ncells_pad, int ncells, int P, float* partial,
                             unsigned* d_err, cudaStream_t st);
+// delta: the contraction's survival kernel was G - c (launch_fast_G's delta)
 cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int ntiles,
                                double c_far, const float* partial, const void* side_part,
                                double* lumi, cudaStream_t st, const double* c_far_d = nullptr,
                                const int* rep_y = nullptr, const int* rep_mir = nullptr,
-                               int n_rep_y = 0, int m0 = 0);
+                               int n_rep_y = 0, int m0 = 0, int delta = 0);
+// The K-tile range [lo, hi) of each N tile (tbn columns) where the delta
+// survival kernel G - c on the radial grid r_i = exp(u0 + i h), i < P, can be
+// nonzero for the azimuths cosk (a superset: b^2 < 400 (1 + 1e-3) somewhere
+// in the tile pair); out[nt] = (lo, hi), hi = lo when none.  Packed into the
+// items' bits 8-23 by pack_item.
+void delta_tile_ranges(int P, double u0, double h, const double* cosk, int ncos, int tbn, int bk,
+                       std::vector<std::pair<int, int>>& out);
+inline int pack_item(int rows, int klo, int khi) { return rows | (klo << 8) | (khi << 16); }
+constexpr int kContractBK = 64;  // K tile of the contraction kernels
 cudaError_t contract_selftest(int ncells, int P, uint64_t seed, double* max_rel, double* ms);
 
 // fold + samplers
@@ -254,11 +282,14 @@ struct FoldParams {
   double mPart, aLep, alpWidth;
 };
 cudaError_t launch_cs_zm(const FoldParams& f, int flag, double* d_out, cudaStream_t st);
-// doubles of launch_fold's d_partial: the per-block sums, then sigma(m) per row
-int fold_partial_doubles(int nm, int ny);
-cudaError_t launch_fold(const FoldParams& f, const double* d_lumi, const double* d_lumi2,
-                        double* d_cs, double* d_ratio, double* d_partial, double* d_tot,
-                        cudaStream_t st);
+// sigma(m) per m-row (both polarized parts, [nm] each, when polarized)
+cudaError_t launch_cs_m_rows(const FoldParams& f, double* d_csm, cudaStream_t st);
+// the fold with sigma(m) from launch_cs_m_rows, sigma_tot into d_tot, and the
+// (m, y) sampling CDF (FP64 and fixed point, n + 1 entries each) in three
+// launches; d_scratch: cdf_2d_scratch_doubles(nm * ny)
+cudaError_t launch_fold_cdf(const FoldParams& f, const double* d_lumi, const double* d_lumi2,
+                            const double* d_csm, double* d_cs, double* d_ratio, double* d_scratch,
+                            double* d_tot, double* d_cdf, uint64_t* d_cdffx, cudaStream_t st);
 cudaError_t launch_cs_m_points(const FoldParams& f, const double* d_m, double* d_out, int n,
                                int flag, cudaStream_t st);
 int cdf_2d_scratch_doubles(int64_t n);
@@ -323,6 +354,9 @@ struct EventParams {
 };
 // guide tables (EventParams) of the built CDFs; d_g2 / d_gz / d_gpt sized
 // g2_n, nm * gz_n, pt_ne * gpt_n
+// the (m, y) guide table from the fixed-point CDF that launch_fold_cdf wrote
+cudaError_t launch_guide2_fx(const EventParams& e, const uint64_t* d_cdf2fx, int* d_g2,
+                             cudaStream_t st);
 cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                           const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
                           cudaStream_t st, uint64_t* d_cdf2fx = nullptr,

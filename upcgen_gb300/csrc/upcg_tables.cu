@@ -74,13 +74,14 @@ __global__ void __launch_bounds__(kSplThreads) k_spline_c(const double* __restri
 // is the uniform h; 1/h and h/3 from the host)
 __global__ void k_spline_coef(const double* __restrict__ y, const double* __restrict__ c, int n,
                               double inv_h, double h3, double inv_3h,
-                              double4* __restrict__ coef) {
+                              double4* __restrict__ coef, float4* __restrict__ coef32) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
   const double dy = y[i + 1] - y[i];
   const double b = dy * inv_h - h3 * (c[i + 1] + 2.0 * c[i]);
   const double d = (c[i + 1] - c[i]) * inv_3h;
   coef[i] = make_double4(y[i], b, c[i], d);
+  if (coef32) coef32[i] = make_float4((float)y[i], (float)b, (float)c[i], (float)d);
 }
 
 // calcFormFac (src/UpcCrossSection.cpp:436-445) on Q2 = Q2min + i*dQ2.
@@ -146,6 +147,69 @@ __global__ void __launch_bounds__(256) k_gaa_rows(const double4* __restrict__ ta
     for (int i = 1; i < nb - 1; i += 2) sum += 4. * vs[i];
     for (int i = 2; i < nb - 1; i += 2) sum += 2. * vs[i];
     gaa_y[ib] = exp(-csNN * (sum * db / 3.));
+  }
+}
+
+// The fast form's T_A and G_AA: the nodes, Simpson weights and order of the
+// sums of k_ta_values / k_gaa_rows, with the integrands in FP32 and the sums
+// in FP64.  The fast form reads only an FP32 copy of the G_AA spline, and
+// FP64 is the scarce unit while the table chains run side by side (GB300
+// issues FP32 at 64x its FP64 rate); G_AA moves by ~1e-6 (the sums' terms
+// carry FP32's 6e-8).
+__global__ void __launch_bounds__(256) k_ta_values_f(float rho0, float R, float a,
+                                                     double* __restrict__ ta_y) {
+  constexpr int nb = 200;
+  __shared__ double v[nb];
+  const float db = 20.f / (nb - 1);
+  const float b = blockIdx.x * db;
+  const int iz = threadIdx.x;
+  if (iz < nb) {
+    const float z = iz * db, r = sqrtf(b * b + z * z);
+    v[iz] = (double)(rho0 / (1.f + expf((r - R) / a)));
+  }
+  __syncthreads();
+  if (iz == 0) {
+    const double dbd = 20. / (nb - 1);
+    double sum = v[0] + v[nb - 1];
+    for (int i = 1; i < nb - 1; i += 2) sum += 4. * v[i];
+    for (int i = 2; i < nb - 1; i += 2) sum += 2. * v[i];
+    ta_y[blockIdx.x] = 2. * (sum * dbd / 3.);
+  }
+}
+
+__device__ __forceinline__ float eval_uf(const float4* coef, int n, float h, float x) {
+  const SplineF s{coef, 0.f, h, 1.f / h, n};
+  return spline_eval_f(s, coef, x);
+}
+
+__global__ void __launch_bounds__(256) k_gaa_rows_f(const float4* __restrict__ ta_coef,
+                                                    double csNN, GaaConsts k,
+                                                    double* __restrict__ gaa_y) {
+  constexpr int nb = 200;
+  __shared__ float4 sTAc[nb - 1];
+  __shared__ double vs[nb];
+  const float bmax = 20.f;
+  const float db = bmax / (nb - 1);
+  for (int i = threadIdx.x; i < nb - 1; i += blockDim.x) sTAc[i] = ta_coef[i];
+  __syncthreads();
+  const int ib = blockIdx.x, is = threadIdx.x;
+  const float b = ib * db;
+  if (is < nb) {
+    const float s = is * db;
+    float sum_phi = 0.f;
+    for (int q = 0; q < 5; ++q) {
+      const float r = sqrtf(b * b + s * s + 2.f * b * s * (float)k.cosk[q]);
+      sum_phi += 2.f * (float)kPi * (float)k.wk[q] * eval_uf(sTAc, nb, db, r < bmax ? r : bmax);
+    }
+    vs[is] = (double)(2.f * s * eval_uf(sTAc, nb, db, s < bmax ? s : bmax) * sum_phi);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // Simpson weights in the reference's order
+    const double dbd = 20. / (nb - 1);
+    double sum = vs[0] + vs[nb - 1];
+    for (int i = 1; i < nb - 1; i += 2) sum += 4. * vs[i];
+    for (int i = 2; i < nb - 1; i += 2) sum += 2. * vs[i];
+    gaa_y[ib] = exp(-csNN * (sum * dbd / 3.));
   }
 }
 
@@ -493,7 +557,7 @@ __global__ void k_coef_f32(const double4* __restrict__ in, float4* __restrict__ 
 }
 
 cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
-                                 double4* d_coef, cudaStream_t st) {
+                                 double4* d_coef, cudaStream_t st, float4* d_coef32) {
   (void)x0;
   if (n < 2 * kSplHalf + 4) return cudaErrorInvalidValue;  // the two end images must not meet
   static SplKernel G = [] {
@@ -511,7 +575,7 @@ cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, 
                                                                          d_c);
   note_launch();
   k_spline_coef<<<(n - 1 + 255) / 256, 256, 0, st>>>(d_y, d_c, n, 1. / h, h / 3., 1. / (3. * h),
-                                                     d_coef);
+                                                     d_coef, d_coef32);
   return cudaGetLastError();
 }
 
@@ -523,7 +587,8 @@ cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, dou
 }
 
 cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaConsts& k,
-                       double4* d_coef, double4* d_ta_coef, double* d_work, cudaStream_t st) {
+                       double4* d_coef, double4* d_ta_coef, double* d_work, cudaStream_t st,
+                       float4* d_coef32, float4* d_ta32) {
   // d_work: T_A values | T_A spline scratch | G_AA values | G_AA spline scratch (200 each)
   constexpr int nb = 200;
   const double db = 20. / (nb - 1);
@@ -532,12 +597,18 @@ cudaError_t launch_gaa(double rho0, double R, double a, double csNN, const GaaCo
   double* g_y = d_work + 2 * nb;
   double* g_c = d_work + 3 * nb;
   note_launch();
-  k_ta_values<<<nb, 256, 0, st>>>(rho0, R, a, ta_y);
-  cudaError_t e = build_spline_uniform(ta_y, nb, 0., db, ta_c, d_ta_coef, st);
+  if (d_ta32)
+    k_ta_values_f<<<nb, 256, 0, st>>>((float)rho0, (float)R, (float)a, ta_y);
+  else
+    k_ta_values<<<nb, 256, 0, st>>>(rho0, R, a, ta_y);
+  cudaError_t e = build_spline_uniform(ta_y, nb, 0., db, ta_c, d_ta_coef, st, d_ta32);
   if (e != cudaSuccess) return e;
   note_launch();
-  k_gaa_rows<<<nb, 256, 0, st>>>(d_ta_coef, csNN, k, g_y);
-  return build_spline_uniform(g_y, nb, 0., db, g_c, d_coef, st);
+  if (d_ta32)
+    k_gaa_rows_f<<<nb, 256, 0, st>>>(d_ta32, csNN, k, g_y);
+  else
+    k_gaa_rows<<<nb, 256, 0, st>>>(d_ta_coef, csNN, k, g_y);
+  return build_spline_uniform(g_y, nb, 0., db, g_c, d_coef, st, d_coef32);
 }
 
 cudaError_t launch_breakup_values(const double* d_tab, int nt, double gammatarg, double omaxx,
