@@ -567,10 +567,11 @@ def main():
     P = FAST_GRID_P
     # the contraction's rows: one cell of each mirror-rapidity pair (the other
     # is a copy); one launch covers up to 2^18 rows
-    rows = fast.contractRows()
-    rows_pad = (rows + 127) // 128 * 128
+    rows, macs_row = fast.contractWork()
     nlaunch_contract = max(1, -(-rows // 262144))
-    alg_flops = 2.0 * rows_pad * P * P  # A1 (rows x P) . G (P x P), per table
+    # A1 (rows x P) times G - c over the tiles where it can be nonzero, per
+    # table (the constant's share, c S0 S1, is a per-cell FP64 product)
+    alg_flops = 2.0 * rows * macs_row
     achieved = alg_flops / (ms_contract * 1e-3) / 1e12
     peak = pk_vals.get("bf16_tflops", 1900.0)
     traffic = CONTRACT_DRAM_BYTES_PER_ROW * rows / nlaunch_contract
@@ -598,9 +599,11 @@ def main():
                      "bound": "tensor",
                      "achieved": achieved / nlaunch_contract * nlaunch_contract, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-                     "note": f"algorithmic 2*rows*P^2 = {alg_flops:.3e} FLOP per table over "
+                     "note": f"algorithmic 2*rows*MACs = {alg_flops:.3e} FLOP per table over "
                              f"{nlaunch_contract} launch(es), rows = {rows} computed cells (one of "
-                             f"each mirror-rapidity pair; the hi/lo split issues it 3x); "
+                             f"each mirror-rapidity pair), {macs_row} multiply-adds per row (the "
+                             f"nonzero tiles of G - c: {macs_row / P / P:.3f} of the dense "
+                             f"P x P; the hi/lo split issues them 3x); "
                              f"peak = {pk_kind} bf16 burst; traffic = DRAM bytes per launch "
                              f"from an ncu capture, scaled by rows"},
         "roofline_weights": {

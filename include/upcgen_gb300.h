@@ -378,6 +378,13 @@ int upcg_copy_bytes(uint64_t* h2d, uint64_t* d2h);
  * one of each pair of mirror rapidities (L(m, -y) = L(m, y), copied to the
  * other); 0 when the last luminosity was not the fast form */
 int upcg_contract_rows(const upcg_generator* g, int64_t* rows);
+/* The same rows and the multiply-adds per row that the last fast-form
+ * contraction needed: A1 (rows x P) times the survival kernel minus its
+ * constant, over the tiles where that can be nonzero (the constant's share
+ * is added per cell in FP64); 0 when the last luminosity was not the fast
+ * form.  The tensor cores issue each multiply-add three times (hi.hi +
+ * hi.lo + lo.hi). */
+int upcg_contract_work(const upcg_generator* g, int64_t* rows, int64_t* macs_per_row);
 const char* upcg_last_error(void);
 const char* upcg_version(void);
 

@@ -29,7 +29,7 @@ ABI_SYMBOLS = [
     "upcg_set_debug_level", "upcg_set_lumi_file_directory", "upcg_set_lumi_cache", "upcg_lumi_cache_file",
     "upcg_particles_per_event", "upcg_event_particles_device", "upcg_format_hepmc3",
     "upcg_write_events", "upcg_run_events", "upcg_sampler_bins", "upcg_photon_flux", "upcg_vm_cross_section_y", "upcg_nuc_cs_y",
-    "upcg_decay_pdg", "upcg_contract_rows",
+    "upcg_decay_pdg", "upcg_contract_rows", "upcg_contract_work",
     "upcg_set_stream", "upcg_set_lumi_method", "upcg_init", "upcg_compute_nucl_xsection",
     "upcg_tot_nucl_x", "upcg_fid_nucl_x", "upcg_get_grid", "upcg_lumi_table",
     "upcg_lumi_table_device", "upcg_nuc_cs_ym", "upcg_cs_zm_table", "upcg_flux_point",
@@ -85,6 +85,7 @@ def load_library(path=None):
         "upcg_photon_flux": [vp, vp, vp, vp, sz], "upcg_vm_cross_section_y": [vp, vp, vp, sz],
         "upcg_nuc_cs_y": [vp, vp, vp, sz, dp], "upcg_decay_pdg": [vp, C.POINTER(i)],
         "upcg_contract_rows": [vp, C.POINTER(i64)],
+        "upcg_contract_work": [vp, C.POINTER(i64), C.POINTER(i64)],
         "upcg_set_stream": [vp, vp], "upcg_set_lumi_method": [vp, i], "upcg_init": [vp],
         "upcg_compute_nucl_xsection": [vp], "upcg_tot_nucl_x": [vp, dp],
         "upcg_fid_nucl_x": [vp, dp],
@@ -605,6 +606,13 @@ class UpcGenerator:
         n = C.c_int64()
         _check(self._L.upcg_contract_rows(self._h, C.byref(n)))
         return n.value
+
+    def contractWork(self):
+        """(rows, multiply-adds per row) of the last fast-form contraction: the
+        tiles where the survival kernel minus its constant can be nonzero."""
+        n, m = C.c_int64(), C.c_int64()
+        _check(self._L.upcg_contract_work(self._h, C.byref(n), C.byref(m)))
+        return n.value, m.value
 
     def decayPDG(self):
         n = C.c_int()

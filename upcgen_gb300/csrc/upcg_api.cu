@@ -321,6 +321,8 @@ struct upcg_generator {
   bool medges_ok = false;
   double mbinlut_key[2] = {0., 0.};
   int64_t contract_rows = 0;  // rows of the last fast-form contraction
+  // multiply-adds per row of its A1 . (G - c) product over the nonzero tiles
+  int64_t contract_macs_row = 0;
   int fast_nrep = 0;          // rapidity bins per m-row the fast form computes (frep), 0: all  // bu_tab: ee | se | ln ee | 1/ee (kBreakupTabMax each)
   std::vector<double> bu_host;
   int bu_nt = 0;
@@ -1479,6 +1481,11 @@ int upcg_generator::build_lumi() {
                                                          kr[nt].first, kr[nt].second)));
       // the radial columns below the first node stencil are zero in every row
       const int kt0 = fast_first_ktile(isPoint ? R : 0.05 * R, fu0, fh);
+      contract_macs_row = 0;
+      for (int nt = 0; nt < P / tbn; ++nt) {
+        const int lo = std::max(kt0, kr[nt].first), hi = std::min(P / kContractBK, kr[nt].second);
+        if (hi > lo) contract_macs_row += (int64_t)(hi - lo) * kContractBK * tbn;
+      }
       // items of unequal work: every CTA meets every N tile
       grid = std::min(grid, (int)items.size());
       rotate_rounds(items, grid);
@@ -1689,14 +1696,17 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_read
   const EventParams e = event_params();
   CK(ptcdf.ensure((size_t)e.pt_ne * (e.pt_nbins + 1)));
   CK(ff32.ensure(ff_n));
-  if (ff_ready) CK(cudaStreamWaitEvent(ss, ff_ready, 0));  // the pT spectra read the form factor
-  CK(launch_photon_pt_tables(e, lumi_params().ff, ff32.p, ptcdf.p, ss));
   CK(guidez.ensure((size_t)nm * e.gz_n));
   CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
   CK(cdfzfx.ensure((size_t)nm * (nz + 1)));
   const EventParams eg = event_params();  // with the guide buffers allocated
-  CK(launch_guides(eg, nullptr, cdfz.p, ptcdf.p, nullptr, guidez.p, guidept.p, ss, nullptr,
-                   cdfzfx.p));
+  if (ff_ready) CK(cudaStreamWaitEvent(ss, ff_ready, 0));  // the pT spectra read the form factor
+  // the pT guide tables (photon pT drawn: NON_ZERO_GAM_PT, vector mesons)
+  // come from the spectra's own kernel
+  const bool pt_guides = eg.useNonzeroGamPt || eg.vm;
+  CK(launch_photon_pt_tables(eg, lumi_params().ff, ff32.p, ptcdf.p, ss,
+                             pt_guides ? guidept.p : nullptr));
+  CK(launch_guides(eg, nullptr, cdfz.p, nullptr, guidez.p, ss, nullptr, cdfzfx.p));
   return UPCG_OK;
 }
 
@@ -1750,8 +1760,7 @@ int upcg_generator::build_xsec() {
     CK(guide2.ensure(e.g2_n));
     const EventParams eg = event_params();  // with the guide buffer allocated
     if (isVM)
-      CK(launch_guides(eg, cdf2.p, nullptr, nullptr, guide2.p, nullptr, nullptr, s, cdf2fx.p,
-                       nullptr));
+      CK(launch_guides(eg, cdf2.p, nullptr, guide2.p, nullptr, s, cdf2fx.p, nullptr));
     else
       CK(launch_guide2_fx(eg, cdf2fx.p, guide2.p, s));
   }
@@ -2657,6 +2666,13 @@ int upcg_particle_pdg(upcg_generator* g, int* pdg, int* charged) {
 int upcg_contract_rows(const upcg_generator* g, int64_t* rows) {
   if (!g || !rows) return fail(UPCG_ERR_ARG, "null argument");
   *rows = g->contract_rows;
+  return UPCG_OK;
+}
+
+int upcg_contract_work(const upcg_generator* g, int64_t* rows, int64_t* macs_per_row) {
+  if (!g || !rows || !macs_per_row) return fail(UPCG_ERR_ARG, "null argument");
+  *rows = g->contract_rows;
+  *macs_per_row = g->contract_rows ? g->contract_macs_row : 0;
   return UPCG_OK;
 }
 

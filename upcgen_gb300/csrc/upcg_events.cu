@@ -642,7 +642,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* __restri
 // [0, 6 hc / R] (content at the upper bin edge), for e = k^2/gtot^2 on a log
 // grid.  FP32 throughout (the tables are FP32), from an FP32 copy of the
 // form-factor spline.
-__global__ void k_pt_tables(EventParams e, SplineF ff, float* __restrict__ out) {
+__global__ void k_pt_tables(EventParams e, SplineF ff, float* __restrict__ out,
+                            uint16_t* __restrict__ guide) {
   extern __shared__ float sdf[];
   const int ie = blockIdx.x;
   const float ered = expf((float)e.pt_lne0 + (float)e.pt_dlne * ie);
@@ -691,7 +692,43 @@ __global__ void k_pt_tables(EventParams e, SplineF ff, float* __restrict__ out) 
   const float inv_tot = 1.f / sdf[nb - 1];
   float* o = out + (size_t)ie * (nb + 1);
   if (threadIdx.x == 0) o[0] = 0.f;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) o[b + 1] = sdf[b] * inv_tot;
+  __syncthreads();  // every thread has read sdf[nb - 1]
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const float c = sdf[b] * inv_tot;
+    o[b + 1] = c;
+    sdf[b] = c;
+  }
+  if (!guide) return;
+  // the row's guide table: entry j = the bin of u = j / K in the CDF
+  // {0, sdf[0], ..., sdf[len - 2]} (cdf_find_f's answer: the largest k < len
+  // with cdf[k] <= u, or 0), from shared memory.  Each thread takes a run of
+  // consecutive points: a binary search for the first, then a forward walk
+  // of at most 8 bins per point, finished by a binary search above the
+  // walk's bin where the CDF is flat (its tail); the CDF is nondecreasing
+  // (a running sum of non-negative terms), so each step keeps the answer.
+  __syncthreads();
+  const int K = e.gpt_n, len = nb;
+  auto cdf_at = [&](int k) { return k == 0 ? 0.f : sdf[k - 1]; };
+  uint16_t* g = guide + (size_t)ie * K;
+  const int per = (K + blockDim.x - 1) / blockDim.x;
+  const int j0 = threadIdx.x * per, j1 = min(K, j0 + per);
+  int lo = 0;
+  for (int j = j0; j < j1; ++j) {
+    const float u = (float)j / (float)K;
+    int steps = 0;
+    while (steps < 8 && lo + 1 < len && u >= cdf_at(lo + 1)) {
+      ++lo;
+      ++steps;
+    }
+    if (lo + 1 < len && u >= cdf_at(lo + 1)) {  // cdf[lo] <= u still holds
+      int hi = len;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (u >= cdf_at(mid)) lo = mid; else hi = mid;
+      }
+    }
+    g[j] = (uint16_t)lo;
+  }
 }
 
 // Guide tables: bucket j of K starts at the answer of the plain search for
@@ -720,36 +757,6 @@ __global__ void k_guide_rows_fx(const uint64_t* __restrict__ cdf, int rows, int 
   const int r = (int)(t >> bits);
   const uint64_t j = (uint64_t)(t - ((int64_t)r << bits));
   guide[t] = cdf_find_fx(cdf + (size_t)r * (len + 1), len, j << (64 - bits));
-}
-
-__global__ void k_guide_rows_f(const float* __restrict__ cdf, int rows, int len, int K,
-                               uint16_t* __restrict__ guide) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)rows * K) return;
-  const int r = (int)(t / K), j = (int)(t - (int64_t)r * K);
-  guide[t] = (uint16_t)cdf_find_f(cdf + (size_t)r * (len + 1), len, (float)j / (float)K);
-}
-
-// The same guide entries, one CTA per row: the row's CDF entries [0, len) --
-// all that cdf_find_f reads -- staged in shared memory, then the same binary
-// search for each of the K points (the global-memory form's searches are
-// chains of dependent L2 reads).
-__global__ void __launch_bounds__(256) k_guide_rows_fs(const float* __restrict__ cdf, int len,
-                                                       int K, uint16_t* __restrict__ guide) {
-  extern __shared__ float sc[];
-  const float* src = cdf + (size_t)blockIdx.x * (len + 1);
-  for (int i = threadIdx.x; i < len; i += blockDim.x) sc[i] = src[i];
-  __syncthreads();
-  uint16_t* g = guide + (size_t)blockIdx.x * K;
-  for (int j = threadIdx.x; j < K; j += blockDim.x) {
-    const float u = (float)j / (float)K;
-    int lo = 0, hi = len;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (u >= sc[mid]) lo = mid; else hi = mid;
-    }
-    g[j] = (uint16_t)lo;
-  }
 }
 
 // Every candidate of [cand0, cand0 + n) with its accept flag (single-event API).
@@ -812,9 +819,8 @@ cudaError_t launch_guide2_fx(const EventParams& e, const uint64_t* d_cdf2fx, int
 }
 
 cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
-                          const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
-                          cudaStream_t st, uint64_t* d_cdf2fx, uint64_t* d_cdfzfx) {
-  if (e.pt_nbins > 65535) return cudaErrorInvalidValue;
+                          int* d_g2, int* d_gz, cudaStream_t st, uint64_t* d_cdf2fx,
+                          uint64_t* d_cdfzfx) {
   if (e.g2_n != (1 << e.g2_bits) || e.gz_n != (1 << e.gz_bits)) return cudaErrorInvalidValue;
   // each guide set is built when its buffer is given (null: skipped), with
   // the fixed-point copy of its CDF
@@ -836,29 +842,19 @@ cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const doub
     k_guide_rows_fx<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(d_cdfzfx, e.nm, e.nz, e.gz_bits,
                                                                   d_gz);
   }
-  if (d_gpt && (e.useNonzeroGamPt || e.vm)) {  // vector mesons always draw a photon pT
-    const size_t smem = sizeof(float) * (size_t)e.pt_nbins;
-    note_launch();
-    if (smem <= 48 * 1024) {
-      k_guide_rows_fs<<<e.pt_ne, 256, smem, st>>>(d_ptcdf, e.pt_nbins, e.gpt_n, d_gpt);
-    } else {
-      const int64_t np = (int64_t)e.pt_ne * e.gpt_n;
-      k_guide_rows_f<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(d_ptcdf, e.pt_ne, e.pt_nbins,
-                                                                   e.gpt_n, d_gpt);
-    }
-  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, float4* d_ff32,
-                                    float* d_cdf, cudaStream_t st) {
+                                    float* d_cdf, cudaStream_t st, uint16_t* d_gpt) {
   const size_t smem = sizeof(float) * e.pt_nbins;
   if (smem > 48 * 1024) return cudaErrorInvalidValue;
+  if (d_gpt && e.pt_nbins > 65535) return cudaErrorInvalidValue;
   note_launch();
   k_coef_f32<<<(ff.n - 1 + 255) / 256, 256, 0, st>>>(ff.coef, d_ff32, ff.n - 1);
   const SplineF f32{d_ff32, (float)ff.x0, (float)ff.h, (float)ff.inv_h, ff.n};
   note_launch();
-  k_pt_tables<<<e.pt_ne, 256, smem, st>>>(e, f32, d_cdf);
+  k_pt_tables<<<e.pt_ne, 256, smem, st>>>(e, f32, d_cdf, d_gpt);
   return cudaGetLastError();
 }
 

@@ -352,23 +352,24 @@ struct EventParams {
   int dght_law;
   unsigned* vm_err;
 };
-// guide tables (EventParams) of the built CDFs; d_g2 / d_gz / d_gpt sized
-// g2_n, nm * gz_n, pt_ne * gpt_n
 // the (m, y) guide table from the fixed-point CDF that launch_fold_cdf wrote
 cudaError_t launch_guide2_fx(const EventParams& e, const uint64_t* d_cdf2fx, int* d_g2,
                              cudaStream_t st);
+// guide tables (EventParams) of the built CDFs, with their fixed-point copies;
+// d_g2 / d_gz sized g2_n, nm * gz_n (null: skipped)
 cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
-                          const float* d_ptcdf, int* d_g2, int* d_gz, uint16_t* d_gpt,
-                          cudaStream_t st, uint64_t* d_cdf2fx = nullptr,
+                          int* d_g2, int* d_gz, cudaStream_t st, uint64_t* d_cdf2fx = nullptr,
                           uint64_t* d_cdfzfx = nullptr);
 struct EventRecord {  // 48 bytes
   float m, y, z, sign;
   float p0[4];
   float p1[4];
 };
-// d_ff32: scratch for the FP32 copy of the form-factor spline (ff.n - 1 intervals)
+// d_ff32: scratch for the FP32 copy of the form-factor spline (ff.n - 1
+// intervals); d_gpt (optional): the pT guide tables (e.gpt_n per photon
+// energy), built by the same kernel
 cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, float4* d_ff32,
-                                    float* d_cdf, cudaStream_t st);
+                                    float* d_cdf, cudaStream_t st, uint16_t* d_gpt = nullptr);
 cudaError_t launch_events_flags(const EventParams& e, const double* d_cdf2, const double* d_cdfz,
                                 const float* d_ptcdf, uint64_t cand0, int64_t ncand,
                                 uint32_t* d_mask, cudaStream_t st, EventRecord* d_stage = nullptr,
