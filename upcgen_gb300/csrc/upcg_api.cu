@@ -329,8 +329,8 @@ struct upcg_generator {
   // side streams of the table set-up (form factor, breakup, the
   // luminosity-independent samplers) and their fork / join events; ev_ff:
   // the form-factor spline is complete (side[0])
-  cudaStream_t side[3] = {nullptr, nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr}, ev_ff = nullptr;
+  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[4] = {nullptr, nullptr, nullptr, nullptr}, ev_ff = nullptr;
   cudaEvent_t ev_ktab = nullptr;  // the point-flux table (side[2]) is complete
   cudaEvent_t ev_qj = nullptr;    // the Q table's Bessel part (side[2]) is complete
   // host event output: generation done / slot copied out (side[1] copies)
@@ -339,10 +339,11 @@ struct upcg_generator {
     int least = 0, greatest = 0;
     cudaError_t pe = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (pe != cudaSuccess) return pe;
-    for (int i = 0; i < 3; ++i) {
+    for (int i = 0; i < 4; ++i) {
       if (!side[i]) {
         // the table chains feed the luminosity: their blocks go first; the
-        // luminosity-independent samplers (side[2]) fill the SMs they leave
+        // luminosity-independent samplers (side[2]: z, side[3]: photon pT)
+        // fill the SMs they leave
         const int prio = i < 2 ? greatest : least;
         cudaError_t e = cudaStreamCreateWithPriority(&side[i], cudaStreamNonBlocking, prio);
         if (e != cudaSuccess) return e;
@@ -352,7 +353,7 @@ struct upcg_generator {
         if (e != cudaSuccess) return e;
       }
     }
-    for (cudaEvent_t* ev : {&ev_ff, &ev_ktab}) {
+    for (cudaEvent_t* ev : {&ev_ff, &ev_ktab, &ev_gaa, &ev_survival}) {
       if (!*ev) {
         cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
         if (e != cudaSuccess) return e;
@@ -409,7 +410,7 @@ struct upcg_generator {
     set_collision(5020.f, 82, 208);
   }
   ~upcg_generator() {
-    for (int i = 0; i < 3; ++i) {
+    for (int i = 0; i < 4; ++i) {
       if (side[i]) cudaStreamDestroy(side[i]);
       if (ev_join[i]) cudaEventDestroy(ev_join[i]);
     }
@@ -417,6 +418,9 @@ struct upcg_generator {
     if (ev_ff) cudaEventDestroy(ev_ff);
     if (ev_ktab) cudaEventDestroy(ev_ktab);
     if (ev_qj) cudaEventDestroy(ev_qj);
+    if (ev_gaa) cudaEventDestroy(ev_gaa);
+    if (ev_pt) cudaEventDestroy(ev_pt);
+    if (ev_survival) cudaEventDestroy(ev_survival);
     if (ev_gen) cudaEventDestroy(ev_gen);
     for (auto e : ev_out)
       if (e) cudaEventDestroy(e);
@@ -512,12 +516,27 @@ struct upcg_generator {
   bool tab_pending = false, lumi_pending = false, lumi_fast = false, xs_pending = false;
   int complete_deferred(int rc);
   cudaEvent_t ev_ft[2] = {nullptr, nullptr};
-  int enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_ready = nullptr);
+  // pts (optional): a stream for the photon-pT part, joined back into ss
+  int enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_ready = nullptr,
+                              cudaStream_t pts = nullptr);
+  cudaEvent_t ev_pt = nullptr;
   // the main stream waits for the form factor + flux-table chain (once)
   cudaError_t join_flux_tables() {
     if (!ff_join_pending) return cudaSuccess;
     ff_join_pending = false;
     return cudaStreamWaitEvent(st(), ev_join[0], 0);
+  }
+  // the breakup chain (side[1]), and the survival kernel the fast form
+  // launches after it there (ev_survival), not yet joined into the main
+  // stream: the projection needs neither, only the contraction does
+  bool brk_join_pending = false, survival_on_side = false;
+  cudaEvent_t ev_gaa = nullptr, ev_survival = nullptr;
+  cudaError_t join_survival() {
+    if (!brk_join_pending) return cudaSuccess;
+    brk_join_pending = false;
+    const bool side_g = survival_on_side;
+    survival_on_side = false;
+    return cudaStreamWaitEvent(st(), side_g ? ev_survival : ev_join[1], 0);
   }
   int fork_static_samplers();
   bool static_pending = false;   // static samplers enqueued on side[2], not yet joined
@@ -817,8 +836,10 @@ int upcg_generator::build_tables() {
   CK(cudaEventRecord(ev_fork, s));
   CK(cudaStreamWaitEvent(side[0], ev_fork, 0));
   CK(cudaStreamWaitEvent(side[1], ev_fork, 0));
-  // side[2] (the luminosity-independent samplers, fork_static_samplers) starts here too
+  // side[2] and side[3] (the luminosity-independent samplers,
+  // fork_static_samplers) start here too
   CK(cudaStreamWaitEvent(side[2], ev_fork, 0));
+  CK(cudaStreamWaitEvent(side[3], ev_fork, 0));
   CK(gaa_coef.ensure(199));
   CK(ta_coef.ensure(199));
   CK(gaa_work.ensure(800));
@@ -827,6 +848,35 @@ int upcg_generator::build_tables() {
   const bool want32 = !cap && !isVM && (lumiMethod == 2 || fast_tables());
   g32_ready = false;
   if (want32) CK(fgaa32.ensure(200));
+  // breakup probability, enqueued first (the longest chain): knots up to 20 fm
+  // + margin (the path evaluates the spline at min(b, 20))
+  CK(bu_tab.ensure(4 * kBreakupTabMax));
+  CK(ntab.ensure(1));
+  if (!cap) {  // a captured replay reuses the table uploaded by the set-up run
+    CK(upload(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double), side[1]));
+    CK(upload(ntab.p, &bu_nt, sizeof(int), side[1]));
+  }
+  const double dbb = (1000. - 1e-6) / 1000000;
+  brk_n = (int)((20. - 1e-6) / dbb) + 257;
+  CK(brk_y.ensure(brk_n));
+  CK(brk_c.ensure(brk_n));
+  CK(brk_coef.ensure(brk_n - 1));
+  if (breakupMode > 1 && cap && brk_donor) {
+    CK(cudaMemcpyAsync(brk_coef.p, brk_donor->brk_coef.p, (size_t)(brk_n - 1) * sizeof(double4),
+                       cudaMemcpyDeviceToDevice, side[1]));
+  } else if (breakupMode > 1) {
+    if (want32) CK(fbrk32.ensure(brk_n));
+    // the fast form (methods 1, 4; budget 1e-4) takes the FP32 sums (~1e-6);
+    // the reference's sum steps where an energy crosses omax(b), so every
+    // knot is summed (an interpolated table smears those steps to 1.5e-5)
+    const int brk_fp32 = fast_tables() ? 1 : 0;
+    CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
+                             1e-6, dbb, brk_y.p, side[1], brk_fp32));
+    CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1],
+                            want32 ? fbrk32.p : nullptr));
+  }
+  g32_ready = want32;
+  CK(cudaEventRecord(ev_join[1], side[1]));
   // in a captured scan, a configuration with the same inputs as an earlier one
   // copies that one's tables instead of rebuilding them
   if (cap && gaa_donor) {
@@ -839,6 +889,7 @@ int upcg_generator::build_tables() {
     CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s,
                   want32 ? fgaa32.p : nullptr, gaa_f ? fta32.p : nullptr));
   }
+  CK(cudaEventRecord(ev_gaa, s));  // the G_AA spline (and its FP32 copy) is complete
   // form factor on 1e6 knots (the reference's), 65,536 for the fast form
   ff_n = fast_tables() ? kNQ2Fast : kNQ2;
   const double dq = (kQ2max - kQ2min) / ff_n;
@@ -873,39 +924,14 @@ int upcg_generator::build_tables() {
     ftab_early = true;
   }
   CK(cudaEventRecord(ev_join[0], side[0]));
-  // breakup probability: knots up to 20 fm + margin (the path evaluates the
-  // spline at min(b, 20))
-  CK(bu_tab.ensure(4 * kBreakupTabMax));
-  CK(ntab.ensure(1));
-  if (!cap) {  // a captured replay reuses the table uploaded by the set-up run
-    CK(upload(bu_tab.p, bu_host.data(), 4 * kBreakupTabMax * sizeof(double), side[1]));
-    CK(upload(ntab.p, &bu_nt, sizeof(int), side[1]));
-  }
-  const double dbb = (1000. - 1e-6) / 1000000;
-  brk_n = (int)((20. - 1e-6) / dbb) + 257;
-  CK(brk_y.ensure(brk_n));
-  CK(brk_c.ensure(brk_n));
-  CK(brk_coef.ensure(brk_n - 1));
-  if (breakupMode > 1 && cap && brk_donor) {
-    CK(cudaMemcpyAsync(brk_coef.p, brk_donor->brk_coef.p, (size_t)(brk_n - 1) * sizeof(double4),
-                       cudaMemcpyDeviceToDevice, side[1]));
-  } else if (breakupMode > 1) {
-    if (want32) CK(fbrk32.ensure(brk_n));
-    // the fast form (methods 1, 4; budget 1e-4) takes the FP32 sums (~1e-6);
-    // the reference's sum steps where an energy crosses omax(b), so every
-    // knot is summed (an interpolated table smears those steps to 1.5e-5)
-    const int brk_fp32 = fast_tables() ? 1 : 0;
-    CK(launch_breakup_values(bu_tab.p, bu_nt, bu_gammatarg, bu_omaxx, bu_zcon, breakupMode, brk_n,
-                             1e-6, dbb, brk_y.p, side[1], brk_fp32));
-    CK(build_spline_uniform(brk_y.p, brk_n, 1e-6, dbb, brk_c.p, brk_coef.p, side[1],
-                            want32 ? fbrk32.p : nullptr));
-  }
-  g32_ready = want32;
-  CK(cudaEventRecord(ev_join[1], side[1]));
   // only inside upcg_init (defer), whose luminosity step joins the chain
   ff_join_pending = defer && ftab_early && fast_tables() && !usePolarizedCS;
   if (!ff_join_pending) CK(cudaStreamWaitEvent(s, ev_join[0], 0));
-  CK(cudaStreamWaitEvent(s, ev_join[1], 0));
+  // the fast form's survival kernel runs after the breakup chain on its
+  // stream; the main stream joins it before the contraction (join_survival)
+  brk_join_pending = ff_join_pending && g32_ready;
+  survival_on_side = false;
+  if (!brk_join_pending) CK(cudaStreamWaitEvent(s, ev_join[1], 0));
   if (ftab_early) CK(cudaStreamWaitEvent(s, ev_ktab, 0));
   if (!cap) {
     cudaEventRecord(t1, s);
@@ -1212,6 +1238,7 @@ int upcg_generator::setup_flux_tables(cudaStream_t ss, int with_ktab, cudaStream
 int upcg_generator::complete_deferred(int rc) {
   defer = false;
   join_flux_tables();  // no side-stream work left behind on any path
+  join_survival();
   if (herr_copy_pending) {
     mcpy(&hstat->herr, ferr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st());
     herr_copy_pending = false;
@@ -1355,10 +1382,22 @@ int upcg_generator::build_lumi() {
     CK(fbrk32.ensure(breakupMode != 1 ? p.brk.n : 1));
     if (!usePolarizedCS && g32_ready) {
       // the FP32 spline copies come from build_tables; k_fast_G also writes
-      // the far constants and resets the error word
-      CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, nullptr, 0, ffc.p,
-                       ferr.p, 1));
+      // the far constants and resets the error word.  With the breakup chain
+      // not joined it runs after that chain on side[1] (and after the G_AA
+      // spline), beside the projection
+      cudaStream_t gs = s;
+      if (brk_join_pending) {
+        gs = side[1];
+        CK(cudaStreamWaitEvent(gs, ev_gaa, 0));
+      }
+      CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, gs, nullptr, 0,
+                       ffc.p, ferr.p, 1));
+      if (brk_join_pending) {
+        CK(cudaEventRecord(ev_survival, gs));
+        survival_on_side = true;
+      }
     } else if (!usePolarizedCS) {
+      CK(join_survival());
       CK(launch_far_consts(p, breakupMode != 1, ffc.p, s));
       CK(launch_fast_G(p, fu0, fh, P, 1.0, fgaa32.p, fbrk32.p, fgh.p, fgl.p, s, ffc.p, 1, nullptr,
                        nullptr, 1));
@@ -1491,6 +1530,7 @@ int upcg_generator::build_lumi() {
       rotate_rounds(items, grid);
       CK(fitems.ensure(items.size()));
       CK(upload(fitems.p, items.data(), items.size() * sizeof(int4), s));
+      CK(join_survival());  // G (side[1]) before its first reader
       b = mark();
       if (fused)
         CK(launch_contract_fused(fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(), fnodes.p,
@@ -1644,7 +1684,8 @@ int upcg_generator::build_vm() {
 // and their CDFs, the photon-pT spectra, their guide tables.  upcg_init
 // enqueues them on a side stream as soon as the nuclear tables exist, so that
 // they run beside the luminosity; build_xsec joins them.
-int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_ready) {
+int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_ready,
+                                            cudaStream_t pts) {
   const FoldParams f = fold_params();
   {  // getBinY (include/UpcSampler.h:130-133) of every numerator int(nm (m - mmin))
     const double lo = mmin, hi = mmin + (mmax - mmin) / nm * nm;
@@ -1700,13 +1741,19 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_read
   CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
   CK(cdfzfx.ensure((size_t)nm * (nz + 1)));
   const EventParams eg = event_params();  // with the guide buffers allocated
-  if (ff_ready) CK(cudaStreamWaitEvent(ss, ff_ready, 0));  // the pT spectra read the form factor
-  // the pT guide tables (photon pT drawn: NON_ZERO_GAM_PT, vector mesons)
-  // come from the spectra's own kernel
-  const bool pt_guides = eg.useNonzeroGamPt || eg.vm;
-  CK(launch_photon_pt_tables(eg, lumi_params().ff, ff32.p, ptcdf.p, ss,
-                             pt_guides ? guidept.p : nullptr));
   CK(launch_guides(eg, nullptr, cdfz.p, nullptr, guidez.p, ss, nullptr, cdfzfx.p));
+  // the photon-pT spectra (they read the form factor) and their guide tables
+  // (photon pT drawn: NON_ZERO_GAM_PT, vector mesons), on pts when given
+  cudaStream_t ps = pts ? pts : ss;
+  if (ff_ready) CK(cudaStreamWaitEvent(ps, ff_ready, 0));
+  const bool pt_guides = eg.useNonzeroGamPt || eg.vm;
+  CK(launch_photon_pt_tables(eg, lumi_params().ff, ff32.p, ptcdf.p, ps,
+                             pt_guides ? guidept.p : nullptr));
+  if (pts) {
+    if (!ev_pt) CK(cudaEventCreateWithFlags(&ev_pt, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev_pt, pts));
+    CK(cudaStreamWaitEvent(ss, ev_pt, 0));
+  }
   return UPCG_OK;
 }
 
@@ -1717,7 +1764,7 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_read
 int upcg_generator::fork_static_samplers() {
   CK(side_streams());
   if (!ev_static) CK(cudaEventCreateWithFlags(&ev_static, cudaEventDisableTiming));
-  const int rc = enqueue_static_samplers(side[2], ev_ff);
+  const int rc = enqueue_static_samplers(side[2], ev_ff, side[3]);
   if (rc) return rc;
   CK(cudaEventRecord(ev_static, side[2]));
   static_pending = true;
@@ -2080,6 +2127,8 @@ int upcg_init(upcg_generator* g) {
   if (rc) return g->complete_deferred(rc);
   rc = g->lumi_cache_usable() ? g->build_lumi_cached() : g->build_lumi();
   if (const cudaError_t je = g->join_flux_tables(); je != cudaSuccess && !rc)
+    rc = fail(UPCG_ERR_CUDA, "upcg_init: %s", cudaGetErrorString(je));
+  if (const cudaError_t je = g->join_survival(); je != cudaSuccess && !rc)
     rc = fail(UPCG_ERR_CUDA, "upcg_init: %s", cudaGetErrorString(je));
   if (rc) {
     if (g->static_pending) {  // leave no side-stream work behind a failed init
