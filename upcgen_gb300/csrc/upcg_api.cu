@@ -341,7 +341,9 @@ struct upcg_generator {
     if (pe != cudaSuccess) return pe;
     for (int i = 0; i < 4; ++i) {
       if (!side[i]) {
-        // the table chains feed the luminosity: their blocks go first; the
+        // the form factor -> flux tables chain (side[0]) feeds the
+        // projection, the breakup / G_AA chain and the survival kernel
+        // (side[1]) the contraction: their blocks go first; the
         // luminosity-independent samplers (side[2]: z, side[3]: photon pT)
         // fill the SMs they leave
         const int prio = i < 2 ? greatest : least;
@@ -418,6 +420,7 @@ struct upcg_generator {
     if (ev_ff) cudaEventDestroy(ev_ff);
     if (ev_ktab) cudaEventDestroy(ev_ktab);
     if (ev_qj) cudaEventDestroy(ev_qj);
+    if (ev_static_go) cudaEventDestroy(ev_static_go);
     if (ev_gaa) cudaEventDestroy(ev_gaa);
     if (ev_pt) cudaEventDestroy(ev_pt);
     if (ev_survival) cudaEventDestroy(ev_survival);
@@ -429,6 +432,9 @@ struct upcg_generator {
     for (auto e : ev_ft)
       if (e) cudaEventDestroy(e);
     if (own) cudaStreamDestroy(own);
+    if (hp) cudaStreamDestroy(hp);
+    for (auto e : ev_hp)
+      if (e) cudaEventDestroy(e);
   }
   void set_collision(float s, int z, int aa) {
     sqrts = s;
@@ -438,9 +444,48 @@ struct upcg_generator {
     A = aa;
   }
   cudaStream_t st() {
+    if (hp_active) return hp;
+    return user_st();
+  }
+  cudaStream_t user_st() {
     if (stream) return stream;
     if (!own) cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking);
     return own;
+  }
+  // upcg_init runs its main-stream work on hp, a high-priority stream forked
+  // from the caller's and joined back before the host synchronisation: the
+  // projection and the contraction take the SMs ahead of the samplers beside
+  // them, the table chains' kernels ahead of theirs
+  cudaStream_t hp = nullptr;
+  cudaEvent_t ev_hp[2] = {nullptr, nullptr};
+  bool hp_active = false;
+  cudaError_t hp_begin() {
+    cudaStream_t u = user_st();
+    if (!hp) {
+      // one level below the table chains' streams (greatest): the chains'
+      // short kernels are dispatched ahead of the projection's pending blocks
+      int least = 0, greatest = 0;
+      cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+      const int prio = greatest < least ? greatest + 1 : greatest;
+      if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&hp, cudaStreamNonBlocking, prio);
+      if (e != cudaSuccess) return e;
+    }
+    for (auto& e : ev_hp)
+      if (!e) {
+        cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        if (r != cudaSuccess) return r;
+      }
+    cudaError_t e = cudaEventRecord(ev_hp[0], u);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(hp, ev_hp[0], 0);
+    if (e == cudaSuccess) hp_active = true;
+    return e;
+  }
+  cudaError_t hp_end() {
+    if (!hp_active) return cudaSuccess;
+    hp_active = false;
+    cudaError_t e = cudaEventRecord(ev_hp[1], hp);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(user_st(), ev_hp[1], 0);
+    return e;
   }
   void invalidate() {
     tables_ready = lumi_ready = xsec_ready = false;
@@ -517,14 +562,17 @@ struct upcg_generator {
   int complete_deferred(int rc);
   cudaEvent_t ev_ft[2] = {nullptr, nullptr};
   // pts (optional): a stream for the photon-pT part, joined back into ss
+  // parts: 1 the z samplers (and the mass-bin tables, sigma(m)), 2 the
+  // photon-pT spectra and guides (on pts when given, ev_pt recorded there)
   int enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_ready = nullptr,
-                              cudaStream_t pts = nullptr);
+                              cudaStream_t pts = nullptr, int parts = 3);
   cudaEvent_t ev_pt = nullptr;
   // the main stream waits for the form factor + flux-table chain (once)
   cudaError_t join_flux_tables() {
     if (!ff_join_pending) return cudaSuccess;
     ff_join_pending = false;
-    return cudaStreamWaitEvent(st(), ev_join[0], 0);
+    const cudaError_t e = cudaStreamWaitEvent(st(), ev_ktab, 0);  // the point-flux table
+    return e != cudaSuccess ? e : cudaStreamWaitEvent(st(), ev_join[0], 0);
   }
   // the breakup chain (side[1]), and the survival kernel the fast form
   // launches after it there (ev_survival), not yet joined into the main
@@ -538,8 +586,17 @@ struct upcg_generator {
     survival_on_side = false;
     return cudaStreamWaitEvent(st(), side_g ? ev_survival : ev_join[1], 0);
   }
-  int fork_static_samplers();
+  // parts as enqueue_static_samplers'; ev_static (side[2]) covers both once
+  // the z part is forked
+  int fork_static_samplers(int parts = 3);
+  bool pt_forked = false;
   bool static_pending = false;   // static samplers enqueued on side[2], not yet joined
+  // upcg_init's samplers not enqueued yet: the fast form's luminosity step
+  // enqueues them right after the side constants' launch, so that the host's
+  // launch order puts the projection's kernels ahead of theirs
+  bool statics_deferred = false;
+  cudaEvent_t ev_static_go = nullptr;  // where the deferred samplers start
+  bool static_go = false;
   // the form factor + flux-table chain (side[0], ev_join[0]) not yet joined
   // into the main stream: the fast form joins it only where the projection
   // first reads the flux tables, so that the survival kernel and the side
@@ -831,8 +888,7 @@ int upcg_generator::build_tables() {
     bu_host[2 * kBreakupTabMax + k] = std::log(bu_host[k]);
     bu_host[3 * kBreakupTabMax + k] = 1. / bu_host[k];
   }
-  // three independent chains: G_AA on the handle's stream, the form factor
-  // and the breakup probability on two side streams
+  // the table chains on forked streams
   CK(cudaEventRecord(ev_fork, s));
   CK(cudaStreamWaitEvent(side[0], ev_fork, 0));
   CK(cudaStreamWaitEvent(side[1], ev_fork, 0));
@@ -848,8 +904,51 @@ int upcg_generator::build_tables() {
   const bool want32 = !cap && !isVM && (lumiMethod == 2 || fast_tables());
   g32_ready = false;
   if (want32) CK(fgaa32.ensure(200));
-  // breakup probability, enqueued first (the longest chain): knots up to 20 fm
-  // + margin (the path evaluates the spline at min(b, 20))
+  // The fast form's projection (k_fast_sides, k_fast_weights) waits for the
+  // form factor -> flux tables chain alone: it is enqueued first, on the
+  // stream of greatest priority.  The breakup and G_AA chains feed only the
+  // survival kernel, which the contraction needs: in the single-configuration
+  // fast form they run one after the other on side[1] (least priority) and the
+  // survival kernel after them there; otherwise G_AA runs on the handle's
+  // stream and the breakup chain on side[1].
+  const bool survival_side = defer && !cap && !isVM && fast_tables() && !usePolarizedCS;
+  cudaStream_t gs = survival_side ? side[1] : s;
+  // form factor on 1e6 knots (the reference's), 65,536 for the fast form
+  ff_n = fast_tables() ? kNQ2Fast : kNQ2;
+  const double dq = (kQ2max - kQ2min) / ff_n;
+  CK(ff_y.ensure(ff_n));
+  CK(ff_c.ensure(ff_n));
+  CK(ff_coef.ensure(ff_n - 1));
+  if (cap && ff_donor && ff_donor->ff_n == ff_n) {
+    CK(cudaMemcpyAsync(ff_coef.p, ff_donor->ff_coef.p, (size_t)(ff_n - 1) * sizeof(double4),
+                       cudaMemcpyDeviceToDevice, side[0]));
+  } else {
+    CK(launch_formfac_values(ff_y.p, ff_n, kQ2min, dq, rho0, R, a, side[0]));
+    CK(build_spline_uniform(ff_y.p, ff_n, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
+  }
+  CK(cudaEventRecord(ev_ff, side[0]));
+  ftab_early = false;
+  if (!cap && !isVM && (lumiMethod == 2 || fast_tables())) {
+    // the fast form's flux tables need only the form factor: they run here,
+    // ahead of the breakup and G_AA chains
+    for (auto& e : ev_ft)
+      if (!e) CK(cudaEventCreate(&e));
+    CK(cudaEventRecord(ev_ft[0], side[0]));
+    // the Q table's Bessel part on side[2] (setup_flux_tables), then the
+    // point-flux table there, ahead of the samplers
+    const int frc = setup_flux_tables(side[0], 0, side[2]);
+    if (frc) return frc;
+    CK(cudaEventRecord(ev_ft[1], side[0]));
+    CK(fk1.ensure(flux_table_ktab_n()));
+    CK(fs32.ensure(flux_table_ktab_n()));
+    CK(fk01.ensure(2 * (size_t)flux_table_ktab_n()));
+    CK(launch_ktab(g1, fk1.p, fs32.p, side[2], fk01.p, fk01_ready ? 1 : 0));
+    CK(cudaEventRecord(ev_ktab, side[2]));
+    fk01_ready = true;
+    ftab_early = true;
+  }
+  // breakup probability: knots up to 20 fm + margin (the path evaluates the
+  // spline at min(b, 20))
   CK(bu_tab.ensure(4 * kBreakupTabMax));
   CK(ntab.ensure(1));
   if (!cap) {  // a captured replay reuses the table uploaded by the set-up run
@@ -881,48 +980,15 @@ int upcg_generator::build_tables() {
   // copies that one's tables instead of rebuilding them
   if (cap && gaa_donor) {
     CK(cudaMemcpyAsync(gaa_coef.p, gaa_donor->gaa_coef.p, 199 * sizeof(double4),
-                       cudaMemcpyDeviceToDevice, s));
+                       cudaMemcpyDeviceToDevice, gs));
   } else {
     // the fast forms (budget 1e-4) evaluate the T_A / G_AA integrands in FP32
     const bool gaa_f = !isVM && fast_tables();
     if (gaa_f) CK(fta32.ensure(199));
-    CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, s,
+    CK(launch_gaa(rho0, R, a, csNN, gk, gaa_coef.p, ta_coef.p, gaa_work.p, gs,
                   want32 ? fgaa32.p : nullptr, gaa_f ? fta32.p : nullptr));
   }
-  CK(cudaEventRecord(ev_gaa, s));  // the G_AA spline (and its FP32 copy) is complete
-  // form factor on 1e6 knots (the reference's), 65,536 for the fast form
-  ff_n = fast_tables() ? kNQ2Fast : kNQ2;
-  const double dq = (kQ2max - kQ2min) / ff_n;
-  CK(ff_y.ensure(ff_n));
-  CK(ff_c.ensure(ff_n));
-  CK(ff_coef.ensure(ff_n - 1));
-  if (cap && ff_donor && ff_donor->ff_n == ff_n) {
-    CK(cudaMemcpyAsync(ff_coef.p, ff_donor->ff_coef.p, (size_t)(ff_n - 1) * sizeof(double4),
-                       cudaMemcpyDeviceToDevice, side[0]));
-  } else {
-    CK(launch_formfac_values(ff_y.p, ff_n, kQ2min, dq, rho0, R, a, side[0]));
-    CK(build_spline_uniform(ff_y.p, ff_n, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
-  }
-  CK(cudaEventRecord(ev_ff, side[0]));
-  ftab_early = false;
-  if (!cap && !isVM && (lumiMethod == 2 || fast_tables())) {
-    // the fast form's flux tables need only the form factor: they run here,
-    // beside the breakup and G_AA chains
-    for (auto& e : ev_ft)
-      if (!e) CK(cudaEventCreate(&e));
-    // the point-flux table on side[2], ahead of the samplers there
-    CK(fk1.ensure(flux_table_ktab_n()));
-    CK(fs32.ensure(flux_table_ktab_n()));
-    CK(fk01.ensure(2 * (size_t)flux_table_ktab_n()));
-    CK(launch_ktab(g1, fk1.p, fs32.p, side[2], fk01.p, fk01_ready ? 1 : 0));
-    CK(cudaEventRecord(ev_ktab, side[2]));
-    fk01_ready = true;
-    CK(cudaEventRecord(ev_ft[0], side[0]));
-    const int frc = setup_flux_tables(side[0], 0, side[2]);
-    if (frc) return frc;
-    CK(cudaEventRecord(ev_ft[1], side[0]));
-    ftab_early = true;
-  }
+  CK(cudaEventRecord(ev_gaa, gs));  // the G_AA spline (and its FP32 copy) is complete
   CK(cudaEventRecord(ev_join[0], side[0]));
   // only inside upcg_init (defer), whose luminosity step joins the chain
   ff_join_pending = defer && ftab_early && fast_tables() && !usePolarizedCS;
@@ -932,7 +998,9 @@ int upcg_generator::build_tables() {
   brk_join_pending = ff_join_pending && g32_ready;
   survival_on_side = false;
   if (!brk_join_pending) CK(cudaStreamWaitEvent(s, ev_join[1], 0));
-  if (ftab_early) CK(cudaStreamWaitEvent(s, ev_ktab, 0));
+  // the point-flux table: joined with the flux tables where the projection
+  // first reads them (join_flux_tables), else here
+  if (ftab_early && !ff_join_pending) CK(cudaStreamWaitEvent(s, ev_ktab, 0));
   if (!cap) {
     cudaEventRecord(t1, s);
     if (defer) {
@@ -1243,7 +1311,8 @@ int upcg_generator::complete_deferred(int rc) {
     mcpy(&hstat->herr, ferr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st());
     herr_copy_pending = false;
   }
-  const cudaError_t se = cudaStreamSynchronize(st());
+  const cudaError_t he = hp_end();  // the caller's stream waits for init's work
+  const cudaError_t se = he != cudaSuccess ? he : cudaStreamSynchronize(st());
   auto elapsed = [](cudaEvent_t a, cudaEvent_t b) {
     float t = 0;
     cudaEventElapsedTime(&t, a, b);
@@ -1531,6 +1600,18 @@ int upcg_generator::build_lumi() {
       CK(fitems.ensure(items.size()));
       CK(upload(fitems.p, items.data(), items.size() * sizeof(int4), s));
       CK(join_survival());  // G (side[1]) before its first reader
+      if (statics_deferred) {
+        // the samplers from here: ready together with the contraction, whose
+        // CTAs (the stream of greatest priority) take the SMs first; theirs
+        // share the SMs with it (the contraction is tensor-bound with 6 warps
+        // per SM) instead of the FP64 pipes with the table chains
+        statics_deferred = false;
+        if (!ev_static_go) CK(cudaEventCreateWithFlags(&ev_static_go, cudaEventDisableTiming));
+        CK(cudaEventRecord(ev_static_go, s));
+        static_go = true;
+        const int frc = fork_static_samplers(1);
+        if (frc) return frc;
+      }
       b = mark();
       if (fused)
         CK(launch_contract_fused(fgh.p, fgl.p, 1, ncp, P, fitems.p, (int)items.size(), fnodes.p,
@@ -1685,9 +1766,9 @@ int upcg_generator::build_vm() {
 // enqueues them on a side stream as soon as the nuclear tables exist, so that
 // they run beside the luminosity; build_xsec joins them.
 int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_ready,
-                                            cudaStream_t pts) {
+                                            cudaStream_t pts, int parts) {
   const FoldParams f = fold_params();
-  {  // getBinY (include/UpcSampler.h:130-133) of every numerator int(nm (m - mmin))
+  if (parts & 1) {  // getBinY (include/UpcSampler.h:130-133) of every numerator int(nm (m - mmin))
     const double lo = mmin, hi = mmin + (mmax - mmin) / nm * nm;
     const double nmax = std::floor(nm * (hi - lo)) + 2;
     mbinlut_n = nmax < (double)(1 << 22) ? (int)nmax : 0;
@@ -1713,11 +1794,13 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_read
       medges_ok = true;
     }
   }
-  if (!isVM) {  // sigma(m) per m-row for the fold (build_xsec)
+  if ((parts & 1) && !isVM) {  // sigma(m) per m-row for the fold (build_xsec)
     CK(csm.ensure(usePolarizedCS ? 2 * (size_t)nm : (size_t)nm));
     CK(launch_cs_m_rows(f, csm.p, ss));
   }
-  if (isVM) {
+  if (!(parts & 1)) {
+    // the photon-pT part only
+  } else if (isVM) {
     CK(cdfz.ensure(1));  // no z distribution (ignoreCSZ)
   } else if (!usePolarizedCS) {
     CK(cszm.ensure((size_t)nm * nz));
@@ -1741,18 +1824,19 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_read
   CK(guidept.ensure((size_t)e.pt_ne * e.gpt_n));
   CK(cdfzfx.ensure((size_t)nm * (nz + 1)));
   const EventParams eg = event_params();  // with the guide buffers allocated
-  CK(launch_guides(eg, nullptr, cdfz.p, nullptr, guidez.p, ss, nullptr, cdfzfx.p));
-  // the photon-pT spectra (they read the form factor) and their guide tables
-  // (photon pT drawn: NON_ZERO_GAM_PT, vector mesons), on pts when given
-  cudaStream_t ps = pts ? pts : ss;
-  if (ff_ready) CK(cudaStreamWaitEvent(ps, ff_ready, 0));
-  const bool pt_guides = eg.useNonzeroGamPt || eg.vm;
-  CK(launch_photon_pt_tables(eg, lumi_params().ff, ff32.p, ptcdf.p, ps,
-                             pt_guides ? guidept.p : nullptr));
-  if (pts) {
-    if (!ev_pt) CK(cudaEventCreateWithFlags(&ev_pt, cudaEventDisableTiming));
-    CK(cudaEventRecord(ev_pt, pts));
-    CK(cudaStreamWaitEvent(ss, ev_pt, 0));
+  if (parts & 1) CK(launch_guides(eg, nullptr, cdfz.p, nullptr, guidez.p, ss, nullptr, cdfzfx.p));
+  if (parts & 2) {
+    // the photon-pT spectra (they read the form factor) and their guide tables
+    // (photon pT drawn: NON_ZERO_GAM_PT, vector mesons), on pts when given
+    cudaStream_t ps = pts ? pts : ss;
+    if (ff_ready) CK(cudaStreamWaitEvent(ps, ff_ready, 0));
+    const bool pt_guides = eg.useNonzeroGamPt || eg.vm;
+    CK(launch_photon_pt_tables(eg, lumi_params().ff, ff32.p, ptcdf.p, ps,
+                               pt_guides ? guidept.p : nullptr));
+    if (pts) {
+      if (!ev_pt) CK(cudaEventCreateWithFlags(&ev_pt, cudaEventDisableTiming));
+      CK(cudaEventRecord(ev_pt, pts));
+    }
   }
   return UPCG_OK;
 }
@@ -1761,13 +1845,28 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_read
 // nothing of the luminosity and, of the tables, only the form factor
 // (ev_ff), so they run beside the table chains, whose small grids leave most
 // SMs idle, and are done before the weights and the contraction fill the GPU.
-int upcg_generator::fork_static_samplers() {
+int upcg_generator::fork_static_samplers(int parts) {
   CK(side_streams());
   if (!ev_static) CK(cudaEventCreateWithFlags(&ev_static, cudaEventDisableTiming));
-  const int rc = enqueue_static_samplers(side[2], ev_ff, side[3]);
-  if (rc) return rc;
-  CK(cudaEventRecord(ev_static, side[2]));
-  static_pending = true;
+  if (parts & 2) {  // the photon-pT part on side[3], after the form factor
+    const int rc = enqueue_static_samplers(side[2], ev_ff, side[3], 2);
+    if (rc) return rc;
+    pt_forked = true;
+  }
+  if (parts & 1) {  // the z part on side[2] (from the go event when one is set)
+    if (static_go) {
+      static_go = false;
+      CK(cudaStreamWaitEvent(side[2], ev_static_go, 0));
+    }
+    const int rc = enqueue_static_samplers(side[2], ev_ff, nullptr, 1);
+    if (rc) return rc;
+    if (pt_forked) {
+      CK(cudaStreamWaitEvent(side[2], ev_pt, 0));
+      pt_forked = false;
+    }
+    CK(cudaEventRecord(ev_static, side[2]));
+    static_pending = true;
+  }
   return UPCG_OK;
 }
 
@@ -2115,6 +2214,8 @@ int upcg_init(upcg_generator* g) {
   if (!g->hstat && cudaMallocHost(&g->hstat, sizeof(upcg_generator::HostStatus)) != cudaSuccess)
     return fail(UPCG_ERR_CUDA, "pinned status block");
   g->defer = true;  // one host synchronisation, at the end (complete_deferred)
+  if (const cudaError_t he = g->hp_begin(); he != cudaSuccess)
+    return g->complete_deferred(fail(UPCG_ERR_CUDA, "upcg_init: %s", cudaGetErrorString(he)));
   int rc = g->build_tables();
   if (rc) return g->complete_deferred(rc);
   g->lumi_cache_hit = -1;
@@ -2123,9 +2224,18 @@ int upcg_init(upcg_generator* g) {
     if (rc) return g->complete_deferred(rc);
     return g->complete_deferred(g->build_xsec());
   }
-  rc = g->fork_static_samplers();  // beside the luminosity
+  // the photon-pT spectra now (beside the table chains); the z samplers from
+  // the luminosity step's contraction launch (beside the contraction)
+  g->pt_forked = false;
+  rc = g->fork_static_samplers(2);
   if (rc) return g->complete_deferred(rc);
+  g->statics_deferred = true;
   rc = g->lumi_cache_usable() ? g->build_lumi_cached() : g->build_lumi();
+  if (!rc && g->statics_deferred) {  // a path that did not enqueue them
+    g->statics_deferred = false;
+    rc = g->fork_static_samplers(1);
+  }
+  g->statics_deferred = false;
   if (const cudaError_t je = g->join_flux_tables(); je != cudaSuccess && !rc)
     rc = fail(UPCG_ERR_CUDA, "upcg_init: %s", cudaGetErrorString(je));
   if (const cudaError_t je = g->join_survival(); je != cudaSuccess && !rc)
@@ -2134,6 +2244,10 @@ int upcg_init(upcg_generator* g) {
     if (g->static_pending) {  // leave no side-stream work behind a failed init
       cudaStreamWaitEvent(g->st(), g->ev_static, 0);
       g->static_pending = false;
+    }
+    if (g->pt_forked) {
+      cudaStreamWaitEvent(g->st(), g->ev_pt, 0);
+      g->pt_forked = false;
     }
     return g->complete_deferred(rc);
   }

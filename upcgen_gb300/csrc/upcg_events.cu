@@ -650,7 +650,8 @@ __global__ void k_pt_tables(EventParams e, SplineF ff, float* __restrict__ out,
   const int nb = e.pt_nbins;
   const float inv_pi2x4 = (float)(1. / (4 * kPi * kPi));
   const float w = (float)e.pt_width;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+#pragma unroll 4
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {  // independent bins: loads overlap
     const float pt = w * (b + 1);
     const float arg = pt * pt + ered;
     const float f = spline_eval_f(ff, ff.coef, arg);
@@ -836,9 +837,11 @@ cudaError_t launch_guides(const EventParams& e, const double* d_cdf2, const doub
     if (!d_cdfzfx) return cudaErrorInvalidValue;
     const int64_t nzc = (int64_t)e.nm * (e.nz + 1);
     note_launch();
+    carveout_max_shared<k_cdf_fixed>();
     k_cdf_fixed<<<(unsigned)((nzc + 255) / 256), 256, 0, st>>>(d_cdfz, nzc, d_cdfzfx);
     const int64_t nz = (int64_t)e.nm * e.gz_n;
     note_launch();
+    carveout_max_shared<k_guide_rows_fx>();
     k_guide_rows_fx<<<(unsigned)((nz + 255) / 256), 256, 0, st>>>(d_cdfzfx, e.nm, e.nz, e.gz_bits,
                                                                   d_gz);
   }
@@ -851,9 +854,11 @@ cudaError_t launch_photon_pt_tables(const EventParams& e, const SplineU& ff, flo
   if (smem > 48 * 1024) return cudaErrorInvalidValue;
   if (d_gpt && e.pt_nbins > 65535) return cudaErrorInvalidValue;
   note_launch();
+  carveout_max_shared<k_coef_f32>();
   k_coef_f32<<<(ff.n - 1 + 255) / 256, 256, 0, st>>>(ff.coef, d_ff32, ff.n - 1);
   const SplineF f32{d_ff32, (float)ff.x0, (float)ff.h, (float)ff.inv_h, ff.n};
   note_launch();
+  carveout_max_shared<k_pt_tables>();
   k_pt_tables<<<e.pt_ne, 256, smem, st>>>(e, f32, d_cdf, d_gpt);
   return cudaGetLastError();
 }

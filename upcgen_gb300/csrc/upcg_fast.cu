@@ -574,10 +574,17 @@ __global__ void k_qtab_H(LumiParams p, const double* __restrict__ qn, const doub
       tail[j] = fc / b * (j0(b * kQNodeMax / kHc) - j0(b * 10. / kHc));
     }
   }
+  // (w / g)^2 of the block's row, once per block: an FP64 exp and two
+  // divisions cost a warp the same for one lane as for 32
+  __shared__ double s_e2;
+  if (threadIdx.x == 0) {
+    const double w = exp(lw0 + iw * hw);
+    s_e2 = w * w / p.g1 / p.g1;
+  }
+  __syncthreads();
   if (n >= nq) return;
-  const double w = exp(lw0 + iw * hw);
   const double q = qn[n];
-  const double t = q * q + w * w / p.g1 / p.g1;
+  const double t = q * q + s_e2;
   const double ffv = spline_eval(p.ff, t < p.q2max ? t : p.q2clamp);
   const double h = wn[n] * (q * q * ffv / t);
   // stored as a double-float pair (hi, lo) for k_qtab_product

@@ -398,6 +398,7 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf_write_fx(const double* __re
 cudaError_t launch_cs_zm(const FoldParams& f, int flag, double* d_out, cudaStream_t st) {
   const int n = f.nm * f.nz;
   note_launch();
+  carveout_max_shared<k_cs_zm>();
   k_cs_zm<<<(n + 255) / 256, 256, 0, st>>>(f, flag, d_out);
   return cudaGetLastError();
 }
@@ -412,6 +413,7 @@ cudaError_t launch_cs_m_points(const FoldParams& f, const double* d_m, double* d
 
 cudaError_t launch_cs_m_rows(const FoldParams& f, double* d_csm, cudaStream_t st) {
   note_launch();
+  carveout_max_shared<k_cs_m_rows>();
   k_cs_m_rows<<<(f.nm + 127) / 128, 128, 0, st>>>(f, d_csm);
   return cudaGetLastError();
 }
@@ -457,6 +459,7 @@ cudaError_t launch_cdf_rows(const double* d_w, int rows, int len, double* d_cdf,
                             cudaStream_t st) {
   note_launch();
   // one warp per row, four rows per block
+  carveout_max_shared<k_cdf_rows>();
   k_cdf_rows<<<(rows + 3) / 4, 128, 0, st>>>(d_w, rows, len, d_cdf);
   return cudaGetLastError();
 }

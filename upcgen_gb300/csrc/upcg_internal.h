@@ -271,6 +271,20 @@ cudaError_t launch_fast_finish(const LumiParams& p, int cell0, int ncells, int n
 void delta_tile_ranges(int P, double u0, double h, const double* cosk, int ncos, int tbn, int bk,
                        std::vector<std::pair<int, int>>& out);
 inline int pack_item(int rows, int klo, int khi) { return rows | (klo << 8) | (khi << 16); }
+// The luminosity-independent samplers share the SMs with the persistent
+// contraction, whose shared memory sets the SM's carveout to its maximum: the
+// samplers' kernels ask for the same carveout, so that their blocks can be
+// resident beside its CTA.  Once per kernel and process.
+template <auto Kernel>
+inline void carveout_max_shared() {
+  static const bool done = [] {
+    cudaFuncSetAttribute(Kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
+    cudaGetLastError();  // a refusal only leaves the default carveout
+    return true;
+  }();
+  (void)done;
+}
 constexpr int kContractBK = 64;  // K tile of the contraction kernels
 cudaError_t contract_selftest(int ncells, int P, uint64_t seed, double* max_rel, double* ms);
 
