@@ -169,6 +169,40 @@ def test_fast_gaa_table_fp32_integrands(ug, nucleus):
     assert rel.max() < 2e-5
 
 
+def test_fast_form_factor_table(ug, oracle_mod):
+    """The fast form's form-factor spline: its 65,536 knot values (the closed
+    form with one sincos and sinh/cosh from one exp) against the oracle's
+    calcFormFac within 2e-9 of F(0) (the plain path's bound: at the smallest
+    Q^2 the closed form cancels to O(Q^4) and the device's and the host's
+    last-bit sin/cos/sinh/cosh differences reach ~1e-9 of F); between the
+    knots within 1e-12 of F(0)
+    above Q^2 = 1e-3 GeV^2, and within 1e-6 of F(0) in the first intervals,
+    where the natural spline's free end (second derivative 0 at Q2min)
+    departs from F (5.4e-7 measured for a natural spline on these knots)."""
+    p = dict(C1, FLUX_POINT=0, BINS_M=3, BINS_Y=3)
+    g = ug.UpcGenerator(p)
+    g.setLumiMethod("fast")
+    g.init()
+    o = oracle_mod.Oracle(p, threads=os.cpu_count())
+    o.init_tables()
+    n, q2min, q2max = 65536, 1e-9, 2.0
+    h = (q2max - q2min) / n
+    knots = q2min + h * np.concatenate([np.arange(0, 64), np.arange(64, n - 1, 97)])
+    f0 = abs(o.form_factor(q2min))
+    at_knots = np.abs(g.nucProcessCS.spline("formfac", knots) -
+                      np.array([o.form_factor(x) for x in knots])).max() / f0
+    mid = np.linspace(1e-3, 1.999, 3001)
+    between = np.abs(g.nucProcessCS.spline("formfac", mid) -
+                     np.array([o.form_factor(x) for x in mid])).max() / f0
+    first = np.geomspace(1e-9, 1e-3, 200)
+    near0 = np.abs(g.nucProcessCS.spline("formfac", first) -
+                   np.array([o.form_factor(x) for x in first])).max() / f0
+    print("fast form factor / F(0): knots", at_knots, "above 1e-3", between, "first intervals", near0)
+    assert at_knots < 2e-9
+    assert between < 1e-12
+    assert near0 < 1e-6
+
+
 def test_fast_contraction_on_reference_fluxes(ug):
     """Method 2: the plain path's node fluxes (the reference's QAGS) through
     the projection and the tensor-core contraction -- isolates the

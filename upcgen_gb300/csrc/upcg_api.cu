@@ -923,7 +923,8 @@ int upcg_generator::build_tables() {
     CK(cudaMemcpyAsync(ff_coef.p, ff_donor->ff_coef.p, (size_t)(ff_n - 1) * sizeof(double4),
                        cudaMemcpyDeviceToDevice, side[0]));
   } else {
-    CK(launch_formfac_values(ff_y.p, ff_n, kQ2min, dq, rho0, R, a, side[0]));
+    CK(launch_formfac_values(ff_y.p, ff_n, kQ2min, dq, rho0, R, a, side[0],
+                             fast_tables() ? 1 : 0));
     CK(build_spline_uniform(ff_y.p, ff_n, kQ2min, dq, ff_c.p, ff_coef.p, side[0]));
   }
   CK(cudaEventRecord(ev_ff, side[0]));
@@ -1848,7 +1849,10 @@ int upcg_generator::enqueue_static_samplers(cudaStream_t ss, cudaEvent_t ff_read
 int upcg_generator::fork_static_samplers(int parts) {
   CK(side_streams());
   if (!ev_static) CK(cudaEventCreateWithFlags(&ev_static, cudaEventDisableTiming));
-  if (parts & 2) {  // the photon-pT part on side[3], after the form factor
+  if (parts & 2) {
+    // the photon-pT part on side[3], after the form factor (beside the flux
+    // tables: after them it would meet the projection's pending blocks and
+    // hold SMs when the contraction starts)
     const int rc = enqueue_static_samplers(side[2], ev_ff, side[3], 2);
     if (rc) return rc;
     pt_forked = true;

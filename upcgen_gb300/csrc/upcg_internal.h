@@ -99,8 +99,9 @@ cudaError_t launch_grid_cells(const LumiParams& p, const GridForm& gf, const flo
 // tables; d_coef32 (optional): an FP32 copy of the coefficients, (float) of each
 cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, double* d_c,
                                  double4* d_coef, cudaStream_t st, float4* d_coef32 = nullptr);
+// fast: the fast form's knots, the closed form with fewer FP64 transcendentals
 cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, double rho0,
-                                  double R, double a, cudaStream_t st);
+                                  double R, double a, cudaStream_t st, int fast = 0);
 // G_AA spline (199 intervals into d_coef); d_ta_coef: 199 intervals of the
 // T_A spline; d_work: 800 doubles of scratch
 // d_coef32: FP32 copy of the G_AA coefficients; d_ta32 (199 float4): the fast

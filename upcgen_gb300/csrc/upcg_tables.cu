@@ -92,6 +92,37 @@ __global__ void k_formfac_values(double* __restrict__ out, int n, double x0, dou
   out[i] = calc_form_fac(x0 + i * h, rho0, R, a);
 }
 
+// The same closed form for the fast form's knots with fewer FP64
+// transcendentals (GB300's FP64 pipe runs at 1/64 of the FP32 rate): one
+// sincos for sin, cos(QR); sinh, cosh(x) from one exp where x = pi Q a >=
+// 0.05 (below, the bracket's terms cancel like (QR)^-2 and e^x - e^-x would
+// pass its rounding on: the library's sinh, cosh there, the first knots
+// only); exp(-R/a) once on the host.  Values move by rounding, not by the
+// formula.
+__global__ void k_formfac_values_fast(double* __restrict__ out, int n, double x0, double h,
+                                      double rho0, double R, double a, double e_ra) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double Q = sqrt(x0 + i * h) / kHc;
+  const double x = kPi * Q * a;
+  double sinhVal, coshVal;
+  if (x < 0.05) {
+    sinhVal = sinh(x);
+    coshVal = cosh(x);
+  } else {
+    const double ex = exp(x), emx = 1. / ex;
+    sinhVal = 0.5 * (ex - emx);
+    coshVal = 0.5 * (ex + emx);
+  }
+  double sqr, cqr;
+  sincos(Q * R, &sqr, &cqr);
+  const double qa2 = 1 + Q * Q * a * a;
+  double ff = 4 * kPi * kPi * rho0 * a * a * a / (Q * a * Q * a * sinhVal * sinhVal) *
+              (x * coshVal * sqr - Q * R * cqr * sinhVal);
+  ff += 8 * kPi * rho0 * a * a * a * e_ra / qa2 / qa2;
+  out[i] = ff;
+}
+
 __device__ __forceinline__ double eval_u(const double4* coef, int n, double h, double x) {
   SplineU s{coef, 0.0, h, 1.0 / h, n};
   return spline_eval_smem(s, coef, x);
@@ -580,9 +611,13 @@ cudaError_t build_spline_uniform(const double* d_y, int n, double x0, double h, 
 }
 
 cudaError_t launch_formfac_values(double* d_out, int n, double x0, double h, double rho0,
-                                  double R, double a, cudaStream_t st) {
+                                  double R, double a, cudaStream_t st, int fast) {
   note_launch();
-  k_formfac_values<<<(n + 255) / 256, 256, 0, st>>>(d_out, n, x0, h, rho0, R, a);
+  if (fast)
+    k_formfac_values_fast<<<(n + 255) / 256, 256, 0, st>>>(d_out, n, x0, h, rho0, R, a,
+                                                           std::exp(-R / a));
+  else
+    k_formfac_values<<<(n + 255) / 256, 256, 0, st>>>(d_out, n, x0, h, rho0, R, a);
   return cudaGetLastError();
 }
 
