@@ -608,15 +608,15 @@ def main():
                              f"peak = {pk_kind} bf16 burst; traffic = DRAM bytes per launch "
                              f"from an ncu capture, scaled by rows"},
         "roofline_weights": {
-            "kernel": "k_fast_G + k_fast_sides + k_fast_weights (the projection phase)",
+            "kernel": "k_fast_weights (the projection's node weights and dense rows)",
             "bound": "hbm",
             "achieved": 8.0 * P * rows / (ms_project * 1e-3) / 1e9 if ms_project else None,
             "peak": pk_vals.get("hbm_gbs", 6800.0), "unit": "GB/s",
             "traffic": WEIGHTS_DRAM_BYTES_PER_ROW * rows / nlaunch_contract,
             "note": "algorithmic bytes = the 8 KB per computed row of dense contraction operands "
-                    "written (A1 bf16 hi + lo, A2 FP32) over the phase's time, which also holds "
-                    f"the survival kernel G and the side constants; peak = {pk_kind} copy rate; "
-                    "traffic = k_fast_weights' DRAM bytes per launch from an ncu capture"},
+                    "written (A1 bf16 hi + lo, A2 FP32) over the kernel's time (events around its "
+                    "launch, after the flux tables are joined); peak = "
+                    f"{pk_kind} copy rate; traffic = its DRAM bytes per launch from an ncu capture"},
         "cold_first_init_ms": cold_init_ms,
         "gpu_launches": n_launch,
         "clocks": clk,

@@ -1565,6 +1565,7 @@ int upcg_generator::build_lumi() {
                                n_rep, r0, staged ? nullptr : fnodes.p, 1));
         CK(join_flux_tables());
         part = 2;
+        b = mark();  // the projection span: the node weights and dense rows alone
       }
       CK(launch_fast_project(p, fu0, fh, P, c0, nc, ncp, flnm2.p, c_far,
                              node_flux ? flux.p : nullptr, &ftab, fsides.p,
