@@ -948,6 +948,7 @@ int upcg_generator::build_tables() {
     fk01_ready = true;
     ftab_early = true;
   }
+  CK(cudaEventRecord(ev_join[0], side[0]));  // the form factor -> flux tables chain
   // breakup probability: knots up to 20 fm + margin (the path evaluates the
   // spline at min(b, 20))
   CK(bu_tab.ensure(4 * kBreakupTabMax));
@@ -990,7 +991,6 @@ int upcg_generator::build_tables() {
                   want32 ? fgaa32.p : nullptr, gaa_f ? fta32.p : nullptr));
   }
   CK(cudaEventRecord(ev_gaa, gs));  // the G_AA spline (and its FP32 copy) is complete
-  CK(cudaEventRecord(ev_join[0], side[0]));
   // only inside upcg_init (defer), whose luminosity step joins the chain
   ff_join_pending = defer && ftab_early && fast_tables() && !usePolarizedCS;
   if (!ff_join_pending) CK(cudaStreamWaitEvent(s, ev_join[0], 0));
