@@ -82,7 +82,11 @@ int upcg_set_lumi_cache(upcg_generator* g, int enable);
  * computed the table, -1 if the cache was not used.  Host only. */
 int upcg_lumi_cache_file(upcg_generator* g, char* path, size_t len, int* last_hit);
 /* CUDA stream (cudaStream_t) for every launch of this handle; NULL = the
- * handle's own stream */
+ * handle's own stream.  upcg_init forks its work from this stream onto the
+ * handle's internal streams (one of high priority for its main chain, side
+ * streams for the table chains and samplers) and joins them back into it
+ * before it returns: work queued on the stream before upcg_init precedes
+ * init's, and init's completes before anything queued after it. */
 int upcg_set_stream(upcg_generator* g, void* stream);
 /* Luminosity method: 0 = plain FP64 (default; the reference's quadrature),
  * 1 = fast form (flux tables + tensor-core contraction, <= 1e-4 relative to

@@ -73,6 +73,14 @@ def test_fast_config1_full_grid(ug, oracle_mod):
     assert rtot < FAST_TOL
     t = g.timings()
     assert t["contract_ms"] > 0
+    # the contraction's work: the rows computed, and per row the multiply-adds
+    # over the tiles where the survival kernel minus its constant can be
+    # nonzero -- whole tiles of 64 x 128 or 64 x 256, fewer than the dense
+    # 1024^2 (the tiles below the first node stencil and those where every
+    # azimuth reaches b >= 20 fm are skipped)
+    rows, macs = g.contractWork()
+    assert rows == g.contractRows() > 0
+    assert 0 < macs < 1024 * 1024 and macs % (64 * 128) == 0, macs
     # one cell of each mirror pair y_j = -y_i (i + j = 61 on this grid; left
     # edges equal and opposite to 8 ulps) is computed and the other copied:
     # L(m, -y) = L(m, y).  Pairs whose edges miss the 8-ulp match are both
