@@ -43,6 +43,11 @@ def test_write_then_read(ug, tmp_path, method):
     assert np.array_equal(g2.lumiTable(), lumi1)
     assert g2.totNuclX() == g1.totNuclX()
     assert g2.timings()["lumi_ms"] < 50
+    # the nuclear tables of a cache-hit init are complete when it returns
+    # (the fast form builds G_AA beside the luminosity step it skipped)
+    b = np.linspace(0.0, 20.0, 401)
+    assert np.array_equal(g2.nucProcessCS.spline("gaa", b), g1.nucProcessCS.spline("gaa", b))
+    assert np.array_equal(g2.nucProcessCS.spline("breakup", b), g1.nucProcessCS.spline("breakup", b))
     # the same events from the same table
     a, _ = g1.generateEvents(5000)
     b, _ = g2.generateEvents(5000)

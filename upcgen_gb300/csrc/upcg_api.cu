@@ -584,7 +584,9 @@ struct upcg_generator {
     brk_join_pending = false;
     const bool side_g = survival_on_side;
     survival_on_side = false;
-    return cudaStreamWaitEvent(st(), side_g ? ev_survival : ev_join[1], 0);
+    // without the survival kernel (a cached luminosity), ev_gaa: the G_AA
+    // chain runs after the breakup chain on side[1]
+    return cudaStreamWaitEvent(st(), side_g ? ev_survival : ev_gaa, 0);
   }
   // parts as enqueue_static_samplers'; ev_static (side[2]) covers both once
   // the z part is forked
