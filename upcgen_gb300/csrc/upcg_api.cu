@@ -593,9 +593,10 @@ struct upcg_generator {
   int fork_static_samplers(int parts = 3);
   bool pt_forked = false;
   bool static_pending = false;   // static samplers enqueued on side[2], not yet joined
-  // upcg_init's samplers not enqueued yet: the fast form's luminosity step
-  // enqueues them right after the side constants' launch, so that the host's
-  // launch order puts the projection's kernels ahead of theirs
+  // upcg_init's z samplers not enqueued yet: the fast form's luminosity step
+  // enqueues them just before the contraction's launch (they wait for
+  // ev_static_go, recorded there), so that the projection's kernels go ahead
+  // of theirs and the samplers share the SMs with the contraction
   bool statics_deferred = false;
   cudaEvent_t ev_static_go = nullptr;  // where the deferred samplers start
   bool static_go = false;
