@@ -56,6 +56,28 @@ def test_bad_values_raise(ug):
         g.setParameterValue("BINS_M", "many")
 
 
+@pytest.mark.parametrize("params,match", [
+    ({"MMIN": 10, "MMAX": 5}, "mass range"),
+    ({"PROC_ID": 51, "ALP_MASS": 0.01, "ALP_WIDTH": 0.01}, "mass range"),  # M - 4 Gamma < 0
+    ({"YMIN": 3, "YMAX": -3}, "rapidity range"),
+    ({"YMIN": float("nan")}, "rapidity range"),
+    ({"ZMIN": 1, "ZMAX": -1}, "z range"),
+    ({"SQRTS": 1.0}, "Lorentz factor"),
+    ({"WS_A": 0}, "must be positive"),
+    ({"NUCLEUS_A": 0}, "must be >= 1"),
+    ({"BINS_M": 100000, "BINS_Y": 1000}, "at most"),
+    ({"BINS_Y": 0}, "empty grid"),
+    ({"BREAKUP_MODE": 5}, "BREAKUP_MODE"),
+    ({"PROC_ID": 22}, "PROC_ID 22"),
+])
+def test_bad_configuration_refused_before_device_work(ug, params, match):
+    """Values no table can be built from are refused by upcg_init on the host,
+    before it looks for a device: the same error with or without a GPU."""
+    g = ug.UpcGenerator(params)
+    with pytest.raises(ug.UpcgError, match=match):
+        g.init()
+
+
 def test_compute_without_gpu_fails_loudly(ug):
     import torch
     if torch.cuda.is_available():

@@ -98,6 +98,9 @@ const int kNQ2 = 1000000;
 // cubic spline error below 1e-9 of F; the Q(w, b) table and the photon-pT
 // spectra are its only users there)
 const int kNQ2Fast = 65536;
+// largest (m, y) or (m, z) table a handle builds: 2^24 cells (138 times the
+// 1001 x 121 grid), so that every per-cell index stays far inside int range
+const int kMaxGridCells = 1 << 24;
 
 template <class T>
 struct DBuf {
@@ -188,8 +191,21 @@ int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid, int fu
   DBuf<float> a2, part, nodes;
   DBuf<int4> items;
   DBuf<unsigned> err;
-  cudaStream_t s;
-  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  // the private stream and the timing events are released on every return
+  struct Owned {
+    cudaStream_t s = nullptr;
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    ~Owned() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+      if (s) cudaStreamDestroy(s);
+    }
+  } own;
+  CK(cudaStreamCreateWithFlags(&own.s, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&own.e[0]));
+  CK(cudaEventCreate(&own.e[1]));
+  cudaStream_t s = own.s;
+  cudaEvent_t e0 = own.e[0], e1 = own.e[1];
   CK(g.ensure((size_t)P * P));
   CK(part.ensure((size_t)rows * (P / 128)));
   CK(err.ensure(1));
@@ -214,26 +230,21 @@ int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid, int fu
       for (int nt = 0; nt < P / tbn; ++nt) it.push_back(make_int4(mt, nt, 0, 128));
     CK(items.ensure(it.size()));
     CK(cudaMemcpyAsync(items.p, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
     float ms = 0;
     for (int rep = 0; rep < 3; ++rep) {  // warm-up, then the best of two
-      cudaEventRecord(e0, s);
+      CK(cudaEventRecord(e0, s));
       if (fused)
         CK(launch_contract_fused(g.p, g.p, 1, rows, P, items.p, (int)it.size(), nodes.p, part.p,
                                  err.p, sh, *grid, s));
       else
         CK(launch_contract_pers(a.p, a.p, g.p, g.p, 1, rows, P, items.p, (int)it.size(), a2.p,
                                 part.p, err.p, sh, *grid, s));
-      cudaEventRecord(e1, s);
+      CK(cudaEventRecord(e1, s));
       CK(cudaEventSynchronize(e1));
       float m = 0;
-      cudaEventElapsedTime(&m, e0, e1);
+      CK(cudaEventElapsedTime(&m, e0, e1));
       if (rep == 1 || (rep == 2 && m < ms)) ms = m;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     t[sh] = ms;
     if (ms < best) {
       best = ms;
@@ -242,7 +253,6 @@ int contract_plan(int rows_pad, int nvalid, int P, int* shape, int* grid, int fu
   }
   unsigned herr = 0;
   CK(cudaMemcpy(&herr, err.p, 4, cudaMemcpyDeviceToHost));
-  cudaStreamDestroy(s);
   if (herr) return fail(UPCG_ERR_CUDA, "contraction autotune timed out (code %u)", herr);
   (void)nvalid;
   std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -505,6 +515,7 @@ struct upcg_generator {
 
   int set_param(const std::string& k, const std::string& v);
   int setup_process();
+  int check_config();
   // vector mesons: the decay-angle draws of the last events all ended
   int vm_check() {
     if (!isVM) return UPCG_OK;
@@ -723,6 +734,32 @@ int upcg_generator::setup_process() {
   return fail(UPCG_ERR_PROCESS, "PROC_ID %d is not on the two-photon luminosity path", procID);
 }
 
+// The process overrides, then the values no table can be built from.  The
+// reference reads these keys unchecked (src/UpcGenerator.cpp:183-305); here a
+// NaN or a reversed range would reach the kernels' index arithmetic, so it is
+// refused on the host before any device work.
+int upcg_generator::check_config() {
+  const int rc = setup_process();
+  if (rc) return rc;
+  if (nm < 1 || ny < 1 || nz < 1) return fail(UPCG_ERR_ARG, "empty grid");
+  if ((int64_t)nm * ny > kMaxGridCells || (int64_t)nm * nz > kMaxGridCells)
+    return fail(UPCG_ERR_SIZE, "grid of %d x %d x %d bins: at most %d (m, y) or (m, z) cells", nm,
+                ny, nz, kMaxGridCells);
+  if (!(mmin > 0.) || !(mmax > mmin) || !std::isfinite(mmax))
+    return fail(UPCG_ERR_ARG, "mass range [%g, %g] GeV: 0 < MMIN < MMAX needed", mmin, mmax);
+  if (!(ymax > ymin) || !std::isfinite(ymin) || !std::isfinite(ymax))
+    return fail(UPCG_ERR_ARG, "rapidity range [%g, %g]: YMIN < YMAX needed", ymin, ymax);
+  if (!(zmax > zmin) || !std::isfinite(zmin) || !std::isfinite(zmax))
+    return fail(UPCG_ERR_ARG, "z range [%g, %g]: ZMIN < ZMAX needed", zmin, zmax);
+  if (!(g1 > 1.) || !(g2 > 1.) || !std::isfinite(g1) || !std::isfinite(g2))
+    return fail(UPCG_ERR_ARG, "SQRTS %g GeV: the beams' Lorentz factor must exceed 1", sqrts);
+  if (!(R > 0.) || !(a > 0.) || !std::isfinite(R) || !std::isfinite(a))
+    return fail(UPCG_ERR_ARG, "WS_R %g, WS_A %g: both must be positive", R, a);
+  if (Z < 1 || A < 1) return fail(UPCG_ERR_ARG, "NUCLEUS_Z %d, NUCLEUS_A %d: both must be >= 1", Z, A);
+  if (breakupMode < 1 || breakupMode > 4) return fail(UPCG_ERR_ARG, "BREAKUP_MODE must be 1..4");
+  return UPCG_OK;
+}
+
 LumiParams upcg_generator::lumi_params() const {
   LumiParams p{};
   p.nm = nm; p.ny = ny;
@@ -857,7 +894,7 @@ double ws_rho_host(double R, double a, int A) {
 }  // namespace
 
 int upcg_generator::build_tables() {
-  int rc = setup_process();
+  int rc = check_config();
   if (rc) return rc;
   cudaStream_t s = st();
   CK(side_streams());
@@ -2214,11 +2251,10 @@ int upcg_set_lumi_method(upcg_generator* g, int method) {
 
 int upcg_init(upcg_generator* g) {
   if (!g) return fail(UPCG_ERR_ARG, "null handle");
+  if (const int rc = g->check_config()) return rc;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(UPCG_ERR_CUDA, "no CUDA device visible");
-  if (g->nm < 1 || g->ny < 1 || g->nz < 1) return fail(UPCG_ERR_ARG, "empty grid");
-  if (g->breakupMode < 1 || g->breakupMode > 4) return fail(UPCG_ERR_ARG, "BREAKUP_MODE must be 1..4");
   if (!g->hstat && cudaMallocHost(&g->hstat, sizeof(upcg_generator::HostStatus)) != cudaSuccess)
     return fail(UPCG_ERR_CUDA, "pinned status block");
   g->defer = true;  // one host synchronisation, at the end (complete_deferred)
