@@ -263,10 +263,20 @@ class FluxSurrogate:
         _check(self._L.upcg_mlp_train(self._h, int(epochs), int(batch), C.c_float(lr), C.byref(loss)))
         return loss.value
 
-    def gradients(self, x, y, w):
+    @staticmethod
+    def _inputs(x, n=None):
+        """(n, 5) float32 network inputs; the library reads 5 floats per point."""
         x = np.ascontiguousarray(x, dtype=np.float32)
-        y = np.ascontiguousarray(y, dtype=np.float32)
-        w = np.ascontiguousarray(w, dtype=np.float32)
+        if x.ndim != 2 or x.shape[1] != 5 or (n is not None and x.shape[0] != n):
+            raise ValueError(f"inputs must have shape ({'n' if n is None else n}, 5), got {x.shape}")
+        return x
+
+    def gradients(self, x, y, w):
+        y = np.ascontiguousarray(y, dtype=np.float32).ravel()
+        w = np.ascontiguousarray(w, dtype=np.float32).ravel()
+        if w.size != y.size:
+            raise ValueError(f"{y.size} labels but {w.size} weights")
+        x = self._inputs(x, y.size)
         g = np.zeros(self.N_PARAMS, dtype=np.float32)
         loss = C.c_double()
         _check(self._L.upcg_mlp_gradients(self._h, _p(x), _p(y), _p(w), len(y), _p(g), g.size,
@@ -283,7 +293,7 @@ class FluxSurrogate:
         _check(self._L.upcg_mlp_set_params(self._h, _p(p), p.size))
 
     def predict(self, x):
-        x = np.ascontiguousarray(x, dtype=np.float32)
+        x = self._inputs(x)
         y = np.zeros(len(x), dtype=np.float32)
         _check(self._L.upcg_mlp_predict(self._h, _p(x), len(x), _p(y)))
         return y
@@ -476,6 +486,8 @@ class UpcGenerator:
     def setLumiTable(self, table, table2=None):
         t = _arr(table).ravel()
         t2 = _arr(table2).ravel() if table2 is not None else None
+        if t2 is not None and t2.size != t.size:
+            raise ValueError(f"the two tables differ in size ({t.size}, {t2.size})")
         _check(self._L.upcg_set_lumi_table(self._h, _p(t), t.size, _p(t2) if t2 is not None else None))
 
     def setLumiTableDevice(self, ptr, n, ptr2=None):
