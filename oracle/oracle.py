@@ -2,8 +2,9 @@
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` import this module, and only as the checker / the timed CPU
-restatement of the reference.  See ``upcg_oracle.h`` for the parity status
-("parity unpinned" end to end: the reference needs ROOT and GSL).
+restatement of the reference.  ``upcg_oracle.h`` states what it is pinned
+to: the reference's own src/UpcCrossSection.cpp compiled here against
+stand-in GSL / ROOT headers (bit-exact), and scipy for the primitives.
 """
 import ctypes as C
 import os

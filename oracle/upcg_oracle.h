@@ -7,14 +7,18 @@
  * the checker for the CUDA library, never part of it.
  *
  * Parity status: the reference needs ROOT and GSL, neither of which is
- * available, so it cannot be built or run here.  The restatement is pinned
- * (a) primitive by primitive against scipy (K0/K1/J1, QUADPACK via
- * scipy.integrate.quad, natural cubic splines), (b) for the elementary
- * gamma-gamma cross sections, bit for bit against the reference's own
- * UpcTwoPhotonDilep.cpp / UpcTwoPhotonALP.cpp compiled from its sources, and
- * (c) against an independent numpy/scipy restatement of the luminosity for a
- * set of cells (tests/golden).  End-to-end parity with upcgen itself is
- * therefore "parity unpinned".
+ * available, so its CMake project cannot be built here.  The restatement is
+ * pinned (a) bit for bit against the reference's own src/UpcCrossSection.cpp
+ * and the process classes it creates, compiled from their sources against
+ * stand-in GSL / ROOT headers (oracle/refshim/) whose luminosity-path calls
+ * run this oracle's restated primitives (oracle/ref_cs_shim.cpp; fixture
+ * tests/golden/ref_cs.json): rho0, G_AA, the form factor, both fluxes, the
+ * breakup probability, luminosity cells and calcPhotonFlux on 8
+ * configurations; (b) for the elementary gamma-gamma cross sections, bit for
+ * bit against UpcTwoPhotonDilep.cpp / UpcTwoPhotonALP.cpp compiled as they
+ * are; (c) the primitives themselves (K0/K1/J1, QAGS, natural cubic splines)
+ * against scipy's independent implementations, not against GSL / ROOT,
+ * which are absent.
  */
 #ifndef UPCG_ORACLE_H_
 #define UPCG_ORACLE_H_
