@@ -14,6 +14,10 @@
   into ``oracle/_ref/libupcref_cs.so``.  This pins the oracle's restatement of
   calcTwoPhotonLumi, fluxForm, calcBreakupProb, prepareGAA, calcPhotonFlux ...
   to the reference's own source text.
+* ``build_ref_gen()`` adds the reference's ``src/UpcGenerator.cpp`` to those
+  units, with ``ref_gen_shim.cpp``, into ``oracle/_ref/libupcref_gen.so``: the
+  reference's own init and event loop, which pin the oracle's samplers and
+  event generation.
 
 ``-ffp-contract=off`` keeps the x86 and aarch64 builds bit-identical (gcc
 contracts a*b+c into FMAs by default on aarch64).
@@ -29,7 +33,7 @@ REF_SO = os.path.join(REF_DIR, "libupcref_elem.so")
 REFERENCE_ROOT = os.environ.get("UPCG_REFERENCE_ROOT", "/root/reference")
 
 _SOURCES = ["oracle_cs.cpp", "oracle_gen.cpp"]
-_HEADERS = ["oracle_num.hpp", "oracle_ctx.hpp", "upcg_oracle.h"]
+_HEADERS = ["oracle_num.hpp", "oracle_ctx.hpp", "oracle_gen_prims.hpp", "upcg_oracle.h"]
 _FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
 
 
@@ -95,7 +99,37 @@ def build_ref_cs(force=False):
     return REF_CS_SO
 
 
+REF_GEN_SO = os.path.join(REF_DIR, "libupcref_gen.so")
+
+
+def build_ref_gen(force=False):
+    """Compile the reference's event generator (src/UpcGenerator.cpp with the
+    units of build_ref_cs) against refshim/ with ref_gen_shim.cpp into
+    oracle/_ref/libupcref_gen.so; None if the reference sources are absent.
+    Pythia is off, as in a reference build without it."""
+    src = os.path.join(REFERENCE_ROOT, "src")
+    inc = os.path.join(REFERENCE_ROOT, "include")
+    units = [os.path.join(src, u) for u in ["UpcGenerator.cpp"] + _REF_CS_UNITS]
+    if not all(os.path.exists(u) for u in units):
+        return REF_GEN_SO if os.path.exists(REF_GEN_SO) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    shim_dir = os.path.join(HERE, "refshim")
+    shim = os.path.join(HERE, "ref_gen_shim.cpp")
+    deps = units + [shim, os.path.join(HERE, "oracle_num.hpp"),
+                    os.path.join(HERE, "oracle_gen_prims.hpp")]
+    deps += [os.path.join(shim_dir, f) for f in os.listdir(shim_dir) if f.endswith(".h")]
+    deps += [os.path.join(shim_dir, "gsl", f) for f in os.listdir(os.path.join(shim_dir, "gsl"))]
+    if force or _stale(REF_GEN_SO, deps):
+        cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+               "-w", '-DCROSS_SEC_DIR="/nonexistent"', "-I", shim_dir, "-I", inc, *units, shim,
+               "-lpthread", "-o", REF_GEN_SO + ".tmp"]
+        subprocess.run(cmd, check=True)
+        os.replace(REF_GEN_SO + ".tmp", REF_GEN_SO)
+    return REF_GEN_SO
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
     print(build_ref_cs(force=True))
+    print(build_ref_gen(force=True))

@@ -3,13 +3,15 @@
 // Restates include/UpcSampler.h:37-142 (GSL histogram PDFs),
 // src/UpcGenerator.cpp:715-889 (generateEvent / generateEvents),
 // src/UpcCrossSection.cpp:1021-1074 (getPhotonPt / getPairMomentum) and the
-// ROOT vector algebra they use (TLorentzVector boosts, TVector3::RotateUz).
-// The random streams follow the reference's engines: GSL's mt19937
-// (std::mt19937, same initialisation; gsl_rng_uniform = x / 2^32) for the
-// samplers -- one engine per sampler, all seeded with SEED as in
-// src/UpcGenerator.cpp:688-700 -- and ROOT's TRandomMT64 (std::mt19937_64,
-// x / 2^64) for gRandom.  The two uniforms of the 2-D sampler are drawn in
-// argument order (r1 first); the reference leaves that order to the compiler.
+// ROOT vector algebra they use (TLorentzVector boosts, TVector3::RotateUz),
+// on the engines and primitives of oracle_gen_prims.hpp.  The random streams
+// follow the reference's engines: GSL's mt19937 for the samplers -- one
+// engine per sampler, all seeded with SEED as in
+// src/UpcGenerator.cpp:688-700 -- and ROOT's TRandomMT64 for gRandom.  The
+// two uniforms of the 2-D sampler are drawn as GCC orders the reference's two
+// argument calls (right to left).  The event stream is bit-exact with the
+// reference's own src/UpcGenerator.cpp compiled here (ref_gen_shim.cpp,
+// tests/test_oracle_pins.py).
 #include <cmath>
 #include <cstdint>
 #include <random>
@@ -17,97 +19,12 @@
 #include <vector>
 
 #include "oracle_ctx.hpp"
+#include "oracle_gen_prims.hpp"
 #include "upcg_oracle.h"
 
 namespace uo {
 
 namespace {
-
-struct GslUniform {  // gsl_rng_default (mt19937) + gsl_rng_uniform
-  std::mt19937 e;
-  explicit GslUniform(unsigned long s) : e((uint32_t)(s == 0 ? 4357 : s)) {}
-  double operator()() { return e() / 4294967296.0; }
-};
-
-struct RootMT64 {  // TRandomMT64::Rndm / Uniform
-  std::mt19937_64 e;
-  explicit RootMT64(uint64_t s) : e(s) {}
-  double rndm() {
-    for (;;) {
-      uint64_t x = e();
-      if (x != 0) return x * (1.0 / 18446744073709551616.0);
-    }
-  }
-  double uniform(double lo, double hi) { return lo + (hi - lo) * rndm(); }
-};
-
-// gsl_histogram_pdf_init: running mean, then cumulative (bin/mean)/n.
-std::vector<double> gsl_cdf(const double* bins, size_t n) {
-  std::vector<double> sum(n + 1);
-  double mean = 0;
-  for (size_t i = 0; i < n; i++) mean += (bins[i] - mean) / ((double)(i + 1));
-  double s = 0;
-  sum[0] = 0;
-  for (size_t i = 0; i < n; i++) {
-    s += (bins[i] / mean) / n;
-    sum[i + 1] = s;
-  }
-  return sum;
-}
-
-// find(): i with sum[i] <= r < sum[i+1]; -1 when r is outside [sum[0], sum[n]).
-long gsl_find(const std::vector<double>& sum, double r) {
-  const size_t n = sum.size() - 1;
-  if (r < sum[0] || r >= sum[n]) return -1;
-  size_t lo = 0, hi = n;
-  while (hi - lo > 1) {
-    size_t mid = (hi + lo) / 2;
-    if (r >= sum[mid]) lo = mid; else hi = mid;
-  }
-  return (long)lo;
-}
-
-struct Vec4 { double x, y, z, t; };
-
-void boost(Vec4& p, double bx, double by, double bz) {  // TLorentzVector::Boost
-  double b2 = bx * bx + by * by + bz * bz;
-  double gamma = 1.0 / std::sqrt(1.0 - b2);
-  double bp = bx * p.x + by * p.y + bz * p.z;
-  double gamma2 = b2 > 0 ? (gamma - 1.0) / b2 : 0.0;
-  double x = p.x + gamma2 * bp * bx + gamma * bx * p.t;
-  double y = p.y + gamma2 * bp * by + gamma * by * p.t;
-  double z = p.z + gamma2 * bp * bz + gamma * bz * p.t;
-  p.t = gamma * (p.t + bp);
-  p.x = x; p.y = y; p.z = z;
-}
-
-void rotate_uz(Vec4& p, double u1, double u2, double u3) {  // TVector3::RotateUz
-  double up = u1 * u1 + u2 * u2;
-  if (up) {
-    up = std::sqrt(up);
-    double px = p.x, py = p.y, pz = p.z;
-    p.x = (u1 * u3 * px - u2 * py + u1 * up * pz) / up;
-    p.y = (u2 * u3 * px + u1 * py + u2 * up * pz) / up;
-    p.z = (u3 * u3 * px - px + u3 * up * pz) / up;
-  } else if (u3 < 0.) {
-    p.x = -p.x;
-    p.z = -p.z;
-  }
-}
-
-double pt_of(const Vec4& p) { return std::sqrt(p.x * p.x + p.y * p.y); }
-
-double eta_of(const Vec4& p) {  // TVector3::PseudoRapidity
-  double mag = std::sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
-  double ct = mag == 0.0 ? 1.0 : p.z / mag;
-  if (ct * ct < 1) return -0.5 * std::log((1.0 - ct) / (1.0 + ct));
-  if (p.z == 0) return 0;
-  return p.z > 0 ? 10e10 : -10e10;
-}
-
-Vec4 set_vect_m(double x, double y, double z, double m) {
-  return Vec4{x, y, z, std::sqrt(x * x + y * y + z * z + m * m)};
-}
 
 // getPhotonPt's cached 5000-bin TH1D + TH1::GetRandom (src/UpcCrossSection.cpp:1021-1051).
 struct PhotonPt {
@@ -123,26 +40,16 @@ struct PhotonPt {
     auto it = cache.find(key);
     if (it == cache.end()) {
       double ereds = (ePhot * ePhot) / (c.gtot * c.gtot);
-      std::vector<double> integ(nbins + 1, 0.0);
+      std::vector<double> prob(nbins);
       for (int bin = 1; bin <= nbins; bin++) {
         double pt = 6. * hc / c.R / nbins * bin;
         double arg = pt * pt + ereds;
         double ff = c.formfac.eval(arg);
-        double prob = (ff * ff) * pt * pt * pt / (pi2x4 * arg * arg);
-        integ[bin] = integ[bin - 1] + prob;
+        prob[bin - 1] = (ff * ff) * pt * pt * pt / (pi2x4 * arg * arg);
       }
-      const double tot = integ[nbins];
-      for (int bin = 1; bin <= nbins; bin++) integ[bin] /= tot;
-      it = cache.emplace(key, std::move(integ)).first;
+      it = cache.emplace(key, th1_integral(prob.data(), nbins)).first;
     }
-    const std::vector<double>& I = it->second;
-    double r1 = rng.rndm();
-    // TMath::BinarySearch over I[0..nbins-1]
-    long ib = (long)(std::lower_bound(I.begin(), I.begin() + nbins, r1) - I.begin());
-    if (!(ib != nbins && I[ib] == r1)) ib -= 1;
-    const double w = hi / nbins;
-    double x = ib * w;
-    if (r1 > I[ib]) x += w * (r1 - I[ib]) / (I[ib + 1] - I[ib]);
+    const double x = th1_sample(it->second, nbins, 0., hi, rng.rndm());
     if (cache.size() > 30000) cache.clear();
     return x;
   }
@@ -197,7 +104,12 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
   int64_t evt = 0, rej = 0;
   while (evt < nevents) {
     // (y, m) from the 2-D pdf (gsl_histogram2d_pdf_sample)
-    double r1 = rng2(), r2 = rng2();
+    // gsl_histogram2d_pdf_sample(hpdf, gsl_rng_uniform(rng), gsl_rng_uniform(rng), ...)
+    // (include/UpcSampler.h:120): C++ leaves the order of the two draws to
+    // the compiler; GCC evaluates the arguments right to left, so r2 (the
+    // position inside the mass bin) is drawn first
+    double r2 = rng2();
+    double r1 = rng2();
     if (r2 == 1.0) r2 = 0.0;
     if (r1 == 1.0) r1 = 0.0;
     long k = gsl_find(sum2, r1);
@@ -298,10 +210,10 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
         double vz = pMag * std::cos(theta);
         d0 = set_vect_m(-vx, -vy, -vz, c.mDght);
         d1 = set_vect_m(vx, vy, vz, c.mDght);
-        double pm = std::sqrt(pp.x * pp.x + pp.y * pp.y + pp.z * pp.z);
-        double u1 = pm > 0 ? pp.x / pm : 0, u2 = pm > 0 ? pp.y / pm : 0, u3 = pm > 0 ? pp.z / pm : 0;
-        rotate_uz(d0, u1, u2, u3);
-        rotate_uz(d1, u1, u2, u3);
+        double u[3];
+        unit3(pp.x, pp.y, pp.z, u);
+        rotate_uz(d0, u[0], u[1], u[2]);
+        rotate_uz(d1, u[0], u[1], u[2]);
         boost(d0, bx, by, bz);
         boost(d1, bx, by, bz);
       }
@@ -334,8 +246,7 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
         if (e < c.minEta || e > c.maxEta) pass = false;
       }
       if (pass) {  // twoPartDecayUniform (src/UpcGenerator.cpp:526-561)
-        double mag = std::sqrt(std::max(0.0, pp.t * pp.t - (pp.x * pp.x + pp.y * pp.y + pp.z * pp.z)));
-        double e1 = mag / 2.;
+        double e1 = mag_of(pp) / 2.;
         double p1 = std::sqrt(e1 * e1);
         double phi1 = groot.uniform(0., 2. * M_PI);
         double cost1 = groot.uniform(-1., 1.);
@@ -345,10 +256,10 @@ extern "C" int uo_generate(uo_ctx* h, const double* cs_ym, const double* cs_zm,
         double vz = p1 * std::cos(th1);
         d0 = set_vect_m(-vx, -vy, -vz, 0.);
         d1 = set_vect_m(vx, vy, vz, 0.);
-        double pm = std::sqrt(pp.x * pp.x + pp.y * pp.y + pp.z * pp.z);
-        double u1 = pm > 0 ? pp.x / pm : 0, u2 = pm > 0 ? pp.y / pm : 0, u3 = pm > 0 ? pp.z / pm : 0;
-        rotate_uz(d0, u1, u2, u3);
-        rotate_uz(d1, u1, u2, u3);
+        double u[3];
+        unit3(pp.x, pp.y, pp.z, u);
+        rotate_uz(d0, u[0], u[1], u[2]);
+        rotate_uz(d1, u[0], u[1], u[2]);
         boost(d0, bx, by, bz);
         boost(d1, bx, by, bz);
       }

@@ -11,18 +11,30 @@
 // Abramowitz & Stegun 9.8.7/9.8.8 polynomials the oracle restates).  So a pin
 // built on them checks the reference's own code around those calls -- node
 // layouts, loops, clamps, branch conditions -- against the oracle's
-// restatement of it.  Everything else (histograms, files, graphs, TF1, 2-D
-// splines, random numbers) only has to compile: calling it stops the process
-// with a message, and no pin calls it.
+// restatement of it.
+//
+// For the generator pin (src/UpcGenerator.cpp with ref_gen_shim.cpp) the
+// event loop's calls are real too, backed by oracle_gen_prims.hpp: GSL's
+// mt19937 and histogram PDFs (gsl_rng, gsl_histogram[2d]_pdf), ROOT's
+// TRandomMT64 behind gRandom, TLorentzVector / TVector3 algebra, TH1D with
+// GetRandom, and TH2D histograms kept in an in-memory stand-in of the
+// luminosity's ROOT file (TFile, gSystem->AccessPathName), so that
+// UpcCrossSection::prepareTwoPhotonLumi / calcNucCrossSectionYM run as
+// written.  Everything else (graphs, TF1, 2-D splines, trees) only has to
+// compile: calling it stops the process with a message, and no pin calls it.
 #pragma once
 
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
+#include "../oracle_gen_prims.hpp"
 #include "../oracle_num.hpp"
 
 namespace refshim {
@@ -123,6 +135,117 @@ inline double gsl_spline2d_eval(const gsl_spline2d*, double, double, gsl_interp_
 }
 inline void gsl_spline2d_free(gsl_spline2d*) {}
 
+// GSL random numbers (gsl_rng_default = mt19937) and histogram PDFs
+struct gsl_rng_type {
+  const char* name;
+};
+inline const gsl_rng_type gsl_rng_mt19937_type{"mt19937"};
+inline const gsl_rng_type* gsl_rng_default = &gsl_rng_mt19937_type;
+struct gsl_rng {
+  uo::GslUniform u;
+};
+inline gsl_rng* gsl_rng_alloc(const gsl_rng_type* t) {
+  if (t != gsl_rng_default) refshim::unavailable("a GSL generator other than mt19937");
+  return new gsl_rng();
+}
+inline void gsl_rng_set(gsl_rng* r, unsigned long seed) { r->u = uo::GslUniform(seed); }
+inline double gsl_rng_uniform(gsl_rng* r) { return r->u(); }
+inline void gsl_rng_free(gsl_rng* r) { delete r; }
+
+struct gsl_histogram {
+  size_t n;
+  double* range;
+  double* bin;
+};
+inline gsl_histogram* gsl_histogram_alloc(size_t n) {
+  auto* h = new gsl_histogram{n, new double[n + 1](), new double[n]()};
+  return h;
+}
+inline int gsl_histogram_set_ranges(gsl_histogram* h, const double* range, size_t size) {
+  if (size != h->n + 1) refshim::unavailable("gsl_histogram_set_ranges of another size");
+  for (size_t i = 0; i < size; ++i) h->range[i] = range[i];
+  return 0;
+}
+inline void gsl_histogram_free(gsl_histogram* h) {
+  delete[] h->range;
+  delete[] h->bin;
+  delete h;
+}
+struct gsl_histogram_pdf {
+  size_t n;
+  std::vector<double> range, sum;
+};
+inline gsl_histogram_pdf* gsl_histogram_pdf_alloc(size_t n) { return new gsl_histogram_pdf{n, {}, {}}; }
+inline int gsl_histogram_pdf_init(gsl_histogram_pdf* p, const gsl_histogram* h) {
+  for (size_t i = 0; i < h->n; ++i)
+    if (h->bin[i] < 0) return GSL_EDOM;
+  p->range.assign(h->range, h->range + h->n + 1);
+  p->sum = uo::gsl_cdf(h->bin, h->n);
+  return 0;
+}
+inline double gsl_histogram_pdf_sample(const gsl_histogram_pdf* p, double r) {
+  if (r == 1.0) r = 0.0;
+  const long i = uo::gsl_find(p->sum, r);
+  if (i < 0) refshim::unavailable("gsl_histogram_pdf_sample outside the pdf");
+  const double delta = (r - p->sum[i]) / (p->sum[i + 1] - p->sum[i]);
+  return p->range[i] + delta * (p->range[i + 1] - p->range[i]);
+}
+inline void gsl_histogram_pdf_free(gsl_histogram_pdf* p) { delete p; }
+
+struct gsl_histogram2d {
+  size_t nx, ny;
+  double* xrange;
+  double* yrange;
+  double* bin;
+};
+inline gsl_histogram2d* gsl_histogram2d_alloc(size_t nx, size_t ny) {
+  return new gsl_histogram2d{nx, ny, new double[nx + 1](), new double[ny + 1](),
+                             new double[nx * ny]()};
+}
+inline int gsl_histogram2d_set_ranges(gsl_histogram2d* h, const double* xr, size_t xs,
+                                      const double* yr, size_t ys) {
+  if (xs != h->nx + 1 || ys != h->ny + 1)
+    refshim::unavailable("gsl_histogram2d_set_ranges of another size");
+  for (size_t i = 0; i < xs; ++i) h->xrange[i] = xr[i];
+  for (size_t i = 0; i < ys; ++i) h->yrange[i] = yr[i];
+  return 0;
+}
+inline void gsl_histogram2d_free(gsl_histogram2d* h) {
+  delete[] h->xrange;
+  delete[] h->yrange;
+  delete[] h->bin;
+  delete h;
+}
+struct gsl_histogram2d_pdf {
+  size_t nx, ny;
+  std::vector<double> xrange, yrange, sum;
+};
+inline gsl_histogram2d_pdf* gsl_histogram2d_pdf_alloc(size_t nx, size_t ny) {
+  return new gsl_histogram2d_pdf{nx, ny, {}, {}, {}};
+}
+inline int gsl_histogram2d_pdf_init(gsl_histogram2d_pdf* p, const gsl_histogram2d* h) {
+  const size_t n = h->nx * h->ny;
+  for (size_t i = 0; i < n; ++i)
+    if (h->bin[i] < 0) return GSL_EDOM;
+  p->xrange.assign(h->xrange, h->xrange + h->nx + 1);
+  p->yrange.assign(h->yrange, h->yrange + h->ny + 1);
+  p->sum = uo::gsl_cdf(h->bin, n);
+  return 0;
+}
+inline int gsl_histogram2d_pdf_sample(const gsl_histogram2d_pdf* p, double r1, double r2,
+                                      double* x, double* y) {
+  if (r2 == 1.0) r2 = 0.0;
+  if (r1 == 1.0) r1 = 0.0;
+  const long k = uo::gsl_find(p->sum, r1);
+  if (k < 0) refshim::unavailable("gsl_histogram2d_pdf_sample outside the pdf");
+  const long i = k / (long)p->ny, j = k - i * (long)p->ny;
+  const double delta = (r1 - p->sum[k]) / (p->sum[k + 1] - p->sum[k]);
+  *x = p->xrange[i] + delta * (p->xrange[i + 1] - p->xrange[i]);
+  *y = p->yrange[j] + r2 * (p->yrange[j + 1] - p->yrange[j]);
+  return 0;
+}
+inline void gsl_histogram2d_pdf_free(gsl_histogram2d_pdf* p) { delete p; }
+
 // ----------------------------------------------------------------- ROOT --
 typedef int Int_t;
 typedef double Double_t;
@@ -194,6 +317,7 @@ class TObject {
   enum { kIsSortedX = 1 };
   void SetBit(unsigned, bool = true) {}
   virtual int Write(const char* = nullptr, int = 0, int = 0) { refshim::unavailable("Write"); }
+  virtual TObject* Clone(const char* = "") const { refshim::unavailable("Clone"); }
 };
 
 class TAxis {
@@ -210,55 +334,146 @@ class TAxis {
 };
 
 class TDirectory;
+inline double refshim_rndm();  // gRandom->Rndm(), defined with TRandom below
+
+// Histograms on uniform bins with ROOT's bin numbering (0 underflow, n + 1
+// overflow; 2-D global bin = bx + (nx + 2) by).  What the luminosity path and
+// the event loop call is real: contents, Clone, Write into the current
+// stand-in file, and the 1-D GetRandom (TH1::ComputeIntegral + GetRandom on
+// gRandom, oracle_gen_prims.hpp).
 class TH1 : public TObject {
  public:
   TH1() = default;
+  static void AddDirectory(bool = true) {}
   void SetDirectory(TDirectory*) {}
-  int GetNbinsX() const { refshim::unavailable("histograms"); }
-  int GetNbinsY() const { refshim::unavailable("histograms"); }
-  TAxis* GetXaxis() { refshim::unavailable("histograms"); }
-  TAxis* GetYaxis() { refshim::unavailable("histograms"); }
-  double GetBinContent(int) const { refshim::unavailable("histograms"); }
-  double GetBinContent(int, int) const { refshim::unavailable("histograms"); }
-  void SetBinContent(int, double) { refshim::unavailable("histograms"); }
-  void SetBinContent(int, int, double) { refshim::unavailable("histograms"); }
-  double GetRandom() { refshim::unavailable("histograms"); }
+  const char* GetName() const { return name_.c_str(); }
+  int GetNbinsX() const { return nx_; }
+  int GetNbinsY() const { return ny_; }
+  TAxis* GetXaxis() { refshim::unavailable("histogram axes"); }
+  TAxis* GetYaxis() { refshim::unavailable("histogram axes"); }
+  double GetBinContent(int bin) const { return a_.at(bin); }
+  double GetBinContent(int bx, int by) const { return a_.at(bx + (nx_ + 2) * by); }
+  void SetBinContent(int bin, double v) {
+    a_.at(bin) = v;
+    integral_.clear();
+  }
+  void SetBinContent(int bx, int by, double v) {
+    a_.at(bx + (nx_ + 2) * by) = v;
+    integral_.clear();
+  }
+  double GetRandom() {
+    if (ny_ != 0) refshim::unavailable("GetRandom of a 2-D histogram");
+    if (integral_.empty()) integral_ = uo::th1_integral(a_.data() + 1, nx_);
+    return uo::th1_sample(integral_, nx_, xmin_, xmax_, refshim_rndm());
+  }
   double Interpolate(double) { refshim::unavailable("histograms"); }
   double Interpolate(double, double) { refshim::unavailable("histograms"); }
   int FindBin(double) { refshim::unavailable("histograms"); }
   int FindBin(double, double) { refshim::unavailable("histograms"); }
   int Fill(double) { refshim::unavailable("histograms"); }
   int Fill(double, double) { refshim::unavailable("histograms"); }
-  TObject* Clone(const char* = "") const { refshim::unavailable("histograms"); }
   void Scale(double) { refshim::unavailable("histograms"); }
+  int Write(const char* = nullptr, int = 0, int = 0) override;
+
+ protected:
+  void book(const char* name, int nx, double x0, double x1, int ny, double y0, double y1) {
+    name_ = name ? name : "";
+    nx_ = nx, ny_ = ny, xmin_ = x0, xmax_ = x1, ymin_ = y0, ymax_ = y1;
+    a_.assign(ny == 0 ? nx + 2 : (size_t)(nx + 2) * (ny + 2), 0.0);
+  }
+  std::string name_;
+  int nx_ = 0, ny_ = 0;  // ny_ = 0: 1-D
+  double xmin_ = 0, xmax_ = 0, ymin_ = 0, ymax_ = 0;
+  std::vector<double> a_;
+  std::vector<double> integral_;
 };
 class TH1D : public TH1 {
  public:
   TH1D() = default;
-  TH1D(const char*, const char*, int, double, double) {}
-  TH1D(const char*, const char*, int, const double*) {}
+  TH1D(const char* name, const char*, int n, double x0, double x1) { book(name, n, x0, x1, 0, 0, 0); }
+  TH1D(const char*, const char*, int, const double*) { refshim::unavailable("variable bins"); }
+  TObject* Clone(const char* name = "") const override {
+    auto* c = new TH1D(*this);
+    if (name && *name) c->name_ = name;
+    return c;
+  }
 };
 class TH2D : public TH1 {
  public:
   TH2D() = default;
-  TH2D(const char*, const char*, int, double, double, int, double, double) {}
+  TH2D(const char* name, const char*, int nx, double x0, double x1, int ny, double y0, double y1) {
+    book(name, nx, x0, x1, ny, y0, y1);
+  }
   TH2D(const char*, const char*, int, const double*, int, const double*) {}
   TH1D* ProjectionX(const char* = "_px") { refshim::unavailable("histograms"); }
   TH1D* ProjectionY(const char* = "_py") { refshim::unavailable("histograms"); }
+  TObject* Clone(const char* name = "") const override {
+    auto* c = new TH2D(*this);
+    if (name && *name) c->name_ = name;
+    return c;
+  }
 };
+
+// The luminosity's ROOT file, in memory: TFile(name, "recreate") opens an
+// empty file and makes it current, an object's Write() stores a copy of it
+// there, TFile(name) opens it again and Get() returns a copy.
+namespace refshim {
+struct FileStore {
+  std::mutex mu;
+  std::map<std::string, std::map<std::string, std::shared_ptr<TObject>>> files;
+  std::string current;
+};
+inline FileStore& files() {
+  static FileStore st;
+  return st;
+}
+}  // namespace refshim
+
+inline int TH1::Write(const char*, int, int) {
+  auto& st = refshim::files();
+  std::lock_guard<std::mutex> lock(st.mu);
+  if (st.current.empty()) refshim::unavailable("TH1::Write without an open file");
+  st.files[st.current][name_] = std::shared_ptr<TObject>(Clone());
+  return 1;
+}
 
 class TDirectory : public TObject {};
 class TFile : public TDirectory {
  public:
   TFile() = default;
-  TFile(const char*, const char* = "", const char* = "", int = 0) {
-    refshim::unavailable("TFile");
+  TFile(const char* name, const char* opt = "", const char* = "", int = 0) : name_(name) {
+    const std::string o = opt ? opt : "";
+    auto& st = refshim::files();
+    std::lock_guard<std::mutex> lock(st.mu);
+    if (o == "recreate" || o == "RECREATE" || o == "new" || o == "NEW" || o == "create" ||
+        o == "CREATE") {
+      st.files[name_].clear();
+    } else if (!st.files.count(name_)) {
+      zombie_ = true;
+      return;
+    }
+    st.current = name_;
   }
-  TObject* Get(const char*) { refshim::unavailable("TFile"); }
-  bool IsOpen() const { return false; }
-  bool IsZombie() const { return true; }
-  void Close(const char* = "") {}
-  int Write(const char* = nullptr, int = 0, int = 0) override { refshim::unavailable("TFile"); }
+  TObject* Get(const char* key) {
+    auto& st = refshim::files();
+    std::lock_guard<std::mutex> lock(st.mu);
+    auto f = st.files.find(name_);
+    if (f == st.files.end()) return nullptr;
+    auto o = f->second.find(key);
+    return o == f->second.end() ? nullptr : o->second->Clone();
+  }
+  bool IsOpen() const { return !zombie_; }
+  bool IsZombie() const { return zombie_; }
+  void Close(const char* = "") {
+    auto& st = refshim::files();
+    std::lock_guard<std::mutex> lock(st.mu);
+    if (st.current == name_) st.current.clear();
+  }
+  int Write(const char* = nullptr, int = 0, int = 0) override { return 0; }
+
+ private:
+  std::string name_;
+  bool zombie_ = false;
 };
 
 class TTree : public TObject {
@@ -311,6 +526,25 @@ class TVector3 {
   double X() const { return x_; }
   double Y() const { return y_; }
   double Z() const { return z_; }
+  double Mag2() const { return x_ * x_ + y_ * y_ + z_ * z_; }
+  double Mag() const { return std::sqrt(Mag2()); }
+  void SetMagThetaPhi(double mag, double theta, double phi) {
+    const double amag = std::fabs(mag);
+    x_ = amag * std::sin(theta) * std::cos(phi);
+    y_ = amag * std::sin(theta) * std::sin(phi);
+    z_ = amag * std::cos(theta);
+  }
+  TVector3 operator-() const { return TVector3(-x_, -y_, -z_); }
+  TVector3 Unit() const {
+    double u[3];
+    uo::unit3(x_, y_, z_, u);
+    return TVector3(u[0], u[1], u[2]);
+  }
+  void RotateUz(const TVector3& u) {
+    uo::Vec4 p{x_, y_, z_, 0.};
+    uo::rotate_uz(p, u.x_, u.y_, u.z_);
+    x_ = p.x, y_ = p.y, z_ = p.z;
+  }
 
  private:
   double x_ = 0, y_ = 0, z_ = 0;
@@ -319,26 +553,31 @@ class TLorentzVector {
  public:
   TLorentzVector() = default;
   TLorentzVector(double px, double py, double pz, double e) : p_{px, py, pz, e} {}
-  void SetPxPyPzE(double px, double py, double pz, double e) { p_[0] = px, p_[1] = py, p_[2] = pz, p_[3] = e; }
-  void SetXYZM(double, double, double, double) { refshim::unavailable("TLorentzVector"); }
-  double Px() const { return p_[0]; }
-  double Py() const { return p_[1]; }
-  double Pz() const { return p_[2]; }
-  double E() const { return p_[3]; }
-  double Pt() const { return std::sqrt(p_[0] * p_[0] + p_[1] * p_[1]); }
-  double M() const { refshim::unavailable("TLorentzVector"); }
-  double Eta() const { refshim::unavailable("TLorentzVector"); }
-  double Phi() const { refshim::unavailable("TLorentzVector"); }
-  double Rapidity() const { refshim::unavailable("TLorentzVector"); }
-  TVector3 BoostVector() const { refshim::unavailable("TLorentzVector"); }
-  void Boost(const TVector3&) { refshim::unavailable("TLorentzVector"); }
-  void Boost(double, double, double) { refshim::unavailable("TLorentzVector"); }
+  void SetPxPyPzE(double px, double py, double pz, double e) { p_ = uo::Vec4{px, py, pz, e}; }
+  void SetXYZM(double x, double y, double z, double m) { p_ = uo::set_vect_m(x, y, z, m); }
+  void SetVectM(const TVector3& v, double m) { SetXYZM(v.X(), v.Y(), v.Z(), m); }
+  double Px() const { return p_.x; }
+  double Py() const { return p_.y; }
+  double Pz() const { return p_.z; }
+  double E() const { return p_.t; }
+  double Pt() const { return uo::pt_of(p_); }
+  double Mag2() const { return uo::mag2_of(p_); }
+  double Mag() const { return uo::mag_of(p_); }
+  double M() const { return uo::mag_of(p_); }
+  double Eta() const { return uo::eta_of(p_); }
+  double Phi() const { refshim::unavailable("TLorentzVector::Phi"); }
+  double Rapidity() const { refshim::unavailable("TLorentzVector::Rapidity"); }
+  TVector3 Vect() const { return TVector3(p_.x, p_.y, p_.z); }
+  TVector3 BoostVector() const { return TVector3(p_.x / p_.t, p_.y / p_.t, p_.z / p_.t); }
+  void Boost(const TVector3& b) { Boost(b.X(), b.Y(), b.Z()); }
+  void Boost(double bx, double by, double bz) { uo::boost(p_, bx, by, bz); }
+  void RotateUz(const TVector3& u) { uo::rotate_uz(p_, u.X(), u.Y(), u.Z()); }
   TLorentzVector operator+(const TLorentzVector& o) const {
-    return TLorentzVector(p_[0] + o.p_[0], p_[1] + o.p_[1], p_[2] + o.p_[2], p_[3] + o.p_[3]);
+    return TLorentzVector(p_.x + o.p_.x, p_.y + o.p_.y, p_.z + o.p_.z, p_.t + o.p_.t);
   }
 
  private:
-  double p_[4] = {0, 0, 0, 0};
+  uo::Vec4 p_{0, 0, 0, 0};
 };
 
 class TParticle : public TObject {
@@ -351,23 +590,41 @@ class TClonesArray : public TObject {};
 
 class TRandom : public TObject {
  public:
-  double Uniform(double = 1.) { refshim::unavailable("gRandom"); }
-  double Uniform(double, double) { refshim::unavailable("gRandom"); }
-  double Rndm() { refshim::unavailable("gRandom"); }
-  void SetSeed(unsigned long) {}
+  virtual double Rndm() { refshim::unavailable("TRandom::Rndm"); }
+  double Uniform(double x1 = 1.) { return x1 * Rndm(); }
+  double Uniform(double x1, double x2) { return x1 + (x2 - x1) * Rndm(); }
+  virtual void SetSeed(unsigned long) {}
 };
 template <class T>
 class TRandomGen : public TRandom {};
-class TRandomMT64 : public TRandom {};
-inline TRandom* gRandom = nullptr;
+class TRandomMT64 : public TRandom {  // the 64-bit Mersenne twister (oracle_gen_prims.hpp)
+ public:
+  double Rndm() override { return g_.rndm(); }
+  void SetSeed(unsigned long s) override { g_ = uo::RootMT64(s); }
 
+ private:
+  uo::RootMT64 g_;
+};
+inline TRandom* gRandom = nullptr;
+inline double refshim_rndm() {
+  if (!gRandom) refshim::unavailable("gRandom before the generator's init");
+  return gRandom->Rndm();
+}
+
+// AccessPathName follows ROOT's sense: true when the path can NOT be accessed
+// (here: a stand-in file not written in this process)
 class TSystem : public TObject {
  public:
-  bool AccessPathName(const char*) { refshim::unavailable("gSystem"); }
+  bool AccessPathName(const char* path) {
+    auto& st = refshim::files();
+    std::lock_guard<std::mutex> lock(st.mu);
+    return st.files.count(path) == 0;
+  }
   int Exec(const char*) { refshim::unavailable("gSystem"); }
   int Unlink(const char*) { refshim::unavailable("gSystem"); }
 };
-inline TSystem* gSystem = nullptr;
+inline TSystem refshim_system;
+inline TSystem* gSystem = &refshim_system;
 class TROOT : public TObject {};
 inline TROOT* gROOT = nullptr;
 namespace ROOT {

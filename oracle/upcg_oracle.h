@@ -14,9 +14,14 @@
  * run this oracle's restated primitives (oracle/ref_cs_shim.cpp; fixture
  * tests/golden/ref_cs.json): rho0, G_AA, the form factor, both fluxes, the
  * breakup probability, luminosity cells and calcPhotonFlux on 8
- * configurations; (b) for the elementary gamma-gamma cross sections, bit for
- * bit against UpcTwoPhotonDilep.cpp / UpcTwoPhotonALP.cpp compiled as they
- * are; (c) the primitives themselves (K0/K1/J1, QAGS, natural cubic splines)
+ * configurations; (b) the event loop, bit for bit against the reference's
+ * own src/UpcGenerator.cpp compiled the same way (oracle/ref_gen_shim.cpp;
+ * fixture tests/golden/ref_gen.npz): every 4-momentum, pdg code, rejected
+ * count and totNuclX of five configurations, with the random engines,
+ * histogram samplers and vector algebra of oracle_gen_prims.hpp behind the
+ * stand-ins; (c) for the elementary gamma-gamma cross sections, bit for bit
+ * against UpcTwoPhotonDilep.cpp / UpcTwoPhotonALP.cpp compiled as they are;
+ * (d) the primitives themselves (K0/K1/J1, QAGS, natural cubic splines)
  * against scipy's independent implementations, not against GSL / ROOT,
  * which are absent.
  */
