@@ -47,13 +47,14 @@ int on_big_stack(std::function<void()> fn) {
 
 extern "C" {
 
-// keys / vals: nkv parameters.in pairs.  pdg [n][max_particles] (0 where an
-// event has fewer particles), p4 [n][max_particles][4] (px, py, pz, E).
-// Returns 0, -1 (thread), -2 (an event with more than max_particles).
+// keys / vals: nkv parameters.in pairs.  pdg, status, mother [n][max_particles]
+// (generateEvent's lists; 0 where an event has fewer particles), p4
+// [n][max_particles][4] (px, py, pz, E).  Returns 0, -1 (thread), -2 (an
+// event with more than max_particles).
 int uref_gen_run(const char* const* keys, const char* const* vals, int nkv, const char* lumi_dir,
-                 int threads, int64_t n, int max_particles, int* pdg, double* p4,
-                 int64_t* rejected, double* tot_mb) {
-  int status = 0;
+                 int threads, int64_t n, int max_particles, int* pdg, int* status, int* mother,
+                 double* p4, int64_t* rejected, double* tot_mb) {
+  int result = 0;
   const int rc = on_big_stack([&] {
     auto* gen = new UpcGenerator();
     for (int i = 0; i < nkv; ++i) gen->setParameterValue(keys[i], vals[i]);
@@ -66,13 +67,15 @@ int uref_gen_run(const char* const* keys, const char* const* vals, int nkv, cons
     while (acc < n) {
       if (gen->generateEvent(pdgs, statuses, mothers, particles) == 1) {
         if ((int)particles.size() > max_particles) {
-          status = -2;
+          result = -2;
           return;
         }
         for (int k = 0; k < max_particles; ++k) {
           const size_t r = (size_t)acc * max_particles + k;
           const bool has = k < (int)particles.size();
           pdg[r] = has ? pdgs[k] : 0;
+          status[r] = has ? statuses[k] : 0;
+          mother[r] = has ? mothers[k] : 0;
           p4[4 * r + 0] = has ? particles[k].Px() : 0.;
           p4[4 * r + 1] = has ? particles[k].Py() : 0.;
           p4[4 * r + 2] = has ? particles[k].Pz() : 0.;
@@ -86,6 +89,6 @@ int uref_gen_run(const char* const* keys, const char* const* vals, int nkv, cons
     *rejected = rej;
     *tot_mb = gen->totNuclX();
   });
-  return rc != 0 ? -1 : status;
+  return rc != 0 ? -1 : result;
 }
 }

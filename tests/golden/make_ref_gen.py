@@ -8,8 +8,9 @@ oracle/ref_gen_shim.cpp runs UpcGenerator::init and the generateEvent loop
 of generateEvents (src/UpcGenerator.cpp:57-181, 630-889) for one
 configuration.  Each configuration runs in a fresh process (the reference
 keeps its nucleus, splines and breakup tables as process globals) with one
-luminosity thread, and its first N accepted events are stored: pdg codes and
-4-momenta of generateEvent's particles, the rejected count and totNuclX.
+luminosity thread, and its first N accepted events are stored: the pdg
+codes, status codes, mothers and 4-momenta of generateEvent's particle lists,
+the rejected count and totNuclX.
 
 The configurations cover the event loop's branches: lepton pairs with and
 without photon pT (NON_ZERO_GAM_PT), the pT and eta cuts (rejections), the
@@ -57,7 +58,8 @@ CONFIGS = {
 
 def run_one(params, n=N_EVENTS, threads=1):
     """The reference's events for one configuration, in this process (call it
-    in a fresh one).  Returns (pdg [n][3], p4 [n][3][4], rejected, tot_mb)."""
+    in a fresh one).  Returns (pdg, status, mother [n][3], p4 [n][3][4],
+    rejected, tot_mb)."""
     sys.path.insert(0, ROOT)
     from oracle import build as ob
     so = ob.build_ref_gen()
@@ -69,15 +71,18 @@ def run_one(params, n=N_EVENTS, threads=1):
     K = (C.c_char_p * len(keys))(*keys)
     V = (C.c_char_p * len(vals))(*vals)
     pdg = np.zeros((n, MAX_PARTICLES), dtype=np.int32)
+    status = np.zeros_like(pdg)
+    mother = np.zeros_like(pdg)
     p4 = np.zeros((n, MAX_PARTICLES, 4))
     rej, tot = C.c_int64(), C.c_double()
     with tempfile.TemporaryDirectory() as d:  # the reference's lock file goes here
         rc = L.uref_gen_run(K, V, len(keys), d.encode(), threads, C.c_int64(n), MAX_PARTICLES,
-                            pdg.ctypes.data_as(C.c_void_p), p4.ctypes.data_as(C.c_void_p),
+                            pdg.ctypes.data_as(C.c_void_p), status.ctypes.data_as(C.c_void_p),
+                            mother.ctypes.data_as(C.c_void_p), p4.ctypes.data_as(C.c_void_p),
                             C.byref(rej), C.byref(tot))
     if rc != 0:
         raise RuntimeError(f"uref_gen_run failed: {rc}")
-    return pdg, p4, rej.value, tot.value
+    return pdg, status, mother, p4, rej.value, tot.value
 
 
 def run_fresh(name, out_path, n=N_EVENTS):
@@ -85,20 +90,22 @@ def run_fresh(name, out_path, n=N_EVENTS):
     subprocess.run([sys.executable, os.path.abspath(__file__), "--one", name, out_path, str(n)],
                    check=True)
     d = np.load(out_path)
-    return d["pdg"], d["p4"], int(d["rejected"]), float(d["tot"])
+    return d["pdg"], d["status"], d["mother"], d["p4"], int(d["rejected"]), float(d["tot"])
 
 
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "--one":
         name, path, n = sys.argv[2], sys.argv[3], int(sys.argv[4])
-        pdg, p4, rej, tot = run_one(CONFIGS[name], n)
-        np.savez(path, pdg=pdg, p4=p4, rejected=rej, tot=tot)
+        pdg, status, mother, p4, rej, tot = run_one(CONFIGS[name], n)
+        np.savez(path, pdg=pdg, status=status, mother=mother, p4=p4, rejected=rej, tot=tot)
         return
     arrays = {}
     with tempfile.TemporaryDirectory() as d:
         for name in CONFIGS:
-            pdg, p4, rej, tot = run_fresh(name, os.path.join(d, name + ".npz"))
+            pdg, status, mother, p4, rej, tot = run_fresh(name, os.path.join(d, name + ".npz"))
             arrays[name + "/pdg"] = pdg
+            arrays[name + "/status"] = status
+            arrays[name + "/mother"] = mother
             arrays[name + "/p4"] = p4
             arrays[name + "/rejected"] = np.int64(rej)
             arrays[name + "/tot"] = np.float64(tot)

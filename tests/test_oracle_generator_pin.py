@@ -14,6 +14,9 @@ rejected count and totNuclX -- which pins its restatement of the samplers
 (src/UpcCrossSection.cpp:1021-1074) and the decays to the reference's code,
 draw order included.  (GCC evaluates the reference's two gsl_rng_uniform
 arguments of the 2-D sampler right to left; the pin is what showed it.)
+The same events also pin the library's particle lists (getParticles,
+particlesOf): pdg codes, charge order, status codes and mothers as the
+reference's generateEvent makes them.
 """
 import json
 import os
@@ -77,8 +80,40 @@ def test_live_reference_generator():
     assert SRC_CONFIGS == CONFIGS
     import tempfile
     with tempfile.TemporaryDirectory() as d:
-        pdg, p4, rej, tot = run_fresh("tautau_cuts_xnxn", os.path.join(d, "o.npz"), n=100)
+        pdg, st, mo, p4, rej, tot = run_fresh("tautau_cuts_xnxn", os.path.join(d, "o.npz"), n=100)
     name = "tautau_cuts_xnxn"
     assert np.array_equal(pdg, FIX[name + "/pdg"][:100])
+    assert np.array_equal(st, FIX[name + "/status"][:100])
+    assert np.array_equal(mo, FIX[name + "/mother"][:100])
     assert np.array_equal(p4, FIX[name + "/p4"][:100])
     assert tot == float(FIX[name + "/tot"])
+
+
+@pytest.mark.parametrize("name", sorted(CONFIGS))
+def test_library_particle_lists_match_reference_generator(ug, name):
+    """The drop-in's particle lists (getParticles / particlesOf, and the C++
+    facade's generateEvent, which builds the same lists) against the
+    reference's own generateEvent on its events: pdg codes with the charge
+    order, status codes and mothers exactly; the momenta are the record's
+    FP32 values; an ALP's own momentum is the sum of its photons'."""
+    params = CONFIGS[name]
+    pdg, st, mo, p4 = (FIX[name + "/" + k] for k in ("pdg", "status", "mother", "p4"))
+    g = ug.UpcGenerator(params)
+    ppe = g.particlesPerEvent()
+    proc = int(params["PROC_ID"])
+    rec = np.zeros(len(pdg), dtype=ug.EVENT_DTYPE)
+    if proc == 51:
+        rec["p0"], rec["p1"], rec["sign"] = p4[:, 1], p4[:, 2], 1.0
+    else:
+        rec["p0"], rec["p1"] = p4[:, 0], p4[:, 1]
+        rec["sign"] = np.sign(pdg[:, 0] * proc)
+    for k in range(len(rec)):
+        got = g.particlesOf(rec[k])
+        assert [q[0] for q in got] == list(pdg[k, :ppe]), k
+        assert [q[1] for q in got] == list(st[k, :ppe]), k
+        assert [q[2] for q in got] == list(mo[k, :ppe]), k
+        first = 1 if proc == 51 else 0
+        for i in range(first, ppe):
+            assert got[i][3] == tuple(float(x) for x in p4[k, i].astype(np.float32)), (k, i)
+        if proc == 51:
+            assert np.allclose(got[0][3], p4[k, 0], rtol=0, atol=2e-6 * p4[k, 0, 3]), k
