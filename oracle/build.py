@@ -104,7 +104,8 @@ REF_GEN_SO = os.path.join(REF_DIR, "libupcref_gen.so")
 
 def build_ref_gen(force=False):
     """Compile the reference's event generator (src/UpcGenerator.cpp with the
-    units of build_ref_cs) against refshim/ with ref_gen_shim.cpp into
+    units of build_ref_cs) against refshim/ with ref_gen_shim.cpp (init and
+    the event loop) and ref_out_shim.cpp (writeEvent's HepMC3 output) into
     oracle/_ref/libupcref_gen.so; None if the reference sources are absent.
     Pythia is off, as in a reference build without it."""
     src = os.path.join(REFERENCE_ROOT, "src")
@@ -115,14 +116,15 @@ def build_ref_gen(force=False):
     os.makedirs(REF_DIR, exist_ok=True)
     shim_dir = os.path.join(HERE, "refshim")
     shim = os.path.join(HERE, "ref_gen_shim.cpp")
-    deps = units + [shim, os.path.join(HERE, "oracle_num.hpp"),
+    out_shim = os.path.join(HERE, "ref_out_shim.cpp")
+    deps = units + [shim, out_shim, os.path.join(HERE, "oracle_num.hpp"),
                     os.path.join(HERE, "oracle_gen_prims.hpp")]
     deps += [os.path.join(shim_dir, f) for f in os.listdir(shim_dir) if f.endswith(".h")]
     deps += [os.path.join(shim_dir, "gsl", f) for f in os.listdir(os.path.join(shim_dir, "gsl"))]
     if force or _stale(REF_GEN_SO, deps):
         cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
                "-w", '-DCROSS_SEC_DIR="/nonexistent"', "-I", shim_dir, "-I", inc, *units, shim,
-               "-lpthread", "-o", REF_GEN_SO + ".tmp"]
+               out_shim, "-lpthread", "-o", REF_GEN_SO + ".tmp"]
         subprocess.run(cmd, check=True)
         os.replace(REF_GEN_SO + ".tmp", REF_GEN_SO)
     return REF_GEN_SO

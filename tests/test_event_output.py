@@ -187,3 +187,38 @@ def test_particle_lists(ug, proc, dpdg):
         assert [p[1] for p in got] == sts and [p[2] for p in got] == mos
         assert all(tuple(q) == tuple(r) for (_, _, _, q), r in zip(got, ps))
         assert [int(x) for x in rows[k * ppe:(k + 1) * ppe, 2]] == pdgs
+
+
+def _ref_hepmc():
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_ref_hepmc
+    return make_ref_hepmc
+
+
+@pytest.mark.parametrize("name", ["mumu", "tautau", "alp"])
+def test_hepmc_text_is_the_reference_writers(ug, name):
+    """The library's HepMC3 text against the reference's own writeEvent and
+    WriterHepMC (src/UpcGenerator.cpp:589-628, include/UpcGenerator.h:192-242),
+    compiled from its sources (tests/golden/make_ref_hepmc.py): for seeded
+    records, the reference's file of the library's particle lists is the
+    library's preamble + formatHepMC3 + end line, byte for byte (SHA-256 and
+    size committed in tests/golden/ref_hepmc.json; compared directly when the
+    reference sources are present).  tests/test_gpu_event_output.py checks
+    that the library's files are that preamble + formatHepMC3 + end line."""
+    import hashlib
+    import json
+    mk = _ref_hepmc()
+    from test_gpu_event_output import HEAD, TAIL
+    with open(os.path.join(os.path.dirname(__file__), "golden", "ref_hepmc.json")) as f:
+        want = json.load(f)[name]
+    proc, n, seed, first = mk.CASES[name]
+    assert (want["proc"], want["records"], want["seed"], want["first_event"]) == (proc, n, seed, first)
+    g = ug.UpcGenerator({"PROC_ID": proc})
+    ev = mk.records(ug.EVENT_DTYPE, n, seed)
+    ours = (HEAD + g.formatHepMC3(ev, first_event=first) + TAIL).encode()
+    assert len(ours) == want["bytes"]
+    assert hashlib.sha256(ours).hexdigest() == want["sha256"]
+    from oracle import build as ob
+    if ob.build_ref_gen() is not None:
+        assert mk.reference_text(*mk.particle_arrays(g, ev), first) == ours
