@@ -92,3 +92,19 @@ int uref_gen_run(const char* const* keys, const char* const* vals, int nkv, cons
   return rc != 0 ? -1 : result;
 }
 }
+
+extern "C" {
+// The reference's UpcSampler2D::getBinX / getBinY (include/UpcSampler.h:124-134)
+// on n values: the sampler built as computeNuclXsection builds it
+// (src/UpcGenerator.cpp:677-700: x = the nx + 1 rapidity edges, y = the ny + 1
+// mass edges; the contents do not enter the bin functions); axis 0 -> getBinX,
+// 1 -> getBinY.
+int uref_sampler_bins(int nx, const double* edges_x, int ny, const double* edges_y,
+                      const double* v, int64_t n, int axis, int* out) {
+  std::vector<std::vector<double>> dist(nx, std::vector<double>(ny, 1.0));
+  std::vector<double> ex(edges_x, edges_x + nx + 1), ey(edges_y, edges_y + ny + 1);
+  UpcSampler2D s(dist, ex, ey, 1);
+  for (int64_t i = 0; i < n; ++i) out[i] = axis == 0 ? s.getBinX(v[i]) : s.getBinY(v[i]);
+  return 0;
+}
+}

@@ -117,3 +117,28 @@ def test_library_particle_lists_match_reference_generator(ug, name):
             assert got[i][3] == tuple(float(x) for x in p4[k, i].astype(np.float32)), (k, i)
         if proc == 51:
             assert np.allclose(got[0][3], p4[k, 0], rtol=0, atol=2e-6 * p4[k, 0, 3]), k
+
+
+def test_sampler_bins_bit_exact_vs_reference_source(oracle_mod):
+    """The oracle's getBinX / getBinY (the restatement the GPU's bin test is
+    held to, tests/test_gpu_parity.py) against the reference's own
+    UpcSampler2D functions compiled from include/UpcSampler.h
+    (tests/golden/make_ref_bins.py): every bin edge, every step of the
+    truncated numerator and 1-2 ulps around each, on the 201 x 61, 1001 x 121
+    and 21 x 13 tau-pair grids, both axes -- including the index n the
+    reference returns an ulp below the top edge."""
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import make_ref_bins as mb
+    fix = np.load(os.path.join(HERE, "golden", "ref_bins.npz"))
+    from oracle import build as ob
+    live = ob.build_ref_gen() is not None
+    for nm, ny in mb.GRIDS:
+        em, ey = mb.edges(mb.MMIN, mb.MMAX, nm), mb.edges(mb.YMIN, mb.YMAX, ny)
+        for axis, name, e, n in ((1, "m", em, nm), (0, "y", ey, ny)):
+            x = mb.edge_values(e, n)
+            ref = fix[f"{nm}x{ny}/{name}/bin"].astype(np.int32)
+            assert len(ref) == len(x)
+            if live:
+                assert np.array_equal(mb.reference_bins(em, ey, x, axis), ref)
+            got = np.array([oracle_mod.sampler_bin(n, e[0], e[-1], float(v)) for v in x])
+            assert np.array_equal(got, ref), (nm, ny, name, np.flatnonzero(got != ref)[:5])
