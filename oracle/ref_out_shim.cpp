@@ -9,6 +9,9 @@
 // its private members public; the layout does not change).  uref_write_hepmc
 // writes given particle lists through the reference's code, so the library's
 // HepMC3 text can be compared with the reference's byte for byte.
+// uref_config_file reads a parameters.in with the reference's own
+// configGeneratorFromFile (src/UpcGenerator.cpp:318-346) and runs its init
+// (the process overrides, :57-181), and returns the resulting grid and flags.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -32,6 +35,8 @@
 #include <unordered_map>
 #include <utility>
 #include <vector>
+
+#include <pthread.h>
 
 #include "refshim.h"
 
@@ -65,6 +70,57 @@ int uref_write_hepmc(const char* path, int64_t n, int ppe, const int* pdg, const
   }
   delete gen.writerHepMC;  // the end-of-listing line, file closed
   gen.writerHepMC = nullptr;
+  return 0;  // ~UpcGenerator deletes gRandom, which this run never set
+}
+}
+
+namespace {
+// prepareBreakupProb keeps two arrays of 10^6 doubles on the stack
+// (src/UpcCrossSection.cpp:422-423, 16 MB): init runs on a thread with a
+// 256 MB stack.
+int on_big_stack_cfg(std::function<void()> fn) {
+  pthread_attr_t attr;
+  pthread_attr_init(&attr);
+  pthread_attr_setstacksize(&attr, (size_t)256 << 20);
+  pthread_t th;
+  auto body = [](void* p) -> void* {
+    (*static_cast<std::function<void()>*>(p))();
+    return nullptr;
+  };
+  const int rc = pthread_create(&th, &attr, body, &fn);
+  pthread_attr_destroy(&attr);
+  if (rc != 0) return -1;
+  pthread_join(th, nullptr);
   return 0;
+}
+}  // namespace
+
+extern "C" {
+
+// grid: mmin, mmax, ymin, ymax, zmin, zmax; ints: nm, ny, nz, procID,
+// breakupMode, isPoint, usePolarizedCS, useNonzeroGamPt, doPtCut, doEtaCut,
+// useROOTOut, useHepMCOut; nevents.  lumi_dir: a fresh directory for the
+// reference's lock file (init computes the luminosity: keep the grid small).
+int uref_config_file(const char* path, const char* lumi_dir, double* grid, int* ints,
+                     int64_t* nevents) {
+  const int rc = on_big_stack_cfg([&] {
+    UpcGenerator gen;
+    gen.setParFile(path);
+    gen.configGeneratorFromFile();
+    gen.setLumiFileDirectory(lumi_dir);
+    gen.setNumThreads(1);
+    gen.init();
+    const UpcCrossSection& c = *gen.nucProcessCS;
+    const double g[6] = {c.mmin, c.mmax, c.ymin, c.ymax, c.zmin, c.zmax};
+    for (int i = 0; i < 6; ++i) grid[i] = g[i];
+    const int v[12] = {c.nm, c.ny, c.nz, gen.procID, c.breakupMode, c.isPoint ? 1 : 0,
+                       gen.usePolarizedCS ? 1 : 0, c.useNonzeroGamPt ? 1 : 0,
+                       gen.doPtCut ? 1 : 0, gen.doEtaCut ? 1 : 0, gen.useROOTOut ? 1 : 0,
+                       gen.useHepMCOut ? 1 : 0};
+    for (int i = 0; i < 12; ++i) ints[i] = v[i];
+    *nevents = gen.nEvents;
+  });
+  gRandom = nullptr;  // deleted by ~UpcGenerator
+  return rc;
 }
 }

@@ -612,13 +612,19 @@ inline double refshim_rndm() {
 }
 
 // AccessPathName follows ROOT's sense: true when the path can NOT be accessed
-// (here: a stand-in file not written in this process)
+// (neither a stand-in file written in this process nor a file on disk)
 class TSystem : public TObject {
  public:
   bool AccessPathName(const char* path) {
-    auto& st = refshim::files();
-    std::lock_guard<std::mutex> lock(st.mu);
-    return st.files.count(path) == 0;
+    {
+      auto& st = refshim::files();
+      std::lock_guard<std::mutex> lock(st.mu);
+      if (st.files.count(path)) return false;
+    }
+    std::FILE* f = std::fopen(path, "r");
+    if (!f) return true;
+    std::fclose(f);
+    return false;
   }
   int Exec(const char*) { refshim::unavailable("gSystem"); }
   int Unlink(const char*) { refshim::unavailable("gSystem"); }

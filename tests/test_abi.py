@@ -196,3 +196,40 @@ def test_cpp_facade_compiles_and_configures(ug, tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stderr
     assert out.stdout.split() == ["13", "1", "1", "1", "1", "1"]
+
+
+def test_parameter_files_read_as_the_reference_reads_them(ug, tmp_path):
+    """parameters.in files through configGeneratorFromFile against the
+    reference's own reader and init, compiled from its sources
+    (tests/golden/make_ref_config.py; fixture ref_config.json, and a live
+    run when the sources are present): the grid after the process overrides
+    (ALP mass window, dilepton MMIN clamp), NEVENTS and the output flags --
+    with the reader's quirks: a key without a value takes the previous
+    line's value, an indented '#' line reads as an unknown key, tokens after
+    the value are ignored."""
+    import json
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_ref_config as mk
+    with open(os.path.join(os.path.dirname(__file__), "golden", "ref_config.json")) as f:
+        fixture = json.load(f)
+    assert set(fixture) == set(mk.FILES)
+    from oracle import build as ob
+    live = ob.build_ref_gen() is not None
+    for name, text in mk.FILES.items():
+        want = fixture[name]["reference"]
+        assert fixture[name]["text"] == text
+        if live:
+            assert mk.run_fresh(name) == want, name
+        p = tmp_path / f"{name}.in"
+        p.write_text(text)
+        g = ug.UpcGenerator()
+        g.setParFile(str(p))
+        g.configGeneratorFromFile()
+        pdg, _ = g.particlePDG()  # applies the process overrides, as init does
+        gr = g.grid()
+        for k in ("mmin", "mmax", "ymin", "ymax", "zmin", "zmax", "nm", "ny", "nz"):
+            assert gr[k] == want[k], (name, k, gr[k], want[k])
+        assert g.eventOutputConfig() == (want["NEVENTS"], want["USE_ROOT_OUTPUT"],
+                                         want["USE_HEPMC_OUTPUT"]), name
+        assert pdg == want["PROC_ID"], name

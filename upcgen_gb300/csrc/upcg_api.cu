@@ -2176,20 +2176,21 @@ int upcg_set_parameter(upcg_generator* g, const char* key, const char* value) {
 }
 
 int upcg_config_from_file(upcg_generator* g, const char* path) {
-  // src/UpcGenerator.cpp:318-346: '#' lines skipped, trailing comments
-  // trimmed, "KEY value" pairs; a missing file keeps the defaults.
+  // src/UpcGenerator.cpp:318-346, read as the reference reads it: a line that
+  // starts with '#' is skipped; every other line is split into "KEY value"
+  // by a stream made before the comment is trimmed, and the key and value
+  // persist from line to line, so a token the line lacks keeps the previous
+  // line's (a key without a value takes the value of the line before; an
+  // empty line repeats the previous pair).  Unknown keys are ignored; a
+  // missing file keeps the defaults.
   if (!g || !path) return fail(UPCG_ERR_ARG, "null argument");
   std::ifstream in(path);
   if (!in) return UPCG_OK;
   std::string line, key, val;
   while (std::getline(in, line)) {
-    if (!line.empty() && line[0] == '#') continue;
-    line.erase(std::find(line.begin(), line.end(), '#'), line.end());
     std::istringstream iss(line);
-    std::string k2, v2;
-    if (!(iss >> k2 >> v2)) continue;
-    key = k2;
-    val = v2;
+    if (line[0] == '#') continue;  // an empty line's [0] is '\0'
+    iss >> key >> val;
     int rc = g->set_param(key, val);
     if (rc < 0) return rc;
   }
