@@ -223,7 +223,8 @@ def run_reference(args):
     v = cells / float(np.mean(times))
     sample = (f"m-row blocks {blocks} of {g['nm']} x {g['ny']} y-bins = {cells} cells per step "
               f"(spread over the mass range)")
-    phases = cpu_phases(params, threads, blocks[:2], 20000 if args.workload == "c2" else 100000)
+    n_ev = args.ref_events if args.ref_events else (20000 if args.workload == "c2" else 100000)
+    phases = cpu_phases(params, threads, blocks[:2], n_ev)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
@@ -388,6 +389,8 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c5"])
     ap.add_argument("--events", type=int, default=None)
     ap.add_argument("--ref-rows", type=int, default=None)
+    ap.add_argument("--ref-events", type=int, default=None,
+                    help="events of the reference arm's single-threaded event phase")
     ap.add_argument("--plain-steps", type=int, default=None)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
