@@ -222,3 +222,25 @@ def test_hepmc_text_is_the_reference_writers(ug, name):
     from oracle import build as ob
     if ob.build_ref_gen() is not None:
         assert mk.reference_text(*mk.particle_arrays(g, ev), first) == ours
+
+
+@pytest.mark.parametrize("proc,pdg", [(13, 13), (51, 51)])
+def test_hepmc_text_extreme_values(ug, proc, pdg):
+    """The %.9g text of every kind of FP32 momentum -- random bit patterns
+    over all exponents, subnormals, +-0, the largest floats -- and of the
+    masses and sums formed from them in FP64, against Python's correctly
+    rounded '%.9g' of the same values."""
+    g = ug.UpcGenerator({"PROC_ID": proc})
+    rng = np.random.default_rng(2024)
+    n = 20000
+    bits = rng.integers(0, 2 ** 32, size=(n, 8), dtype=np.uint64).astype(np.uint32)
+    vals = bits.view(np.float32)
+    vals[~np.isfinite(vals)] = 1.0
+    special = np.array([0.0, -0.0, 1e-45, -1e-45, 1.1754942e-38, 3.4028235e38, -3.4028235e38,
+                        0.1, 1e-10, 123456789.0, 999999999.0, 1e9, 9.99999999e-5], dtype=np.float32)
+    vals[: len(special), 0] = special
+    ev = np.zeros(n, dtype=ug.EVENT_DTYPE)
+    ev["sign"] = rng.choice([-1.0, 1.0], n)
+    ev["p0"], ev["p1"] = vals[:, :4], vals[:, 4:]
+    text = g.formatHepMC3(ev, first_event=3)
+    assert text == _hepmc_reference(ev, pdg, True, 3)
